@@ -1,0 +1,383 @@
+#!/usr/bin/env python3
+"""VarDCT front-end throughput on GB300 (MP/s).
+
+Workload: one 3840x2160 RGB8 frame from the seeded synthetic generator
+(noise 4, 200 rectangles, 30 % 1/f^2 texture), encoded at qualities 75, 90
+and 95 with the UltraFast gates; one step = those three frames through the
+whole front end (XYB, AQ field, CfL maps, DCT8 + quantisation, tokens and
+per-context histograms).  `value` is timed with CUDA events on the launching
+stream with the input resident in HBM; `e2e` runs the public C ABI with host
+buffers (pinned), the upload and the result download inside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WIDTH, HEIGHT = 3840, 2160
+QUALITIES = (75, 90, 95)
+METRIC = "VarDCT MP/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def workload_config(impl: str) -> dict:
+    return {
+        "workload": "VarDCT front end, 3840x2160 RGB8 sRGB, q75/q90/q95 per step, "
+                    "UltraFast effort gates (all-DCT8 layout, one pass)",
+        "width": WIDTH, "height": HEIGHT, "frames_per_step": len(QUALITIES),
+        "qualities": list(QUALITIES), "effort": "ultrafast",
+        "input": "synthetic seeded generator (seed 2): cosine gradients, noise sigma 4, "
+                 "200 rectangles, 30% 1/f^2 texture, 8-px checker",
+        "l2": "256 MB buffer written between timed steps, outside the timed events",
+        "parallelism": "replicas only (one independent frame stream per GPU)",
+        "impl": impl,
+    }
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[5 + i].lower().startswith("active")})
+        return {
+            "sm_mhz": float(np.median(sm)) if sm else None,
+            "sm_max_mhz": max(smax) if smax else None,
+            "reasons": reasons,
+            "samples": len(self.rows),
+        }
+
+
+def measured_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def algorithmic_bytes(kernel: str, w: int, h: int, tokens_per_frame: float) -> float | None:
+    """Bytes one launch of `kernel` must move at minimum (per frame)."""
+    px = w * h
+    blocks = ((w + 7) // 8) * ((h + 7) // 8)
+    table = {
+        # RGB8 in, three f32 planes out
+        "k_xyb_rgb8": px * (3 + 12),
+        # three f32 planes in, one u8 per block out
+        "k_adaptive_quant": px * 12 + blocks,
+        # three f32 planes in; i32 levels (192 per block), 3 x i16 DC, 3 u8 counts,
+        # 3 u32 token counts out
+        "k_tile_quantize": px * 12 + blocks * (192 * 4 + 6 + 3 + 12),
+        # levels + counts in, 8-byte tokens out, one 4-byte histogram update per token
+        "k_tokenize": blocks * (192 * 4 + 3 + 1 + 12) + tokens_per_frame * (8 + 4),
+        "k_constant_blocks": px * 12,
+    }
+    return table.get(kernel)
+
+
+def traffic_from_profiles(kernel: str) -> float | None:
+    """DRAM bytes per launch for a full-size frame from a committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_dram.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_full_frame_launch:"):
+            return float(line.split(":", 1)[1])
+    return None
+
+
+def cpu_baseline_run(img, threads: int | None = None) -> dict:
+    """The oracle (C restatement of the reference's scalar path) on the host cores."""
+    from jixel_gb300 import distance_from_quality
+    from oracle import oracle as O
+
+    O.lib()
+    cores = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    for q in QUALITIES:
+        O.frontend(img, distance_from_quality(q), num_threads=cores, keep_coeffs=False)
+    dt = time.perf_counter() - t0
+    mp = len(QUALITIES) * img.shape[0] * img.shape[1] / 1e6
+    return {"value": mp / dt, "unit": "MP/s", "cores": cores, "kind": "port",
+            "sample": f"one step: {img.shape[1]}x{img.shape[0]} at q75/q90/q95 "
+                      f"({dt:.2f} s, OpenMP over DC groups, tiles and AC groups)"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from jixel_gb300 import synthetic
+
+    img = synthetic.config2_image()
+    for _ in range(args.warmup):
+        cpu_baseline_run(img)
+    times = []
+    for _ in range(args.steps):
+        r = cpu_baseline_run(img)
+        times.append(len(QUALITIES) * WIDTH * HEIGHT / 1e6 / r["value"])
+    total = sum(times)
+    value = args.steps * len(QUALITIES) * WIDTH * HEIGHT / 1e6 / total
+    line = {
+        "metric": METRIC, "value": value, "unit": "MP/s", "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config("reference"), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "MP/s", "cores": os.cpu_count() or 1,
+                         "kind": "port",
+                         "sample": "every step the full workload step (three 3840x2160 frames)"},
+        "e2e": {"value": value, "unit": "MP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+
+    import jixel_gb300 as J
+    from jixel_gb300 import _lib as L
+    from jixel_gb300 import synthetic
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    img = synthetic.config2_image()
+    d_img = torch.from_numpy(img).to(dev).contiguous()
+    stream = torch.cuda.current_stream(dev)
+    ctx = J.FrontendContext(local)
+    ctx.set_stream(stream.cuda_stream)
+    cfgs = [J.EncodeConfig(speed=J.Speed.ULTRA_FAST).with_quality(q) for q in QUALITIES]
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+
+    def step():
+        for cfg in cfgs:
+            ctx.run_device(d_img.data_ptr(), WIDTH, HEIGHT, 3, 8, cfg)
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    torch.cuda.synchronize(dev)
+    tokens = []
+    for cfg in cfgs:
+        ctx.run_device(d_img.data_ptr(), WIDTH, HEIGHT, 3, 8, cfg)
+        tokens.append(ctx.params()["num_tokens"])
+    ctx.enable_kernel_timing(True)
+    ctx.reset_kernel_times()
+    sampler = ClockSampler(local)
+    sampler.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.zero_()
+        starts[k].record(stream)
+        step()
+        ends[k].record(stream)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop()
+    ktimes = ctx.kernel_times()
+    ctx.enable_kernel_timing(False)
+    elapsed_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    t = torch.tensor([elapsed_ms], device=dev, dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    max_ms = float(t.item())
+    mp_per_step = len(QUALITIES) * WIDTH * HEIGHT / 1e6
+    value = world * args.steps * mp_per_step / (max_ms / 1000.0)
+
+    # roofline of the dominant kernel (event-timed launches inside the timed region)
+    peaks = measured_peaks()
+    dom = max(ktimes.items(), key=lambda kv: kv[1][0])
+    dom_name, (dom_ms, dom_n) = dom
+    avg_ms = dom_ms / max(dom_n, 1)
+    algo = algorithmic_bytes(dom_name, WIDTH, HEIGHT, float(np.mean(tokens)))
+    achieved = algo / (avg_ms / 1000.0) / 1e9 if algo else None
+    traffic = traffic_from_profiles(dom_name)
+    roofline = {
+        "kernel": dom_name, "bound": "hbm",
+        "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+        "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
+        "peak_source": peaks["source"], "traffic": traffic,
+        "algorithmic_bytes_per_launch": algo, "avg_launch_ms": avg_ms,
+        "share_of_kernel_time": dom_ms / sum(v[0] for v in ktimes.values()),
+    }
+    launches = int(sum(v[1] for v in ktimes.values()))
+
+    # end to end through the public C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(ctx, img, cfgs, args, world, dev)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_run(img)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "MP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config("gb300"),
+            "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+            "clocks": clocks,
+            "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(ktimes.items())},
+            "tokens_per_frame": [int(x) for x in tokens],
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_e2e(ctx, img, cfgs, args, world, dev):
+    import ctypes
+
+    import torch
+
+    from jixel_gb300 import _lib as L
+    from jixel_gb300 import frame_info
+
+    lib = L.load()
+    fi = frame_info(WIDTH, HEIGHT)
+    pin = lambda n, dt: torch.empty(n, dtype=dt, pin_memory=True)  # noqa: E731
+    h_img = pin(img.size, torch.uint8)
+    h_img.numpy()[:] = img.reshape(-1)
+    nb = fi.xsize_blocks * fi.ysize_blocks
+    nt = fi.xsize_tiles * fi.ysize_tiles
+    bufs = {
+        "quant_field": pin(nb, torch.uint8), "ytox": pin(nt, torch.int8),
+        "ytob": pin(nt, torch.int8), "quant_dc": pin(3 * nb, torch.int16),
+        "tokens": pin(2 * fi.max_tokens, torch.int32),
+        "group_offsets": pin(fi.num_groups + 1, torch.int64),
+        "histograms": pin(L.NUM_FINE_AC_CONTEXTS * L.ALPHABET_SIZE, torch.int32),
+    }
+    out = L.FrontendOutput()
+    out.quant_field = bufs["quant_field"].data_ptr()
+    out.ytox_map = bufs["ytox"].data_ptr()
+    out.ytob_map = bufs["ytob"].data_ptr()
+    out.quant_dc = bufs["quant_dc"].data_ptr()
+    out.tokens = bufs["tokens"].data_ptr()
+    out.token_capacity = fi.max_tokens
+    out.group_offsets = bufs["group_offsets"].data_ptr()
+    out.histograms = bufs["histograms"].data_ptr()
+    params = L.FrameParams()
+    c_cfgs = [c._c() for c in cfgs]
+    d2h = [0]
+
+    def step():
+        d2h[0] = 0
+        for c in c_cfgs:
+            st = lib.jxg_frontend(ctx.handle, ctypes.c_void_p(h_img.data_ptr()), WIDTH, HEIGHT, 3, 8,
+                                  ctypes.byref(c), ctypes.byref(params), ctypes.byref(out))
+            if st:
+                raise RuntimeError(f"jxg_frontend status {st}")
+            d2h[0] += (nb + 2 * nt + 6 * nb + params.num_tokens * 8 + (fi.num_groups + 1) * 8
+                       + L.NUM_FINE_AC_CONTEXTS * L.ALPHABET_SIZE * 4)
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize(dev)
+    dt = time.perf_counter() - t0
+    t = torch.tensor([dt], device=dev, dtype=torch.float64)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    dt = float(t.item())
+    value = world * args.steps * len(QUALITIES) * WIDTH * HEIGHT / 1e6 / dt
+    return {"value": value, "unit": "MP/s", "h2d_bytes_per_step": len(QUALITIES) * img.size,
+            "d2h_bytes_per_step": int(d2h[0]),
+            "path": "jxg_frontend (C ABI): pinned host RGB in; maps, DC levels, tokens, group "
+                    "offsets and histograms out"}
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

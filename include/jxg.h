@@ -1,0 +1,198 @@
+/*
+ * jxg.h -- C ABI of the GB300 VarDCT front end.
+ *
+ * Plain pointers and sizes only.  One jxg_context owns one CUDA stream and the
+ * device buffers of one frame; calls on different contexts are thread-safe,
+ * calls on one context are serialised by the caller.  Status codes mirror the
+ * reference's `EncodeError` variants (src/util.rs:129-160); 0 is success.
+ *
+ * Each entry point names the reference interface it stands in for.
+ */
+#ifndef JXG_H_
+#define JXG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes: EncodeError (src/util.rs:129-160) plus device failures. */
+#define JXG_OK 0
+#define JXG_ERR_EMPTY_IMAGE 1         /* EncodeError::EmptyImage */
+#define JXG_ERR_INPUT_SIZE_MISMATCH 2 /* EncodeError::InputSizeMismatch */
+#define JXG_ERR_ALPHA_SIZE_MISMATCH 3 /* EncodeError::AlphaSizeMismatch */
+#define JXG_ERR_INVALID_DISTANCE 4    /* EncodeError::InvalidDistance */
+#define JXG_ERR_QUALITY_IS_NAN 5      /* EncodeError::QualityIsNaN */
+#define JXG_ERR_DIMENSION_TOO_LARGE 6 /* EncodeError::DimensionTooLarge */
+#define JXG_ERR_ALLOCATION_FAILED 7   /* EncodeError::AllocationFailed */
+#define JXG_ERR_UNSUPPORTED 8         /* EncodeError::Unsupported */
+#define JXG_ERR_BAD_CHANNEL_COUNT 9   /* EncodeError::BadChannelCount */
+#define JXG_ERR_BAD_BIT_DEPTH 10      /* EncodeError::BadBitDepth */
+#define JXG_ERR_INVALID_ARGUMENT 100  /* null pointer, short output buffer, ... */
+#define JXG_ERR_CUDA 101              /* a CUDA runtime call failed */
+#define JXG_ERR_DEVICE_TIMEOUT 102    /* a bounded device wait gave up */
+
+/* Speed (src/encode_image.rs:256-286).  This build runs UltraFast's gates
+ * (src/effort.rs:305-309); other tiers return JXG_ERR_UNSUPPORTED. */
+#define JXG_SPEED_ULTRAFAST 0
+#define JXG_SPEED_FASTEST 1
+#define JXG_SPEED_FAST 2
+#define JXG_SPEED_MEDIUM 3
+#define JXG_SPEED_MEDIUM_SLOW 4
+#define JXG_SPEED_SLOW 5
+#define JXG_SPEED_EXTRA_SLOW 6
+
+/* The part of `EncodeConfig` (src/encode_image.rs:326-588) the front end
+ * reads: distance (set it from a quality with jxg_distance_from_quality, as
+ * `with_quality`, src/encode_image.rs:986, does), speed and the host thread
+ * budget (`with_num_threads`, :1251).  The device result never depends on
+ * num_threads. */
+typedef struct jxg_config {
+  float distance;
+  int32_t speed;
+  int32_t num_threads;
+  int32_t reserved[5];
+} jxg_config;
+
+/* Frame geometry (`ImageDim`, src/frame.rs:84-124). */
+typedef struct jxg_frame_info {
+  uint64_t width, height;
+  uint64_t xsize_blocks, ysize_blocks; /* 8x8 blocks */
+  uint64_t xsize_tiles, ysize_tiles;   /* 64x64 chroma-from-luma tiles */
+  uint64_t xsize_groups, ysize_groups; /* 256x256 AC groups */
+  uint64_t num_groups, num_dc_groups;  /* groups; 2048x2048 DC groups */
+  uint64_t max_tokens;                 /* upper bound of the token count */
+} jxg_frame_info;
+
+/* Per-frame scalars: `DistanceParams` (src/frame/quantization.rs:35-48)
+ * after the frame's chroma gates, plus what pass one derives. */
+typedef struct jxg_frame_params {
+  float distance;
+  int32_t global_scale;
+  int32_t quant_dc;
+  float scale;
+  float scale_dc;
+  uint32_t x_qm_scale;
+  uint32_t b_qm_scale;
+  uint32_t epf_iters;
+  float dc_step[3];
+  uint32_t qf_threshold;    /* ac_qf_threshold, src/frame/ac_groups.rs:92 */
+  uint32_t screen_content;  /* is_screen_content, src/frame/chroma.rs:42 */
+  int32_t epf_sharpness;    /* epf_sharpness_id, src/frame/quantization.rs:218 */
+  uint32_t reserved;
+  uint64_t constant_blocks; /* numerator of constant_block_fraction */
+  uint64_t num_tokens;
+} jxg_frame_params;
+
+/* `Token` (src/entropy/token.rs:30-34): fine AC context and value. */
+typedef struct jxg_token {
+  uint32_t context;
+  uint32_t value;
+} jxg_token;
+
+/* Number of fine AC contexts (`K_NUM_FINE_AC_CONTEXTS`,
+ * src/ac_context.rs:113-114) and the histogram alphabet (`ALPHABET_SIZE`,
+ * src/entropy/prefix_code.rs:30). */
+#define JXG_NUM_FINE_AC_CONTEXTS 14850
+#define JXG_ALPHABET_SIZE 128
+
+/* Caller-allocated outputs of one front-end pass; NULL members are skipped.
+ * Sizes follow jxg_frame_info.  Block maps are image rasters of blocks;
+ * the tile maps are rasters of 64x64 tiles. */
+typedef struct jxg_frontend_output {
+  uint8_t* quant_field;    /* xb*yb raw quant field (DcGroupData::raw_quant_field) */
+  uint8_t* ac_strategy;    /* xb*yb (raw << 1) | first (AcStrategyImage cells) */
+  int8_t* ytox_map;        /* tiles */
+  int8_t* ytob_map;        /* tiles */
+  int16_t* quant_dc;       /* 3 planes X, Y, B of xb*yb (DcGroupData::quant_dc) */
+  int32_t* coefficients;   /* xb*yb*192: per block X, Y, B, 64 levels each */
+  uint8_t* num_nzeros;     /* 3 planes of xb*yb */
+  float* xyb;              /* 3 planes of w*h (the opsin image) */
+  jxg_token* tokens;       /* pass-one tokens, groups in raster order */
+  uint64_t token_capacity; /* entries available in `tokens` */
+  uint64_t* group_offsets; /* num_groups + 1 token offsets */
+  uint32_t* histograms;    /* JXG_NUM_FINE_AC_CONTEXTS * JXG_ALPHABET_SIZE */
+} jxg_frontend_output;
+
+/* Library lifetime ---------------------------------------------------- */
+
+/* EncodingContext::new (src/encoding_context.rs:609): device state of one
+ * encoder on `device`. */
+int32_t jxg_context_create(int32_t device, void** out_ctx);
+void jxg_context_destroy(void* ctx);
+/* Run this context's launches on `cuda_stream` (a cudaStream_t; NULL
+ * restores the context's own stream). */
+int32_t jxg_context_set_stream(void* ctx, void* cuda_stream);
+/* Text of the last error on this context (empty when none). */
+const char* jxg_context_last_error(void* ctx);
+
+/* distance_from_quality (src/encode_image.rs:1321-1338). */
+float jxg_distance_from_quality(float quality);
+/* ImageDim::new (src/frame.rs:100-123). */
+int32_t jxg_frame_info_for(uint64_t width, uint64_t height, jxg_frame_info* out);
+/* The input checks of encode_image_rgb / encode_with_coded_planes
+ * (src/encode_image.rs:1785-1801, :4818-4827) plus this build's limits,
+ * without touching a device: returns the status jxg_frontend_run would. */
+int32_t jxg_validate_input(uint64_t width, uint64_t height, int32_t channels, int32_t bits,
+                           const jxg_config* config);
+
+/* Front end ------------------------------------------------------------
+ * Pass one of encode_frame_core_inner (src/frame/vardct_encoder.rs:798-1100)
+ * at the configured speed: linearise + XYB (src/encode_image.rs:1498,
+ * src/xyb.rs:439), chroma gates (src/frame/chroma.rs:389), per-DC-group
+ * setup_dc_group (src/frame/dc_groups.rs:127: fill_quant_field, fill_cmap,
+ * fill_ac_strategy), ac_qf_threshold (src/frame/ac_groups.rs:92) and every
+ * process_ac_group (src/frame/ac_groups.rs:116 -> write_ac_group,
+ * src/group.rs:1259), with the tokens' per-context histograms
+ * (build_histograms_with, src/entropy/write.rs:840).
+ *
+ * `pixels`: interleaved samples, `channels` 3 (RGB) or 4 (RGBA, alpha not
+ * read), `bits` 8 (sRGB, as encode_image) or 16 (linear, as
+ * encode_image_16bit with a linear transfer). */
+
+/* Host input: copies the pixels in, runs, and waits for the device. */
+int32_t jxg_frontend_run(void* ctx, const void* pixels, uint64_t width, uint64_t height,
+                         int32_t channels, int32_t bits, const jxg_config* config);
+/* Device input (`pixels` in this device's memory): enqueues the pass on the
+ * context's stream and returns without waiting. */
+int32_t jxg_frontend_run_device(void* ctx, const void* pixels, uint64_t width, uint64_t height,
+                                int32_t channels, int32_t bits, const jxg_config* config);
+/* Waits for the pass and returns its scalars. */
+int32_t jxg_frontend_params(void* ctx, jxg_frame_params* out);
+/* Waits for the pass and copies the requested outputs to host memory. */
+int32_t jxg_frontend_fetch(void* ctx, jxg_frontend_output* out);
+/* jxg_frontend_run + jxg_frontend_params + jxg_frontend_fetch. */
+int32_t jxg_frontend(void* ctx, const void* pixels, uint64_t width, uint64_t height,
+                     int32_t channels, int32_t bits, const jxg_config* config,
+                     jxg_frame_params* params, jxg_frontend_output* out);
+
+/* Operator table --------------------------------------------------------
+ * Single-stage entry points standing in for the reference's kernel
+ * dispatch table (EncodingContext, src/encoding_context.rs:224-294).  They
+ * take host buffers and run the same device kernels as the front end. */
+
+/* FillQuantFieldFn (src/adaptive_quant.rs:474) over every DC group of an XYB
+ * image: `xyb` is 3 planes of w*h floats; writes xb*yb raw field values. */
+int32_t jxg_op_fill_quant_field(void* ctx, const float* xyb, uint64_t width, uint64_t height,
+                                float distance, float inv_scale, uint8_t* quant_field);
+/* DctFn<8, 8, 64> (src/dct.rs:172, scalar dct8x8 :631): `count` blocks of 64
+ * row-major samples in, 64 coefficients (transposed storage, 1/64 scale) out. */
+int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coefficients);
+
+/* Kernel timing -------------------------------------------------------- */
+/* With `enable`, every launch of this context is bracketed by CUDA events on
+ * its stream; jxg_kernel_times sums their durations per kernel. */
+int32_t jxg_enable_kernel_timing(void* ctx, int32_t enable);
+/* Fills up to `capacity` entries of names (static strings), total
+ * milliseconds and launch counts; returns the number of kernels. */
+int32_t jxg_kernel_times(void* ctx, const char** names, double* total_ms, uint64_t* launches,
+                         int32_t capacity);
+int32_t jxg_reset_kernel_times(void* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JXG_H_ */

@@ -1,0 +1,131 @@
+"""ctypes binding of the C ABI declared in include/jxg.h.
+
+The shared library is the product; it must be built (``jixel_gb300.build``)
+before use.  There is no fallback path: a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libjxg.so")
+
+# Every symbol include/jxg.h declares, in header order.
+EXPORTS = [
+    "jxg_context_create",
+    "jxg_context_destroy",
+    "jxg_context_set_stream",
+    "jxg_context_last_error",
+    "jxg_distance_from_quality",
+    "jxg_frame_info_for",
+    "jxg_validate_input",
+    "jxg_frontend_run",
+    "jxg_frontend_run_device",
+    "jxg_frontend_params",
+    "jxg_frontend_fetch",
+    "jxg_frontend",
+    "jxg_op_fill_quant_field",
+    "jxg_op_dct8x8",
+    "jxg_enable_kernel_timing",
+    "jxg_kernel_times",
+    "jxg_reset_kernel_times",
+]
+
+NUM_FINE_AC_CONTEXTS = 14850
+ALPHABET_SIZE = 128
+
+
+class Config(ctypes.Structure):
+    _fields_ = [
+        ("distance", ctypes.c_float),
+        ("speed", ctypes.c_int32),
+        ("num_threads", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 5),
+    ]
+
+
+class FrameInfo(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "width", "height", "xsize_blocks", "ysize_blocks", "xsize_tiles", "ysize_tiles",
+        "xsize_groups", "ysize_groups", "num_groups", "num_dc_groups", "max_tokens")]
+
+
+class FrameParams(ctypes.Structure):
+    _fields_ = [
+        ("distance", ctypes.c_float),
+        ("global_scale", ctypes.c_int32),
+        ("quant_dc", ctypes.c_int32),
+        ("scale", ctypes.c_float),
+        ("scale_dc", ctypes.c_float),
+        ("x_qm_scale", ctypes.c_uint32),
+        ("b_qm_scale", ctypes.c_uint32),
+        ("epf_iters", ctypes.c_uint32),
+        ("dc_step", ctypes.c_float * 3),
+        ("qf_threshold", ctypes.c_uint32),
+        ("screen_content", ctypes.c_uint32),
+        ("epf_sharpness", ctypes.c_int32),
+        ("reserved", ctypes.c_uint32),
+        ("constant_blocks", ctypes.c_uint64),
+        ("num_tokens", ctypes.c_uint64),
+    ]
+
+
+class FrontendOutput(ctypes.Structure):
+    _fields_ = [
+        ("quant_field", ctypes.c_void_p),
+        ("ac_strategy", ctypes.c_void_p),
+        ("ytox_map", ctypes.c_void_p),
+        ("ytob_map", ctypes.c_void_p),
+        ("quant_dc", ctypes.c_void_p),
+        ("coefficients", ctypes.c_void_p),
+        ("num_nzeros", ctypes.c_void_p),
+        ("xyb", ctypes.c_void_p),
+        ("tokens", ctypes.c_void_p),
+        ("token_capacity", ctypes.c_uint64),
+        ("group_offsets", ctypes.c_void_p),
+        ("histograms", ctypes.c_void_p),
+    ]
+
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    """Load the in-tree library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build it with `python -m jixel_gb300.build` "
+            "(the front end has no CPU fallback)")
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, u64, i32, f32 = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, ctypes.c_float
+    sig = {
+        "jxg_context_create": (i32, [i32, ctypes.POINTER(vp)]),
+        "jxg_context_destroy": (None, [vp]),
+        "jxg_context_set_stream": (i32, [vp, vp]),
+        "jxg_context_last_error": (ctypes.c_char_p, [vp]),
+        "jxg_distance_from_quality": (f32, [f32]),
+        "jxg_frame_info_for": (i32, [u64, u64, ctypes.POINTER(FrameInfo)]),
+        "jxg_validate_input": (i32, [u64, u64, i32, i32, ctypes.POINTER(Config)]),
+        "jxg_frontend_run": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config)]),
+        "jxg_frontend_run_device": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config)]),
+        "jxg_frontend_params": (i32, [vp, ctypes.POINTER(FrameParams)]),
+        "jxg_frontend_fetch": (i32, [vp, ctypes.POINTER(FrontendOutput)]),
+        "jxg_frontend": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config),
+                               ctypes.POINTER(FrameParams), ctypes.POINTER(FrontendOutput)]),
+        "jxg_op_fill_quant_field": (i32, [vp, vp, u64, u64, f32, f32, vp]),
+        "jxg_op_dct8x8": (i32, [vp, vp, u64, vp]),
+        "jxg_enable_kernel_timing": (i32, [vp, i32]),
+        "jxg_kernel_times": (i32, [vp, ctypes.POINTER(ctypes.c_char_p),
+                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(u64), i32]),
+        "jxg_reset_kernel_times": (i32, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib

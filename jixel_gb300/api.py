@@ -1,0 +1,285 @@
+"""Host-side mirror of the reference encoder's front-end interface.
+
+Names follow jixel's public API (`EncodeConfig`, `Speed`, `EncodeError`,
+`distance_from_quality`, src/encode_image.rs) and its stage boundary
+(`DcGroupData` maps and `PendingAcGroup` tokens, src/dc_group_data.rs:325,
+src/frame/ac_groups.rs:78).  Every call goes to the CUDA library through the
+C ABI; nothing here computes a result itself.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+
+
+class Speed(enum.IntEnum):
+    """`Speed` (src/encode_image.rs:256-286)."""
+    ULTRA_FAST = 0
+    FASTEST = 1
+    FAST = 2
+    MEDIUM = 3
+    MEDIUM_SLOW = 4
+    SLOW = 5
+    EXTRA_SLOW = 6
+
+
+_ERRORS = {
+    1: "EmptyImage", 2: "InputSizeMismatch", 3: "AlphaSizeMismatch", 4: "InvalidDistance",
+    5: "QualityIsNaN", 6: "DimensionTooLarge", 7: "AllocationFailed", 8: "Unsupported",
+    9: "BadChannelCount", 10: "BadBitDepth", 100: "InvalidArgument", 101: "Cuda",
+    102: "DeviceTimeout",
+}
+
+
+class EncodeError(Exception):
+    """`EncodeError` (src/util.rs:129-160); `variant` names the reference case."""
+
+    def __init__(self, code: int, detail: str = ""):
+        self.code = code
+        self.variant = _ERRORS.get(code, f"Status{code}")
+        super().__init__(f"{self.variant}: {detail}" if detail else self.variant)
+
+
+def distance_from_quality(quality: float) -> float:
+    """`distance_from_quality` (src/encode_image.rs:1321-1338)."""
+    if quality != quality:
+        raise EncodeError(5, "quality must not be NaN")
+    return float(L.load().jxg_distance_from_quality(float(quality)))
+
+
+@dataclass
+class EncodeConfig:
+    """The part of `EncodeConfig` (src/encode_image.rs:326-588) the front end reads."""
+    distance: float = 1.0
+    speed: Speed = Speed.FAST
+    num_threads: int = field(default_factory=lambda: os.cpu_count() or 1)
+
+    def with_quality(self, quality: float) -> "EncodeConfig":
+        self.distance = distance_from_quality(quality)
+        return self
+
+    def with_distance(self, distance: float) -> "EncodeConfig":
+        self.distance = float(distance)
+        return self
+
+    def with_speed(self, speed: Speed) -> "EncodeConfig":
+        self.speed = Speed(speed)
+        return self
+
+    def with_num_threads(self, n: int) -> "EncodeConfig":
+        self.num_threads = max(1, int(n))
+        return self
+
+    def _c(self) -> L.Config:
+        c = L.Config()
+        c.distance = self.distance
+        c.speed = int(self.speed)
+        c.num_threads = self.num_threads
+        return c
+
+
+def validate_input(width: int, height: int, channels: int, bits: int,
+                   config: EncodeConfig) -> None:
+    """Raise the `EncodeError` the front end would return for these inputs."""
+    cfg = config._c()
+    st = L.load().jxg_validate_input(width, height, channels, bits, ctypes.byref(cfg))
+    if st:
+        raise EncodeError(st)
+
+
+@dataclass
+class FrameInfo:
+    width: int
+    height: int
+    xsize_blocks: int
+    ysize_blocks: int
+    xsize_tiles: int
+    ysize_tiles: int
+    xsize_groups: int
+    ysize_groups: int
+    num_groups: int
+    num_dc_groups: int
+    max_tokens: int
+
+
+def frame_info(width: int, height: int) -> FrameInfo:
+    fi = L.FrameInfo()
+    st = L.load().jxg_frame_info_for(width, height, ctypes.byref(fi))
+    if st:
+        raise EncodeError(st)
+    return FrameInfo(*[getattr(fi, n) for n, _ in L.FrameInfo._fields_])
+
+
+@dataclass
+class FrontendResult:
+    """Pass-one output of the VarDCT front end for one frame."""
+    params: dict
+    quant_field: np.ndarray   # (yb, xb) u8
+    ac_strategy: np.ndarray   # (yb, xb) u8, (raw << 1) | first
+    ytox: np.ndarray          # (ty, tx) i8
+    ytob: np.ndarray
+    quant_dc: np.ndarray      # (3, yb, xb) i16, X Y B
+    coefficients: np.ndarray | None  # (yb, xb, 3, 64) i32
+    num_nzeros: np.ndarray    # (3, yb, xb) u8
+    tokens: np.ndarray        # (n, 2) u32: context, value
+    group_offsets: np.ndarray  # (groups + 1,) u64
+    histograms: np.ndarray    # (14850, 128) u32
+    xyb: np.ndarray | None = None
+
+
+def _pixels_kind(pixels: np.ndarray) -> tuple[int, int]:
+    if pixels.ndim != 3 or pixels.shape[2] not in (3, 4):
+        raise EncodeError(9, f"expected (h, w, 3|4) samples, got {pixels.shape}")
+    if pixels.dtype == np.uint8:
+        return pixels.shape[2], 8
+    if pixels.dtype == np.uint16:
+        return pixels.shape[2], 16
+    raise EncodeError(10, f"unsupported sample type {pixels.dtype}")
+
+
+class FrontendContext:
+    """One device encoder (`EncodingContext`, src/encoding_context.rs:609)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = L.load()
+        self._ctx = ctypes.c_void_p()
+        st = self._lib.jxg_context_create(device, ctypes.byref(self._ctx))
+        if st:
+            raise EncodeError(st, "could not create a CUDA context for the front end")
+
+    def close(self):
+        if self._ctx:
+            self._lib.jxg_context_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int):
+        if st:
+            msg = self._lib.jxg_context_last_error(self._ctx)
+            raise EncodeError(st, msg.decode() if msg else "")
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._ctx
+
+    def set_stream(self, stream_ptr: int | None):
+        self._check(self._lib.jxg_context_set_stream(self._ctx, stream_ptr or None))
+
+    def run(self, pixels: np.ndarray, config: EncodeConfig):
+        """Host input: copy in, run, wait (jxg_frontend_run)."""
+        pixels = np.ascontiguousarray(pixels)
+        ch, bits = _pixels_kind(pixels)
+        h, w = pixels.shape[:2]
+        cfg = config._c()
+        self._check(self._lib.jxg_frontend_run(self._ctx, pixels.ctypes.data, w, h, ch, bits,
+                                               ctypes.byref(cfg)))
+
+    def run_device(self, device_ptr: int, width: int, height: int, channels: int, bits: int,
+                   config: EncodeConfig):
+        """Device input: enqueue only (jxg_frontend_run_device)."""
+        cfg = config._c()
+        self._check(self._lib.jxg_frontend_run_device(self._ctx, device_ptr, width, height,
+                                                      channels, bits, ctypes.byref(cfg)))
+
+    def params(self) -> dict:
+        p = L.FrameParams()
+        self._check(self._lib.jxg_frontend_params(self._ctx, ctypes.byref(p)))
+        out = {n: getattr(p, n) for n, _ in L.FrameParams._fields_ if n != "reserved"}
+        out["dc_step"] = list(p.dc_step)
+        out["screen_content"] = bool(out["screen_content"])
+        return out
+
+    def fetch(self, width: int, height: int, *, coefficients: bool = True,
+              xyb: bool = False) -> FrontendResult:
+        fi = frame_info(width, height)
+        p = self.params()
+        xb, yb = fi.xsize_blocks, fi.ysize_blocks
+        r = FrontendResult(
+            params=p,
+            quant_field=np.zeros((yb, xb), np.uint8),
+            ac_strategy=np.zeros((yb, xb), np.uint8),
+            ytox=np.zeros((fi.ysize_tiles, fi.xsize_tiles), np.int8),
+            ytob=np.zeros((fi.ysize_tiles, fi.xsize_tiles), np.int8),
+            quant_dc=np.zeros((3, yb, xb), np.int16),
+            coefficients=np.zeros((yb, xb, 3, 64), np.int32) if coefficients else None,
+            num_nzeros=np.zeros((3, yb, xb), np.uint8),
+            tokens=np.zeros((max(int(p["num_tokens"]), 1), 2), np.uint32),
+            group_offsets=np.zeros(fi.num_groups + 1, np.uint64),
+            histograms=np.zeros((L.NUM_FINE_AC_CONTEXTS, L.ALPHABET_SIZE), np.uint32),
+            xyb=np.zeros((3, height, width), np.float32) if xyb else None,
+        )
+        o = L.FrontendOutput()
+        o.quant_field = r.quant_field.ctypes.data
+        o.ac_strategy = r.ac_strategy.ctypes.data
+        o.ytox_map = r.ytox.ctypes.data
+        o.ytob_map = r.ytob.ctypes.data
+        o.quant_dc = r.quant_dc.ctypes.data
+        o.coefficients = r.coefficients.ctypes.data if coefficients else None
+        o.num_nzeros = r.num_nzeros.ctypes.data
+        o.xyb = r.xyb.ctypes.data if xyb else None
+        o.tokens = r.tokens.ctypes.data
+        o.token_capacity = r.tokens.shape[0]
+        o.group_offsets = r.group_offsets.ctypes.data
+        o.histograms = r.histograms.ctypes.data
+        self._check(self._lib.jxg_frontend_fetch(self._ctx, ctypes.byref(o)))
+        r.tokens = r.tokens[: int(p["num_tokens"])]
+        return r
+
+    def frontend(self, pixels: np.ndarray, config: EncodeConfig, *, coefficients: bool = True,
+                 xyb: bool = False) -> FrontendResult:
+        self.run(pixels, config)
+        return self.fetch(pixels.shape[1], pixels.shape[0], coefficients=coefficients, xyb=xyb)
+
+    # operator table -----------------------------------------------------
+    def fill_quant_field(self, xyb: np.ndarray, distance: float, inv_scale: float) -> np.ndarray:
+        xyb = np.ascontiguousarray(xyb, np.float32)
+        _, h, w = xyb.shape
+        fi = frame_info(w, h)
+        out = np.zeros((fi.ysize_blocks, fi.xsize_blocks), np.uint8)
+        self._check(self._lib.jxg_op_fill_quant_field(self._ctx, xyb.ctypes.data, w, h, distance,
+                                                      inv_scale, out.ctypes.data))
+        return out
+
+    def dct8x8(self, blocks: np.ndarray) -> np.ndarray:
+        blocks = np.ascontiguousarray(blocks, np.float32).reshape(-1, 64)
+        out = np.zeros_like(blocks)
+        self._check(self._lib.jxg_op_dct8x8(self._ctx, blocks.ctypes.data, blocks.shape[0],
+                                            out.ctypes.data))
+        return out
+
+    # timing -------------------------------------------------------------
+    def enable_kernel_timing(self, on: bool = True):
+        self._check(self._lib.jxg_enable_kernel_timing(self._ctx, 1 if on else 0))
+
+    def kernel_times(self) -> dict:
+        cap = 64
+        names = (ctypes.c_char_p * cap)()
+        ms = (ctypes.c_double * cap)()
+        cnt = (ctypes.c_uint64 * cap)()
+        n = self._lib.jxg_kernel_times(self._ctx, names, ms, cnt, cap)
+        if n < 0:
+            self._check(n)
+        return {names[i].decode(): (ms[i], cnt[i]) for i in range(min(n, cap))}
+
+    def reset_kernel_times(self):
+        self._check(self._lib.jxg_reset_kernel_times(self._ctx))
+
+
+def encode_frontend(pixels: np.ndarray, config: EncodeConfig, device: int = 0) -> FrontendResult:
+    """One-shot front end: the device half of `encode_image` (src/encode_image.rs:1610)."""
+    ctx = FrontendContext(device)
+    try:
+        return ctx.frontend(pixels, config)
+    finally:
+        ctx.close()

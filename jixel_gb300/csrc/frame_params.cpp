@@ -1,0 +1,330 @@
+// Host-side per-frame constants.  Compiled with -ffp-contract=off: every
+// fused multiply-add below is an explicit std::fma, as the reference's
+// `fmla` (src/dct.rs:31-41) is on aarch64.
+#include "frame_params.h"
+#include "library_dct8.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace jxg {
+namespace {
+
+inline float fmla(float a, float b, float c) { return std::fma(a, b, c); }
+
+inline int32_t cast_i32(float v) {  // Rust `as i32`
+  if (std::isnan(v)) return 0;
+  if (v >= 2147483647.0f) return INT32_MAX;
+  if (v <= -2147483648.0f) return INT32_MIN;
+  return static_cast<int32_t>(v);
+}
+
+inline float clamp(float v, float lo, float hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+uint16_t to_half(float v) {  // IEEE binary16, round to nearest even
+  uint32_t bits;
+  std::memcpy(&bits, &v, 4);
+  uint16_t sign = static_cast<uint16_t>((bits >> 16) & 0x8000u);
+  int32_t e = static_cast<int32_t>((bits >> 23) & 0xFF) - 112;
+  uint32_t mant = bits & 0x7FFFFFu;
+  if (e >= 31) return sign | 0x7BFF;
+  if (e <= 0) {
+    if (e < -10) return sign;
+    uint32_t m = mant | 0x800000u;
+    uint32_t shift = static_cast<uint32_t>(14 - e);
+    uint32_t r = (m + (1u << (shift - 1)) - 1 + ((m >> shift) & 1)) >> shift;
+    return sign | static_cast<uint16_t>(r);
+  }
+  uint32_t m = (mant + 0xFFFu + ((mant >> 13) & 1)) >> 13;
+  uint32_t ex = static_cast<uint32_t>(e);
+  if (m == 0x400) {
+    m = 0;
+    if (++ex >= 31) return sign | 0x7BFF;
+  }
+  return sign | static_cast<uint16_t>(ex << 10) | static_cast<uint16_t>(m);
+}
+
+float from_half(uint16_t h) {
+  uint32_t e = (h >> 10) & 0x1F, m = h & 0x3FF;
+  float v;
+  if (e == 0) {
+    v = (1.0f / 16384.0f) * (static_cast<float>(m) * (1.0f / 1024.0f));
+  } else if (e == 31) {
+    v = m ? NAN : INFINITY;
+  } else {
+    uint32_t b = ((e + 112u) << 23) | (m << 13);
+    std::memcpy(&v, &b, 4);
+  }
+  return (h >> 15) ? -v : v;
+}
+
+inline float half_round(float v) { return from_half(to_half(v)); }
+
+// dcepf_vlq_t, src/frame/quantization.rs:72-75
+inline float vlq_t(float d) { return clamp((d - 8.0f) / (15.0f - 8.0f), 0.0f, 1.0f); }
+
+// quant_dc, src/frame/quantization.rs:56-86
+float luma_dc_quant(float d) {
+  float refine;
+  if (d <= 3.0f) {
+    refine = 1.35f;
+  } else if (d >= 5.0f) {
+    refine = 1.0f;
+  } else {
+    const float recip = 1.0f / (5.0f - 3.0f);
+    refine = fmla(1.0f - 1.35f, (d - 3.0f) * recip, 1.35f);
+  }
+  float vlq = fmla(vlq_t(d), 0.7f - 1.0f, 1.0f);
+  float eff = 2.9f * std::pow(d / 2.9f, 0.57f);
+  eff = clamp(eff, 0.5f * d, d);
+  return std::min(1.12f / eff, 50.0f) * refine * vlq;
+}
+
+// luma_dc_coarsening, src/frame/quantization.rs:163-178
+float dc_coarsening(float d) {
+  float t;
+  if (d <= 1.25f || d >= 5.0f) t = 0.0f;
+  else if (d < 1.75f) t = (d - 1.25f) / (1.75f - 1.25f);
+  else if (d <= 4.25f) t = 1.0f;
+  else t = (5.0f - d) / (5.0f - 4.25f);
+  return fmla(t, 1.15f - 1.0f, 1.0f);
+}
+
+const float kDcQuant[3] = {1.0f / 4096.0f, 1.0f / 512.0f, 1.0f / 256.0f};
+const float kInvDcQuant[3] = {4096.0f, 512.0f, 256.0f};
+
+// signaled_dc_step, src/color_correlation.rs:1835-1838
+float wire_dc_step(int c, float mul) {
+  return half_round(kDcQuant[c] * 128.0f * mul) / (kDcQuant[c] * 128.0f);
+}
+
+// DCT8 band parameters (src/quant_weights.rs:123-131)
+const float kDct8Bands[3][6] = {{3150.0f, 0.0f, -0.4f, -0.4f, -0.4f, -2.0f},
+                                {560.0f, 0.0f, -0.3f, -0.3f, -0.3f, -0.3f},
+                                {512.0f, -2.0f, -1.0f, 0.0f, -1.0f, -2.0f}};
+const float kFlatB8Hq[6] = {512.0f, -0.5f, -0.25f, 0.0f, -0.25f, -0.5f};
+const float kFlatB8Mid[6] = {512.0f, -0.13f, -0.235f, -0.276f, -0.609f, -0.339f};
+
+inline float band_mult(float v) { return v > 0.0f ? 1.0f + v : 1.0f / (1.0f - v); }
+
+void round_bands(float b[3][6]) {
+  for (int c = 0; c < 3; ++c)
+    for (int i = 0; i < 6; ++i)
+      b[c][i] = i == 0 ? half_round(b[c][i] / 64.0f) * 64.0f : half_round(b[c][i]);
+}
+
+}  // namespace
+
+float distance_from_quality(float quality) {
+  float q = clamp(quality, 0.0f, 100.0f);
+  float d;
+  if (q >= 99.0f) d = 0.05f * std::pow(2.0f, 100.0f - q);
+  else if (q >= 90.0f) d = std::pow(10.0f, (99.0f - q) / 9.0f - 1.0f);
+  else if (q >= 30.0f) d = 0.1f + (100.0f - q) * 0.09f;
+  else d = 6.24f + std::pow(2.5f, (30.0f - q) / 5.0f) / 6.25f;
+  return std::min(d, 25.0f);
+}
+
+int compute_distance_params(float distance, DistanceParams* p) {
+  if (!(distance > 0.0f) || std::isinf(distance)) return 1;
+  const float d = std::max(distance, 0.05f);  // MIN_DISTANCE, src/encode_image.rs:95
+  float fine = luma_dc_quant(d);
+  float coarsen = dc_coarsening(d);
+  float qdc = fine / coarsen;
+  float scale = 65536.0f * 0.8f / (d * 10.0f);
+  int32_t gs = std::clamp(cast_i32(std::round(scale)), 1, 1 << 15);
+  float scale_f = static_cast<float>(gs) / 65536.0f;
+  int32_t qd = std::clamp(cast_i32((qdc / scale_f) + 0.5f), 1, 1 << 16);
+  p->distance = d;
+  p->global_scale = gs;
+  p->quant_dc = qd;
+  p->scale = scale_f;
+  p->scale_dc = static_cast<float>(qd) * scale_f;
+  p->x_qm_scale = 2u + (d >= 1.25f) + (d > 9.0f) + (d < 0.299f);
+  p->b_qm_scale = 2;
+  uint32_t iters = (d >= 0.7f) + (d >= 1.5f);
+  float t = vlq_t(d);
+  bool pass0 = d >= 2.5f && t < 0.5f;  // epf_pass0_scale is Some
+  if (pass0 || t >= 0.5f) iters = 3;
+  p->epf_iters = iters;
+  // chroma_dc_steps, src/frame/quantization.rs:188-194
+  float growth = std::max(luma_dc_quant(3.5f) / fine, 1.0f);
+  float x = 2.0f * std::pow(growth, 0.75f - 1.0f);
+  float b = std::pow(growth, 0.5f - 1.0f);
+  p->dc_step[0] = wire_dc_step(0, x / coarsen);
+  p->dc_step[1] = wire_dc_step(1, 1.0f);
+  p->dc_step[2] = wire_dc_step(2, b / coarsen);
+  p->x_qm_mul = std::pow(1.25f, static_cast<float>(p->x_qm_scale) - 2.0f);
+  static const float kBMul[6] = {1.0f, 1.25f, 1.5625f, 1.953125f, 2.4414062f, 3.0517578f};
+  p->b_qm_mul = kBMul[p->b_qm_scale - 2];
+  return 0;
+}
+
+int dct8_tables(float distance, float matrix[3][64], float inv[3][64]) {
+  const float d = std::max(distance, 0.05f);
+  if (d < 0.3f) {
+    // DequantMatrices::new below the flat-B gate: the library table
+    // (src/quant_weights.rs:2261-2291, :1986-1992)
+    for (int c = 0; c < 3; ++c) {
+      std::memcpy(matrix[c], kLibraryDct8Bits[c], sizeof(float) * 64);
+      inv[c][0] = 0.0f;
+      for (int k = 1; k < 64; ++k) inv[c][k] = 1.0f / matrix[c][k];
+    }
+    return 0;
+  }
+  const bool ss2 = d >= 2.25f;
+  const bool coarse = ss2 && d >= 3.5f;
+  const float* flat = d >= 1.25f ? kFlatB8Mid : kFlatB8Hq;
+  float bands[3][6];
+  std::memcpy(bands, kDct8Bands, sizeof(bands));
+  if (coarse) {  // coarse_dct8_override, src/quant_weights.rs:170-200
+    float step = std::pow(1.25f, 1.0f / 5.0f);
+    for (int i = 1; i < 6; ++i) {
+      float r = band_mult(kDct8Bands[1][i]) * step;
+      bands[1][i] = r > 1.0f ? r - 1.0f : 1.0f - 1.0f / r;
+    }
+    round_bands(bands);
+  }
+  std::memcpy(bands[2], flat, sizeof(float) * 6);
+  round_bands(bands);
+  // compute_dct8x8_matrix, src/quant_weights.rs:1564-1586
+  for (int c = 0; c < 3; ++c) {
+    float acc[6];
+    acc[0] = bands[c][0];
+    for (int i = 1; i < 6; ++i) acc[i] = acc[i - 1] * band_mult(bands[c][i]);
+    float sc = (6.0f - 1.0f) / (1.41421356237309505f + 1e-6f);
+    float rcp = sc / 7.0f;
+    for (int y = 0; y < 8; ++y) {
+      float dy = static_cast<float>(y) * rcp;
+      float dy2 = dy * dy;
+      for (int x = 0; x < 8; ++x) {
+        float dx = static_cast<float>(x) * rcp;
+        float pos = std::sqrt(fmla(dx, dx, dy2));
+        float fl = std::floor(pos);
+        float frac = pos - fl;
+        size_t idx = static_cast<size_t>(fl);
+        float a = acc[idx], bb = acc[idx + 1];
+        matrix[c][y * 8 + x] = 1.0f / (std::pow(bb / a, frac) * a);
+      }
+    }
+    inv[c][0] = 0.0f;
+    for (int k = 1; k < 64; ++k) inv[c][k] = 1.0f / matrix[c][k];
+  }
+  return 0;
+}
+
+void fill_kernel_args(const DistanceParams& p, KernelArgs* a) {
+  const float d = p.distance;
+  a->distance = d;
+  a->scale = p.scale;
+  a->inv_scale = 1.0f / p.scale;
+  for (int c = 0; c < 3; ++c) a->inv_dc_factor[c] = kInvDcQuant[c] / p.dc_step[c] * p.scale_dc;
+  // dc_cfl_factor_x / dc_cfl_factor, src/color_correlation.rs:1598-1611
+  a->cfl_dc_factor_x = kInvDcQuant[0] / p.dc_step[0] * (kDcQuant[1] * p.dc_step[1]) * 0.0f;
+  a->cfl_dc_factor_b =
+      kInvDcQuant[2] / p.dc_step[2] * (kDcQuant[1] * p.dc_step[1]) * (1.0f + 0.0f / 84.0f);
+  a->qm_mul[0] = p.x_qm_mul;
+  a->qm_mul[1] = 1.0f;
+  a->qm_mul[2] = p.b_qm_mul;
+  // quantize_ac_thresholds_scaled, src/group.rs:420-455 (one 8x8 block)
+  for (int c = 0; c < 3; ++c) {
+    float normal[4] = {0.58f, 0.635f, 0.66f, 0.7f};
+    if (c == 0) {
+      float up = clamp((d - 0.5f) / (0.75f - 0.5f), 0.0f, 1.0f);
+      float down = clamp((2.0f - d) / (2.0f - 1.5f), 0.0f, 1.0f);
+      float w = std::min(up, down);
+      normal[0] += w * (0.5f - normal[0]);
+      for (int i = 1; i < 4; ++i) normal[i] += (1.0f - w) * 0.08f;
+    } else if (c == 2) {
+      float hf = a->qm_mul[2] > 1.0f ? 0.65f : 0.75f;
+      for (int i = 1; i < 4; ++i) normal[i] = hf;
+    }
+    const float hq_y[4] = {0.50f, 0.51f, 0.52f, 0.54f};
+    const float* hq = c == 1 ? hq_y : normal;
+    float t = clamp((d - 0.1f) / 0.9f, 0.0f, 1.0f);
+    for (int i = 0; i < 4; ++i) a->thresholds[c][i] = hq[i] + t * (normal[i] - hq[i]);
+  }
+  // fill_quant_field_scalar stage 3 and FuzzyErosion weights,
+  // src/adaptive_quant.rs:658-700 and :103-120
+  static const float knots[7] = {0.5f, 1.0f, 1.4f, 1.75f, 3.0f, 5.0f, 8.0f};
+  static const float strength[7] = {0.26565f, 0.275459f, 0.058287f, 0.0f, 0.0f, 0.0f, 0.0f};
+  static const float base[7] = {0.636493f, 0.648351f, 0.606759f, 0.48f, 0.48f, 0.48f, 0.48f};
+  auto sched = [&](const float* v) {
+    if (d <= knots[0]) return v[0];
+    for (int i = 1; i < 7; ++i)
+      if (d <= knots[i]) {
+        float f = (d - knots[i - 1]) / (knots[i] - knots[i - 1]);
+        return v[i - 1] + f * (v[i] - v[i - 1]);
+      }
+    return v[6];
+  };
+  float aq_scale = 0.8294f / d;
+  float base_level = sched(base) * aq_scale;
+  float dampen = clamp(sched(strength), 0.0f, 1.0f);
+  a->aq_mul = aq_scale * dampen;
+  a->aq_add = (1.0f - dampen) * base_level;
+  a->aq_hf_strength = clamp(1.06836f * d, 0.1f, 0.890398f);
+  float fe_mul = d < 2.0f ? (2.0f - d) * 0.5f : 0.0f;
+  const float fe_base[4] = {0.125f, 0.1f, 0.09f, 0.06f};
+  const float fe_add[4] = {0.0f, -0.1f, -0.09f, -0.06f};
+  float norm = 0.0f;
+  for (int i = 0; i < 4; ++i) {
+    a->aq_fe_weights[i] = fe_base[i] + fe_mul * fe_add[i];
+    norm += a->aq_fe_weights[i];
+  }
+  const float total = 0.29959705784054957f;
+  for (int i = 0; i < 4; ++i) a->aq_fe_weights[i] *= total / norm;
+  // cfl_deadzone, src/color_correlation.rs:384-394
+  if (d <= 1.0f) a->cfl_deadzone = 1.5f;
+  else if (d >= 2.0f) a->cfl_deadzone = 0.0f;
+  else a->cfl_deadzone = (1.5f / (2.0f - 1.0f)) * (2.0f - d);
+}
+
+int32_t epf_sharpness_id(float d, bool screen) {
+  float t = vlq_t(d);
+  if (t >= 0.75f) return 1;
+  if (t >= 0.5f) return 2;
+  if (t >= 0.25f) return 3;
+  if (d < 1.4f || (screen && d < 5.0f)) return 7;
+  if (d < 1.75f) return 6;
+  if (d < 3.5f) return 5;
+  return 4;
+}
+
+bool is_screen_content(uint64_t constant_blocks, uint64_t w, uint64_t h) {
+  uint64_t bw = w / 8, bh = h / 8;
+  if (bw == 0 || bh == 0) return false;
+  return static_cast<float>(constant_blocks) / static_cast<float>(bw * bh) >= 0.15f;
+}
+
+void srgb_to_linear_table(float out[256]) {
+  // srgb_to_linear_u8_ref, src/color.rs:35-42: f64 math, f32 result
+  for (int v = 0; v < 256; ++v) {
+    double x = static_cast<double>(v) * (1.0 / 255.0);
+    out[v] = static_cast<float>(x <= 0.04045 ? x / 12.92 : std::pow((x + 0.055) / 1.055, 2.4));
+  }
+}
+
+void exp2_table(float out[64]) {
+  // fast_exp2's table: 2^((i - 32) / 64) rounded to f32
+  for (int i = 0; i < 64; ++i) out[i] = static_cast<float>(std::exp2((i - 32) / 64.0));
+}
+
+void natural_order_8x8(uint8_t scan[64], uint8_t position[64]) {
+  // Zig-zag over anti-diagonals, odd diagonals walked with x and y swapped,
+  // DC first (CoeffOrderAndLut with cx = cy = 1, src/coeff_order.rs:203-244).
+  int k = 0;
+  for (int s = 0; s < 15; ++s) {
+    int lo = std::max(0, s - 7), hi = std::min(7, s);
+    for (int j = lo; j <= hi; ++j) {
+      int a = (s & 1) ? j : s - j;  // row in storage
+      int b = s - a;
+      // even diagonals run up-right from (row=s..), matching the scan table
+      scan[k++] = static_cast<uint8_t>(a * 8 + b);
+    }
+  }
+  for (int i = 0; i < 64; ++i) position[scan[i]] = static_cast<uint8_t>(i);
+}
+
+}  // namespace jxg

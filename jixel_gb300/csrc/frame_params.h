@@ -1,0 +1,71 @@
+// Host-side per-frame constants of the VarDCT front end: distance parameters,
+// quant tables, the sRGB transfer table and the kernel argument block.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+namespace jxg {
+
+constexpr int kBlockDim = 8;
+constexpr int kTileDim = 64;
+constexpr int kGroupDim = 256;
+constexpr int kDcGroupDim = 2048;
+constexpr int kGroupBlocks = 32;
+constexpr int kTileBlocks = 8;
+constexpr int kFineBlockCtxs = 30;
+constexpr int kNonZeroBuckets = 37;
+constexpr int kZeroDensityCtxs = 458;
+constexpr int kNumFineAcContexts = kFineBlockCtxs * (kNonZeroBuckets + kZeroDensityCtxs);
+constexpr int kAlphabet = 128;
+
+// DistanceParams (src/frame/quantization.rs:35-48) resolved for an
+// UltraFast XYB frame.
+struct DistanceParams {
+  float distance;
+  int32_t global_scale;
+  int32_t quant_dc;
+  float scale;
+  float scale_dc;
+  uint32_t x_qm_scale;
+  uint32_t b_qm_scale;
+  uint32_t epf_iters;
+  float dc_step[3];
+  float x_qm_mul;
+  float b_qm_mul;
+};
+
+// Everything a kernel needs about one frame, passed by value (< 4 KB).
+struct KernelArgs {
+  int32_t width, height;
+  int32_t xb, yb;          // blocks
+  int32_t tiles_x, tiles_y;
+  int32_t groups_x, groups_y;
+  int32_t plane;           // float elements between XYB planes
+  float distance;
+  float scale;             // quantizer scale (global_scale / 2^16)
+  float inv_scale;         // 1 / scale, the AQ field's divisor
+  float inv_dc_factor[3];  // INV_DC_QUANT / dc_step * scale_dc
+  float cfl_dc_factor_x;   // dc_cfl_factor_x (0 for XYB bases)
+  float cfl_dc_factor_b;   // dc_cfl_factor with ytob_dc = 0
+  float qm_mul[3];         // x_qm_mul, 1, b_qm_mul
+  float thresholds[3][4];  // quantize_ac_thresholds_scaled per channel
+  float aq_mul, aq_add, aq_hf_strength, aq_fe_weights[4];
+  float cfl_deadzone;
+  float matrix[3][64];     // DCT8 dequant weights
+  float inv_matrix[3][64]; // their reciprocals (index 0 = 0)
+};
+
+int compute_distance_params(float distance, DistanceParams* out);
+// DCT8 tables of DequantMatrices::new_fast (the library table below d = 0.3).
+int dct8_tables(float distance, float matrix[3][64], float inv[3][64]);
+void fill_kernel_args(const DistanceParams& p, KernelArgs* a);
+float distance_from_quality(float quality);
+int32_t epf_sharpness_id(float distance, bool screen_content);
+bool is_screen_content(uint64_t constant_blocks, uint64_t width, uint64_t height);
+void srgb_to_linear_table(float out[256]);
+void exp2_table(float out[64]);
+// libjxl natural 8x8 order: scan position -> raw coefficient index.
+void natural_order_8x8(uint8_t scan[64], uint8_t position[64]);
+
+}  // namespace jxg

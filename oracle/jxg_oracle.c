@@ -1,0 +1,1363 @@
+/*
+ * jxg_oracle.c -- CPU oracle for the VarDCT front end.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file restates, in plain C, the scalar path
+ * of the Rust JPEG XL encoder jixel 0.5.14 for the UltraFast VarDCT front end
+ * (XYB, frame statistics, adaptive quant field, chroma-from-luma tiles,
+ * DCT8 + quantisation, tokens and per-context histograms).  It exists to check
+ * the CUDA path and to be timed as the CPU baseline; the product library never
+ * links, loads or calls it.  Only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference legs of bench.py use it.
+ *
+ * Semantics fixed here (the reference's result depends on CPU dispatch):
+ *   - the scalar twins of every kernel;
+ *   - `fmla` is a fused multiply-add (src/dct.rs:31-41, aarch64 semantic);
+ *   - `round` rounds half away from zero (Rust f32::round);
+ *   - float -> int casts saturate and send NaN to 0 (Rust `as`);
+ *   - num_threads does not change any result (each unit owns its outputs).
+ *
+ * Every function names the reference file:line it follows.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_OK 0
+#define ORC_ERR_EMPTY 1
+#define ORC_ERR_INPUT 2
+#define ORC_ERR_DISTANCE 4
+#define ORC_ERR_UNSUPPORTED 8
+#define ORC_ERR_ALLOC 9
+
+#define BLOCK 8
+#define TILE 64
+#define GROUP 256
+#define DC_GROUP 2048
+#define GROUP_BLOCKS 32
+#define TILE_BLOCKS 8
+
+#define NUM_FINE_BLOCK_CTXS 30
+#define NON_ZERO_BUCKETS 37
+#define ZERO_DENSITY_CONTEXTS 458
+#define NUM_FINE_AC_CONTEXTS (NUM_FINE_BLOCK_CTXS * (NON_ZERO_BUCKETS + ZERO_DENSITY_CONTEXTS))
+#define ALPHABET 128
+
+/* ------------------------------------------------------------------ */
+/* Rust scalar semantics                                               */
+/* ------------------------------------------------------------------ */
+
+static inline float fmla(float a, float b, float c) { return fmaf(a, b, c); }
+
+static inline int32_t sat_i32(float v) {
+  if (v != v) return 0;
+  if (v >= 2147483647.0f) return INT32_MAX;
+  if (v <= -2147483648.0f) return INT32_MIN;
+  return (int32_t)v;
+}
+
+static inline int16_t sat_i16(float v) {
+  if (v != v) return 0;
+  if (v >= 32767.0f) return 32767;
+  if (v <= -32768.0f) return -32768;
+  return (int16_t)v;
+}
+
+static inline float clampf(float v, float lo, float hi) {
+  return v < lo ? lo : (v > hi ? hi : v);
+}
+
+static inline float rmin(float a, float b) { return fminf(a, b); }
+static inline float rmax(float a, float b) { return fmaxf(a, b); }
+
+static inline uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+static inline float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+
+/* IEEE binary16 conversion with round-to-nearest-even
+ * (src/util.rs:382-411 and its hardware twins). */
+static uint16_t f32_to_f16(float v) {
+  uint32_t bits = f2u(v);
+  uint16_t sign = (uint16_t)((bits >> 16) & 0x8000u);
+  int32_t exp = (int32_t)((bits >> 23) & 0xFF);
+  uint32_t mant = bits & 0x7FFFFFu;
+  int32_t e16 = exp - 112;
+  if (e16 >= 31) return sign | 0x7BFF;
+  if (e16 <= 0) {
+    if (e16 < -10) return sign;
+    uint32_t m = mant | 0x800000u;
+    uint32_t shift = (uint32_t)(14 - e16);
+    uint32_t rounded = (m + (1u << (shift - 1)) - 1 + ((m >> shift) & 1)) >> shift;
+    return sign | (uint16_t)rounded;
+  }
+  uint32_t m = mant + 0xFFFu + ((mant >> 13) & 1);
+  uint32_t e = (uint32_t)e16;
+  uint32_t m16 = m >> 13;
+  if (m16 == 0x400) {
+    m16 = 0;
+    e += 1;
+    if (e >= 31) return sign | 0x7BFF;
+  }
+  return sign | (uint16_t)(e << 10) | (uint16_t)m16;
+}
+
+static float f16_to_f32(uint16_t b) {
+  uint32_t sign = b >> 15;
+  uint32_t e = (b >> 10) & 0x1F;
+  uint32_t m = b & 0x3FF;
+  float v;
+  if (e == 0) {
+    v = (1.0f / 16384.0f) * ((float)m * (1.0f / 1024.0f));
+  } else if (e == 31) {
+    v = m ? NAN : INFINITY;
+  } else {
+    v = u2f(((e + 112u) << 23) | (m << 13));
+  }
+  return sign ? -v : v;
+}
+
+static inline float f16_round(float v) { return f16_to_f32(f32_to_f16(v)); }
+
+/* ------------------------------------------------------------------ */
+/* Quality and distance parameters                                      */
+/* ------------------------------------------------------------------ */
+
+/* src/encode_image.rs:1321-1338 */
+float orc_distance_from_quality(float quality) {
+  float q = clampf(quality, 0.0f, 100.0f);
+  float d;
+  if (q >= 99.0f) d = 0.05f * powf(2.0f, 100.0f - q);
+  else if (q >= 90.0f) d = powf(10.0f, (99.0f - q) / 9.0f - 1.0f);
+  else if (q >= 30.0f) d = 0.1f + (100.0f - q) * 0.09f;
+  else d = 6.24f + powf(2.5f, (30.0f - q) / 5.0f) / 6.25f;
+  return rmin(d, 25.0f);
+}
+
+/* src/frame/quantization.rs:56-66 */
+static float dc_refinement(float d) {
+  if (d <= 3.0f) return 1.35f;
+  if (d >= 5.0f) return 1.0f;
+  const float recip = 1.0f / (5.0f - 3.0f);
+  float t = (d - 3.0f) * recip;
+  return fmla(1.0f - 1.35f, t, 1.35f);
+}
+
+/* src/frame/quantization.rs:72-75 */
+static float dcepf_vlq_t(float d) {
+  return clampf((d - 8.0f) / (15.0f - 8.0f), 0.0f, 1.0f);
+}
+
+/* src/frame/quantization.rs:77-86 */
+static float quant_dc_of(float d) {
+  float refine = dc_refinement(d);
+  float vlq = fmla(dcepf_vlq_t(d), 0.7f - 1.0f, 1.0f);
+  float effective = 2.9f * powf(d / 2.9f, 0.57f);
+  effective = clampf(effective, 0.5f * d, d);
+  return rmin(1.12f / effective, 50.0f) * refine * vlq;
+}
+
+/* src/frame/quantization.rs:163-178 */
+static float luma_dc_coarsening(float d) {
+  const float a = 1.25f, b = 1.75f, c = 4.25f, e = 5.0f;
+  float t;
+  if (d <= a || d >= e) t = 0.0f;
+  else if (d < b) t = (d - a) / (b - a);
+  else if (d <= c) t = 1.0f;
+  else t = (e - d) / (e - c);
+  return fmla(t, 1.15f - 1.0f, 1.0f);
+}
+
+/* src/color_correlation.rs:1835-1844 */
+static float signaled_dc_step(int c, float mul) {
+  static const float dc_quant[3] = {1.0f / 4096.0f, 1.0f / 512.0f, 1.0f / 256.0f};
+  float wire = dc_quant[c] * 128.0f * mul;
+  return f16_round(wire) / (dc_quant[c] * 128.0f);
+}
+
+/* src/frame/quantization.rs:196-216 */
+static float epf_pass0_scale(float d, int* some) {
+  *some = 0;
+  if (d < 2.5f) return 0.0f;
+  float t = dcepf_vlq_t(d);
+  if (t >= 0.5f) return 0.0f;
+  *some = 1;
+  return fmla(2.0f * t, 0.9f - 3.6f, 3.6f);
+}
+
+typedef struct {
+  float distance;
+  int32_t global_scale;
+  int32_t quant_dc;
+  float scale;
+  float scale_dc;
+  uint32_t x_qm_scale;
+  uint32_t b_qm_scale;
+  uint32_t epf_iters;
+  float dc_step[3];
+  float x_qm_mul;
+  float b_qm_mul;
+} orc_params;
+
+/* src/frame/quantization.rs:89-156 plus the XYB floors of
+ * src/frame/vardct_encoder.rs:834-840 and src/frame/chroma.rs:410-413
+ * (UltraFast: no pixel-chromacity steps, so both floors are 2). */
+int orc_params_for(float distance, orc_params* p) {
+  if (!(distance > 0.0f) || isinf(distance)) return ORC_ERR_DISTANCE;
+  float d = rmax(distance, 0.05f);
+  memset(p, 0, sizeof(*p));
+  float qdc_fine = quant_dc_of(d);
+  float coarsen = luma_dc_coarsening(d);
+  float qdc = qdc_fine / coarsen;
+  float scale = 65536.0f * 0.8f / (d * 10.0f);
+  int32_t gs = sat_i32(roundf(scale));
+  if (gs < 1) gs = 1;
+  if (gs > (1 << 15)) gs = 1 << 15;
+  float scale_f = (float)gs / 65536.0f;
+  int32_t qd = sat_i32((qdc / scale_f) + 0.5f);
+  if (qd < 1) qd = 1;
+  if (qd > (1 << 16)) qd = 1 << 16;
+  p->distance = d;
+  p->global_scale = gs;
+  p->quant_dc = qd;
+  p->scale = scale_f;
+  p->scale_dc = (float)qd * scale_f;
+  uint32_t x = 2;
+  if (d >= 1.25f) x += 1;
+  if (d > 9.0f) x += 1;
+  if (d < 0.299f) x += 1;
+  p->x_qm_scale = x; /* max(x, floor=2) */
+  p->b_qm_scale = 2;
+  uint32_t iters = 0;
+  if (d >= 0.7f) iters++;
+  if (d >= 1.5f) iters++;
+  int some;
+  (void)epf_pass0_scale(d, &some);
+  if (some || dcepf_vlq_t(d) >= 0.5f) iters = 3;
+  p->epf_iters = iters;
+  /* src/frame/quantization.rs:188-194 */
+  float growth = rmax(quant_dc_of(3.5f) / qdc_fine, 1.0f);
+  float steps[3] = {2.0f * powf(growth, 0.75f - 1.0f), 1.0f, powf(growth, 0.5f - 1.0f)};
+  float in[3] = {steps[0] / coarsen, steps[1], steps[2] / coarsen};
+  for (int c = 0; c < 3; c++) p->dc_step[c] = signaled_dc_step(c, in[c]);
+  p->x_qm_mul = powf(1.25f, (float)p->x_qm_scale - 2.0f);
+  static const float b_mul[6] = {1.0f, 1.25f, 1.5625f, 1.953125f, 2.4414062f, 3.0517578f};
+  p->b_qm_mul = b_mul[p->b_qm_scale - 2];
+  return ORC_OK;
+}
+
+/* src/frame/quantization.rs:218-239 */
+int32_t orc_epf_sharpness_id(float distance, int screen_content) {
+  float t = dcepf_vlq_t(distance);
+  if (t >= 0.75f) return 1;
+  if (t >= 0.5f) return 2;
+  if (t >= 0.25f) return 3;
+  if (distance < 1.4f || (screen_content && distance < 5.0f)) return 7;
+  if (distance < 1.75f) return 6;
+  if (distance < 3.5f) return 5;
+  return 4;
+}
+
+/* ------------------------------------------------------------------ */
+/* DCT8 quant table (src/quant_weights.rs)                              */
+/* ------------------------------------------------------------------ */
+
+static const float DCT8_BANDS[3][6] = {
+    {3150.0f, 0.0f, -0.4f, -0.4f, -0.4f, -2.0f},
+    {560.0f, 0.0f, -0.3f, -0.3f, -0.3f, -0.3f},
+    {512.0f, -2.0f, -1.0f, 0.0f, -1.0f, -2.0f},
+};
+static const float FLAT_B8_HQ[6] = {512.0f, -0.5f, -0.25f, 0.0f, -0.25f, -0.5f};
+static const float FLAT_B8_MID[6] = {512.0f, -0.13f, -0.235f, -0.276f, -0.609f, -0.339f};
+
+/* src/quant_weights.rs:1002-1004 */
+static float band_mult(float v) { return v > 0.0f ? 1.0f + v : 1.0f / (1.0f - v); }
+
+/* src/quant_weights.rs:1372-1379 */
+static float interpolate_bands(float pos, const float* bands) {
+  float idx_f = floorf(pos);
+  float frac = pos - idx_f;
+  size_t idx = (size_t)idx_f;
+  float a = bands[idx];
+  float b = bands[idx + 1];
+  return powf(b / a, frac) * a;
+}
+
+/* src/quant_weights.rs:140-200: default / coarse DCT8 override, B row
+ * replaced by `flat`, every parameter F16 round-tripped. */
+static void dct8_override(int coarse, const float* flat, float out[3][6]) {
+  for (int c = 0; c < 3; c++)
+    for (int i = 0; i < 6; i++) out[c][i] = DCT8_BANDS[c][i];
+  if (coarse) {
+    float hf_step = powf(1.25f, 1.0f / 5.0f);
+    for (int i = 1; i < 6; i++) {
+      float ratio = band_mult(DCT8_BANDS[1][i]) * hf_step;
+      out[1][i] = ratio > 1.0f ? ratio - 1.0f : 1.0f - 1.0f / ratio;
+    }
+    for (int c = 0; c < 3; c++)
+      for (int i = 0; i < 6; i++)
+        out[c][i] = i == 0 ? f16_round(out[c][i] / 64.0f) * 64.0f : f16_round(out[c][i]);
+  }
+  for (int i = 0; i < 6; i++) out[2][i] = flat[i];
+  for (int c = 0; c < 3; c++)
+    for (int i = 0; i < 6; i++)
+      out[c][i] = i == 0 ? f16_round(out[c][i] / 64.0f) * 64.0f : f16_round(out[c][i]);
+}
+
+/* src/quant_weights.rs:1564-1586 and fill_ac_reciprocals :3136-3141 */
+static void dct8_matrix_from(const float bands_in[3][6], float* matrix, float* inv) {
+  for (int c = 0; c < 3; c++) {
+    float bands[6];
+    bands[0] = bands_in[c][0];
+    for (int i = 1; i < 6; i++) bands[i] = bands[i - 1] * band_mult(bands_in[c][i]);
+    float scale = (6.0f - 1.0f) / (1.41421356237309505f + 1e-6f);
+    float rcp = scale / 7.0f;
+    for (int y = 0; y < 8; y++) {
+      float dy = (float)y * rcp;
+      float dy2 = dy * dy;
+      for (int x = 0; x < 8; x++) {
+        float dx = (float)x * rcp;
+        float dist = sqrtf(fmla(dx, dx, dy2));
+        matrix[c * 64 + y * 8 + x] = 1.0f / interpolate_bands(dist, bands);
+      }
+    }
+    inv[c * 64] = 0.0f;
+    for (int k = 1; k < 64; k++) inv[c * 64 + k] = 1.0f / matrix[c * 64 + k];
+  }
+}
+
+#include "library_dct8.inc"
+
+/* DequantMatrices::new_fast (src/quant_weights.rs:2294-2339) restricted to
+ * its DCT8 table; arbiter SSIMULACRA2 (qm_ss2_distance 2.25).  Below 0.3 it
+ * falls to DequantMatrices::new -> the library table (src/quant_weights.rs:
+ * 2261-2291, shared_tables :1986-1992). */
+int orc_dct8_tables(float distance, float* matrix, float* inv) {
+  float d = rmax(distance, 0.05f);
+  if (d < 0.3f) {
+    for (int c = 0; c < 3; c++) {
+      for (int k = 0; k < 64; k++) matrix[c * 64 + k] = u2f(LIBRARY_DCT8_BITS[c][k]);
+      inv[c * 64] = 0.0f;
+      for (int k = 1; k < 64; k++) inv[c * 64 + k] = 1.0f / matrix[c * 64 + k];
+    }
+    return ORC_OK;
+  }
+  float bands[3][6];
+  if (d >= 2.25f) dct8_override(d >= 3.5f, FLAT_B8_MID, bands);
+  else if (d >= 1.25f) dct8_override(0, FLAT_B8_MID, bands);
+  else dct8_override(0, FLAT_B8_HQ, bands);
+  dct8_matrix_from(bands, matrix, inv);
+  return ORC_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* sRGB -> linear and XYB                                               */
+/* ------------------------------------------------------------------ */
+
+/* src/color.rs:35-42 */
+void orc_srgb_lut(float* lut) {
+  for (int v = 0; v < 256; v++) {
+    double x = (double)v * (1.0 / 255.0);
+    lut[v] = (float)(x <= 0.04045 ? x / 12.92 : pow((x + 0.055) / 1.055, 2.4));
+  }
+}
+
+#define OPSIN_BIAS 0.0037930734f
+#define NEG_BIAS_CBRT (-0.1559542f)
+
+/* src/xyb.rs:145-150 */
+static inline float halley(float x, float a) {
+  float tx = x * x * x;
+  return x * fmla(2.0f, a, tx) / fmla(2.0f, tx, a);
+}
+
+/* src/xyb.rs:152-167: bit-hack seed (B1 = 709958130) + two Halley steps */
+static inline float xyb_cbrtf(float x) {
+  if (x == 0.0f) return x;
+  uint32_t ui = f2u(x);
+  uint32_t hx = ui & 0x7fffffffu;
+  hx = hx / 3u + 709958130u;
+  ui &= 0x80000000u;
+  ui |= hx;
+  float t = u2f(ui);
+  t = halley(t, x);
+  return halley(t, x);
+}
+
+/* XybMatrix::SPEC (src/xyb.rs:35-48, :81-85) */
+static void opsin_matrix(float m[9]) {
+  const float m00 = 0.30f, m02 = 0.078f;
+  const float m01 = 1.0f - m02 - m00;
+  const float m10 = 0.23f, m12 = 0.078f;
+  const float m11 = 1.0f - m12 - m10;
+  const float b_bias = 0.55180986f;
+  const float ratio = 0.24342269f / (0.24342269f + 0.20476745f);
+  const float m20 = ratio * (1.0f - b_bias);
+  const float m21 = (1.0f - ratio) * (1.0f - b_bias);
+  const float m22 = 1.0f - m20 - m21;
+  m[0] = m00; m[1] = m01; m[2] = m02;
+  m[3] = m10; m[4] = m11; m[5] = m12;
+  m[6] = m20; m[7] = m21; m[8] = m22;
+}
+
+void orc_opsin_matrix(float* m) { opsin_matrix(m); }
+
+/* src/xyb.rs:172-185 */
+static inline void rgb_to_xyb(const float m[9], float r, float g, float b, float* ox,
+                              float* oy, float* ob) {
+  float mixed0 = fmla(m[0], r, fmla(m[1], g, fmla(m[2], b, OPSIN_BIAS)));
+  float mixed1 = fmla(m[3], r, fmla(m[4], g, fmla(m[5], b, OPSIN_BIAS)));
+  float mixed2 = fmla(m[6], r, fmla(m[7], g, fmla(m[8], b, OPSIN_BIAS)));
+  float tm0 = xyb_cbrtf(rmax(mixed0, 0.0f)) + NEG_BIAS_CBRT;
+  float tm1 = xyb_cbrtf(rmax(mixed1, 0.0f)) + NEG_BIAS_CBRT;
+  float tm2 = xyb_cbrtf(rmax(mixed2, 0.0f)) + NEG_BIAS_CBRT;
+  *ox = 0.5f * (tm0 - tm1);
+  *oy = 0.5f * (tm0 + tm1);
+  *ob = tm2;
+}
+
+/* linearize_rgb (src/encode_image.rs:1498-1519) + to_xyb_in_place
+ * (src/xyb.rs:439-470): RGB8 (3 or 4 channels, alpha ignored) or 16-bit
+ * linear RGB (TransferLut::build with the Linear transfer,
+ * src/color.rs:318-323: v / 65535 clamped to [0, 1]). */
+void orc_to_xyb(const void* pixels, int bytes_per_sample, int channels, size_t w, size_t h,
+                float* xyb) {
+  float lut[256];
+  float m[9];
+  orc_srgb_lut(lut);
+  opsin_matrix(m);
+  size_t n = w * h;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+  for (size_t i = 0; i < n; i++) {
+    float r, g, b;
+    if (bytes_per_sample == 1) {
+      const uint8_t* p = (const uint8_t*)pixels + i * (size_t)channels;
+      r = lut[p[0]];
+      g = lut[p[1]];
+      b = lut[p[2]];
+    } else {
+      const uint16_t* p = (const uint16_t*)pixels + i * (size_t)channels;
+      r = clampf((float)p[0] / 65535.0f, 0.0f, 1.0f);
+      g = clampf((float)p[1] / 65535.0f, 0.0f, 1.0f);
+      b = clampf((float)p[2] / 65535.0f, 0.0f, 1.0f);
+    }
+    rgb_to_xyb(m, r, g, b, &xyb[i], &xyb[n + i], &xyb[2 * n + i]);
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Frame statistics (src/frame/chroma.rs)                               */
+/* ------------------------------------------------------------------ */
+
+/* constant_block_fraction numerator (src/frame/chroma.rs:48-68) */
+uint64_t orc_constant_blocks(const float* xyb, size_t w, size_t h) {
+  size_t bw = w / 8, bh = h / 8, n = w * h;
+  uint64_t count = 0;
+  for (size_t by = 0; by < bh; by++)
+    for (size_t bx = 0; bx < bw; bx++) {
+      int constant = 1;
+      for (int c = 0; c < 3 && constant; c++) {
+        const float* p = xyb + (size_t)c * n;
+        float v = p[by * 8 * w + bx * 8];
+        for (int iy = 0; iy < 8 && constant; iy++)
+          for (int ix = 0; ix < 8; ix++)
+            if (!(p[(by * 8 + iy) * w + bx * 8 + ix] == v)) { constant = 0; break; }
+      }
+      count += (uint64_t)constant;
+    }
+  return count;
+}
+
+/* is_screen_content (src/frame/chroma.rs:42-44) */
+int orc_is_screen_content(uint64_t constant, size_t w, size_t h) {
+  size_t bw = w / 8, bh = h / 8;
+  if (bw == 0 || bh == 0) return 0;
+  return (float)constant / (float)(bw * bh) >= 0.15f;
+}
+
+/* ------------------------------------------------------------------ */
+/* Adaptive quantisation (src/adaptive_quant.rs)                        */
+/* ------------------------------------------------------------------ */
+
+#define K_SG_MUL 226.77216153508914f
+#define K_SG_MUL2 (1.0f / 73.377132366608819f)
+#define K_LOG2 0.693147181f
+#define K_SG_RET_MUL (K_SG_MUL2 * 18.6580932135f * K_LOG2)
+#define K_SG_V_OFFSET 7.7825991679894591f
+
+/* src/adaptive_quant.rs:53-64 (both INVERT forms) */
+static inline float ratio_gamma(float v, int invert) {
+  const float eps = 1e-2f;
+  v = v < 0.0f ? 0.0f : v;
+  const float num_mul = K_SG_RET_MUL * 3.0f * K_SG_MUL;
+  const float v_offset = K_SG_V_OFFSET * K_LOG2 + eps;
+  const float den_mul = K_LOG2 * K_SG_MUL;
+  float v2 = v * v;
+  float num = num_mul * v2 + eps;
+  float den = (den_mul * v) * v2 + v_offset;
+  return invert ? num / den : den / num;
+}
+
+/* src/adaptive_quant.rs:67-83 */
+static inline float compute_mask(float out_val) {
+  const float k_base = -0.699765f;
+  const float k_mul4 = 9.4708735624378946f;
+  const float k_mul2 = 17.35036561631863f;
+  const float k_offset2 = 302.59587815579727f;
+  const float k_mul3 = 6.7943250517376494f;
+  const float k_offset3 = 3.7179635626140772f;
+  const float k_offset4 = 0.25f * k_offset3;
+  const float k_mul0 = 1.07267f;
+  float v1 = rmax(out_val * k_mul0, 1e-3f);
+  float v2 = 1.0f / (v1 + k_offset2);
+  float v3 = 1.0f / (v1 * v1 + k_offset3);
+  float v4 = 1.0f / (v1 * v1 + k_offset4);
+  return fmla(k_mul4, v4, fmla(k_mul2, v2, fmla(k_mul3, v3, k_base)));
+}
+
+/* src/adaptive_quant.rs:86-92 */
+static inline float masking_sqrt(float v) {
+  const float k_log_offset = 27.505837037000106f;
+  const float k_mul = 211.66567973503678f;
+  const float mul_v = k_mul * 1e8f;
+  return 0.25f * sqrtf(fmla(v, sqrtf(mul_v), k_log_offset));
+}
+
+static const float AQ_KNOTS[7] = {0.5f, 1.0f, 1.4f, 1.75f, 3.0f, 5.0f, 8.0f};
+static const float AQ_STRENGTH[7] = {0.26565f, 0.275459f, 0.058287f, 0.0f, 0.0f, 0.0f, 0.0f};
+static const float AQ_BASE[7] = {0.636493f, 0.648351f, 0.606759f, 0.48f, 0.48f, 0.48f, 0.48f};
+
+/* src/adaptive_quant.rs:105-116 */
+static float aq_schedule(const float* values, float d) {
+  if (d <= AQ_KNOTS[0]) return values[0];
+  for (int i = 1; i < 7; i++)
+    if (d <= AQ_KNOTS[i]) {
+      float f = (d - AQ_KNOTS[i - 1]) / (AQ_KNOTS[i] - AQ_KNOTS[i - 1]);
+      return values[i - 1] + f * (values[i] - values[i - 1]);
+    }
+  return values[6];
+}
+
+/* src/adaptive_quant.rs:739-765 fast_exp2: 2^(i/64) table lookup, where the
+ * table holds 2^((i - 32) / 64) rounded to f32 (FreeBSD exp2f method). */
+static float exp2_table[64];
+static int exp2_table_ready = 0;
+static void init_exp2_table(void) {
+  if (exp2_table_ready) return;
+  for (int i = 0; i < 64; i++) exp2_table[i] = (float)exp2((double)(i - 32) / 64.0);
+  exp2_table_ready = 1;
+}
+void orc_exp2_table(float* out) {
+  init_exp2_table();
+  memcpy(out, exp2_table, sizeof(exp2_table));
+}
+
+static inline float fast_exp2(float d) {
+  const float redux = u2f(0x4b400000u) / 64.0f;
+  uint32_t ui = f2u(d + redux);
+  uint32_t i0 = ui + 32u;
+  uint32_t k = i0 / 64u;
+  i0 &= 63u;
+  float uf = u2f(ui);
+  uf -= redux;
+  float z0 = exp2_table[i0];
+  float f = d - uf;
+  float u = 0.24022650695908768f;
+  u = fmla(u, f, 0.69314718055994973f);
+  u *= f;
+  float i2 = u2f((uint32_t)((int32_t)k + 0x7f) << 23);
+  return fmla(u, z0, z0) * i2;
+}
+
+/* src/adaptive_quant.rs:768-783 */
+static inline float dirty_log2f(float d) {
+  uint32_t ix = f2u(d);
+  ix += 0x3f800000u - 0x3f3504f3u;
+  int32_t n = (int32_t)(ix >> 23) - 0x7f;
+  ix = (ix & 0x007fffffu) + 0x3f3504f3u;
+  float a = u2f(ix);
+  float x = (a - 1.0f) / (a + 1.0f);
+  float x2 = x * x;
+  float u = 0.4121985850084821691e+0f;
+  u = fmla(u, x2, 0.5770780163490337802e+0f);
+  u = fmla(u, x2, 0.9617966939259845749e+0f);
+  return fmla(x2 * x, u, fmla(x, 0.2885390081777926802e+1f, (float)n));
+}
+
+float orc_fast_exp2(float d) { init_exp2_table(); return fast_exp2(d); }
+float orc_dirty_log2f(float d) { return dirty_log2f(d); }
+
+static inline size_t minz(size_t a, size_t b) { return a < b ? a : b; }
+
+/* src/adaptive_quant.rs:410-433 */
+static float gamma_modulation(size_t x, size_t y, const float* xyb, size_t w, size_t h,
+                              float out_val) {
+  const float k_bias = 0.16f;
+  float overall = 0.0f;
+  const float* px = xyb;
+  const float* py = xyb + w * h;
+  for (size_t dy = 0; dy < 8; dy++) {
+    size_t ry = minz(y + dy, h - 1);
+    for (size_t dx = 0; dx < 8; dx++) {
+      size_t cx = minz(x + dx, w - 1);
+      float iny = py[ry * w + cx] + k_bias;
+      float inx = px[ry * w + cx];
+      float r = iny - inx;
+      float g = iny + inx;
+      float rr = ratio_gamma(r, 1);
+      float rg = ratio_gamma(g, 1);
+      overall = fmla(0.5f, rr + rg, overall);
+    }
+  }
+  overall *= 1.0f / 64.0f;
+  const float k_gam = 0.119146f;
+  return fmla(k_gam, dirty_log2f(overall), out_val);
+}
+
+/* src/adaptive_quant.rs:122-148 */
+static float hf_modulation(size_t x, size_t y, const float* xyb, size_t w, size_t h,
+                           float out_val, float strength) {
+  const float* yp = xyb + w * h;
+  const float valmin = 0.0206f;
+  float sum = 0.0f;
+  for (size_t dy = 0; dy < 8; dy++) {
+    const float* row = yp + minz(y + dy, h - 1) * w;
+    const float* next = dy == 7 ? row : yp + minz(y + dy + 1, h - 1) * w;
+    for (size_t dx = 0; dx < 8; dx++) {
+      size_t c0 = minz(x + dx, w - 1);
+      float p = row[c0];
+      if (dx < 7) sum += rmin(valmin, fabsf(p - row[minz(x + dx + 1, w - 1)]));
+      sum += rmin(valmin, fabsf(p - next[c0]));
+    }
+  }
+  float k_mul = -0.506626f * strength;
+  const float k_offset = 0.655866f;
+  return fmla(sum, k_mul, k_offset) + out_val;
+}
+
+/* src/adaptive_quant.rs:153-183 */
+static float blue_modulation(size_t x, size_t y, const float* xyb, size_t w, size_t h,
+                             float out_val) {
+  const float k_limit = 0.010474084867598155f;
+  const float k_offset = 0.0031994768654636393f;
+  const float* xp = xyb;
+  const float* yp = xyb + w * h;
+  const float* bp = xyb + 2 * w * h;
+  float sum = 0.0f;
+  for (size_t dy = 0; dy < 8; dy++) {
+    size_t ry = minz(y + dy, h - 1);
+    for (size_t dx = 0; dx < 8; dx++) {
+      size_t cx = minz(x + dx, w - 1);
+      float p_x = xp[ry * w + cx];
+      float p_b = bp[ry * w + cx];
+      float p_y = yp[ry * w + cx] + k_offset + fabsf(p_x);
+      if (p_b > p_y) sum += rmin(p_b - p_y, k_limit);
+    }
+  }
+  const float k_mul = 0.127191f;
+  float s = sum;
+  if (s >= 32.0f * k_limit) s = 64.0f * k_limit - s;
+  const float k_max_limit = 15.463398341612438f;
+  if (s >= k_max_limit * k_limit) s = k_max_limit * k_limit;
+  s *= k_mul;
+  return s + out_val;
+}
+
+static inline void sort4(float a[4]) {
+#define CSWAP(i, j) if (a[i] > a[j]) { float t_ = a[i]; a[i] = a[j]; a[j] = t_; }
+  CSWAP(0, 1) CSWAP(2, 3) CSWAP(0, 2) CSWAP(1, 3) CSWAP(1, 2)
+#undef CSWAP
+}
+
+static inline void store_min4(float v, float m[4]) {
+  if (v < m[3]) {
+    if (v < m[0]) { m[3] = m[2]; m[2] = m[1]; m[1] = m[0]; m[0] = v; }
+    else if (v < m[1]) { m[3] = m[2]; m[2] = m[1]; m[1] = v; }
+    else if (v < m[2]) { m[3] = m[2]; m[2] = v; }
+    else m[3] = v;
+  }
+}
+
+/* fill_quant_field_scalar (src/adaptive_quant.rs:547-727) for the DC group
+ * whose pixel origin is (x0, y0) and whose block extent is xb x yb.  Writes
+ * the raw field into `qf` (image block raster, stride `qf_stride`). */
+static void fill_quant_field(const float* xyb, size_t w, size_t h, size_t x0, size_t y0,
+                             size_t xb, size_t yb, float distance, float inv_scale,
+                             uint8_t* qf, size_t qf_stride) {
+  const float* yp = xyb + w * h;
+  float scale = 0.8294f / distance;
+  size_t rw = xb * 8, rh = yb * 8;
+  size_t pw = rw / 4, ph = rh / 4;
+  float* acc = (float*)malloc(rw * sizeof(float));
+  float* pre = (float*)malloc(pw * ph * sizeof(float));
+  float* aq = (float*)malloc(xb * yb * sizeof(float));
+  for (size_t ry = 0; ry < rh; ry++) {
+    long gy = (long)(y0 + ry);
+    size_t gyc = (size_t)(gy < (long)h - 1 ? gy : (long)h - 1);
+    size_t gy1 = (size_t)(gy - 1 < 0 ? 0 : (gy - 1 > (long)h - 1 ? (long)h - 1 : gy - 1));
+    size_t gy2 = (size_t)(gy + 1 > (long)h - 1 ? (long)h - 1 : gy + 1);
+    const float* row = yp + gyc * w;
+    const float* row1 = yp + gy1 * w;
+    const float* row2 = yp + gy2 * w;
+    for (size_t rx = 0; rx < rw; rx++) {
+      long gx = (long)(x0 + rx);
+      size_t gxc = (size_t)(gx < (long)w - 1 ? gx : (long)w - 1);
+      size_t gx1 = (size_t)(gx - 1 < 0 ? 0 : (gx - 1 > (long)w - 1 ? (long)w - 1 : gx - 1));
+      size_t gx2 = (size_t)(gx + 1 > (long)w - 1 ? (long)w - 1 : gx + 1);
+      float in_y = row[gxc];
+      float base = 0.25f * (row2[gxc] + row1[gxc] + row[gx1] + row[gx2]);
+      float gammac = ratio_gamma(in_y + 0.019f, 0);
+      float diff = gammac * (in_y - base);
+      diff *= diff;
+      if (diff >= 0.2f) diff = 0.2f;
+      diff = masking_sqrt(diff);
+      if ((ry & 3) != 0) acc[rx] += diff;
+      else acc[rx] = diff;
+    }
+    if (ry % 4 == 3) {
+      float* prow = pre + (ry / 4) * pw;
+      for (size_t px = 0; px < pw; px++)
+        prow[px] = (acc[px * 4] + acc[px * 4 + 1] + acc[px * 4 + 2] + acc[px * 4 + 3]) * 0.25f;
+    }
+  }
+  float fe_mul = distance < 2.0f ? (2.0f - distance) * 0.5f : 0.0f;
+  const float fe_base[4] = {0.125f, 0.1f, 0.09f, 0.06f};
+  const float fe_add[4] = {0.0f, -0.1f, -0.09f, -0.06f};
+  float kmul[4];
+  float norm = 0.0f;
+  for (int i = 0; i < 4; i++) {
+    kmul[i] = fe_base[i] + fe_mul * fe_add[i];
+    norm += kmul[i];
+  }
+  const float k_total = 0.29959705784054957f;
+  for (int i = 0; i < 4; i++) kmul[i] *= k_total / norm;
+  for (size_t fy = 0; fy < ph; fy++) {
+    size_t ym1 = fy >= 1 ? fy - 1 : fy;
+    size_t yp1 = fy + 1 < ph ? fy + 1 : fy;
+    const float* rt = pre + ym1 * pw;
+    const float* r = pre + fy * pw;
+    const float* rb = pre + yp1 * pw;
+    for (size_t fx = 0; fx < pw; fx++) {
+      size_t xm1 = fx >= 1 ? fx - 1 : fx;
+      size_t xp1 = fx + 1 < pw ? fx + 1 : fx;
+      float m[4] = {r[fx], r[xm1], r[xp1], rt[xm1]};
+      sort4(m);
+      store_min4(rt[fx], m);
+      store_min4(rt[xp1], m);
+      store_min4(rb[xm1], m);
+      store_min4(rb[fx], m);
+      store_min4(rb[xp1], m);
+      float v = kmul[0] * m[0] + kmul[1] * m[1] + kmul[2] * m[2] + kmul[3] * m[3];
+      size_t idx = (fy / 2) * xb + fx / 2;
+      if (fx % 2 == 0 && fy % 2 == 0) aq[idx] = v;
+      else aq[idx] += v;
+    }
+  }
+  float base_level = aq_schedule(AQ_BASE, distance) * scale;
+  float dampen = clampf(aq_schedule(AQ_STRENGTH, distance), 0.0f, 1.0f);
+  float mul = scale * dampen;
+  float add = (1.0f - dampen) * base_level;
+  float strength = clampf(1.06836f * distance, 0.1f, 0.890398f);
+  for (size_t by = 0; by < yb; by++) {
+    size_t py = y0 + by * 8;
+    for (size_t bx = 0; bx < xb; bx++) {
+      size_t px = x0 + bx * 8;
+      uint8_t* out = qf + (y0 / 8 + by) * qf_stride + x0 / 8 + bx;
+      if (px >= w || py >= h) { *out = 1; continue; }
+      size_t bxp = minz(px, w >= 8 ? w - 8 : 0);
+      size_t byp = minz(py, h >= 8 ? h - 8 : 0);
+      float mask = compute_mask(aq[by * xb + bx]);
+      mask = gamma_modulation(bxp, byp, xyb, w, h, mask);
+      float out_val = hf_modulation(bxp, byp, xyb, w, h, mask, strength);
+      out_val = rmin(out_val, blue_modulation(bxp, byp, xyb, w, h, mask));
+      float q = fast_exp2(out_val * 1.442695041f) * mul + add;
+      int32_t qi = sat_i32(fmla(q, inv_scale, 0.5f));
+      *out = (uint8_t)(qi < 1 ? 1 : (qi > 255 ? 255 : qi));
+    }
+  }
+  free(acc);
+  free(pre);
+  free(aq);
+}
+
+/* ------------------------------------------------------------------ */
+/* DCT8 (src/dct.rs:55-133, :631-659)                                   */
+/* ------------------------------------------------------------------ */
+
+static const float WC4_0 = 0.5411961f, WC4_1 = 1.306563f;
+static const float WC8[4] = {0.5097956f, 0.6013449f, 0.8999762f, 2.5629156f};
+#define SQRT2F 1.41421356237309505f
+
+static inline void dct1d_4(float* b) {
+  float t0 = b[0] + b[3];
+  float t1 = b[1] + b[2];
+  float a = t0, c = t1;
+  t0 = a + c;
+  t1 = a - c;
+  float t2 = b[0] - b[3];
+  float t3 = b[1] - b[2];
+  t2 *= WC4_0;
+  t3 *= WC4_1;
+  a = t2;
+  c = t3;
+  t2 = a + c;
+  t3 = a - c;
+  t2 = fmla(t2, SQRT2F, t3);
+  b[0] = t0;
+  b[2] = t1;
+  b[1] = t2;
+  b[3] = t3;
+}
+
+static inline void dct1d_8(float* b) {
+  float t[8];
+  for (int i = 0; i < 4; i++) t[i] = b[i] + b[7 - i];
+  dct1d_4(t);
+  for (int i = 0; i < 4; i++) t[4 + i] = (b[i] - b[7 - i]) * WC8[i];
+  dct1d_4(t + 4);
+  t[4] = fmla(t[4], SQRT2F, t[5]);
+  t[5] += t[6];
+  t[6] += t[7];
+  for (int i = 0; i < 4; i++) {
+    b[2 * i] = t[i];
+    b[2 * i + 1] = t[4 + i];
+  }
+}
+
+/* dct8x8_scalar_input: rows, then columns stored transposed, scaled 1/64. */
+static void dct8x8(const float* in, size_t stride, float* out) {
+  float tmp[64];
+  for (int y = 0; y < 8; y++) {
+    float row[8];
+    for (int x = 0; x < 8; x++) row[x] = in[y * stride + x];
+    dct1d_8(row);
+    for (int x = 0; x < 8; x++) tmp[y * 8 + x] = row[x];
+  }
+  for (int x = 0; x < 8; x++) {
+    float col[8];
+    for (int y = 0; y < 8; y++) col[y] = tmp[y * 8 + x];
+    dct1d_8(col);
+    for (int y = 0; y < 8; y++) out[x * 8 + y] = col[y] * (1.0f / 64.0f);
+  }
+}
+
+void orc_dct8x8(const float* in, float* out) { dct8x8(in, 8, out); }
+
+/* ------------------------------------------------------------------ */
+/* Chroma-from-luma tiles (src/color_correlation.rs:333-512)            */
+/* ------------------------------------------------------------------ */
+
+#define K_INV_COLOR_FACTOR (1.0f / 84.0f)
+
+/* src/color_correlation.rs:384-394 */
+static float cfl_deadzone(float d) {
+  if (d <= 1.0f) return 1.5f;
+  if (d >= 2.0f) return 0.0f;
+  const float s = 1.5f / (2.0f - 1.0f);
+  return s * (2.0f - d);
+}
+
+/* src/color_correlation.rs:397-409 */
+static int32_t solve_multiplier(float ca, float cb, size_t num, float dmul, float dz,
+                                float units) {
+  if (num == 0) return 0;
+  float x = -cb / fmla((float)num * dmul, 0.5f, ca);
+  if (fabsf(x) < dz) x = 0.0f;
+  float r = clampf(roundf(x * units), -128.0f, 127.0f);
+  return sat_i32(r);
+}
+
+/* compute_cmap_tile (src/color_correlation.rs:441-508) */
+static void cmap_tile(const float* xyb, size_t w, size_t h, size_t bx0, size_t by0, size_t bxc,
+                      size_t byc, float distance, const float* inv_x, const float* inv_b,
+                      int8_t* ytox, int8_t* ytob) {
+  size_t n = w * h;
+  float ca_x = 0.0f, cb_x = 0.0f, ca_b = 0.0f, cb_b = 0.0f;
+  size_t num = 0;
+  float by_[64], bx_[64], bb_[64];
+  for (size_t by = 0; by < byc; by++)
+    for (size_t bx = 0; bx < bxc; bx++) {
+      size_t px = (bx0 + bx) * 8, py = (by0 + by) * 8;
+      if (px + 8 > w || py + 8 > h) continue;
+      size_t off = py * w + px;
+      dct8x8(xyb + n + off, w, by_);
+      dct8x8(xyb + off, w, bx_);
+      dct8x8(xyb + 2 * n + off, w, bb_);
+      by_[0] = 0.0f;
+      bx_[0] = 0.0f;
+      bb_[0] = 0.0f;
+      float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+      for (int i = 0; i < 64; i++) {
+        float m_x = by_[i] * inv_x[i];
+        float s_x = bx_[i] * inv_x[i];
+        float a_x = K_INV_COLOR_FACTOR * m_x;
+        float b_x = -s_x;
+        s0 = fmla(a_x, a_x, s0);
+        s1 = fmla(a_x, b_x, s1);
+        float m_b = by_[i] * inv_b[i];
+        float s_b = bb_[i] * inv_b[i];
+        float a_b = K_INV_COLOR_FACTOR * m_b;
+        float b_b = fmla(1.0f, m_b, -s_b);
+        s2 = fmla(a_b, a_b, s2);
+        s3 = fmla(a_b, b_b, s3);
+      }
+      ca_x += s0;
+      cb_x += s1;
+      ca_b += s2;
+      cb_b += s3;
+      num += 64;
+    }
+  float dz = cfl_deadzone(distance);
+  *ytox = (int8_t)solve_multiplier(ca_x, cb_x, num, 1e-3f, dz, 84.0f / 84.0f);
+  *ytob = (int8_t)solve_multiplier(ca_b, cb_b, num, 1e-3f, dz, 84.0f / 84.0f);
+}
+
+/* ------------------------------------------------------------------ */
+/* Quantisation (src/group.rs)                                          */
+/* ------------------------------------------------------------------ */
+
+/* src/group.rs:406-455 for a single 8x8 block */
+static void ac_thresholds(int c, float d, float qm_mul, float thr[4]) {
+  float normal[4] = {0.58f, 0.635f, 0.66f, 0.7f};
+  if (c == 0) {
+    float up = clampf((d - 0.5f) / (0.75f - 0.5f), 0.0f, 1.0f);
+    float down = clampf((2.0f - d) / (2.0f - 1.5f), 0.0f, 1.0f);
+    float wv = rmin(up, down);
+    normal[0] += wv * (0.5f - normal[0]);
+    for (int i = 1; i < 4; i++) normal[i] += (1.0f - wv) * 0.08f;
+  }
+  if (c == 2) {
+    float b_hf = qm_mul > 1.0f ? 0.65f : 0.75f;
+    for (int i = 1; i < 4; i++) normal[i] = b_hf;
+  }
+  float hq[4];
+  if (c == 1) { hq[0] = 0.50f; hq[1] = 0.51f; hq[2] = 0.52f; hq[3] = 0.54f; }
+  else memcpy(hq, normal, sizeof(hq));
+  float t = clampf((d - 0.1f) / 0.9f, 0.0f, 1.0f);
+  for (int i = 0; i < 4; i++) thr[i] = hq[i] + t * (normal[i] - hq[i]);
+}
+
+/* quantize_block_ac_scalar (src/group.rs:560-612), 8x8 case */
+static void quantize_ac(const float* in, int c, const float* qm, int32_t quant, float scale,
+                        float qm_mul, float d, int32_t* out) {
+  float thr[4];
+  ac_thresholds(c, d, qm_mul, thr);
+  float q_scaled = scale * (float)quant * qm_mul;
+  for (int y = 0; y < 8; y++) {
+    int yfix = y >= 4 ? 2 : 0;
+    for (int x = 0; x < 8; x++) {
+      float threshold = x >= 4 ? thr[yfix + 1] : thr[yfix];
+      float q = qm[y * 8 + x] * q_scaled;
+      float val = q * in[y * 8 + x];
+      out[y * 8 + x] = fabsf(val) >= threshold ? sat_i32(roundf(val)) : 0;
+    }
+  }
+}
+
+static const float DEFAULT_BIAS_ONE[3] = {1.0f - 0.05465007330715401f,
+                                          1.0f - 0.07005449891748593f,
+                                          1.0f - 0.049935103337343655f};
+#define BIAS_NUMERATOR 0.145f
+
+/* DequantBias::level (src/group.rs:767-790) */
+static inline float bias_level(int c, int32_t q) {
+  uint32_t a = q < 0 ? (uint32_t)(-(int64_t)q) : (uint32_t)q;
+  if (a <= 1) return q == 0 ? 0.0f : (q > 0 ? DEFAULT_BIAS_ONE[c] : -DEFAULT_BIAS_ONE[c]);
+  float qf = (float)q;
+  return qf - BIAS_NUMERATOR / qf;
+}
+
+/* ------------------------------------------------------------------ */
+/* Contexts, scans and tokens                                          */
+/* ------------------------------------------------------------------ */
+
+/* libjxl CoeffOrderAndLut natural order as used by
+ * src/coeff_order.rs:203-244 (cx = cy = 1). */
+static void natural_scan_8x8(uint8_t* scan) {
+  int cur = 1;
+  for (int i = 0; i < 8; i++)
+    for (int j = 0; j <= i; j++) {
+      int x = j, y = i - j;
+      if (i & 1) { int t = x; x = y; y = t; }
+      int val = (x < 1 && y < 1) ? 0 : cur++;
+      scan[val] = (uint8_t)(y * 8 + x);
+    }
+  for (int ip = 7; ip >= 1; ip--) {
+    int i = ip - 1;
+    for (int j = 0; j <= i; j++) {
+      int x = 7 - (i - j), y = 7 - j;
+      if (i & 1) { int t = x; x = y; y = t; }
+      scan[cur++] = (uint8_t)(y * 8 + x);
+    }
+  }
+}
+
+void orc_natural_scan_8x8(uint8_t* scan) { natural_scan_8x8(scan); }
+
+/* K_COEFF_FREQ_CONTEXT (src/ac_context.rs:40-44), written as its bands. */
+static int freq_context(int k) {
+  if (k < 16) return k - 1;
+  if (k < 32) return 15 + (k - 16) / 2;
+  return 23 + (k - 32) / 4;
+}
+
+/* K_COEFF_NUM_NONZERO_CONTEXT (src/ac_context.rs:47-53), as its bands. */
+static int nonzero_context(int n) {
+  if (n <= 1) return 0;
+  if (n == 2) return 31;
+  if (n <= 4) return 62;
+  if (n <= 8) return 93;
+  if (n <= 12) return 123;
+  if (n <= 20) return 152;
+  if (n <= 32) return 180;
+  return 206;
+}
+
+int32_t orc_freq_context(int32_t k) { return freq_context(k); }
+int32_t orc_nonzero_context(int32_t n) { return nonzero_context(n); }
+
+/* src/ac_context.rs:96-105 */
+static uint32_t non_zero_bucket(uint32_t n) {
+  if (n < 8) return n;
+  if (n >= 64) return 36;
+  return 4 + n / 2;
+}
+
+/* block_context for the DCT8 order: Y -> 0, X -> 7, B -> 7
+ * (K_COMPACT_BLOCK_CONTEXT_MAP / K_STRATEGY_ORDER / CHANNEL_ROW,
+ * src/ac_context.rs:62-92). */
+static uint32_t fine_block_context_dct8(int c, int qf_hi) {
+  uint32_t bc = c == 1 ? 0u : 7u;
+  return bc * 2u + (uint32_t)qf_hi;
+}
+
+/* src/group.rs:89-106 */
+static uint8_t predict_top_left(const uint8_t* top, const uint8_t* row, size_t x) {
+  if (x == 0) return top ? top[x] : 32;
+  if (!top) return row[x - 1];
+  return (uint8_t)(((uint32_t)top[x] + (uint32_t)row[x - 1] + 1u) / 2u);
+}
+
+/* src/entropy/token.rs:159-162 */
+static inline uint32_t pack_signed(int32_t v) {
+  int64_t x = v;
+  return (uint32_t)((x << 1) ^ (x >> 63));
+}
+
+/* src/entropy/token.rs:115-127 */
+static inline uint32_t hybrid_token(uint32_t value) {
+  if (value < 16) return value;
+  uint32_t n = 31u - (uint32_t)__builtin_clz(value);
+  uint32_t m = value - (1u << n);
+  return (n << 2) + (m >> (n - 2));
+}
+
+uint32_t orc_hybrid_token(uint32_t v) { return hybrid_token(v); }
+
+/* src/frame/ac_groups.rs:92-113 */
+static uint32_t qf_threshold_of(const uint8_t* qf, size_t n) {
+  uint64_t hist[257];
+  memset(hist, 0, sizeof(hist));
+  for (size_t i = 0; i < n; i++) hist[qf[i]]++;
+  uint64_t total = n, acc = 0;
+  for (uint32_t v = 0; v < 257; v++) {
+    acc += hist[v];
+    if (acc * 2 >= total) return v;
+  }
+  return 1;
+}
+
+/* ------------------------------------------------------------------ */
+/* Whole front end                                                      */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+  /* inputs */
+  const void* pixels;
+  int32_t bytes_per_sample; /* 1 = sRGB 8-bit, 2 = 16-bit linear */
+  int32_t channels;         /* 3 or 4 (alpha ignored) */
+  uint64_t width, height;
+  float distance;
+  int32_t num_threads;
+  /* outputs (caller-allocated; NULL skips) */
+  float* xyb;            /* 3 * w * h */
+  uint8_t* quant_field;  /* xb * yb */
+  int8_t* ytox;          /* tx * ty */
+  int8_t* ytob;          /* tx * ty */
+  int16_t* quant_dc;     /* 3 * xb * yb, planes X, Y, B */
+  int32_t* coeffs;       /* xb * yb * 192, [block][X,Y,B][64] */
+  uint8_t* nzeros;       /* 3 * xb * yb */
+  uint32_t* tokens;      /* 2 * token_capacity: (context, value) pairs */
+  uint64_t token_capacity;
+  uint64_t* group_offsets; /* num_groups + 1 */
+  uint32_t* histograms;    /* NUM_FINE_AC_CONTEXTS * 128 */
+  /* scalar outputs */
+  orc_params params;
+  uint32_t qf_threshold;
+  uint64_t constant_blocks;
+  int32_t screen_content;
+  int32_t epf_sharpness;
+  uint64_t num_tokens;
+  double stage_seconds[5]; /* xyb+stats, AQ, CfL, AC groups, merge */
+} orc_frame;
+
+static double now_seconds(void) {
+#ifdef _OPENMP
+  return omp_get_wtime();
+#else
+  return 0.0;
+#endif
+}
+
+uint64_t orc_sizeof_frame(void) { return sizeof(orc_frame); }
+int32_t orc_num_fine_contexts(void) { return NUM_FINE_AC_CONTEXTS; }
+
+/* One AC group (process_ac_group + write_ac_group for an all-DCT8 layout,
+ * src/frame/ac_groups.rs:116-250, src/group.rs:1259-2426). */
+typedef struct {
+  uint32_t* tok; /* pairs */
+  uint64_t count;
+} group_tokens;
+
+static void encode_ac_group(const orc_frame* f, const float* xyb, const float* mat,
+                            const float* inv, const uint8_t* qf, const int8_t* ytox,
+                            const int8_t* ytob, int16_t* quant_dc, int32_t* coeffs_out,
+                            uint8_t* nz_out, size_t gx, size_t gy, uint32_t qf_threshold,
+                            const uint8_t* scan, group_tokens* gt, uint32_t* hist) {
+  const orc_params* p = &f->params;
+  size_t w = f->width, h = f->height, n = w * h;
+  size_t xb = (w + 7) / 8, yb = (h + 7) / 8;
+  size_t tx_count = (xb + 7) / 8;
+  size_t bx0 = gx * GROUP_BLOCKS, by0 = gy * GROUP_BLOCKS;
+  size_t gwb = minz(GROUP_BLOCKS, xb - bx0), ghb = minz(GROUP_BLOCKS, yb - by0);
+  float inv_factor[3];
+  static const float inv_dc_quant[3] = {4096.0f, 512.0f, 256.0f};
+  static const float dc_quant[3] = {1.0f / 4096.0f, 1.0f / 512.0f, 1.0f / 256.0f};
+  for (int c = 0; c < 3; c++) inv_factor[c] = inv_dc_quant[c] / p->dc_step[c] * p->scale_dc;
+  float cfl_b = inv_dc_quant[2] / p->dc_step[2] * (dc_quant[1] * p->dc_step[1]) *
+                (1.0f + 0.0f / 84.0f);
+  float cfl_x = inv_dc_quant[0] / p->dc_step[0] * (dc_quant[1] * p->dc_step[1]) * 0.0f;
+  uint8_t nzmap[3][GROUP_BLOCKS * GROUP_BLOCKS];
+  memset(nzmap, 0, sizeof(nzmap));
+  uint64_t cap = (uint64_t)gwb * ghb * 3 * 64;
+  gt->tok = (uint32_t*)malloc(cap * 2 * sizeof(uint32_t));
+  gt->count = 0;
+  float src[3][64], coef[3][64];
+  int32_t q[3][64];
+  for (size_t by = 0; by < ghb; by++)
+    for (size_t bx = 0; bx < gwb; bx++) {
+      size_t ibx = bx0 + bx, iby = by0 + by, bi = iby * xb + ibx;
+      int32_t quant = qf[bi];
+      /* footprint with edge replication (src/ac_strategy.rs:451-478) */
+      for (int c = 0; c < 3; c++)
+        for (int yy = 0; yy < 8; yy++)
+          for (int xx = 0; xx < 8; xx++) {
+            size_t sx = minz(ibx * 8 + xx, w - 1), sy = minz(iby * 8 + yy, h - 1);
+            src[c][yy * 8 + xx] = xyb[(size_t)c * n + sy * w + sx];
+          }
+      for (int c = 0; c < 3; c++) dct8x8(src[c], 8, coef[c]);
+      /* Y DC + AC round trip */
+      int16_t ydc = sat_i16(roundf(coef[1][0] * inv_factor[1]));
+      quantize_ac(coef[1], 1, inv + 64, quant, p->scale, 1.0f, p->distance, q[1]);
+      float inv_qac = 1.0f / (p->scale * (float)quant);
+      for (int k = 0; k < 64; k++) coef[1][k] = bias_level(1, q[1][k]) * mat[64 + k] * inv_qac;
+      /* CfL */
+      size_t t = (iby / 8) * tx_count + ibx / 8;
+      float xf = fmla((float)ytox[t], 1.0f / 84.0f, 0.0f);
+      float bf = fmla((float)ytob[t], 1.0f / 84.0f, 1.0f);
+      coef[1][0] = 0.0f;
+      for (int k = 0; k < 64; k++) {
+        coef[0][k] = fmla(-xf, coef[1][k], coef[0][k]);
+        coef[2][k] = fmla(-bf, coef[1][k], coef[2][k]);
+      }
+      int16_t xdc;
+      if (cfl_x != 0.0f) xdc = sat_i16(roundf(fmla(coef[0][0], inv_factor[0], -(float)ydc * cfl_x)));
+      else xdc = sat_i16(roundf(coef[0][0] * inv_factor[0]));
+      quantize_ac(coef[0], 0, inv, quant, p->scale, p->x_qm_mul, p->distance, q[0]);
+      int16_t bdc = sat_i16(roundf(fmla(coef[2][0], inv_factor[2], -(float)ydc * cfl_b)));
+      quantize_ac(coef[2], 2, inv + 128, quant, p->scale, p->b_qm_mul, p->distance, q[2]);
+      size_t nb = xb * yb;
+      quant_dc[0 * nb + bi] = xdc;
+      quant_dc[1 * nb + bi] = ydc;
+      quant_dc[2 * nb + bi] = bdc;
+      if (coeffs_out)
+        for (int c = 0; c < 3; c++) memcpy(coeffs_out + bi * 192 + c * 64, q[c], 64 * 4);
+      /* tokens in channel order Y, X, B */
+      static const int order[3] = {1, 0, 2};
+      for (int oi = 0; oi < 3; oi++) {
+        int c = order[oi];
+        const int32_t* blk = q[c];
+        int32_t nzeros = 0;
+        for (int k = 1; k < 64; k++) nzeros += blk[k] != 0;
+        nzmap[c][by * GROUP_BLOCKS + bx] = (uint8_t)nzeros;
+        if (nz_out) nz_out[(size_t)c * nb + bi] = (uint8_t)nzeros;
+        const uint8_t* top = by ? &nzmap[c][(by - 1) * GROUP_BLOCKS] : NULL;
+        uint8_t predicted = predict_top_left(top, &nzmap[c][by * GROUP_BLOCKS], bx);
+        uint32_t bctx = fine_block_context_dct8(c, (uint32_t)quant > qf_threshold);
+        uint32_t nz_ctx = non_zero_bucket(predicted) * NUM_FINE_BLOCK_CTXS + bctx;
+        uint32_t histo = NUM_FINE_BLOCK_CTXS * NON_ZERO_BUCKETS + ZERO_DENSITY_CONTEXTS * bctx;
+        uint32_t* o = gt->tok + gt->count * 2;
+        o[0] = nz_ctx;
+        o[1] = (uint32_t)nzeros;
+        gt->count++;
+        hist[nz_ctx * ALPHABET + hybrid_token((uint32_t)nzeros)]++;
+        int prev = nzeros > 64 / 16 ? 0 : 1;
+        int32_t remaining = nzeros;
+        for (int k = 1; k < 64 && remaining != 0; k++) {
+          int32_t v = blk[scan[k]];
+          uint32_t ctx = histo + (uint32_t)((nonzero_context(remaining) + freq_context(k)) * 2 + prev);
+          uint32_t val = pack_signed(v);
+          o = gt->tok + gt->count * 2;
+          o[0] = ctx;
+          o[1] = val;
+          gt->count++;
+          hist[ctx * ALPHABET + hybrid_token(val)]++;
+          prev = v != 0;
+          if (v != 0) remaining--;
+        }
+      }
+    }
+}
+
+/* encode_frame_core_inner through pass one (src/frame/vardct_encoder.rs:798-1100)
+ * for Speed::UltraFast: DC-group setup (AQ + CfL, all-DCT8 layout), the qf
+ * threshold, then every AC group. */
+int orc_frontend(orc_frame* f) {
+  size_t w = f->width, h = f->height;
+  if (w == 0 || h == 0) return ORC_ERR_EMPTY;
+  if (!(f->bytes_per_sample == 1 || f->bytes_per_sample == 2)) return ORC_ERR_INPUT;
+  if (!(f->channels == 3 || f->channels == 4)) return ORC_ERR_INPUT;
+  int st = orc_params_for(f->distance, &f->params);
+  if (st) return st;
+  float mat[192], inv[192];
+  st = orc_dct8_tables(f->params.distance, mat, inv);
+  if (st) return st;
+  init_exp2_table();
+#ifdef _OPENMP
+  int threads = f->num_threads > 0 ? f->num_threads : omp_get_max_threads();
+  omp_set_num_threads(threads);
+#endif
+  size_t n = w * h;
+  size_t xb = (w + 7) / 8, yb = (h + 7) / 8, nb = xb * yb;
+  size_t txn = (xb + 7) / 8, tyn = (yb + 7) / 8;
+  size_t xg = (w + GROUP - 1) / GROUP, yg = (h + GROUP - 1) / GROUP;
+  size_t xdc = (w + DC_GROUP - 1) / DC_GROUP, ydc = (h + DC_GROUP - 1) / DC_GROUP;
+  float* xyb = f->xyb ? f->xyb : (float*)malloc(3 * n * sizeof(float));
+  uint8_t* qf = f->quant_field ? f->quant_field : (uint8_t*)malloc(nb);
+  int8_t* ytox = f->ytox ? f->ytox : (int8_t*)malloc(txn * tyn);
+  int8_t* ytob = f->ytob ? f->ytob : (int8_t*)malloc(txn * tyn);
+  int16_t* qdc = f->quant_dc ? f->quant_dc : (int16_t*)malloc(3 * nb * sizeof(int16_t));
+  if (!xyb || !qf || !ytox || !ytob || !qdc) return ORC_ERR_ALLOC;
+  double t0 = now_seconds();
+  orc_to_xyb(f->pixels, f->bytes_per_sample, f->channels, w, h, xyb);
+  f->constant_blocks = orc_constant_blocks(xyb, w, h);
+  f->screen_content = orc_is_screen_content(f->constant_blocks, w, h);
+  f->epf_sharpness = orc_epf_sharpness_id(f->params.distance, f->screen_content);
+  float inv_scale = 1.0f / f->params.scale;
+  double t1 = now_seconds();
+  /* DC groups: AQ field, then CfL tiles (setup_dc_group, src/frame/dc_groups.rs:127-180) */
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic) num_threads(threads)
+#endif
+  for (long g = 0; g < (long)(xdc * ydc); g++) {
+    size_t gx = (size_t)g % xdc, gy = (size_t)g / xdc;
+    size_t x0 = gx * DC_GROUP, y0 = gy * DC_GROUP;
+    size_t gxs = minz(DC_GROUP, w - x0), gys = minz(DC_GROUP, h - y0);
+    size_t gxb = (gxs + 7) / 8, gyb = (gys + 7) / 8;
+    fill_quant_field(xyb, w, h, x0, y0, gxb, gyb, f->params.distance, inv_scale, qf, xb);
+  }
+  double t2 = now_seconds();
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic) num_threads(threads)
+#endif
+  for (long t = 0; t < (long)(txn * tyn); t++) {
+    size_t tx = (size_t)t % txn, ty = (size_t)t / txn;
+    /* tiles never cross DC groups (2048 = 32 tiles); clip to the DC group */
+    size_t bx0 = tx * 8, by0 = ty * 8;
+    size_t dcbx_end = minz(((bx0 / 256) + 1) * 256, xb);
+    size_t dcby_end = minz(((by0 / 256) + 1) * 256, yb);
+    size_t bxc = minz(8, dcbx_end - bx0), byc = minz(8, dcby_end - by0);
+    cmap_tile(xyb, w, h, bx0, by0, bxc, byc, f->params.distance, inv, inv + 128, &ytox[t],
+              &ytob[t]);
+  }
+  double t3 = now_seconds();
+  f->qf_threshold = qf_threshold_of(qf, nb);
+  uint8_t scan[64];
+  natural_scan_8x8(scan);
+  size_t ng = xg * yg;
+  group_tokens* gts = (group_tokens*)calloc(ng, sizeof(group_tokens));
+  size_t hist_len = (size_t)NUM_FINE_AC_CONTEXTS * ALPHABET;
+  if (f->histograms) memset(f->histograms, 0, hist_len * sizeof(uint32_t));
+  uint32_t* hist = f->histograms ? f->histograms : (uint32_t*)calloc(hist_len, 4);
+#ifdef _OPENMP
+#pragma omp parallel num_threads(threads)
+#endif
+  {
+    uint32_t* local = (uint32_t*)calloc(hist_len, 4);
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic)
+#endif
+    for (long g = 0; g < (long)ng; g++) {
+      size_t gx = (size_t)g % xg, gy = (size_t)g / xg;
+      encode_ac_group(f, xyb, mat, inv, qf, ytox, ytob, qdc, f->coeffs, f->nzeros, gx, gy,
+                      f->qf_threshold, scan, &gts[g], local);
+    }
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+    for (size_t i = 0; i < hist_len; i++) hist[i] += local[i];
+    free(local);
+  }
+  double t4 = now_seconds();
+  uint64_t total = 0;
+  uint64_t* starts = (uint64_t*)malloc((ng + 1) * sizeof(uint64_t));
+  for (size_t g = 0; g < ng; g++) {
+    starts[g] = total;
+    total += gts[g].count;
+  }
+  starts[ng] = total;
+  if (f->group_offsets) memcpy(f->group_offsets, starts, (ng + 1) * sizeof(uint64_t));
+  int fits = f->tokens && total <= f->token_capacity;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic) num_threads(threads)
+#endif
+  for (long g = 0; g < (long)ng; g++) {
+    if (fits) memcpy(f->tokens + starts[g] * 2, gts[g].tok, gts[g].count * 2 * sizeof(uint32_t));
+    free(gts[g].tok);
+  }
+  free(starts);
+  f->num_tokens = total;
+  double t5 = now_seconds();
+  f->stage_seconds[0] = t1 - t0;
+  f->stage_seconds[1] = t2 - t1;
+  f->stage_seconds[2] = t3 - t2;
+  f->stage_seconds[3] = t4 - t3;
+  f->stage_seconds[4] = t5 - t4;
+  free(gts);
+  if (!f->histograms) free(hist);
+  if (!f->xyb) free(xyb);
+  if (!f->quant_field) free(qf);
+  if (!f->ytox) free(ytox);
+  if (!f->ytob) free(ytob);
+  if (!f->quant_dc) free(qdc);
+  if (f->tokens && total > f->token_capacity) return ORC_ERR_ALLOC;
+  return ORC_OK;
+}
+
+/* fill_quant_field over every DC group of an XYB image (the oracle side of
+ * the FillQuantFieldFn operator, src/adaptive_quant.rs:474). */
+void orc_fill_quant_field_image(const float* xyb, size_t w, size_t h, float distance,
+                                float inv_scale, uint8_t* qf) {
+  init_exp2_table();
+  size_t xb = (w + 7) / 8;
+  size_t xdc = (w + DC_GROUP - 1) / DC_GROUP, ydc = (h + DC_GROUP - 1) / DC_GROUP;
+  for (size_t gy = 0; gy < ydc; gy++)
+    for (size_t gx = 0; gx < xdc; gx++) {
+      size_t x0 = gx * DC_GROUP, y0 = gy * DC_GROUP;
+      size_t gxb = (minz(DC_GROUP, w - x0) + 7) / 8, gyb = (minz(DC_GROUP, h - y0) + 7) / 8;
+      fill_quant_field(xyb, w, h, x0, y0, gxb, gyb, distance, inv_scale, qf, xb);
+    }
+}

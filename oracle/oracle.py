@@ -1,0 +1,232 @@
+"""ctypes front of the CPU oracle (test infrastructure only).
+
+The oracle restates jixel 0.5.14's scalar UltraFast VarDCT front end in C
+(``oracle/jxg_oracle.c``).  Tests, ``__graft_entry__.smoke()`` and the CPU
+legs of ``bench.py`` call it as the checker; the product never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libjxg_oracle.so")
+
+NUM_FINE_AC_CONTEXTS = 30 * (37 + 458)
+ALPHABET = 128
+
+
+class OrcParams(ctypes.Structure):
+    _fields_ = [
+        ("distance", ctypes.c_float),
+        ("global_scale", ctypes.c_int32),
+        ("quant_dc", ctypes.c_int32),
+        ("scale", ctypes.c_float),
+        ("scale_dc", ctypes.c_float),
+        ("x_qm_scale", ctypes.c_uint32),
+        ("b_qm_scale", ctypes.c_uint32),
+        ("epf_iters", ctypes.c_uint32),
+        ("dc_step", ctypes.c_float * 3),
+        ("x_qm_mul", ctypes.c_float),
+        ("b_qm_mul", ctypes.c_float),
+    ]
+
+
+class OrcFrame(ctypes.Structure):
+    _fields_ = [
+        ("pixels", ctypes.c_void_p),
+        ("bytes_per_sample", ctypes.c_int32),
+        ("channels", ctypes.c_int32),
+        ("width", ctypes.c_uint64),
+        ("height", ctypes.c_uint64),
+        ("distance", ctypes.c_float),
+        ("num_threads", ctypes.c_int32),
+        ("xyb", ctypes.c_void_p),
+        ("quant_field", ctypes.c_void_p),
+        ("ytox", ctypes.c_void_p),
+        ("ytob", ctypes.c_void_p),
+        ("quant_dc", ctypes.c_void_p),
+        ("coeffs", ctypes.c_void_p),
+        ("nzeros", ctypes.c_void_p),
+        ("tokens", ctypes.c_void_p),
+        ("token_capacity", ctypes.c_uint64),
+        ("group_offsets", ctypes.c_void_p),
+        ("histograms", ctypes.c_void_p),
+        ("params", OrcParams),
+        ("qf_threshold", ctypes.c_uint32),
+        ("constant_blocks", ctypes.c_uint64),
+        ("screen_content", ctypes.c_int32),
+        ("epf_sharpness", ctypes.c_int32),
+        ("num_tokens", ctypes.c_uint64),
+        ("stage_seconds", ctypes.c_double * 5),
+    ]
+
+
+def build() -> None:
+    """Compile the oracle with its Makefile (gcc only)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        _lib.orc_distance_from_quality.restype = ctypes.c_float
+        _lib.orc_distance_from_quality.argtypes = [ctypes.c_float]
+        _lib.orc_params_for.restype = ctypes.c_int
+        _lib.orc_params_for.argtypes = [ctypes.c_float, ctypes.POINTER(OrcParams)]
+        _lib.orc_dct8_tables.restype = ctypes.c_int
+        _lib.orc_dct8_tables.argtypes = [ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p]
+        _lib.orc_frontend.restype = ctypes.c_int
+        _lib.orc_frontend.argtypes = [ctypes.POINTER(OrcFrame)]
+        _lib.orc_sizeof_frame.restype = ctypes.c_uint64
+        _lib.orc_epf_sharpness_id.restype = ctypes.c_int32
+        _lib.orc_epf_sharpness_id.argtypes = [ctypes.c_float, ctypes.c_int]
+        _lib.orc_fast_exp2.restype = ctypes.c_float
+        _lib.orc_fast_exp2.argtypes = [ctypes.c_float]
+        _lib.orc_dirty_log2f.restype = ctypes.c_float
+        _lib.orc_dirty_log2f.argtypes = [ctypes.c_float]
+        _lib.orc_hybrid_token.restype = ctypes.c_uint32
+        _lib.orc_hybrid_token.argtypes = [ctypes.c_uint32]
+        _lib.orc_freq_context.restype = ctypes.c_int32
+        _lib.orc_freq_context.argtypes = [ctypes.c_int32]
+        _lib.orc_nonzero_context.restype = ctypes.c_int32
+        _lib.orc_nonzero_context.argtypes = [ctypes.c_int32]
+        _lib.orc_constant_blocks.restype = ctypes.c_uint64
+        _lib.orc_constant_blocks.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t]
+        assert _lib.orc_sizeof_frame() == ctypes.sizeof(OrcFrame), "OrcFrame layout mismatch"
+    return _lib
+
+
+def distance_from_quality(q: float) -> float:
+    return float(lib().orc_distance_from_quality(q))
+
+
+def params(distance: float) -> dict:
+    p = OrcParams()
+    st = lib().orc_params_for(distance, ctypes.byref(p))
+    if st:
+        raise ValueError(f"oracle params status {st}")
+    return {
+        "distance": p.distance,
+        "global_scale": p.global_scale,
+        "quant_dc": p.quant_dc,
+        "scale": p.scale,
+        "scale_dc": p.scale_dc,
+        "x_qm_scale": p.x_qm_scale,
+        "b_qm_scale": p.b_qm_scale,
+        "epf_iters": p.epf_iters,
+        "dc_step": list(p.dc_step),
+        "x_qm_mul": p.x_qm_mul,
+        "b_qm_mul": p.b_qm_mul,
+    }
+
+
+def dct8_tables(distance: float):
+    m = np.zeros(192, np.float32)
+    inv = np.zeros(192, np.float32)
+    st = lib().orc_dct8_tables(distance, m.ctypes.data, inv.ctypes.data)
+    if st:
+        raise ValueError(f"oracle tables status {st}")
+    return m.reshape(3, 64), inv.reshape(3, 64)
+
+
+def natural_scan_8x8() -> np.ndarray:
+    s = np.zeros(64, np.uint8)
+    lib().orc_natural_scan_8x8(s.ctypes.data_as(ctypes.c_void_p))
+    return s
+
+
+def dct8x8(block: np.ndarray) -> np.ndarray:
+    b = np.ascontiguousarray(block, np.float32).reshape(64)
+    out = np.zeros(64, np.float32)
+    lib().orc_dct8x8(b.ctypes.data_as(ctypes.c_void_p), out.ctypes.data_as(ctypes.c_void_p))
+    return out
+
+
+@dataclass
+class OracleFrame:
+    width: int
+    height: int
+    params: dict
+    xyb: np.ndarray
+    quant_field: np.ndarray
+    ytox: np.ndarray
+    ytob: np.ndarray
+    quant_dc: np.ndarray
+    coeffs: np.ndarray
+    nzeros: np.ndarray
+    tokens: np.ndarray          # (N, 2) uint32: context, value
+    group_offsets: np.ndarray
+    histograms: np.ndarray      # (contexts, 128) uint32
+    qf_threshold: int
+    constant_blocks: int
+    screen_content: bool
+    epf_sharpness: int
+    stage_seconds: list
+
+
+def frontend(pixels: np.ndarray, distance: float, num_threads: int = 0,
+             keep_coeffs: bool = True) -> OracleFrame:
+    """Run the oracle on an (h, w, c) uint8 (sRGB) or uint16 (linear) image."""
+    pixels = np.ascontiguousarray(pixels)
+    h, w, ch = pixels.shape
+    bps = 1 if pixels.dtype == np.uint8 else 2
+    xb, yb = (w + 7) // 8, (h + 7) // 8
+    tx, ty = (xb + 7) // 8, (yb + 7) // 8
+    ng = ((w + 255) // 256) * ((h + 255) // 256)
+    cap = xb * yb * 192
+    xyb = np.zeros((3, h, w), np.float32)
+    qf = np.zeros((yb, xb), np.uint8)
+    ytox = np.zeros((ty, tx), np.int8)
+    ytob = np.zeros((ty, tx), np.int8)
+    qdc = np.zeros((3, yb, xb), np.int16)
+    coeffs = np.zeros((yb, xb, 3, 64), np.int32) if keep_coeffs else None
+    nz = np.zeros((3, yb, xb), np.uint8)
+    tokens = np.zeros((cap, 2), np.uint32)
+    offs = np.zeros(ng + 1, np.uint64)
+    hist = np.zeros((NUM_FINE_AC_CONTEXTS, ALPHABET), np.uint32)
+    f = OrcFrame()
+    f.pixels = pixels.ctypes.data
+    f.bytes_per_sample = bps
+    f.channels = ch
+    f.width = w
+    f.height = h
+    f.distance = distance
+    f.num_threads = num_threads
+    f.xyb = xyb.ctypes.data
+    f.quant_field = qf.ctypes.data
+    f.ytox = ytox.ctypes.data
+    f.ytob = ytob.ctypes.data
+    f.quant_dc = qdc.ctypes.data
+    f.coeffs = coeffs.ctypes.data if coeffs is not None else None
+    f.nzeros = nz.ctypes.data
+    f.tokens = tokens.ctypes.data
+    f.token_capacity = cap
+    f.group_offsets = offs.ctypes.data
+    f.histograms = hist.ctypes.data
+    st = lib().orc_frontend(ctypes.byref(f))
+    if st:
+        raise ValueError(f"oracle frontend status {st}")
+    p = f.params
+    return OracleFrame(
+        width=w, height=h,
+        params={"distance": p.distance, "global_scale": p.global_scale, "quant_dc": p.quant_dc,
+                "scale": p.scale, "scale_dc": p.scale_dc, "x_qm_scale": p.x_qm_scale,
+                "b_qm_scale": p.b_qm_scale, "epf_iters": p.epf_iters,
+                "dc_step": list(p.dc_step)},
+        xyb=xyb, quant_field=qf, ytox=ytox, ytob=ytob, quant_dc=qdc, coeffs=coeffs,
+        nzeros=nz, tokens=tokens[: f.num_tokens], group_offsets=offs, histograms=hist,
+        qf_threshold=f.qf_threshold, constant_blocks=f.constant_blocks,
+        screen_content=bool(f.screen_content), epf_sharpness=f.epf_sharpness,
+        stage_seconds=list(f.stage_seconds),
+    )

@@ -1,0 +1,66 @@
+"""Extract known-answer vectors from the reference's own sources and tests.
+
+Run in the container that holds the reference checkout (it is not available
+on the GPU machines):
+
+    python tests/golden/gen_golden.py /root/reference
+
+The reference is Rust and cannot be built here, so its golden data are the
+constant tables and asserted values that its own unit tests pin:
+  - the natural 8x8 coefficient order (src/ac_context.rs K_COEFF_ORDER_8X8,
+    checked by `generic_natural_scan_reproduces_the_spec_tables`);
+  - the zero-density context tables (src/ac_context.rs:40-53);
+  - the high words of the fast_exp2 table (src/adaptive_quant.rs:732-737);
+  - quality->distance anchors (src/encode_image.rs:5758-5771);
+  - hybrid-uint boundaries and pack_signed values (src/entropy/token.rs tests);
+  - dirty_log2f on powers of two (src/adaptive_quant.rs:896-902).
+The output is tests/golden/reference_tables.json.
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import sys
+
+
+def _array(src: str, name: str) -> list[int]:
+    start = src.index(name)
+    body = src[src.index("[", src.index("=", start)) + 1:]
+    body = body[: body.index("];")]
+    body = re.sub(r"//[^\n]*", "", body)
+    return [int(v, 0) for v in re.findall(r"0x[0-9A-Fa-f]+|\d+", body)]
+
+
+def main(root: str) -> None:
+    ac = open(os.path.join(root, "src/ac_context.rs")).read()
+    aq = open(os.path.join(root, "src/adaptive_quant.rs")).read()
+    order8 = _array(ac, "K_COEFF_ORDER_8X8:")
+    freq = _array(ac, "K_COEFF_FREQ_CONTEXT:")
+    nonzero = _array(ac, "K_COEFF_NUM_NONZERO_CONTEXT:")
+    assert len(order8) == 64 and len(freq) == 64 and len(nonzero) == 64
+    exp2 = re.findall(r"\((0x[0-9A-F]+), 0x[0-9A-F]+\)", aq[aq.index("static EXP2FT"):])
+    assert len(exp2) == 64
+    out = {
+        "source": "jixel 0.5.14",
+        "coeff_order_8x8": order8,
+        # index 0 is the DC slot (0xBAD sentinel in the reference)
+        "coeff_freq_context": [None] + freq[1:],
+        "coeff_num_nonzero_context": [None] + nonzero[1:],
+        "exp2_table_hi_bits": [int(v, 16) for v in exp2],
+        "quality_anchors": [[100.0, 0.05], [99.0, 0.1], [90.0, 1.0], [30.0, 6.4],
+                            [0.0, 25.0], [-50.0, 25.0], [110.0, 0.05]],
+        "quality_anchor_tolerance": 1e-4,
+        "quality_25_range": [6.4, 7.0],
+        "hybrid_uint": [[16, 16], [17, 16], [20, 17], [31, 19]],
+        "pack_signed": [[0, 0], [-1, 1], [1, 2], [-2, 3], [2, 4]],
+        "dirty_log2f_pow2_exponents": [-20, 20],
+    }
+    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_tables.json")
+    with open(dst, "w") as fh:
+        json.dump(out, fh, indent=1)
+    print("wrote", dst)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,163 @@
+"""Parity of the CUDA front end with the CPU oracle (bit-exact).
+
+Every integer output must equal the oracle's: quant field, CfL maps, DC
+levels, AC levels, non-zero counts, tokens, group offsets and histograms;
+the XYB planes must match to the bit as well.
+"""
+import numpy as np
+import pytest
+
+import jixel_gb300 as J
+from jixel_gb300 import synthetic
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = J.FrontendContext(0)
+    yield c
+    c.close()
+
+
+def ultrafast(distance):
+    return J.EncodeConfig(distance=distance, speed=J.Speed.ULTRA_FAST)
+
+
+def compare(ctx, img, distance, check_xyb=True):
+    want = O.frontend(img, distance)
+    got = ctx.frontend(img, ultrafast(distance), xyb=check_xyb)
+    p = got.params
+    for k in ("global_scale", "quant_dc", "x_qm_scale", "b_qm_scale", "epf_iters"):
+        assert p[k] == want.params[k], k
+    assert p["scale"] == want.params["scale"] and p["scale_dc"] == want.params["scale_dc"]
+    assert p["dc_step"] == want.params["dc_step"]
+    if check_xyb:
+        assert np.array_equal(got.xyb.view(np.uint32), want.xyb.view(np.uint32)), "xyb"
+    assert p["constant_blocks"] == want.constant_blocks
+    assert p["screen_content"] == want.screen_content
+    assert p["epf_sharpness"] == want.epf_sharpness
+    assert np.array_equal(got.quant_field, want.quant_field), "quant field"
+    assert p["qf_threshold"] == want.qf_threshold
+    assert np.array_equal(got.ytox, want.ytox), "ytox"
+    assert np.array_equal(got.ytob, want.ytob), "ytob"
+    assert np.array_equal(got.quant_dc, want.quant_dc), "quant_dc"
+    assert np.array_equal(got.coefficients, want.coeffs), "coefficients"
+    assert np.array_equal(got.num_nzeros, want.nzeros), "nzeros"
+    assert np.array_equal(got.group_offsets, want.group_offsets), "group offsets"
+    assert got.tokens.shape == want.tokens.shape, "token count"
+    assert np.array_equal(got.tokens, want.tokens), "tokens"
+    assert np.array_equal(got.histograms, want.histograms), "histograms"
+    assert np.all(got.ac_strategy == 1)
+    return got, want
+
+
+def test_config1_q90(ctx):
+    compare(ctx, synthetic.config1_image(), 1.0)
+
+
+@pytest.mark.parametrize("q", [30, 50, 75, 85, 90, 94])
+def test_config1_qualities(ctx, q):
+    compare(ctx, synthetic.config1_image(), J.distance_from_quality(q))
+
+
+@pytest.mark.parametrize("w,h", [(1, 1), (7, 9), (27, 28), (33, 33), (64, 17), (65, 65),
+                                 (257, 65), (300, 7), (255, 257)])
+def test_ragged_sizes(ctx, w, h):
+    img = synthetic.generate(w, h, 11 + w + h, rectangles=3)
+    compare(ctx, img, 1.0)
+
+
+def test_multiple_dc_groups(ctx):
+    img = synthetic.generate(2100, 300, 21, rectangles=30)
+    compare(ctx, img, 1.5, check_xyb=False)
+
+
+def test_rgba_and_sixteen_bit(ctx):
+    compare(ctx, synthetic.generate(200, 120, 31, alpha=True), 1.0)
+    compare(ctx, synthetic.generate(200, 120, 32, sixteen_bit=True), 1.45)
+    compare(ctx, synthetic.generate(130, 70, 33, sixteen_bit=True, alpha=True), 2.0)
+
+
+def test_screen_content_flat_image(ctx):
+    img = np.zeros((128, 192, 3), np.uint8)
+    img[:, :96] = (200, 30, 40)
+    img[40:90, 100:180] = (10, 220, 90)
+    got, want = compare(ctx, img, 1.0)
+    assert got.params["screen_content"]
+
+
+def test_fill_quant_field_operator(ctx):
+    # the reference's own AQ fixture: src/adaptive_quant.rs:855-893
+    for (w, h) in [(27, 28), (1, 1), (7, 9), (32, 32), (33, 33), (64, 17), (65, 65)]:
+        y, x = np.mgrid[0:h, 0:w]
+        xyb = np.stack([np.sin((x * 7 + y * 13 + c * 29).astype(np.float32) * np.float32(0.017))
+                        .astype(np.float32) * np.float32(0.4) + np.float32(c * 0.05)
+                        for c in range(3)]).astype(np.float32)
+        got = ctx.fill_quant_field(xyb, 1.0, 1.0)
+        # the oracle runs the same AQ through its front end on an XYB input
+        want = oracle_aq(xyb, 1.0, 1.0)
+        assert np.array_equal(got, want), (w, h)
+
+
+def oracle_aq(xyb, distance, inv_scale):
+    import ctypes
+    _, h, w = xyb.shape
+    xb, yb = (w + 7) // 8, (h + 7) // 8
+    out = np.zeros((yb, xb), np.uint8)
+    lib = O.lib()
+    lib.orc_fill_quant_field_image.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
+                                               ctypes.c_float, ctypes.c_float, ctypes.c_void_p]
+    lib.orc_fill_quant_field_image(np.ascontiguousarray(xyb).ctypes.data, w, h, distance,
+                                   inv_scale, out.ctypes.data)
+    return out
+
+
+def test_dct8x8_operator(ctx):
+    rng = np.random.default_rng(3)
+    blocks = rng.uniform(-1, 1, (257, 64)).astype(np.float32)
+    got = ctx.dct8x8(blocks)
+    want = np.stack([O.dct8x8(b) for b in blocks])
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_large_frame_invariants(ctx):
+    img = synthetic.config2_image()
+    got = ctx.frontend(img, ultrafast(1.0), coefficients=True)
+    fi = J.frame_info(3840, 2160)
+    # every block-channel emits its non-zero count; histograms count every token
+    assert int(got.histograms.sum()) == got.tokens.shape[0]
+    assert got.group_offsets[-1] == got.tokens.shape[0]
+    assert np.all(np.diff(got.group_offsets.astype(np.int64)) >= 3)
+    nz = (got.coefficients[..., 1:] != 0).sum(-1).transpose(2, 0, 1)
+    assert np.array_equal(nz, got.num_nzeros)
+    # the non-zero-count tokens carry exactly the stored counts, channel order Y, X, B
+    assert got.quant_field.min() >= 1
+    assert got.tokens[:, 0].max() < 14850
+    # a full-frame oracle comparison on a 1/4 crop keeps the CPU time small
+    crop = np.ascontiguousarray(img[:1080, :1920])
+    compare(ctx, crop, 1.0, check_xyb=False)
+
+
+def test_invalid_inputs_raise(ctx):
+    img = np.zeros((8, 8, 3), np.uint8)
+    with pytest.raises(J.EncodeError) as e:
+        ctx.run(img, J.EncodeConfig(distance=1.0, speed=J.Speed.FAST))
+    assert e.value.variant == "Unsupported"
+    with pytest.raises(J.EncodeError) as e:
+        ctx.run(img, ultrafast(-1.0))
+    assert e.value.variant == "InvalidDistance"
+    with pytest.raises(J.EncodeError) as e:
+        ctx.run(np.zeros((0, 8, 3), np.uint8), ultrafast(1.0))
+    assert e.value.variant == "EmptyImage"
+    # the context stays usable
+    compare(ctx, synthetic.generate(40, 40, 5), 1.0)
+
+
+def test_repeat_runs_are_identical(ctx):
+    img = synthetic.generate(300, 200, 77)
+    a = ctx.frontend(img, ultrafast(1.0))
+    b = ctx.frontend(img, ultrafast(1.0))
+    assert np.array_equal(a.tokens, b.tokens)
+    assert np.array_equal(a.histograms, b.histograms)

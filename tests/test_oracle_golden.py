@@ -1,0 +1,144 @@
+"""Pin the CPU oracle against the reference's own known answers.
+
+The reference ships no golden images; what it pins are constant tables and
+asserted values in its unit tests (extracted by tests/golden/gen_golden.py).
+"""
+import json
+import math
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_tables.json")))
+
+
+def f32_bits(v):
+    return struct.unpack("<I", struct.pack("<f", v))[0]
+
+
+def test_natural_scan_matches_reference_table():
+    assert O.natural_scan_8x8().tolist() == GOLD["coeff_order_8x8"]
+
+
+def test_zero_density_context_tables():
+    lib = O.lib()
+    for k in range(1, 64):
+        assert lib.orc_freq_context(k) == GOLD["coeff_freq_context"][k]
+        assert lib.orc_nonzero_context(k) == GOLD["coeff_num_nonzero_context"][k]
+
+
+def test_exp2_table_matches_reference():
+    import ctypes
+    t = np.zeros(64, np.float32)
+    O.lib().orc_exp2_table(t.ctypes.data_as(ctypes.c_void_p))
+    assert [f32_bits(float(v)) for v in t] == GOLD["exp2_table_hi_bits"]
+
+
+def test_quality_anchor_points():
+    tol = GOLD["quality_anchor_tolerance"]
+    for q, d in GOLD["quality_anchors"]:
+        assert abs(O.distance_from_quality(q) - d) < tol, (q, d)
+    lo, hi = GOLD["quality_25_range"]
+    assert lo < O.distance_from_quality(25.0) < hi
+
+
+def test_hybrid_uint_and_pack_signed():
+    lib = O.lib()
+    for v, tok in GOLD["hybrid_uint"]:
+        assert lib.orc_hybrid_token(v) == tok
+    assert lib.orc_hybrid_token(0xFFFFFFFF) == 127
+
+
+def test_dirty_log2f_exact_on_powers_of_two():
+    lo, hi = GOLD["dirty_log2f_pow2_exponents"]
+    for e in range(lo, hi + 1):
+        assert O.lib().orc_dirty_log2f(2.0 ** e) == float(e)
+
+
+def test_dirty_log2f_accuracy():
+    # src/adaptive_quant.rs:903-916: max abs error < 2e-6 over [1e-6, 1e6]
+    x = 1.0e-6
+    worst = 0.0
+    while x <= 1.0e6:
+        xf = np.float32(x)
+        worst = max(worst, abs(O.lib().orc_dirty_log2f(float(xf)) - math.log2(float(xf))))
+        x *= 1.01
+    assert worst < 2.0e-6
+
+
+def test_dc_steps_are_f16_exact():
+    # src/frame/quantization.rs:246-275: signalled DC steps survive the wire
+    for d in [1.4, 2.0, 4.5, 6.0, 11.0, 25.0]:
+        p = O.params(d)
+        for c, s in enumerate(p["dc_step"]):
+            dq = [1 / 4096, 1 / 512, 1 / 256][c]
+            wire = np.float32(np.float32(dq) * np.float32(128.0) * np.float32(s))
+            assert np.float32(np.float16(wire)) == wire
+
+
+def test_params_known_values_q90():
+    p = O.params(O.distance_from_quality(90))
+    assert p["global_scale"] == 5243
+    assert p["x_qm_scale"] == 2 and p["epf_iters"] == 1
+    assert p["dc_step"] == [2.0, 1.0, 1.0]
+
+
+def test_epf_sharpness_schedule():
+    lib = O.lib()
+    assert lib.orc_epf_sharpness_id(1.0, 0) == 7
+    assert lib.orc_epf_sharpness_id(1.5, 0) == 6
+    assert lib.orc_epf_sharpness_id(2.0, 1) == 7
+    assert lib.orc_epf_sharpness_id(2.0, 0) == 5
+    assert lib.orc_epf_sharpness_id(4.0, 0) == 4
+    assert lib.orc_epf_sharpness_id(25.0, 0) == 1
+
+
+def test_constant_block_fraction_reference_case():
+    # src/frame/chroma.rs:496-511: left half flat, right half ramp -> 4 of 8
+    xyb = np.zeros((3, 16, 32), np.float32)
+    xyb[:, :, 16:] = (np.arange(16, 32, dtype=np.float32) * 0.01)[None, None, :]
+    n = O.lib().orc_constant_blocks(xyb.ctypes.data, 32, 16)
+    assert n == 4
+    assert O.lib().orc_constant_blocks(np.zeros((3, 7, 7), np.float32).ctypes.data, 7, 7) == 0
+
+
+def test_dct8_round_trip_against_float64():
+    # forward DCT8 (scaled 1/64, transposed storage) vs an exact float64 DCT-II
+    rng = np.random.default_rng(5)
+    blk = rng.uniform(-1, 1, (8, 8)).astype(np.float32)
+    got = O.dct8x8(blk).reshape(8, 8)
+    n = np.arange(8)
+    c = np.cos(np.pi * (2 * n[None, :] + 1) * n[:, None] / 16)
+    scale = np.where(n == 0, 1 / 8, 1 / (8 * np.sqrt(2)) * 2 / np.sqrt(2) * np.sqrt(2) / 2)
+    # reference scaling: DC = mean, AC = 2/N-normalised with sqrt(2) gain
+    ref = c @ blk.astype(np.float64) @ c.T
+    dc_expected = blk.astype(np.float64).mean()
+    assert abs(got[0, 0] - dc_expected) < 1e-6
+    # coefficient (u, v) lands at [v][u]: transposed storage
+    ratio = got[1:, 0] / (ref[0, 1:] / 64.0)
+    assert np.allclose(ratio, ratio[0], rtol=1e-4)
+
+
+def test_frontend_token_accounting():
+    img = np.random.default_rng(7).integers(0, 256, (40, 72, 3), dtype=np.uint8)
+    f = O.frontend(img, 1.0)
+    # every block-channel emits its non-zero count token; histogram counts every token
+    xb, yb = 9, 5
+    assert int(f.histograms.sum()) == len(f.tokens)
+    assert len(f.tokens) >= 3 * xb * yb
+    assert f.group_offsets[-1] == len(f.tokens)
+    # the quantized coefficients' non-zero counts equal the stored counts
+    nz = (f.coeffs[..., 1:] != 0).sum(-1)  # (yb, xb, 3)
+    assert np.array_equal(nz.transpose(2, 0, 1), f.nzeros)
+
+
+def test_low_distance_uses_library_table():
+    m, inv = O.dct8_tables(0.2)
+    # spec DCT8 X/Y/B base weights: 1/3150, 1/560, 1/512 at the DC position
+    assert abs(m[0, 0] - 1 / 3150) < 1e-9 and abs(m[1, 0] - 1 / 560) < 1e-8
+    assert abs(m[2, 0] - 1 / 512) < 1e-8
+    assert np.all(inv[:, 0] == 0) and np.allclose(inv[:, 1:] * m[:, 1:], 1, rtol=1e-6)
