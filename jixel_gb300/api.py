@@ -174,6 +174,8 @@ class FrontendContext:
         return self._ctx
 
     def set_stream(self, stream_ptr: int | None):
+        """Launch on `stream_ptr` (a cudaStream_t); None or 0 restores the
+        context's own stream (the legacy default stream cannot be selected)."""
         self._check(self._lib.jxg_context_set_stream(self._ctx, stream_ptr or None))
 
     def run(self, pixels: np.ndarray, config: EncodeConfig):
