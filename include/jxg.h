@@ -181,6 +181,37 @@ int32_t jxg_op_fill_quant_field(void* ctx, const float* xyb, uint64_t width, uin
  * row-major samples in, 64 coefficients (transposed storage, 1/64 scale) out. */
 int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coefficients);
 
+/* Allocation-free token offsets -----------------------------------------
+ * This entry point has no counterpart in the reference encoder.  It is for
+ * callers that cannot allocate device memory at encode time: a host that
+ * owns every device buffer through its own pool or arena, a real-time
+ * pipeline that forbids allocation after start-up, or code that enqueues
+ * work where a cudaMalloc would stall or serialise other streams.  It runs
+ * the same exclusive scan the front end uses to place tokens (token counts
+ * in the [group][1024 blocks][Y, X, B] layout -> per-entry offsets, per-group
+ * offsets and, in group_offsets[num_groups], the token total), reading and
+ * writing only the caller's device buffers plus one fixed scratch array
+ * compiled into the library (a file-scope __device__ array of 16 KiB of
+ * chunk sums and 1 KiB of pass scalars, held by every GPU that loads the
+ * library until the process exits).
+ *
+ * - counts:        device, num_groups * 3072 uint32 token counts;
+ * - offsets:       device, num_groups * 3072 uint32 exclusive offsets out;
+ * - group_offsets: device, num_groups + 1 uint64 out;
+ * - cuda_stream:   a cudaStream_t (NULL = the legacy default stream).
+ * Limit: num_groups <= JXG_NOALLOC_MAX_GROUPS (frames up to about 2.8
+ * gigapixels); larger requests return JXG_ERR_DIMENSION_TOO_LARGE.  The call
+ * only enqueues work on the stream; it calls no cudaMalloc, cudaFree or
+ * allocating library routine.  The first call on a device looks up the
+ * scratch array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  All calls share
+ * the one scratch array, which keeps the last call's contents: calls whose
+ * work overlaps on the GPU (different streams, or different host threads on
+ * one device) race and must be serialised by the caller. */
+#define JXG_NOALLOC_MAX_GROUPS 10922
+int32_t jxg_token_offsets_noalloc(const uint32_t* counts, uint64_t num_groups, uint32_t* offsets,
+                                  uint64_t* group_offsets, void* cuda_stream);
+
 /* Kernel timing -------------------------------------------------------- */
 /* With `enable`, every launch of this context is bracketed by CUDA events on
  * its stream; jxg_kernel_times sums their durations per kernel. */

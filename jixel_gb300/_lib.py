@@ -27,12 +27,14 @@ EXPORTS = [
     "jxg_frontend",
     "jxg_op_fill_quant_field",
     "jxg_op_dct8x8",
+    "jxg_token_offsets_noalloc",
     "jxg_enable_kernel_timing",
     "jxg_kernel_times",
     "jxg_reset_kernel_times",
 ]
 
 NUM_FINE_AC_CONTEXTS = 14850
+NOALLOC_MAX_GROUPS = 10922
 ALPHABET_SIZE = 128
 
 
@@ -118,6 +120,7 @@ def load() -> ctypes.CDLL:
                                ctypes.POINTER(FrameParams), ctypes.POINTER(FrontendOutput)]),
         "jxg_op_fill_quant_field": (i32, [vp, vp, u64, u64, f32, f32, vp]),
         "jxg_op_dct8x8": (i32, [vp, vp, u64, vp]),
+        "jxg_token_offsets_noalloc": (i32, [vp, u64, vp, vp, vp]),
         "jxg_enable_kernel_timing": (i32, [vp, i32]),
         "jxg_kernel_times": (i32, [vp, ctypes.POINTER(ctypes.c_char_p),
                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(u64), i32]),

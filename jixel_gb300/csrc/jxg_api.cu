@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -368,6 +369,37 @@ int read_params(Context* c, jxg_frame_params* out) {
   return JXG_OK;
 }
 
+// Scratch of jxg_token_offsets_noalloc (see include/jxg.h): the chunk sums of
+// the scan and the scalars its middle step writes.  A file-scope device array,
+// so the entry point never allocates; every call shares it.
+constexpr int kNoAllocMaxChunks = 4096;
+static_assert(static_cast<int64_t>(kNoAllocMaxChunks) * kScanChunk >=
+                  static_cast<int64_t>(JXG_NOALLOC_MAX_GROUPS) * 3 * 1024,
+              "scratch must cover the stated group limit");
+struct NoAllocScanScratch {
+  uint32_t chunk_sums[kNoAllocMaxChunks];
+  DeviceStats stats;
+};
+static __device__ __align__(256) NoAllocScanScratch g_noalloc_scan_scratch;
+
+// Device address of the scratch array per device, looked up on the first
+// call with that device current.
+constexpr int kMaxDevices = 64;
+NoAllocScanScratch* g_noalloc_scratch_ptr[kMaxDevices] = {};
+std::mutex g_noalloc_mutex;
+
+int noalloc_scratch(int device, NoAllocScanScratch** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_scratch_ptr[device]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scan_scratch);
+    if (e != cudaSuccess || !ptr) return JXG_ERR_CUDA;
+    g_noalloc_scratch_ptr[device] = static_cast<NoAllocScanScratch*>(ptr);
+  }
+  *out = g_noalloc_scratch_ptr[device];
+  return JXG_OK;
+}
+
 }  // namespace
 }  // namespace jxg
 
@@ -607,6 +639,30 @@ int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coe
   if (st) return st;
   JXG_CUDA(c, cudaMemcpyAsync(coefficients, c->op_out.ptr, bytes, cudaMemcpyDeviceToHost, s));
   return jxg::wait(c);
+}
+
+int32_t jxg_token_offsets_noalloc(const uint32_t* counts, uint64_t num_groups, uint32_t* offsets,
+                                  uint64_t* group_offsets, void* cuda_stream) {
+  if (!counts || !offsets || !group_offsets || num_groups == 0) return JXG_ERR_INVALID_ARGUMENT;
+  if (num_groups > JXG_NOALLOC_MAX_GROUPS) return JXG_ERR_DIMENSION_TOO_LARGE;
+  int device = -1;
+  if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= jxg::kMaxDevices)
+    return JXG_ERR_CUDA;
+  jxg::NoAllocScanScratch* scratch = nullptr;
+  int st = jxg::noalloc_scratch(device, &scratch);
+  if (st) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+  const int64_t n = static_cast<int64_t>(num_groups) * 3 * 1024;
+  const int chunks = static_cast<int>((n + jxg::kScanChunk - 1) / jxg::kScanChunk);
+  // the middle step reads the pass scalars: start them from zero
+  if (cudaMemsetAsync(&scratch->stats, 0, sizeof(scratch->stats), s) != cudaSuccess)
+    return JXG_ERR_CUDA;
+  jxg::k_scan_reduce<<<chunks, jxg::kScanThreads, 0, s>>>(counts, n, scratch->chunk_sums);
+  jxg::k_scan_chunks<<<1, jxg::kScanThreads, 0, s>>>(scratch->chunk_sums, chunks, &scratch->stats,
+                                                     group_offsets, static_cast<int>(num_groups));
+  jxg::k_scan_apply<<<chunks, jxg::kScanThreads, 0, s>>>(counts, n, scratch->chunk_sums, offsets,
+                                                         group_offsets);
+  return cudaGetLastError() == cudaSuccess ? JXG_OK : JXG_ERR_CUDA;
 }
 
 int32_t jxg_enable_kernel_timing(void* ctx, int32_t enable) {
