@@ -136,11 +136,10 @@ def algorithmic_bytes(kernel: str, w: int, h: int, tokens_per_frame: float) -> f
         # three f32 planes in, one u8 per block out
         "k_adaptive_quant": px * 12 + blocks,
         # three f32 planes in; i32 levels (192 per block), 3 x i16 DC, 3 u8 counts,
-        # 3 u32 token counts out
+        # 3 u32 token counts out (the constant-block count rides along)
         "k_tile_quantize": px * 12 + blocks * (192 * 4 + 6 + 3 + 12),
         # levels + counts in, 8-byte tokens out, one 4-byte histogram update per token
         "k_tokenize": blocks * (192 * 4 + 3 + 1 + 12) + tokens_per_frame * (8 + 4),
-        "k_constant_blocks": px * 12,
     }
     return table.get(kernel)
 

@@ -275,6 +275,9 @@ void fill_kernel_args(const DistanceParams& p, KernelArgs* a) {
   }
   const float total = 0.29959705784054957f;
   for (int i = 0; i < 4; ++i) a->aq_fe_weights[i] *= total / norm;
+  const float k_mul = 211.66567973503678f;
+  const float mul_v = k_mul * 1e8f;
+  a->aq_masking_sqrt_mul = std::sqrt(mul_v);
   // cfl_deadzone, src/color_correlation.rs:384-394
   if (d <= 1.0f) a->cfl_deadzone = 1.5f;
   else if (d >= 2.0f) a->cfl_deadzone = 0.0f;

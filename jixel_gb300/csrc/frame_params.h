@@ -51,6 +51,7 @@ struct KernelArgs {
   float qm_mul[3];         // x_qm_mul, 1, b_qm_mul
   float thresholds[3][4];  // quantize_ac_thresholds_scaled per channel
   float aq_mul, aq_add, aq_hf_strength, aq_fe_weights[4];
+  float aq_masking_sqrt_mul;  // sqrt(211.66567973503678 * 1e8) in f32
   float cfl_deadzone;
   float matrix[3][64];     // DCT8 dequant weights
   float inv_matrix[3][64]; // their reciprocals (index 0 = 0)

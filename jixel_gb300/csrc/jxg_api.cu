@@ -262,15 +262,6 @@ int enqueue_frontend(Context* c, const void* pixels, uint64_t w, uint64_t h, int
     });
   }
   if (st) return st;
-  // 2. frame statistics (screen content)
-  {
-    const int64_t full = static_cast<int64_t>((w / 8) * (h / 8));
-    const int grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>((full + 255) / 256, sms * 4)));
-    st = launch(c, "k_constant_blocks", [&] {
-      k_constant_blocks<<<grid, 256, 0, s>>>(xyb, a.width, a.height, plane, stats);
-    });
-    if (st) return st;
-  }
   // 3. adaptive quant field per DC group
   {
     dim3 grid(a.tiles_x, a.tiles_y);
@@ -290,6 +281,7 @@ int enqueue_frontend(Context* c, const void* pixels, uint64_t w, uint64_t h, int
     to.quant_dc = static_cast<int16_t*>(c->quant_dc.ptr);
     to.nzeros = static_cast<uint8_t*>(c->nzeros.ptr);
     to.token_counts = static_cast<uint32_t*>(c->counts.ptr);
+    to.stats = stats;
     dim3 grid(a.tiles_x, a.tiles_y);
     st = launch(c, "k_tile_quantize", [&] {
       k_tile_quantize<<<grid, kTileThreads, kTileSmemBytes, s>>>(a, xyb, c->d_pos, to);
@@ -328,7 +320,7 @@ int enqueue_frontend(Context* c, const void* pixels, uint64_t w, uint64_t h, int
     ta.stats = stats;
     ta.tokens = static_cast<uint2*>(c->tokens.ptr);
     ta.histograms = static_cast<uint32_t*>(c->hist.ptr);
-    const int64_t warps = nb * 3;
+    const int64_t warps = nb;
     const int grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, sms * 16)));
     st = launch(c, "k_tokenize", [&] { k_tokenize<<<grid, 256, 0, s>>>(ta, c->d_scan); });
     if (st) return st;
