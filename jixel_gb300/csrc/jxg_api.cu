@@ -47,8 +47,8 @@ struct Context {
   uint8_t* d_scan = nullptr;    // natural 8x8 order, 64
   uint8_t* d_pos = nullptr;     // its inverse, 64
   // frame buffers
-  DevBuf pixels, xyb, qf, ytox, ytob, quant_dc, coeffs, nzeros, counts, offsets, chunks, tokens,
-      hist, stats, group_offsets, op_in, op_out;
+  DevBuf pixels, xyb, qf, ytox, ytob, quant_dc, levels, wide_levels, coeffs, nzeros, counts,
+      offsets, chunks, tokens, hist, stats, group_offsets, op_in, op_out;
   // last pass
   bool have_frame = false;
   uint64_t width = 0, height = 0;
@@ -227,7 +227,8 @@ int enqueue_frontend(Context* c, const void* pixels, uint64_t w, uint64_t h, int
   if ((st = ensure(c, c->xyb, 3 * plane * sizeof(float))) ||
       (st = ensure(c, c->qf, nb)) || (st = ensure(c, c->ytox, ntiles)) ||
       (st = ensure(c, c->ytob, ntiles)) || (st = ensure(c, c->quant_dc, 3 * nb * 2)) ||
-      (st = ensure(c, c->coeffs, nb * 192 * 4)) || (st = ensure(c, c->nzeros, 3 * nb)) ||
+      (st = ensure(c, c->levels, nb * 192 * 2)) || (st = ensure(c, c->wide_levels, nb * 192 * 4)) ||
+      (st = ensure(c, c->nzeros, 3 * nb)) ||
       (st = ensure(c, c->counts, ncounts * 4)) || (st = ensure(c, c->offsets, ncounts * 4)) ||
       (st = ensure(c, c->chunks, nchunks * 4)) ||
       (st = ensure(c, c->tokens, fi.max_tokens * sizeof(uint2))) ||
@@ -277,7 +278,8 @@ int enqueue_frontend(Context* c, const void* pixels, uint64_t w, uint64_t h, int
     to.ytox = static_cast<int8_t*>(c->ytox.ptr);
     to.ytob = static_cast<int8_t*>(c->ytob.ptr);
     to.qf = static_cast<const uint8_t*>(c->qf.ptr);
-    to.coeffs = static_cast<int32_t*>(c->coeffs.ptr);
+    to.levels = static_cast<int16_t*>(c->levels.ptr);
+    to.wide_levels = static_cast<int32_t*>(c->wide_levels.ptr);
     to.quant_dc = static_cast<int16_t*>(c->quant_dc.ptr);
     to.nzeros = static_cast<uint8_t*>(c->nzeros.ptr);
     to.token_counts = static_cast<uint32_t*>(c->counts.ptr);
@@ -313,7 +315,8 @@ int enqueue_frontend(Context* c, const void* pixels, uint64_t w, uint64_t h, int
     ta.xb = a.xb;
     ta.yb = a.yb;
     ta.groups_x = a.groups_x;
-    ta.coeffs = static_cast<const int32_t*>(c->coeffs.ptr);
+    ta.levels = static_cast<const int16_t*>(c->levels.ptr);
+    ta.wide_levels = static_cast<const int32_t*>(c->wide_levels.ptr);
     ta.nzeros = static_cast<const uint8_t*>(c->nzeros.ptr);
     ta.qf = static_cast<const uint8_t*>(c->qf.ptr);
     ta.offsets = static_cast<const uint32_t*>(c->offsets.ptr);
@@ -322,7 +325,7 @@ int enqueue_frontend(Context* c, const void* pixels, uint64_t w, uint64_t h, int
     ta.histograms = static_cast<uint32_t*>(c->hist.ptr);
     const int64_t warps = nb;
     const int grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, sms * 16)));
-    st = launch(c, "k_tokenize", [&] { k_tokenize<<<grid, 256, 0, s>>>(ta, c->d_scan); });
+    st = launch(c, "k_tokenize", [&] { k_tokenize<<<grid, 256, 0, s>>>(ta); });
     if (st) return st;
   }
   c->have_frame = true;
@@ -441,6 +444,7 @@ void jxg_context_destroy(void* ctx) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (jxg::DevBuf* b : {&c->pixels, &c->xyb, &c->qf, &c->ytox, &c->ytob, &c->quant_dc, &c->coeffs,
+                         &c->levels, &c->wide_levels,
                          &c->nzeros, &c->counts, &c->offsets, &c->chunks, &c->tokens, &c->hist,
                          &c->stats, &c->group_offsets, &c->op_in, &c->op_out})
     if (b->ptr) cudaFree(b->ptr);
@@ -535,6 +539,17 @@ int32_t jxg_frontend_fetch(void* ctx, jxg_frontend_output* out) {
   };
   if (out->tokens && out->token_capacity < p.num_tokens)
     return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "token buffer too small");
+  if (out->coefficients) {
+    if ((st = jxg::ensure(c, c->coeffs, nb * 192 * 4))) return st;
+    const int64_t count = static_cast<int64_t>(nb) * 192;
+    const int grid = static_cast<int>(std::min<int64_t>((count + 255) / 256, 4096));
+    st = jxg::launch(c, "k_levels_to_raw", [&] {
+      jxg::k_levels_to_raw<<<grid, 256, 0, s>>>(static_cast<const int16_t*>(c->levels.ptr),
+                                                static_cast<const int32_t*>(c->wide_levels.ptr),
+                                                c->d_pos, count, static_cast<int32_t*>(c->coeffs.ptr));
+    });
+    if (st) return st;
+  }
   if ((st = copy(out->quant_field, c->qf.ptr, nb)) || (st = copy(out->ytox_map, c->ytox.ptr, nt)) ||
       (st = copy(out->ytob_map, c->ytob.ptr, nt)) ||
       (st = copy(out->quant_dc, c->quant_dc.ptr, 3 * nb * 2)) ||

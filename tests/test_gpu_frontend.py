@@ -57,9 +57,20 @@ def test_config1_q90(ctx):
     compare(ctx, synthetic.config1_image(), 1.0)
 
 
-@pytest.mark.parametrize("q", [30, 50, 75, 85, 90, 94])
+@pytest.mark.parametrize("q", [0, 30, 50, 75, 85, 90, 94, 95, 98, 100])
 def test_config1_qualities(ctx, q):
     compare(ctx, synthetic.config1_image(), J.distance_from_quality(q))
+
+
+def test_full_contrast_at_minimum_distance(ctx):
+    # full-swing 16-bit checker at the minimum distance: about the largest
+    # levels the quantiser reaches (a few hundred, far inside the 16-bit
+    # level store; wider levels would take its exact int32 side buffer)
+    y, x = np.mgrid[0:96, 0:128]
+    img = np.where(((x // 3) + (y // 5)) % 2 == 0, 65535, 0).astype(np.uint16)
+    img = np.stack([img, 65535 - img, img // 2], axis=-1)
+    got, _ = compare(ctx, img, 0.05)
+    assert 100 < int(np.abs(got.coefficients).max()) < 32767
 
 
 @pytest.mark.parametrize("w,h", [(1, 1), (7, 9), (27, 28), (33, 33), (64, 17), (65, 65),
