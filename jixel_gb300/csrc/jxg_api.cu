@@ -47,7 +47,7 @@ struct Context {
   uint8_t* d_scan = nullptr;    // natural 8x8 order, 64
   uint8_t* d_pos = nullptr;     // its inverse, 64
   // frame buffers
-  DevBuf pixels, xyb, qf, ytox, ytob, quant_dc, levels, wide_levels, coeffs, nzeros, counts,
+  DevBuf pixels, xyb, qf, ytox, ytob, quant_dc, levels, wide_levels, coeffs, nzeros, nz_packed, counts,
       offsets, chunks, tokens, hist, stats, group_offsets, op_in, op_out;
   // last pass
   bool have_frame = false;
@@ -222,13 +222,13 @@ int enqueue_frontend(Context* c, const void* pixels, uint64_t w, uint64_t h, int
   c->height = h;
   const int64_t nb = static_cast<int64_t>(fi.xsize_blocks * fi.ysize_blocks);
   const int64_t ntiles = static_cast<int64_t>(fi.xsize_tiles * fi.ysize_tiles);
-  const int64_t ncounts = static_cast<int64_t>(fi.num_groups) * 1024 * 3;
+  const int64_t ncounts = static_cast<int64_t>(fi.num_groups) * 1024 * 4;
   const int64_t nchunks = (ncounts + kScanChunk - 1) / kScanChunk;
   if ((st = ensure(c, c->xyb, 3 * plane * sizeof(float))) ||
       (st = ensure(c, c->qf, nb)) || (st = ensure(c, c->ytox, ntiles)) ||
       (st = ensure(c, c->ytob, ntiles)) || (st = ensure(c, c->quant_dc, 3 * nb * 2)) ||
       (st = ensure(c, c->levels, nb * 192 * 2)) || (st = ensure(c, c->wide_levels, nb * 192 * 4)) ||
-      (st = ensure(c, c->nzeros, 3 * nb)) ||
+      (st = ensure(c, c->nzeros, 3 * nb)) || (st = ensure(c, c->nz_packed, 4 * nb)) ||
       (st = ensure(c, c->counts, ncounts * 4)) || (st = ensure(c, c->offsets, ncounts * 4)) ||
       (st = ensure(c, c->chunks, nchunks * 4)) ||
       (st = ensure(c, c->tokens, fi.max_tokens * sizeof(uint2))) ||
@@ -282,6 +282,7 @@ int enqueue_frontend(Context* c, const void* pixels, uint64_t w, uint64_t h, int
     to.wide_levels = static_cast<int32_t*>(c->wide_levels.ptr);
     to.quant_dc = static_cast<int16_t*>(c->quant_dc.ptr);
     to.nzeros = static_cast<uint8_t*>(c->nzeros.ptr);
+    to.nz_packed = static_cast<uint32_t*>(c->nz_packed.ptr);
     to.token_counts = static_cast<uint32_t*>(c->counts.ptr);
     to.stats = stats;
     dim3 grid(a.tiles_x, a.tiles_y);
@@ -305,7 +306,7 @@ int enqueue_frontend(Context* c, const void* pixels, uint64_t w, uint64_t h, int
                                                      static_cast<int>(fi.num_groups));
          })) ||
         (st = launch(c, "k_scan_apply", [&] {
-           k_scan_apply<<<ch, kScanThreads, 0, s>>>(counts, ncounts, chunks, offs, goffs);
+           k_scan_apply<<<ch, kScanThreads, 0, s>>>(counts, ncounts, chunks, offs, goffs, 4 * 1024);
          })))
       return st;
   }
@@ -317,7 +318,7 @@ int enqueue_frontend(Context* c, const void* pixels, uint64_t w, uint64_t h, int
     ta.groups_x = a.groups_x;
     ta.levels = static_cast<const int16_t*>(c->levels.ptr);
     ta.wide_levels = static_cast<const int32_t*>(c->wide_levels.ptr);
-    ta.nzeros = static_cast<const uint8_t*>(c->nzeros.ptr);
+    ta.nz_packed = static_cast<const uint32_t*>(c->nz_packed.ptr);
     ta.qf = static_cast<const uint8_t*>(c->qf.ptr);
     ta.offsets = static_cast<const uint32_t*>(c->offsets.ptr);
     ta.stats = stats;
@@ -444,7 +445,7 @@ void jxg_context_destroy(void* ctx) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (jxg::DevBuf* b : {&c->pixels, &c->xyb, &c->qf, &c->ytox, &c->ytob, &c->quant_dc, &c->coeffs,
-                         &c->levels, &c->wide_levels,
+                         &c->levels, &c->wide_levels, &c->nz_packed,
                          &c->nzeros, &c->counts, &c->offsets, &c->chunks, &c->tokens, &c->hist,
                          &c->stats, &c->group_offsets, &c->op_in, &c->op_out})
     if (b->ptr) cudaFree(b->ptr);
@@ -668,7 +669,7 @@ int32_t jxg_token_offsets_noalloc(const uint32_t* counts, uint64_t num_groups, u
   jxg::k_scan_chunks<<<1, jxg::kScanThreads, 0, s>>>(scratch->chunk_sums, chunks, &scratch->stats,
                                                      group_offsets, static_cast<int>(num_groups));
   jxg::k_scan_apply<<<chunks, jxg::kScanThreads, 0, s>>>(counts, n, scratch->chunk_sums, offsets,
-                                                         group_offsets);
+                                                         group_offsets, 3 * 1024);
   return cudaGetLastError() == cudaSuccess ? JXG_OK : JXG_ERR_CUDA;
 }
 
