@@ -8,6 +8,8 @@ whole front end (XYB, AQ field, CfL maps, DCT8 + quantisation, tokens and
 per-context histograms).  `value` is timed with CUDA events on the launching
 stream with the input resident in HBM; `e2e` runs the public C ABI with host
 buffers (pinned), the upload and the result download inside the timed region.
+`batch` compares, on 256 images of log-uniform sizes (half RGBA8) at q90,
+one pass per image against one batched pass replayed as a CUDA graph.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 """
@@ -30,6 +32,7 @@ WIDTH, HEIGHT = 3840, 2160
 QUALITIES = (75, 90, 95)
 METRIC = "VarDCT MP/s"
 L2_FLUSH_BYTES = 256 << 20
+BATCH_IMAGES = 256
 
 
 def parse_args():
@@ -40,6 +43,9 @@ def parse_args():
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-batch", action="store_true",
+                   help="skip the 256-image plain-vs-batched comparison")
+    p.add_argument("--batch-images", type=int, default=BATCH_IMAGES)
     return p.parse_args()
 
 
@@ -132,7 +138,7 @@ def algorithmic_bytes(kernel: str, w: int, h: int, tokens_per_frame: float) -> f
     blocks = ((w + 7) // 8) * ((h + 7) // 8)
     table = {
         # RGB8 in, three f32 planes out
-        "k_xyb_rgb8": px * (3 + 12),
+        "k_xyb": px * (3 + 12),
         # three f32 planes in, one u8 per block out
         "k_adaptive_quant": px * 12 + blocks,
         # three f32 planes in; i32 levels (192 per block), 3 x i16 DC, 3 u8 counts,
@@ -286,6 +292,10 @@ def run_gpu(args):
     }
     launches = int(sum(v[1] for v in ktimes.values()))
 
+    batch = None
+    if not args.no_batch:
+        batch = run_batch(ctx, stream, flush, args, world, dev)
+
     # end to end through the public C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
@@ -305,11 +315,85 @@ def run_gpu(args):
             "clocks": clocks,
             "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(ktimes.items())},
             "tokens_per_frame": [int(x) for x in tokens],
+            "batch": batch,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_batch(ctx, stream, flush, args, world, dev) -> dict:
+    """256 images of log-uniform sizes 64x64..2048x1536 (odd ones RGBA8), q90:
+    one pass per image (`plain`) against one pass for the whole set
+    (`batched`: one launch per stage over every frame, replayed as a CUDA
+    graph).  Pixels are resident in HBM for both; CUDA events time each step
+    on the launching stream."""
+    import torch
+
+    import jixel_gb300 as J
+    from jixel_gb300 import synthetic
+
+    imgs = synthetic.config3_batch(args.batch_images)
+    mp = sum(i.shape[0] * i.shape[1] for i in imgs) / 1e6
+    cfg = J.EncodeConfig(speed=J.Speed.ULTRA_FAST).with_quality(90)
+    d_imgs = [torch.from_numpy(i.reshape(-1)).to(dev) for i in imgs]
+    torch.cuda.synchronize(dev)
+
+    def plain_step():
+        for img, d in zip(imgs, d_imgs):
+            h, w, ch = img.shape
+            ctx.run_device(d.data_ptr(), w, h, ch, 8, cfg)
+
+    b = ctx.batch(pixels_on_device=True)
+    for img, d in zip(imgs, d_imgs):
+        h, w, ch = img.shape
+        b.add_device(d.data_ptr(), w, h, ch, 8, cfg, keep=d)
+
+    def batched_step():
+        b.run(use_graph=True)
+
+    def timed(fn) -> float:
+        for _ in range(max(args.warmup, 1)):
+            fn()
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+        total = 0.0
+        for _ in range(args.steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            fn()
+            e.record(stream)
+            torch.cuda.synchronize(dev)
+            total += s.elapsed_time(e)
+        t = torch.tensor([total], device=dev, dtype=torch.float64)
+        if world > 1:
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    plain_ms = timed(plain_step)
+    ctx.enable_kernel_timing(True)
+    ctx.reset_kernel_times()
+    b.run(use_graph=False)  # per-kernel times of one batched pass (graphs carry no events)
+    ktimes = ctx.kernel_times()
+    ctx.enable_kernel_timing(False)
+    batched_ms = timed(batched_step)
+    b.close()
+    plain = world * args.steps * mp / (plain_ms / 1000.0)
+    batched = world * args.steps * mp / (batched_ms / 1000.0)
+    return {
+        "workload": f"{len(imgs)} images, log-uniform 64x64..2048x1536, half RGB8 half RGBA8, "
+                    "q90, UltraFast gates",
+        "megapixels_per_step": mp, "unit": "MP/s",
+        "plain": {"value": plain, "ms_per_step": plain_ms / args.steps,
+                  "launches_per_step": 8 * len(imgs)},
+        "batched": {"value": batched, "ms_per_step": batched_ms / args.steps,
+                    "launches_per_step": 8, "cuda_graph": True},
+        "batched_over_plain": batched / plain,
+        "batched_kernels_ms": {k: v[0] for k, v in sorted(ktimes.items())},
+    }
 
 
 def run_e2e(ctx, img, cfgs, args, world, dev):

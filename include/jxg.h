@@ -168,6 +168,34 @@ int32_t jxg_frontend(void* ctx, const void* pixels, uint64_t width, uint64_t hei
                      int32_t channels, int32_t bits, const jxg_config* config,
                      jxg_frame_params* params, jxg_frontend_output* out);
 
+/* Batch -----------------------------------------------------------------
+ * Many frames of any sizes, layouts and distances in one pass: each stage is
+ * one launch over the (frame, work unit) list of the whole batch, and the
+ * pass can be recorded once as a CUDA graph and replayed.  Every frame's
+ * results equal those of a one-frame jxg_frontend call on it.  The reference
+ * encodes one image per call (encode_image, src/encode_image.rs:1610); a
+ * caller with many images calls this instead of looping.
+ *
+ * jxg_batch_create: `pixels_on_device` nonzero = the pixel pointers given to
+ *   jxg_batch_add are device memory of the context's GPU, else host memory.
+ * jxg_batch_add: appends one frame (arguments as jxg_frontend_run); returns
+ *   its index, or the negated status when the input is rejected.  The
+ *   pointer is read at every jxg_batch_run, so it must stay valid.
+ * jxg_batch_run: runs the pass and waits.  `use_graph` nonzero records the
+ *   pass as a CUDA graph on the first run and replays it afterwards; adding
+ *   a frame, or running another pass on the context, re-records it.
+ * jxg_batch_result: scalars and outputs of frame `index` of the last run
+ *   (either pointer may be NULL); as jxg_frontend_params + _fetch.
+ * One context holds one pass at a time: results of a batch are readable
+ * until the context runs another pass. */
+int32_t jxg_batch_create(void* ctx, int32_t pixels_on_device, void** out_batch);
+int64_t jxg_batch_add(void* batch, const void* pixels, uint64_t width, uint64_t height,
+                      int32_t channels, int32_t bits, const jxg_config* config);
+int32_t jxg_batch_run(void* batch, int32_t use_graph);
+int32_t jxg_batch_result(void* batch, uint64_t index, jxg_frame_params* params,
+                         jxg_frontend_output* out);
+void jxg_batch_destroy(void* batch);
+
 /* Operator table --------------------------------------------------------
  * Single-stage entry points standing in for the reference's kernel
  * dispatch table (EncodingContext, src/encoding_context.rs:224-294).  They

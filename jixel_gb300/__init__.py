@@ -3,10 +3,10 @@
 The compute runs in the CUDA library ``_build/libjxg.so`` (C ABI in
 ``include/jxg.h``); this package is its host-side mirror.
 """
-from .api import (EncodeConfig, EncodeError, FrontendContext, FrontendResult, Speed,
+from .api import (EncodeConfig, EncodeError, FrontendBatch, FrontendContext, FrontendResult, Speed,
                   distance_from_quality, encode_frontend, frame_info)
 
 __all__ = [
-    "EncodeConfig", "EncodeError", "FrontendContext", "FrontendResult", "Speed",
+    "EncodeConfig", "EncodeError", "FrontendBatch", "FrontendContext", "FrontendResult", "Speed",
     "distance_from_quality", "encode_frontend", "frame_info",
 ]

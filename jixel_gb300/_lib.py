@@ -25,6 +25,11 @@ EXPORTS = [
     "jxg_frontend_params",
     "jxg_frontend_fetch",
     "jxg_frontend",
+    "jxg_batch_create",
+    "jxg_batch_add",
+    "jxg_batch_run",
+    "jxg_batch_result",
+    "jxg_batch_destroy",
     "jxg_op_fill_quant_field",
     "jxg_op_dct8x8",
     "jxg_token_offsets_noalloc",
@@ -118,6 +123,12 @@ def load() -> ctypes.CDLL:
         "jxg_frontend_fetch": (i32, [vp, ctypes.POINTER(FrontendOutput)]),
         "jxg_frontend": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config),
                                ctypes.POINTER(FrameParams), ctypes.POINTER(FrontendOutput)]),
+        "jxg_batch_create": (i32, [vp, i32, ctypes.POINTER(vp)]),
+        "jxg_batch_add": (ctypes.c_int64, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config)]),
+        "jxg_batch_run": (i32, [vp, i32]),
+        "jxg_batch_result": (i32, [vp, u64, ctypes.POINTER(FrameParams),
+                                   ctypes.POINTER(FrontendOutput)]),
+        "jxg_batch_destroy": (None, [vp]),
         "jxg_op_fill_quant_field": (i32, [vp, vp, u64, u64, f32, f32, vp]),
         "jxg_op_dct8x8": (i32, [vp, vp, u64, vp]),
         "jxg_token_offsets_noalloc": (i32, [vp, u64, vp, vp, vp]),

@@ -143,6 +143,47 @@ def _pixels_kind(pixels: np.ndarray) -> tuple[int, int]:
     raise EncodeError(10, f"unsupported sample type {pixels.dtype}")
 
 
+def _params_dict(p) -> dict:
+    out = {n: getattr(p, n) for n, _ in L.FrameParams._fields_ if n != "reserved"}
+    out["dc_step"] = list(p.dc_step)
+    out["screen_content"] = bool(out["screen_content"])
+    return out
+
+
+def _result_buffers(p: dict, width: int, height: int, coefficients: bool, xyb: bool):
+    """Host arrays for every output of one frame and the C struct pointing at them."""
+    fi = frame_info(width, height)
+    xb, yb = fi.xsize_blocks, fi.ysize_blocks
+    r = FrontendResult(
+        params=p,
+        quant_field=np.zeros((yb, xb), np.uint8),
+        ac_strategy=np.zeros((yb, xb), np.uint8),
+        ytox=np.zeros((fi.ysize_tiles, fi.xsize_tiles), np.int8),
+        ytob=np.zeros((fi.ysize_tiles, fi.xsize_tiles), np.int8),
+        quant_dc=np.zeros((3, yb, xb), np.int16),
+        coefficients=np.zeros((yb, xb, 3, 64), np.int32) if coefficients else None,
+        num_nzeros=np.zeros((3, yb, xb), np.uint8),
+        tokens=np.zeros((max(int(p["num_tokens"]), 1), 2), np.uint32),
+        group_offsets=np.zeros(fi.num_groups + 1, np.uint64),
+        histograms=np.zeros((L.NUM_FINE_AC_CONTEXTS, L.ALPHABET_SIZE), np.uint32),
+        xyb=np.zeros((3, height, width), np.float32) if xyb else None,
+    )
+    o = L.FrontendOutput()
+    o.quant_field = r.quant_field.ctypes.data
+    o.ac_strategy = r.ac_strategy.ctypes.data
+    o.ytox_map = r.ytox.ctypes.data
+    o.ytob_map = r.ytob.ctypes.data
+    o.quant_dc = r.quant_dc.ctypes.data
+    o.coefficients = r.coefficients.ctypes.data if coefficients else None
+    o.num_nzeros = r.num_nzeros.ctypes.data
+    o.xyb = r.xyb.ctypes.data if xyb else None
+    o.tokens = r.tokens.ctypes.data
+    o.token_capacity = r.tokens.shape[0]
+    o.group_offsets = r.group_offsets.ctypes.data
+    o.histograms = r.histograms.ctypes.data
+    return r, o
+
+
 class FrontendContext:
     """One device encoder (`EncodingContext`, src/encoding_context.rs:609)."""
 
@@ -197,46 +238,19 @@ class FrontendContext:
     def params(self) -> dict:
         p = L.FrameParams()
         self._check(self._lib.jxg_frontend_params(self._ctx, ctypes.byref(p)))
-        out = {n: getattr(p, n) for n, _ in L.FrameParams._fields_ if n != "reserved"}
-        out["dc_step"] = list(p.dc_step)
-        out["screen_content"] = bool(out["screen_content"])
-        return out
+        return _params_dict(p)
 
     def fetch(self, width: int, height: int, *, coefficients: bool = True,
               xyb: bool = False) -> FrontendResult:
-        fi = frame_info(width, height)
         p = self.params()
-        xb, yb = fi.xsize_blocks, fi.ysize_blocks
-        r = FrontendResult(
-            params=p,
-            quant_field=np.zeros((yb, xb), np.uint8),
-            ac_strategy=np.zeros((yb, xb), np.uint8),
-            ytox=np.zeros((fi.ysize_tiles, fi.xsize_tiles), np.int8),
-            ytob=np.zeros((fi.ysize_tiles, fi.xsize_tiles), np.int8),
-            quant_dc=np.zeros((3, yb, xb), np.int16),
-            coefficients=np.zeros((yb, xb, 3, 64), np.int32) if coefficients else None,
-            num_nzeros=np.zeros((3, yb, xb), np.uint8),
-            tokens=np.zeros((max(int(p["num_tokens"]), 1), 2), np.uint32),
-            group_offsets=np.zeros(fi.num_groups + 1, np.uint64),
-            histograms=np.zeros((L.NUM_FINE_AC_CONTEXTS, L.ALPHABET_SIZE), np.uint32),
-            xyb=np.zeros((3, height, width), np.float32) if xyb else None,
-        )
-        o = L.FrontendOutput()
-        o.quant_field = r.quant_field.ctypes.data
-        o.ac_strategy = r.ac_strategy.ctypes.data
-        o.ytox_map = r.ytox.ctypes.data
-        o.ytob_map = r.ytob.ctypes.data
-        o.quant_dc = r.quant_dc.ctypes.data
-        o.coefficients = r.coefficients.ctypes.data if coefficients else None
-        o.num_nzeros = r.num_nzeros.ctypes.data
-        o.xyb = r.xyb.ctypes.data if xyb else None
-        o.tokens = r.tokens.ctypes.data
-        o.token_capacity = r.tokens.shape[0]
-        o.group_offsets = r.group_offsets.ctypes.data
-        o.histograms = r.histograms.ctypes.data
+        r, o = _result_buffers(p, width, height, coefficients, xyb)
         self._check(self._lib.jxg_frontend_fetch(self._ctx, ctypes.byref(o)))
         r.tokens = r.tokens[: int(p["num_tokens"])]
         return r
+
+    def batch(self, pixels_on_device: bool = False) -> "FrontendBatch":
+        """A batch of frames run as one pass on this context."""
+        return FrontendBatch(self, pixels_on_device)
 
     def frontend(self, pixels: np.ndarray, config: EncodeConfig, *, coefficients: bool = True,
                  xyb: bool = False) -> FrontendResult:
@@ -276,6 +290,74 @@ class FrontendContext:
 
     def reset_kernel_times(self):
         self._check(self._lib.jxg_reset_kernel_times(self._ctx))
+
+
+class FrontendBatch:
+    """Many frames in one pass (jxg_batch_*): one launch per stage over all
+    frames, optionally recorded as a CUDA graph and replayed.  The pixel
+    arrays (or device pointers) handed to `add` are kept referenced and read
+    again at every `run`."""
+
+    def __init__(self, ctx: FrontendContext, pixels_on_device: bool = False):
+        self._ctx = ctx
+        self._lib = ctx._lib
+        self._b = ctypes.c_void_p()
+        self._keep = []
+        self._sizes = []
+        self._check(self._lib.jxg_batch_create(ctx.handle, 1 if pixels_on_device else 0,
+                                               ctypes.byref(self._b)))
+
+    def _check(self, st: int):
+        self._ctx._check(st)
+
+    def close(self):
+        if self._b:
+            self._lib.jxg_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self):
+        return len(self._sizes)
+
+    def add(self, pixels: np.ndarray, config: EncodeConfig) -> int:
+        pixels = np.ascontiguousarray(pixels)
+        ch, bits = _pixels_kind(pixels)
+        h, w = pixels.shape[:2]
+        return self._add(pixels.ctypes.data, w, h, ch, bits, config, pixels)
+
+    def add_device(self, device_ptr: int, width: int, height: int, channels: int, bits: int,
+                   config: EncodeConfig, keep=None) -> int:
+        return self._add(device_ptr, width, height, channels, bits, config, keep)
+
+    def _add(self, ptr, w, h, ch, bits, config, keep) -> int:
+        cfg = config._c()
+        idx = self._lib.jxg_batch_add(self._b, ptr, w, h, ch, bits, ctypes.byref(cfg))
+        if idx < 0:
+            self._check(-idx)
+        self._keep.append(keep)
+        self._sizes.append((w, h))
+        return idx
+
+    def run(self, use_graph: bool = True):
+        self._check(self._lib.jxg_batch_run(self._b, 1 if use_graph else 0))
+
+    def params(self, index: int) -> dict:
+        p = L.FrameParams()
+        self._check(self._lib.jxg_batch_result(self._b, index, ctypes.byref(p), None))
+        return _params_dict(p)
+
+    def result(self, index: int, *, coefficients: bool = True, xyb: bool = False) -> FrontendResult:
+        w, h = self._sizes[index]
+        p = self.params(index)
+        r, o = _result_buffers(p, w, h, coefficients, xyb)
+        self._check(self._lib.jxg_batch_result(self._b, index, None, ctypes.byref(o)))
+        r.tokens = r.tokens[: int(p["num_tokens"])]
+        return r
 
 
 def encode_frontend(pixels: np.ndarray, config: EncodeConfig, device: int = 0) -> FrontendResult:

@@ -37,6 +37,7 @@ struct DistanceParams {
 
 // Everything a kernel needs about one frame, passed by value (< 4 KB).
 struct KernelArgs {
+  float opsin[9];          // forward opsin matrix (XybMatrix::SPEC)
   int32_t width, height;
   int32_t xb, yb;          // blocks
   int32_t tiles_x, tiles_y;

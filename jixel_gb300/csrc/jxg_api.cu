@@ -1,4 +1,5 @@
-// C ABI of the GB300 VarDCT front end: context, buffers, launches, fetch.
+// C ABI of the GB300 VarDCT front end: contexts, passes (one frame or a
+// batch of frames), launches and result fetch.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -18,8 +19,14 @@ namespace jxg {
 namespace {
 
 constexpr uint64_t kMaxDimension = 0x3FFFFFFFull;  // MAX_DIMENSION, src/encode_image.rs:99
+constexpr size_t kHistBytes = static_cast<size_t>(kNumFineAcContexts) * kAlphabet * 4;
 
 struct DevBuf {
+  void* ptr = nullptr;
+  size_t cap = 0;
+};
+
+struct HostBuf {  // pinned host staging
   void* ptr = nullptr;
   size_t cap = 0;
 };
@@ -34,7 +41,26 @@ struct PendingEvent {
   cudaEvent_t start, stop;
 };
 
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
 }  // namespace
+
+// One image of a pass as the caller describes it.
+struct PassImage {
+  const void* pixels;
+  uint64_t width, height;
+  int32_t channels, bits;
+  jxg_config config;
+};
+
+// Where one frame of the last pass lives, for fetching its results.
+struct FrameLayout {
+  uint64_t width = 0, height = 0;
+  DistanceParams dp{};
+  jxg_frame_info info{};
+  int64_t plane = 0;
+  size_t pix_off = 0, xyb_off = 0, block_off = 0, tile_off = 0, group_off = 0, count_off = 0;
+};
 
 struct Context {
   int device = 0;
@@ -44,24 +70,40 @@ struct Context {
   // constant tables
   float* d_lut = nullptr;       // sRGB -> linear, 256
   float* d_exp2 = nullptr;      // fast_exp2 table, 64
-  uint8_t* d_scan = nullptr;    // natural 8x8 order, 64
-  uint8_t* d_pos = nullptr;     // its inverse, 64
-  // frame buffers
-  DevBuf pixels, xyb, qf, ytox, ytob, quant_dc, levels, wide_levels, coeffs, nzeros, nz_packed, counts,
-      offsets, chunks, tokens, hist, stats, group_offsets, op_in, op_out;
+  uint8_t* d_pos = nullptr;     // natural 8x8 order, raw index -> scan position
+  // pass buffers (grown, never shrunk)
+  DevBuf pixels, xyb, qf, ytox, ytob, quant_dc, levels, wide_levels, coeffs, nzeros, nz_packed,
+      counts, offsets, chunks, tokens, hist, stats, group_offsets, plan, total, op_in, op_out;
+  HostBuf plan_host, pixels_host;
+  // The plan (frame descriptors + chunk prefixes) lives in a ring of slots,
+  // pinned on the host and mirrored on the device, so a pass can be planned
+  // while earlier passes that were only enqueued still wait for their upload.
+  static constexpr int kPlanSlots = 4;
+  size_t plan_slot_cap = 0;
+  int plan_slot = 0;
+  cudaEvent_t plan_uploaded[kPlanSlots] = {};
   // last pass
+  std::vector<FrameLayout> layouts;
+  int64_t total_tiles = 0, xyb_chunks = 0, token_chunks = 0, total_counts = 0, total_groups = 0;
+  size_t frames_bytes = 0, pixel_bytes = 0;
   bool have_frame = false;
-  uint64_t width = 0, height = 0;
-  jxg_frame_info info{};
-  DistanceParams dp{};
-  KernelArgs args{};
-  int64_t plane = 0;
+  uint64_t epoch = 0;  // bumped by every plan: batches recorded earlier re-plan
   // timing
   bool timing = false;
   std::vector<PendingEvent> pending;
   std::vector<cudaEvent_t> spare_events;
   std::map<std::string, TimedKernel> times;
   std::vector<std::string> time_names;
+};
+
+struct Batch {
+  Context* ctx = nullptr;
+  bool on_device = false;
+  std::vector<PassImage> images;
+  bool planned = false;       // buffers sized and layout fixed for `images`
+  uint64_t epoch = 0;         // context epoch of that plan
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
 };
 
 namespace {
@@ -71,10 +113,10 @@ int fail(Context* c, int code, const std::string& msg) {
   return code;
 }
 
-#define JXG_CUDA(ctx, call)                                                              \
-  do {                                                                                   \
-    cudaError_t e_ = (call);                                                             \
-    if (e_ != cudaSuccess)                                                               \
+#define JXG_CUDA(ctx, call)                                                                    \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess)                                                                     \
       return ::jxg::fail(ctx, JXG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
@@ -94,6 +136,22 @@ int ensure(Context* c, DevBuf& b, size_t bytes) {
   return JXG_OK;
 }
 
+int ensure_host(Context* c, HostBuf& b, size_t bytes) {
+  if (bytes <= b.cap) return JXG_OK;
+  if (b.ptr) cudaFreeHost(b.ptr);
+  b.ptr = nullptr;
+  b.cap = 0;
+  size_t want = std::max<size_t>(bytes, 4096);
+  cudaError_t e = cudaMallocHost(&b.ptr, want);
+  if (e != cudaSuccess) {
+    b.ptr = nullptr;
+    return fail(c, JXG_ERR_ALLOCATION_FAILED,
+                "cudaMallocHost(" + std::to_string(want) + "): " + cudaGetErrorString(e));
+  }
+  b.cap = want;
+  return JXG_OK;
+}
+
 cudaEvent_t take_event(Context* c) {
   if (!c->spare_events.empty()) {
     cudaEvent_t e = c->spare_events.back();
@@ -107,9 +165,9 @@ cudaEvent_t take_event(Context* c) {
 
 // Launch wrapper: records start/stop events around the launch when timing.
 template <typename Launch>
-int launch(Context* c, const char* name, Launch&& fn) {
+int launch(Context* c, const char* name, bool timed, Launch&& fn) {
   cudaEvent_t s = nullptr, e = nullptr;
-  if (c->timing) {
+  if (timed) {
     s = take_event(c);
     e = take_event(c);
     cudaEventRecord(s, c->stream);
@@ -117,7 +175,7 @@ int launch(Context* c, const char* name, Launch&& fn) {
   fn();
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return fail(c, JXG_ERR_CUDA, std::string(name) + ": " + cudaGetErrorString(err));
-  if (c->timing) {
+  if (timed) {
     cudaEventRecord(e, c->stream);
     c->pending.push_back({name, s, e});
   }
@@ -150,12 +208,6 @@ void frame_info(uint64_t w, uint64_t h, jxg_frame_info* o) {
   o->num_groups = o->xsize_groups * o->ysize_groups;
   o->num_dc_groups = ((w + kDcGroupDim - 1) / kDcGroupDim) * ((h + kDcGroupDim - 1) / kDcGroupDim);
   o->max_tokens = o->xsize_blocks * o->ysize_blocks * 3 * 64;
-}
-
-int sm_count(int device) {
-  int n = 0;
-  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device);
-  return n > 0 ? n : 1;
 }
 
 void opsin_matrix(float m[9]) {
@@ -191,162 +243,287 @@ int validate(Context* c, const void* pixels, uint64_t w, uint64_t h, int32_t cha
   return JXG_OK;
 }
 
-// Enqueue the whole pass on the context's stream; `pixels` is device memory.
-int enqueue_frontend(Context* c, const void* pixels, uint64_t w, uint64_t h, int32_t channels,
-                     int32_t bits, const jxg_config* cfg) {
-  int st = validate(c, pixels, w, h, channels, bits, cfg);
-  if (st) return st;
-  DistanceParams dp;
-  if (compute_distance_params(cfg->distance, &dp))
-    return fail(c, JXG_ERR_INVALID_DISTANCE, "distance");
-  KernelArgs& a = c->args;
-  std::memset(&a, 0, sizeof(a));
-  dct8_tables(dp.distance, a.matrix, a.inv_matrix);
-  fill_kernel_args(dp, &a);
-  jxg_frame_info& fi = c->info;
-  frame_info(w, h, &fi);
-  a.width = static_cast<int32_t>(w);
-  a.height = static_cast<int32_t>(h);
-  a.xb = static_cast<int32_t>(fi.xsize_blocks);
-  a.yb = static_cast<int32_t>(fi.ysize_blocks);
-  a.tiles_x = static_cast<int32_t>(fi.xsize_tiles);
-  a.tiles_y = static_cast<int32_t>(fi.ysize_tiles);
-  a.groups_x = static_cast<int32_t>(fi.xsize_groups);
-  a.groups_y = static_cast<int32_t>(fi.ysize_groups);
-  const int64_t n = static_cast<int64_t>(w * h);
-  const int64_t plane = (n + 63) / 64 * 64;
-  a.plane = static_cast<int32_t>(plane);
-  c->plane = plane;
-  c->dp = dp;
-  c->width = w;
-  c->height = h;
-  const int64_t nb = static_cast<int64_t>(fi.xsize_blocks * fi.ysize_blocks);
-  const int64_t ntiles = static_cast<int64_t>(fi.xsize_tiles * fi.ysize_tiles);
-  const int64_t ncounts = static_cast<int64_t>(fi.num_groups) * 1024 * 4;
-  const int64_t nchunks = (ncounts + kScanChunk - 1) / kScanChunk;
-  if ((st = ensure(c, c->xyb, 3 * plane * sizeof(float))) ||
-      (st = ensure(c, c->qf, nb)) || (st = ensure(c, c->ytox, ntiles)) ||
-      (st = ensure(c, c->ytob, ntiles)) || (st = ensure(c, c->quant_dc, 3 * nb * 2)) ||
-      (st = ensure(c, c->levels, nb * 192 * 2)) || (st = ensure(c, c->wide_levels, nb * 192 * 4)) ||
-      (st = ensure(c, c->nzeros, 3 * nb)) || (st = ensure(c, c->nz_packed, 4 * nb)) ||
-      (st = ensure(c, c->counts, ncounts * 4)) || (st = ensure(c, c->offsets, ncounts * 4)) ||
+// Device buffers of 16-bit samples must be 2-byte aligned.
+int check_device_pixels(Context* c, const void* pixels, int32_t bits) {
+  if (bits == 16 && (reinterpret_cast<uintptr_t>(pixels) & 1))
+    return fail(c, JXG_ERR_INVALID_ARGUMENT, "16-bit device pixels must be 2-byte aligned");
+  return JXG_OK;
+}
+
+// Lays out a pass of `n` frames in the context's buffers, sizes them, and
+// fills the pinned plan (frame descriptors + chunk prefixes).  No launch.
+// `stage`: host pixels go through the context's pinned staging buffer (what
+// a recorded graph replays) instead of one copy per image from the caller.
+int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, bool stage) {
+  if (n <= 0) return fail(c, JXG_ERR_INVALID_ARGUMENT, "empty pass");
+  int st;
+  for (int i = 0; i < n; ++i)
+    if ((st = validate(c, imgs[i].pixels, imgs[i].width, imgs[i].height, imgs[i].channels,
+                       imgs[i].bits, &imgs[i].config)))
+      return st;
+  c->have_frame = false;
+  c->layouts.assign(n, FrameLayout{});
+  size_t pix = 0, xyb = 0, blocks = 0, tiles = 0, groups = 0, counts = 0, tokens = 0;
+  int64_t xyb_chunks = 0, token_chunks = 0;
+  for (int i = 0; i < n; ++i) {
+    FrameLayout& L = c->layouts[i];
+    const PassImage& im = imgs[i];
+    L.width = im.width;
+    L.height = im.height;
+    if (compute_distance_params(im.config.distance, &L.dp))
+      return fail(c, JXG_ERR_INVALID_DISTANCE, "distance");
+    frame_info(im.width, im.height, &L.info);
+    const int64_t px = static_cast<int64_t>(im.width * im.height);
+    L.plane = (px + 63) / 64 * 64;
+    L.pix_off = pix;
+    pix += align_up(static_cast<size_t>(px) * im.channels * (im.bits / 8), 256);
+    L.xyb_off = xyb;
+    xyb += 3 * static_cast<size_t>(L.plane);
+    L.block_off = blocks;
+    blocks += L.info.xsize_blocks * L.info.ysize_blocks;
+    L.tile_off = tiles;
+    tiles += L.info.xsize_tiles * L.info.ysize_tiles;
+    L.group_off = groups;
+    groups += L.info.num_groups;
+    L.count_off = counts;
+    counts += L.info.num_groups * 4096;
+    tokens += L.info.max_tokens;
+    if (tokens > 0xFFFFFFFFull)  // token offsets are 32-bit
+      return fail(c, JXG_ERR_DIMENSION_TOO_LARGE,
+                  "pass holds more than 2^32 possible tokens: split the batch");
+    xyb_chunks += (px + kXybChunk - 1) / kXybChunk;
+    token_chunks += (static_cast<int64_t>(L.info.xsize_blocks * L.info.ysize_blocks) +
+                     kTokenChunk - 1) / kTokenChunk;
+  }
+  c->total_tiles = static_cast<int64_t>(tiles);
+  c->xyb_chunks = xyb_chunks;
+  c->token_chunks = token_chunks;
+  c->total_counts = static_cast<int64_t>(counts);
+  c->total_groups = static_cast<int64_t>(groups);
+  c->epoch += 1;
+  {
+    const FrameLayout& last = c->layouts.back();
+    c->pixel_bytes = last.pix_off + static_cast<size_t>(last.width * last.height) *
+                                        imgs[n - 1].channels * (imgs[n - 1].bits / 8);
+  }
+  const int64_t nchunks = (c->total_counts + kScanChunk - 1) / kScanChunk;
+  c->frames_bytes = align_up(sizeof(Frame) * n, 256);
+  const size_t prefix_bytes = align_up(sizeof(int64_t) * (n + 1), 256);
+  const size_t plan_bytes = align_up(c->frames_bytes + 3 * prefix_bytes, 256);
+  if (plan_bytes > c->plan_slot_cap) {
+    // grow every slot; the stream drains first, so no queued upload reads them
+    JXG_CUDA(c, cudaStreamSynchronize(c->stream));
+    const size_t cap = std::max<size_t>(plan_bytes, 64 << 10);
+    if ((st = ensure(c, c->plan, cap * Context::kPlanSlots)) ||
+        (st = ensure_host(c, c->plan_host, cap * Context::kPlanSlots)))
+      return st;
+    c->plan_slot_cap = cap;
+  }
+  c->plan_slot = (c->plan_slot + 1) % Context::kPlanSlots;
+  // the slot's last upload must have left the host buffer before it is rewritten
+  JXG_CUDA(c, cudaEventSynchronize(c->plan_uploaded[c->plan_slot]));
+  char* plan_h = static_cast<char*>(c->plan_host.ptr) + c->plan_slot * c->plan_slot_cap;
+  if ((!pixels_on_device && (st = ensure(c, c->pixels, pix))) ||
+      (st = ensure(c, c->xyb, xyb * 4)) || (st = ensure(c, c->qf, blocks)) ||
+      (st = ensure(c, c->ytox, tiles)) || (st = ensure(c, c->ytob, tiles)) ||
+      (st = ensure(c, c->quant_dc, 3 * blocks * 2)) ||
+      (st = ensure(c, c->levels, blocks * 192 * 2)) ||
+      (st = ensure(c, c->wide_levels, blocks * 192 * 4)) ||
+      (st = ensure(c, c->nzeros, 3 * blocks)) || (st = ensure(c, c->nz_packed, 4 * blocks)) ||
+      (st = ensure(c, c->counts, counts * 4)) || (st = ensure(c, c->offsets, counts * 4)) ||
       (st = ensure(c, c->chunks, nchunks * 4)) ||
-      (st = ensure(c, c->tokens, fi.max_tokens * sizeof(uint2))) ||
-      (st = ensure(c, c->hist, (size_t)kNumFineAcContexts * kAlphabet * 4)) ||
-      (st = ensure(c, c->stats, sizeof(DeviceStats))) ||
-      (st = ensure(c, c->group_offsets, (fi.num_groups + 1) * 8)))
+      (st = ensure(c, c->tokens, tokens * sizeof(uint2))) ||
+      (st = ensure(c, c->hist, n * kHistBytes)) ||
+      (st = ensure(c, c->stats, n * sizeof(DeviceStats))) ||
+      (st = ensure(c, c->group_offsets, (groups + 1) * 8)) || (st = ensure(c, c->total, 256)) ||
+      (!pixels_on_device && stage && (st = ensure_host(c, c->pixels_host, pix))))
     return st;
+  // frame descriptors
+  Frame* frames = reinterpret_cast<Frame*>(plan_h);
+  std::memset(frames, 0, sizeof(Frame) * n);
+  float opsin[9];
+  opsin_matrix(opsin);
+  int64_t* pre_xyb = reinterpret_cast<int64_t*>(plan_h + c->frames_bytes);
+  int64_t* pre_tile = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(pre_xyb) + prefix_bytes);
+  int64_t* pre_tok = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(pre_tile) + prefix_bytes);
+  int64_t ax = 0, at = 0, ak = 0;
+  for (int i = 0; i < n; ++i) {
+    const FrameLayout& L = c->layouts[i];
+    const PassImage& im = imgs[i];
+    Frame& f = frames[i];
+    KernelArgs& a = f.a;
+    dct8_tables(L.dp.distance, a.matrix, a.inv_matrix);
+    fill_kernel_args(L.dp, &a);
+    std::memcpy(a.opsin, opsin, sizeof(opsin));
+    a.width = static_cast<int32_t>(L.width);
+    a.height = static_cast<int32_t>(L.height);
+    a.xb = static_cast<int32_t>(L.info.xsize_blocks);
+    a.yb = static_cast<int32_t>(L.info.ysize_blocks);
+    a.tiles_x = static_cast<int32_t>(L.info.xsize_tiles);
+    a.tiles_y = static_cast<int32_t>(L.info.ysize_tiles);
+    a.groups_x = static_cast<int32_t>(L.info.xsize_groups);
+    a.groups_y = static_cast<int32_t>(L.info.ysize_groups);
+    a.plane = static_cast<int32_t>(L.plane);
+    f.pixels = pixels_on_device ? im.pixels : static_cast<const char*>(c->pixels.ptr) + L.pix_off;
+    f.channels = im.channels;
+    f.bits = im.bits;
+    f.xyb = static_cast<float*>(c->xyb.ptr) + L.xyb_off;
+    f.qf = static_cast<uint8_t*>(c->qf.ptr) + L.block_off;
+    f.ytox = static_cast<int8_t*>(c->ytox.ptr) + L.tile_off;
+    f.ytob = static_cast<int8_t*>(c->ytob.ptr) + L.tile_off;
+    f.quant_dc = static_cast<int16_t*>(c->quant_dc.ptr) + 3 * L.block_off;
+    f.levels = static_cast<int16_t*>(c->levels.ptr) + 192 * L.block_off;
+    f.wide_levels = static_cast<int32_t*>(c->wide_levels.ptr) + 192 * L.block_off;
+    f.nzeros = static_cast<uint8_t*>(c->nzeros.ptr) + 3 * L.block_off;
+    f.nz_packed = static_cast<uint32_t*>(c->nz_packed.ptr) + L.block_off;
+    f.counts = static_cast<uint32_t*>(c->counts.ptr) + L.count_off;
+    f.offsets = static_cast<uint32_t*>(c->offsets.ptr) + L.count_off;
+    f.histograms = reinterpret_cast<uint32_t*>(static_cast<char*>(c->hist.ptr) + i * kHistBytes);
+    f.stats = static_cast<DeviceStats*>(c->stats.ptr) + i;
+    const int64_t px = static_cast<int64_t>(L.width * L.height);
+    const int64_t nb = static_cast<int64_t>(L.info.xsize_blocks * L.info.ysize_blocks);
+    pre_xyb[i] = ax;
+    pre_tile[i] = at;
+    pre_tok[i] = ak;
+    ax += (px + kXybChunk - 1) / kXybChunk;
+    at += static_cast<int64_t>(L.info.xsize_tiles * L.info.ysize_tiles);
+    ak += (nb + kTokenChunk - 1) / kTokenChunk;
+  }
+  pre_xyb[n] = ax;
+  pre_tile[n] = at;
+  pre_tok[n] = ak;
+  return JXG_OK;
+}
+
+// Enqueues a planned pass: uploads, clears, launches.  With `capturing` the
+// launches are recorded into a graph, so no per-kernel timing events.
+enum class PixelSource { kDevice, kStaged, kCaller };
+
+int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool capturing) {
   cudaStream_t s = c->stream;
-  JXG_CUDA(c, cudaMemsetAsync(c->stats.ptr, 0, sizeof(DeviceStats), s));
-  JXG_CUDA(c, cudaMemsetAsync(c->hist.ptr, 0, (size_t)kNumFineAcContexts * kAlphabet * 4, s));
-  JXG_CUDA(c, cudaMemsetAsync(c->counts.ptr, 0, ncounts * 4, s));
-  const int sms = sm_count(c->device);
-  float* xyb = static_cast<float*>(c->xyb.ptr);
-  DeviceStats* stats = static_cast<DeviceStats*>(c->stats.ptr);
-  // 1. linearise + XYB
-  XybArgs xa;
-  opsin_matrix(xa.opsin);
-  xa.pixels = n;
-  xa.plane = plane;
-  const bool fast_rgb8 = bits == 8 && channels == 3 &&
-                         (reinterpret_cast<uintptr_t>(pixels) & 3u) == 0;
-  if (fast_rgb8) {
-    const int64_t quads = n / 4;
-    const int grid = static_cast<int>(std::min<int64_t>((quads + 255) / 256 + 1, sms * 8));
-    st = launch(c, "k_xyb_rgb8", [&] {
-      k_xyb_rgb8<<<grid, 256, 0, s>>>(xa, static_cast<const uint8_t*>(pixels), c->d_lut, xyb);
-    });
+  const size_t prefix_bytes = align_up(sizeof(int64_t) * (n + 1), 256);
+  const size_t plan_bytes = c->frames_bytes + 3 * prefix_bytes;
+  const size_t slot_off = c->plan_slot * c->plan_slot_cap;
+  char* plan_d = static_cast<char*>(c->plan.ptr) + slot_off;
+  const char* plan_h = static_cast<const char*>(c->plan_host.ptr) + slot_off;
+  // one frame: its descriptor travels as a kernel parameter; a batch reads
+  // the uploaded descriptor table
+  const bool single = n == 1;
+  if (!single) {
+    JXG_CUDA(c, cudaMemcpyAsync(plan_d, plan_h, plan_bytes, cudaMemcpyHostToDevice, s));
+    // a recorded graph replays the upload itself; every batch run waits for it
+    if (!capturing) JXG_CUDA(c, cudaEventRecord(c->plan_uploaded[c->plan_slot], s));
+  }
+  const Frame& f0 = *reinterpret_cast<const Frame*>(plan_h);
+  if (src == PixelSource::kStaged)
+    JXG_CUDA(c, cudaMemcpyAsync(c->pixels.ptr, c->pixels_host.ptr, c->pixel_bytes,
+                                cudaMemcpyHostToDevice, s));
+  if (src == PixelSource::kCaller)
+    for (int i = 0; i < n; ++i) {
+      const FrameLayout& L = c->layouts[i];
+      const size_t bytes =
+          static_cast<size_t>(L.width * L.height) * imgs[i].channels * (imgs[i].bits / 8);
+      JXG_CUDA(c, cudaMemcpyAsync(static_cast<char*>(c->pixels.ptr) + L.pix_off, imgs[i].pixels,
+                                  bytes, cudaMemcpyHostToDevice, s));
+    }
+  JXG_CUDA(c, cudaMemsetAsync(c->stats.ptr, 0, n * sizeof(DeviceStats), s));
+  JXG_CUDA(c, cudaMemsetAsync(c->hist.ptr, 0, n * kHistBytes, s));
+  JXG_CUDA(c, cudaMemsetAsync(c->counts.ptr, 0, c->total_counts * 4, s));
+  const Frame* frames = reinterpret_cast<const Frame*>(plan_d);
+  const int64_t* pre_xyb = reinterpret_cast<const int64_t*>(plan_d + c->frames_bytes);
+  const int64_t* pre_tile = reinterpret_cast<const int64_t*>(reinterpret_cast<const char*>(pre_xyb) + prefix_bytes);
+  const int64_t* pre_tok = reinterpret_cast<const int64_t*>(reinterpret_cast<const char*>(pre_tile) + prefix_bytes);
+  const bool timed = c->timing && !capturing;
+  int st;
+  if (single) {
+    if ((st = launch(c, "k_xyb", timed, [&] {
+           k_xyb<<<static_cast<unsigned>(c->xyb_chunks), 256, 0, s>>>(f0, c->d_lut);
+         })) ||
+        (st = launch(c, "k_adaptive_quant", timed, [&] {
+           k_adaptive_quant<<<static_cast<unsigned>(c->total_tiles), 256, 0, s>>>(f0, c->d_exp2);
+         })) ||
+        (st = launch(c, "k_tile_quantize", timed, [&] {
+           k_tile_quantize<<<static_cast<unsigned>(c->total_tiles), kTileThreads, kTileSmemBytes, s>>>(
+               f0, c->d_pos);
+         })))
+      return st;
   } else {
-    const int grid = static_cast<int>(std::min<int64_t>((n + 255) / 256, sms * 8));
-    st = launch(c, "k_xyb_generic", [&] {
-      k_xyb_generic<<<grid, 256, 0, s>>>(xa, pixels, bits / 8, channels, c->d_lut, xyb);
-    });
-  }
-  if (st) return st;
-  // 3. adaptive quant field per DC group
-  {
-    dim3 grid(a.tiles_x, a.tiles_y);
-    st = launch(c, "k_adaptive_quant", [&] {
-      k_adaptive_quant<<<grid, 256, 0, s>>>(a, xyb, c->d_exp2, static_cast<uint8_t*>(c->qf.ptr),
-                                            stats);
-    });
-    if (st) return st;
-  }
-  // 4. CfL tiles + DCT8 quantisation
-  {
-    TileOutputs to;
-    to.ytox = static_cast<int8_t*>(c->ytox.ptr);
-    to.ytob = static_cast<int8_t*>(c->ytob.ptr);
-    to.qf = static_cast<const uint8_t*>(c->qf.ptr);
-    to.levels = static_cast<int16_t*>(c->levels.ptr);
-    to.wide_levels = static_cast<int32_t*>(c->wide_levels.ptr);
-    to.quant_dc = static_cast<int16_t*>(c->quant_dc.ptr);
-    to.nzeros = static_cast<uint8_t*>(c->nzeros.ptr);
-    to.nz_packed = static_cast<uint32_t*>(c->nz_packed.ptr);
-    to.token_counts = static_cast<uint32_t*>(c->counts.ptr);
-    to.stats = stats;
-    dim3 grid(a.tiles_x, a.tiles_y);
-    st = launch(c, "k_tile_quantize", [&] {
-      k_tile_quantize<<<grid, kTileThreads, kTileSmemBytes, s>>>(a, xyb, c->d_pos, to);
-    });
-    if (st) return st;
-  }
-  // 5. token offsets (+ qf threshold)
-  {
-    uint32_t* counts = static_cast<uint32_t*>(c->counts.ptr);
-    uint32_t* offs = static_cast<uint32_t*>(c->offsets.ptr);
-    uint32_t* chunks = static_cast<uint32_t*>(c->chunks.ptr);
-    uint64_t* goffs = static_cast<uint64_t*>(c->group_offsets.ptr);
-    const int ch = static_cast<int>(nchunks);
-    if ((st = launch(c, "k_scan_reduce", [&] {
-           k_scan_reduce<<<ch, kScanThreads, 0, s>>>(counts, ncounts, chunks);
+    if ((st = launch(c, "k_xyb_batch", timed, [&] {
+           k_xyb_batch<<<static_cast<unsigned>(c->xyb_chunks), 256, 0, s>>>(frames, pre_xyb, n,
+                                                                            c->d_lut);
          })) ||
-        (st = launch(c, "k_scan_chunks", [&] {
-           k_scan_chunks<<<1, kScanThreads, 0, s>>>(chunks, ch, stats, goffs,
-                                                     static_cast<int>(fi.num_groups));
+        (st = launch(c, "k_adaptive_quant_batch", timed, [&] {
+           k_adaptive_quant_batch<<<static_cast<unsigned>(c->total_tiles), 256, 0, s>>>(
+               frames, pre_tile, n, c->d_exp2);
          })) ||
-        (st = launch(c, "k_scan_apply", [&] {
-           k_scan_apply<<<ch, kScanThreads, 0, s>>>(counts, ncounts, chunks, offs, goffs, 4 * 1024);
+        (st = launch(c, "k_tile_quantize_batch", timed, [&] {
+           k_tile_quantize_batch<<<static_cast<unsigned>(c->total_tiles), kTileThreads,
+                                   kTileSmemBytes, s>>>(frames, pre_tile, n, c->d_pos);
          })))
       return st;
   }
-  // 6. tokens + histograms
-  {
-    TokenArgs ta;
-    ta.xb = a.xb;
-    ta.yb = a.yb;
-    ta.groups_x = a.groups_x;
-    ta.levels = static_cast<const int16_t*>(c->levels.ptr);
-    ta.wide_levels = static_cast<const int32_t*>(c->wide_levels.ptr);
-    ta.nz_packed = static_cast<const uint32_t*>(c->nz_packed.ptr);
-    ta.qf = static_cast<const uint8_t*>(c->qf.ptr);
-    ta.offsets = static_cast<const uint32_t*>(c->offsets.ptr);
-    ta.stats = stats;
-    ta.tokens = static_cast<uint2*>(c->tokens.ptr);
-    ta.histograms = static_cast<uint32_t*>(c->hist.ptr);
-    const int64_t warps = nb;
-    const int grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, sms * 16)));
-    st = launch(c, "k_tokenize", [&] { k_tokenize<<<grid, 256, 0, s>>>(ta); });
-    if (st) return st;
-  }
+  uint32_t* counts = static_cast<uint32_t*>(c->counts.ptr);
+  uint32_t* offs = static_cast<uint32_t*>(c->offsets.ptr);
+  uint32_t* chunks = static_cast<uint32_t*>(c->chunks.ptr);
+  uint64_t* goffs = static_cast<uint64_t*>(c->group_offsets.ptr);
+  const int64_t ncounts = c->total_counts;
+  const int nchunks = static_cast<int>((ncounts + kScanChunk - 1) / kScanChunk);
+  if ((st = launch(c, "k_scan_reduce", timed, [&] {
+         k_scan_reduce<<<nchunks, kScanThreads, 0, s>>>(counts, ncounts, chunks);
+       })) ||
+      (st = launch(c, "k_scan_chunks", timed, [&] {
+         k_scan_chunks<<<1, kScanThreads, 0, s>>>(chunks, nchunks, static_cast<uint32_t*>(c->total.ptr),
+                                                   goffs, static_cast<int>(c->total_groups));
+       })) ||
+      (st = launch(c, "k_scan_apply", timed, [&] {
+         k_scan_apply<<<nchunks, kScanThreads, 0, s>>>(counts, ncounts, chunks, offs, goffs, 4 * 1024);
+       })) ||
+      (st = single ? launch(c, "k_tokenize", timed, [&] {
+         k_tokenize<<<static_cast<unsigned>(c->token_chunks), 256, 0, s>>>(
+             f0, static_cast<uint2*>(c->tokens.ptr));
+       })
+                   : launch(c, "k_tokenize_batch", timed, [&] {
+         k_tokenize_batch<<<static_cast<unsigned>(c->token_chunks), 256, 0, s>>>(
+             frames, pre_tok, n, static_cast<uint2*>(c->tokens.ptr));
+       })))
+    return st;
   c->have_frame = true;
+  return JXG_OK;
+}
+
+int stage_host_pixels(Context* c, const PassImage* imgs, int n) {
+  for (int i = 0; i < n; ++i) {
+    const FrameLayout& L = c->layouts[i];
+    const size_t bytes = static_cast<size_t>(L.width * L.height) * imgs[i].channels * (imgs[i].bits / 8);
+    std::memcpy(static_cast<char*>(c->pixels_host.ptr) + L.pix_off, imgs[i].pixels, bytes);
+  }
   return JXG_OK;
 }
 
 int wait(Context* c) {
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return fail(c, JXG_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e));
-  if (c->timing) collect_times(c);
+  if (!c->pending.empty()) collect_times(c);
   return JXG_OK;
 }
 
-int read_params(Context* c, jxg_frame_params* out) {
+int read_params(Context* c, int index, jxg_frame_params* out) {
+  if (!c->have_frame || index < 0 || index >= static_cast<int>(c->layouts.size()))
+    return fail(c, JXG_ERR_INVALID_ARGUMENT, "no such frame in the last pass");
+  const FrameLayout& L = c->layouts[index];
   DeviceStats ds;
-  JXG_CUDA(c, cudaMemcpyAsync(&ds, c->stats.ptr, sizeof(ds), cudaMemcpyDeviceToHost, c->stream));
+  uint64_t goffs[2];
+  JXG_CUDA(c, cudaMemcpyAsync(&ds, static_cast<DeviceStats*>(c->stats.ptr) + index, sizeof(ds),
+                              cudaMemcpyDeviceToHost, c->stream));
+  JXG_CUDA(c, cudaMemcpyAsync(&goffs[0], static_cast<uint64_t*>(c->group_offsets.ptr) + L.group_off, 8,
+                              cudaMemcpyDeviceToHost, c->stream));
+  JXG_CUDA(c, cudaMemcpyAsync(&goffs[1],
+                              static_cast<uint64_t*>(c->group_offsets.ptr) + L.group_off + L.info.num_groups,
+                              8, cudaMemcpyDeviceToHost, c->stream));
   int st = wait(c);
   if (st) return st;
   std::memset(out, 0, sizeof(*out));
-  const DistanceParams& p = c->dp;
+  const DistanceParams& p = L.dp;
   out->distance = p.distance;
   out->global_scale = p.global_scale;
   out->quant_dc = p.quant_dc;
@@ -358,10 +535,65 @@ int read_params(Context* c, jxg_frame_params* out) {
   for (int i = 0; i < 3; ++i) out->dc_step[i] = p.dc_step[i];
   out->qf_threshold = ds.qf_threshold;
   out->constant_blocks = ds.constant_blocks;
-  bool screen = is_screen_content(ds.constant_blocks, c->width, c->height);
+  bool screen = is_screen_content(ds.constant_blocks, L.width, L.height);
   out->screen_content = screen;
   out->epf_sharpness = epf_sharpness_id(p.distance, screen);
-  out->num_tokens = ds.num_tokens;
+  out->num_tokens = goffs[1] - goffs[0];
+  return JXG_OK;
+}
+
+int fetch_frame(Context* c, int index, jxg_frontend_output* out) {
+  jxg_frame_params p;
+  int st = read_params(c, index, &p);
+  if (st) return st;
+  const FrameLayout& L = c->layouts[index];
+  const jxg_frame_info& fi = L.info;
+  const size_t nb = fi.xsize_blocks * fi.ysize_blocks;
+  const size_t nt = fi.xsize_tiles * fi.ysize_tiles;
+  cudaStream_t s = c->stream;
+  auto copy = [&](void* dst, const void* src, size_t bytes) -> int {
+    if (!dst || bytes == 0) return JXG_OK;
+    JXG_CUDA(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+    return JXG_OK;
+  };
+  if (out->tokens && out->token_capacity < p.num_tokens)
+    return fail(c, JXG_ERR_INVALID_ARGUMENT, "token buffer too small");
+  if (out->coefficients) {
+    if ((st = ensure(c, c->coeffs, nb * 192 * 4))) return st;
+    const int64_t count = static_cast<int64_t>(nb) * 192;
+    const int grid = static_cast<int>(std::min<int64_t>((count + 255) / 256, 4096));
+    st = launch(c, "k_levels_to_raw", c->timing, [&] {
+      k_levels_to_raw<<<grid, 256, 0, s>>>(static_cast<const int16_t*>(c->levels.ptr) + 192 * L.block_off,
+                                           static_cast<const int32_t*>(c->wide_levels.ptr) + 192 * L.block_off,
+                                           c->d_pos, count, static_cast<int32_t*>(c->coeffs.ptr));
+    });
+    if (st) return st;
+  }
+  uint64_t first = 0;
+  JXG_CUDA(c, cudaMemcpyAsync(&first, static_cast<uint64_t*>(c->group_offsets.ptr) + L.group_off, 8,
+                              cudaMemcpyDeviceToHost, s));
+  if ((st = wait(c))) return st;
+  if ((st = copy(out->quant_field, static_cast<uint8_t*>(c->qf.ptr) + L.block_off, nb)) ||
+      (st = copy(out->ytox_map, static_cast<int8_t*>(c->ytox.ptr) + L.tile_off, nt)) ||
+      (st = copy(out->ytob_map, static_cast<int8_t*>(c->ytob.ptr) + L.tile_off, nt)) ||
+      (st = copy(out->quant_dc, static_cast<int16_t*>(c->quant_dc.ptr) + 3 * L.block_off, 3 * nb * 2)) ||
+      (st = copy(out->coefficients, c->coeffs.ptr, nb * 192 * 4)) ||
+      (st = copy(out->num_nzeros, static_cast<uint8_t*>(c->nzeros.ptr) + 3 * L.block_off, 3 * nb)) ||
+      (st = copy(out->tokens, static_cast<uint2*>(c->tokens.ptr) + first, p.num_tokens * sizeof(jxg_token))) ||
+      (st = copy(out->group_offsets, static_cast<uint64_t*>(c->group_offsets.ptr) + L.group_off,
+                 (fi.num_groups + 1) * 8)) ||
+      (st = copy(out->histograms, static_cast<char*>(c->hist.ptr) + index * kHistBytes, kHistBytes)))
+    return st;
+  if (out->xyb) {
+    const size_t px = L.width * L.height;
+    for (int ch = 0; ch < 3; ++ch)
+      if ((st = copy(out->xyb + ch * px, static_cast<float*>(c->xyb.ptr) + L.xyb_off + ch * L.plane, px * 4)))
+        return st;
+  }
+  if ((st = wait(c))) return st;
+  if (out->group_offsets)  // frame-local token offsets
+    for (uint64_t g = 0; g <= fi.num_groups; ++g) out->group_offsets[g] -= first;
+  if (out->ac_strategy) std::memset(out->ac_strategy, 1, nb);  // all DCT8, first blocks
   return JXG_OK;
 }
 
@@ -396,9 +628,21 @@ int noalloc_scratch(int device, NoAllocScanScratch** out) {
   return JXG_OK;
 }
 
+int single_pass(Context* c, const void* pixels, uint64_t w, uint64_t h, int32_t channels,
+                int32_t bits, const jxg_config* cfg, bool on_device) {
+  if (!cfg) return fail(c, JXG_ERR_INVALID_ARGUMENT, "null config");
+  PassImage im{pixels, w, h, channels, bits, *cfg};
+  int st = on_device ? check_device_pixels(c, pixels, bits) : JXG_OK;
+  if (st) return st;
+  st = plan_pass(c, &im, 1, on_device, false);
+  if (st) return st;
+  return enqueue_pass(c, &im, 1, on_device ? PixelSource::kDevice : PixelSource::kCaller, false);
+}
+
 }  // namespace
 }  // namespace jxg
 
+using jxg::Batch;
 using jxg::Context;
 
 extern "C" {
@@ -422,14 +666,19 @@ int32_t jxg_context_create(int32_t device, void** out_ctx) {
   jxg::srgb_to_linear_table(lut);
   jxg::exp2_table(e2);
   jxg::natural_order_8x8(scan, pos);
-  bool ok = cudaMalloc(&c->d_lut, sizeof(lut)) == cudaSuccess &&
+  bool ok = true;
+  for (auto& e : c->plan_uploaded)
+    ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+  ok = ok && cudaMalloc(&c->d_lut, sizeof(lut)) == cudaSuccess &&
             cudaMalloc(&c->d_exp2, sizeof(e2)) == cudaSuccess &&
-            cudaMalloc(&c->d_scan, 64) == cudaSuccess && cudaMalloc(&c->d_pos, 64) == cudaSuccess &&
+            cudaMalloc(&c->d_pos, 64) == cudaSuccess &&
             cudaMemcpy(c->d_lut, lut, sizeof(lut), cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(c->d_exp2, e2, sizeof(e2), cudaMemcpyHostToDevice) == cudaSuccess &&
-            cudaMemcpy(c->d_scan, scan, 64, cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(c->d_pos, pos, 64, cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaFuncSetAttribute(jxg::k_tile_quantize, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(jxg::kTileSmemBytes)) == cudaSuccess &&
+            cudaFuncSetAttribute(jxg::k_tile_quantize_batch,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(jxg::kTileSmemBytes)) == cudaSuccess;
   if (!ok) {
     jxg_context_destroy(c);
@@ -444,20 +693,23 @@ void jxg_context_destroy(void* ctx) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  for (jxg::DevBuf* b : {&c->pixels, &c->xyb, &c->qf, &c->ytox, &c->ytob, &c->quant_dc, &c->coeffs,
-                         &c->levels, &c->wide_levels, &c->nz_packed,
-                         &c->nzeros, &c->counts, &c->offsets, &c->chunks, &c->tokens, &c->hist,
-                         &c->stats, &c->group_offsets, &c->op_in, &c->op_out})
+  for (jxg::DevBuf* b : {&c->pixels, &c->xyb, &c->qf, &c->ytox, &c->ytob, &c->quant_dc, &c->levels,
+                         &c->wide_levels, &c->coeffs, &c->nzeros, &c->nz_packed, &c->counts,
+                         &c->offsets, &c->chunks, &c->tokens, &c->hist, &c->stats,
+                         &c->group_offsets, &c->plan, &c->total, &c->op_in, &c->op_out})
     if (b->ptr) cudaFree(b->ptr);
+  for (jxg::HostBuf* b : {&c->plan_host, &c->pixels_host})
+    if (b->ptr) cudaFreeHost(b->ptr);
   cudaFree(c->d_lut);
   cudaFree(c->d_exp2);
-  cudaFree(c->d_scan);
   cudaFree(c->d_pos);
   for (auto& p : c->pending) {
     cudaEventDestroy(p.start);
     cudaEventDestroy(p.stop);
   }
   for (auto e : c->spare_events) cudaEventDestroy(e);
+  for (auto e : c->plan_uploaded)
+    if (e) cudaEventDestroy(e);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
 }
@@ -495,7 +747,7 @@ int32_t jxg_frontend_run_device(void* ctx, const void* pixels, uint64_t width, u
   Context* c = static_cast<Context*>(ctx);
   if (!c) return JXG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(c->device);
-  return jxg::enqueue_frontend(c, pixels, width, height, channels, bits, config);
+  return jxg::single_pass(c, pixels, width, height, channels, bits, config, true);
 }
 
 int32_t jxg_frontend_run(void* ctx, const void* pixels, uint64_t width, uint64_t height,
@@ -503,12 +755,7 @@ int32_t jxg_frontend_run(void* ctx, const void* pixels, uint64_t width, uint64_t
   Context* c = static_cast<Context*>(ctx);
   if (!c) return JXG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(c->device);
-  int st = jxg::validate(c, pixels, width, height, channels, bits, config);
-  if (st) return st;
-  const size_t bytes = static_cast<size_t>(width * height) * channels * (bits / 8);
-  if ((st = jxg::ensure(c, c->pixels, bytes))) return st;
-  JXG_CUDA(c, cudaMemcpyAsync(c->pixels.ptr, pixels, bytes, cudaMemcpyHostToDevice, c->stream));
-  st = jxg::enqueue_frontend(c, c->pixels.ptr, width, height, channels, bits, config);
+  int st = jxg::single_pass(c, pixels, width, height, channels, bits, config, false);
   if (st) return st;
   return jxg::wait(c);
 }
@@ -516,58 +763,15 @@ int32_t jxg_frontend_run(void* ctx, const void* pixels, uint64_t width, uint64_t
 int32_t jxg_frontend_params(void* ctx, jxg_frame_params* out) {
   Context* c = static_cast<Context*>(ctx);
   if (!c || !out) return JXG_ERR_INVALID_ARGUMENT;
-  if (!c->have_frame) return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "no front-end pass yet");
   cudaSetDevice(c->device);
-  return jxg::read_params(c, out);
+  return jxg::read_params(c, 0, out);
 }
 
 int32_t jxg_frontend_fetch(void* ctx, jxg_frontend_output* out) {
   Context* c = static_cast<Context*>(ctx);
   if (!c || !out) return JXG_ERR_INVALID_ARGUMENT;
-  if (!c->have_frame) return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "no front-end pass yet");
   cudaSetDevice(c->device);
-  jxg_frame_params p;
-  int st = jxg::read_params(c, &p);
-  if (st) return st;
-  const jxg_frame_info& fi = c->info;
-  const size_t nb = fi.xsize_blocks * fi.ysize_blocks;
-  const size_t nt = fi.xsize_tiles * fi.ysize_tiles;
-  cudaStream_t s = c->stream;
-  auto copy = [&](void* dst, const void* src, size_t bytes) -> int {
-    if (!dst || bytes == 0) return JXG_OK;
-    JXG_CUDA(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
-    return JXG_OK;
-  };
-  if (out->tokens && out->token_capacity < p.num_tokens)
-    return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "token buffer too small");
-  if (out->coefficients) {
-    if ((st = jxg::ensure(c, c->coeffs, nb * 192 * 4))) return st;
-    const int64_t count = static_cast<int64_t>(nb) * 192;
-    const int grid = static_cast<int>(std::min<int64_t>((count + 255) / 256, 4096));
-    st = jxg::launch(c, "k_levels_to_raw", [&] {
-      jxg::k_levels_to_raw<<<grid, 256, 0, s>>>(static_cast<const int16_t*>(c->levels.ptr),
-                                                static_cast<const int32_t*>(c->wide_levels.ptr),
-                                                c->d_pos, count, static_cast<int32_t*>(c->coeffs.ptr));
-    });
-    if (st) return st;
-  }
-  if ((st = copy(out->quant_field, c->qf.ptr, nb)) || (st = copy(out->ytox_map, c->ytox.ptr, nt)) ||
-      (st = copy(out->ytob_map, c->ytob.ptr, nt)) ||
-      (st = copy(out->quant_dc, c->quant_dc.ptr, 3 * nb * 2)) ||
-      (st = copy(out->coefficients, c->coeffs.ptr, nb * 192 * 4)) ||
-      (st = copy(out->num_nzeros, c->nzeros.ptr, 3 * nb)) ||
-      (st = copy(out->tokens, c->tokens.ptr, p.num_tokens * sizeof(jxg_token))) ||
-      (st = copy(out->group_offsets, c->group_offsets.ptr, (fi.num_groups + 1) * 8)) ||
-      (st = copy(out->histograms, c->hist.ptr, (size_t)jxg::kNumFineAcContexts * jxg::kAlphabet * 4)))
-    return st;
-  if (out->xyb) {
-    const size_t n = c->width * c->height;
-    for (int ch = 0; ch < 3; ++ch)
-      if ((st = copy(out->xyb + ch * n, static_cast<float*>(c->xyb.ptr) + ch * c->plane, n * 4)))
-        return st;
-  }
-  if (out->ac_strategy) std::memset(out->ac_strategy, 1, nb);  // all DCT8, first blocks
-  return jxg::wait(c);
+  return jxg::fetch_frame(c, 0, out);
 }
 
 int32_t jxg_frontend(void* ctx, const void* pixels, uint64_t width, uint64_t height,
@@ -578,6 +782,105 @@ int32_t jxg_frontend(void* ctx, const void* pixels, uint64_t width, uint64_t hei
   if (params && (st = jxg_frontend_params(ctx, params))) return st;
   if (out) return jxg_frontend_fetch(ctx, out);
   return JXG_OK;
+}
+
+int32_t jxg_batch_create(void* ctx, int32_t pixels_on_device, void** out_batch) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !out_batch) return JXG_ERR_INVALID_ARGUMENT;
+  Batch* b = new Batch();
+  b->ctx = c;
+  b->on_device = pixels_on_device != 0;
+  *out_batch = b;
+  return JXG_OK;
+}
+
+static void drop_graph(Batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  b->planned = false;
+}
+
+int64_t jxg_batch_add(void* batch, const void* pixels, uint64_t width, uint64_t height,
+                      int32_t channels, int32_t bits, const jxg_config* config) {
+  Batch* b = static_cast<Batch*>(batch);
+  if (!b || !config) return -JXG_ERR_INVALID_ARGUMENT;
+  int st = jxg::validate(b->ctx, pixels, width, height, channels, bits, config);
+  if (!st && b->on_device) st = jxg::check_device_pixels(b->ctx, pixels, bits);
+  if (st) return -st;
+  drop_graph(b);
+  b->images.push_back(jxg::PassImage{pixels, width, height, channels, bits, *config});
+  return static_cast<int64_t>(b->images.size()) - 1;
+}
+
+int32_t jxg_batch_run(void* batch, int32_t use_graph) {
+  Batch* b = static_cast<Batch*>(batch);
+  if (!b || b->images.empty()) return JXG_ERR_INVALID_ARGUMENT;
+  Context* c = b->ctx;
+  cudaSetDevice(c->device);
+  const int n = static_cast<int>(b->images.size());
+  int st;
+  if (!b->planned || b->epoch != c->epoch) {
+    drop_graph(b);
+    if ((st = jxg::plan_pass(c, b->images.data(), n, b->on_device, !b->on_device))) return st;
+    b->planned = true;
+    b->epoch = c->epoch;
+  }
+  using jxg::PixelSource;
+  if (!use_graph) {
+    // host pixels: one copy per image straight from the caller's buffers
+    const PixelSource src = b->on_device ? PixelSource::kDevice : PixelSource::kCaller;
+    if ((st = jxg::enqueue_pass(c, b->images.data(), n, src, false))) return st;
+    return jxg::wait(c);
+  }
+  // a graph replays fixed copies: host pixels go through the pinned staging buffer
+  if (!b->on_device) jxg::stage_host_pixels(c, b->images.data(), n);
+  if (!b->exec) {
+    // the pass is recorded once and replayed; its buffers stay fixed while
+    // the batch is unchanged
+    JXG_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    st = jxg::enqueue_pass(c, b->images.data(), n,
+                           b->on_device ? PixelSource::kDevice : PixelSource::kStaged, true);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (st) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (e != cudaSuccess) return jxg::fail(c, JXG_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+    b->graph = g;
+    JXG_CUDA(c, cudaGraphInstantiate(&b->exec, g, 0));
+  }
+  JXG_CUDA(c, cudaGraphLaunch(b->exec, c->stream));
+  c->have_frame = true;
+  return jxg::wait(c);
+}
+
+static bool batch_current(const Batch* b) {
+  return b->planned && b->epoch == b->ctx->epoch && b->ctx->have_frame;
+}
+
+int32_t jxg_batch_result(void* batch, uint64_t index, jxg_frame_params* params,
+                         jxg_frontend_output* out) {
+  Batch* b = static_cast<Batch*>(batch);
+  if (!b) return JXG_ERR_INVALID_ARGUMENT;
+  if (!batch_current(b))
+    return jxg::fail(b->ctx, JXG_ERR_INVALID_ARGUMENT, "the context ran another pass since this batch");
+  if (index >= b->images.size()) return jxg::fail(b->ctx, JXG_ERR_INVALID_ARGUMENT, "index");
+  cudaSetDevice(b->ctx->device);
+  int st;
+  if (params && (st = jxg::read_params(b->ctx, static_cast<int>(index), params))) return st;
+  if (out) return jxg::fetch_frame(b->ctx, static_cast<int>(index), out);
+  return JXG_OK;
+}
+
+void jxg_batch_destroy(void* batch) {
+  Batch* b = static_cast<Batch*>(batch);
+  if (!b) return;
+  cudaSetDevice(b->ctx->device);
+  drop_graph(b);
+  delete b;
 }
 
 int32_t jxg_op_fill_quant_field(void* ctx, const float* xyb, uint64_t width, uint64_t height,
@@ -592,8 +895,9 @@ int32_t jxg_op_fill_quant_field(void* ctx, const float* xyb, uint64_t width, uin
   jxg::DistanceParams dp;
   jxg::compute_distance_params(distance, &dp);
   dp.distance = distance;
-  jxg::KernelArgs a;
-  std::memset(&a, 0, sizeof(a));
+  jxg::Frame f;
+  std::memset(&f, 0, sizeof(f));
+  jxg::KernelArgs& a = f.a;
   jxg::fill_kernel_args(dp, &a);
   a.inv_scale = inv_scale;
   jxg_frame_info fi;
@@ -608,23 +912,27 @@ int32_t jxg_op_fill_quant_field(void* ctx, const float* xyb, uint64_t width, uin
   const int64_t plane = (n + 63) / 64 * 64;
   a.plane = static_cast<int32_t>(plane);
   const size_t nb = fi.xsize_blocks * fi.ysize_blocks;
+  const int64_t tiles = static_cast<int64_t>(fi.xsize_tiles * fi.ysize_tiles);
+  const size_t in_bytes = jxg::align_up(3 * plane * 4, 256);
+  const size_t out_bytes = jxg::align_up(nb, 256);
   int st;
-  if ((st = jxg::ensure(c, c->op_in, 3 * plane * 4)) || (st = jxg::ensure(c, c->op_out, nb)) ||
-      (st = jxg::ensure(c, c->stats, sizeof(jxg::DeviceStats))))
+  if ((st = jxg::ensure(c, c->op_in, in_bytes)) ||
+      (st = jxg::ensure(c, c->op_out, out_bytes + sizeof(jxg::DeviceStats))))
     return st;
+  char* in = static_cast<char*>(c->op_in.ptr);
+  char* outp = static_cast<char*>(c->op_out.ptr);
+  f.xyb = reinterpret_cast<float*>(in);
+  f.qf = reinterpret_cast<uint8_t*>(outp);
+  f.stats = reinterpret_cast<jxg::DeviceStats*>(outp + out_bytes);
   cudaStream_t s = c->stream;
   for (int ch = 0; ch < 3; ++ch)
-    JXG_CUDA(c, cudaMemcpyAsync(static_cast<float*>(c->op_in.ptr) + ch * plane, xyb + ch * n, n * 4,
-                                cudaMemcpyHostToDevice, s));
-  JXG_CUDA(c, cudaMemsetAsync(c->stats.ptr, 0, sizeof(jxg::DeviceStats), s));
-  dim3 grid(a.tiles_x, a.tiles_y);
-  st = jxg::launch(c, "k_adaptive_quant", [&] {
-    jxg::k_adaptive_quant<<<grid, 256, 0, s>>>(a, static_cast<float*>(c->op_in.ptr), c->d_exp2,
-                                               static_cast<uint8_t*>(c->op_out.ptr),
-                                               static_cast<jxg::DeviceStats*>(c->stats.ptr));
+    JXG_CUDA(c, cudaMemcpyAsync(f.xyb + ch * plane, xyb + ch * n, n * 4, cudaMemcpyHostToDevice, s));
+  JXG_CUDA(c, cudaMemsetAsync(f.stats, 0, sizeof(jxg::DeviceStats), s));
+  st = jxg::launch(c, "k_adaptive_quant", c->timing, [&] {
+    jxg::k_adaptive_quant<<<static_cast<unsigned>(tiles), 256, 0, s>>>(f, c->d_exp2);
   });
   if (st) return st;
-  JXG_CUDA(c, cudaMemcpyAsync(quant_field, c->op_out.ptr, nb, cudaMemcpyDeviceToHost, s));
+  JXG_CUDA(c, cudaMemcpyAsync(quant_field, f.qf, nb, cudaMemcpyDeviceToHost, s));
   return jxg::wait(c);
 }
 
@@ -639,7 +947,7 @@ int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coe
   cudaStream_t s = c->stream;
   JXG_CUDA(c, cudaMemcpyAsync(c->op_in.ptr, blocks, bytes, cudaMemcpyHostToDevice, s));
   const int grid = static_cast<int>((count + 31) / 32);
-  st = jxg::launch(c, "k_dct8x8_blocks", [&] {
+  st = jxg::launch(c, "k_dct8x8_blocks", c->timing, [&] {
     jxg::k_dct8x8_blocks<<<grid, 256, 0, s>>>(static_cast<const float*>(c->op_in.ptr),
                                               static_cast<int64_t>(count),
                                               static_cast<float*>(c->op_out.ptr));
@@ -662,12 +970,13 @@ int32_t jxg_token_offsets_noalloc(const uint32_t* counts, uint64_t num_groups, u
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
   const int64_t n = static_cast<int64_t>(num_groups) * 3 * 1024;
   const int chunks = static_cast<int>((n + jxg::kScanChunk - 1) / jxg::kScanChunk);
-  // the middle step reads the pass scalars: start them from zero
+  // the middle step writes the pass scalars: start them from zero
   if (cudaMemsetAsync(&scratch->stats, 0, sizeof(scratch->stats), s) != cudaSuccess)
     return JXG_ERR_CUDA;
   jxg::k_scan_reduce<<<chunks, jxg::kScanThreads, 0, s>>>(counts, n, scratch->chunk_sums);
-  jxg::k_scan_chunks<<<1, jxg::kScanThreads, 0, s>>>(scratch->chunk_sums, chunks, &scratch->stats,
-                                                     group_offsets, static_cast<int>(num_groups));
+  jxg::k_scan_chunks<<<1, jxg::kScanThreads, 0, s>>>(scratch->chunk_sums, chunks,
+                                                     &scratch->stats.num_tokens, group_offsets,
+                                                     static_cast<int>(num_groups));
   jxg::k_scan_apply<<<chunks, jxg::kScanThreads, 0, s>>>(counts, n, scratch->chunk_sums, offsets,
                                                          group_offsets, 3 * 1024);
   return cudaGetLastError() == cudaSuccess ? JXG_OK : JXG_ERR_CUDA;

@@ -14,7 +14,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def header_functions():
     src = open(os.path.join(ROOT, "include", "jxg.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int32_t|void|float|const char\*)\s+(jxg_\w+)\(", src, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int32_t|int64_t|void|float|const char\*)\s+(jxg_\w+)\(", src, re.M)))
 
 
 def test_library_exports_every_declared_symbol():
