@@ -70,6 +70,20 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(value: float, device=None) -> float:
+    """The largest `value` over all ranks (the slowest replica's time); the
+    value itself in a single-process run.  `device` is where the process
+    group's backend keeps its tensors (a CUDA device for NCCL, None for gloo)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
 
@@ -151,12 +165,13 @@ def algorithmic_bytes(kernel: str, w: int, h: int, tokens_per_frame: float) -> f
 
 
 def traffic_from_profiles(kernel: str) -> float | None:
-    """DRAM bytes per launch for a full-size frame from a committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", f"{kernel}_dram.txt")
+    """DRAM bytes per launch of `kernel` on one 3840x2160 frame, from the
+    committed ncu summary (the capture's own command is in its header)."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic_4k_q90.txt")
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.startswith("dram_bytes_per_full_frame_launch:"):
+        if line.startswith(kernel + ":"):
             return float(line.split(":", 1)[1])
     return None
 
@@ -267,10 +282,7 @@ def run_gpu(args):
     ktimes = ctx.kernel_times()
     ctx.enable_kernel_timing(False)
     elapsed_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    t = torch.tensor([elapsed_ms], device=dev, dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    max_ms = float(t.item())
+    max_ms = max_over_ranks(elapsed_ms, dev)
     mp_per_step = len(QUALITIES) * WIDTH * HEIGHT / 1e6
     value = world * args.steps * mp_per_step / (max_ms / 1000.0)
 
@@ -291,6 +303,19 @@ def run_gpu(args):
         "share_of_kernel_time": dom_ms / sum(v[0] for v in ktimes.values()),
     }
     launches = int(sum(v[1] for v in ktimes.values()))
+    # the whole front end per frame: input bytes + 4 B per token + block side
+    # data (qf, strategy, 3 DC levels: 0.125 B/px) + CfL maps (2 B per 4096
+    # px) + one histogram set (14850 x 128 x 4 B), over the frame's summed
+    # kernel time
+    px = WIDTH * HEIGHT
+    fe_bytes = (3 * px + 4 * float(np.mean(tokens)) + 0.125 * px + 2 * px / 4096
+                + L.NUM_FINE_AC_CONTEXTS * L.ALPHABET_SIZE * 4)
+    fe_ms = sum(v[0] for v in ktimes.values()) / (args.steps * len(QUALITIES))
+    roofline["frontend"] = {
+        "algorithmic_bytes_per_frame": fe_bytes, "kernel_ms_per_frame": fe_ms,
+        "achieved": fe_bytes / (fe_ms / 1000.0) / 1e9,
+        "frac": fe_bytes / (fe_ms / 1000.0) / 1e9 / peaks["hbm_gbs"],
+    }
 
     batch = None
     if not args.no_batch:
@@ -368,10 +393,7 @@ def run_batch(ctx, stream, flush, args, world, dev) -> dict:
             e.record(stream)
             torch.cuda.synchronize(dev)
             total += s.elapsed_time(e)
-        t = torch.tensor([total], device=dev, dtype=torch.float64)
-        if world > 1:
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return max_over_ranks(total, dev)
 
     plain_ms = timed(plain_step)
     ctx.enable_kernel_timing(True)
@@ -388,9 +410,9 @@ def run_batch(ctx, stream, flush, args, world, dev) -> dict:
                     "q90, UltraFast gates",
         "megapixels_per_step": mp, "unit": "MP/s",
         "plain": {"value": plain, "ms_per_step": plain_ms / args.steps,
-                  "launches_per_step": 8 * len(imgs)},
+                  "launches_per_step": 7 * len(imgs)},
         "batched": {"value": batched, "ms_per_step": batched_ms / args.steps,
-                    "launches_per_step": 8, "cuda_graph": True},
+                    "launches_per_step": 7, "cuda_graph": True},
         "batched_over_plain": batched / plain,
         "batched_kernels_ms": {k: v[0] for k, v in sorted(ktimes.items())},
     }
@@ -451,10 +473,7 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
         step()
     torch.cuda.synchronize(dev)
     dt = time.perf_counter() - t0
-    t = torch.tensor([dt], device=dev, dtype=torch.float64)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    dt = float(t.item())
+    dt = max_over_ranks(dt, dev)
     value = world * args.steps * len(QUALITIES) * WIDTH * HEIGHT / 1e6 / dt
     return {"value": value, "unit": "MP/s", "h2d_bytes_per_step": len(QUALITIES) * img.size,
             "d2h_bytes_per_step": int(d2h[0]),
