@@ -114,6 +114,8 @@ typedef struct jxg_frontend_output {
   uint64_t token_capacity; /* entries available in `tokens` */
   uint64_t* group_offsets; /* num_groups + 1 token offsets */
   uint32_t* histograms;    /* JXG_NUM_FINE_AC_CONTEXTS * JXG_ALPHABET_SIZE */
+  uint16_t* alpha;         /* RGBA input: w*h alpha after fringe clearing (the
+                              plane the extra channel codes); untouched for RGB */
 } jxg_frontend_output;
 
 /* Library lifetime ---------------------------------------------------- */
@@ -148,9 +150,13 @@ int32_t jxg_validate_input(uint64_t width, uint64_t height, int32_t channels, in
  * src/group.rs:1259), with the tokens' per-context histograms
  * (build_histograms_with, src/entropy/write.rs:840).
  *
- * `pixels`: interleaved samples, `channels` 3 (RGB) or 4 (RGBA, alpha not
- * read), `bits` 8 (sRGB, as encode_image) or 16 (linear, as
- * encode_image_16bit with a linear transfer). */
+ * `pixels`: interleaved samples, `channels` 3 (RGB) or 4 (RGBA, as
+ * encode_image_with_alpha / _16bit with their defaults: lossy alpha, so the
+ * near-transparent fringe is cleared (src/alpha_fringe.rs:78), zero-alpha
+ * colours are filled from their neighbours (src/invisible.rs:34) and a
+ * non-constant alpha scales each block's quant field by its peak alpha
+ * (src/adaptive_quant.rs:953-1070)), `bits` 8 (sRGB, as encode_image) or
+ * 16 (linear, as encode_image_16bit with a linear transfer). */
 
 /* Host input: copies the pixels in, runs, and waits for the device. */
 int32_t jxg_frontend_run(void* ctx, const void* pixels, uint64_t width, uint64_t height,
@@ -239,6 +245,15 @@ int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coe
 #define JXG_NOALLOC_MAX_GROUPS 10922
 int32_t jxg_token_offsets_noalloc(const uint32_t* counts, uint64_t num_groups, uint32_t* offsets,
                                   uint64_t* group_offsets, void* cuda_stream);
+
+/* Bounded device waits ---------------------------------------------------
+ * The invisible-colour fill lets a warp wait for neighbouring tiles that
+ * other warps fill; every such wait polls at most a fixed number of times
+ * and, when that runs out, records JXG_ERR_DEVICE_TIMEOUT for the frame
+ * instead of spinning on.  This entry point runs the same wait on a flag
+ * that is never set, for `polls` polls, and returns JXG_ERR_DEVICE_TIMEOUT:
+ * the error path, exercised without faulting or hanging the device. */
+int32_t jxg_selftest_bounded_wait(void* ctx, uint32_t polls);
 
 /* Kernel timing -------------------------------------------------------- */
 /* With `enable`, every launch of this context is bracketed by CUDA events on

@@ -33,6 +33,7 @@ EXPORTS = [
     "jxg_op_fill_quant_field",
     "jxg_op_dct8x8",
     "jxg_token_offsets_noalloc",
+    "jxg_selftest_bounded_wait",
     "jxg_enable_kernel_timing",
     "jxg_kernel_times",
     "jxg_reset_kernel_times",
@@ -92,6 +93,7 @@ class FrontendOutput(ctypes.Structure):
         ("token_capacity", ctypes.c_uint64),
         ("group_offsets", ctypes.c_void_p),
         ("histograms", ctypes.c_void_p),
+        ("alpha", ctypes.c_void_p),
     ]
 
 
@@ -132,6 +134,7 @@ def load() -> ctypes.CDLL:
         "jxg_op_fill_quant_field": (i32, [vp, vp, u64, u64, f32, f32, vp]),
         "jxg_op_dct8x8": (i32, [vp, vp, u64, vp]),
         "jxg_token_offsets_noalloc": (i32, [vp, u64, vp, vp, vp]),
+        "jxg_selftest_bounded_wait": (i32, [vp, ctypes.c_uint32]),
         "jxg_enable_kernel_timing": (i32, [vp, i32]),
         "jxg_kernel_times": (i32, [vp, ctypes.POINTER(ctypes.c_char_p),
                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(u64), i32]),

@@ -131,6 +131,7 @@ class FrontendResult:
     group_offsets: np.ndarray  # (groups + 1,) u64
     histograms: np.ndarray    # (14850, 128) u32
     xyb: np.ndarray | None = None
+    alpha: np.ndarray | None = None  # (h, w) u16 alpha after fringe clearing (RGBA input)
 
 
 def _pixels_kind(pixels: np.ndarray) -> tuple[int, int]:
@@ -150,7 +151,8 @@ def _params_dict(p) -> dict:
     return out
 
 
-def _result_buffers(p: dict, width: int, height: int, coefficients: bool, xyb: bool):
+def _result_buffers(p: dict, width: int, height: int, coefficients: bool, xyb: bool,
+                    alpha: bool = False):
     """Host arrays for every output of one frame and the C struct pointing at them."""
     fi = frame_info(width, height)
     xb, yb = fi.xsize_blocks, fi.ysize_blocks
@@ -167,6 +169,7 @@ def _result_buffers(p: dict, width: int, height: int, coefficients: bool, xyb: b
         group_offsets=np.zeros(fi.num_groups + 1, np.uint64),
         histograms=np.zeros((L.NUM_FINE_AC_CONTEXTS, L.ALPHABET_SIZE), np.uint32),
         xyb=np.zeros((3, height, width), np.float32) if xyb else None,
+        alpha=np.zeros((height, width), np.uint16) if alpha else None,
     )
     o = L.FrontendOutput()
     o.quant_field = r.quant_field.ctypes.data
@@ -181,6 +184,7 @@ def _result_buffers(p: dict, width: int, height: int, coefficients: bool, xyb: b
     o.token_capacity = r.tokens.shape[0]
     o.group_offsets = r.group_offsets.ctypes.data
     o.histograms = r.histograms.ctypes.data
+    o.alpha = r.alpha.ctypes.data if alpha else None
     return r, o
 
 
@@ -241,9 +245,9 @@ class FrontendContext:
         return _params_dict(p)
 
     def fetch(self, width: int, height: int, *, coefficients: bool = True,
-              xyb: bool = False) -> FrontendResult:
+              xyb: bool = False, alpha: bool = False) -> FrontendResult:
         p = self.params()
-        r, o = _result_buffers(p, width, height, coefficients, xyb)
+        r, o = _result_buffers(p, width, height, coefficients, xyb, alpha)
         self._check(self._lib.jxg_frontend_fetch(self._ctx, ctypes.byref(o)))
         r.tokens = r.tokens[: int(p["num_tokens"])]
         return r
@@ -255,7 +259,8 @@ class FrontendContext:
     def frontend(self, pixels: np.ndarray, config: EncodeConfig, *, coefficients: bool = True,
                  xyb: bool = False) -> FrontendResult:
         self.run(pixels, config)
-        return self.fetch(pixels.shape[1], pixels.shape[0], coefficients=coefficients, xyb=xyb)
+        return self.fetch(pixels.shape[1], pixels.shape[0], coefficients=coefficients, xyb=xyb,
+                          alpha=pixels.shape[2] == 4)
 
     # operator table -----------------------------------------------------
     def fill_quant_field(self, xyb: np.ndarray, distance: float, inv_scale: float) -> np.ndarray:
@@ -340,7 +345,7 @@ class FrontendBatch:
         if idx < 0:
             self._check(-idx)
         self._keep.append(keep)
-        self._sizes.append((w, h))
+        self._sizes.append((w, h, ch))
         return idx
 
     def run(self, use_graph: bool = True):
@@ -352,9 +357,9 @@ class FrontendBatch:
         return _params_dict(p)
 
     def result(self, index: int, *, coefficients: bool = True, xyb: bool = False) -> FrontendResult:
-        w, h = self._sizes[index]
+        w, h, ch = self._sizes[index]
         p = self.params(index)
-        r, o = _result_buffers(p, w, h, coefficients, xyb)
+        r, o = _result_buffers(p, w, h, coefficients, xyb, ch == 4)
         self._check(self._lib.jxg_batch_result(self._b, index, None, ctypes.byref(o)))
         r.tokens = r.tokens[: int(p["num_tokens"])]
         return r

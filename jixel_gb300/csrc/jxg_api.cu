@@ -43,6 +43,17 @@ struct PendingEvent {
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// Work prefixes in a plan: XYB chunks, tiles, token chunks, RGBA tiles,
+// invisible-fill tiles.
+constexpr int kPlanPrefixes = 5;
+
+// Invisible-fill tiles of a w x h frame (32-row bands of sheared 32-column
+// tiles, as the fill kernel walks them).
+inline int64_t fill_tiles(uint64_t w, uint64_t h) {
+  return static_cast<int64_t>((h + kFillBand - 1) / kFillBand) *
+         static_cast<int64_t>((w + kFillBand - 1 + kFillCols - 1) / kFillCols);
+}
+
 }  // namespace
 
 // One image of a pass as the caller describes it.
@@ -60,6 +71,8 @@ struct FrameLayout {
   jxg_frame_info info{};
   int64_t plane = 0;
   size_t pix_off = 0, xyb_off = 0, block_off = 0, tile_off = 0, group_off = 0, count_off = 0;
+  bool has_alpha = false;
+  size_t alpha_off = 0, alpha_block_off = 0;  // RGBA frames only
 };
 
 struct Context {
@@ -73,7 +86,8 @@ struct Context {
   uint8_t* d_pos = nullptr;     // natural 8x8 order, raw index -> scan position
   // pass buffers (grown, never shrunk)
   DevBuf pixels, xyb, qf, ytox, ytob, quant_dc, levels, wide_levels, coeffs, nzeros, nz_packed,
-      counts, offsets, chunks, tokens, hist, stats, group_offsets, plan, total, op_in, op_out;
+      counts, offsets, chunks, tokens, hist, stats, group_offsets, plan, total, op_in, op_out,
+      alpha, alpha_peak, fill_done;
   HostBuf plan_host, pixels_host;
   // The plan (frame descriptors + chunk prefixes) lives in a ring of slots,
   // pinned on the host and mirrored on the device, so a pass can be planned
@@ -85,6 +99,9 @@ struct Context {
   // last pass
   std::vector<FrameLayout> layouts;
   int64_t total_tiles = 0, xyb_chunks = 0, token_chunks = 0, total_counts = 0, total_groups = 0;
+  int64_t alpha_tiles = 0;  // 64x64 tiles of the pass's RGBA frames
+  int64_t fill_tiles = 0;   // invisible-fill tiles of the pass's RGBA frames
+  int num_sms = 0;
   size_t frames_bytes = 0, pixel_bytes = 0;
   bool have_frame = false;
   uint64_t epoch = 0;  // bumped by every plan: batches recorded earlier re-plan
@@ -264,7 +281,8 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
   c->have_frame = false;
   c->layouts.assign(n, FrameLayout{});
   size_t pix = 0, xyb = 0, blocks = 0, tiles = 0, groups = 0, counts = 0, tokens = 0;
-  int64_t xyb_chunks = 0, token_chunks = 0;
+  size_t alpha_px = 0, alpha_blocks = 0;
+  int64_t xyb_chunks = 0, token_chunks = 0, alpha_tiles = 0, fill_total = 0;
   for (int i = 0; i < n; ++i) {
     FrameLayout& L = c->layouts[i];
     const PassImage& im = imgs[i];
@@ -287,6 +305,15 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     groups += L.info.num_groups;
     L.count_off = counts;
     counts += L.info.num_groups * 4096;
+    L.has_alpha = im.channels == 4;
+    if (L.has_alpha) {
+      L.alpha_off = alpha_px;
+      alpha_px += align_up(static_cast<size_t>(px), 128);
+      L.alpha_block_off = alpha_blocks;
+      alpha_blocks += align_up(L.info.xsize_blocks * L.info.ysize_blocks, 128);
+      alpha_tiles += static_cast<int64_t>(L.info.xsize_tiles * L.info.ysize_tiles);
+      fill_total += fill_tiles(L.width, L.height);
+    }
     tokens += L.info.max_tokens;
     if (tokens > 0xFFFFFFFFull)  // token offsets are 32-bit
       return fail(c, JXG_ERR_DIMENSION_TOO_LARGE,
@@ -300,6 +327,8 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
   c->token_chunks = token_chunks;
   c->total_counts = static_cast<int64_t>(counts);
   c->total_groups = static_cast<int64_t>(groups);
+  c->alpha_tiles = alpha_tiles;
+  c->fill_tiles = fill_total;
   c->epoch += 1;
   {
     const FrameLayout& last = c->layouts.back();
@@ -309,7 +338,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
   const int64_t nchunks = (c->total_counts + kScanChunk - 1) / kScanChunk;
   c->frames_bytes = align_up(sizeof(Frame) * n, 256);
   const size_t prefix_bytes = align_up(sizeof(int64_t) * (n + 1), 256);
-  const size_t plan_bytes = align_up(c->frames_bytes + 3 * prefix_bytes, 256);
+  const size_t plan_bytes = align_up(c->frames_bytes + kPlanPrefixes * prefix_bytes, 256);
   if (plan_bytes > c->plan_slot_cap) {
     // grow every slot; the stream drains first, so no queued upload reads them
     JXG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -336,6 +365,9 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
       (st = ensure(c, c->hist, n * kHistBytes)) ||
       (st = ensure(c, c->stats, n * sizeof(DeviceStats))) ||
       (st = ensure(c, c->group_offsets, (groups + 1) * 8)) || (st = ensure(c, c->total, 256)) ||
+      (alpha_px && (st = ensure(c, c->alpha, alpha_px * 2))) ||
+      (alpha_blocks && (st = ensure(c, c->alpha_peak, alpha_blocks * 2))) ||
+      (fill_total && (st = ensure(c, c->fill_done, fill_total * 4))) ||
       (!pixels_on_device && stage && (st = ensure_host(c, c->pixels_host, pix))))
     return st;
   // frame descriptors
@@ -346,7 +378,9 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
   int64_t* pre_xyb = reinterpret_cast<int64_t*>(plan_h + c->frames_bytes);
   int64_t* pre_tile = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(pre_xyb) + prefix_bytes);
   int64_t* pre_tok = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(pre_tile) + prefix_bytes);
-  int64_t ax = 0, at = 0, ak = 0;
+  int64_t* pre_alpha = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(pre_tok) + prefix_bytes);
+  int64_t* pre_fill = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(pre_alpha) + prefix_bytes);
+  int64_t ax = 0, at = 0, ak = 0, aa = 0, af = 0;
   for (int i = 0; i < n; ++i) {
     const FrameLayout& L = c->layouts[i];
     const PassImage& im = imgs[i];
@@ -380,11 +414,22 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     f.offsets = static_cast<uint32_t*>(c->offsets.ptr) + L.count_off;
     f.histograms = reinterpret_cast<uint32_t*>(static_cast<char*>(c->hist.ptr) + i * kHistBytes);
     f.stats = static_cast<DeviceStats*>(c->stats.ptr) + i;
+    if (L.has_alpha) {
+      f.alpha = static_cast<uint16_t*>(c->alpha.ptr) + L.alpha_off;
+      f.alpha_peak = static_cast<uint16_t*>(c->alpha_peak.ptr) + L.alpha_block_off;
+      f.alpha_full = im.bits == 8 ? 255 : 65535;
+    }
     const int64_t px = static_cast<int64_t>(L.width * L.height);
     const int64_t nb = static_cast<int64_t>(L.info.xsize_blocks * L.info.ysize_blocks);
     pre_xyb[i] = ax;
     pre_tile[i] = at;
     pre_tok[i] = ak;
+    pre_alpha[i] = aa;
+    pre_fill[i] = af;
+    if (L.has_alpha) {
+      aa += static_cast<int64_t>(L.info.xsize_tiles * L.info.ysize_tiles);
+      af += fill_tiles(L.width, L.height);
+    }
     ax += (px + kXybChunk - 1) / kXybChunk;
     at += static_cast<int64_t>(L.info.xsize_tiles * L.info.ysize_tiles);
     ak += (nb + kTokenChunk - 1) / kTokenChunk;
@@ -392,6 +437,8 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
   pre_xyb[n] = ax;
   pre_tile[n] = at;
   pre_tok[n] = ak;
+  pre_alpha[n] = aa;
+  pre_fill[n] = af;
   return JXG_OK;
 }
 
@@ -402,7 +449,7 @@ enum class PixelSource { kDevice, kStaged, kCaller };
 int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool capturing) {
   cudaStream_t s = c->stream;
   const size_t prefix_bytes = align_up(sizeof(int64_t) * (n + 1), 256);
-  const size_t plan_bytes = c->frames_bytes + 3 * prefix_bytes;
+  const size_t plan_bytes = c->frames_bytes + kPlanPrefixes * prefix_bytes;
   const size_t slot_off = c->plan_slot * c->plan_slot_cap;
   char* plan_d = static_cast<char*>(c->plan.ptr) + slot_off;
   const char* plan_h = static_cast<const char*>(c->plan_host.ptr) + slot_off;
@@ -433,13 +480,37 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
   const int64_t* pre_xyb = reinterpret_cast<const int64_t*>(plan_d + c->frames_bytes);
   const int64_t* pre_tile = reinterpret_cast<const int64_t*>(reinterpret_cast<const char*>(pre_xyb) + prefix_bytes);
   const int64_t* pre_tok = reinterpret_cast<const int64_t*>(reinterpret_cast<const char*>(pre_tile) + prefix_bytes);
+  const int64_t* pre_alpha = reinterpret_cast<const int64_t*>(reinterpret_cast<const char*>(pre_tok) + prefix_bytes);
+  const int64_t* pre_fill = reinterpret_cast<const int64_t*>(reinterpret_cast<const char*>(pre_alpha) + prefix_bytes);
+  // the fill's tile queue and per-tile completion flags start from zero
+  uint32_t* fill_queue = reinterpret_cast<uint32_t*>(static_cast<char*>(c->total.ptr) + 64);
+  const unsigned fill_grid = static_cast<unsigned>(std::max<int64_t>(
+      1, std::min<int64_t>((c->fill_tiles + kFillThreads / 32 - 1) / (kFillThreads / 32),
+                           static_cast<int64_t>(c->num_sms) * 3)));
+  if (c->fill_tiles) {
+    JXG_CUDA(c, cudaMemsetAsync(c->fill_done.ptr, 0, c->fill_tiles * 4, s));
+    JXG_CUDA(c, cudaMemsetAsync(fill_queue, 0, 4, s));
+  }
   const bool timed = c->timing && !capturing;
   int st;
   if (single) {
     if ((st = launch(c, "k_xyb", timed, [&] {
            k_xyb<<<static_cast<unsigned>(c->xyb_chunks), 256, 0, s>>>(f0, c->d_lut);
+         })))
+      return st;
+    if (c->alpha_tiles &&
+        ((st = launch(c, "k_alpha_count", timed, [&] {
+           k_alpha_count<<<static_cast<unsigned>(c->alpha_tiles), 256, 0, s>>>(f0);
          })) ||
-        (st = launch(c, "k_adaptive_quant", timed, [&] {
+         (st = launch(c, "k_alpha_final", timed, [&] {
+           k_alpha_final<<<static_cast<unsigned>(c->alpha_tiles), 256, 0, s>>>(f0);
+         })) ||
+         (st = launch(c, "k_fill_invisible", timed, [&] {
+           k_fill_invisible<<<fill_grid, kFillThreads, kFillSmemBytes, s>>>(
+               f0, fill_queue, static_cast<uint32_t*>(c->fill_done.ptr), c->fill_tiles);
+         }))))
+      return st;
+    if ((st = launch(c, "k_adaptive_quant", timed, [&] {
            k_adaptive_quant<<<static_cast<unsigned>(c->total_tiles), 256, 0, s>>>(f0, c->d_exp2);
          })) ||
         (st = launch(c, "k_tile_quantize", timed, [&] {
@@ -451,8 +522,24 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
     if ((st = launch(c, "k_xyb_batch", timed, [&] {
            k_xyb_batch<<<static_cast<unsigned>(c->xyb_chunks), 256, 0, s>>>(frames, pre_xyb, n,
                                                                             c->d_lut);
+         })))
+      return st;
+    if (c->alpha_tiles &&
+        ((st = launch(c, "k_alpha_count_batch", timed, [&] {
+           k_alpha_count_batch<<<static_cast<unsigned>(c->alpha_tiles), 256, 0, s>>>(
+               frames, pre_alpha, n);
          })) ||
-        (st = launch(c, "k_adaptive_quant_batch", timed, [&] {
+         (st = launch(c, "k_alpha_final_batch", timed, [&] {
+           k_alpha_final_batch<<<static_cast<unsigned>(c->alpha_tiles), 256, 0, s>>>(
+               frames, pre_alpha, n);
+         })) ||
+         (st = launch(c, "k_fill_invisible_batch", timed, [&] {
+           k_fill_invisible_batch<<<fill_grid, kFillThreads, kFillSmemBytes, s>>>(
+               frames, pre_fill, n, fill_queue, static_cast<uint32_t*>(c->fill_done.ptr),
+               c->fill_tiles);
+         }))))
+      return st;
+    if ((st = launch(c, "k_adaptive_quant_batch", timed, [&] {
            k_adaptive_quant_batch<<<static_cast<unsigned>(c->total_tiles), 256, 0, s>>>(
                frames, pre_tile, n, c->d_exp2);
          })) ||
@@ -522,6 +609,8 @@ int read_params(Context* c, int index, jxg_frame_params* out) {
                               8, cudaMemcpyDeviceToHost, c->stream));
   int st = wait(c);
   if (st) return st;
+  if (ds.flags & kFlagFillTimeout)
+    return fail(c, JXG_ERR_DEVICE_TIMEOUT, "a bounded device wait of the invisible fill ran out");
   std::memset(out, 0, sizeof(*out));
   const DistanceParams& p = L.dp;
   out->distance = p.distance;
@@ -583,6 +672,10 @@ int fetch_frame(Context* c, int index, jxg_frontend_output* out) {
       (st = copy(out->group_offsets, static_cast<uint64_t*>(c->group_offsets.ptr) + L.group_off,
                  (fi.num_groups + 1) * 8)) ||
       (st = copy(out->histograms, static_cast<char*>(c->hist.ptr) + index * kHistBytes, kHistBytes)))
+    return st;
+  if (out->alpha && L.has_alpha &&
+      (st = copy(out->alpha, static_cast<uint16_t*>(c->alpha.ptr) + L.alpha_off,
+                 L.width * L.height * 2)))
     return st;
   if (out->xyb) {
     const size_t px = L.width * L.height;
@@ -661,6 +754,9 @@ int32_t jxg_context_create(int32_t device, void** out_ctx) {
     return JXG_ERR_CUDA;
   }
   c->stream = c->own_stream;
+  if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      c->num_sms <= 0)
+    c->num_sms = 1;
   float lut[256], e2[64];
   uint8_t scan[64], pos[64];
   jxg::srgb_to_linear_table(lut);
@@ -679,7 +775,12 @@ int32_t jxg_context_create(int32_t device, void** out_ctx) {
                                  static_cast<int>(jxg::kTileSmemBytes)) == cudaSuccess &&
             cudaFuncSetAttribute(jxg::k_tile_quantize_batch,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(jxg::kTileSmemBytes)) == cudaSuccess;
+                                 static_cast<int>(jxg::kTileSmemBytes)) == cudaSuccess &&
+            cudaFuncSetAttribute(jxg::k_fill_invisible, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(jxg::kFillSmemBytes)) == cudaSuccess &&
+            cudaFuncSetAttribute(jxg::k_fill_invisible_batch,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(jxg::kFillSmemBytes)) == cudaSuccess;
   if (!ok) {
     jxg_context_destroy(c);
     return JXG_ERR_CUDA;
@@ -696,7 +797,8 @@ void jxg_context_destroy(void* ctx) {
   for (jxg::DevBuf* b : {&c->pixels, &c->xyb, &c->qf, &c->ytox, &c->ytob, &c->quant_dc, &c->levels,
                          &c->wide_levels, &c->coeffs, &c->nzeros, &c->nz_packed, &c->counts,
                          &c->offsets, &c->chunks, &c->tokens, &c->hist, &c->stats,
-                         &c->group_offsets, &c->plan, &c->total, &c->op_in, &c->op_out})
+                         &c->group_offsets, &c->plan, &c->total, &c->op_in, &c->op_out,
+                         &c->alpha, &c->alpha_peak, &c->fill_done})
     if (b->ptr) cudaFree(b->ptr);
   for (jxg::HostBuf* b : {&c->plan_host, &c->pixels_host})
     if (b->ptr) cudaFreeHost(b->ptr);
@@ -980,6 +1082,24 @@ int32_t jxg_token_offsets_noalloc(const uint32_t* counts, uint64_t num_groups, u
   jxg::k_scan_apply<<<chunks, jxg::kScanThreads, 0, s>>>(counts, n, scratch->chunk_sums, offsets,
                                                          group_offsets, 3 * 1024);
   return cudaGetLastError() == cudaSuccess ? JXG_OK : JXG_ERR_CUDA;
+}
+
+int32_t jxg_selftest_bounded_wait(void* ctx, uint32_t polls) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c) return JXG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(c->device);
+  int st;
+  if ((st = jxg::ensure(c, c->op_out, 256))) return st;
+  uint32_t* flag = static_cast<uint32_t*>(c->op_out.ptr);  // never set
+  uint32_t* result = flag + 1;
+  JXG_CUDA(c, cudaMemsetAsync(flag, 0, 8, c->stream));
+  jxg::k_wait_selftest<<<1, 32, 0, c->stream>>>(flag, polls, result);
+  JXG_CUDA(c, cudaGetLastError());
+  uint32_t r = 0;
+  JXG_CUDA(c, cudaMemcpyAsync(&r, result, 4, cudaMemcpyDeviceToHost, c->stream));
+  if ((st = jxg::wait(c))) return st;
+  if (r == 2u) return jxg::fail(c, JXG_ERR_DEVICE_TIMEOUT, "bounded wait ran out (self-test)");
+  return r == 1u ? JXG_OK : JXG_ERR_CUDA;
 }
 
 int32_t jxg_enable_kernel_timing(void* ctx, int32_t enable) {

@@ -89,13 +89,27 @@ def generate(width: int, height: int, seed: int, *, noise_sigma: float = 6.0,
     else:
         out = np.rint(img).astype(np.uint8)
     if alpha:
+        # smooth radial ramp, minus fully transparent discs covering ~10 % of
+        # the area (disc radii 2 px .. 6 % of the short side)
         r = np.hypot((xx - width / 2) / max(width, 1), (yy - height / 2) / max(height, 1))
         a = np.clip(1.0 - r * 1.4, 0, 1)
-        holes = max(1, (width * height) // 20000)
-        for _ in range(holes):
+        hole = np.zeros((height, width), bool)
+        target = 0.10 * width * height
+        covered = 0
+        for _ in range(10000):
+            if covered >= target:
+                break
             hx, hy = rng.uniform(0, width), rng.uniform(0, height)
-            rad = rng.uniform(2, max(3.0, 0.08 * min(width, height)))
-            a[(xx - hx) ** 2 + (yy - hy) ** 2 <= rad * rad] = 0.0
+            rad = rng.uniform(2, max(3.0, 0.06 * min(width, height)))
+            x0, x1 = int(max(hx - rad, 0)), int(min(hx + rad + 1, width))
+            y0, y1 = int(max(hy - rad, 0)), int(min(hy + rad + 1, height))
+            if x0 >= x1 or y0 >= y1:
+                continue
+            sub = (xx[:, x0:x1] - hx) ** 2 + (yy[y0:y1, :] - hy) ** 2 <= rad * rad
+            view = hole[y0:y1, x0:x1]
+            covered += int(np.count_nonzero(sub & ~view))
+            view |= sub
+        a[hole] = 0.0
         amax = 65535 if sixteen_bit else 255
         a_ch = (a * amax).astype(out.dtype)[..., None]
         out = np.concatenate([out, a_ch], axis=2)

@@ -1071,6 +1071,184 @@ static uint32_t qf_threshold_of(const uint8_t* qf, size_t n) {
 }
 
 /* ------------------------------------------------------------------ */
+/* Alpha: fringe clearing, invisible fill, AQ factors                   */
+/* ------------------------------------------------------------------ */
+
+/* Fringe level of a sample for one sweep of alpha_fringe::sweep
+ * (src/alpha_fringe.rs:121-124): its distance from one end of the range
+ * (`invert` = from full opacity), kept when within REACH levels, else 0. */
+static inline uint32_t fringe_level(uint32_t a, uint32_t maxv, int invert) {
+  uint32_t reach = 4u * maxv / 255u;
+  uint32_t level = invert ? maxv - (a < maxv ? a : maxv) : a;
+  return level <= reach ? level : 0u;
+}
+
+/* alpha_fringe::sweep (src/alpha_fringe.rs:112-223): a sample with a
+ * non-zero fringe level is replaced when the fringe levels over the 9x9
+ * window around it (clipped to the plane, original samples) average at most
+ * half a level: sum * 2 * 255 <= window_samples * max.  The reference slides
+ * the window row by row and defers replacements until a row leaves it; here
+ * the window sums come from a summed-area table of the original levels,
+ * which gives the same sums.  Marks go to `mark` (1 = replace); returns the
+ * number marked. */
+static size_t fringe_marks(const uint16_t* alpha, size_t w, size_t h, uint32_t maxv, int invert,
+                           uint8_t* mark) {
+  uint64_t* sat = (uint64_t*)calloc((w + 1) * (h + 1), sizeof(uint64_t));
+  for (size_t y = 0; y < h; y++) {
+    uint64_t row = 0;
+    for (size_t x = 0; x < w; x++) {
+      row += fringe_level(alpha[y * w + x], maxv, invert);
+      sat[(y + 1) * (w + 1) + x + 1] = sat[y * (w + 1) + x + 1] + row;
+    }
+  }
+  size_t marked = 0;
+  for (size_t y = 0; y < h; y++) {
+    size_t y0 = y >= 4 ? y - 4 : 0, y1 = minz(y + 5, h);
+    for (size_t x = 0; x < w; x++) {
+      mark[y * w + x] = 0;
+      if (fringe_level(alpha[y * w + x], maxv, invert) == 0) continue;
+      size_t x0 = x >= 4 ? x - 4 : 0, x1 = minz(x + 5, w);
+      uint64_t sum = sat[y1 * (w + 1) + x1] - sat[y0 * (w + 1) + x1] - sat[y1 * (w + 1) + x0] +
+                     sat[y0 * (w + 1) + x0];
+      if (sum * 2u * 255u <= (uint64_t)((y1 - y0) * (x1 - x0)) * maxv) {
+        mark[y * w + x] = 1;
+        marked++;
+      }
+    }
+  }
+  free(sat);
+  return marked;
+}
+
+/* alpha_fringe::clear (src/alpha_fringe.rs:78-108), in place: clear the
+ * near-transparent fringe to 0, then, when at least one sample in 12 sits
+ * within REACH below full opacity and the second sweep would change at
+ * least one in 12, fill those to full opacity. */
+void orc_alpha_fringe_clear(uint16_t* alpha, size_t w, size_t h, uint32_t maxv) {
+  if (w == 0 || h == 0) return;
+  size_t n = w * h;
+  uint8_t* mark = (uint8_t*)malloc(n);
+  fringe_marks(alpha, w, h, maxv, 0, mark);
+  for (size_t i = 0; i < n; i++)
+    if (mark[i]) alpha[i] = 0;
+  uint32_t reach = 4u * maxv / 255u;
+  size_t near_opaque = 0;
+  for (size_t i = 0; i < n; i++) {
+    uint32_t d = maxv - (alpha[i] < maxv ? alpha[i] : maxv);
+    if (d >= 1 && d <= reach) near_opaque++;
+  }
+  if (near_opaque * 12 >= n) {
+    size_t changed = fringe_marks(alpha, w, h, maxv, 1, mark);
+    if (changed * 12 >= n)
+      for (size_t i = 0; i < n; i++)
+        if (mark[i]) alpha[i] = (uint16_t)maxv;
+  }
+  free(mark);
+}
+
+/* invisible::fill_invisible (src/invisible.rs:34-149) on one plane: every
+ * zero-alpha sample, in raster order and in place, becomes the weighted
+ * mean of its left (weight 1, +1 when visible), upper-right (1, +2 when
+ * visible), and visible right, up, down and lower-right (2 each) neighbours,
+ * summed in that order. */
+static void fill_invisible_plane(float* p, const uint16_t* alpha, size_t w, size_t h) {
+  for (size_t y = 0; y < h; y++) {
+    int up = y > 0, down = y + 1 < h;
+    const float* pu = up ? p + (y - 1) * w : p + y * w;
+    const float* pd = down ? p + (y + 1) * w : p + y * w;
+    const uint16_t* au = up ? alpha + (y - 1) * w : alpha + y * w;
+    const uint16_t* ad = down ? alpha + (y + 1) * w : alpha + y * w;
+    float* row = p + y * w;
+    const uint16_t* ar = alpha + y * w;
+    for (size_t x = 0; x < w; x++) {
+      if (ar[x] != 0) continue;
+      float sum = 0.0f, weight = 0.0f;
+      if (x > 0) {
+        sum += row[x - 1];
+        weight += 1.0f;
+        if (ar[x - 1] != 0) {
+          sum += row[x - 1];
+          weight += 1.0f;
+        }
+      }
+      if (x + 1 < w) {
+        if (up) {
+          sum += pu[x + 1];
+          weight += 1.0f;
+        }
+        if (ar[x + 1] != 0) {
+          sum += 2.0f * row[x + 1];
+          weight += 2.0f;
+        }
+        if (up && au[x + 1] != 0) {
+          sum += 2.0f * pu[x + 1];
+          weight += 2.0f;
+        }
+        if (down && ad[x + 1] != 0) {
+          sum += 2.0f * pd[x + 1];
+          weight += 2.0f;
+        }
+      }
+      if (up && au[x] != 0) {
+        sum += 2.0f * pu[x];
+        weight += 2.0f;
+      }
+      if (down && ad[x] != 0) {
+        sum += 2.0f * pd[x];
+        weight += 2.0f;
+      }
+      row[x] = weight > 1.0f ? sum / weight : sum;
+    }
+  }
+}
+
+void orc_fill_invisible(float* xyb, const uint16_t* alpha, size_t w, size_t h) {
+  size_t n = w * h;
+  int any = 0;
+  for (size_t i = 0; i < n && !any; i++) any = alpha[i] == 0;
+  if (!any) return; /* src/invisible.rs:45-47 */
+  for (int c = 0; c < 3; c++) fill_invisible_plane(xyb + c * n, alpha, w, h);
+}
+
+/* alpha_block_factors (src/adaptive_quant.rs:953-1028): per 8x8 block, the
+ * largest alpha over the block, normalised by the full-opacity value; 1 for
+ * fully transparent or fully opaque blocks, else at least ALPHA_AQ_FLOOR
+ * (0.1). */
+void orc_alpha_block_factors(const uint16_t* alpha, size_t w, size_t h, uint32_t maxv,
+                             float* factors) {
+  size_t xb = (w + 7) / 8, yb = (h + 7) / 8;
+  for (size_t by = 0; by < yb; by++)
+    for (size_t bx = 0; bx < xb; bx++) {
+      uint32_t peak = 0;
+      for (size_t y = by * 8; y < minz(by * 8 + 8, h); y++)
+        for (size_t x = bx * 8; x < minz(bx * 8 + 8, w); x++)
+          if (alpha[y * w + x] > peak) peak = alpha[y * w + x];
+      float a = (float)peak / (float)maxv;
+      factors[by * xb + bx] = (a == 0.0f || a >= 1.0f) ? 1.0f : (a > 0.1f ? a : 0.1f);
+    }
+}
+
+/* apply_alpha_factors (src/adaptive_quant.rs:1036-1070) for an all-DCT8
+ * layout: each block's raw field value times its factor, rounded half away
+ * and clamped to 1..255.  Skipped for a constant alpha plane
+ * (src/frame/encoder.rs:60-70). */
+void orc_apply_alpha_factors(uint8_t* qf, const uint16_t* alpha, size_t w, size_t h,
+                             uint32_t maxv) {
+  size_t n = w * h;
+  int constant = 1;
+  for (size_t i = 1; i < n && constant; i++) constant = alpha[i] == alpha[0];
+  if (constant) return;
+  size_t xb = (w + 7) / 8, yb = (h + 7) / 8;
+  float* k = (float*)malloc(xb * yb * sizeof(float));
+  orc_alpha_block_factors(alpha, w, h, maxv, k);
+  for (size_t i = 0; i < xb * yb; i++) {
+    int32_t q = sat_i32(roundf((float)qf[i] * k[i]));
+    qf[i] = (uint8_t)(q < 1 ? 1 : (q > 255 ? 255 : q));
+  }
+  free(k);
+}
+
+/* ------------------------------------------------------------------ */
 /* Whole front end                                                      */
 /* ------------------------------------------------------------------ */
 
@@ -1078,7 +1256,7 @@ typedef struct {
   /* inputs */
   const void* pixels;
   int32_t bytes_per_sample; /* 1 = sRGB 8-bit, 2 = 16-bit linear */
-  int32_t channels;         /* 3 or 4 (alpha ignored) */
+  int32_t channels;         /* 3 or 4 (RGBA: lossy alpha, fill_invisible on) */
   uint64_t width, height;
   float distance;
   int32_t num_threads;
@@ -1094,6 +1272,7 @@ typedef struct {
   uint64_t token_capacity;
   uint64_t* group_offsets; /* num_groups + 1 */
   uint32_t* histograms;    /* NUM_FINE_AC_CONTEXTS * 128 */
+  uint16_t* alpha;         /* w * h: the alpha plane after fringe clearing (RGBA only) */
   /* scalar outputs */
   orc_params params;
   uint32_t qf_threshold;
@@ -1253,6 +1432,20 @@ int orc_frontend(orc_frame* f) {
   if (!xyb || !qf || !ytox || !ytob || !qdc) return ORC_ERR_ALLOC;
   double t0 = now_seconds();
   orc_to_xyb(f->pixels, f->bytes_per_sample, f->channels, w, h, xyb);
+  /* RGBA (encode_lossy_u8_alpha_arms, src/encode_image.rs:3639-3657, and
+   * encode_high_depth_rgba :4290-4303): the alpha plane loses its fringe,
+   * then the XYB planes their invisible colours (src/frame/encoder.rs:152) */
+  uint16_t* alpha = NULL;
+  uint32_t alpha_max = f->bytes_per_sample == 1 ? 255u : 65535u;
+  if (f->channels == 4) {
+    alpha = f->alpha ? f->alpha : (uint16_t*)malloc(n * sizeof(uint16_t));
+    if (!alpha) return ORC_ERR_ALLOC;
+    for (size_t i = 0; i < n; i++)
+      alpha[i] = f->bytes_per_sample == 1 ? ((const uint8_t*)f->pixels)[i * 4 + 3]
+                                          : ((const uint16_t*)f->pixels)[i * 4 + 3];
+    orc_alpha_fringe_clear(alpha, w, h, alpha_max);
+    orc_fill_invisible(xyb, alpha, w, h);
+  }
   f->constant_blocks = orc_constant_blocks(xyb, w, h);
   f->screen_content = orc_is_screen_content(f->constant_blocks, w, h);
   f->epf_sharpness = orc_epf_sharpness_id(f->params.distance, f->screen_content);
@@ -1269,6 +1462,8 @@ int orc_frontend(orc_frame* f) {
     size_t gxb = (gxs + 7) / 8, gyb = (gys + 7) / 8;
     fill_quant_field(xyb, w, h, x0, y0, gxb, gyb, f->params.distance, inv_scale, qf, xb);
   }
+  /* the alpha factors come last in setup_dc_group (src/frame/dc_groups.rs:303-312) */
+  if (alpha) orc_apply_alpha_factors(qf, alpha, w, h, alpha_max);
   double t2 = now_seconds();
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic) num_threads(threads)
@@ -1339,6 +1534,7 @@ int orc_frontend(orc_frame* f) {
   free(gts);
   if (!f->histograms) free(hist);
   if (!f->xyb) free(xyb);
+  if (alpha && !f->alpha) free(alpha);
   if (!f->quant_field) free(qf);
   if (!f->ytox) free(ytox);
   if (!f->ytob) free(ytob);

@@ -56,6 +56,7 @@ class OrcFrame(ctypes.Structure):
         ("token_capacity", ctypes.c_uint64),
         ("group_offsets", ctypes.c_void_p),
         ("histograms", ctypes.c_void_p),
+        ("alpha", ctypes.c_void_p),
         ("params", OrcParams),
         ("qf_threshold", ctypes.c_uint32),
         ("constant_blocks", ctypes.c_uint64),
@@ -168,6 +169,7 @@ class OracleFrame:
     tokens: np.ndarray          # (N, 2) uint32: context, value
     group_offsets: np.ndarray
     histograms: np.ndarray      # (contexts, 128) uint32
+    alpha: np.ndarray | None    # (h, w) uint16 alpha after fringe clearing (RGBA only)
     qf_threshold: int
     constant_blocks: int
     screen_content: bool
@@ -195,6 +197,7 @@ def frontend(pixels: np.ndarray, distance: float, num_threads: int = 0,
     tokens = np.zeros((cap, 2), np.uint32)
     offs = np.zeros(ng + 1, np.uint64)
     hist = np.zeros((NUM_FINE_AC_CONTEXTS, ALPHABET), np.uint32)
+    alpha = np.zeros((h, w), np.uint16) if ch == 4 else None
     f = OrcFrame()
     f.pixels = pixels.ctypes.data
     f.bytes_per_sample = bps
@@ -214,6 +217,7 @@ def frontend(pixels: np.ndarray, distance: float, num_threads: int = 0,
     f.token_capacity = cap
     f.group_offsets = offs.ctypes.data
     f.histograms = hist.ctypes.data
+    f.alpha = alpha.ctypes.data if alpha is not None else None
     st = lib().orc_frontend(ctypes.byref(f))
     if st:
         raise ValueError(f"oracle frontend status {st}")
@@ -225,8 +229,38 @@ def frontend(pixels: np.ndarray, distance: float, num_threads: int = 0,
                 "b_qm_scale": p.b_qm_scale, "epf_iters": p.epf_iters,
                 "dc_step": list(p.dc_step)},
         xyb=xyb, quant_field=qf, ytox=ytox, ytob=ytob, quant_dc=qdc, coeffs=coeffs,
-        nzeros=nz, tokens=tokens[: f.num_tokens], group_offsets=offs, histograms=hist,
+        nzeros=nz, tokens=tokens[: f.num_tokens], group_offsets=offs, histograms=hist, alpha=alpha,
         qf_threshold=f.qf_threshold, constant_blocks=f.constant_blocks,
         screen_content=bool(f.screen_content), epf_sharpness=f.epf_sharpness,
         stage_seconds=list(f.stage_seconds),
     )
+
+
+def alpha_fringe_clear(alpha: np.ndarray, maxv: int) -> np.ndarray:
+    """alpha_fringe::clear on a copy of an (h, w) integer alpha plane."""
+    a = np.ascontiguousarray(alpha, np.uint16).copy()
+    h, w = a.shape
+    lib().orc_alpha_fringe_clear(a.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(w),
+                                 ctypes.c_size_t(h), ctypes.c_uint32(maxv))
+    return a
+
+
+def fill_invisible(xyb: np.ndarray, alpha: np.ndarray) -> np.ndarray:
+    """invisible::fill_invisible on a copy of (3, h, w) float planes."""
+    x = np.ascontiguousarray(xyb, np.float32).copy()
+    a = np.ascontiguousarray(alpha, np.uint16)
+    _, h, w = x.shape
+    lib().orc_fill_invisible(x.ctypes.data_as(ctypes.c_void_p), a.ctypes.data_as(ctypes.c_void_p),
+                             ctypes.c_size_t(w), ctypes.c_size_t(h))
+    return x
+
+
+def alpha_block_factors(alpha: np.ndarray, maxv: int) -> np.ndarray:
+    """alpha_block_factors of an (h, w) integer alpha plane: (yb, xb) float32."""
+    a = np.ascontiguousarray(alpha, np.uint16)
+    h, w = a.shape
+    out = np.zeros(((h + 7) // 8, (w + 7) // 8), np.float32)
+    lib().orc_alpha_block_factors(a.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(w),
+                                  ctypes.c_size_t(h), ctypes.c_uint32(maxv),
+                                  out.ctypes.data_as(ctypes.c_void_p))
+    return out

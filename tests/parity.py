@@ -26,3 +26,5 @@ def assert_same(got, want, check_xyb=True):
     assert np.array_equal(got.tokens, want.tokens), "tokens"
     assert np.array_equal(got.histograms, want.histograms), "histograms"
     assert np.all(got.ac_strategy == 1)
+    if getattr(want, "alpha", None) is not None and getattr(got, "alpha", None) is not None:
+        assert np.array_equal(got.alpha, want.alpha), "alpha"

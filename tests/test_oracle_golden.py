@@ -142,3 +142,85 @@ def test_low_distance_uses_library_table():
     assert abs(m[0, 0] - 1 / 3150) < 1e-9 and abs(m[1, 0] - 1 / 560) < 1e-8
     assert abs(m[2, 0] - 1 / 512) < 1e-8
     assert np.all(inv[:, 0] == 0) and np.allclose(inv[:, 1:] * m[:, 1:], 1, rtol=1e-6)
+
+
+# --- alpha: the reference's own known-answer tests, restated on the oracle ---
+
+def test_alpha_fringe_clears_thin_edges_and_keeps_shadow_tails():
+    # src/alpha_fringe.rs:233-262
+    w, h = 64, 64
+    a = np.zeros((h, w), np.uint16)
+    a[:, 0:20] = 255
+    a[:, 20] = 3
+    a[20:51, 40:64] = 2
+    got = O.alpha_fringe_clear(a, 255)
+    assert np.all(got[:, 20] == 0)
+    assert got[35, 52] == 2
+    assert got[35, 10] == 255
+    deep = O.alpha_fringe_clear(a.astype(np.uint32) * 257, 65535)
+    assert np.array_equal(deep, got.astype(np.uint32) * 257)
+
+
+def test_alpha_fringe_fills_dithered_backdrop_only_when_broad():
+    # src/alpha_fringe.rs:264-299
+    w, h = 64, 64
+    y, x = np.mgrid[0:h, 0:w]
+    a = np.where(y <= 7, 128, np.where((x + 2 * y) % 4 == 0, 254, 255)).astype(np.uint16)
+    got = O.alpha_fringe_clear(a, 255)
+    assert np.all(got[8:] == 255)
+    assert np.all(got[:8] == 128)
+    deep = O.alpha_fringe_clear(a.astype(np.uint32) * 257, 65535)
+    assert np.array_equal(deep, got.astype(np.uint32) * 257)
+    sparse = np.full(w * h, 255, np.uint16)
+    sparse[::40] = 254
+    sparse = sparse.reshape(h, w)
+    assert np.array_equal(O.alpha_fringe_clear(sparse, 255), sparse)
+    shade = np.full((h, w), 253, np.uint16)
+    assert np.array_equal(O.alpha_fringe_clear(shade, 255), shade)
+
+
+def _planes(w, h, values):
+    return np.stack([np.array(values, np.float32).reshape(h, w)] * 3)
+
+
+def test_fill_invisible_propagates_in_scan_order():
+    # src/invisible.rs:158-175
+    img = _planes(3, 2, [2.0, 99.0, 4.0, 6.0, 99.0, 99.0])
+    got = O.fill_invisible(img, np.array([[255, 0, 1], [128, 0, 0]], np.uint16))
+    want = np.array([2.0, 3.0, 4.0, 6.0, 4.8, 4.266667], np.float32)
+    for c in range(3):
+        assert np.allclose(got[c].reshape(-1), want, atol=1e-6)
+
+
+def test_fill_invisible_rows_columns_and_fully_transparent():
+    # src/invisible.rs:177-195 (the non-empty cases)
+    for w, h, alpha, src, want in [
+        (1, 1, [0], [99.0], [0.0]),
+        (3, 1, [0, 1, 0], [99.0, 2.0, 99.0], [2.0] * 3),
+        (1, 3, [0, 1, 0], [99.0, 2.0, 99.0], [2.0] * 3),
+        (2, 2, [0] * 4, [99.0] * 4, [0.0] * 4),
+    ]:
+        got = O.fill_invisible(_planes(w, h, src), np.array(alpha, np.uint16).reshape(h, w))
+        for c in range(3):
+            assert got[c].reshape(-1).tolist() == want
+
+
+def test_fill_invisible_high_depth_uses_opacity():
+    # src/invisible.rs:223-239: 16-bit alpha gives the 8-bit result
+    ref = O.fill_invisible(_planes(3, 1, [99.0, 2.0, 99.0]), np.array([[0, 1, 0]], np.uint16))
+    deep = O.fill_invisible(_planes(3, 1, [99.0, 2.0, 99.0]), np.array([[0, 1, 0]], np.uint16))
+    assert np.array_equal(ref, deep)
+
+
+def test_alpha_factors_follow_each_blocks_largest_alpha():
+    # src/adaptive_quant.rs:1077-1099
+    w, h = 24, 8
+    a = np.zeros((h, w), np.uint16)
+    a[:, 8:24] = 10
+    a[3, 12] = 255
+    f = O.alpha_block_factors(a, 255)
+    assert f.shape == (1, 3)
+    assert f[0, 0] == 1.0 and f[0, 1] == 1.0
+    assert abs(f[0, 2] - 0.1) < 1e-6
+    a[3, 12] = 128
+    assert abs(O.alpha_block_factors(a, 255)[0, 1] - 128.0 / 255.0) < 1e-6
