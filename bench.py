@@ -419,66 +419,79 @@ def run_batch(ctx, stream, flush, args, world, dev) -> dict:
 
 
 def run_e2e(ctx, img, cfgs, args, world, dev):
+    """End to end through the public C ABI: every frame is uploaded from
+    pinned host memory and its outputs (maps, DC levels, tokens, group
+    offsets, histograms) land in pinned host memory, all inside the timed
+    region.  The caller pipelines frames over two contexts with
+    jxg_frontend_enqueue / jxg_frontend_wait, so one frame's transfers
+    overlap the other's kernels."""
     import ctypes
 
     import torch
 
+    import jixel_gb300 as J
     from jixel_gb300 import _lib as L
     from jixel_gb300 import frame_info
 
     lib = L.load()
     fi = frame_info(WIDTH, HEIGHT)
-    pin = lambda n, dt: torch.empty(n, dtype=dt, pin_memory=True)  # noqa: E731
-    h_img = pin(img.size, torch.uint8)
+    h_img = torch.empty(img.size, dtype=torch.uint8, pin_memory=True)
     h_img.numpy()[:] = img.reshape(-1)
+    ctxs = [J.FrontendContext(dev.index or 0) for _ in range(2)]
+    outs = [J.PinnedOutputs(WIDTH, HEIGHT) for _ in range(2)]
+    for o in outs:  # the strategy map is filled on the host; the rest is downloaded
+        o.c.ac_strategy = None
+    c_cfgs = [c._c() for c in cfgs]
     nb = fi.xsize_blocks * fi.ysize_blocks
     nt = fi.xsize_tiles * fi.ysize_tiles
-    bufs = {
-        "quant_field": pin(nb, torch.uint8), "ytox": pin(nt, torch.int8),
-        "ytob": pin(nt, torch.int8), "quant_dc": pin(3 * nb, torch.int16),
-        "tokens": pin(2 * fi.max_tokens, torch.int32),
-        "group_offsets": pin(fi.num_groups + 1, torch.int64),
-        "histograms": pin(L.NUM_FINE_AC_CONTEXTS * L.ALPHABET_SIZE, torch.int32),
-    }
-    out = L.FrontendOutput()
-    out.quant_field = bufs["quant_field"].data_ptr()
-    out.ytox_map = bufs["ytox"].data_ptr()
-    out.ytob_map = bufs["ytob"].data_ptr()
-    out.quant_dc = bufs["quant_dc"].data_ptr()
-    out.tokens = bufs["tokens"].data_ptr()
-    out.token_capacity = fi.max_tokens
-    out.group_offsets = bufs["group_offsets"].data_ptr()
-    out.histograms = bufs["histograms"].data_ptr()
-    params = L.FrameParams()
-    c_cfgs = [c._c() for c in cfgs]
-    d2h = [0]
+    fixed_d2h = (nb + 2 * nt + 6 * nb + (fi.num_groups + 1) * 8
+                 + L.NUM_FINE_AC_CONTEXTS * L.ALPHABET_SIZE * 4)
+    state = {"pending": [False, False], "d2h": 0, "k": 0}
+
+    def finish(slot):
+        if state["pending"][slot]:
+            st = lib.jxg_frontend_wait(ctxs[slot].handle)
+            if st:
+                raise RuntimeError(f"jxg_frontend_wait status {st}")
+            state["pending"][slot] = False
+            state["d2h"] += fixed_d2h + outs[slot].params.num_tokens * 8
 
     def step():
-        d2h[0] = 0
         for c in c_cfgs:
-            st = lib.jxg_frontend(ctx.handle, ctypes.c_void_p(h_img.data_ptr()), WIDTH, HEIGHT, 3, 8,
-                                  ctypes.byref(c), ctypes.byref(params), ctypes.byref(out))
+            slot = state["k"] % 2
+            state["k"] += 1
+            finish(slot)
+            st = lib.jxg_frontend_enqueue(ctxs[slot].handle, ctypes.c_void_p(h_img.data_ptr()),
+                                          WIDTH, HEIGHT, 3, 8, ctypes.byref(c),
+                                          ctypes.byref(outs[slot].params), ctypes.byref(outs[slot].c))
             if st:
-                raise RuntimeError(f"jxg_frontend status {st}")
-            d2h[0] += (nb + 2 * nt + 6 * nb + params.num_tokens * 8 + (fi.num_groups + 1) * 8
-                       + L.NUM_FINE_AC_CONTEXTS * L.ALPHABET_SIZE * 4)
+                raise RuntimeError(f"jxg_frontend_enqueue status {st}")
+            state["pending"][slot] = True
 
     for _ in range(max(args.warmup, 1)):
         step()
+    finish(0)
+    finish(1)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
+    state["d2h"] = 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
         step()
+    finish(0)
+    finish(1)
     torch.cuda.synchronize(dev)
     dt = time.perf_counter() - t0
     dt = max_over_ranks(dt, dev)
+    for c in ctxs:
+        c.close()
     value = world * args.steps * len(QUALITIES) * WIDTH * HEIGHT / 1e6 / dt
     return {"value": value, "unit": "MP/s", "h2d_bytes_per_step": len(QUALITIES) * img.size,
-            "d2h_bytes_per_step": int(d2h[0]),
-            "path": "jxg_frontend (C ABI): pinned host RGB in; maps, DC levels, tokens, group "
-                    "offsets and histograms out"}
+            "d2h_bytes_per_step": int(state["d2h"] / args.steps),
+            "path": "jxg_frontend_enqueue / jxg_frontend_wait (C ABI), two contexts alternating "
+                    "frames: pinned host RGB in; maps, DC levels, tokens, group offsets and "
+                    "histograms out to pinned host memory"}
 
 
 def main():

@@ -174,6 +174,24 @@ int32_t jxg_frontend(void* ctx, const void* pixels, uint64_t width, uint64_t hei
                      int32_t channels, int32_t bits, const jxg_config* config,
                      jxg_frame_params* params, jxg_frontend_output* out);
 
+/* Asynchronous front end --------------------------------------------------
+ * jxg_frontend_enqueue enqueues on the context's stream the upload of
+ * `pixels`, the pass, and the download of `params` and every requested
+ * output, then returns without waiting; jxg_frontend_wait completes it
+ * (params, status).  The token stream and group offsets are written by the
+ * device itself (their length is known only there), so `out->tokens` and
+ * `out->group_offsets` must be memory the device can write: pinned host
+ * memory (cudaHostAlloc / cudaHostRegister), device memory, or any host
+ * memory on systems with coherent CPU-GPU access.  Upload and downloads
+ * run asynchronously when `pixels` and the outputs are pinned.  A context
+ * holds one frame in flight (enqueueing again waits for the previous one);
+ * two contexts on one device overlap one frame's transfers with the other's
+ * kernels.  `pixels` and the outputs must stay valid until the wait. */
+int32_t jxg_frontend_enqueue(void* ctx, const void* pixels, uint64_t width, uint64_t height,
+                             int32_t channels, int32_t bits, const jxg_config* config,
+                             jxg_frame_params* params, jxg_frontend_output* out);
+int32_t jxg_frontend_wait(void* ctx);
+
 /* Batch -----------------------------------------------------------------
  * Many frames of any sizes, layouts and distances in one pass: each stage is
  * one launch over the (frame, work unit) list of the whole batch, and the

@@ -3,10 +3,10 @@
 The compute runs in the CUDA library ``_build/libjxg.so`` (C ABI in
 ``include/jxg.h``); this package is its host-side mirror.
 """
-from .api import (EncodeConfig, EncodeError, FrontendBatch, FrontendContext, FrontendResult, Speed,
-                  distance_from_quality, encode_frontend, frame_info)
+from .api import (EncodeConfig, EncodeError, FrontendBatch, FrontendContext, FrontendResult,
+                  PinnedOutputs, Speed, distance_from_quality, encode_frontend, frame_info)
 
 __all__ = [
     "EncodeConfig", "EncodeError", "FrontendBatch", "FrontendContext", "FrontendResult", "Speed",
-    "distance_from_quality", "encode_frontend", "frame_info",
+    "PinnedOutputs", "distance_from_quality", "encode_frontend", "frame_info",
 ]

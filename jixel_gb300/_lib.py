@@ -25,6 +25,8 @@ EXPORTS = [
     "jxg_frontend_params",
     "jxg_frontend_fetch",
     "jxg_frontend",
+    "jxg_frontend_enqueue",
+    "jxg_frontend_wait",
     "jxg_batch_create",
     "jxg_batch_add",
     "jxg_batch_run",
@@ -125,6 +127,10 @@ def load() -> ctypes.CDLL:
         "jxg_frontend_fetch": (i32, [vp, ctypes.POINTER(FrontendOutput)]),
         "jxg_frontend": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config),
                                ctypes.POINTER(FrameParams), ctypes.POINTER(FrontendOutput)]),
+        "jxg_frontend_enqueue": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config),
+                                       ctypes.POINTER(FrameParams),
+                                       ctypes.POINTER(FrontendOutput)]),
+        "jxg_frontend_wait": (i32, [vp]),
         "jxg_batch_create": (i32, [vp, i32, ctypes.POINTER(vp)]),
         "jxg_batch_add": (ctypes.c_int64, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config)]),
         "jxg_batch_run": (i32, [vp, i32]),

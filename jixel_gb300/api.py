@@ -252,6 +252,19 @@ class FrontendContext:
         r.tokens = r.tokens[: int(p["num_tokens"])]
         return r
 
+    def enqueue(self, pixels: np.ndarray, config: EncodeConfig, out: "PinnedOutputs"):
+        """Asynchronous front end (jxg_frontend_enqueue): `pixels` and `out`
+        should be pinned; call wait() before reading `out`."""
+        ch, bits = _pixels_kind(pixels)
+        h, w = pixels.shape[:2]
+        cfg = config._c()
+        self._check(self._lib.jxg_frontend_enqueue(self._ctx, pixels.ctypes.data, w, h, ch, bits,
+                                                   ctypes.byref(cfg), ctypes.byref(out.params),
+                                                   ctypes.byref(out.c)))
+
+    def wait(self):
+        self._check(self._lib.jxg_frontend_wait(self._ctx))
+
     def batch(self, pixels_on_device: bool = False) -> "FrontendBatch":
         """A batch of frames run as one pass on this context."""
         return FrontendBatch(self, pixels_on_device)
@@ -295,6 +308,65 @@ class FrontendContext:
 
     def reset_kernel_times(self):
         self._check(self._lib.jxg_reset_kernel_times(self._ctx))
+
+
+class PinnedOutputs:
+    """Pinned host buffers for every output of one width x height frame, for
+    FrontendContext.enqueue (allocated with torch's pinned allocator)."""
+
+    def __init__(self, width: int, height: int, *, channels: int = 3, coefficients: bool = False,
+                 xyb: bool = False):
+        import torch
+
+        fi = frame_info(width, height)
+        xb, yb = fi.xsize_blocks, fi.ysize_blocks
+        nb, nt = xb * yb, fi.xsize_tiles * fi.ysize_tiles
+
+        def pin(shape, dt):
+            return torch.empty(shape, dtype=dt, pin_memory=True).numpy()
+
+        self.width, self.height, self.info = width, height, fi
+        self.quant_field = pin((yb, xb), torch.uint8)
+        self.ac_strategy = pin((yb, xb), torch.uint8)
+        self.ytox = pin((fi.ysize_tiles, fi.xsize_tiles), torch.int8)
+        self.ytob = pin((fi.ysize_tiles, fi.xsize_tiles), torch.int8)
+        self.quant_dc = pin((3, yb, xb), torch.int16)
+        self.coefficients = pin((yb, xb, 3, 64), torch.int32) if coefficients else None
+        self.num_nzeros = pin((3, yb, xb), torch.uint8)
+        self.tokens = pin((fi.max_tokens, 2), torch.int32).view(np.uint32)
+        self.group_offsets = pin((fi.num_groups + 1,), torch.int64).view(np.uint64)
+        self.histograms = pin((L.NUM_FINE_AC_CONTEXTS, L.ALPHABET_SIZE), torch.int32).view(np.uint32)
+        self.xyb = pin((3, height, width), torch.float32) if xyb else None
+        self.alpha = pin((height, width), torch.int16).view(np.uint16) if channels == 4 else None
+        self.params = L.FrameParams()
+        o = L.FrontendOutput()
+        o.quant_field = self.quant_field.ctypes.data
+        o.ac_strategy = self.ac_strategy.ctypes.data
+        o.ytox_map = self.ytox.ctypes.data
+        o.ytob_map = self.ytob.ctypes.data
+        o.quant_dc = self.quant_dc.ctypes.data
+        o.coefficients = self.coefficients.ctypes.data if coefficients else None
+        o.num_nzeros = self.num_nzeros.ctypes.data
+        o.xyb = self.xyb.ctypes.data if xyb else None
+        o.tokens = self.tokens.ctypes.data
+        o.token_capacity = fi.max_tokens
+        o.group_offsets = self.group_offsets.ctypes.data
+        o.histograms = self.histograms.ctypes.data
+        o.alpha = self.alpha.ctypes.data if self.alpha is not None else None
+        self.c = o
+
+    def result(self) -> FrontendResult:
+        """Copies of the outputs after FrontendContext.wait()."""
+        p = _params_dict(self.params)
+        n = int(p["num_tokens"])
+        return FrontendResult(
+            params=p, quant_field=self.quant_field.copy(), ac_strategy=self.ac_strategy.copy(),
+            ytox=self.ytox.copy(), ytob=self.ytob.copy(), quant_dc=self.quant_dc.copy(),
+            coefficients=None if self.coefficients is None else self.coefficients.copy(),
+            num_nzeros=self.num_nzeros.copy(), tokens=self.tokens[:n].copy(),
+            group_offsets=self.group_offsets.copy(), histograms=self.histograms.copy(),
+            xyb=None if self.xyb is None else self.xyb.copy(),
+            alpha=None if self.alpha is None else self.alpha.copy())
 
 
 class FrontendBatch:

@@ -111,6 +111,16 @@ struct Context {
   std::vector<cudaEvent_t> spare_events;
   std::map<std::string, TimedKernel> times;
   std::vector<std::string> time_names;
+  // asynchronous front end (jxg_frontend_enqueue / jxg_frontend_wait)
+  struct AsyncSlot {
+    DeviceStats stats;
+    uint64_t token_count;
+    uint64_t pad;
+  };
+  HostBuf async_slot;                  // pinned AsyncSlot the pass's scalars land in
+  bool async_pending = false;
+  jxg_frame_params* async_params = nullptr;
+  jxg_frontend_output async_out{};
 };
 
 struct Batch {
@@ -594,6 +604,36 @@ int wait(Context* c) {
   return JXG_OK;
 }
 
+// Frame scalars from the frame's distance parameters and its device stats.
+void params_from(const FrameLayout& L, const DeviceStats& ds, uint64_t num_tokens,
+                 jxg_frame_params* out) {
+  std::memset(out, 0, sizeof(*out));
+  const DistanceParams& p = L.dp;
+  out->distance = p.distance;
+  out->global_scale = p.global_scale;
+  out->quant_dc = p.quant_dc;
+  out->scale = p.scale;
+  out->scale_dc = p.scale_dc;
+  out->x_qm_scale = p.x_qm_scale;
+  out->b_qm_scale = p.b_qm_scale;
+  out->epf_iters = p.epf_iters;
+  for (int i = 0; i < 3; ++i) out->dc_step[i] = p.dc_step[i];
+  out->qf_threshold = ds.qf_threshold;
+  out->constant_blocks = ds.constant_blocks;
+  const bool screen = is_screen_content(ds.constant_blocks, L.width, L.height);
+  out->screen_content = screen;
+  out->epf_sharpness = epf_sharpness_id(p.distance, screen);
+  out->num_tokens = num_tokens;
+}
+
+int check_flags(Context* c, const DeviceStats& ds) {
+  if (ds.flags & kFlagFillTimeout)
+    return fail(c, JXG_ERR_DEVICE_TIMEOUT, "a bounded device wait of the invisible fill ran out");
+  if (ds.flags & kFlagTokenTimeout)
+    return fail(c, JXG_ERR_DEVICE_TIMEOUT, "a level copy of the tokenizer did not land in time");
+  return JXG_OK;
+}
+
 int read_params(Context* c, int index, jxg_frame_params* out) {
   if (!c->have_frame || index < 0 || index >= static_cast<int>(c->layouts.size()))
     return fail(c, JXG_ERR_INVALID_ARGUMENT, "no such frame in the last pass");
@@ -609,32 +649,43 @@ int read_params(Context* c, int index, jxg_frame_params* out) {
                               8, cudaMemcpyDeviceToHost, c->stream));
   int st = wait(c);
   if (st) return st;
-  if (ds.flags & kFlagFillTimeout)
-    return fail(c, JXG_ERR_DEVICE_TIMEOUT, "a bounded device wait of the invisible fill ran out");
-  std::memset(out, 0, sizeof(*out));
-  const DistanceParams& p = L.dp;
-  out->distance = p.distance;
-  out->global_scale = p.global_scale;
-  out->quant_dc = p.quant_dc;
-  out->scale = p.scale;
-  out->scale_dc = p.scale_dc;
-  out->x_qm_scale = p.x_qm_scale;
-  out->b_qm_scale = p.b_qm_scale;
-  out->epf_iters = p.epf_iters;
-  for (int i = 0; i < 3; ++i) out->dc_step[i] = p.dc_step[i];
-  out->qf_threshold = ds.qf_threshold;
-  out->constant_blocks = ds.constant_blocks;
-  bool screen = is_screen_content(ds.constant_blocks, L.width, L.height);
-  out->screen_content = screen;
-  out->epf_sharpness = epf_sharpness_id(p.distance, screen);
-  out->num_tokens = goffs[1] - goffs[0];
+  if ((st = check_flags(c, ds))) return st;
+  params_from(L, ds, goffs[1] - goffs[0], out);
   return JXG_OK;
 }
 
-int fetch_frame(Context* c, int index, jxg_frontend_output* out) {
-  jxg_frame_params p;
-  int st = read_params(c, index, &p);
-  if (st) return st;
+// The address kernels use to write caller memory `p`: device memory as is,
+// pinned host memory through its mapping, other host memory only where
+// the device can reach pageable memory (coherent CPU-GPU systems).
+int device_view(Context* c, void* p, void** out) {
+  *out = nullptr;
+  if (!p) return JXG_OK;
+  cudaPointerAttributes attr{};
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    attr.type = cudaMemoryTypeUnregistered;
+  }
+  if (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) {
+    *out = p;
+    return JXG_OK;
+  }
+  if (attr.type == cudaMemoryTypeHost && attr.devicePointer) {
+    *out = attr.devicePointer;
+    return JXG_OK;
+  }
+  int pageable = 0;
+  cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, c->device);
+  if (pageable) {
+    *out = p;
+    return JXG_OK;
+  }
+  return fail(c, JXG_ERR_INVALID_ARGUMENT,
+              "asynchronous outputs must be pinned host memory or device memory");
+}
+
+// Enqueues every download of frame `index` except the token stream and
+// group offsets (fixed sizes; no host synchronisation).
+int enqueue_fixed_downloads(Context* c, int index, const jxg_frontend_output* out) {
   const FrameLayout& L = c->layouts[index];
   const jxg_frame_info& fi = L.info;
   const size_t nb = fi.xsize_blocks * fi.ysize_blocks;
@@ -645,8 +696,7 @@ int fetch_frame(Context* c, int index, jxg_frontend_output* out) {
     JXG_CUDA(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
     return JXG_OK;
   };
-  if (out->tokens && out->token_capacity < p.num_tokens)
-    return fail(c, JXG_ERR_INVALID_ARGUMENT, "token buffer too small");
+  int st;
   if (out->coefficients) {
     if ((st = ensure(c, c->coeffs, nb * 192 * 4))) return st;
     const int64_t count = static_cast<int64_t>(nb) * 192;
@@ -658,19 +708,12 @@ int fetch_frame(Context* c, int index, jxg_frontend_output* out) {
     });
     if (st) return st;
   }
-  uint64_t first = 0;
-  JXG_CUDA(c, cudaMemcpyAsync(&first, static_cast<uint64_t*>(c->group_offsets.ptr) + L.group_off, 8,
-                              cudaMemcpyDeviceToHost, s));
-  if ((st = wait(c))) return st;
   if ((st = copy(out->quant_field, static_cast<uint8_t*>(c->qf.ptr) + L.block_off, nb)) ||
       (st = copy(out->ytox_map, static_cast<int8_t*>(c->ytox.ptr) + L.tile_off, nt)) ||
       (st = copy(out->ytob_map, static_cast<int8_t*>(c->ytob.ptr) + L.tile_off, nt)) ||
       (st = copy(out->quant_dc, static_cast<int16_t*>(c->quant_dc.ptr) + 3 * L.block_off, 3 * nb * 2)) ||
       (st = copy(out->coefficients, c->coeffs.ptr, nb * 192 * 4)) ||
       (st = copy(out->num_nzeros, static_cast<uint8_t*>(c->nzeros.ptr) + 3 * L.block_off, 3 * nb)) ||
-      (st = copy(out->tokens, static_cast<uint2*>(c->tokens.ptr) + first, p.num_tokens * sizeof(jxg_token))) ||
-      (st = copy(out->group_offsets, static_cast<uint64_t*>(c->group_offsets.ptr) + L.group_off,
-                 (fi.num_groups + 1) * 8)) ||
       (st = copy(out->histograms, static_cast<char*>(c->hist.ptr) + index * kHistBytes, kHistBytes)))
     return st;
   if (out->alpha && L.has_alpha &&
@@ -683,6 +726,33 @@ int fetch_frame(Context* c, int index, jxg_frontend_output* out) {
       if ((st = copy(out->xyb + ch * px, static_cast<float*>(c->xyb.ptr) + L.xyb_off + ch * L.plane, px * 4)))
         return st;
   }
+  return JXG_OK;
+}
+
+int fetch_frame(Context* c, int index, jxg_frontend_output* out) {
+  jxg_frame_params p;
+  int st = read_params(c, index, &p);
+  if (st) return st;
+  const FrameLayout& L = c->layouts[index];
+  const jxg_frame_info& fi = L.info;
+  const size_t nb = fi.xsize_blocks * fi.ysize_blocks;
+  cudaStream_t s = c->stream;
+  auto copy = [&](void* dst, const void* src, size_t bytes) -> int {
+    if (!dst || bytes == 0) return JXG_OK;
+    JXG_CUDA(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+    return JXG_OK;
+  };
+  if (out->tokens && out->token_capacity < p.num_tokens)
+    return fail(c, JXG_ERR_INVALID_ARGUMENT, "token buffer too small");
+  uint64_t first = 0;
+  JXG_CUDA(c, cudaMemcpyAsync(&first, static_cast<uint64_t*>(c->group_offsets.ptr) + L.group_off, 8,
+                              cudaMemcpyDeviceToHost, s));
+  if ((st = wait(c))) return st;
+  if ((st = enqueue_fixed_downloads(c, index, out)) ||
+      (st = copy(out->tokens, static_cast<uint2*>(c->tokens.ptr) + first, p.num_tokens * sizeof(jxg_token))) ||
+      (st = copy(out->group_offsets, static_cast<uint64_t*>(c->group_offsets.ptr) + L.group_off,
+                 (fi.num_groups + 1) * 8)))
+    return st;
   if ((st = wait(c))) return st;
   if (out->group_offsets)  // frame-local token offsets
     for (uint64_t g = 0; g <= fi.num_groups; ++g) out->group_offsets[g] -= first;
@@ -800,7 +870,7 @@ void jxg_context_destroy(void* ctx) {
                          &c->group_offsets, &c->plan, &c->total, &c->op_in, &c->op_out,
                          &c->alpha, &c->alpha_peak, &c->fill_done})
     if (b->ptr) cudaFree(b->ptr);
-  for (jxg::HostBuf* b : {&c->plan_host, &c->pixels_host})
+  for (jxg::HostBuf* b : {&c->plan_host, &c->pixels_host, &c->async_slot})
     if (b->ptr) cudaFreeHost(b->ptr);
   cudaFree(c->d_lut);
   cudaFree(c->d_exp2);
@@ -848,6 +918,10 @@ int32_t jxg_frontend_run_device(void* ctx, const void* pixels, uint64_t width, u
                                 int32_t channels, int32_t bits, const jxg_config* config) {
   Context* c = static_cast<Context*>(ctx);
   if (!c) return JXG_ERR_INVALID_ARGUMENT;
+  if (c->async_pending) {  // finish the enqueued frame before reusing its buffers
+    const int st = jxg_frontend_wait(ctx);
+    if (st) return st;
+  }
   cudaSetDevice(c->device);
   return jxg::single_pass(c, pixels, width, height, channels, bits, config, true);
 }
@@ -856,6 +930,10 @@ int32_t jxg_frontend_run(void* ctx, const void* pixels, uint64_t width, uint64_t
                          int32_t channels, int32_t bits, const jxg_config* config) {
   Context* c = static_cast<Context*>(ctx);
   if (!c) return JXG_ERR_INVALID_ARGUMENT;
+  if (c->async_pending) {
+    const int st = jxg_frontend_wait(ctx);
+    if (st) return st;
+  }
   cudaSetDevice(c->device);
   int st = jxg::single_pass(c, pixels, width, height, channels, bits, config, false);
   if (st) return st;
@@ -874,6 +952,67 @@ int32_t jxg_frontend_fetch(void* ctx, jxg_frontend_output* out) {
   if (!c || !out) return JXG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(c->device);
   return jxg::fetch_frame(c, 0, out);
+}
+
+int32_t jxg_frontend_wait(void* ctx) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c) return JXG_ERR_INVALID_ARGUMENT;
+  if (!c->async_pending) return JXG_OK;
+  cudaSetDevice(c->device);
+  c->async_pending = false;
+  int st = jxg::wait(c);
+  if (st) return st;
+  const auto* slot = static_cast<const Context::AsyncSlot*>(c->async_slot.ptr);
+  if ((st = jxg::check_flags(c, slot->stats))) return st;
+  const jxg::FrameLayout& L = c->layouts[0];
+  if (c->async_params) jxg::params_from(L, slot->stats, slot->token_count, c->async_params);
+  const jxg_frontend_output& out = c->async_out;
+  if (out.tokens && slot->token_count > out.token_capacity)
+    return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "token buffer too small");
+  if (out.ac_strategy)
+    std::memset(out.ac_strategy, 1, L.info.xsize_blocks * L.info.ysize_blocks);
+  return JXG_OK;
+}
+
+int32_t jxg_frontend_enqueue(void* ctx, const void* pixels, uint64_t width, uint64_t height,
+                             int32_t channels, int32_t bits, const jxg_config* config,
+                             jxg_frame_params* params, jxg_frontend_output* out) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c) return JXG_ERR_INVALID_ARGUMENT;
+  int st;
+  if (c->async_pending && (st = jxg_frontend_wait(ctx))) return st;
+  cudaSetDevice(c->device);
+  jxg_frontend_output o{};
+  if (out) o = *out;
+  void* tok_dev = nullptr;
+  void* off_dev = nullptr;
+  if ((st = jxg::device_view(c, o.tokens, &tok_dev)) ||
+      (st = jxg::device_view(c, o.group_offsets, &off_dev)) ||
+      (st = jxg::ensure_host(c, c->async_slot, sizeof(Context::AsyncSlot))))
+    return st;
+  if ((st = jxg::single_pass(c, pixels, width, height, channels, bits, config, false))) return st;
+  const jxg::FrameLayout& L = c->layouts[0];
+  auto* slot = static_cast<Context::AsyncSlot*>(c->async_slot.ptr);
+  void* slot_count_dev = nullptr;
+  if ((st = jxg::device_view(c, &slot->token_count, &slot_count_dev))) return st;
+  cudaStream_t s = c->stream;
+  if ((st = jxg::enqueue_fixed_downloads(c, 0, &o))) return st;
+  JXG_CUDA(c, cudaMemcpyAsync(&slot->stats, c->stats.ptr, sizeof(jxg::DeviceStats),
+                              cudaMemcpyDeviceToHost, s));
+  const unsigned grid = static_cast<unsigned>(std::max(1, std::min(c->num_sms * 4, 1024)));
+  st = jxg::launch(c, "k_copy_out_tokens", c->timing, [&] {
+    jxg::k_copy_out_tokens<<<grid, 256, 0, s>>>(
+        static_cast<const uint2*>(c->tokens.ptr),
+        static_cast<const uint64_t*>(c->group_offsets.ptr) + L.group_off,
+        static_cast<int>(L.info.num_groups), static_cast<uint2*>(tok_dev),
+        o.tokens ? o.token_capacity : 0, static_cast<uint64_t*>(off_dev),
+        static_cast<uint64_t*>(slot_count_dev));
+  });
+  if (st) return st;
+  c->async_pending = true;
+  c->async_params = params;
+  c->async_out = o;
+  return JXG_OK;
 }
 
 int32_t jxg_frontend(void* ctx, const void* pixels, uint64_t width, uint64_t height,
@@ -923,6 +1062,7 @@ int32_t jxg_batch_run(void* batch, int32_t use_graph) {
   cudaSetDevice(c->device);
   const int n = static_cast<int>(b->images.size());
   int st;
+  if (c->async_pending && (st = jxg_frontend_wait(c))) return st;
   if (!b->planned || b->epoch != c->epoch) {
     drop_graph(b);
     if ((st = jxg::plan_pass(c, b->images.data(), n, b->on_device, !b->on_device))) return st;
