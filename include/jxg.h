@@ -273,6 +273,14 @@ int32_t jxg_token_offsets_noalloc(const uint32_t* counts, uint64_t num_groups, u
  * the error path, exercised without faulting or hanging the device. */
 int32_t jxg_selftest_bounded_wait(void* ctx, uint32_t polls);
 
+/* The XYB cube root divides with a fused-multiply-add sequence instead of
+ * the IEEE division; this entry point compares both on the device for every
+ * float bit pattern in [lo_bits, hi_bits) and returns the number of
+ * differing results (and the smallest differing pattern, or 0xFFFFFFFF).
+ * [0, 0x40000000) covers every input XYB can produce. */
+int32_t jxg_selftest_cbrt(void* ctx, uint32_t lo_bits, uint32_t hi_bits, uint64_t* mismatches,
+                          uint32_t* first_bad);
+
 /* Kernel timing -------------------------------------------------------- */
 /* With `enable`, every launch of this context is bracketed by CUDA events on
  * its stream; jxg_kernel_times sums their durations per kernel. */

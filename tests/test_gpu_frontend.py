@@ -152,3 +152,14 @@ def test_repeat_runs_are_identical(ctx):
     b = ctx.frontend(img, ultrafast(1.0))
     assert np.array_equal(a.tokens, b.tokens)
     assert np.array_equal(a.histograms, b.histograms)
+
+
+def test_cube_root_division_is_exact_for_every_xyb_input(ctx):
+    # every float in [0, 2): the fast quotient equals the IEEE division's
+    import ctypes
+    from jixel_gb300 import _lib as L
+    lib = L.load()
+    n = ctypes.c_uint64()
+    first = ctypes.c_uint32()
+    assert lib.jxg_selftest_cbrt(ctx.handle, 0, 0x40000000, ctypes.byref(n), ctypes.byref(first)) == 0
+    assert n.value == 0, hex(first.value)
