@@ -576,11 +576,11 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
          k_scan_apply<<<nchunks, kScanThreads, 0, s>>>(counts, ncounts, chunks, offs, goffs, 4 * 1024);
        })) ||
       (st = single ? launch(c, "k_tokenize", timed, [&] {
-         k_tokenize<<<static_cast<unsigned>(c->token_chunks), 256, 0, s>>>(
+         k_tokenize<<<static_cast<unsigned>(c->token_chunks), kTokThreads, 0, s>>>(
              f0, static_cast<uint2*>(c->tokens.ptr));
        })
                    : launch(c, "k_tokenize_batch", timed, [&] {
-         k_tokenize_batch<<<static_cast<unsigned>(c->token_chunks), 256, 0, s>>>(
+         k_tokenize_batch<<<static_cast<unsigned>(c->token_chunks), kTokThreads, 0, s>>>(
              frames, pre_tok, n, static_cast<uint2*>(c->tokens.ptr));
        })))
     return st;
@@ -629,8 +629,6 @@ void params_from(const FrameLayout& L, const DeviceStats& ds, uint64_t num_token
 int check_flags(Context* c, const DeviceStats& ds) {
   if (ds.flags & kFlagFillTimeout)
     return fail(c, JXG_ERR_DEVICE_TIMEOUT, "a bounded device wait of the invisible fill ran out");
-  if (ds.flags & kFlagTokenTimeout)
-    return fail(c, JXG_ERR_DEVICE_TIMEOUT, "a level copy of the tokenizer did not land in time");
   return JXG_OK;
 }
 
