@@ -273,13 +273,17 @@ int32_t jxg_token_offsets_noalloc(const uint32_t* counts, uint64_t num_groups, u
  * the error path, exercised without faulting or hanging the device. */
 int32_t jxg_selftest_bounded_wait(void* ctx, uint32_t polls);
 
-/* The XYB cube root divides with a fused-multiply-add sequence instead of
- * the IEEE division; this entry point compares both on the device for every
- * float bit pattern in [lo_bits, hi_bits) and returns the number of
- * differing results (and the smallest differing pattern, or 0xFFFFFFFF).
- * [0, 0x40000000) covers every input XYB can produce. */
-int32_t jxg_selftest_cbrt(void* ctx, uint32_t lo_bits, uint32_t hi_bits, uint64_t* mismatches,
-                          uint32_t* first_bad);
+/* The XYB cube root and the AQ pre-pass and gamma terms divide and take
+ * square roots with fused-multiply-add sequences instead of the IEEE
+ * operations, on input ranges where they give the same results.  This entry
+ * point compares both on the device for every float bit pattern in
+ * [lo_bits, hi_bits): `which` 0 = the cube root (XYB inputs lie in
+ * [0, 0x40000000)), 1 / 2 = the AQ gamma ratio inverted / direct (inputs in
+ * [0, 0x44800000)), 3 = the AQ masking square root (inputs in
+ * [0, 0x3E4CCCCD]).  It returns the number of differing results and the
+ * smallest differing pattern (0xFFFFFFFF when none). */
+int32_t jxg_selftest_math(void* ctx, int32_t which, uint32_t lo_bits, uint32_t hi_bits,
+                          uint64_t* mismatches, uint32_t* first_bad);
 
 /* Kernel timing -------------------------------------------------------- */
 /* With `enable`, every launch of this context is bracketed by CUDA events on

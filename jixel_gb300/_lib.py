@@ -36,7 +36,7 @@ EXPORTS = [
     "jxg_op_dct8x8",
     "jxg_token_offsets_noalloc",
     "jxg_selftest_bounded_wait",
-    "jxg_selftest_cbrt",
+    "jxg_selftest_math",
     "jxg_enable_kernel_timing",
     "jxg_kernel_times",
     "jxg_reset_kernel_times",
@@ -142,7 +142,7 @@ def load() -> ctypes.CDLL:
         "jxg_op_dct8x8": (i32, [vp, vp, u64, vp]),
         "jxg_token_offsets_noalloc": (i32, [vp, u64, vp, vp, vp]),
         "jxg_selftest_bounded_wait": (i32, [vp, ctypes.c_uint32]),
-        "jxg_selftest_cbrt": (i32, [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(u64),
+        "jxg_selftest_math": (i32, [vp, i32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(u64),
                                     ctypes.POINTER(ctypes.c_uint32)]),
         "jxg_enable_kernel_timing": (i32, [vp, i32]),
         "jxg_kernel_times": (i32, [vp, ctypes.POINTER(ctypes.c_char_p),

@@ -1240,18 +1240,25 @@ int32_t jxg_selftest_bounded_wait(void* ctx, uint32_t polls) {
   return r == 1u ? JXG_OK : JXG_ERR_CUDA;
 }
 
-int32_t jxg_selftest_cbrt(void* ctx, uint32_t lo_bits, uint32_t hi_bits, uint64_t* mismatches,
-                          uint32_t* first_bad) {
+int32_t jxg_selftest_math(void* ctx, int32_t which, uint32_t lo_bits, uint32_t hi_bits,
+                          uint64_t* mismatches, uint32_t* first_bad) {
   Context* c = static_cast<Context*>(ctx);
-  if (!c || !mismatches || !first_bad || hi_bits < lo_bits) return JXG_ERR_INVALID_ARGUMENT;
+  if (!c || !mismatches || !first_bad || hi_bits < lo_bits || which < 0 || which > 3)
+    return JXG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(c->device);
   int st;
   if ((st = jxg::ensure(c, c->op_out, 256))) return st;
   auto* count = static_cast<unsigned long long*>(c->op_out.ptr);
   auto* first = reinterpret_cast<uint32_t*>(count + 1);
+  // masking_sqrt's multiplier as the front end computes it
+  jxg::DistanceParams dp;
+  jxg::compute_distance_params(1.0f, &dp);
+  jxg::KernelArgs ka;
+  jxg::fill_kernel_args(dp, &ka);
   JXG_CUDA(c, cudaMemsetAsync(count, 0, 8, c->stream));
   JXG_CUDA(c, cudaMemsetAsync(first, 0xFF, 4, c->stream));
-  jxg::k_cbrt_selftest<<<c->num_sms * 8, 256, 0, c->stream>>>(lo_bits, hi_bits, count, first);
+  jxg::k_math_selftest<<<c->num_sms * 8, 256, 0, c->stream>>>(which, ka.aq_masking_sqrt_mul, lo_bits,
+                                                               hi_bits, count, first);
   JXG_CUDA(c, cudaGetLastError());
   unsigned long long n = 0;
   JXG_CUDA(c, cudaMemcpyAsync(&n, count, 8, cudaMemcpyDeviceToHost, c->stream));

@@ -154,12 +154,19 @@ def test_repeat_runs_are_identical(ctx):
     assert np.array_equal(a.histograms, b.histograms)
 
 
-def test_cube_root_division_is_exact_for_every_xyb_input(ctx):
-    # every float in [0, 2): the fast quotient equals the IEEE division's
+@pytest.mark.parametrize("which,lo,hi", [
+    (0, 0, 0x40000000),           # cube root: every float in [0, 2)
+    (1, 0, 0x44800000),           # gamma ratio, inverted: [0, 1024)
+    (2, 0, 0x44800000),           # gamma ratio, direct: [0, 1024)
+    (3, 0, 0x3E4CCCCD + 1),       # masking square root: [0, 0.2]
+])
+def test_fast_math_equals_ieee_on_every_input(ctx, which, lo, hi):
+    # the fused sequences replacing IEEE division / sqrt on the hot paths give
+    # bit-identical results on every input those paths can see
     import ctypes
     from jixel_gb300 import _lib as L
     lib = L.load()
     n = ctypes.c_uint64()
     first = ctypes.c_uint32()
-    assert lib.jxg_selftest_cbrt(ctx.handle, 0, 0x40000000, ctypes.byref(n), ctypes.byref(first)) == 0
+    assert lib.jxg_selftest_math(ctx.handle, which, lo, hi, ctypes.byref(n), ctypes.byref(first)) == 0
     assert n.value == 0, hex(first.value)
