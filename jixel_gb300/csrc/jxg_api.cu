@@ -87,7 +87,7 @@ struct Context {
   // pass buffers (grown, never shrunk)
   DevBuf pixels, xyb, qf, ytox, ytob, quant_dc, levels, wide_levels, coeffs, nzeros, nz_packed,
       counts, offsets, chunks, tokens, hist, stats, group_offsets, plan, total, op_in, op_out,
-      alpha, alpha_peak, fill_done;
+      alpha, alpha_peak, alpha_zero, fill_done;
   HostBuf plan_host, pixels_host;
   // The plan (frame descriptors + chunk prefixes) lives in a ring of slots,
   // pinned on the host and mirrored on the device, so a pass can be planned
@@ -377,6 +377,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
       (st = ensure(c, c->group_offsets, (groups + 1) * 8)) || (st = ensure(c, c->total, 256)) ||
       (alpha_px && (st = ensure(c, c->alpha, alpha_px * 2))) ||
       (alpha_blocks && (st = ensure(c, c->alpha_peak, alpha_blocks * 2))) ||
+      (alpha_blocks && (st = ensure(c, c->alpha_zero, alpha_blocks))) ||
       (fill_total && (st = ensure(c, c->fill_done, fill_total * 4))) ||
       (!pixels_on_device && stage && (st = ensure_host(c, c->pixels_host, pix))))
     return st;
@@ -427,6 +428,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     if (L.has_alpha) {
       f.alpha = static_cast<uint16_t*>(c->alpha.ptr) + L.alpha_off;
       f.alpha_peak = static_cast<uint16_t*>(c->alpha_peak.ptr) + L.alpha_block_off;
+      f.alpha_zero = static_cast<uint8_t*>(c->alpha_zero.ptr) + L.alpha_block_off;
       f.alpha_full = im.bits == 8 ? 255 : 65535;
     }
     const int64_t px = static_cast<int64_t>(L.width * L.height);
@@ -866,7 +868,7 @@ void jxg_context_destroy(void* ctx) {
                          &c->wide_levels, &c->coeffs, &c->nzeros, &c->nz_packed, &c->counts,
                          &c->offsets, &c->chunks, &c->tokens, &c->hist, &c->stats,
                          &c->group_offsets, &c->plan, &c->total, &c->op_in, &c->op_out,
-                         &c->alpha, &c->alpha_peak, &c->fill_done})
+                         &c->alpha, &c->alpha_peak, &c->alpha_zero, &c->fill_done})
     if (b->ptr) cudaFree(b->ptr);
   for (jxg::HostBuf* b : {&c->plan_host, &c->pixels_host, &c->async_slot})
     if (b->ptr) cudaFreeHost(b->ptr);
