@@ -87,7 +87,7 @@ struct Context {
   // pass buffers (grown, never shrunk)
   DevBuf pixels, xyb, qf, ytox, ytob, quant_dc, levels, wide_levels, coeffs, nzeros, nz_packed,
       counts, offsets, chunks, tokens, hist, stats, group_offsets, plan, total, op_in, op_out,
-      alpha, alpha_peak, alpha_zero, fill_done;
+      alpha, alpha_peak, alpha_zero, fill_flags, fill_deps, fill_queue;
   HostBuf plan_host, pixels_host;
   // The plan (frame descriptors + chunk prefixes) lives in a ring of slots,
   // pinned on the host and mirrored on the device, so a pass can be planned
@@ -378,7 +378,9 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
       (alpha_px && (st = ensure(c, c->alpha, alpha_px * 2))) ||
       (alpha_blocks && (st = ensure(c, c->alpha_peak, alpha_blocks * 2))) ||
       (alpha_blocks && (st = ensure(c, c->alpha_zero, alpha_blocks))) ||
-      (fill_total && (st = ensure(c, c->fill_done, fill_total * 4))) ||
+      (fill_total && (st = ensure(c, c->fill_flags, fill_total))) ||
+      (fill_total && (st = ensure(c, c->fill_deps, fill_total * 4))) ||
+      (fill_total && (st = ensure(c, c->fill_queue, fill_total * 4))) ||
       (!pixels_on_device && stage && (st = ensure_host(c, c->pixels_host, pix))))
     return st;
   // frame descriptors
@@ -494,14 +496,17 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
   const int64_t* pre_tok = reinterpret_cast<const int64_t*>(reinterpret_cast<const char*>(pre_tile) + prefix_bytes);
   const int64_t* pre_alpha = reinterpret_cast<const int64_t*>(reinterpret_cast<const char*>(pre_tok) + prefix_bytes);
   const int64_t* pre_fill = reinterpret_cast<const int64_t*>(reinterpret_cast<const char*>(pre_alpha) + prefix_bytes);
-  // the fill's tile queue and per-tile completion flags start from zero
-  uint32_t* fill_queue = reinterpret_cast<uint32_t*>(static_cast<char*>(c->total.ptr) + 64);
+  // the fill's ready queue starts empty, its counters at zero
+  FillQueue* fill_q = reinterpret_cast<FillQueue*>(static_cast<char*>(c->total.ptr) + 64);
+  uint8_t* fill_flags = static_cast<uint8_t*>(c->fill_flags.ptr);
+  uint32_t* fill_deps = static_cast<uint32_t*>(c->fill_deps.ptr);
+  uint32_t* fill_queue = static_cast<uint32_t*>(c->fill_queue.ptr);
   const unsigned fill_grid = static_cast<unsigned>(std::max<int64_t>(
       1, std::min<int64_t>((c->fill_tiles + kFillThreads / 32 - 1) / (kFillThreads / 32),
                            static_cast<int64_t>(c->num_sms) * 3)));
   if (c->fill_tiles) {
-    JXG_CUDA(c, cudaMemsetAsync(c->fill_done.ptr, 0, c->fill_tiles * 4, s));
-    JXG_CUDA(c, cudaMemsetAsync(fill_queue, 0, 4, s));
+    JXG_CUDA(c, cudaMemsetAsync(fill_queue, 0xFF, c->fill_tiles * 4, s));
+    JXG_CUDA(c, cudaMemsetAsync(fill_q, 0, sizeof(FillQueue), s));
   }
   const bool timed = c->timing && !capturing;
   int st;
@@ -517,9 +522,13 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
          (st = launch(c, "k_alpha_final", timed, [&] {
            k_alpha_final<<<static_cast<unsigned>(c->alpha_tiles), 256, 0, s>>>(f0);
          })) ||
+         (st = launch(c, "k_fill_plan", timed, [&] {
+           k_fill_plan<<<fill_grid, kFillThreads, kFillSmemBytes, s>>>(
+               f0, c->fill_tiles, fill_flags, fill_deps, fill_queue, fill_q);
+         })) ||
          (st = launch(c, "k_fill_invisible", timed, [&] {
            k_fill_invisible<<<fill_grid, kFillThreads, kFillSmemBytes, s>>>(
-               f0, fill_queue, static_cast<uint32_t*>(c->fill_done.ptr), c->fill_tiles);
+               f0, fill_flags, fill_deps, fill_queue, fill_q);
          }))))
       return st;
     if ((st = launch(c, "k_adaptive_quant", timed, [&] {
@@ -545,10 +554,13 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
            k_alpha_final_batch<<<static_cast<unsigned>(c->alpha_tiles), 256, 0, s>>>(
                frames, pre_alpha, n);
          })) ||
+         (st = launch(c, "k_fill_plan_batch", timed, [&] {
+           k_fill_plan_batch<<<fill_grid, kFillThreads, kFillSmemBytes, s>>>(
+               frames, pre_fill, n, c->fill_tiles, fill_flags, fill_deps, fill_queue, fill_q);
+         })) ||
          (st = launch(c, "k_fill_invisible_batch", timed, [&] {
            k_fill_invisible_batch<<<fill_grid, kFillThreads, kFillSmemBytes, s>>>(
-               frames, pre_fill, n, fill_queue, static_cast<uint32_t*>(c->fill_done.ptr),
-               c->fill_tiles);
+               frames, pre_fill, n, fill_flags, fill_deps, fill_queue, fill_q);
          }))))
       return st;
     if ((st = launch(c, "k_adaptive_quant_batch", timed, [&] {
@@ -850,6 +862,11 @@ int32_t jxg_context_create(int32_t device, void** out_ctx) {
                                  static_cast<int>(jxg::kFillSmemBytes)) == cudaSuccess &&
             cudaFuncSetAttribute(jxg::k_fill_invisible_batch,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(jxg::kFillSmemBytes)) == cudaSuccess &&
+            cudaFuncSetAttribute(jxg::k_fill_plan, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(jxg::kFillSmemBytes)) == cudaSuccess &&
+            cudaFuncSetAttribute(jxg::k_fill_plan_batch,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(jxg::kFillSmemBytes)) == cudaSuccess;
   if (!ok) {
     jxg_context_destroy(c);
@@ -868,7 +885,8 @@ void jxg_context_destroy(void* ctx) {
                          &c->wide_levels, &c->coeffs, &c->nzeros, &c->nz_packed, &c->counts,
                          &c->offsets, &c->chunks, &c->tokens, &c->hist, &c->stats,
                          &c->group_offsets, &c->plan, &c->total, &c->op_in, &c->op_out,
-                         &c->alpha, &c->alpha_peak, &c->alpha_zero, &c->fill_done})
+                         &c->alpha, &c->alpha_peak, &c->alpha_zero, &c->fill_flags,
+                         &c->fill_deps, &c->fill_queue})
     if (b->ptr) cudaFree(b->ptr);
   for (jxg::HostBuf* b : {&c->plan_host, &c->pixels_host, &c->async_slot})
     if (b->ptr) cudaFreeHost(b->ptr);
