@@ -46,6 +46,8 @@ def parse_args():
     p.add_argument("--no-batch", action="store_true",
                    help="skip the 256-image plain-vs-batched comparison")
     p.add_argument("--batch-images", type=int, default=BATCH_IMAGES)
+    p.add_argument("--c5", action="store_true",
+                   help="also time one 8192x8192 RGB16 linear frame at q85 per step")
     return p.parse_args()
 
 
@@ -341,6 +343,7 @@ def run_gpu(args):
         "frac": fe_bytes / (fe_ms / 1000.0) / 1e9 / peaks["hbm_gbs"],
     }
 
+    c5 = run_c5(ctxs, streams, flush, args, dev) if args.c5 else None
     batch = None
     if not args.no_batch:
         batch = run_batch(ctx, streams[0], flush, args, world, dev)
@@ -365,12 +368,50 @@ def run_gpu(args):
             "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(ktimes.items())},
             "tokens_per_frame": [int(x) for x in tokens],
             "batch": batch,
+            "c5": c5,
         }
         print(json.dumps(line), flush=True)
     for c in ctxs:
         c.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_c5(ctxs, streams, flush, args, dev) -> dict:
+    """One 8192x8192 RGB 16-bit linear frame (50 % 1/f^2 texture) at q85 per
+    step, pixels resident in HBM, the two contexts taking steps in turn."""
+    import torch
+
+    import jixel_gb300 as J
+    from jixel_gb300 import synthetic
+
+    size = 8192
+    img = synthetic.config5_image(size)
+    d_img = torch.from_numpy(img.reshape(-1).view(np.uint8)).to(dev)
+    cfg = J.EncodeConfig(speed=J.Speed.ULTRA_FAST).with_quality(85)
+
+    def frame(k):
+        ctxs[k % 2].run_device(d_img.data_ptr(), size, size, 3, 16, cfg)
+
+    for k in range(max(args.warmup, 1)):
+        frame(k)
+    torch.cuda.synchronize(dev)
+    total = 0.0
+    for k in range(args.steps):
+        flush.zero_()
+        s, eb, e = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        s.record(streams[0])
+        streams[1].wait_event(s)
+        frame(k)
+        eb.record(streams[1])
+        streams[0].wait_event(eb)
+        e.record(streams[0])
+        e.synchronize()
+        total += s.elapsed_time(e)
+    mp = size * size / 1e6
+    return {"workload": "8192x8192 RGB 16-bit linear, q85 (d 1.45), UltraFast gates, one frame "
+                        "per step", "value": args.steps * mp / (total / 1000.0), "unit": "MP/s",
+            "ms_per_frame": total / args.steps}
 
 
 def run_batch(ctx, stream, flush, args, world, dev) -> dict:

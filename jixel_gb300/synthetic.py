@@ -126,6 +126,11 @@ def config2_image(width: int = 3840, height: int = 2160) -> np.ndarray:
     return generate(width, height, 2, noise_sigma=4.0, rectangles=200, texture_weight=0.3)
 
 
+def config5_image(size: int = 8192) -> np.ndarray:
+    """size x size RGB 16-bit linear, seed 5: 50 % 1/f^2 texture."""
+    return generate(size, size, 5, sixteen_bit=True, texture_weight=0.5)
+
+
 def config3_batch(count: int = 256, seed0: int = 3000):
     """Log-uniform sizes 64x64..2048x1536; odd indices carry alpha."""
     out = []

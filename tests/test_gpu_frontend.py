@@ -170,3 +170,23 @@ def test_fast_math_equals_ieee_on_every_input(ctx, which, lo, hi):
     first = ctypes.c_uint32()
     assert lib.jxg_selftest_math(ctx.handle, which, lo, hi, ctypes.byref(n), ctypes.byref(first)) == 0
     assert n.value == 0, hex(first.value)
+
+
+def test_8192_square_rgb16_invariants(ctx):
+    # the configs' largest frame: 8192x8192 RGB 16-bit linear at q85 (67 MP,
+    # 1024 groups); size-independent checks on the whole frame, bit-exact
+    # parity on a 2048x2048 crop
+    img = synthetic.config5_image()
+    d = J.distance_from_quality(85)
+    got = ctx.frontend(img, ultrafast(d), coefficients=False)
+    fi = J.frame_info(8192, 8192)
+    assert fi.num_groups == 1024
+    ntok = got.tokens.shape[0]
+    assert int(got.histograms.sum()) == ntok == int(got.group_offsets[-1])
+    # every block-channel emits at least its non-zero-count token
+    assert np.all(np.diff(got.group_offsets.astype(np.int64)) >= 3 * 1024)
+    # the non-zero counts add up to the non-zero coefficient tokens
+    assert int((got.tokens[:, 1] != 0).sum()) >= int(got.num_nzeros.astype(np.int64).sum())
+    assert got.quant_field.min() >= 1 and got.tokens[:, 0].max() < 14850
+    crop = np.ascontiguousarray(img[2048:4096, 4096:6144])
+    compare(ctx, crop, d, check_xyb=False)
