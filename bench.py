@@ -46,6 +46,10 @@ def parse_args():
     p.add_argument("--no-batch", action="store_true",
                    help="skip the 256-image plain-vs-batched comparison")
     p.add_argument("--batch-images", type=int, default=BATCH_IMAGES)
+    p.add_argument("--contexts", type=int, default=3,
+                   help="contexts (one stream each) the device-resident run alternates frames over")
+    p.add_argument("--e2e-contexts", type=int, default=3,
+                   help="contexts the end-to-end run alternates frames over")
     p.add_argument("--c5", action="store_true",
                    help="also time one 8192x8192 RGB16 linear frame at q85 per step")
     return p.parse_args()
@@ -60,8 +64,9 @@ def workload_config(impl: str) -> dict:
         "input": "synthetic seeded generator (seed 2): cosine gradients, noise sigma 4, "
                  "200 rectangles, 30% 1/f^2 texture, 8-px checker",
         "l2": "256 MB buffer written between timed steps, outside the timed events",
-        "streams": "two contexts on two streams take the frames in turn (two frames in flight); "
-                   "per-kernel times come from a serialised pass of the same steps",
+        "streams": "contexts on separate streams take the frames in turn (--contexts, default "
+                   "3 frames in flight); per-kernel times come from a serialised pass of the "
+                   "same steps",
         "parallelism": "replicas only (one independent frame stream per GPU)",
         "impl": impl,
     }
@@ -247,11 +252,12 @@ def run_gpu(args):
         dist.init_process_group("nccl", device_id=dev)
     img = synthetic.config2_image()
     d_img = torch.from_numpy(img).to(dev).contiguous()
-    # two frames in flight: two contexts on two dedicated streams take the
-    # frames in turn, so one frame's kernel tails overlap the next frame's
-    streams = [torch.cuda.Stream(dev) for _ in range(2)]
+    # frames in flight: contexts on dedicated streams take the frames in
+    # turn, so one frame's kernel tails overlap the next frame's
+    nctx = max(2, args.contexts)
+    streams = [torch.cuda.Stream(dev) for _ in range(nctx)]
     torch.cuda.set_stream(streams[0])
-    ctxs = [J.FrontendContext(local) for _ in range(2)]
+    ctxs = [J.FrontendContext(local) for _ in range(nctx)]
     for c, st in zip(ctxs, streams):
         assert st.cuda_stream != 0
         c.set_stream(st.cuda_stream)
@@ -262,7 +268,7 @@ def run_gpu(args):
 
     def step():
         for cfg in cfgs:
-            ctxs[turn[0] % 2].run_device(d_img.data_ptr(), WIDTH, HEIGHT, 3, 8, cfg)
+            ctxs[turn[0] % nctx].run_device(d_img.data_ptr(), WIDTH, HEIGHT, 3, 8, cfg)
             turn[0] += 1
 
     for _ in range(max(args.warmup, 1)):
@@ -281,12 +287,15 @@ def run_gpu(args):
     elapsed_ms = 0.0
     for k in range(args.steps):
         flush.zero_()
-        start, end_b, end = ev(), ev(), ev()
+        start, end = ev(), ev()
         start.record(streams[0])
-        streams[1].wait_event(start)
+        for st in streams[1:]:
+            st.wait_event(start)
         step()
-        end_b.record(streams[1])
-        streams[0].wait_event(end_b)
+        for st in streams[1:]:
+            e_k = ev()
+            e_k.record(st)
+            streams[0].wait_event(e_k)
         end.record(streams[0])
         end.synchronize()
         elapsed_ms += start.elapsed_time(end)
@@ -503,8 +512,9 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
     fi = frame_info(WIDTH, HEIGHT)
     h_img = torch.empty(img.size, dtype=torch.uint8, pin_memory=True)
     h_img.numpy()[:] = img.reshape(-1)
-    ctxs = [J.FrontendContext(dev.index or 0) for _ in range(2)]
-    outs = [J.PinnedOutputs(WIDTH, HEIGHT) for _ in range(2)]
+    nctx = max(1, args.e2e_contexts)
+    ctxs = [J.FrontendContext(dev.index or 0) for _ in range(nctx)]
+    outs = [J.PinnedOutputs(WIDTH, HEIGHT) for _ in range(nctx)]
     for o in outs:  # the strategy map is filled on the host; the rest is downloaded
         o.c.ac_strategy = None
     c_cfgs = [c._c() for c in cfgs]
@@ -512,7 +522,7 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
     nt = fi.xsize_tiles * fi.ysize_tiles
     fixed_d2h = (nb + 2 * nt + 6 * nb + (fi.num_groups + 1) * 8
                  + L.NUM_FINE_AC_CONTEXTS * L.ALPHABET_SIZE * 4)
-    state = {"pending": [False, False], "d2h": 0, "k": 0}
+    state = {"pending": [False] * nctx, "d2h": 0, "k": 0}
 
     def finish(slot):
         if state["pending"][slot]:
@@ -524,7 +534,7 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
 
     def step():
         for c in c_cfgs:
-            slot = state["k"] % 2
+            slot = state["k"] % nctx
             state["k"] += 1
             finish(slot)
             st = lib.jxg_frontend_enqueue(ctxs[slot].handle, ctypes.c_void_p(h_img.data_ptr()),
@@ -536,8 +546,8 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
 
     for _ in range(max(args.warmup, 1)):
         step()
-    finish(0)
-    finish(1)
+    for slot in range(nctx):
+        finish(slot)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
@@ -545,8 +555,8 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         step()
-    finish(0)
-    finish(1)
+    for slot in range(nctx):
+        finish(slot)
     torch.cuda.synchronize(dev)
     dt = time.perf_counter() - t0
     dt = max_over_ranks(dt, dev)
@@ -555,9 +565,9 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
     value = world * args.steps * len(QUALITIES) * WIDTH * HEIGHT / 1e6 / dt
     return {"value": value, "unit": "MP/s", "h2d_bytes_per_step": len(QUALITIES) * img.size,
             "d2h_bytes_per_step": int(state["d2h"] / args.steps),
-            "path": "jxg_frontend_enqueue / jxg_frontend_wait (C ABI), two contexts alternating "
-                    "frames: pinned host RGB in; maps, DC levels, tokens, group offsets and "
-                    "histograms out to pinned host memory"}
+            "path": f"jxg_frontend_enqueue / jxg_frontend_wait (C ABI), {nctx} contexts taking "
+                    "frames in turn: pinned host RGB in; maps, DC levels, tokens, group offsets "
+                    "and histograms out to pinned host memory"}
 
 
 def main():
