@@ -280,7 +280,8 @@ int32_t jxg_selftest_bounded_wait(void* ctx, uint32_t polls);
  * [lo_bits, hi_bits): `which` 0 = the cube root (XYB inputs lie in
  * [0, 0x40000000)), 1 / 2 = the AQ gamma ratio inverted / direct (inputs in
  * [0, 0x44800000)), 3 = the AQ masking square root (inputs in
- * [0, 0x3E4CCCCD]).  It returns the number of differing results and the
+ * [0, 0x3E4CCCCD]), 4 = the cube root on the packed two-lane FP32 path.
+ * It returns the number of differing results and the
  * smallest differing pattern (0xFFFFFFFF when none). */
 int32_t jxg_selftest_math(void* ctx, int32_t which, uint32_t lo_bits, uint32_t hi_bits,
                           uint64_t* mismatches, uint32_t* first_bad);

@@ -159,6 +159,7 @@ def test_repeat_runs_are_identical(ctx):
     (1, 0, 0x44800000),           # gamma ratio, inverted: [0, 1024)
     (2, 0, 0x44800000),           # gamma ratio, direct: [0, 1024)
     (3, 0, 0x3E4CCCCD + 1),       # masking square root: [0, 0.2]
+    (4, 0, 0x40000000),           # cube root, packed two-lane path: [0, 2)
 ])
 def test_fast_math_equals_ieee_on_every_input(ctx, which, lo, hi):
     # the fused sequences replacing IEEE division / sqrt on the hot paths give
