@@ -327,6 +327,18 @@ static void dct8_matrix_from(const float bands_in[3][6], float* matrix, float* i
   }
 }
 
+void orc_dct8_matrix_from_bands(const float* bands18, float* matrix, float* inv) {
+  float b[3][6];
+  for (int c = 0; c < 3; c++)
+    for (int i = 0; i < 6; i++) b[c][i] = bands18[c * 6 + i];
+  dct8_matrix_from(b, matrix, inv);
+}
+
+void orc_dct8_default_bands(float* bands18) {
+  for (int c = 0; c < 3; c++)
+    for (int i = 0; i < 6; i++) bands18[c * 6 + i] = DCT8_BANDS[c][i];
+}
+
 #include "library_dct8.inc"
 
 /* DequantMatrices::new_fast (src/quant_weights.rs:2294-2339) restricted to

@@ -264,3 +264,20 @@ def alpha_block_factors(alpha: np.ndarray, maxv: int) -> np.ndarray:
                                   ctypes.c_size_t(h), ctypes.c_uint32(maxv),
                                   out.ctypes.data_as(ctypes.c_void_p))
     return out
+
+
+def dct8_default_bands() -> np.ndarray:
+    out = np.zeros(18, np.float32)
+    lib().orc_dct8_default_bands(out.ctypes.data_as(ctypes.c_void_p))
+    return out.reshape(3, 6)
+
+
+def dct8_matrix_from_bands(bands: np.ndarray) -> np.ndarray:
+    """compute_dct8x8_matrix of (3, 6) band parameters: (3, 64) weights."""
+    b = np.ascontiguousarray(bands, np.float32).reshape(18)
+    m = np.zeros(192, np.float32)
+    inv = np.zeros(192, np.float32)
+    lib().orc_dct8_matrix_from_bands(b.ctypes.data_as(ctypes.c_void_p),
+                                     m.ctypes.data_as(ctypes.c_void_p),
+                                     inv.ctypes.data_as(ctypes.c_void_p))
+    return m.reshape(3, 64)

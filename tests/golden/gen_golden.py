@@ -13,7 +13,10 @@ constant tables and asserted values that its own unit tests pin:
   - the high words of the fast_exp2 table (src/adaptive_quant.rs:732-737);
   - quality->distance anchors (src/encode_image.rs:5758-5771);
   - hybrid-uint boundaries and pack_signed values (src/entropy/token.rs tests);
-  - dirty_log2f on powers of two (src/adaptive_quant.rs:896-902).
+  - dirty_log2f on powers of two (src/adaptive_quant.rs:896-902);
+  - the DCT8 band parameters and the static DCT8 dequant table they must
+    reproduce within 2e-6 (src/quant_weights.rs:123-128, :246,
+    `dct8_matrix_from_bands_matches_static` :3367-3390).
 The output is tests/golden/reference_tables.json.
 """
 from __future__ import annotations
@@ -32,6 +35,20 @@ def _array(src: str, name: str) -> list[int]:
     return [int(v, 0) for v in re.findall(r"0x[0-9A-Fa-f]+|\d+", body)]
 
 
+def _floats(src: str, name: str) -> list[float]:
+    start = src.index(name)
+    body = src[src.index("[", src.index("=", start)) + 1:]
+    depth, end = 1, 0
+    for i, ch in enumerate(body):
+        depth += ch == "["
+        depth -= ch == "]"
+        if depth == 0:
+            end = i
+            break
+    body = re.sub(r"//[^\n]*", "", body[:end])
+    return [float(v) for v in re.findall(r"-?\d+\.\d*(?:e-?\d+)?|-?\d+e-?\d+", body)]
+
+
 def main(root: str) -> None:
     ac = open(os.path.join(root, "src/ac_context.rs")).read()
     aq = open(os.path.join(root, "src/adaptive_quant.rs")).read()
@@ -41,8 +58,14 @@ def main(root: str) -> None:
     assert len(order8) == 64 and len(freq) == 64 and len(nonzero) == 64
     exp2 = re.findall(r"\((0x[0-9A-F]+), 0x[0-9A-F]+\)", aq[aq.index("static EXP2FT"):])
     assert len(exp2) == 64
+    qw = open(os.path.join(root, "src/quant_weights.rs")).read()
+    dct8_bands = _floats(qw, "static DCT8_BANDS:")
+    dct8_static = _floats(qw, "static DEQUANT_MATRIX_8X8:")
+    assert len(dct8_bands) == 18 and len(dct8_static) == 192, (len(dct8_bands), len(dct8_static))
     out = {
         "source": "jixel 0.5.14",
+        "dct8_bands": dct8_bands,
+        "dequant_matrix_8x8": dct8_static,
         "coeff_order_8x8": order8,
         # index 0 is the DC slot (0xBAD sentinel in the reference)
         "coeff_freq_context": [None] + freq[1:],

@@ -224,3 +224,34 @@ def test_alpha_factors_follow_each_blocks_largest_alpha():
     assert abs(f[0, 2] - 0.1) < 1e-6
     a[3, 12] = 128
     assert abs(O.alpha_block_factors(a, 255)[0, 1] - 128.0 / 255.0) < 1e-6
+
+
+def test_dct8_bands_and_matrix_match_the_static_table():
+    # src/quant_weights.rs:3367-3390: the band parameters reproduce the
+    # static DCT8 table within 2e-6 relative
+    bands = np.array(GOLD["dct8_bands"], np.float32).reshape(3, 6)
+    assert np.array_equal(O.dct8_default_bands(), bands)
+    got = O.dct8_matrix_from_bands(bands)
+    want = np.array(GOLD["dequant_matrix_8x8"], np.float32).reshape(3, 64)
+    assert np.all(np.abs(got - want) <= 2e-6 * np.abs(want))
+
+
+def test_fast_tables_flat_b_row_above_the_ss2_distance():
+    # src/quant_weights.rs:3350-3364: new_fast's B row starts at 512 from d = 2.25;
+    # its DC weight is 1 / 512 in the decoded table
+    for d in [2.25, 3.0, 3.5, 5.0]:
+        m, _ = O.dct8_tables(d)
+        assert m[2][0] == np.float32(1.0) / np.float32(512.0)
+
+
+def test_oracle_is_thread_invariant():
+    # src/encode_image.rs:6602 (thread invariance): the fan-out over DC
+    # groups, tiles and AC groups does not change any output
+    from jixel_gb300 import synthetic
+    img = synthetic.generate(600, 300, 77, rectangles=10, alpha=True)
+    a = O.frontend(img, 1.0, num_threads=1)
+    b = O.frontend(img, 1.0, num_threads=4)
+    for k in ("quant_field", "ytox", "ytob", "quant_dc", "coeffs", "nzeros", "tokens",
+              "group_offsets", "histograms", "alpha"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
+    assert np.array_equal(a.xyb.view(np.uint32), b.xyb.view(np.uint32))
