@@ -1082,6 +1082,18 @@ static uint32_t qf_threshold_of(const uint8_t* qf, size_t n) {
   return 1;
 }
 
+/* compute_cmap_tile on the tile at blocks (0, 0) of an XYB image (3 planes
+ * of w*h), for known-answer tests. */
+int orc_cmap_tile0(const float* xyb, size_t w, size_t h, float distance, int8_t* ytox,
+                   int8_t* ytob) {
+  float mat[192], inv[192];
+  int st = orc_dct8_tables(distance, mat, inv);
+  if (st) return st;
+  size_t xb = (w + 7) / 8, yb = (h + 7) / 8;
+  cmap_tile(xyb, w, h, 0, 0, minz(8, xb), minz(8, yb), distance, inv, inv + 128, ytox, ytob);
+  return ORC_OK;
+}
+
 /* ------------------------------------------------------------------ */
 /* Alpha: fringe clearing, invisible fill, AQ factors                   */
 /* ------------------------------------------------------------------ */

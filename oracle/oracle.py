@@ -281,3 +281,21 @@ def dct8_matrix_from_bands(bands: np.ndarray) -> np.ndarray:
                                      m.ctypes.data_as(ctypes.c_void_p),
                                      inv.ctypes.data_as(ctypes.c_void_p))
     return m.reshape(3, 64)
+
+
+def cmap_tile0(xyb: np.ndarray, distance: float) -> tuple[int, int]:
+    """compute_cmap_tile of the first 64x64 tile of (3, h, w) XYB planes."""
+    x = np.ascontiguousarray(xyb, np.float32)
+    _, h, w = x.shape
+    ytox, ytob = ctypes.c_int8(), ctypes.c_int8()
+    st = lib().orc_cmap_tile0(x.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(w),
+                              ctypes.c_size_t(h), ctypes.c_float(distance), ctypes.byref(ytox),
+                              ctypes.byref(ytob))
+    assert st == 0
+    return ytox.value, ytob.value
+
+
+def srgb_lut() -> np.ndarray:
+    out = np.zeros(256, np.float32)
+    lib().orc_srgb_lut(out.ctypes.data_as(ctypes.c_void_p))
+    return out

@@ -255,3 +255,21 @@ def test_oracle_is_thread_invariant():
               "group_offsets", "histograms", "alpha"):
         assert np.array_equal(getattr(a, k), getattr(b, k)), k
     assert np.array_equal(a.xyb.view(np.uint32), b.xyb.view(np.uint32))
+
+
+def test_cfl_perfectly_correlated_chroma_finds_the_slope():
+    # src/color_correlation.rs:2335-2357: X = 0.3 Y gives ytox ~ 25, B = Y ytob ~ 0
+    y, x = np.mgrid[0:64, 0:64]
+    v = ((x ^ y).astype(np.float32) / np.float32(64.0)).astype(np.float32)
+    xyb = np.stack([np.float32(0.3) * v, v, v]).astype(np.float32)
+    ytox, ytob = O.cmap_tile0(xyb, 2.0)
+    assert abs(ytox - 25) < 3, ytox
+    assert abs(ytob) < 3, ytob
+
+
+def test_srgb_lut_is_the_reference_formula():
+    # src/color.rs:35-42 (lut_matches_reference :628): f64 sRGB EOTF of v / 255
+    # (v * (1 / 255.0)), rounded once to f32
+    v = np.arange(256, dtype=np.float64) * (1.0 / 255.0)
+    want = np.where(v <= 0.04045, v / 12.92, ((v + 0.055) / 1.055) ** 2.4).astype(np.float32)
+    assert np.array_equal(O.srgb_lut().view(np.uint32), want.view(np.uint32))
