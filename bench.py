@@ -50,6 +50,8 @@ def parse_args():
                    help="contexts (one stream each) the device-resident run alternates frames over")
     p.add_argument("--e2e-contexts", type=int, default=3,
                    help="contexts the end-to-end run alternates frames over")
+    p.add_argument("--e2e-wide-tokens", action="store_true",
+                   help="download (context, value) token pairs instead of packed AcToken words")
     p.add_argument("--c5", action="store_true",
                    help="also time one 8192x8192 RGB16 linear frame at q85 per step")
     return p.parse_args()
@@ -497,9 +499,10 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
     """End to end through the public C ABI: every frame is uploaded from
     pinned host memory and its outputs (maps, DC levels, tokens, group
     offsets, histograms) land in pinned host memory, all inside the timed
-    region.  The caller pipelines frames over two contexts with
-    jxg_frontend_enqueue / jxg_frontend_wait, so one frame's transfers
-    overlap the other's kernels."""
+    region.  Tokens come in the groups' storage form (AcTokens: one word per
+    token), or as (context, value) pairs with --e2e-wide-tokens.  The caller
+    pipelines frames over several contexts with jxg_frontend_enqueue /
+    jxg_frontend_wait, so one frame's transfers overlap another's kernels."""
     import ctypes
 
     import torch
@@ -514,7 +517,8 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
     h_img.numpy()[:] = img.reshape(-1)
     nctx = max(1, args.e2e_contexts)
     ctxs = [J.FrontendContext(dev.index or 0) for _ in range(nctx)]
-    outs = [J.PinnedOutputs(WIDTH, HEIGHT) for _ in range(nctx)]
+    packed = not args.e2e_wide_tokens
+    outs = [J.PinnedOutputs(WIDTH, HEIGHT, packed=packed) for _ in range(nctx)]
     for o in outs:  # the strategy map is filled on the host; the rest is downloaded
         o.c.ac_strategy = None
     c_cfgs = [c._c() for c in cfgs]
@@ -530,7 +534,11 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
             if st:
                 raise RuntimeError(f"jxg_frontend_wait status {st}")
             state["pending"][slot] = False
-            state["d2h"] += fixed_d2h + outs[slot].params.num_tokens * 8
+            o = outs[slot]
+            if packed:
+                state["d2h"] += fixed_d2h + int(o.packed_offsets[-1]) * 4 + (fi.num_groups + 1) * 8
+            else:
+                state["d2h"] += fixed_d2h + o.params.num_tokens * 8
 
     def step():
         for c in c_cfgs:
@@ -566,8 +574,9 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
     return {"value": value, "unit": "MP/s", "h2d_bytes_per_step": len(QUALITIES) * img.size,
             "d2h_bytes_per_step": int(state["d2h"] / args.steps),
             "path": f"jxg_frontend_enqueue / jxg_frontend_wait (C ABI), {nctx} contexts taking "
-                    "frames in turn: pinned host RGB in; maps, DC levels, tokens, group offsets "
-                    "and histograms out to pinned host memory"}
+                    "frames in turn: pinned host RGB in; maps, DC levels, tokens "
+                    f"({'packed AcToken words' if packed else 'context/value pairs'}), group "
+                    "offsets and histograms out to pinned host memory"}
 
 
 def main():

@@ -116,6 +116,15 @@ typedef struct jxg_frontend_output {
   uint32_t* histograms;    /* JXG_NUM_FINE_AC_CONTEXTS * JXG_ALPHABET_SIZE */
   uint16_t* alpha;         /* RGBA input: w*h alpha after fringe clearing (the
                               plane the extra channel codes); untouched for RGB */
+  /* The same tokens in the groups' storage form (AcTokens,
+   * src/entropy/token_stream.rs:37-76, as PendingAcGroup holds them,
+   * src/frame/ac_groups.rs:78-82): a group whose contexts all fit 14 bits
+   * and values 18 bits is one word per token, context << 18 | value; any
+   * other group is two words per token, context then value. */
+  uint32_t* packed_tokens;
+  uint64_t packed_capacity; /* words available in `packed_tokens` */
+  uint64_t* packed_offsets; /* num_groups + 1 word offsets; a group is wide when
+                               it holds twice as many words as tokens */
 } jxg_frontend_output;
 
 /* Library lifetime ---------------------------------------------------- */
@@ -232,6 +241,14 @@ int32_t jxg_op_fill_quant_field(void* ctx, const float* xyb, uint64_t width, uin
 /* DctFn<8, 8, 64> (src/dct.rs:172, scalar dct8x8 :631): `count` blocks of 64
  * row-major samples in, 64 coefficients (transposed storage, 1/64 scale) out. */
 int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coefficients);
+/* AcTokens::from (src/entropy/token_stream.rs:59-76) per group: `tokens`
+ * from group_offsets[0] to group_offsets[num_groups] (host arrays) into the
+ * storage form of jxg_frontend_output.packed_tokens; `word_offsets` gets
+ * num_groups + 1 offsets from zero.  At most `capacity` words are written;
+ * a larger stream returns JXG_ERR_INVALID_ARGUMENT after the offsets. */
+int32_t jxg_op_pack_tokens(void* ctx, const jxg_token* tokens, const uint64_t* group_offsets,
+                           uint64_t num_groups, uint32_t* words, uint64_t capacity,
+                           uint64_t* word_offsets);
 
 /* Allocation-free token offsets -----------------------------------------
  * This entry point has no counterpart in the reference encoder.  It is for

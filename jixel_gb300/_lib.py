@@ -34,6 +34,7 @@ EXPORTS = [
     "jxg_batch_destroy",
     "jxg_op_fill_quant_field",
     "jxg_op_dct8x8",
+    "jxg_op_pack_tokens",
     "jxg_token_offsets_noalloc",
     "jxg_selftest_bounded_wait",
     "jxg_selftest_math",
@@ -97,6 +98,9 @@ class FrontendOutput(ctypes.Structure):
         ("group_offsets", ctypes.c_void_p),
         ("histograms", ctypes.c_void_p),
         ("alpha", ctypes.c_void_p),
+        ("packed_tokens", ctypes.c_void_p),
+        ("packed_capacity", ctypes.c_uint64),
+        ("packed_offsets", ctypes.c_void_p),
     ]
 
 
@@ -140,6 +144,7 @@ def load() -> ctypes.CDLL:
         "jxg_batch_destroy": (None, [vp]),
         "jxg_op_fill_quant_field": (i32, [vp, vp, u64, u64, f32, f32, vp]),
         "jxg_op_dct8x8": (i32, [vp, vp, u64, vp]),
+        "jxg_op_pack_tokens": (i32, [vp, vp, vp, u64, vp, u64, vp]),
         "jxg_token_offsets_noalloc": (i32, [vp, u64, vp, vp, vp]),
         "jxg_selftest_bounded_wait": (i32, [vp, ctypes.c_uint32]),
         "jxg_selftest_math": (i32, [vp, i32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(u64),

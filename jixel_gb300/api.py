@@ -132,6 +132,8 @@ class FrontendResult:
     histograms: np.ndarray    # (14850, 128) u32
     xyb: np.ndarray | None = None
     alpha: np.ndarray | None = None  # (h, w) u16 alpha after fringe clearing (RGBA input)
+    packed_tokens: np.ndarray | None = None   # u32 words: the groups' storage form (AcTokens)
+    packed_offsets: np.ndarray | None = None  # (groups + 1,) u64 word offsets
 
 
 def _pixels_kind(pixels: np.ndarray) -> tuple[int, int]:
@@ -151,8 +153,30 @@ def _params_dict(p) -> dict:
     return out
 
 
+def unpack_tokens(words: np.ndarray, word_offsets: np.ndarray,
+                  group_offsets: np.ndarray) -> np.ndarray:
+    """(n, 2) context/value tokens from the groups' storage form
+    (AcToken::unpack, src/entropy/token_stream.rs:44-48): a group with as
+    many words as tokens is packed (context << 18 | value), one with twice
+    as many holds (context, value) pairs."""
+    out = np.zeros((int(group_offsets[-1] - group_offsets[0]), 2), np.uint32)
+    base = int(group_offsets[0])
+    for g in range(len(group_offsets) - 1):
+        t0, t1 = int(group_offsets[g]) - base, int(group_offsets[g + 1]) - base
+        w0, w1 = int(word_offsets[g]), int(word_offsets[g + 1])
+        w = words[w0:w1]
+        if w1 - w0 == t1 - t0:
+            out[t0:t1, 0] = w >> 18
+            out[t0:t1, 1] = w & 0x3FFFF
+        elif w1 - w0 == 2 * (t1 - t0):
+            out[t0:t1] = w.reshape(-1, 2)
+        else:
+            raise ValueError(f"group {g}: {w1 - w0} words for {t1 - t0} tokens")
+    return out
+
+
 def _result_buffers(p: dict, width: int, height: int, coefficients: bool, xyb: bool,
-                    alpha: bool = False):
+                    alpha: bool = False, packed: bool = False):
     """Host arrays for every output of one frame and the C struct pointing at them."""
     fi = frame_info(width, height)
     xb, yb = fi.xsize_blocks, fi.ysize_blocks
@@ -170,6 +194,8 @@ def _result_buffers(p: dict, width: int, height: int, coefficients: bool, xyb: b
         histograms=np.zeros((L.NUM_FINE_AC_CONTEXTS, L.ALPHABET_SIZE), np.uint32),
         xyb=np.zeros((3, height, width), np.float32) if xyb else None,
         alpha=np.zeros((height, width), np.uint16) if alpha else None,
+        packed_tokens=np.zeros(max(2 * int(p["num_tokens"]), 1), np.uint32) if packed else None,
+        packed_offsets=np.zeros(fi.num_groups + 1, np.uint64) if packed else None,
     )
     o = L.FrontendOutput()
     o.quant_field = r.quant_field.ctypes.data
@@ -185,7 +211,18 @@ def _result_buffers(p: dict, width: int, height: int, coefficients: bool, xyb: b
     o.group_offsets = r.group_offsets.ctypes.data
     o.histograms = r.histograms.ctypes.data
     o.alpha = r.alpha.ctypes.data if alpha else None
+    if packed:
+        o.packed_tokens = r.packed_tokens.ctypes.data
+        o.packed_capacity = r.packed_tokens.shape[0]
+        o.packed_offsets = r.packed_offsets.ctypes.data
     return r, o
+
+
+def _trim(r: FrontendResult) -> FrontendResult:
+    r.tokens = r.tokens[: int(r.params["num_tokens"])]
+    if r.packed_tokens is not None:
+        r.packed_tokens = r.packed_tokens[: int(r.packed_offsets[-1])]
+    return r
 
 
 class FrontendContext:
@@ -245,12 +282,11 @@ class FrontendContext:
         return _params_dict(p)
 
     def fetch(self, width: int, height: int, *, coefficients: bool = True,
-              xyb: bool = False, alpha: bool = False) -> FrontendResult:
+              xyb: bool = False, alpha: bool = False, packed: bool = False) -> FrontendResult:
         p = self.params()
-        r, o = _result_buffers(p, width, height, coefficients, xyb, alpha)
+        r, o = _result_buffers(p, width, height, coefficients, xyb, alpha, packed)
         self._check(self._lib.jxg_frontend_fetch(self._ctx, ctypes.byref(o)))
-        r.tokens = r.tokens[: int(p["num_tokens"])]
-        return r
+        return _trim(r)
 
     def enqueue(self, pixels: np.ndarray, config: EncodeConfig, out: "PinnedOutputs"):
         """Asynchronous front end (jxg_frontend_enqueue): `pixels` and `out`
@@ -270,10 +306,10 @@ class FrontendContext:
         return FrontendBatch(self, pixels_on_device)
 
     def frontend(self, pixels: np.ndarray, config: EncodeConfig, *, coefficients: bool = True,
-                 xyb: bool = False) -> FrontendResult:
+                 xyb: bool = False, packed: bool = False) -> FrontendResult:
         self.run(pixels, config)
         return self.fetch(pixels.shape[1], pixels.shape[0], coefficients=coefficients, xyb=xyb,
-                          alpha=pixels.shape[2] == 4)
+                          alpha=pixels.shape[2] == 4, packed=packed)
 
     # operator table -----------------------------------------------------
     def fill_quant_field(self, xyb: np.ndarray, distance: float, inv_scale: float) -> np.ndarray:
@@ -291,6 +327,20 @@ class FrontendContext:
         self._check(self._lib.jxg_op_dct8x8(self._ctx, blocks.ctypes.data, blocks.shape[0],
                                             out.ctypes.data))
         return out
+
+    def pack_tokens(self, tokens: np.ndarray, group_offsets: np.ndarray
+                    ) -> tuple[np.ndarray, np.ndarray]:
+        """AcTokens::from per group (src/entropy/token_stream.rs:59-76) on the
+        device: (words, word offsets) of the groups' storage form."""
+        tokens = np.ascontiguousarray(tokens, np.uint32).reshape(-1, 2)
+        goffs = np.ascontiguousarray(group_offsets, np.uint64)
+        n = int(goffs[-1] - goffs[0])
+        words = np.zeros(max(2 * n, 1), np.uint32)
+        woffs = np.zeros(goffs.shape[0], np.uint64)
+        self._check(self._lib.jxg_op_pack_tokens(
+            self._ctx, tokens.ctypes.data if tokens.size else None, goffs.ctypes.data,
+            goffs.shape[0] - 1, words.ctypes.data, words.shape[0], woffs.ctypes.data))
+        return words[: int(woffs[-1])], woffs
 
     # timing -------------------------------------------------------------
     def enable_kernel_timing(self, on: bool = True):
@@ -312,10 +362,13 @@ class FrontendContext:
 
 class PinnedOutputs:
     """Pinned host buffers for every output of one width x height frame, for
-    FrontendContext.enqueue (allocated with torch's pinned allocator)."""
+    FrontendContext.enqueue (allocated with torch's pinned allocator).  With
+    `packed` the tokens come in the groups' storage form only (one word per
+    token unless a group holds values of 2^18 or more; room for max_tokens
+    words)."""
 
     def __init__(self, width: int, height: int, *, channels: int = 3, coefficients: bool = False,
-                 xyb: bool = False):
+                 xyb: bool = False, packed: bool = False):
         import torch
 
         fi = frame_info(width, height)
@@ -333,7 +386,10 @@ class PinnedOutputs:
         self.quant_dc = pin((3, yb, xb), torch.int16)
         self.coefficients = pin((yb, xb, 3, 64), torch.int32) if coefficients else None
         self.num_nzeros = pin((3, yb, xb), torch.uint8)
-        self.tokens = pin((fi.max_tokens, 2), torch.int32).view(np.uint32)
+        self.tokens = None if packed else pin((fi.max_tokens, 2), torch.int32).view(np.uint32)
+        self.packed_tokens = pin((fi.max_tokens,), torch.int32).view(np.uint32) if packed else None
+        self.packed_offsets = (pin((fi.num_groups + 1,), torch.int64).view(np.uint64)
+                               if packed else None)
         self.group_offsets = pin((fi.num_groups + 1,), torch.int64).view(np.uint64)
         self.histograms = pin((L.NUM_FINE_AC_CONTEXTS, L.ALPHABET_SIZE), torch.int32).view(np.uint32)
         self.xyb = pin((3, height, width), torch.float32) if xyb else None
@@ -348,8 +404,13 @@ class PinnedOutputs:
         o.coefficients = self.coefficients.ctypes.data if coefficients else None
         o.num_nzeros = self.num_nzeros.ctypes.data
         o.xyb = self.xyb.ctypes.data if xyb else None
-        o.tokens = self.tokens.ctypes.data
-        o.token_capacity = fi.max_tokens
+        if packed:
+            o.packed_tokens = self.packed_tokens.ctypes.data
+            o.packed_capacity = fi.max_tokens
+            o.packed_offsets = self.packed_offsets.ctypes.data
+        else:
+            o.tokens = self.tokens.ctypes.data
+            o.token_capacity = fi.max_tokens
         o.group_offsets = self.group_offsets.ctypes.data
         o.histograms = self.histograms.ctypes.data
         o.alpha = self.alpha.ctypes.data if self.alpha is not None else None
@@ -363,10 +424,14 @@ class PinnedOutputs:
             params=p, quant_field=self.quant_field.copy(), ac_strategy=self.ac_strategy.copy(),
             ytox=self.ytox.copy(), ytob=self.ytob.copy(), quant_dc=self.quant_dc.copy(),
             coefficients=None if self.coefficients is None else self.coefficients.copy(),
-            num_nzeros=self.num_nzeros.copy(), tokens=self.tokens[:n].copy(),
+            num_nzeros=self.num_nzeros.copy(),
+            tokens=None if self.tokens is None else self.tokens[:n].copy(),
             group_offsets=self.group_offsets.copy(), histograms=self.histograms.copy(),
             xyb=None if self.xyb is None else self.xyb.copy(),
-            alpha=None if self.alpha is None else self.alpha.copy())
+            alpha=None if self.alpha is None else self.alpha.copy(),
+            packed_tokens=(None if self.packed_tokens is None
+                           else self.packed_tokens[: int(self.packed_offsets[-1])].copy()),
+            packed_offsets=None if self.packed_offsets is None else self.packed_offsets.copy())
 
 
 class FrontendBatch:
@@ -428,13 +493,13 @@ class FrontendBatch:
         self._check(self._lib.jxg_batch_result(self._b, index, ctypes.byref(p), None))
         return _params_dict(p)
 
-    def result(self, index: int, *, coefficients: bool = True, xyb: bool = False) -> FrontendResult:
+    def result(self, index: int, *, coefficients: bool = True, xyb: bool = False,
+               packed: bool = False) -> FrontendResult:
         w, h, ch = self._sizes[index]
         p = self.params(index)
-        r, o = _result_buffers(p, w, h, coefficients, xyb, ch == 4)
+        r, o = _result_buffers(p, w, h, coefficients, xyb, ch == 4, packed)
         self._check(self._lib.jxg_batch_result(self._b, index, None, ctypes.byref(o)))
-        r.tokens = r.tokens[: int(p["num_tokens"])]
-        return r
+        return _trim(r)
 
 
 def encode_frontend(pixels: np.ndarray, config: EncodeConfig, device: int = 0) -> FrontendResult:

@@ -87,7 +87,8 @@ struct Context {
   // pass buffers (grown, never shrunk)
   DevBuf pixels, xyb, qf, ytox, ytob, quant_dc, levels, wide_levels, coeffs, nzeros, nz_packed,
       counts, offsets, chunks, tokens, hist, stats, group_offsets, plan, total, op_in, op_out,
-      alpha, alpha_peak, alpha_zero, fill_flags, fill_deps, fill_queue;
+      alpha, alpha_peak, alpha_zero, fill_flags, fill_deps, fill_queue, group_wide, packed,
+      packed_offs;
   HostBuf plan_host, pixels_host;
   // The plan (frame descriptors + chunk prefixes) lives in a ring of slots,
   // pinned on the host and mirrored on the device, so a pass can be planned
@@ -115,7 +116,7 @@ struct Context {
   struct AsyncSlot {
     DeviceStats stats;
     uint64_t token_count;
-    uint64_t pad;
+    uint64_t packed_count;  // words of the group storage form
   };
   HostBuf async_slot;                  // pinned AsyncSlot the pass's scalars land in
   bool async_pending = false;
@@ -375,6 +376,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
       (st = ensure(c, c->hist, n * kHistBytes)) ||
       (st = ensure(c, c->stats, n * sizeof(DeviceStats))) ||
       (st = ensure(c, c->group_offsets, (groups + 1) * 8)) || (st = ensure(c, c->total, 256)) ||
+      (st = ensure(c, c->group_wide, (groups + 1) * 4)) ||
       (alpha_px && (st = ensure(c, c->alpha, alpha_px * 2))) ||
       (alpha_blocks && (st = ensure(c, c->alpha_peak, alpha_blocks * 2))) ||
       (alpha_blocks && (st = ensure(c, c->alpha_zero, alpha_blocks))) ||
@@ -427,6 +429,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     f.offsets = static_cast<uint32_t*>(c->offsets.ptr) + L.count_off;
     f.histograms = reinterpret_cast<uint32_t*>(static_cast<char*>(c->hist.ptr) + i * kHistBytes);
     f.stats = static_cast<DeviceStats*>(c->stats.ptr) + i;
+    f.group_wide = static_cast<uint32_t*>(c->group_wide.ptr) + L.group_off;
     if (L.has_alpha) {
       f.alpha = static_cast<uint16_t*>(c->alpha.ptr) + L.alpha_off;
       f.alpha_peak = static_cast<uint16_t*>(c->alpha_peak.ptr) + L.alpha_block_off;
@@ -587,7 +590,8 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
                                                    goffs, static_cast<int>(c->total_groups));
        })) ||
       (st = launch(c, "k_scan_apply", timed, [&] {
-         k_scan_apply<<<nchunks, kScanThreads, 0, s>>>(counts, ncounts, chunks, offs, goffs, 4 * 1024);
+         k_scan_apply<<<nchunks, kScanThreads, 0, s>>>(counts, ncounts, chunks, offs, goffs, 4 * 1024,
+                                                      static_cast<uint32_t*>(c->group_wide.ptr));
        })) ||
       (st = single ? launch(c, "k_tokenize", timed, [&] {
          k_tokenize<<<static_cast<unsigned>(c->token_chunks), kTokThreads, 0, s>>>(
@@ -741,6 +745,52 @@ int enqueue_fixed_downloads(Context* c, int index, const jxg_frontend_output* ou
   return JXG_OK;
 }
 
+// k_pack_tokens over frame `L` of the last pass (see the kernel).
+constexpr int kPackCtasPerGroup = 8;
+int launch_pack(Context* c, int index, uint32_t* words, uint64_t capacity, uint64_t* word_offsets,
+                uint64_t* count_out) {
+  const FrameLayout& L = c->layouts[index];
+  const int groups = static_cast<int>(L.info.num_groups);
+  const dim3 grid(kPackCtasPerGroup, static_cast<unsigned>(std::min(groups, 65535)));
+  cudaStream_t s = c->stream;
+  return launch(c, "k_pack_tokens", c->timing, [&] {
+    k_pack_tokens<<<grid, 256, 0, s>>>(
+        static_cast<const uint2*>(c->tokens.ptr),
+        static_cast<const uint64_t*>(c->group_offsets.ptr) + L.group_off,
+        static_cast<const uint32_t*>(c->group_wide.ptr) + L.group_off,
+        &(static_cast<const DeviceStats*>(c->stats.ptr) + index)->any_wide, groups, words, capacity,
+        word_offsets, count_out);
+  });
+}
+
+// The group storage form of frame `index` into host memory through a device
+// staging buffer (the caller's memory may be pageable).
+int fetch_packed(Context* c, int index, uint64_t num_tokens, jxg_frontend_output* out) {
+  const FrameLayout& L = c->layouts[index];
+  const uint64_t groups = L.info.num_groups;
+  const uint64_t cap = 2 * num_tokens;  // every group wide
+  int st;
+  if ((st = ensure(c, c->packed, std::max<uint64_t>(cap, 1) * 4)) ||
+      (st = ensure(c, c->packed_offs, (groups + 2) * 8)))
+    return st;
+  uint64_t* offs = static_cast<uint64_t*>(c->packed_offs.ptr);
+  if ((st = launch_pack(c, index, out->packed_tokens ? static_cast<uint32_t*>(c->packed.ptr) : nullptr,
+                        cap, offs, offs + groups + 1)))
+    return st;
+  uint64_t words = 0;
+  JXG_CUDA(c, cudaMemcpyAsync(&words, offs + groups + 1, 8, cudaMemcpyDeviceToHost, c->stream));
+  if ((st = wait(c))) return st;
+  if (out->packed_tokens && words > out->packed_capacity)
+    return fail(c, JXG_ERR_INVALID_ARGUMENT, "packed token buffer too small");
+  if (out->packed_tokens && words)
+    JXG_CUDA(c, cudaMemcpyAsync(out->packed_tokens, c->packed.ptr, words * 4, cudaMemcpyDeviceToHost,
+                                c->stream));
+  if (out->packed_offsets)
+    JXG_CUDA(c, cudaMemcpyAsync(out->packed_offsets, offs, (groups + 1) * 8, cudaMemcpyDeviceToHost,
+                                c->stream));
+  return JXG_OK;
+}
+
 int fetch_frame(Context* c, int index, jxg_frontend_output* out) {
   jxg_frame_params p;
   int st = read_params(c, index, &p);
@@ -764,6 +814,9 @@ int fetch_frame(Context* c, int index, jxg_frontend_output* out) {
       (st = copy(out->tokens, static_cast<uint2*>(c->tokens.ptr) + first, p.num_tokens * sizeof(jxg_token))) ||
       (st = copy(out->group_offsets, static_cast<uint64_t*>(c->group_offsets.ptr) + L.group_off,
                  (fi.num_groups + 1) * 8)))
+    return st;
+  if ((out->packed_tokens || out->packed_offsets) &&
+      (st = fetch_packed(c, index, p.num_tokens, out)))
     return st;
   if ((st = wait(c))) return st;
   if (out->group_offsets)  // frame-local token offsets
@@ -886,7 +939,8 @@ void jxg_context_destroy(void* ctx) {
                          &c->offsets, &c->chunks, &c->tokens, &c->hist, &c->stats,
                          &c->group_offsets, &c->plan, &c->total, &c->op_in, &c->op_out,
                          &c->alpha, &c->alpha_peak, &c->alpha_zero, &c->fill_flags,
-                         &c->fill_deps, &c->fill_queue})
+                         &c->fill_deps, &c->fill_queue, &c->group_wide, &c->packed,
+                         &c->packed_offs})
     if (b->ptr) cudaFree(b->ptr);
   for (jxg::HostBuf* b : {&c->plan_host, &c->pixels_host, &c->async_slot})
     if (b->ptr) cudaFreeHost(b->ptr);
@@ -987,6 +1041,8 @@ int32_t jxg_frontend_wait(void* ctx) {
   const jxg_frontend_output& out = c->async_out;
   if (out.tokens && slot->token_count > out.token_capacity)
     return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "token buffer too small");
+  if (out.packed_tokens && slot->packed_count > out.packed_capacity)
+    return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "packed token buffer too small");
   if (out.ac_strategy)
     std::memset(out.ac_strategy, 1, L.info.xsize_blocks * L.info.ysize_blocks);
   return JXG_OK;
@@ -1004,15 +1060,22 @@ int32_t jxg_frontend_enqueue(void* ctx, const void* pixels, uint64_t width, uint
   if (out) o = *out;
   void* tok_dev = nullptr;
   void* off_dev = nullptr;
+  void* words_dev = nullptr;
+  void* woff_dev = nullptr;
   if ((st = jxg::device_view(c, o.tokens, &tok_dev)) ||
       (st = jxg::device_view(c, o.group_offsets, &off_dev)) ||
+      (st = jxg::device_view(c, o.packed_tokens, &words_dev)) ||
+      (st = jxg::device_view(c, o.packed_offsets, &woff_dev)) ||
       (st = jxg::ensure_host(c, c->async_slot, sizeof(Context::AsyncSlot))))
     return st;
   if ((st = jxg::single_pass(c, pixels, width, height, channels, bits, config, false))) return st;
   const jxg::FrameLayout& L = c->layouts[0];
   auto* slot = static_cast<Context::AsyncSlot*>(c->async_slot.ptr);
   void* slot_count_dev = nullptr;
-  if ((st = jxg::device_view(c, &slot->token_count, &slot_count_dev))) return st;
+  void* slot_words_dev = nullptr;
+  if ((st = jxg::device_view(c, &slot->token_count, &slot_count_dev)) ||
+      (st = jxg::device_view(c, &slot->packed_count, &slot_words_dev)))
+    return st;
   cudaStream_t s = c->stream;
   if ((st = jxg::enqueue_fixed_downloads(c, 0, &o))) return st;
   JXG_CUDA(c, cudaMemcpyAsync(&slot->stats, c->stats.ptr, sizeof(jxg::DeviceStats),
@@ -1027,6 +1090,13 @@ int32_t jxg_frontend_enqueue(void* ctx, const void* pixels, uint64_t width, uint
         static_cast<uint64_t*>(slot_count_dev));
   });
   if (st) return st;
+  slot->packed_count = 0;
+  if ((o.packed_tokens || o.packed_offsets) &&
+      (st = jxg::launch_pack(c, 0, static_cast<uint32_t*>(words_dev),
+                             o.packed_tokens ? o.packed_capacity : 0,
+                             static_cast<uint64_t*>(woff_dev),
+                             static_cast<uint64_t*>(slot_words_dev))))
+    return st;
   c->async_pending = true;
   c->async_params = params;
   c->async_out = o;
@@ -1214,6 +1284,64 @@ int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coe
   });
   if (st) return st;
   JXG_CUDA(c, cudaMemcpyAsync(coefficients, c->op_out.ptr, bytes, cudaMemcpyDeviceToHost, s));
+  return jxg::wait(c);
+}
+
+int32_t jxg_op_pack_tokens(void* ctx, const jxg_token* tokens, const uint64_t* group_offsets,
+                           uint64_t num_groups, uint32_t* words, uint64_t capacity,
+                           uint64_t* word_offsets) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !group_offsets || num_groups == 0 || num_groups > 0x7FFFFFFFull)
+    return JXG_ERR_INVALID_ARGUMENT;
+  for (uint64_t g = 0; g < num_groups; ++g)
+    if (group_offsets[g + 1] < group_offsets[g]) return JXG_ERR_INVALID_ARGUMENT;
+  const uint64_t first = group_offsets[0];
+  const uint64_t n = group_offsets[num_groups] - first;
+  if (n && !tokens) return JXG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(c->device);
+  const size_t tok_bytes = (n * 8 + 15) / 16 * 16, off_bytes = (num_groups + 1) * 8;
+  const size_t flag_bytes = (num_groups * 4 + 15) / 16 * 16;
+  const uint64_t cap = std::min<uint64_t>(capacity, 2 * n);
+  int st;
+  if ((st = jxg::ensure(c, c->op_in, tok_bytes + off_bytes + flag_bytes)) ||
+      (st = jxg::ensure(c, c->op_out, (cap * 4 + 15) / 16 * 16 + off_bytes + 8)))
+    return st;
+  char* in = static_cast<char*>(c->op_in.ptr);
+  uint2* d_tok = reinterpret_cast<uint2*>(in);
+  uint64_t* d_goffs = reinterpret_cast<uint64_t*>(in + tok_bytes);
+  uint32_t* d_wide = reinterpret_cast<uint32_t*>(in + tok_bytes + off_bytes);
+  char* outp = static_cast<char*>(c->op_out.ptr);
+  uint32_t* d_words = reinterpret_cast<uint32_t*>(outp);
+  uint64_t* d_woffs = reinterpret_cast<uint64_t*>(outp + (cap * 4 + 15) / 16 * 16);
+  uint64_t* d_count = d_woffs + num_groups + 1;
+  cudaStream_t s = c->stream;
+  if (n) JXG_CUDA(c, cudaMemcpyAsync(d_tok, tokens + first, n * 8, cudaMemcpyHostToDevice, s));
+  std::vector<uint64_t> rebased(group_offsets, group_offsets + num_groups + 1);
+  for (uint64_t& o : rebased) o -= first;
+  JXG_CUDA(c, cudaMemcpyAsync(d_goffs, rebased.data(), off_bytes, cudaMemcpyHostToDevice, s));
+  JXG_CUDA(c, cudaMemsetAsync(d_wide, 0, num_groups * 4, s));
+  const dim3 grid(jxg::kPackCtasPerGroup, static_cast<unsigned>(std::min<uint64_t>(num_groups, 65535)));
+  if ((st = jxg::launch(c, "k_token_group_flags", c->timing, [&] {
+         jxg::k_token_group_flags<<<grid, 256, 0, s>>>(d_tok, d_goffs, static_cast<int>(num_groups),
+                                                       d_wide);
+       })) ||
+      (st = jxg::launch(c, "k_pack_tokens", c->timing, [&] {
+         jxg::k_pack_tokens<<<grid, 256, 0, s>>>(d_tok, d_goffs, d_wide, nullptr,
+                                                 static_cast<int>(num_groups),
+                                                 words ? d_words : nullptr, cap, d_woffs, d_count);
+       })))
+    return st;
+  uint64_t count = 0;
+  JXG_CUDA(c, cudaMemcpyAsync(&count, d_count, 8, cudaMemcpyDeviceToHost, s));
+  if ((st = jxg::wait(c))) return st;
+  if (word_offsets)
+    JXG_CUDA(c, cudaMemcpyAsync(word_offsets, d_woffs, off_bytes, cudaMemcpyDeviceToHost, s));
+  if (words && count > capacity) {
+    if ((st = jxg::wait(c))) return st;
+    return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "packed token buffer too small");
+  }
+  if (words && count)
+    JXG_CUDA(c, cudaMemcpyAsync(words, d_words, count * 4, cudaMemcpyDeviceToHost, s));
   return jxg::wait(c);
 }
 

@@ -299,3 +299,40 @@ def srgb_lut() -> np.ndarray:
     out = np.zeros(256, np.float32)
     lib().orc_srgb_lut(out.ctypes.data_as(ctypes.c_void_p))
     return out
+
+
+# AcToken storage (src/entropy/token_stream.rs:32-48): 14 context bits over
+# 18 value bits in one u32.
+PACKED_VALUE_BITS = 18
+PACKED_MAX_VALUE = (1 << PACKED_VALUE_BITS) - 1
+PACKED_MAX_CONTEXT = (1 << (32 - PACKED_VALUE_BITS)) - 1
+
+
+def ac_tokens_from(tokens: np.ndarray, group_offsets: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """`AcTokens::from` (src/entropy/token_stream.rs:59-76) applied to each
+    group's tokens, as `process_ac_group` stores them
+    (src/frame/ac_groups.rs:243): a group whose OR of contexts is at most
+    PACKED_MAX_CONTEXT and OR of values at most PACKED_MAX_VALUE becomes one
+    word per token (context << 18 | value); any other group keeps its
+    (context, value) pairs.  Returns the concatenated words and the groups'
+    word offsets (from zero)."""
+    tokens = np.asarray(tokens, np.uint32).reshape(-1, 2)
+    goffs = np.asarray(group_offsets, np.uint64)
+    base = int(goffs[0])
+    parts, woffs = [], [0]
+    for g in range(len(goffs) - 1):
+        t = tokens[int(goffs[g]) - base:int(goffs[g + 1]) - base]
+        ctx_or = int(np.bitwise_or.reduce(t[:, 0])) if len(t) else 0
+        val_or = int(np.bitwise_or.reduce(t[:, 1])) if len(t) else 0
+        if ctx_or <= PACKED_MAX_CONTEXT and val_or <= PACKED_MAX_VALUE:
+            parts.append((t[:, 0] << np.uint32(PACKED_VALUE_BITS)) | t[:, 1])
+        else:
+            parts.append(t.reshape(-1))
+        woffs.append(woffs[-1] + len(parts[-1]))
+    words = np.concatenate(parts).astype(np.uint32) if parts else np.zeros(0, np.uint32)
+    return words, np.asarray(woffs, np.uint64)
+
+
+def ac_token_unpack(word: int) -> tuple[int, int]:
+    """`AcToken::unpack` (src/entropy/token_stream.rs:44-48)."""
+    return word >> PACKED_VALUE_BITS, word & PACKED_MAX_VALUE

@@ -273,3 +273,51 @@ def test_srgb_lut_is_the_reference_formula():
     v = np.arange(256, dtype=np.float64) * (1.0 / 255.0)
     want = np.where(v <= 0.04045, v / 12.92, ((v + 0.055) / 1.055) ** 2.4).astype(np.float32)
     assert np.array_equal(O.srgb_lut().view(np.uint32), want.view(np.uint32))
+
+
+def _pairs(words, woffs, goffs):
+    from jixel_gb300.api import unpack_tokens
+    return unpack_tokens(words, woffs, goffs).tolist()
+
+
+def test_packed_token_boundaries_and_wide_fallback():
+    # src/entropy/token_stream.rs:250-277: the largest context and value still
+    # pack (one word each); one value or context past them, or u32::MAX, keeps
+    # the whole stream wide; both forms give back every bit
+    mc, mv = O.PACKED_MAX_CONTEXT, O.PACKED_MAX_VALUE
+    assert (mc, mv) == ((1 << 14) - 1, (1 << 18) - 1)
+    assert O.NUM_FINE_AC_CONTEXTS - 1 <= mc
+    source = [[0, 0], [mc, mv], [O.NUM_FINE_AC_CONTEXTS - 1, 31]]
+    words, woffs = O.ac_tokens_from(np.array(source), np.array([0, 3]))
+    assert woffs.tolist() == [0, 3] and words.dtype == np.uint32
+    assert [O.ac_token_unpack(int(w)) for w in words] == [tuple(t) for t in source]
+    for wide in ([0, mv + 1], [mc + 1, 0], [0xFFFFFFFF, 0xFFFFFFFF]):
+        src = source + [wide]
+        words, woffs = O.ac_tokens_from(np.array(src, np.uint64).astype(np.uint32), np.array([0, 4]))
+        assert woffs.tolist() == [0, 8]
+        assert _pairs(words, woffs, np.array([0, 4], np.uint64)) == src
+
+
+def test_packed_token_views_and_empty_streams():
+    # src/entropy/token_stream.rs:279-310: 97 tokens (i % 7, 13 i), with and
+    # without a u32::MAX value at the end; an empty stream packs to nothing
+    for wide in (False, True):
+        src = np.array([[i % 7, 0xFFFFFFFF if wide and i == 96 else 13 * i] for i in range(97)],
+                       np.uint64).astype(np.uint32)
+        words, woffs = O.ac_tokens_from(src, np.array([0, 97]))
+        assert int(woffs[-1]) == (194 if wide else 97)
+        assert np.array_equal(np.array(_pairs(words, woffs, np.array([0, 97], np.uint64))), src)
+    words, woffs = O.ac_tokens_from(np.zeros((0, 2), np.uint32), np.array([0, 0]))
+    assert words.size == 0 and woffs.tolist() == [0, 0]
+
+
+def test_packed_form_is_decided_per_group():
+    # AcTokens::from runs on each group's own stream (src/frame/ac_groups.rs:243):
+    # a wide group leaves its neighbours packed; offsets need not start at 0
+    toks = np.array([[1, 2], [3, 4], [5, 1 << 18], [6, 7], [8, 9]], np.uint32)
+    goffs = np.array([10, 12, 13, 13, 15], np.uint64)
+    words, woffs = O.ac_tokens_from(toks, goffs)
+    assert woffs.tolist() == [0, 2, 4, 4, 6]
+    assert words[:2].tolist() == [(1 << 18) | 2, (3 << 18) | 4]
+    assert words[2:4].tolist() == [5, 1 << 18]
+    assert _pairs(words, woffs, goffs) == toks.tolist()
