@@ -187,12 +187,14 @@ int32_t jxg_frontend(void* ctx, const void* pixels, uint64_t width, uint64_t hei
  * jxg_frontend_enqueue enqueues on the context's stream the upload of
  * `pixels`, the pass, and the download of `params` and every requested
  * output, then returns without waiting; jxg_frontend_wait completes it
- * (params, status).  The token stream and group offsets are written by the
- * device itself (their length is known only there), so `out->tokens` and
- * `out->group_offsets` must be memory the device can write: pinned host
- * memory (cudaHostAlloc / cudaHostRegister), device memory, or any host
- * memory on systems with coherent CPU-GPU access.  Upload and downloads
- * run asynchronously when `pixels` and the outputs are pinned.  A context
+ * (params, status).  The group and word offsets are written by the device
+ * itself (the group sizes are known only there), so `out->group_offsets`
+ * and `out->packed_offsets` must be memory the device can write: pinned
+ * host memory (cudaHostAlloc / cudaHostRegister), device memory, or any
+ * host memory on systems with coherent CPU-GPU access.  The token streams
+ * (`tokens`, `packed_tokens`), whose lengths the host learns at the wait,
+ * are copied by the wait, which returns once they have landed.  Upload and
+ * downloads run asynchronously when `pixels` and the outputs are pinned.  A context
  * holds one frame in flight (enqueueing again waits for the previous one);
  * two contexts on one device overlap one frame's transfers with the other's
  * kernels.  `pixels` and the outputs must stay valid until the wait. */

@@ -1045,6 +1045,16 @@ int32_t jxg_frontend_wait(void* ctx) {
     return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "packed token buffer too small");
   if (out.ac_strategy)
     std::memset(out.ac_strategy, 1, L.info.xsize_blocks * L.info.ysize_blocks);
+  // The token streams, whose lengths the host learns only now, leave the
+  // device by the copy engine (a single-frame pass starts at token 0).
+  if (out.tokens && slot->token_count)
+    JXG_CUDA(c, cudaMemcpyAsync(out.tokens, c->tokens.ptr, slot->token_count * sizeof(jxg_token),
+                                cudaMemcpyDefault, c->stream));
+  if (out.packed_tokens && slot->packed_count)
+    JXG_CUDA(c, cudaMemcpyAsync(out.packed_tokens, c->packed.ptr, slot->packed_count * 4,
+                                cudaMemcpyDefault, c->stream));
+  if ((out.tokens && slot->token_count) || (out.packed_tokens && slot->packed_count))
+    return jxg::wait(c);
   return JXG_OK;
 }
 
@@ -1058,18 +1068,18 @@ int32_t jxg_frontend_enqueue(void* ctx, const void* pixels, uint64_t width, uint
   cudaSetDevice(c->device);
   jxg_frontend_output o{};
   if (out) o = *out;
-  void* tok_dev = nullptr;
   void* off_dev = nullptr;
-  void* words_dev = nullptr;
   void* woff_dev = nullptr;
-  if ((st = jxg::device_view(c, o.tokens, &tok_dev)) ||
-      (st = jxg::device_view(c, o.group_offsets, &off_dev)) ||
-      (st = jxg::device_view(c, o.packed_tokens, &words_dev)) ||
+  if ((st = jxg::device_view(c, o.group_offsets, &off_dev)) ||
       (st = jxg::device_view(c, o.packed_offsets, &woff_dev)) ||
       (st = jxg::ensure_host(c, c->async_slot, sizeof(Context::AsyncSlot))))
     return st;
   if ((st = jxg::single_pass(c, pixels, width, height, channels, bits, config, false))) return st;
   const jxg::FrameLayout& L = c->layouts[0];
+  // packed words are staged on the device; jxg_frontend_wait copies them out
+  const uint64_t words_cap = std::min<uint64_t>(o.packed_capacity, 2 * L.info.max_tokens);
+  if (o.packed_tokens && (st = jxg::ensure(c, c->packed, std::max<uint64_t>(words_cap, 1) * 4)))
+    return st;
   auto* slot = static_cast<Context::AsyncSlot*>(c->async_slot.ptr);
   void* slot_count_dev = nullptr;
   void* slot_words_dev = nullptr;
@@ -1085,15 +1095,14 @@ int32_t jxg_frontend_enqueue(void* ctx, const void* pixels, uint64_t width, uint
     jxg::k_copy_out_tokens<<<grid, 256, 0, s>>>(
         static_cast<const uint2*>(c->tokens.ptr),
         static_cast<const uint64_t*>(c->group_offsets.ptr) + L.group_off,
-        static_cast<int>(L.info.num_groups), static_cast<uint2*>(tok_dev),
-        o.tokens ? o.token_capacity : 0, static_cast<uint64_t*>(off_dev),
+        static_cast<int>(L.info.num_groups), nullptr, 0, static_cast<uint64_t*>(off_dev),
         static_cast<uint64_t*>(slot_count_dev));
   });
   if (st) return st;
   slot->packed_count = 0;
   if ((o.packed_tokens || o.packed_offsets) &&
-      (st = jxg::launch_pack(c, 0, static_cast<uint32_t*>(words_dev),
-                             o.packed_tokens ? o.packed_capacity : 0,
+      (st = jxg::launch_pack(c, 0, o.packed_tokens ? static_cast<uint32_t*>(c->packed.ptr) : nullptr,
+                             o.packed_tokens ? words_cap : 0,
                              static_cast<uint64_t*>(woff_dev),
                              static_cast<uint64_t*>(slot_words_dev))))
     return st;
