@@ -291,6 +291,10 @@ int32_t jxg_token_offsets_noalloc(const uint32_t* counts, uint64_t num_groups, u
  * that is never set, for `polls` polls, and returns JXG_ERR_DEVICE_TIMEOUT:
  * the error path, exercised without faulting or hanging the device. */
 int32_t jxg_selftest_bounded_wait(void* ctx, uint32_t polls);
+/* The tokenizer's look-back on token offsets waiting on a chunk that never
+ * publishes, for `polls` polls: returns JXG_ERR_DEVICE_TIMEOUT with the
+ * context still usable. */
+int32_t jxg_selftest_token_lookback(void* ctx, uint32_t polls);
 
 /* The XYB cube root and the AQ pre-pass and gamma terms divide and take
  * square roots with fused-multiply-add sequences instead of the IEEE

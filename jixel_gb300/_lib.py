@@ -37,6 +37,7 @@ EXPORTS = [
     "jxg_op_pack_tokens",
     "jxg_token_offsets_noalloc",
     "jxg_selftest_bounded_wait",
+    "jxg_selftest_token_lookback",
     "jxg_selftest_math",
     "jxg_enable_kernel_timing",
     "jxg_kernel_times",
@@ -147,6 +148,7 @@ def load() -> ctypes.CDLL:
         "jxg_op_pack_tokens": (i32, [vp, vp, vp, u64, vp, u64, vp]),
         "jxg_token_offsets_noalloc": (i32, [vp, u64, vp, vp, vp]),
         "jxg_selftest_bounded_wait": (i32, [vp, ctypes.c_uint32]),
+        "jxg_selftest_token_lookback": (i32, [vp, ctypes.c_uint32]),
         "jxg_selftest_math": (i32, [vp, i32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(u64),
                                     ctypes.POINTER(ctypes.c_uint32)]),
         "jxg_enable_kernel_timing": (i32, [vp, i32]),

@@ -64,6 +64,23 @@ struct PassImage {
   jxg_config config;
 };
 
+// Token chunks of one frame: runs of up to kTokenChunk blocks in token order
+// (each group's blocks in raster order), as the tokenizer's chunk_place
+// enumerates them.
+int64_t token_chunks_of(const jxg_frame_info& fi) {
+  auto per_group = [](uint64_t w, uint64_t h) {
+    return static_cast<int64_t>((w * h + kTokenChunk - 1) / kTokenChunk);
+  };
+  const uint64_t gxn = fi.xsize_groups, gyn = fi.ysize_groups;
+  const uint64_t gw_last = fi.xsize_blocks - (gxn - 1) * kGroupBlocks;
+  const uint64_t gh_last = fi.ysize_blocks - (gyn - 1) * kGroupBlocks;
+  const int64_t full_row = static_cast<int64_t>(gxn - 1) * per_group(kGroupBlocks, kGroupBlocks) +
+                           per_group(gw_last, kGroupBlocks);
+  const int64_t last_row = static_cast<int64_t>(gxn - 1) * per_group(kGroupBlocks, gh_last) +
+                           per_group(gw_last, gh_last);
+  return static_cast<int64_t>(gyn - 1) * full_row + last_row;
+}
+
 // Where one frame of the last pass lives, for fetching its results.
 struct FrameLayout {
   uint64_t width = 0, height = 0;
@@ -86,9 +103,9 @@ struct Context {
   uint8_t* d_pos = nullptr;     // natural 8x8 order, raw index -> scan position
   // pass buffers (grown, never shrunk)
   DevBuf pixels, xyb, qf, ytox, ytob, quant_dc, levels, wide_levels, coeffs, nzeros, nz_packed,
-      counts, offsets, chunks, tokens, hist, stats, group_offsets, plan, total, op_in, op_out,
+      counts, tokens, hist, stats, group_offsets, plan, total, op_in, op_out,
       alpha, alpha_peak, alpha_zero, fill_flags, fill_deps, fill_queue, group_wide, packed,
-      packed_offs;
+      packed_offs, tok_status;
   HostBuf plan_host, pixels_host;
   // The plan (frame descriptors + chunk prefixes) lives in a ring of slots,
   // pinned on the host and mirrored on the device, so a pass can be planned
@@ -330,8 +347,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
       return fail(c, JXG_ERR_DIMENSION_TOO_LARGE,
                   "pass holds more than 2^32 possible tokens: split the batch");
     xyb_chunks += (px + kXybChunk - 1) / kXybChunk;
-    token_chunks += (static_cast<int64_t>(L.info.xsize_blocks * L.info.ysize_blocks) +
-                     kTokenChunk - 1) / kTokenChunk;
+    token_chunks += token_chunks_of(L.info);
   }
   c->total_tiles = static_cast<int64_t>(tiles);
   c->xyb_chunks = xyb_chunks;
@@ -346,7 +362,6 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     c->pixel_bytes = last.pix_off + static_cast<size_t>(last.width * last.height) *
                                         imgs[n - 1].channels * (imgs[n - 1].bits / 8);
   }
-  const int64_t nchunks = (c->total_counts + kScanChunk - 1) / kScanChunk;
   c->frames_bytes = align_up(sizeof(Frame) * n, 256);
   const size_t prefix_bytes = align_up(sizeof(int64_t) * (n + 1), 256);
   const size_t plan_bytes = align_up(c->frames_bytes + kPlanPrefixes * prefix_bytes, 256);
@@ -370,8 +385,8 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
       (st = ensure(c, c->levels, blocks * 192 * 2)) ||
       (st = ensure(c, c->wide_levels, blocks * 192 * 4)) ||
       (st = ensure(c, c->nzeros, 3 * blocks)) || (st = ensure(c, c->nz_packed, 4 * blocks)) ||
-      (st = ensure(c, c->counts, counts * 4)) || (st = ensure(c, c->offsets, counts * 4)) ||
-      (st = ensure(c, c->chunks, nchunks * 4)) ||
+      (st = ensure(c, c->counts, counts * 4)) ||
+      (st = ensure(c, c->tok_status, (token_chunks + 1) * 8)) ||
       (st = ensure(c, c->tokens, tokens * sizeof(uint2))) ||
       (st = ensure(c, c->hist, n * kHistBytes)) ||
       (st = ensure(c, c->stats, n * sizeof(DeviceStats))) ||
@@ -426,7 +441,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     f.nzeros = static_cast<uint8_t*>(c->nzeros.ptr) + 3 * L.block_off;
     f.nz_packed = static_cast<uint32_t*>(c->nz_packed.ptr) + L.block_off;
     f.counts = static_cast<uint32_t*>(c->counts.ptr) + L.count_off;
-    f.offsets = static_cast<uint32_t*>(c->offsets.ptr) + L.count_off;
+    f.group_offsets = static_cast<uint64_t*>(c->group_offsets.ptr) + L.group_off;
     f.histograms = reinterpret_cast<uint32_t*>(static_cast<char*>(c->hist.ptr) + i * kHistBytes);
     f.stats = static_cast<DeviceStats*>(c->stats.ptr) + i;
     f.group_wide = static_cast<uint32_t*>(c->group_wide.ptr) + L.group_off;
@@ -437,7 +452,6 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
       f.alpha_full = im.bits == 8 ? 255 : 65535;
     }
     const int64_t px = static_cast<int64_t>(L.width * L.height);
-    const int64_t nb = static_cast<int64_t>(L.info.xsize_blocks * L.info.ysize_blocks);
     pre_xyb[i] = ax;
     pre_tile[i] = at;
     pre_tok[i] = ak;
@@ -449,7 +463,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     }
     ax += (px + kXybChunk - 1) / kXybChunk;
     at += static_cast<int64_t>(L.info.xsize_tiles * L.info.ysize_tiles);
-    ak += (nb + kTokenChunk - 1) / kTokenChunk;
+    ak += token_chunks_of(L.info);
   }
   pre_xyb[n] = ax;
   pre_tile[n] = at;
@@ -492,7 +506,7 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
     }
   JXG_CUDA(c, cudaMemsetAsync(c->stats.ptr, 0, n * sizeof(DeviceStats), s));
   JXG_CUDA(c, cudaMemsetAsync(c->hist.ptr, 0, n * kHistBytes, s));
-  JXG_CUDA(c, cudaMemsetAsync(c->counts.ptr, 0, c->total_counts * 4, s));
+  JXG_CUDA(c, cudaMemsetAsync(c->tok_status.ptr, 0, (c->token_chunks + 1) * 8, s));
   const Frame* frames = reinterpret_cast<const Frame*>(plan_d);
   const int64_t* pre_xyb = reinterpret_cast<const int64_t*>(plan_d + c->frames_bytes);
   const int64_t* pre_tile = reinterpret_cast<const int64_t*>(reinterpret_cast<const char*>(pre_xyb) + prefix_bytes);
@@ -576,30 +590,18 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
          })))
       return st;
   }
-  uint32_t* counts = static_cast<uint32_t*>(c->counts.ptr);
-  uint32_t* offs = static_cast<uint32_t*>(c->offsets.ptr);
-  uint32_t* chunks = static_cast<uint32_t*>(c->chunks.ptr);
-  uint64_t* goffs = static_cast<uint64_t*>(c->group_offsets.ptr);
-  const int64_t ncounts = c->total_counts;
-  const int nchunks = static_cast<int>((ncounts + kScanChunk - 1) / kScanChunk);
-  if ((st = launch(c, "k_scan_reduce", timed, [&] {
-         k_scan_reduce<<<nchunks, kScanThreads, 0, s>>>(counts, ncounts, chunks);
-       })) ||
-      (st = launch(c, "k_scan_chunks", timed, [&] {
-         k_scan_chunks<<<1, kScanThreads, 0, s>>>(chunks, nchunks, static_cast<uint32_t*>(c->total.ptr),
-                                                   goffs, static_cast<int>(c->total_groups));
-       })) ||
-      (st = launch(c, "k_scan_apply", timed, [&] {
-         k_scan_apply<<<nchunks, kScanThreads, 0, s>>>(counts, ncounts, chunks, offs, goffs, 4 * 1024,
-                                                      static_cast<uint32_t*>(c->group_wide.ptr));
-       })) ||
-      (st = single ? launch(c, "k_tokenize", timed, [&] {
+  // token offsets come from the tokenizer's own look-back over its chunks
+  TokenScan scan;
+  scan.status = static_cast<unsigned long long*>(c->tok_status.ptr);
+  scan.chunks = c->token_chunks;
+  scan.pass_end = static_cast<uint64_t*>(c->group_offsets.ptr) + c->total_groups;
+  if ((st = single ? launch(c, "k_tokenize", timed, [&] {
          k_tokenize<<<static_cast<unsigned>(c->token_chunks), kTokThreads, 0, s>>>(
-             f0, static_cast<uint2*>(c->tokens.ptr));
+             f0, static_cast<uint2*>(c->tokens.ptr), scan);
        })
                    : launch(c, "k_tokenize_batch", timed, [&] {
          k_tokenize_batch<<<static_cast<unsigned>(c->token_chunks), kTokThreads, 0, s>>>(
-             frames, pre_tok, n, static_cast<uint2*>(c->tokens.ptr));
+             frames, pre_tok, n, static_cast<uint2*>(c->tokens.ptr), scan);
        })))
     return st;
   c->have_frame = true;
@@ -647,6 +649,8 @@ void params_from(const FrameLayout& L, const DeviceStats& ds, uint64_t num_token
 int check_flags(Context* c, const DeviceStats& ds) {
   if (ds.flags & kFlagFillTimeout)
     return fail(c, JXG_ERR_DEVICE_TIMEOUT, "a bounded device wait of the invisible fill ran out");
+  if (ds.flags & kFlagTokenTimeout)
+    return fail(c, JXG_ERR_DEVICE_TIMEOUT, "a bounded device wait of the token offsets ran out");
   return JXG_OK;
 }
 
@@ -936,11 +940,11 @@ void jxg_context_destroy(void* ctx) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (jxg::DevBuf* b : {&c->pixels, &c->xyb, &c->qf, &c->ytox, &c->ytob, &c->quant_dc, &c->levels,
                          &c->wide_levels, &c->coeffs, &c->nzeros, &c->nz_packed, &c->counts,
-                         &c->offsets, &c->chunks, &c->tokens, &c->hist, &c->stats,
+                         &c->tokens, &c->hist, &c->stats,
                          &c->group_offsets, &c->plan, &c->total, &c->op_in, &c->op_out,
                          &c->alpha, &c->alpha_peak, &c->alpha_zero, &c->fill_flags,
                          &c->fill_deps, &c->fill_queue, &c->group_wide, &c->packed,
-                         &c->packed_offs})
+                         &c->packed_offs, &c->tok_status})
     if (b->ptr) cudaFree(b->ptr);
   for (jxg::HostBuf* b : {&c->plan_host, &c->pixels_host, &c->async_slot})
     if (b->ptr) cudaFreeHost(b->ptr);
@@ -1395,6 +1399,25 @@ int32_t jxg_selftest_bounded_wait(void* ctx, uint32_t polls) {
   if ((st = jxg::wait(c))) return st;
   if (r == 2u) return jxg::fail(c, JXG_ERR_DEVICE_TIMEOUT, "bounded wait ran out (self-test)");
   return r == 1u ? JXG_OK : JXG_ERR_CUDA;
+}
+
+int32_t jxg_selftest_token_lookback(void* ctx, uint32_t polls) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c) return JXG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(c->device);
+  int st;
+  if ((st = jxg::ensure(c, c->op_out, 256))) return st;
+  auto* status = static_cast<unsigned long long*>(c->op_out.ptr);  // ticket, chunk 0, chunk 1
+  auto* flags = reinterpret_cast<uint32_t*>(status + 4);
+  JXG_CUDA(c, cudaMemsetAsync(status, 0, 64, c->stream));
+  jxg::k_lookback_selftest<<<1, 32, 0, c->stream>>>(status, polls, flags);
+  JXG_CUDA(c, cudaGetLastError());
+  uint32_t r = 0;
+  JXG_CUDA(c, cudaMemcpyAsync(&r, flags, 4, cudaMemcpyDeviceToHost, c->stream));
+  if ((st = jxg::wait(c))) return st;
+  if (r & jxg::kFlagTokenTimeout)
+    return jxg::fail(c, JXG_ERR_DEVICE_TIMEOUT, "token look-back wait ran out (self-test)");
+  return JXG_ERR_CUDA;
 }
 
 int32_t jxg_selftest_math(void* ctx, int32_t which, uint32_t lo_bits, uint32_t hi_bits,

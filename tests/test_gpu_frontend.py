@@ -60,6 +60,22 @@ def test_ragged_sizes(ctx, w, h):
     compare(ctx, img, 1.0)
 
 
+@pytest.mark.parametrize("w,h", [(8, 2400), (2400, 8), (520, 264), (1032, 72)])
+def test_token_chunks_of_partial_groups(ctx, w, h):
+    # the tokenizer's chunks run through each group's blocks in token order:
+    # one-block-wide and one-block-tall groups, odd partial groups at the
+    # right and bottom edges, several chunks per row of groups
+    img = synthetic.generate(w, h, 31 + w, rectangles=4)
+    compare(ctx, img, 1.0, check_xyb=False)
+
+
+def test_token_lookback_timeout_is_reported_and_the_context_stays_usable(ctx):
+    from jixel_gb300 import _lib as L
+    lib = L.load()
+    assert lib.jxg_selftest_token_lookback(ctx.handle, 2000) == 102  # JXG_ERR_DEVICE_TIMEOUT
+    compare(ctx, synthetic.generate(96, 64, 41), 1.0)
+
+
 def test_multiple_dc_groups(ctx):
     img = synthetic.generate(2100, 300, 21, rectangles=30)
     compare(ctx, img, 1.5, check_xyb=False)
