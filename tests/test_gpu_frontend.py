@@ -176,6 +176,7 @@ def test_repeat_runs_are_identical(ctx):
     (2, 0, 0x44800000),           # gamma ratio, direct: [0, 1024)
     (3, 0, 0x3E4CCCCD + 1),       # masking square root: [0, 0.2]
     (4, 0, 0x40000000),           # cube root, packed two-lane path: [0, 2)
+    (5, 0, 65536),                # 16-bit sample / 65535: every sample value
 ])
 def test_fast_math_equals_ieee_on_every_input(ctx, which, lo, hi):
     # the fused sequences replacing IEEE division / sqrt on the hot paths give
