@@ -304,7 +304,9 @@ int32_t jxg_selftest_token_lookback(void* ctx, uint32_t polls);
  * [0, 0x40000000)), 1 / 2 = the AQ gamma ratio inverted / direct (inputs in
  * [0, 0x44800000)), 3 = the AQ masking square root (inputs in
  * [0, 0x3E4CCCCD]), 4 = the cube root on the packed two-lane FP32 path,
- * 5 = a 16-bit sample over 65535 (here [lo, hi) are sample values, 0..65536).
+ * 5 = a 16-bit sample over 65535 (here [lo, hi) are sample values, 0..65536),
+ * 6 / 7 / 8 = the gamma ratio inverted / direct and the masking square root
+ * on the packed two-lane FP32 path.
  * It returns the number of differing results and the
  * smallest differing pattern (0xFFFFFFFF when none). */
 int32_t jxg_selftest_math(void* ctx, int32_t which, uint32_t lo_bits, uint32_t hi_bits,

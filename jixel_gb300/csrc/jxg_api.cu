@@ -1423,7 +1423,7 @@ int32_t jxg_selftest_token_lookback(void* ctx, uint32_t polls) {
 int32_t jxg_selftest_math(void* ctx, int32_t which, uint32_t lo_bits, uint32_t hi_bits,
                           uint64_t* mismatches, uint32_t* first_bad) {
   Context* c = static_cast<Context*>(ctx);
-  if (!c || !mismatches || !first_bad || hi_bits < lo_bits || which < 0 || which > 5)
+  if (!c || !mismatches || !first_bad || hi_bits < lo_bits || which < 0 || which > 8)
     return JXG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(c->device);
   int st;

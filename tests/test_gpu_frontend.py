@@ -177,6 +177,9 @@ def test_repeat_runs_are_identical(ctx):
     (3, 0, 0x3E4CCCCD + 1),       # masking square root: [0, 0.2]
     (4, 0, 0x40000000),           # cube root, packed two-lane path: [0, 2)
     (5, 0, 65536),                # 16-bit sample / 65535: every sample value
+    (6, 0, 0x44800000),           # gamma ratio, inverted, packed two-lane path
+    (7, 0, 0x44800000),           # gamma ratio, direct, packed two-lane path
+    (8, 0, 0x3E4CCCCD + 1),       # masking square root, packed two-lane path
 ])
 def test_fast_math_equals_ieee_on_every_input(ctx, which, lo, hi):
     # the fused sequences replacing IEEE division / sqrt on the hot paths give
