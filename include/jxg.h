@@ -243,6 +243,22 @@ int32_t jxg_op_fill_quant_field(void* ctx, const float* xyb, uint64_t width, uin
 /* DctFn<8, 8, 64> (src/dct.rs:172, scalar dct8x8 :631): `count` blocks of 64
  * row-major samples in, 64 coefficients (transposed storage, 1/64 scale) out. */
 int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coefficients);
+/* DctFn<W, H, N> of the larger blocks (src/dct.rs: dct8x16 :823, dct16x8
+ * :904, dct16x16 :1010, dct32x32 :1980, dct32x16 :2251, dct16x32 :2340;
+ * kind 0 is dct8x8 as jxg_op_dct8x8) with the DC values of every covered
+ * 8x8 block (dc_from_dct*, :930-2400).  `blocks` holds `count` row-major
+ * blocks of H rows of W samples; `coefficients` receives W H coefficients
+ * per block in the reference's order, `dc_values` (optional) 1, 2, 2, 4, 8,
+ * 8 or 16 values per block for kinds 0..6. */
+#define JXG_DCT8X8 0
+#define JXG_DCT8X16 1  /* 8 rows x 16 columns */
+#define JXG_DCT16X8 2
+#define JXG_DCT16X16 3
+#define JXG_DCT16X32 4
+#define JXG_DCT32X16 5
+#define JXG_DCT32X32 6
+int32_t jxg_op_dct(void* ctx, int32_t kind, const float* blocks, uint64_t count,
+                   float* coefficients, float* dc_values);
 /* AcTokens::from (src/entropy/token_stream.rs:59-76) per group: `tokens`
  * from group_offsets[0] to group_offsets[num_groups] (host arrays) into the
  * storage form of jxg_frontend_output.packed_tokens; `word_offsets` gets

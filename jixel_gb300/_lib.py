@@ -35,6 +35,7 @@ EXPORTS = [
     "jxg_op_fill_quant_field",
     "jxg_op_dct8x8",
     "jxg_op_pack_tokens",
+    "jxg_op_dct",
     "jxg_token_offsets_noalloc",
     "jxg_selftest_bounded_wait",
     "jxg_selftest_token_lookback",
@@ -146,6 +147,7 @@ def load() -> ctypes.CDLL:
         "jxg_op_fill_quant_field": (i32, [vp, vp, u64, u64, f32, f32, vp]),
         "jxg_op_dct8x8": (i32, [vp, vp, u64, vp]),
         "jxg_op_pack_tokens": (i32, [vp, vp, vp, u64, vp, u64, vp]),
+        "jxg_op_dct": (i32, [vp, i32, vp, u64, vp, vp]),
         "jxg_token_offsets_noalloc": (i32, [vp, u64, vp, vp, vp]),
         "jxg_selftest_bounded_wait": (i32, [vp, ctypes.c_uint32]),
         "jxg_selftest_token_lookback": (i32, [vp, ctypes.c_uint32]),

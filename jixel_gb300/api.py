@@ -328,6 +328,22 @@ class FrontendContext:
                                             out.ctypes.data))
         return out
 
+    DCT_KINDS = {"8x8": (0, 8, 8, 1), "8x16": (1, 16, 8, 2), "16x8": (2, 8, 16, 2),
+                 "16x16": (3, 16, 16, 4), "16x32": (4, 32, 16, 8), "32x16": (5, 16, 32, 8),
+                 "32x32": (6, 32, 32, 16)}
+
+    def dct(self, name: str, blocks: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """DctFn<W, H, N> (src/dct.rs) of (count, H, W) blocks named rows x
+        columns as the reference does ("8x16" = 8 rows of 16): (count, W H)
+        coefficients and (count, D) DC values of the covered 8x8 blocks."""
+        kind, w, h, ndc = self.DCT_KINDS[name]
+        b = np.ascontiguousarray(blocks, np.float32).reshape(-1, h * w)
+        out = np.zeros_like(b)
+        dc = np.zeros((b.shape[0], ndc), np.float32)
+        self._check(self._lib.jxg_op_dct(self._ctx, kind, b.ctypes.data, b.shape[0],
+                                         out.ctypes.data, dc.ctypes.data))
+        return out, dc
+
     def pack_tokens(self, tokens: np.ndarray, group_offsets: np.ndarray
                     ) -> tuple[np.ndarray, np.ndarray]:
         """AcTokens::from per group (src/entropy/token_stream.rs:59-76) on the

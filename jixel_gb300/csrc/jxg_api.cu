@@ -1300,6 +1300,62 @@ int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coe
   return jxg::wait(c);
 }
 
+int32_t jxg_op_dct(void* ctx, int32_t kind, const float* blocks, uint64_t count,
+                   float* coefficients, float* dc_values) {
+  Context* c = static_cast<Context*>(ctx);
+  static const int kW[7] = {8, 16, 8, 16, 32, 16, 32}, kH[7] = {8, 8, 16, 16, 16, 32, 32};
+  static const int kDc[7] = {1, 2, 2, 4, 8, 8, 16};
+  if (!c || !blocks || !coefficients || kind < 0 || kind > 6) return JXG_ERR_INVALID_ARGUMENT;
+  if (count == 0) return JXG_OK;
+  if (count > (1ull << 31)) return JXG_ERR_DIMENSION_TOO_LARGE;
+  cudaSetDevice(c->device);
+  const int n = kW[kind] * kH[kind], ndc = kDc[kind];
+  const size_t bytes = count * n * 4, dc_bytes = count * ndc * 4;
+  int st;
+  if ((st = jxg::ensure(c, c->op_in, bytes)) || (st = jxg::ensure(c, c->op_out, bytes + dc_bytes)))
+    return st;
+  cudaStream_t s = c->stream;
+  const float* din = static_cast<const float*>(c->op_in.ptr);
+  float* dout = static_cast<float*>(c->op_out.ptr);
+  float* ddc = dout + count * n;
+  JXG_CUDA(c, cudaMemcpyAsync(c->op_in.ptr, blocks, bytes, cudaMemcpyHostToDevice, s));
+  const unsigned grid = static_cast<unsigned>((count + jxg::kDctWarps - 1) / jxg::kDctWarps);
+  const unsigned threads = 32 * jxg::kDctWarps;
+  const int64_t cnt = static_cast<int64_t>(count);
+  st = jxg::launch(c, "k_dct_blocks", c->timing, [&] {
+    switch (kind) {
+      case jxg::kDct8x8:
+        jxg::k_dct8x8_blocks<<<static_cast<unsigned>((count + 31) / 32), 256, 0, s>>>(din, cnt, dout);
+        break;
+      case jxg::kDct8x16:
+        jxg::k_dct_blocks<16, 8, false><<<grid, threads, 0, s>>>(din, cnt, dout, ddc, kind, ndc);
+        break;
+      case jxg::kDct16x8:
+        jxg::k_dct_blocks<8, 16, true><<<grid, threads, 0, s>>>(din, cnt, dout, ddc, kind, ndc);
+        break;
+      case jxg::kDct16x16:
+        jxg::k_dct_blocks<16, 16, true><<<grid, threads, 0, s>>>(din, cnt, dout, ddc, kind, ndc);
+        break;
+      case jxg::kDct16x32:
+        jxg::k_dct_blocks<32, 16, false><<<grid, threads, 0, s>>>(din, cnt, dout, ddc, kind, ndc);
+        break;
+      case jxg::kDct32x16:
+        jxg::k_dct_blocks<16, 32, true><<<grid, threads, 0, s>>>(din, cnt, dout, ddc, kind, ndc);
+        break;
+      default:
+        jxg::k_dct_blocks<32, 32, true><<<grid, threads, 0, s>>>(din, cnt, dout, ddc, kind, ndc);
+    }
+  });
+  if (st) return st;
+  JXG_CUDA(c, cudaMemcpyAsync(coefficients, dout, bytes, cudaMemcpyDeviceToHost, s));
+  if (dc_values && kind != jxg::kDct8x8)
+    JXG_CUDA(c, cudaMemcpyAsync(dc_values, ddc, dc_bytes, cudaMemcpyDeviceToHost, s));
+  if ((st = jxg::wait(c))) return st;
+  if (dc_values && kind == jxg::kDct8x8)  // an 8x8 block's DC is its first coefficient
+    for (uint64_t i = 0; i < count; ++i) dc_values[i] = coefficients[i * 64];
+  return JXG_OK;
+}
+
 int32_t jxg_op_pack_tokens(void* ctx, const jxg_token* tokens, const uint64_t* group_offsets,
                            uint64_t num_groups, uint32_t* words, uint64_t capacity,
                            uint64_t* word_offsets) {

@@ -50,6 +50,12 @@
 /* Rust scalar semantics                                               */
 /* ------------------------------------------------------------------ */
 
+/* transform kinds of orc_dct (rows x columns, as the reference names them) */
+enum {
+  JXG_ORC_DCT8X8 = 0, JXG_ORC_DCT8X16 = 1, JXG_ORC_DCT16X8 = 2, JXG_ORC_DCT16X16 = 3,
+  JXG_ORC_DCT16X32 = 4, JXG_ORC_DCT32X16 = 5, JXG_ORC_DCT32X32 = 6
+};
+
 static inline float fmla(float a, float b, float c) { return fmaf(a, b, c); }
 
 static inline int32_t sat_i32(float v) {
@@ -857,6 +863,199 @@ static void dct8x8(const float* in, size_t stride, float* out) {
 }
 
 void orc_dct8x8(const float* in, float* out) { dct8x8(in, 8, out); }
+
+/* ---- transforms of the larger DCT blocks (src/dct.rs) ---------------- */
+
+static const float WC16[8] = {0.5024193f, 0.5224986f, 0.566944f,  0.6468218f,
+                              0.7881546f, 1.0606777f, 1.7224471f, 5.1011486f};
+static const float WC32[16] = {0.50060298f, 0.50547096f, 0.5154473f, 0.5310426f,
+                               0.5531039f,  0.582935f,   0.6225041f, 0.67480834f,
+                               0.7445363f,  0.83934965f, 0.97256825f, 1.16944f,
+                               1.4841646f,  2.057781f,   3.4076084f, 10.190008f};
+
+/* dct1d_16 (src/dct.rs:687-716): mirrored sums and differences, the sums
+ * through dct1d_8, the differences scaled by WC16 and through dct1d_8, the
+ * odd half's running sums, interleaved. */
+static inline void dct1d_16(float* b) {
+  float t[16];
+  for (int i = 0; i < 8; i++) {
+    t[i] = b[i] + b[15 - i];
+    t[8 + i] = b[i] - b[15 - i];
+  }
+  dct1d_8(t);
+  for (int i = 0; i < 8; i++) t[8 + i] *= WC16[i];
+  dct1d_8(t + 8);
+  t[8] = fmla(t[8], SQRT2F, t[9]);
+  for (int i = 9; i < 15; i++) t[i] += t[i + 1];
+  for (int i = 0; i < 8; i++) {
+    b[2 * i] = t[i];
+    b[2 * i + 1] = t[8 + i];
+  }
+}
+
+/* dct1d_32 (src/dct.rs:1477-1496), the same recursion over dct1d_16. */
+static inline void dct1d_32(float* b) {
+  float t[32];
+  for (int i = 0; i < 16; i++) {
+    t[i] = b[i] + b[31 - i];
+    t[16 + i] = b[i] - b[31 - i];
+  }
+  dct1d_16(t);
+  for (int i = 0; i < 16; i++) t[16 + i] *= WC32[i];
+  dct1d_16(t + 16);
+  t[16] = fmla(t[16], SQRT2F, t[17]);
+  for (int i = 17; i < 31; i++) t[i] += t[i + 1];
+  for (int i = 0; i < 16; i++) {
+    b[2 * i] = t[i];
+    b[2 * i + 1] = t[16 + i];
+  }
+}
+
+static inline void dct1d_n(float* b, int n) {
+  if (n == 8) dct1d_8(b);
+  else if (n == 16) dct1d_16(b);
+  else dct1d_32(b);
+}
+
+/* An H x W block (H rows of W samples), columns first: each column through
+ * the H-point transform, then each row through the W-point one, stored
+ * out[u * H + v] scaled by 1 / (W H) -- dct16x8 (src/dct.rs:904),
+ * dct16x16 (:1010), dct32x32 (:1980), dct32x16 (:2251). */
+static void dct_cols_first(const float* in, int W, int H, float* out) {
+  float after[1024], col[32], row[32];
+  for (int u = 0; u < W; u++) {
+    for (int i = 0; i < H; i++) col[i] = in[i * W + u];
+    dct1d_n(col, H);
+    for (int v = 0; v < H; v++) after[v * W + u] = col[v];
+  }
+  const float scale = 1.0f / (float)(W * H);
+  for (int v = 0; v < H; v++) {
+    for (int u = 0; u < W; u++) row[u] = after[v * W + u];
+    dct1d_n(row, W);
+    for (int u = 0; u < W; u++) out[u * H + v] = row[u] * scale;
+  }
+}
+
+/* Rows first, then columns, stored out[v * W + u] -- dct8x16
+ * (src/dct.rs:823), dct16x32 (:2340). */
+static void dct_rows_first(const float* in, int W, int H, float* out) {
+  float after[1024], col[32], row[32];
+  for (int i = 0; i < H; i++) {
+    for (int u = 0; u < W; u++) row[u] = in[i * W + u];
+    dct1d_n(row, W);
+    for (int u = 0; u < W; u++) after[i * W + u] = row[u];
+  }
+  const float scale = 1.0f / (float)(W * H);
+  for (int u = 0; u < W; u++) {
+    for (int i = 0; i < H; i++) col[i] = after[i * W + u];
+    dct1d_n(col, H);
+    for (int v = 0; v < H; v++) out[v * W + u] = col[v] * scale;
+  }
+}
+
+/* idct1d_4 of the DC extraction (src/dct.rs:2144-2167). */
+static void idct1d_4(const float v[4], float out[4]) {
+  float t0 = v[0], t1 = v[2], t2 = v[1], t3 = v[3];
+  const float e0 = t0 + t1, e1 = t0 - t1;
+  t0 = e0;
+  t1 = e1;
+  t3 += t2;
+  t2 *= SQRT2F;
+  const float o0 = t2 + t3, o1 = t2 - t3;
+  t2 = o0;
+  t3 = o1;
+  out[0] = fmla(WC4_0, t2, t0);
+  out[3] = fmla(-WC4_0, t2, t0);
+  out[1] = fmla(WC4_1, t3, t1);
+  out[2] = fmla(-WC4_1, t3, t1);
+}
+
+static const float R16_2[2] = {1.0f, 0.9017642f};                         /* :927 */
+static const float R32_4[4] = {1.0f, 0.9748868f, 0.9017642f, 0.7870549f};  /* :2018 */
+
+/* The DC values a transform's lowest coefficients resample to, one per
+ * covered 8x8 block (dc_from_dct16x8 :930, dc_from_dct8x16 :939,
+ * dc_from_dct16x16 :1033, dc_from_dct32x32 :2170, dc_from_dct32x16 :2356,
+ * dc_from_dct16x32 :2381); an 8x8 block's DC is its first coefficient. */
+static void dc_from(int kind, const float* c, float* dc) {
+  switch (kind) {
+    case JXG_ORC_DCT8X8:
+      dc[0] = c[0];
+      break;
+    case JXG_ORC_DCT8X16:
+    case JXG_ORC_DCT16X8: {
+      const float s0 = c[0] * R16_2[0], s1 = c[1] * R16_2[1];
+      dc[0] = s0 + s1;
+      dc[1] = s0 - s1;
+      break;
+    }
+    case JXG_ORC_DCT16X16: {
+      /* the products of the resample scales, as f32 */
+      const float r00 = 1.0f, r01 = 0.9017642f, r11 = 0x1.a058f6p-1f;
+      const float s00 = c[0] * r00, s01 = c[1] * r01, s10 = c[16] * r01, s11 = c[17] * r11;
+      const float a00 = s00 + s01, a01 = s00 - s01, a10 = s10 + s11, a11 = s10 - s11;
+      dc[0] = a00 + a10;
+      dc[1] = a00 - a10;
+      dc[2] = a01 + a11;
+      dc[3] = a01 - a11;
+      break;
+    }
+    case JXG_ORC_DCT16X32:
+    case JXG_ORC_DCT32X16: {
+      float rr[2][4];
+      for (int a = 0; a < 2; a++) {
+        float s[4];
+        for (int b = 0; b < 4; b++) s[b] = c[a * 32 + b] * R16_2[a] * R32_4[b];
+        idct1d_4(s, rr[a]);
+      }
+      for (int bb = 0; bb < 4; bb++) {
+        const float c0 = rr[0][bb], c1 = rr[1][bb];
+        if (kind == JXG_ORC_DCT32X16) {
+          dc[bb * 2] = c0 + c1;
+          dc[bb * 2 + 1] = c0 - c1;
+        } else {
+          dc[bb] = c0 + c1;
+          dc[4 + bb] = c0 - c1;
+        }
+      }
+      break;
+    }
+    default: { /* 32x32 */
+      float rr[4][4];
+      for (int a = 0; a < 4; a++) {
+        float s[4];
+        for (int b = 0; b < 4; b++) s[b] = c[a * 32 + b] * R32_4[a] * R32_4[b];
+        idct1d_4(s, rr[a]);
+      }
+      for (int bb = 0; bb < 4; bb++) {
+        const float col[4] = {rr[0][bb], rr[1][bb], rr[2][bb], rr[3][bb]};
+        float o[4];
+        idct1d_4(col, o);
+        for (int r = 0; r < 4; r++) dc[bb * 4 + r] = o[r];
+      }
+    }
+  }
+}
+
+/* DctFn<W, H, N> of one block (row-major H x W samples) and its DC values;
+ * `kind` as JXG_ORC_DCT*.  Returns 0, or -1 for an unknown kind. */
+int orc_dct(int kind, const float* in, float* out, float* dc) {
+  switch (kind) {
+    case JXG_ORC_DCT8X8: dct8x8(in, 8, out); break;
+    case JXG_ORC_DCT8X16: dct_rows_first(in, 16, 8, out); break;
+    case JXG_ORC_DCT16X8: dct_cols_first(in, 8, 16, out); break;
+    case JXG_ORC_DCT16X16: dct_cols_first(in, 16, 16, out); break;
+    case JXG_ORC_DCT16X32: dct_rows_first(in, 32, 16, out); break;
+    case JXG_ORC_DCT32X16: dct_cols_first(in, 16, 32, out); break;
+    case JXG_ORC_DCT32X32: dct_cols_first(in, 32, 32, out); break;
+    default: return -1;
+  }
+  if (dc) dc_from(kind, out, dc);
+  return 0;
+}
+
+/* dct1d_16 / dct1d_32 of one vector in place (n = 8, 16 or 32). */
+void orc_dct1d(float* b, int n) { dct1d_n(b, n); }
 
 /* ------------------------------------------------------------------ */
 /* Chroma-from-luma tiles (src/color_correlation.rs:333-512)            */

@@ -336,3 +336,31 @@ def ac_tokens_from(tokens: np.ndarray, group_offsets: np.ndarray) -> tuple[np.nd
 def ac_token_unpack(word: int) -> tuple[int, int]:
     """`AcToken::unpack` (src/entropy/token_stream.rs:44-48)."""
     return word >> PACKED_VALUE_BITS, word & PACKED_MAX_VALUE
+
+
+# DctFn kinds of orc_dct: name (rows x columns) -> (kind, W, H, DC values)
+DCT_KINDS = {
+    "8x8": (0, 8, 8, 1), "8x16": (1, 16, 8, 2), "16x8": (2, 8, 16, 2), "16x16": (3, 16, 16, 4),
+    "16x32": (4, 32, 16, 8), "32x16": (5, 16, 32, 8), "32x32": (6, 32, 32, 16),
+}
+
+
+def dct(name: str, block: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """`DctFn<W, H, N>` of one (H, W) block (src/dct.rs: dct8x16 :823, dct16x8
+    :904, dct16x16 :1010, dct32x32 :1980, dct32x16 :2251, dct16x32 :2340) and
+    its per-8x8 DC values (dc_from_dct*): (N coefficients, DC values)."""
+    kind, w, h, ndc = DCT_KINDS[name]
+    b = np.ascontiguousarray(block, np.float32).reshape(h, w)
+    out = np.zeros(w * h, np.float32)
+    dc = np.zeros(ndc, np.float32)
+    assert lib().orc_dct(ctypes.c_int(kind), b.ctypes.data_as(ctypes.c_void_p),
+                         out.ctypes.data_as(ctypes.c_void_p), dc.ctypes.data_as(ctypes.c_void_p)) == 0
+    return out, dc
+
+
+def dct1d(vec: np.ndarray) -> np.ndarray:
+    """dct1d_8 / dct1d_16 / dct1d_32 (src/dct.rs:109, :687, :1477) of one vector."""
+    v = np.ascontiguousarray(vec, np.float32).copy()
+    assert v.size in (8, 16, 32)
+    lib().orc_dct1d(v.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(v.size))
+    return v

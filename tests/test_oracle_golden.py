@@ -321,3 +321,63 @@ def test_packed_form_is_decided_per_group():
     assert words[:2].tolist() == [(1 << 18) | 2, (3 << 18) | 4]
     assert words[2:4].tolist() == [5, 1 << 18]
     assert _pairs(words, woffs, goffs) == toks.tolist()
+
+
+def test_dct1d_32_diagonalizes_the_dct_basis():
+    # src/dct.rs:3265-3289: the k0-th DCT-II basis vector peaks at k0 only
+    n = 32
+    for k0 in range(n):
+        x = np.array([math.cos(np.float32(math.pi) * (2.0 * i + 1.0) * k0 / (2.0 * n))
+                      for i in range(n)], np.float32)
+        y = O.dct1d(x)
+        mi = int(np.argmax(np.abs(y)))
+        mv = float(abs(y[mi]))
+        assert mi == k0, (k0, mi)
+        off = float(sum(float(y[i]) ** 2 for i in range(n) if i != k0))
+        assert off < 1e-6 * max(mv * mv, 1.0), (k0, off)
+
+
+def _lcg_block(count):
+    # the reference test's generator (src/dct.rs:3305-3310)
+    rng, out = 0x9E3779B9, []
+    for _ in range(count):
+        rng = (rng * 1664525 + 1013904223) & 0xFFFFFFFF
+        out.append(np.float32(rng >> 8) / np.float32(1 << 24) - np.float32(0.5))
+    return np.array(out, np.float32)
+
+
+@pytest.mark.parametrize("name,n", [("32x32", 32), ("16x16", 16)])
+def test_square_dct_matches_separable_reference(name, n):
+    # src/dct.rs:3291-3337: the 2-D transform equals columns then rows of the
+    # probed 1-D kernel, scaled 1/n^2, stored transposed
+    m1 = np.zeros((n, n), np.float32)
+    for k in range(n):
+        e = np.zeros(n, np.float32)
+        e[k] = 1.0
+        m1[:, k] = O.dct1d(e)
+    inp = _lcg_block(n * n).reshape(n, n)
+    col = (m1.astype(np.float64) @ inp.astype(np.float64))          # col[j][u]
+    ref = (m1.astype(np.float64) @ col.T.astype(np.float64)) / (n * n)  # ref[u][v]
+    out, _ = O.dct(name, inp)
+    assert np.abs(out.reshape(n, n) - ref).max() < 1e-5
+
+
+@pytest.mark.parametrize("name", ["8x16", "16x8", "16x16", "16x32", "32x16", "32x32"])
+def test_dc_of_a_constant_block_is_the_8x8_dc(name):
+    # src/dct.rs:3185-3213 (32x16 / 16x32; the other sizes alike): every
+    # covered block's DC equals the 8x8 DCT's DC of the same constant
+    _, w, h, _ = O.DCT_KINDS[name]
+    _, d8 = O.dct("8x8", np.full((8, 8), 2.3, np.float32))
+    _, dc = O.dct(name, np.full((h, w), 2.3, np.float32))
+    assert np.abs(dc - d8[0]).max() < 1e-3
+
+
+def test_rectangular_dc_follows_the_halves():
+    # a block whose halves differ: the DC pair of 8x16 (left/right) and 16x8
+    # (top/bottom) orders the halves' means
+    a = np.zeros((8, 16), np.float32)
+    a[:, 8:] = 1.0
+    _, dc = O.dct("8x16", a)
+    assert dc[0] < dc[1]
+    _, dc = O.dct("16x8", a.T.copy())
+    assert dc[0] < dc[1]
