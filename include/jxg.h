@@ -259,6 +259,12 @@ int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coe
 #define JXG_DCT32X32 6
 int32_t jxg_op_dct(void* ctx, int32_t kind, const float* blocks, uint64_t count,
                    float* coefficients, float* dc_values);
+/* The inverse transforms (IdctMethods, src/dct.rs:358-416; inv_dct8x16
+ * :1634, inv_dct16x8 :1658, inv_dct16x32 :1683, inv_dct32x16 :1705, the
+ * square inverses :1590-1620): `count` blocks of W H coefficients in
+ * jxg_op_dct's order back to row-major H x W samples. */
+int32_t jxg_op_idct(void* ctx, int32_t kind, const float* coefficients, uint64_t count,
+                    float* blocks);
 /* AcTokens::from (src/entropy/token_stream.rs:59-76) per group: `tokens`
  * from group_offsets[0] to group_offsets[num_groups] (host arrays) into the
  * storage form of jxg_frontend_output.packed_tokens; `word_offsets` gets

@@ -344,6 +344,15 @@ class FrontendContext:
                                          out.ctypes.data, dc.ctypes.data))
         return out, dc
 
+    def idct(self, name: str, coefficients: np.ndarray) -> np.ndarray:
+        """The inverse of `dct` (IdctMethods, src/dct.rs:358): (count, H, W) samples."""
+        kind, w, h, _ = self.DCT_KINDS[name]
+        c = np.ascontiguousarray(coefficients, np.float32).reshape(-1, h * w)
+        out = np.zeros_like(c)
+        self._check(self._lib.jxg_op_idct(self._ctx, kind, c.ctypes.data, c.shape[0],
+                                          out.ctypes.data))
+        return out.reshape(-1, h, w)
+
     def pack_tokens(self, tokens: np.ndarray, group_offsets: np.ndarray
                     ) -> tuple[np.ndarray, np.ndarray]:
         """AcTokens::from per group (src/entropy/token_stream.rs:59-76) on the

@@ -1356,6 +1356,53 @@ int32_t jxg_op_dct(void* ctx, int32_t kind, const float* blocks, uint64_t count,
   return JXG_OK;
 }
 
+int32_t jxg_op_idct(void* ctx, int32_t kind, const float* coefficients, uint64_t count,
+                    float* blocks) {
+  Context* c = static_cast<Context*>(ctx);
+  static const int kW[7] = {8, 16, 8, 16, 32, 16, 32}, kH[7] = {8, 8, 16, 16, 16, 32, 32};
+  if (!c || !coefficients || !blocks || kind < 0 || kind > 6) return JXG_ERR_INVALID_ARGUMENT;
+  if (count == 0) return JXG_OK;
+  if (count > (1ull << 31)) return JXG_ERR_DIMENSION_TOO_LARGE;
+  cudaSetDevice(c->device);
+  const size_t bytes = count * kW[kind] * kH[kind] * 4;
+  int st;
+  if ((st = jxg::ensure(c, c->op_in, bytes)) || (st = jxg::ensure(c, c->op_out, bytes))) return st;
+  cudaStream_t s = c->stream;
+  const float* din = static_cast<const float*>(c->op_in.ptr);
+  float* dout = static_cast<float*>(c->op_out.ptr);
+  JXG_CUDA(c, cudaMemcpyAsync(c->op_in.ptr, coefficients, bytes, cudaMemcpyHostToDevice, s));
+  const unsigned grid = static_cast<unsigned>((count + jxg::kDctWarps - 1) / jxg::kDctWarps);
+  const unsigned threads = 32 * jxg::kDctWarps;
+  const int64_t cnt = static_cast<int64_t>(count);
+  st = jxg::launch(c, "k_idct_blocks", c->timing, [&] {
+    switch (kind) {
+      case jxg::kDct8x8:
+        jxg::k_idct_blocks<8, 8, jxg::kIdctSquare><<<grid, threads, 0, s>>>(din, cnt, dout);
+        break;
+      case jxg::kDct8x16:
+        jxg::k_idct_blocks<16, 8, jxg::kIdctRowsFirst><<<grid, threads, 0, s>>>(din, cnt, dout);
+        break;
+      case jxg::kDct16x8:
+        jxg::k_idct_blocks<8, 16, jxg::kIdctColsFirst><<<grid, threads, 0, s>>>(din, cnt, dout);
+        break;
+      case jxg::kDct16x16:
+        jxg::k_idct_blocks<16, 16, jxg::kIdctSquare><<<grid, threads, 0, s>>>(din, cnt, dout);
+        break;
+      case jxg::kDct16x32:
+        jxg::k_idct_blocks<32, 16, jxg::kIdctRowsFirst><<<grid, threads, 0, s>>>(din, cnt, dout);
+        break;
+      case jxg::kDct32x16:
+        jxg::k_idct_blocks<16, 32, jxg::kIdctColsFirst><<<grid, threads, 0, s>>>(din, cnt, dout);
+        break;
+      default:
+        jxg::k_idct_blocks<32, 32, jxg::kIdctSquare><<<grid, threads, 0, s>>>(din, cnt, dout);
+    }
+  });
+  if (st) return st;
+  JXG_CUDA(c, cudaMemcpyAsync(blocks, dout, bytes, cudaMemcpyDeviceToHost, s));
+  return jxg::wait(c);
+}
+
 int32_t jxg_op_pack_tokens(void* ctx, const jxg_token* tokens, const uint64_t* group_offsets,
                            uint64_t num_groups, uint32_t* words, uint64_t capacity,
                            uint64_t* word_offsets) {

@@ -1054,6 +1054,165 @@ int orc_dct(int kind, const float* in, float* out, float* dc) {
   return 0;
 }
 
+/* ---- inverse transforms (src/dct.rs:1498-1730) ----------------------
+ * The reciprocal tables are 1 / WC rounded to f32, written as their values;
+ * IS2 is 1 / sqrt(2) as f32. */
+static const float IS2F = 0x1.6a09e6p-1f;
+static const float INV_WC4[2] = {0x1.d906bcp+0f, 0x1.87de2ap-1f};
+static const float INV_WC8[4] = {0x1.f6297cp+0f, 0x1.a9b662p+0f, 0x1.1c73b4p+0f, 0x1.8f8b82p-2f};
+static const float INV_WC16[8] = {0x1.fd88dap+0f, 0x1.e9f416p+0f, 0x1.c38b30p+0f, 0x1.8bc806p+0f,
+                                  0x1.44cf32p+0f, 0x1.e2b5d4p-1f, 0x1.294062p-1f, 0x1.917a6cp-3f};
+static const float INV_WC32[16] = {0x1.ff6220p+0f, 0x1.fa755ap+0f, 0x1.f0a7f0p+0f, 0x1.e21212p+0f,
+                                   0x1.ced7aep+0f, 0x1.b72834p+0f, 0x1.9b3e04p+0f, 0x1.7b5df2p+0f,
+                                   0x1.57d692p+0f, 0x1.30ff80p+0f, 0x1.073878p+0f, 0x1.b5d0fep-1f,
+                                   0x1.58f9a8p-1f, 0x1.f19f98p-2f, 0x1.2c8106p-2f, 0x1.91f65ep-4f};
+
+/* inv_dct1d_2 (:1500): the half sum and half difference. */
+static inline void inv_dct1d_2(float* b) {
+  const float s = b[0], d = b[1];
+  b[0] = (s + d) * 0.5f;
+  b[1] = (s - d) * 0.5f;
+}
+
+/* inv_dct1d_4 (:1508-1523). */
+static inline void inv_dct1d_4(float* b) {
+  float t[4] = {b[0], b[2], b[1], b[3]};
+  t[2] = (t[2] - t[3]) * IS2F;
+  inv_dct1d_2(t + 2);
+  t[2] *= INV_WC4[0];
+  t[3] *= INV_WC4[1];
+  inv_dct1d_2(t);
+  b[0] = (t[0] + t[2]) * 0.5f;
+  b[3] = (t[0] - t[2]) * 0.5f;
+  b[1] = (t[1] + t[3]) * 0.5f;
+  b[2] = (t[1] - t[3]) * 0.5f;
+}
+
+/* inv_dct1d_8 (:1525-1542), inv_dct1d_16 (:1546-1566), inv_dct1d_32
+ * (:1568-1588): de-interleave, undo the odd half's running sums from the
+ * top, the odd half through the half-size inverse and 1 / WC, the even half
+ * through the half-size inverse, half sums and differences mirrored. */
+static inline void inv_dct1d_8(float* b) {
+  float t[8];
+  for (int i = 0; i < 4; i++) {
+    t[i] = b[2 * i];
+    t[4 + i] = b[2 * i + 1];
+  }
+  t[6] -= t[7];
+  t[5] -= t[6];
+  t[4] = (t[4] - t[5]) * IS2F;
+  inv_dct1d_4(t + 4);
+  for (int i = 0; i < 4; i++) t[4 + i] *= INV_WC8[i];
+  inv_dct1d_4(t);
+  for (int i = 0; i < 4; i++) {
+    b[i] = (t[i] + t[4 + i]) * 0.5f;
+    b[7 - i] = (t[i] - t[4 + i]) * 0.5f;
+  }
+}
+
+static inline void inv_dct1d_16(float* b) {
+  float t[16];
+  for (int i = 0; i < 8; i++) {
+    t[i] = b[2 * i];
+    t[8 + i] = b[2 * i + 1];
+  }
+  for (int i = 14; i >= 9; i--) t[i] -= t[i + 1];
+  t[8] = (t[8] - t[9]) * IS2F;
+  inv_dct1d_8(t + 8);
+  for (int i = 0; i < 8; i++) t[8 + i] *= INV_WC16[i];
+  inv_dct1d_8(t);
+  for (int i = 0; i < 8; i++) {
+    b[i] = (t[i] + t[8 + i]) * 0.5f;
+    b[15 - i] = (t[i] - t[8 + i]) * 0.5f;
+  }
+}
+
+static inline void inv_dct1d_32(float* b) {
+  float t[32];
+  for (int i = 0; i < 16; i++) {
+    t[i] = b[2 * i];
+    t[16 + i] = b[2 * i + 1];
+  }
+  for (int i = 30; i >= 17; i--) t[i] -= t[i + 1];
+  t[16] = (t[16] - t[17]) * IS2F;
+  inv_dct1d_16(t + 16);
+  for (int i = 0; i < 16; i++) t[16 + i] *= INV_WC32[i];
+  inv_dct1d_16(t);
+  for (int i = 0; i < 16; i++) {
+    b[i] = (t[i] + t[16 + i]) * 0.5f;
+    b[31 - i] = (t[i] - t[16 + i]) * 0.5f;
+  }
+}
+
+static inline void inv_dct1d_n(float* b, int n) {
+  if (n == 8) inv_dct1d_8(b);
+  else if (n == 16) inv_dct1d_16(b);
+  else inv_dct1d_32(b);
+}
+
+/* Inverse of a square transform (inv_dct_square, :1590-1620): coefficients
+ * transposed and scaled by N, columns, then rows. */
+static void idct_square(const float* c, int n, float* out) {
+  float col[32];
+  const float scale = (float)(n * n);
+  for (int a = 0; a < n; a++)
+    for (int b = 0; b < n; b++) out[b * n + a] = c[a * n + b] * scale;
+  for (int u = 0; u < n; u++) {
+    for (int v = 0; v < n; v++) col[v] = out[v * n + u];
+    inv_dct1d_n(col, n);
+    for (int v = 0; v < n; v++) out[v * n + u] = col[v];
+  }
+  for (int v = 0; v < n; v++) inv_dct1d_n(out + v * n, n);
+}
+
+/* Inverse of a rows-first transform (inv_dct8x16 :1634, inv_dct16x32
+ * :1683): coefficients in place scaled by N, columns (length H), rows. */
+static void idct_rows_first(const float* c, int W, int H, float* out) {
+  float col[32];
+  const float scale = (float)(W * H);
+  for (int k = 0; k < W * H; k++) out[k] = c[k] * scale;
+  for (int u = 0; u < W; u++) {
+    for (int v = 0; v < H; v++) col[v] = out[v * W + u];
+    inv_dct1d_n(col, H);
+    for (int v = 0; v < H; v++) out[v * W + u] = col[v];
+  }
+  for (int r = 0; r < H; r++) inv_dct1d_n(out + r * W, W);
+}
+
+/* Inverse of a columns-first transform (inv_dct16x8 :1658, inv_dct32x16
+ * :1705): per pixel row v the W-point inverse of coefficients c[u H + v]
+ * scaled by N, then per column the H-point inverse. */
+static void idct_cols_first(const float* c, int W, int H, float* out) {
+  float acd[1024], row[32], col[32];
+  const float scale = (float)(W * H);
+  for (int v = 0; v < H; v++) {
+    for (int u = 0; u < W; u++) row[u] = c[u * H + v] * scale;
+    inv_dct1d_n(row, W);
+    for (int u = 0; u < W; u++) acd[v * W + u] = row[u];
+  }
+  for (int u = 0; u < W; u++) {
+    for (int v = 0; v < H; v++) col[v] = acd[v * W + u];
+    inv_dct1d_n(col, H);
+    for (int i = 0; i < H; i++) out[i * W + u] = col[i];
+  }
+}
+
+/* The inverse of orc_dct's transform `kind`: W H coefficients back to a
+ * row-major H x W block.  Returns 0, or -1 for an unknown kind. */
+int orc_idct(int kind, const float* coeffs, float* out) {
+  switch (kind) {
+    case JXG_ORC_DCT8X8: idct_square(coeffs, 8, out); break;
+    case JXG_ORC_DCT8X16: idct_rows_first(coeffs, 16, 8, out); break;
+    case JXG_ORC_DCT16X8: idct_cols_first(coeffs, 8, 16, out); break;
+    case JXG_ORC_DCT16X16: idct_square(coeffs, 16, out); break;
+    case JXG_ORC_DCT16X32: idct_rows_first(coeffs, 32, 16, out); break;
+    case JXG_ORC_DCT32X16: idct_cols_first(coeffs, 16, 32, out); break;
+    case JXG_ORC_DCT32X32: idct_square(coeffs, 32, out); break;
+    default: return -1;
+  }
+  return 0;
+}
+
 /* dct1d_16 / dct1d_32 of one vector in place (n = 8, 16 or 32). */
 void orc_dct1d(float* b, int n) { dct1d_n(b, n); }
 

@@ -364,3 +364,16 @@ def dct1d(vec: np.ndarray) -> np.ndarray:
     assert v.size in (8, 16, 32)
     lib().orc_dct1d(v.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(v.size))
     return v
+
+
+def idct(name: str, coeffs: np.ndarray) -> np.ndarray:
+    """The inverse of `dct(name, ...)` (IdctMethods, src/dct.rs:358-416;
+    inv_dct8x16 :1634, inv_dct16x8 :1658, inv_dct16x32 :1683, inv_dct32x16
+    :1705, the square inverses :1590-1620): (H, W) samples."""
+    kind, w, h, _ = DCT_KINDS[name]
+    c = np.ascontiguousarray(coeffs, np.float32).reshape(-1)
+    assert c.size == w * h
+    out = np.zeros((h, w), np.float32)
+    assert lib().orc_idct(ctypes.c_int(kind), c.ctypes.data_as(ctypes.c_void_p),
+                          out.ctypes.data_as(ctypes.c_void_p)) == 0
+    return out

@@ -39,3 +39,16 @@ def test_dct_operator_rejects_bad_kinds(ctx):
     assert lib.jxg_op_dct(ctx.handle, 7, b.ctypes.data, 1, b.ctypes.data, None) != 0
     assert lib.jxg_op_dct(ctx.handle, -1, b.ctypes.data, 1, b.ctypes.data, None) != 0
     assert lib.jxg_op_dct(ctx.handle, 3, b.ctypes.data, 0, b.ctypes.data, None) == 0  # no blocks
+
+
+@pytest.mark.parametrize("name", ["8x8", "8x16", "16x8", "16x16", "16x32", "32x16", "32x32"])
+def test_inverse_matches_oracle_and_round_trips(ctx, name):
+    _, w, h, _ = O.DCT_KINDS[name]
+    rng = np.random.default_rng(w * 7 + h)
+    blocks = rng.uniform(-1.0, 1.0, (120, h, w)).astype(np.float32)
+    coeffs, _ = ctx.dct(name, blocks)
+    back = ctx.idct(name, coeffs)
+    for i in range(blocks.shape[0]):
+        want = O.idct(name, coeffs[i])
+        assert np.array_equal(back[i].view(np.uint32), want.view(np.uint32)), (name, i)
+    assert np.abs(back - blocks).max() < 1e-4

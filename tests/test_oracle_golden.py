@@ -381,3 +381,14 @@ def test_rectangular_dc_follows_the_halves():
     assert dc[0] < dc[1]
     _, dc = O.dct("16x8", a.T.copy())
     assert dc[0] < dc[1]
+
+
+@pytest.mark.parametrize("name", ["8x8", "8x16", "16x8", "16x16", "16x32", "32x16", "32x32"])
+def test_transforms_round_trip(name):
+    # src/dct.rs:2916-2926 (and the other round-trip tests): the inverse of
+    # each transform gives back the samples ((i * 53) % 97 / 97) within 1e-4
+    _, w, h, _ = O.DCT_KINDS[name]
+    px = (np.array([(i * 53) % 97 for i in range(w * h)], np.float32) / np.float32(97.0)).reshape(h, w)
+    coeffs, _ = O.dct(name, px)
+    back = O.idct(name, coeffs)
+    assert np.abs(back - px).max() < 1e-4
