@@ -265,6 +265,12 @@ int32_t jxg_op_dct(void* ctx, int32_t kind, const float* blocks, uint64_t count,
  * jxg_op_dct's order back to row-major H x W samples. */
 int32_t jxg_op_idct(void* ctx, int32_t kind, const float* coefficients, uint64_t count,
                     float* blocks);
+/* The 8x8-sized transforms besides DCT8 on `count` row-major 8x8 blocks:
+ * kind 0 identity8x8 (src/dct.rs:185), 1 dct2x2_8x8 (:306), 2 dct4x4
+ * (:1163), 3 dct4x8 (:1238), 4 dct8x4 (:1319), 5 inv_identity8x8 (:225),
+ * 6 inv_dct2x2_8x8 (:345); 64 values out per block. */
+int32_t jxg_op_small_transform(void* ctx, int32_t kind, const float* blocks, uint64_t count,
+                               float* out);
 /* AcTokens::from (src/entropy/token_stream.rs:59-76) per group: `tokens`
  * from group_offsets[0] to group_offsets[num_groups] (host arrays) into the
  * storage form of jxg_frontend_output.packed_tokens; `word_offsets` gets

@@ -37,6 +37,7 @@ EXPORTS = [
     "jxg_op_pack_tokens",
     "jxg_op_dct",
     "jxg_op_idct",
+    "jxg_op_small_transform",
     "jxg_token_offsets_noalloc",
     "jxg_selftest_bounded_wait",
     "jxg_selftest_token_lookback",
@@ -150,6 +151,7 @@ def load() -> ctypes.CDLL:
         "jxg_op_pack_tokens": (i32, [vp, vp, vp, u64, vp, u64, vp]),
         "jxg_op_dct": (i32, [vp, i32, vp, u64, vp, vp]),
         "jxg_op_idct": (i32, [vp, i32, vp, u64, vp]),
+        "jxg_op_small_transform": (i32, [vp, i32, vp, u64, vp]),
         "jxg_token_offsets_noalloc": (i32, [vp, u64, vp, vp, vp]),
         "jxg_selftest_bounded_wait": (i32, [vp, ctypes.c_uint32]),
         "jxg_selftest_token_lookback": (i32, [vp, ctypes.c_uint32]),

@@ -353,6 +353,19 @@ class FrontendContext:
                                           out.ctypes.data))
         return out.reshape(-1, h, w)
 
+    SMALL_TRANSFORMS = {"identity": 0, "dct2x2": 1, "dct4x4": 2, "dct4x8": 3, "dct8x4": 4,
+                        "inv_identity": 5, "inv_dct2x2": 6}
+
+    def small_transform(self, name: str, blocks: np.ndarray) -> np.ndarray:
+        """The 8x8-sized transforms besides DCT8 (identity8x8, dct2x2_8x8,
+        dct4x4, dct4x8, dct8x4 and the identity / DCT2x2 inverses, src/dct.rs)
+        of (count, 8, 8) blocks: (count, 64)."""
+        b = np.ascontiguousarray(blocks, np.float32).reshape(-1, 64)
+        out = np.zeros_like(b)
+        self._check(self._lib.jxg_op_small_transform(self._ctx, self.SMALL_TRANSFORMS[name],
+                                                     b.ctypes.data, b.shape[0], out.ctypes.data))
+        return out
+
     def pack_tokens(self, tokens: np.ndarray, group_offsets: np.ndarray
                     ) -> tuple[np.ndarray, np.ndarray]:
         """AcTokens::from per group (src/entropy/token_stream.rs:59-76) on the

@@ -1403,6 +1403,28 @@ int32_t jxg_op_idct(void* ctx, int32_t kind, const float* coefficients, uint64_t
   return jxg::wait(c);
 }
 
+int32_t jxg_op_small_transform(void* ctx, int32_t kind, const float* blocks, uint64_t count,
+                               float* out) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !blocks || !out || kind < 0 || kind > 6) return JXG_ERR_INVALID_ARGUMENT;
+  if (count == 0) return JXG_OK;
+  if (count > (1ull << 31)) return JXG_ERR_DIMENSION_TOO_LARGE;
+  cudaSetDevice(c->device);
+  const size_t bytes = count * 64 * 4;
+  int st;
+  if ((st = jxg::ensure(c, c->op_in, bytes)) || (st = jxg::ensure(c, c->op_out, bytes))) return st;
+  cudaStream_t s = c->stream;
+  JXG_CUDA(c, cudaMemcpyAsync(c->op_in.ptr, blocks, bytes, cudaMemcpyHostToDevice, s));
+  st = jxg::launch(c, "k_small_transform_blocks", c->timing, [&] {
+    jxg::k_small_transform_blocks<<<static_cast<unsigned>((count + 127) / 128), 128, 0, s>>>(
+        kind, static_cast<const float*>(c->op_in.ptr), static_cast<int64_t>(count),
+        static_cast<float*>(c->op_out.ptr));
+  });
+  if (st) return st;
+  JXG_CUDA(c, cudaMemcpyAsync(out, c->op_out.ptr, bytes, cudaMemcpyDeviceToHost, s));
+  return jxg::wait(c);
+}
+
 int32_t jxg_op_pack_tokens(void* ctx, const jxg_token* tokens, const uint64_t* group_offsets,
                            uint64_t num_groups, uint32_t* words, uint64_t capacity,
                            uint64_t* word_offsets) {

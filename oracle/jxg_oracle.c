@@ -1213,6 +1213,205 @@ int orc_idct(int kind, const float* coeffs, float* out) {
   return 0;
 }
 
+/* ---- the 8x8-sized transforms besides DCT8 (src/dct.rs) ------------- */
+
+/* The 2x2 Hadamard of coefficients 0, 1, 8, 9, scaled 1/4. */
+static void hadamard_0189(float* o) {
+  const float b00 = o[0], b01 = o[1], b10 = o[8], b11 = o[9];
+  o[0] = (b00 + b01 + b10 + b11) * 0.25f;
+  o[1] = (b00 + b01 - b10 - b11) * 0.25f;
+  o[8] = (b00 - b01 + b10 - b11) * 0.25f;
+  o[9] = (b00 - b01 - b10 + b11) * 0.25f;
+}
+
+/* identity8x8 (:185-214): per 4x4 quadrant the residuals from its (1, 1)
+ * anchor, the displaced top-left residual in the anchor's slot, the
+ * quadrant mean in coefficient (qy, qx); then the Hadamard of the means. */
+static void identity8x8(const float* in, float* o) {
+  for (int qy = 0; qy < 2; qy++)
+    for (int qx = 0; qx < 2; qx++) {
+      const float anchor = in[(qy * 4 + 1) * 8 + qx * 4 + 1];
+      float mean = 0.0f;
+      for (int iy = 0; iy < 4; iy++)
+        for (int ix = 0; ix < 4; ix++) {
+          const float v = in[(qy * 4 + iy) * 8 + qx * 4 + ix];
+          mean += v;
+          if (ix == 1 && iy == 1) continue;
+          o[(qy + iy * 2) * 8 + qx + ix * 2] = v - anchor;
+        }
+      o[(qy + 2) * 8 + qx + 2] = o[qy * 8 + qx];
+      o[qy * 8 + qx] = mean * (1.0f / 16.0f);
+    }
+  hadamard_0189(o);
+}
+
+/* inv_identity8x8 (:225-264). */
+static void inv_identity8x8(const float* c, float* o) {
+  const float means[4] = {c[0] + c[1] + c[8] + c[9], c[0] + c[1] - c[8] - c[9],
+                          c[0] - c[1] + c[8] - c[9], c[0] - c[1] - c[8] + c[9]};
+  for (int qy = 0; qy < 2; qy++)
+    for (int qx = 0; qx < 2; qx++) {
+      float residual_sum = 0.0f;
+      for (int iy = 0; iy < 4; iy++)
+        for (int ix = 0; ix < 4; ix++) {
+          if (ix == 1 && iy == 1) continue;
+          residual_sum += (ix == 0 && iy == 0) ? c[(qy + 2) * 8 + qx + 2] : c[(qy + iy * 2) * 8 + qx + ix * 2];
+        }
+      const float anchor = means[qy * 2 + qx] - residual_sum * (1.0f / 16.0f);
+      for (int iy = 0; iy < 4; iy++)
+        for (int ix = 0; ix < 4; ix++) {
+          const float r = (ix == 1 && iy == 1) ? 0.0f
+                          : (ix == 0 && iy == 0) ? c[(qy + 2) * 8 + qx + 2]
+                                                 : c[(qy + iy * 2) * 8 + qx + ix * 2];
+          o[(qy * 4 + iy) * 8 + qx * 4 + ix] = anchor + r;
+        }
+    }
+}
+
+/* dct2_top_block::<S> (:274-299) and dct2x2_8x8 (:306-312). */
+static void dct2_top_block(const float* in, int S, float* o) {
+  float temp[64] = {0};
+  const int half = S / 2;
+  for (int y = 0; y < half; y++)
+    for (int x = 0; x < half; x++) {
+      const float c00 = in[(y * 2) * 8 + x * 2], c01 = in[(y * 2) * 8 + x * 2 + 1];
+      const float c10 = in[(y * 2 + 1) * 8 + x * 2], c11 = in[(y * 2 + 1) * 8 + x * 2 + 1];
+      temp[y * 8 + x] = (c00 + c01 + c10 + c11) * 0.25f;
+      temp[y * 8 + half + x] = (c00 + c01 - c10 - c11) * 0.25f;
+      temp[(y + half) * 8 + x] = (c00 - c01 + c10 - c11) * 0.25f;
+      temp[(y + half) * 8 + half + x] = (c00 - c01 - c10 + c11) * 0.25f;
+    }
+  for (int y = 0; y < S; y++)
+    for (int x = 0; x < S; x++) o[y * 8 + x] = temp[y * 8 + x];
+}
+
+static void dct2x2_8x8(const float* in, float* o) {
+  float snap[64];
+  dct2_top_block(in, 8, o);
+  memcpy(snap, o, sizeof(snap));
+  dct2_top_block(snap, 4, o);
+  memcpy(snap, o, sizeof(snap));
+  dct2_top_block(snap, 2, o);
+}
+
+/* inv_dct2_top_block::<S> (:322-341) and inv_dct2x2_8x8 (:345-354). */
+static void inv_dct2_top_block(const float* in, int S, float* o) {
+  const int half = S / 2;
+  for (int y = 0; y < half; y++)
+    for (int x = 0; x < half; x++) {
+      const float r00 = in[y * 8 + x], r01 = in[y * 8 + half + x];
+      const float r10 = in[(y + half) * 8 + x], r11 = in[(y + half) * 8 + half + x];
+      o[(y * 2) * 8 + x * 2] = r00 + r01 + r10 + r11;
+      o[(y * 2) * 8 + x * 2 + 1] = r00 + r01 - r10 - r11;
+      o[(y * 2 + 1) * 8 + x * 2] = r00 - r01 + r10 - r11;
+      o[(y * 2 + 1) * 8 + x * 2 + 1] = r00 - r01 - r10 + r11;
+    }
+}
+
+static void inv_dct2x2_8x8(const float* c, float* o) {
+  float a[64], snap[64];
+  memcpy(a, c, sizeof(a));
+  memcpy(snap, a, sizeof(snap));
+  inv_dct2_top_block(snap, 2, a);
+  memcpy(snap, a, sizeof(snap));
+  inv_dct2_top_block(snap, 4, a);
+  memcpy(snap, a, sizeof(snap));
+  inv_dct2_top_block(snap, 8, o);
+}
+
+/* dct4x4_2d (:1061-1075) and dct4x4 (:1163-1190): each 4x4 quadrant through
+ * rows then columns of dct1d_4 (transposed, 1/16), interleaved, then the
+ * Hadamard of the quadrant DCs. */
+static void dct4x4_2d(const float* in, float* out) {
+  float tmp[16];
+  memcpy(tmp, in, sizeof(tmp));
+  for (int r = 0; r < 4; r++) dct1d_4(tmp + r * 4);
+  for (int x = 0; x < 4; x++) {
+    float col[4] = {tmp[x], tmp[4 + x], tmp[8 + x], tmp[12 + x]};
+    dct1d_4(col);
+    for (int i = 0; i < 4; i++) out[x * 4 + i] = col[i] * (1.0f / 16.0f);
+  }
+}
+
+static void dct4x4(const float* in, float* o) {
+  for (int qy = 0; qy < 2; qy++)
+    for (int qx = 0; qx < 2; qx++) {
+      float blk[16], d[16];
+      for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) blk[r * 4 + c] = in[(qy * 4 + r) * 8 + qx * 4 + c];
+      dct4x4_2d(blk, d);
+      for (int iy = 0; iy < 4; iy++)
+        for (int ix = 0; ix < 4; ix++) o[(qy + iy * 2) * 8 + qx + ix * 2] = d[iy * 4 + ix];
+    }
+  hadamard_0189(o);
+}
+
+/* dct4x8_2d (:1198-1220) and dct4x8 (:1238-1262): each 4-row half through
+ * column dct1d_4 then row dct1d_8 (1/32), rows interleaved, the 2-point
+ * Hadamard of the half DCs. */
+static void dct4x8(const float* in, float* o) {
+  for (int y = 0; y < 2; y++) {
+    float t[32];
+    for (int r = 0; r < 4; r++)
+      for (int c = 0; c < 8; c++) t[r * 8 + c] = in[(y * 4 + r) * 8 + c];
+    for (int c = 0; c < 8; c++) {
+      float col[4] = {t[c], t[8 + c], t[16 + c], t[24 + c]};
+      dct1d_4(col);
+      for (int vf = 0; vf < 4; vf++) t[vf * 8 + c] = col[vf];
+    }
+    for (int vf = 0; vf < 4; vf++) {
+      dct1d_8(t + vf * 8);
+      for (int k = 0; k < 8; k++) t[vf * 8 + k] *= 1.0f / 32.0f;
+    }
+    for (int iy = 0; iy < 4; iy++)
+      for (int ix = 0; ix < 8; ix++) o[(y + iy * 2) * 8 + ix] = t[iy * 8 + ix];
+  }
+  const float b0 = o[0], b1 = o[8];
+  o[0] = (b0 + b1) * 0.5f;
+  o[8] = (b0 - b1) * 0.5f;
+}
+
+/* dct8x4_2d (:1267-1298) and dct8x4 (:1319-1340): each 4-column half
+ * through column dct1d_8 then row dct1d_4 (transposed, 1/32). */
+static void dct8x4(const float* in, float* o) {
+  for (int x = 0; x < 2; x++) {
+    float tmp[32], d[32];
+    for (int c = 0; c < 4; c++) {
+      float col[8];
+      for (int r = 0; r < 8; r++) col[r] = in[r * 8 + x * 4 + c];
+      dct1d_8(col);
+      for (int vf = 0; vf < 8; vf++) tmp[vf * 4 + c] = col[vf];
+    }
+    for (int vf = 0; vf < 8; vf++) {
+      float row[4] = {tmp[vf * 4], tmp[vf * 4 + 1], tmp[vf * 4 + 2], tmp[vf * 4 + 3]};
+      dct1d_4(row);
+      for (int hf = 0; hf < 4; hf++) d[hf * 8 + vf] = row[hf] * (1.0f / 32.0f);
+    }
+    for (int iy = 0; iy < 4; iy++)
+      for (int ix = 0; ix < 8; ix++) o[(x + iy * 2) * 8 + ix] = d[iy * 8 + ix];
+  }
+  const float b0 = o[0], b1 = o[8];
+  o[0] = (b0 + b1) * 0.5f;
+  o[8] = (b0 - b1) * 0.5f;
+}
+
+/* The 8x8-sized transforms: 0 identity, 1 DCT2x2, 2 DCT4x4, 3 DCT4x8,
+ * 4 DCT8x4 (forward), 5 / 6 the identity / DCT2x2 inverses.  Returns 0, or
+ * -1 for an unknown kind. */
+int orc_small_transform(int kind, const float* in, float* out) {
+  switch (kind) {
+    case 0: identity8x8(in, out); break;
+    case 1: dct2x2_8x8(in, out); break;
+    case 2: dct4x4(in, out); break;
+    case 3: dct4x8(in, out); break;
+    case 4: dct8x4(in, out); break;
+    case 5: inv_identity8x8(in, out); break;
+    case 6: inv_dct2x2_8x8(in, out); break;
+    default: return -1;
+  }
+  return 0;
+}
+
 /* dct1d_16 / dct1d_32 of one vector in place (n = 8, 16 or 32). */
 void orc_dct1d(float* b, int n) { dct1d_n(b, n); }
 

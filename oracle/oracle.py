@@ -377,3 +377,20 @@ def idct(name: str, coeffs: np.ndarray) -> np.ndarray:
     assert lib().orc_idct(ctypes.c_int(kind), c.ctypes.data_as(ctypes.c_void_p),
                           out.ctypes.data_as(ctypes.c_void_p)) == 0
     return out
+
+
+# The 8x8-sized transforms besides DCT8 (orc_small_transform kinds)
+SMALL_TRANSFORMS = {"identity": 0, "dct2x2": 1, "dct4x4": 2, "dct4x8": 3, "dct8x4": 4,
+                    "inv_identity": 5, "inv_dct2x2": 6}
+
+
+def small_transform(name: str, block: np.ndarray) -> np.ndarray:
+    """identity8x8 (src/dct.rs:185), dct2x2_8x8 (:306), dct4x4 (:1163),
+    dct4x8 (:1238), dct8x4 (:1319), inv_identity8x8 (:225), inv_dct2x2_8x8
+    (:345) of one 8x8 block: 64 values."""
+    b = np.ascontiguousarray(block, np.float32).reshape(64)
+    out = np.zeros(64, np.float32)
+    assert lib().orc_small_transform(ctypes.c_int(SMALL_TRANSFORMS[name]),
+                                     b.ctypes.data_as(ctypes.c_void_p),
+                                     out.ctypes.data_as(ctypes.c_void_p)) == 0
+    return out

@@ -52,3 +52,16 @@ def test_inverse_matches_oracle_and_round_trips(ctx, name):
         want = O.idct(name, coeffs[i])
         assert np.array_equal(back[i].view(np.uint32), want.view(np.uint32)), (name, i)
     assert np.abs(back - blocks).max() < 1e-4
+
+
+@pytest.mark.parametrize("name", ["identity", "dct2x2", "dct4x4", "dct4x8", "dct8x4",
+                                  "inv_identity", "inv_dct2x2"])
+def test_small_transforms_match_oracle(ctx, name):
+    rng = np.random.default_rng(len(name) * 31)
+    blocks = rng.uniform(-1.0, 1.0, (300, 8, 8)).astype(np.float32)
+    blocks[0] = 0.5
+    blocks[1] *= 1e5
+    got = ctx.small_transform(name, blocks)
+    for i, b in enumerate(blocks):
+        want = O.small_transform(name, b)
+        assert np.array_equal(got[i].view(np.uint32), want.view(np.uint32)), (name, i)

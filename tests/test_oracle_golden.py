@@ -392,3 +392,33 @@ def test_transforms_round_trip(name):
     coeffs, _ = O.dct(name, px)
     back = O.idct(name, coeffs)
     assert np.abs(back - px).max() < 1e-4
+
+
+def _pattern(fn):
+    return np.array([fn(float(i % 8), float(i // 8)) for i in range(64)], np.float32)
+
+
+@pytest.mark.parametrize("fwd,inv,fn", [
+    # src/dct.rs:3469-3485 and :3488-3504
+    ("identity", "inv_identity",
+     lambda x, y: np.float32(0.31) * np.float32(x) - np.float32(0.17) * np.float32(y)
+     + np.float32(math.sin(np.float32(x * y * np.float32(0.23))))),
+    ("dct2x2", "inv_dct2x2",
+     lambda x, y: np.float32(math.sin(np.float32(0.37) * np.float32(x) + np.float32(0.61) * np.float32(y)))
+     + np.float32(0.07) * np.float32(x) * np.float32(y)),
+])
+def test_identity_and_dct2x2_round_trip_and_keep_the_dc(fwd, inv, fn):
+    inp = _pattern(fn)
+    coeffs = O.small_transform(fwd, inp)
+    assert abs(float(coeffs[0]) - float(inp.sum(dtype=np.float32)) * (1.0 / 64.0)) < 1e-6
+    back = O.small_transform(inv, coeffs)
+    assert np.abs(back - inp).max() < 2e-6
+
+
+@pytest.mark.parametrize("name", ["dct4x4", "dct4x8", "dct8x4"])
+def test_dct4_family_dc_is_the_block_mean(name):
+    # the quadrant / half DCs go through a Hadamard scaled to the mean, so a
+    # block's first coefficient is its mean (constant and ramp blocks)
+    for blk in (np.full(64, 1.75, np.float32), np.arange(64, dtype=np.float32) / np.float32(7.0)):
+        c = O.small_transform(name, blk)
+        assert abs(float(c[0]) - float(blk.mean())) < 1e-5, (name, c[0])
