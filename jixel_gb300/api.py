@@ -127,7 +127,7 @@ class FrontendResult:
     quant_dc: np.ndarray      # (3, yb, xb) i16, X Y B
     coefficients: np.ndarray | None  # (yb, xb, 3, 64) i32
     num_nzeros: np.ndarray    # (3, yb, xb) u8
-    tokens: np.ndarray        # (n, 2) u32: context, value
+    tokens: np.ndarray | None  # (n, 2) u32: context, value (None when only the packed form was asked for)
     group_offsets: np.ndarray  # (groups + 1,) u64
     histograms: np.ndarray    # (14850, 128) u32
     xyb: np.ndarray | None = None
