@@ -189,6 +189,18 @@ def traffic_from_profiles(kernel: str) -> float | None:
     return None
 
 
+def instructions_from_profiles(kernel: str) -> float | None:
+    """Warp instructions (smsp__inst_executed.sum) of one launch of `kernel`
+    on one 3840x2160 q90 frame, from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "warp_instructions_4k_q90.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith(kernel + ":"):
+            return float(line.split(":", 1)[1])
+    return None
+
+
 def cpu_baseline_run(img, threads: int | None = None, min_seconds: float = 10.0) -> dict:
     """The oracle (C restatement of the reference's scalar path) on the host cores."""
     from jixel_gb300 import distance_from_quality
@@ -338,6 +350,19 @@ def run_gpu(args):
         "algorithmic_bytes_per_launch": algo, "avg_launch_ms": avg_ms,
         "share_of_kernel_time": dom_ms / sum(v[0] for v in ktimes.values()),
     }
+    # the kernels are issue-bound, not DRAM-bound: the dominant kernel's warp
+    # instructions per launch (ncu) over its event-timed launch, against the
+    # SMs' issue rate (four schedulers each issuing one warp instruction a
+    # cycle at the sampled SM clock)
+    inst = instructions_from_profiles(dom_name)
+    sm_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    if inst and sm_mhz:
+        issue_peak = torch.cuda.get_device_properties(dev).multi_processor_count * 4 * sm_mhz * 1e6
+        issue_rate = inst / (avg_ms / 1000.0)
+        roofline["issue"] = {
+            "warp_instructions_per_launch": inst, "achieved": issue_rate, "peak": issue_peak,
+            "unit": "warp instructions/s", "frac": issue_rate / issue_peak,
+        }
     # the timed region ran the same launch sequence as the per-kernel pass
     launches = int(sum(v[1] for v in ktimes.values()))
     # the whole front end per frame: input bytes + 4 B per token + block side
