@@ -244,12 +244,14 @@ int32_t jxg_op_fill_quant_field(void* ctx, const float* xyb, uint64_t width, uin
  * row-major samples in, 64 coefficients (transposed storage, 1/64 scale) out. */
 int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coefficients);
 /* DctFn<W, H, N> of the larger blocks (src/dct.rs: dct8x16 :823, dct16x8
- * :904, dct16x16 :1010, dct32x32 :1980, dct32x16 :2251, dct16x32 :2340;
- * kind 0 is dct8x8 as jxg_op_dct8x8) with the DC values of every covered
- * 8x8 block (dc_from_dct*, :930-2400).  `blocks` holds `count` row-major
- * blocks of H rows of W samples; `coefficients` receives W H coefficients
- * per block in the reference's order, `dc_values` (optional) 1, 2, 2, 4, 8,
- * 8 or 16 values per block for kinds 0..6. */
+ * :904, dct16x16 :1010, dct32x32 :1980, dct32x16 :2251, dct16x32 :2340,
+ * dct32x8 :1742, dct8x32 :1777, dct64x64 :2576, dct64x32 :2659, dct32x64
+ * :2689; kind 0 is dct8x8 as jxg_op_dct8x8) with the DC values of every
+ * covered 8x8 block (dc_from_dct*, :930-2806).  `blocks` holds `count`
+ * row-major blocks of H rows of W samples; `coefficients` receives W H
+ * coefficients per block in the reference's order, `dc_values` (optional)
+ * one value per covered 8x8 block (1, 2, 2, 4, 8, 8, 16, 4, 4, 64, 32, 32
+ * for kinds 0..11) in raster order of those blocks. */
 #define JXG_DCT8X8 0
 #define JXG_DCT8X16 1  /* 8 rows x 16 columns */
 #define JXG_DCT16X8 2
@@ -257,18 +259,26 @@ int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coe
 #define JXG_DCT16X32 4
 #define JXG_DCT32X16 5
 #define JXG_DCT32X32 6
+#define JXG_DCT32X8 7   /* 32 rows x 8 columns */
+#define JXG_DCT8X32 8
+#define JXG_DCT64X64 9
+#define JXG_DCT64X32 10 /* 64 rows x 32 columns */
+#define JXG_DCT32X64 11
 int32_t jxg_op_dct(void* ctx, int32_t kind, const float* blocks, uint64_t count,
                    float* coefficients, float* dc_values);
 /* The inverse transforms (IdctMethods, src/dct.rs:358-416; inv_dct8x16
- * :1634, inv_dct16x8 :1658, inv_dct16x32 :1683, inv_dct32x16 :1705, the
- * square inverses :1590-1620): `count` blocks of W H coefficients in
- * jxg_op_dct's order back to row-major H x W samples. */
+ * :1634, inv_dct16x8 :1658, inv_dct16x32 :1683, inv_dct32x16 :1705,
+ * inv_dct8x32 :1804, inv_dct32x8 :1833, inv_dct64x32 :2710, inv_dct32x64
+ * :2735, the square inverses :1590-1627): `count` blocks of W H
+ * coefficients in jxg_op_dct's order back to row-major H x W samples. */
 int32_t jxg_op_idct(void* ctx, int32_t kind, const float* coefficients, uint64_t count,
                     float* blocks);
 /* The 8x8-sized transforms besides DCT8 on `count` row-major 8x8 blocks:
  * kind 0 identity8x8 (src/dct.rs:185), 1 dct2x2_8x8 (:306), 2 dct4x4
  * (:1163), 3 dct4x8 (:1238), 4 dct8x4 (:1319), 5 inv_identity8x8 (:225),
- * 6 inv_dct2x2_8x8 (:345); 64 values out per block. */
+ * 6 inv_dct2x2_8x8 (:345), 7..10 afv_from_pixels kinds 0..3 (src/afv.rs:207;
+ * AFV corner at the left/right, top/bottom of the block by kind bits 0/1);
+ * 64 values out per block. */
 int32_t jxg_op_small_transform(void* ctx, int32_t kind, const float* blocks, uint64_t count,
                                float* out);
 /* AcTokens::from (src/entropy/token_stream.rs:59-76) per group: `tokens`

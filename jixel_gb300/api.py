@@ -330,7 +330,8 @@ class FrontendContext:
 
     DCT_KINDS = {"8x8": (0, 8, 8, 1), "8x16": (1, 16, 8, 2), "16x8": (2, 8, 16, 2),
                  "16x16": (3, 16, 16, 4), "16x32": (4, 32, 16, 8), "32x16": (5, 16, 32, 8),
-                 "32x32": (6, 32, 32, 16)}
+                 "32x32": (6, 32, 32, 16), "32x8": (7, 8, 32, 4), "8x32": (8, 32, 8, 4),
+                 "64x64": (9, 64, 64, 64), "64x32": (10, 32, 64, 32), "32x64": (11, 64, 32, 32)}
 
     def dct(self, name: str, blocks: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
         """DctFn<W, H, N> (src/dct.rs) of (count, H, W) blocks named rows x
@@ -354,12 +355,14 @@ class FrontendContext:
         return out.reshape(-1, h, w)
 
     SMALL_TRANSFORMS = {"identity": 0, "dct2x2": 1, "dct4x4": 2, "dct4x8": 3, "dct8x4": 4,
-                        "inv_identity": 5, "inv_dct2x2": 6}
+                        "inv_identity": 5, "inv_dct2x2": 6,
+                        "afv0": 7, "afv1": 8, "afv2": 9, "afv3": 10}
 
     def small_transform(self, name: str, blocks: np.ndarray) -> np.ndarray:
         """The 8x8-sized transforms besides DCT8 (identity8x8, dct2x2_8x8,
-        dct4x4, dct4x8, dct8x4 and the identity / DCT2x2 inverses, src/dct.rs)
-        of (count, 8, 8) blocks: (count, 64)."""
+        dct4x4, dct4x8, dct8x4 and the identity / DCT2x2 inverses, src/dct.rs;
+        afv_from_pixels kinds 0..3, src/afv.rs:207) of (count, 8, 8) blocks:
+        (count, 64)."""
         b = np.ascontiguousarray(blocks, np.float32).reshape(-1, 64)
         out = np.zeros_like(b)
         self._check(self._lib.jxg_op_small_transform(self._ctx, self.SMALL_TRANSFORMS[name],

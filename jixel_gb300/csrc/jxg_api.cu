@@ -1303,9 +1303,10 @@ int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coe
 int32_t jxg_op_dct(void* ctx, int32_t kind, const float* blocks, uint64_t count,
                    float* coefficients, float* dc_values) {
   Context* c = static_cast<Context*>(ctx);
-  static const int kW[7] = {8, 16, 8, 16, 32, 16, 32}, kH[7] = {8, 8, 16, 16, 16, 32, 32};
-  static const int kDc[7] = {1, 2, 2, 4, 8, 8, 16};
-  if (!c || !blocks || !coefficients || kind < 0 || kind > 6) return JXG_ERR_INVALID_ARGUMENT;
+  static const int kW[12] = {8, 16, 8, 16, 32, 16, 32, 8, 32, 64, 32, 64};
+  static const int kH[12] = {8, 8, 16, 16, 16, 32, 32, 32, 8, 64, 64, 32};
+  static const int kDc[12] = {1, 2, 2, 4, 8, 8, 16, 4, 4, 64, 32, 32};
+  if (!c || !blocks || !coefficients || kind < 0 || kind > 11) return JXG_ERR_INVALID_ARGUMENT;
   if (count == 0) return JXG_OK;
   if (count > (1ull << 31)) return JXG_ERR_DIMENSION_TOO_LARGE;
   cudaSetDevice(c->device);
@@ -1319,31 +1320,29 @@ int32_t jxg_op_dct(void* ctx, int32_t kind, const float* blocks, uint64_t count,
   float* dout = static_cast<float*>(c->op_out.ptr);
   float* ddc = dout + count * n;
   JXG_CUDA(c, cudaMemcpyAsync(c->op_in.ptr, blocks, bytes, cudaMemcpyHostToDevice, s));
-  const unsigned grid = static_cast<unsigned>((count + jxg::kDctWarps - 1) / jxg::kDctWarps);
-  const unsigned threads = 32 * jxg::kDctWarps;
   const int64_t cnt = static_cast<int64_t>(count);
+  // one warp per block, dct_warps<W, H>() blocks per CTA
+  auto run = [&](auto kernel, int warps) {
+    kernel<<<static_cast<unsigned>((count + warps - 1) / warps), 32 * warps, 0, s>>>(
+        din, cnt, dout, ddc, kind, ndc);
+  };
   st = jxg::launch(c, "k_dct_blocks", c->timing, [&] {
+    using namespace jxg;
     switch (kind) {
-      case jxg::kDct8x8:
-        jxg::k_dct8x8_blocks<<<static_cast<unsigned>((count + 31) / 32), 256, 0, s>>>(din, cnt, dout);
+      case kDct8x8:
+        k_dct8x8_blocks<<<static_cast<unsigned>((count + 31) / 32), 256, 0, s>>>(din, cnt, dout);
         break;
-      case jxg::kDct8x16:
-        jxg::k_dct_blocks<16, 8, false><<<grid, threads, 0, s>>>(din, cnt, dout, ddc, kind, ndc);
-        break;
-      case jxg::kDct16x8:
-        jxg::k_dct_blocks<8, 16, true><<<grid, threads, 0, s>>>(din, cnt, dout, ddc, kind, ndc);
-        break;
-      case jxg::kDct16x16:
-        jxg::k_dct_blocks<16, 16, true><<<grid, threads, 0, s>>>(din, cnt, dout, ddc, kind, ndc);
-        break;
-      case jxg::kDct16x32:
-        jxg::k_dct_blocks<32, 16, false><<<grid, threads, 0, s>>>(din, cnt, dout, ddc, kind, ndc);
-        break;
-      case jxg::kDct32x16:
-        jxg::k_dct_blocks<16, 32, true><<<grid, threads, 0, s>>>(din, cnt, dout, ddc, kind, ndc);
-        break;
-      default:
-        jxg::k_dct_blocks<32, 32, true><<<grid, threads, 0, s>>>(din, cnt, dout, ddc, kind, ndc);
+      case kDct8x16: run(k_dct_blocks<16, 8, false>, dct_warps<16, 8>()); break;
+      case kDct16x8: run(k_dct_blocks<8, 16, true>, dct_warps<8, 16>()); break;
+      case kDct16x16: run(k_dct_blocks<16, 16, true>, dct_warps<16, 16>()); break;
+      case kDct16x32: run(k_dct_blocks<32, 16, false>, dct_warps<32, 16>()); break;
+      case kDct32x16: run(k_dct_blocks<16, 32, true>, dct_warps<16, 32>()); break;
+      case kDct32x32: run(k_dct_blocks<32, 32, true>, dct_warps<32, 32>()); break;
+      case kDct32x8: run(k_dct_blocks<8, 32, true>, dct_warps<8, 32>()); break;
+      case kDct8x32: run(k_dct_blocks<32, 8, false>, dct_warps<32, 8>()); break;
+      case kDct64x64: run(k_dct_blocks<64, 64, true>, dct_warps<64, 64>()); break;
+      case kDct64x32: run(k_dct_blocks<32, 64, true>, dct_warps<32, 64>()); break;
+      default: run(k_dct_blocks<64, 32, false>, dct_warps<64, 32>());  // 32x64
     }
   });
   if (st) return st;
@@ -1359,8 +1358,9 @@ int32_t jxg_op_dct(void* ctx, int32_t kind, const float* blocks, uint64_t count,
 int32_t jxg_op_idct(void* ctx, int32_t kind, const float* coefficients, uint64_t count,
                     float* blocks) {
   Context* c = static_cast<Context*>(ctx);
-  static const int kW[7] = {8, 16, 8, 16, 32, 16, 32}, kH[7] = {8, 8, 16, 16, 16, 32, 32};
-  if (!c || !coefficients || !blocks || kind < 0 || kind > 6) return JXG_ERR_INVALID_ARGUMENT;
+  static const int kW[12] = {8, 16, 8, 16, 32, 16, 32, 8, 32, 64, 32, 64};
+  static const int kH[12] = {8, 8, 16, 16, 16, 32, 32, 32, 8, 64, 64, 32};
+  if (!c || !coefficients || !blocks || kind < 0 || kind > 11) return JXG_ERR_INVALID_ARGUMENT;
   if (count == 0) return JXG_OK;
   if (count > (1ull << 31)) return JXG_ERR_DIMENSION_TOO_LARGE;
   cudaSetDevice(c->device);
@@ -1371,31 +1371,25 @@ int32_t jxg_op_idct(void* ctx, int32_t kind, const float* coefficients, uint64_t
   const float* din = static_cast<const float*>(c->op_in.ptr);
   float* dout = static_cast<float*>(c->op_out.ptr);
   JXG_CUDA(c, cudaMemcpyAsync(c->op_in.ptr, coefficients, bytes, cudaMemcpyHostToDevice, s));
-  const unsigned grid = static_cast<unsigned>((count + jxg::kDctWarps - 1) / jxg::kDctWarps);
-  const unsigned threads = 32 * jxg::kDctWarps;
   const int64_t cnt = static_cast<int64_t>(count);
+  auto run = [&](auto kernel, int warps) {
+    kernel<<<static_cast<unsigned>((count + warps - 1) / warps), 32 * warps, 0, s>>>(din, cnt, dout);
+  };
   st = jxg::launch(c, "k_idct_blocks", c->timing, [&] {
+    using namespace jxg;
     switch (kind) {
-      case jxg::kDct8x8:
-        jxg::k_idct_blocks<8, 8, jxg::kIdctSquare><<<grid, threads, 0, s>>>(din, cnt, dout);
-        break;
-      case jxg::kDct8x16:
-        jxg::k_idct_blocks<16, 8, jxg::kIdctRowsFirst><<<grid, threads, 0, s>>>(din, cnt, dout);
-        break;
-      case jxg::kDct16x8:
-        jxg::k_idct_blocks<8, 16, jxg::kIdctColsFirst><<<grid, threads, 0, s>>>(din, cnt, dout);
-        break;
-      case jxg::kDct16x16:
-        jxg::k_idct_blocks<16, 16, jxg::kIdctSquare><<<grid, threads, 0, s>>>(din, cnt, dout);
-        break;
-      case jxg::kDct16x32:
-        jxg::k_idct_blocks<32, 16, jxg::kIdctRowsFirst><<<grid, threads, 0, s>>>(din, cnt, dout);
-        break;
-      case jxg::kDct32x16:
-        jxg::k_idct_blocks<16, 32, jxg::kIdctColsFirst><<<grid, threads, 0, s>>>(din, cnt, dout);
-        break;
-      default:
-        jxg::k_idct_blocks<32, 32, jxg::kIdctSquare><<<grid, threads, 0, s>>>(din, cnt, dout);
+      case kDct8x8: run(k_idct_blocks<8, 8, kIdctSquare>, dct_warps<8, 8>()); break;
+      case kDct8x16: run(k_idct_blocks<16, 8, kIdctRowsFirst>, dct_warps<16, 8>()); break;
+      case kDct16x8: run(k_idct_blocks<8, 16, kIdctColsFirst>, dct_warps<8, 16>()); break;
+      case kDct16x16: run(k_idct_blocks<16, 16, kIdctSquare>, dct_warps<16, 16>()); break;
+      case kDct16x32: run(k_idct_blocks<32, 16, kIdctRowsFirst>, dct_warps<32, 16>()); break;
+      case kDct32x16: run(k_idct_blocks<16, 32, kIdctColsFirst>, dct_warps<16, 32>()); break;
+      case kDct32x32: run(k_idct_blocks<32, 32, kIdctSquare>, dct_warps<32, 32>()); break;
+      case kDct32x8: run(k_idct_blocks<8, 32, kIdctColsFirst>, dct_warps<8, 32>()); break;
+      case kDct8x32: run(k_idct_blocks<32, 8, kIdctRowsFirst>, dct_warps<32, 8>()); break;
+      case kDct64x64: run(k_idct_blocks<64, 64, kIdctSquare>, dct_warps<64, 64>()); break;
+      case kDct64x32: run(k_idct_blocks<32, 64, kIdctColsFirst>, dct_warps<32, 64>()); break;
+      default: run(k_idct_blocks<64, 32, kIdctRowsFirst>, dct_warps<64, 32>());  // 32x64
     }
   });
   if (st) return st;
@@ -1406,7 +1400,7 @@ int32_t jxg_op_idct(void* ctx, int32_t kind, const float* coefficients, uint64_t
 int32_t jxg_op_small_transform(void* ctx, int32_t kind, const float* blocks, uint64_t count,
                                float* out) {
   Context* c = static_cast<Context*>(ctx);
-  if (!c || !blocks || !out || kind < 0 || kind > 6) return JXG_ERR_INVALID_ARGUMENT;
+  if (!c || !blocks || !out || kind < 0 || kind > 10) return JXG_ERR_INVALID_ARGUMENT;
   if (count == 0) return JXG_OK;
   if (count > (1ull << 31)) return JXG_ERR_DIMENSION_TOO_LARGE;
   cudaSetDevice(c->device);

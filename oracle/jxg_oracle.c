@@ -53,7 +53,8 @@
 /* transform kinds of orc_dct (rows x columns, as the reference names them) */
 enum {
   JXG_ORC_DCT8X8 = 0, JXG_ORC_DCT8X16 = 1, JXG_ORC_DCT16X8 = 2, JXG_ORC_DCT16X16 = 3,
-  JXG_ORC_DCT16X32 = 4, JXG_ORC_DCT32X16 = 5, JXG_ORC_DCT32X32 = 6
+  JXG_ORC_DCT16X32 = 4, JXG_ORC_DCT32X16 = 5, JXG_ORC_DCT32X32 = 6, JXG_ORC_DCT32X8 = 7,
+  JXG_ORC_DCT8X32 = 8, JXG_ORC_DCT64X64 = 9, JXG_ORC_DCT64X32 = 10, JXG_ORC_DCT32X64 = 11
 };
 
 static inline float fmla(float a, float b, float c) { return fmaf(a, b, c); }
@@ -911,18 +912,49 @@ static inline void dct1d_32(float* b) {
   }
 }
 
+/* WC64 (src/dct.rs:2404-2437), the reference's literals rounded to float. */
+static const float WC64[32] = {
+    0x1.0013bep-1f, 0x1.00b20ep-1f, 0x1.01f098p-1f, 0x1.03d342p-1f,
+    0x1.06600ap-1f, 0x1.099f32p-1f, 0x1.0d9b8ap-1f, 0x1.1262c6p-1f,
+    0x1.1805f4p-1f, 0x1.1e9a26p-1f, 0x1.263934p-1f, 0x1.2f02d6p-1f,
+    0x1.391e0cp-1f, 0x1.44baf8p-1f, 0x1.52157p-1f, 0x1.617874p-1f,
+    0x1.7343p-1f, 0x1.87eedap-1f, 0x1.a01a7ep-1f, 0x1.bc97aep-1f,
+    0x1.de81bep-1f, 0x1.03b042p+0f, 0x1.1cb0bap+0f, 0x1.3bdc76p+0f,
+    0x1.63a8c4p+0f, 0x1.980e92p+0f, 0x1.dfeac4p+0f, 0x1.241a36p+1f,
+    0x1.765a3ap+1f, 0x1.056a44p+2f, 0x1.b2fdf6p+2f, 0x1.45fb68p+4f,
+};
+
+/* dct1d_64 (src/dct.rs:2529-2546), the same recursion over dct1d_32. */
+static inline void dct1d_64(float* b) {
+  float t[64];
+  for (int i = 0; i < 32; i++) {
+    t[i] = b[i] + b[63 - i];
+    t[32 + i] = (b[i] - b[63 - i]) * WC64[i];
+  }
+  dct1d_32(t);
+  dct1d_32(t + 32);
+  t[32] = fmla(t[32], SQRT2F, t[33]);
+  for (int i = 33; i < 63; i++) t[i] += t[i + 1];
+  for (int i = 0; i < 32; i++) {
+    b[2 * i] = t[i];
+    b[2 * i + 1] = t[32 + i];
+  }
+}
+
 static inline void dct1d_n(float* b, int n) {
   if (n == 8) dct1d_8(b);
   else if (n == 16) dct1d_16(b);
-  else dct1d_32(b);
+  else if (n == 32) dct1d_32(b);
+  else dct1d_64(b);
 }
 
 /* An H x W block (H rows of W samples), columns first: each column through
  * the H-point transform, then each row through the W-point one, stored
  * out[u * H + v] scaled by 1 / (W H) -- dct16x8 (src/dct.rs:904),
- * dct16x16 (:1010), dct32x32 (:1980), dct32x16 (:2251). */
+ * dct16x16 (:1010), dct32x32 (:1980), dct32x16 (:2251), dct32x8 (:1742),
+ * dct64x64 (:2576), dct64x32 (:2659). */
 static void dct_cols_first(const float* in, int W, int H, float* out) {
-  float after[1024], col[32], row[32];
+  float after[4096], col[64], row[64];
   for (int u = 0; u < W; u++) {
     for (int i = 0; i < H; i++) col[i] = in[i * W + u];
     dct1d_n(col, H);
@@ -937,9 +969,9 @@ static void dct_cols_first(const float* in, int W, int H, float* out) {
 }
 
 /* Rows first, then columns, stored out[v * W + u] -- dct8x16
- * (src/dct.rs:823), dct16x32 (:2340). */
+ * (src/dct.rs:823), dct16x32 (:2340), dct8x32 (:1777), dct32x64 (:2689). */
 static void dct_rows_first(const float* in, int W, int H, float* out) {
-  float after[1024], col[32], row[32];
+  float after[4096], col[64], row[64];
   for (int i = 0; i < H; i++) {
     for (int u = 0; u < W; u++) row[u] = in[i * W + u];
     dct1d_n(row, W);
@@ -970,8 +1002,35 @@ static void idct1d_4(const float v[4], float out[4]) {
   out[2] = fmla(-WC4_1, t3, t1);
 }
 
+static inline void inv_dct1d_8(float* b);
+static void idct_square(const float* c, int n, float* out);
+
 static const float R16_2[2] = {1.0f, 0.9017642f};                         /* :927 */
 static const float R32_4[4] = {1.0f, 0.9748868f, 0.9017642f, 0.7870549f};  /* :2018 */
+/* RESAMPLE_SCALE_64_TO_8 (:2005-2014) */
+static const float R64_8[8] = {
+    0x1p+0f, 0x1.fcc47ep-1f, 0x1.f3245ep-1f, 0x1.e35656p-1f,
+    0x1.cdb40ap-1f, 0x1.b2b7aap-1f, 0x1.92f8dcp-1f, 0x1.6f28ccp-1f,
+};
+
+/* dc_from_dct64x32_normalized (:2767-2786): per low horizontal-or-vertical
+ * frequency a of the 32-point axis, the 8-point axis' lowest coefficients
+ * scaled by r4[a] r8[b] through the unnormalised 8-point inverse; then per
+ * position the 4-point inverse across a.  norm[i][j]: i along the 4-point
+ * axis, j along the 8-point one. */
+static void dc_64x32_normalized(const float* c, float norm[4][8]) {
+  float rows[4][8];
+  for (int a = 0; a < 4; a++) {
+    for (int b = 0; b < 8; b++) rows[a][b] = c[a * 64 + b] * (R32_4[a] * R64_8[b]) * 8.0f;
+    inv_dct1d_8(rows[a]);
+  }
+  for (int x = 0; x < 8; x++) {
+    const float col[4] = {rows[0][x], rows[1][x], rows[2][x], rows[3][x]};
+    float o[4];
+    idct1d_4(col, o);
+    for (int y = 0; y < 4; y++) norm[y][x] = o[y];
+  }
+}
 
 /* The DC values a transform's lowest coefficients resample to, one per
  * covered 8x8 block (dc_from_dct16x8 :930, dc_from_dct8x16 :939,
@@ -1020,6 +1079,31 @@ static void dc_from(int kind, const float* c, float* dc) {
       }
       break;
     }
+    case JXG_ORC_DCT32X8:
+    case JXG_ORC_DCT8X32: { /* dc_from_dct8x32 (:1864-1867) */
+      float sv[4];
+      for (int b = 0; b < 4; b++) sv[b] = c[b] * R32_4[b];
+      idct1d_4(sv, dc);
+      break;
+    }
+    case JXG_ORC_DCT64X64: { /* dc_from_dct64x64 (:2602-2612) */
+      float low[64];
+      for (int y = 0; y < 8; y++)
+        for (int x = 0; x < 8; x++) low[y * 8 + x] = c[y * 64 + x] * (R64_8[x] * R64_8[y]);
+      idct_square(low, 8, dc);
+      break;
+    }
+    case JXG_ORC_DCT64X32:
+    case JXG_ORC_DCT32X64: { /* dc_from_dct64x32 (:2789), dc_from_dct32x64 (:2800) */
+      float norm[4][8];
+      dc_64x32_normalized(c, norm);
+      for (int y = 0; y < 4; y++)
+        for (int x = 0; x < 8; x++) {
+          if (kind == JXG_ORC_DCT64X32) dc[x * 4 + y] = norm[y][x];
+          else dc[y * 8 + x] = norm[y][x];
+        }
+      break;
+    }
     default: { /* 32x32 */
       float rr[4][4];
       for (int a = 0; a < 4; a++) {
@@ -1048,6 +1132,11 @@ int orc_dct(int kind, const float* in, float* out, float* dc) {
     case JXG_ORC_DCT16X32: dct_rows_first(in, 32, 16, out); break;
     case JXG_ORC_DCT32X16: dct_cols_first(in, 16, 32, out); break;
     case JXG_ORC_DCT32X32: dct_cols_first(in, 32, 32, out); break;
+    case JXG_ORC_DCT32X8: dct_cols_first(in, 8, 32, out); break;
+    case JXG_ORC_DCT8X32: dct_rows_first(in, 32, 8, out); break;
+    case JXG_ORC_DCT64X64: dct_cols_first(in, 64, 64, out); break;
+    case JXG_ORC_DCT64X32: dct_cols_first(in, 32, 64, out); break;
+    case JXG_ORC_DCT32X64: dct_rows_first(in, 64, 32, out); break;
     default: return -1;
   }
   if (dc) dc_from(kind, out, dc);
@@ -1144,16 +1233,47 @@ static inline void inv_dct1d_32(float* b) {
   }
 }
 
+/* INV_WC64 (src/dct.rs:2495-2527): 1 / WC64 as float. */
+static const float INV_WC64[32] = {
+    0x1.ffd888p+0f, 0x1.fe9cdcp+0f, 0x1.fc2648p+0f, 0x1.f87652p+0f,
+    0x1.f38f3cp+0f, 0x1.ed741p+0f, 0x1.e6289p+0f, 0x1.ddb13ap+0f,
+    0x1.d4134ep+0f, 0x1.c954b2p+0f, 0x1.bd7c0cp+0f, 0x1.b090a6p+0f,
+    0x1.a29a7ap+0f, 0x1.93a224p+0f, 0x1.83b0ep+0f, 0x1.72d084p+0f,
+    0x1.610b74p+0f, 0x1.4e6cacp+0f, 0x1.3affa2p+0f, 0x1.26d054p+0f,
+    0x1.11eb36p+0f, 0x1.f8ba4ep-1f, 0x1.cc66eap-1f, 0x1.9ef794p-1f,
+    0x1.708854p-1f, 0x1.4135c8p-1f, 0x1.111d26p-1f, 0x1.c0b828p-2f,
+    0x1.5e2144p-2f, 0x1.f564e6p-3f, 0x1.2d520ap-3f, 0x1.92156p-5f,
+};
+
+/* inv_dct1d_64 (src/dct.rs:2548-2570). */
+static inline void inv_dct1d_64(float* b) {
+  float t[64];
+  for (int i = 0; i < 32; i++) {
+    t[i] = b[2 * i];
+    t[32 + i] = b[2 * i + 1];
+  }
+  for (int i = 62; i >= 33; i--) t[i] -= t[i + 1];
+  t[32] = (t[32] - t[33]) * IS2F;
+  inv_dct1d_32(t + 32);
+  for (int i = 0; i < 32; i++) t[32 + i] *= INV_WC64[i];
+  inv_dct1d_32(t);
+  for (int i = 0; i < 32; i++) {
+    b[i] = (t[i] + t[32 + i]) * 0.5f;
+    b[63 - i] = (t[i] - t[32 + i]) * 0.5f;
+  }
+}
+
 static inline void inv_dct1d_n(float* b, int n) {
   if (n == 8) inv_dct1d_8(b);
   else if (n == 16) inv_dct1d_16(b);
-  else inv_dct1d_32(b);
+  else if (n == 32) inv_dct1d_32(b);
+  else inv_dct1d_64(b);
 }
 
 /* Inverse of a square transform (inv_dct_square, :1590-1620): coefficients
  * transposed and scaled by N, columns, then rows. */
 static void idct_square(const float* c, int n, float* out) {
-  float col[32];
+  float col[64];
   const float scale = (float)(n * n);
   for (int a = 0; a < n; a++)
     for (int b = 0; b < n; b++) out[b * n + a] = c[a * n + b] * scale;
@@ -1166,9 +1286,10 @@ static void idct_square(const float* c, int n, float* out) {
 }
 
 /* Inverse of a rows-first transform (inv_dct8x16 :1634, inv_dct16x32
- * :1683): coefficients in place scaled by N, columns (length H), rows. */
+ * :1683, inv_dct8x32 :1804, inv_dct32x64 :2735): coefficients in place
+ * scaled by N, columns (length H), rows. */
 static void idct_rows_first(const float* c, int W, int H, float* out) {
-  float col[32];
+  float col[64];
   const float scale = (float)(W * H);
   for (int k = 0; k < W * H; k++) out[k] = c[k] * scale;
   for (int u = 0; u < W; u++) {
@@ -1180,10 +1301,11 @@ static void idct_rows_first(const float* c, int W, int H, float* out) {
 }
 
 /* Inverse of a columns-first transform (inv_dct16x8 :1658, inv_dct32x16
- * :1705): per pixel row v the W-point inverse of coefficients c[u H + v]
- * scaled by N, then per column the H-point inverse. */
+ * :1705, inv_dct32x8 :1833, inv_dct64x32 :2710): per pixel row v the
+ * W-point inverse of coefficients c[u H + v] scaled by N, then per column
+ * the H-point inverse. */
 static void idct_cols_first(const float* c, int W, int H, float* out) {
-  float acd[1024], row[32], col[32];
+  float acd[4096], row[64], col[64];
   const float scale = (float)(W * H);
   for (int v = 0; v < H; v++) {
     for (int u = 0; u < W; u++) row[u] = c[u * H + v] * scale;
@@ -1208,6 +1330,11 @@ int orc_idct(int kind, const float* coeffs, float* out) {
     case JXG_ORC_DCT16X32: idct_rows_first(coeffs, 32, 16, out); break;
     case JXG_ORC_DCT32X16: idct_cols_first(coeffs, 16, 32, out); break;
     case JXG_ORC_DCT32X32: idct_square(coeffs, 32, out); break;
+    case JXG_ORC_DCT32X8: idct_cols_first(coeffs, 8, 32, out); break;
+    case JXG_ORC_DCT8X32: idct_rows_first(coeffs, 32, 8, out); break;
+    case JXG_ORC_DCT64X64: idct_square(coeffs, 64, out); break;
+    case JXG_ORC_DCT64X32: idct_cols_first(coeffs, 32, 64, out); break;
+    case JXG_ORC_DCT32X64: idct_rows_first(coeffs, 64, 32, out); break;
     default: return -1;
   }
   return 0;
@@ -1346,23 +1473,27 @@ static void dct4x4(const float* in, float* o) {
   hadamard_0189(o);
 }
 
-/* dct4x8_2d (:1198-1220) and dct4x8 (:1238-1262): each 4-row half through
- * column dct1d_4 then row dct1d_8 (1/32), rows interleaved, the 2-point
- * Hadamard of the half DCs. */
+/* dct4x8_2d (:1198-1220): a 4-row, 8-column block through column dct1d_4
+ * then row dct1d_8 (1/32), frequencies [vertical][horizontal]. */
+static void dct4x8_2d(const float* in, float* t) {
+  memcpy(t, in, 32 * sizeof(float));
+  for (int c = 0; c < 8; c++) {
+    float col[4] = {t[c], t[8 + c], t[16 + c], t[24 + c]};
+    dct1d_4(col);
+    for (int vf = 0; vf < 4; vf++) t[vf * 8 + c] = col[vf];
+  }
+  for (int vf = 0; vf < 4; vf++) {
+    dct1d_8(t + vf * 8);
+    for (int k = 0; k < 8; k++) t[vf * 8 + k] *= 1.0f / 32.0f;
+  }
+}
+
+/* dct4x8 (:1238-1262): each 4-row half through dct4x8_2d, rows
+ * interleaved, the 2-point Hadamard of the half DCs. */
 static void dct4x8(const float* in, float* o) {
   for (int y = 0; y < 2; y++) {
     float t[32];
-    for (int r = 0; r < 4; r++)
-      for (int c = 0; c < 8; c++) t[r * 8 + c] = in[(y * 4 + r) * 8 + c];
-    for (int c = 0; c < 8; c++) {
-      float col[4] = {t[c], t[8 + c], t[16 + c], t[24 + c]};
-      dct1d_4(col);
-      for (int vf = 0; vf < 4; vf++) t[vf * 8 + c] = col[vf];
-    }
-    for (int vf = 0; vf < 4; vf++) {
-      dct1d_8(t + vf * 8);
-      for (int k = 0; k < 8; k++) t[vf * 8 + k] *= 1.0f / 32.0f;
-    }
+    dct4x8_2d(in + y * 32, t);
     for (int iy = 0; iy < 4; iy++)
       for (int ix = 0; ix < 8; ix++) o[(y + iy * 2) * 8 + ix] = t[iy * 8 + ix];
   }
@@ -1395,9 +1526,146 @@ static void dct8x4(const float* in, float* o) {
   o[8] = (b0 - b1) * 0.5f;
 }
 
+/* The AFV basis of the JPEG XL standard (libjxl k4x4AFVBasisTranspose,
+ * src/afv.rs:48-180), stored vector-major: AFV_BASIS[i][j] is basis vector
+ * i sampled at pixel j of the mirrored 4x4 corner; the reference stores the
+ * transpose.  Each value is the reference's decimal literal rounded to
+ * float, written in hex. */
+static const float AFV_BASIS[16][16] = {
+    {// basis vector 0
+     0x1p-2f, 0x1p-2f, 0x1p-2f, 0x1p-2f,
+     0x1p-2f, 0x1p-2f, 0x1p-2f, 0x1p-2f,
+     0x1p-2f, 0x1p-2f, 0x1p-2f, 0x1p-2f,
+     0x1p-2f, 0x1p-2f, 0x1p-2f, 0x1p-2f},
+    {// basis vector 1
+     0x1.c0f96cp-1f, 0x1.c3e518p-3f, -0x1.9f5622p-4f, -0x1.9f5622p-4f,
+     0x1.c3e518p-3f, -0x1.9f5622p-4f, -0x1.9f5622p-4f, -0x1.9f5622p-4f,
+     -0x1.9f5622p-4f, -0x1.9f5622p-4f, -0x1.9f5622p-4f, -0x1.9f5622p-4f,
+     -0x1.9f5622p-4f, -0x1.9f5622p-4f, -0x1.9f5622p-4f, -0x1.9f5622p-4f},
+    {// basis vector 2
+     0.0f, 0.0f, 0x1.a0762ap-2f, 0x1.c71d6cp-2f,
+     0.0f, 0.0f, 0x1.90e23ap-3f, 0x1.2bf09ap-2f,
+     -0x1.a0762ap-2f, -0x1.90e23ap-3f, 0.0f, 0x1.d2163ep-4f,
+     -0x1.c71d6cp-2f, -0x1.2bf09ap-2f, -0x1.d2163ep-4f, 0.0f},
+    {// basis vector 3
+     0.0f, 0.0f, -0x1.b35156p-3f, 0x1.3bf474p-2f,
+     0.0f, 0x1.e1f76p-2f, -0x1.4c05d8p-3f, 0.0f,
+     -0x1.b35156p-3f, -0x1.4c05d8p-3f, -0x1.e1f76p-2f, -0x1.2be31p-3f,
+     0x1.3bf474p-2f, 0.0f, -0x1.2be31p-3f, 0x1.b35156p-2f},
+    {// basis vector 4
+     0.0f, -0x1.6a09e6p-1f, 0.0f, 0.0f,
+     0x1.6a09e6p-1f, 0.0f, 0.0f, 0.0f,
+     0.0f, 0.0f, 0.0f, 0.0f,
+     0.0f, 0.0f, 0.0f, 0.0f},
+    {// basis vector 5
+     -0x1.a46402p-2f, 0x1.3f41cp-1f, -0x1.07949ep-4f, -0x1.07949ep-4f,
+     0x1.3f41cp-1f, -0x1.07949ep-4f, -0x1.07949ep-4f, -0x1.07949ep-4f,
+     -0x1.07949ep-4f, -0x1.07949ep-4f, -0x1.07949ep-4f, -0x1.07949ep-4f,
+     -0x1.07949ep-4f, -0x1.07949ep-4f, -0x1.07949ep-4f, -0x1.07949ep-4f},
+    {// basis vector 6
+     0.0f, 0.0f, -0x1.ce990ap-2f, 0x1.44b342p-3f,
+     0.0f, -0x1.4ad5cep-5f, 0x1.e6293p-8f, 0x1.92f46p-2f,
+     -0x1.ce990ap-2f, 0x1.e6293p-8f, 0x1.c5990cp-4f, 0x1.53e48cp-4f,
+     0x1.44b342p-3f, 0x1.92f46p-2f, 0x1.53e48cp-4f, -0x1.ce990ap-2f},
+    {// basis vector 7
+     0.0f, 0.0f, -0x1.37ff48p-2f, 0x1.05c416p-1f,
+     0.0f, 0.0f, -0x1.2973ap-2f, -0x1.0d76bp-4f,
+     0x1.37ff48p-2f, 0x1.2973ap-2f, 0.0f, -0x1.e94338p-3f,
+     -0x1.05c416p-1f, 0x1.0d76bp-4f, 0x1.e94338p-3f, 0.0f},
+    {// basis vector 8
+     0.0f, 0.0f, 0x1.350936p-2f, 0x1.081d22p-2f,
+     0.0f, 0x1.4d41eep-3f, 0x1.85f0acp-4f, 0.0f,
+     0x1.350936p-2f, 0x1.85f0acp-4f, -0x1.4d41eep-3f, -0x1.69994cp-2f,
+     0x1.081d22p-2f, 0.0f, -0x1.69994cp-2f, -0x1.350936p-1f},
+    {// basis vector 9
+     0.0f, 0.0f, 0x1.a20bd8p-2f, 0.0f,
+     0.0f, 0.0f, 0.0f, -0x1.a20bd8p-2f,
+     -0x1.a20bd8p-2f, 0.0f, 0.0f, -0x1.a20bd8p-2f,
+     0.0f, 0x1.a20bd8p-2f, 0x1.a20bd8p-2f, 0.0f},
+    {// basis vector 10
+     0.0f, 0.0f, 0x1.65f692p-3f, 0x1.4cd876p-4f,
+     0.0f, 0.0f, -0x1.785c5ap-2f, -0x1.3b457ap-2f,
+     -0x1.65f692p-3f, 0x1.785c5ap-2f, 0.0f, 0x1.ee40c2p-2f,
+     -0x1.4cd876p-4f, 0x1.3b457ap-2f, -0x1.ee40c2p-2f, 0.0f},
+    {// basis vector 11
+     0.0f, 0.0f, -0x1.b03e22p-3f, 0x1.7c418p-3f,
+     0.0f, 0.0f, 0x1.f7f86cp-2f, -0x1.8a7f04p-2f,
+     0x1.b03e22p-3f, -0x1.f7f86cp-2f, 0.0f, 0x1.64bfe4p-3f,
+     -0x1.7c418p-3f, 0x1.8a7f04p-2f, -0x1.64bfe4p-3f, 0.0f},
+    {// basis vector 12
+     0.0f, 0.0f, -0x1.242b5ep-3f, -0x1.5dd81ap-2f,
+     0.0f, 0x1.793744p-1f, 0x1.f85cf8p-3f, -0x1.5f311cp-4f,
+     -0x1.242b5ep-3f, 0x1.f85cf8p-3f, 0x1.30cfep-3f, -0x1.86a67ap-5f,
+     -0x1.5dd81ap-2f, -0x1.5f311cp-4f, -0x1.86a67ap-5f, -0x1.242b5ep-3f},
+    {// basis vector 13
+     0.0f, 0.0f, -0x1.1ae6bcp-3f, 0x1.52275cp-2f,
+     0.0f, 0x1.669c08p-4f, -0x1.457f42p-4f, -0x1.d868dap-2f,
+     -0x1.1ae6bcp-3f, -0x1.457f42p-4f, 0x1.fd2e2ep-2f, 0x1.00c78ap-3f,
+     0x1.52275cp-2f, -0x1.d868dap-2f, 0x1.00c78ap-3f, -0x1.1ae6bcp-3f},
+    {// basis vector 14
+     0.0f, 0.0f, -0x1.651f42p-3f, 0x1.1fdcf2p-4f,
+     0.0f, -0x1.2b1cf6p-2f, 0x1.731432p-2f, 0.0f,
+     -0x1.651f42p-3f, 0x1.731432p-2f, 0x1.2b1cf6p-2f, -0x1.bb0b6ep-2f,
+     0x1.1fdcf2p-4f, 0.0f, -0x1.bb0b6ep-2f, 0x1.651f42p-2f},
+    {// basis vector 15
+     0.0f, 0.0f, 0x1.d119acp-4f, -0x1.2fd22cp-4f,
+     0.0f, 0x1.8d5f0ap-3f, -0x1.bda294p-2f, 0x1.c0e508p-3f,
+     0x1.d119acp-4f, -0x1.bda294p-2f, 0x1.1c2ec6p-1f, -0x1.04cb9p-2f,
+     -0x1.2fd22cp-4f, 0x1.c0e508p-3f, -0x1.04cb9p-2f, 0x1.d119acp-4f},
+};
+
+void orc_afv_basis(float* out) { memcpy(out, AFV_BASIS, sizeof(AFV_BASIS)); }
+
+/* The AFV parts' sub-transforms on their own, for the decoder-side round
+ * trip: dct4x4_2d of a 4x4 block, dct4x8_2d of a 4-row, 8-column block. */
+void orc_dct4x4_2d(const float* in, float* out) { dct4x4_2d(in, out); }
+void orc_dct4x8_2d(const float* in, float* out) { dct4x8_2d(in, out); }
+
+/* afv_dct4x4 (src/afv.rs:188-196): coefficient i is the fused dot product
+ * of the corner's pixels with basis vector i, pixels in order. */
+static void afv_dct4x4(const float* px, float* coeff) {
+  for (int i = 0; i < 16; i++) {
+    float acc = 0.0f;
+    for (int j = 0; j < 16; j++) acc = fmla(px[j], AFV_BASIS[i][j], acc);
+    coeff[i] = acc;
+  }
+}
+
+/* afv_from_pixels (src/afv.rs:207-259): AFV of the mirrored corner quadrant
+ * into the (even, even) positions, DCT4x4 of the horizontally adjacent
+ * quadrant into (even, odd), DCT4x8 of the other vertical half into the odd
+ * rows, then the three sub-part DCs rewritten so coefficient 0 is the block
+ * mean.  kind bit 0 = right half, bit 1 = bottom half. */
+static void afv_8x8(int kind, const float* in, float* o) {
+  const int afv_x = kind & 1, afv_y = kind >> 1;
+  float quad[16], coeff[16];
+  for (int i = 0; i < 16; i++) {
+    const int dy = i / 4, dx = i % 4;
+    const int sy = afv_y ? 3 - dy : dy, sx = afv_x ? 3 - dx : dx;
+    quad[i] = in[(sy + 4 * afv_y) * 8 + sx + 4 * afv_x];
+  }
+  afv_dct4x4(quad, coeff);
+  for (int iy = 0; iy < 4; iy++)
+    for (int ix = 0; ix < 4; ix++) o[iy * 16 + ix * 2] = coeff[iy * 4 + ix];
+  const int qx = afv_x ? 0 : 4;
+  for (int i = 0; i < 16; i++) quad[i] = in[(i / 4 + 4 * afv_y) * 8 + qx + i % 4];
+  dct4x4_2d(quad, coeff);
+  for (int iy = 0; iy < 4; iy++)
+    for (int ix = 0; ix < 4; ix++) o[iy * 16 + ix * 2 + 1] = coeff[iy * 4 + ix];
+  const int hy = afv_y ? 0 : 4;
+  float half[32];
+  dct4x8_2d(in + hy * 8, half);
+  for (int iy = 0; iy < 4; iy++)
+    for (int ix = 0; ix < 8; ix++) o[(1 + iy * 2) * 8 + ix] = half[iy * 8 + ix];
+  const float block00 = o[0] * 0.25f, block01 = o[1], block10 = o[8];
+  o[0] = (block00 + block01 + 2.0f * block10) * 0.25f;
+  o[1] = (block00 - block01) * 0.5f;
+  o[8] = (block00 + block01 - 2.0f * block10) * 0.25f;
+}
+
 /* The 8x8-sized transforms: 0 identity, 1 DCT2x2, 2 DCT4x4, 3 DCT4x8,
- * 4 DCT8x4 (forward), 5 / 6 the identity / DCT2x2 inverses.  Returns 0, or
- * -1 for an unknown kind. */
+ * 4 DCT8x4 (forward), 5 / 6 the identity / DCT2x2 inverses, 7..10 AFV0..3
+ * (forward).  Returns 0, or -1 for an unknown kind. */
 int orc_small_transform(int kind, const float* in, float* out) {
   switch (kind) {
     case 0: identity8x8(in, out); break;
@@ -1407,6 +1675,10 @@ int orc_small_transform(int kind, const float* in, float* out) {
     case 4: dct8x4(in, out); break;
     case 5: inv_identity8x8(in, out); break;
     case 6: inv_dct2x2_8x8(in, out); break;
+    case 7:
+    case 8:
+    case 9:
+    case 10: afv_8x8(kind - 7, in, out); break;
     default: return -1;
   }
   return 0;

@@ -342,13 +342,17 @@ def ac_token_unpack(word: int) -> tuple[int, int]:
 DCT_KINDS = {
     "8x8": (0, 8, 8, 1), "8x16": (1, 16, 8, 2), "16x8": (2, 8, 16, 2), "16x16": (3, 16, 16, 4),
     "16x32": (4, 32, 16, 8), "32x16": (5, 16, 32, 8), "32x32": (6, 32, 32, 16),
+    "32x8": (7, 8, 32, 4), "8x32": (8, 32, 8, 4), "64x64": (9, 64, 64, 64),
+    "64x32": (10, 32, 64, 32), "32x64": (11, 64, 32, 32),
 }
 
 
 def dct(name: str, block: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
     """`DctFn<W, H, N>` of one (H, W) block (src/dct.rs: dct8x16 :823, dct16x8
-    :904, dct16x16 :1010, dct32x32 :1980, dct32x16 :2251, dct16x32 :2340) and
-    its per-8x8 DC values (dc_from_dct*): (N coefficients, DC values)."""
+    :904, dct16x16 :1010, dct32x32 :1980, dct32x16 :2251, dct16x32 :2340,
+    dct32x8 :1742, dct8x32 :1777, dct64x64 :2576, dct64x32 :2659, dct32x64
+    :2689) and its per-8x8 DC values (dc_from_dct*): (N coefficients, DC
+    values)."""
     kind, w, h, ndc = DCT_KINDS[name]
     b = np.ascontiguousarray(block, np.float32).reshape(h, w)
     out = np.zeros(w * h, np.float32)
@@ -359,9 +363,10 @@ def dct(name: str, block: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
 
 
 def dct1d(vec: np.ndarray) -> np.ndarray:
-    """dct1d_8 / dct1d_16 / dct1d_32 (src/dct.rs:109, :687, :1477) of one vector."""
+    """dct1d_8 / dct1d_16 / dct1d_32 / dct1d_64 (src/dct.rs:109, :687, :1477,
+    :2529) of one vector."""
     v = np.ascontiguousarray(vec, np.float32).copy()
-    assert v.size in (8, 16, 32)
+    assert v.size in (8, 16, 32, 64)
     lib().orc_dct1d(v.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(v.size))
     return v
 
@@ -381,16 +386,35 @@ def idct(name: str, coeffs: np.ndarray) -> np.ndarray:
 
 # The 8x8-sized transforms besides DCT8 (orc_small_transform kinds)
 SMALL_TRANSFORMS = {"identity": 0, "dct2x2": 1, "dct4x4": 2, "dct4x8": 3, "dct8x4": 4,
-                    "inv_identity": 5, "inv_dct2x2": 6}
+                    "inv_identity": 5, "inv_dct2x2": 6,
+                    "afv0": 7, "afv1": 8, "afv2": 9, "afv3": 10}
 
 
 def small_transform(name: str, block: np.ndarray) -> np.ndarray:
     """identity8x8 (src/dct.rs:185), dct2x2_8x8 (:306), dct4x4 (:1163),
     dct4x8 (:1238), dct8x4 (:1319), inv_identity8x8 (:225), inv_dct2x2_8x8
-    (:345) of one 8x8 block: 64 values."""
+    (:345), afv_from_pixels (src/afv.rs:207, afv0..afv3) of one 8x8 block:
+    64 values."""
     b = np.ascontiguousarray(block, np.float32).reshape(64)
     out = np.zeros(64, np.float32)
     assert lib().orc_small_transform(ctypes.c_int(SMALL_TRANSFORMS[name]),
                                      b.ctypes.data_as(ctypes.c_void_p),
                                      out.ctypes.data_as(ctypes.c_void_p)) == 0
+    return out
+
+
+def afv_basis() -> np.ndarray:
+    """The oracle's AFV basis (src/afv.rs:48-180) as [vector][pixel], 16x16."""
+    out = np.zeros(256, np.float32)
+    lib().orc_afv_basis(out.ctypes.data_as(ctypes.c_void_p))
+    return out.reshape(16, 16)
+
+
+def dct4_2d(block: np.ndarray) -> np.ndarray:
+    """dct4x4_2d (src/dct.rs:1061) of a 4x4 block (16 values, transposed
+    output) or dct4x8_2d (:1198) of a 4-row, 8-column block (32 values)."""
+    b = np.ascontiguousarray(block, np.float32).reshape(-1).copy()
+    out = np.zeros_like(b)
+    fn = {16: lib().orc_dct4x4_2d, 32: lib().orc_dct4x8_2d}[b.size]
+    fn(b.ctypes.data_as(ctypes.c_void_p), out.ctypes.data_as(ctypes.c_void_p))
     return out

@@ -16,7 +16,9 @@ constant tables and asserted values that its own unit tests pin:
   - dirty_log2f on powers of two (src/adaptive_quant.rs:896-902);
   - the DCT8 band parameters and the static DCT8 dequant table they must
     reproduce within 2e-6 (src/quant_weights.rs:123-128, :246,
-    `dct8_matrix_from_bands_matches_static` :3367-3390).
+    `dct8_matrix_from_bands_matches_static` :3367-3390);
+  - the AFV basis (src/afv.rs:48-180, [pixel][vector], the decimal literals
+    as written), checked orthonormal by `afv_basis_is_orthonormal` (:413).
 The output is tests/golden/reference_tables.json.
 """
 from __future__ import annotations
@@ -62,8 +64,14 @@ def main(root: str) -> None:
     dct8_bands = _floats(qw, "static DCT8_BANDS:")
     dct8_static = _floats(qw, "static DEQUANT_MATRIX_8X8:")
     assert len(dct8_bands) == 18 and len(dct8_static) == 192, (len(dct8_bands), len(dct8_static))
+    afv = open(os.path.join(root, "src/afv.rs")).read()
+    afv = afv[afv.index("= [", afv.index("AFV_BASIS_TRANSPOSE:")):]
+    afv = afv[: afv.index("];")]
+    afv_basis = re.findall(r"-?\d+\.\d+", afv)
+    assert len(afv_basis) == 256, len(afv_basis)
     out = {
         "source": "jixel 0.5.14",
+        "afv_basis_transpose": afv_basis,
         "dct8_bands": dct8_bands,
         "dequant_matrix_8x8": dct8_static,
         "coeff_order_8x8": order8,

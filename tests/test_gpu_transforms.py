@@ -16,7 +16,11 @@ def ctx():
     c.close()
 
 
-@pytest.mark.parametrize("name", ["8x8", "8x16", "16x8", "16x16", "16x32", "32x16", "32x32"])
+ALL_DCT = ["8x8", "8x16", "16x8", "16x16", "16x32", "32x16", "32x32", "32x8", "8x32",
+           "64x64", "64x32", "32x64"]
+
+
+@pytest.mark.parametrize("name", ALL_DCT)
 def test_transform_and_dc_match_oracle(ctx, name):
     _, w, h, ndc = O.DCT_KINDS[name]
     rng = np.random.default_rng(w * 100 + h)
@@ -36,12 +40,14 @@ def test_transform_and_dc_match_oracle(ctx, name):
 def test_dct_operator_rejects_bad_kinds(ctx):
     lib = ctx._lib
     b = np.zeros(64, np.float32)
-    assert lib.jxg_op_dct(ctx.handle, 7, b.ctypes.data, 1, b.ctypes.data, None) != 0
+    assert lib.jxg_op_dct(ctx.handle, 12, b.ctypes.data, 1, b.ctypes.data, None) != 0
+    assert lib.jxg_op_idct(ctx.handle, 12, b.ctypes.data, 1, b.ctypes.data) != 0
+    assert lib.jxg_op_small_transform(ctx.handle, 11, b.ctypes.data, 1, b.ctypes.data) != 0
     assert lib.jxg_op_dct(ctx.handle, -1, b.ctypes.data, 1, b.ctypes.data, None) != 0
     assert lib.jxg_op_dct(ctx.handle, 3, b.ctypes.data, 0, b.ctypes.data, None) == 0  # no blocks
 
 
-@pytest.mark.parametrize("name", ["8x8", "8x16", "16x8", "16x16", "16x32", "32x16", "32x32"])
+@pytest.mark.parametrize("name", ALL_DCT)
 def test_inverse_matches_oracle_and_round_trips(ctx, name):
     _, w, h, _ = O.DCT_KINDS[name]
     rng = np.random.default_rng(w * 7 + h)
@@ -55,7 +61,7 @@ def test_inverse_matches_oracle_and_round_trips(ctx, name):
 
 
 @pytest.mark.parametrize("name", ["identity", "dct2x2", "dct4x4", "dct4x8", "dct8x4",
-                                  "inv_identity", "inv_dct2x2"])
+                                  "inv_identity", "inv_dct2x2", "afv0", "afv1", "afv2", "afv3"])
 def test_small_transforms_match_oracle(ctx, name):
     rng = np.random.default_rng(len(name) * 31)
     blocks = rng.uniform(-1.0, 1.0, (300, 8, 8)).astype(np.float32)

@@ -323,9 +323,10 @@ def test_packed_form_is_decided_per_group():
     assert _pairs(words, woffs, goffs) == toks.tolist()
 
 
-def test_dct1d_32_diagonalizes_the_dct_basis():
-    # src/dct.rs:3265-3289: the k0-th DCT-II basis vector peaks at k0 only
-    n = 32
+@pytest.mark.parametrize("n", [32, 64])
+def test_dct1d_diagonalizes_the_dct_basis(n):
+    # src/dct.rs:3265-3289 (32 points; the 64-point recursion alike): the
+    # k0-th DCT-II basis vector peaks at k0 only
     for k0 in range(n):
         x = np.array([math.cos(np.float32(math.pi) * (2.0 * i + 1.0) * k0 / (2.0 * n))
                       for i in range(n)], np.float32)
@@ -362,7 +363,8 @@ def test_square_dct_matches_separable_reference(name, n):
     assert np.abs(out.reshape(n, n) - ref).max() < 1e-5
 
 
-@pytest.mark.parametrize("name", ["8x16", "16x8", "16x16", "16x32", "32x16", "32x32"])
+@pytest.mark.parametrize("name", ["8x16", "16x8", "16x16", "16x32", "32x16", "32x32",
+                                  "32x8", "8x32", "64x64", "64x32", "32x64"])
 def test_dc_of_a_constant_block_is_the_8x8_dc(name):
     # src/dct.rs:3185-3213 (32x16 / 16x32; the other sizes alike): every
     # covered block's DC equals the 8x8 DCT's DC of the same constant
@@ -383,7 +385,8 @@ def test_rectangular_dc_follows_the_halves():
     assert dc[0] < dc[1]
 
 
-@pytest.mark.parametrize("name", ["8x8", "8x16", "16x8", "16x16", "16x32", "32x16", "32x32"])
+@pytest.mark.parametrize("name", ["8x8", "8x16", "16x8", "16x16", "16x32", "32x16", "32x32",
+                                  "32x8", "8x32"])
 def test_transforms_round_trip(name):
     # src/dct.rs:2916-2926 (and the other round-trip tests): the inverse of
     # each transform gives back the samples ((i * 53) % 97 / 97) within 1e-4
@@ -422,3 +425,154 @@ def test_dct4_family_dc_is_the_block_mean(name):
     for blk in (np.full(64, 1.75, np.float32), np.arange(64, dtype=np.float32) / np.float32(7.0)):
         c = O.small_transform(name, blk)
         assert abs(float(c[0]) - float(blk.mean())) < 1e-5, (name, c[0])
+
+
+def _f32_nearest(text):
+    # a decimal literal rounded once to the nearest float (ties to even)
+    from fractions import Fraction
+    exact = Fraction(text)
+    a = np.float32(float(exact))
+    cands = [np.nextafter(a, np.float32(-np.inf)), a, np.nextafter(a, np.float32(np.inf))]
+    return min(cands, key=lambda c: (abs(Fraction(float(c)) - exact), f32_bits(c) & 1))
+
+
+def test_afv_basis_is_the_reference_table():
+    # src/afv.rs:48-180 stores [pixel][vector]; the oracle stores the transpose
+    gold = np.array([_f32_nearest(t) for t in GOLD["afv_basis_transpose"]], np.float32).reshape(16, 16)
+    basis = O.afv_basis()
+    assert [f32_bits(v) for v in basis.T.reshape(-1)] == [f32_bits(v) for v in gold.reshape(-1)]
+
+
+def test_afv_basis_is_orthonormal():
+    # src/afv.rs:412-426
+    b = O.afv_basis()
+    for a in range(16):
+        for c in range(16):
+            dot = np.float32(0.0)
+            for j in range(16):
+                dot = np.float32(dot + b[a, j] * b[c, j])
+            assert abs(float(dot) - (1.0 if a == c else 0.0)) < 1e-5, (a, c, dot)
+
+
+def _afv_rnd(seed, count):
+    # the AFV tests' generator (src/afv.rs:430-434)
+    s, out = seed, []
+    for _ in range(count):
+        s = (s * 1664525 + 1013904223) & 0xFFFFFFFF
+        out.append(np.float32(s >> 8) / np.float32(1 << 24) - np.float32(0.5))
+    return out
+
+
+def test_afv_dc_equals_block_mean():
+    # src/afv.rs:428-448: one generator across the four kinds
+    vals = _afv_rnd(123456789, 256)
+    for kind in range(4):
+        inp = np.array(vals[kind * 64:(kind + 1) * 64], np.float32)
+        mean = np.float32(0.0)
+        for v in inp:
+            mean = np.float32(mean + v)
+        mean = np.float32(mean / np.float32(64.0))
+        out = O.small_transform(f"afv{kind}", inp)
+        assert abs(float(out[0]) - float(mean)) < 1e-5, (kind, out[0], mean)
+
+
+def _numeric_inverse(n, forward):
+    m = np.zeros((n, n), np.float64)
+    for i in range(n):
+        e = np.zeros(n, np.float32)
+        e[i] = 1.0
+        m[:, i] = forward(e).astype(np.float64)
+    return np.linalg.inv(m)
+
+
+def _afv_to_pixels(kind, c):
+    # the decoder's AFV inverse as the reference's test restates it
+    # (src/afv.rs:505-589): inverse AFV of the (even, even) positions, inverse
+    # DCT4x4 of (even, odd), inverse DCT4x8 of the odd rows, from the
+    # un-mixed sub-part DCs; the DCT4 inverses are numeric
+    afv_x, afv_y = kind & 1, kind >> 1
+    b00, b01, b10 = c[0], c[1], c[8]
+    dcs = [np.float32((b00 + b10 + b01) * np.float32(4.0)), np.float32(b00 + b10 - b01),
+           np.float32(b00 - b10)]
+    px = np.full(64, np.nan, np.float32)
+    coeff = np.array([c[iy * 16 + ix * 2] for iy in range(4) for ix in range(4)], np.float32)
+    coeff[0] = dcs[0]
+    quad = (O.afv_basis().T.astype(np.float64) @ coeff.astype(np.float64)).astype(np.float32)
+    for iy in range(4):
+        for ix in range(4):
+            sy = 3 - iy if afv_y else iy
+            sx = 3 - ix if afv_x else ix
+            px[(iy + afv_y * 4) * 8 + afv_x * 4 + ix] = quad[sy * 4 + sx]
+    blk = np.array([c[iy * 16 + ix * 2 + 1] for iy in range(4) for ix in range(4)], np.float32)
+    blk[0] = dcs[1]
+    qp = (_numeric_inverse(16, O.dct4_2d) @ blk.astype(np.float64)).astype(np.float32)
+    qx = 0 if afv_x else 4
+    for iy in range(4):
+        px[(afv_y * 4 + iy) * 8 + qx:(afv_y * 4 + iy) * 8 + qx + 4] = qp[iy * 4:iy * 4 + 4]
+    half = np.array([c[(1 + iy * 2) * 8 + ix] for iy in range(4) for ix in range(8)], np.float32)
+    half[0] = dcs[2]
+    hp = (_numeric_inverse(32, O.dct4_2d) @ half.astype(np.float64)).astype(np.float32)
+    hy = 0 if afv_y else 4
+    px[hy * 8:hy * 8 + 32] = hp
+    return px
+
+
+def test_afv_round_trips_through_the_decoder_reference():
+    # src/afv.rs:591-614
+    vals = _afv_rnd(987654321, 256)
+    for kind in range(4):
+        inp = np.array(vals[kind * 64:(kind + 1) * 64], np.float32)
+        coeffs = O.small_transform(f"afv{kind}", inp)
+        back = _afv_to_pixels(kind, coeffs)
+        assert np.abs(back - inp).max() < 1e-4, (kind, np.abs(back - inp).max())
+
+
+def test_dct64_round_trips():
+    # src/dct.rs:2999-3014 (64x64, 1e-4) and :3072-3097 (64x32 and 32x64, 2e-4)
+    y, x = np.mgrid[0:64, 0:64]
+    xf, yf = x.astype(np.float32), y.astype(np.float32)
+    sq = (np.float32(0.01) * xf + np.float32(0.003) * yf
+          + ((x // 8 + y // 8) % 3).astype(np.float32) * np.float32(0.05)).astype(np.float32)
+    c, _ = O.dct("64x64", sq)
+    assert np.abs(O.idct("64x64", c) - sq).max() < 1e-4
+    tall = (np.float32(0.01) * xf[:, :32] + np.float32(0.003) * yf[:, :32]).astype(np.float32)
+    c, _ = O.dct("64x32", tall)
+    assert np.abs(O.idct("64x32", c) - tall).max() < 2e-4
+    wide = (np.float32(0.004) * xf[:32] + np.float32(0.007) * yf[:32]).astype(np.float32)
+    c, _ = O.dct("32x64", wide)
+    assert np.abs(O.idct("32x64", c) - wide).max() < 2e-4
+
+
+def test_rectangular_dct64_constant_dc_extracts():
+    # src/dct.rs:3100-3113
+    for name in ("64x32", "32x64"):
+        _, w, h, _ = O.DCT_KINDS[name]
+        _, dc = O.dct(name, np.full((h, w), 1.5, np.float32))
+        assert dc.size == 32 and np.abs(dc - 1.5).max() < 2e-4
+
+
+def test_dct32x8_dc_matches_the_wider_transforms():
+    # src/dct.rs:2880-2912: a 32x8 block's four DC values equal those of the
+    # 32x16 block made by repeating it sideways, and of its transpose as 8x32
+    half = np.array([(((i // 8) * 37) % 101) / 101.0 - 0.3 for i in range(256)], np.float32)
+    _, dc = O.dct("32x8", half.reshape(32, 8))
+    wide = np.array([half[(i // 16) * 8 + (i % 16) % 8] for i in range(512)], np.float32)
+    _, dc16 = O.dct("32x16", wide.reshape(32, 16))
+    for row in range(4):
+        assert abs(dc[row] - dc16[row * 2]) < 1e-4 and abs(dc[row] - dc16[row * 2 + 1]) < 1e-4
+    transposed = np.array([half[(i % 32) * 8 + i // 32] for i in range(256)], np.float32)
+    _, dc_wide = O.dct("8x32", transposed.reshape(8, 32))
+    assert np.abs(dc - dc_wide).max() < 1e-4
+
+
+@pytest.mark.parametrize("name", ["8x16", "16x8", "16x16", "16x32", "32x16", "32x32",
+                                  "32x8", "8x32", "64x64", "64x32", "32x64"])
+def test_dc_grid_follows_the_block_means(name):
+    # on a ramp the DC values approximate the covered 8x8 blocks' means in
+    # raster order of the blocks (a transposed grid would be off by 0.2+)
+    _, w, h, _ = O.DCT_KINDS[name]
+    y, x = np.mgrid[0:h, 0:w]
+    blk = (np.float32(0.01) * x + np.float32(0.03) * y).astype(np.float32)
+    _, dc = O.dct(name, blk)
+    means = blk.reshape(h // 8, 8, w // 8, 8).mean(axis=(1, 3)).reshape(-1)
+    assert np.abs(dc - means).max() < 0.01
