@@ -246,12 +246,14 @@ int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coe
 /* DctFn<W, H, N> of the larger blocks (src/dct.rs: dct8x16 :823, dct16x8
  * :904, dct16x16 :1010, dct32x32 :1980, dct32x16 :2251, dct16x32 :2340,
  * dct32x8 :1742, dct8x32 :1777, dct64x64 :2576, dct64x32 :2659, dct32x64
- * :2689; kind 0 is dct8x8 as jxg_op_dct8x8) with the DC values of every
- * covered 8x8 block (dc_from_dct*, :930-2806).  `blocks` holds `count`
- * row-major blocks of H rows of W samples; `coefficients` receives W H
- * coefficients per block in the reference's order, `dc_values` (optional)
- * one value per covered 8x8 block (1, 2, 2, 4, 8, 8, 16, 4, 4, 64, 32, 32
- * for kinds 0..11) in raster order of those blocks. */
+ * :2689; src/dct128.rs dct128x128 :385, dct128x64 :416, dct64x128 :446;
+ * kind 0 is dct8x8 as jxg_op_dct8x8) with the DC values of every covered
+ * 8x8 block (dc_from_dct*, src/dct.rs:930-2806, src/dct128.rs:561-636).
+ * `blocks` holds `count` row-major blocks of H rows of W samples;
+ * `coefficients` receives W H coefficients per block in the reference's
+ * order, `dc_values` (optional) one value per covered 8x8 block (1, 2, 2,
+ * 4, 8, 8, 16, 4, 4, 64, 32, 32, 256, 128, 128 for kinds 0..14) in raster
+ * order of those blocks. */
 #define JXG_DCT8X8 0
 #define JXG_DCT8X16 1  /* 8 rows x 16 columns */
 #define JXG_DCT16X8 2
@@ -264,12 +266,16 @@ int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coe
 #define JXG_DCT64X64 9
 #define JXG_DCT64X32 10 /* 64 rows x 32 columns */
 #define JXG_DCT32X64 11
+#define JXG_DCT128X128 12
+#define JXG_DCT128X64 13 /* 128 rows x 64 columns */
+#define JXG_DCT64X128 14
 int32_t jxg_op_dct(void* ctx, int32_t kind, const float* blocks, uint64_t count,
                    float* coefficients, float* dc_values);
 /* The inverse transforms (IdctMethods, src/dct.rs:358-416; inv_dct8x16
  * :1634, inv_dct16x8 :1658, inv_dct16x32 :1683, inv_dct32x16 :1705,
  * inv_dct8x32 :1804, inv_dct32x8 :1833, inv_dct64x32 :2710, inv_dct32x64
- * :2735, the square inverses :1590-1627): `count` blocks of W H
+ * :2735, the square inverses :1590-1627; src/dct128.rs:473-555): `count`
+ * blocks of W H
  * coefficients in jxg_op_dct's order back to row-major H x W samples. */
 int32_t jxg_op_idct(void* ctx, int32_t kind, const float* coefficients, uint64_t count,
                     float* blocks);

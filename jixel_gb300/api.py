@@ -331,7 +331,9 @@ class FrontendContext:
     DCT_KINDS = {"8x8": (0, 8, 8, 1), "8x16": (1, 16, 8, 2), "16x8": (2, 8, 16, 2),
                  "16x16": (3, 16, 16, 4), "16x32": (4, 32, 16, 8), "32x16": (5, 16, 32, 8),
                  "32x32": (6, 32, 32, 16), "32x8": (7, 8, 32, 4), "8x32": (8, 32, 8, 4),
-                 "64x64": (9, 64, 64, 64), "64x32": (10, 32, 64, 32), "32x64": (11, 64, 32, 32)}
+                 "64x64": (9, 64, 64, 64), "64x32": (10, 32, 64, 32), "32x64": (11, 64, 32, 32),
+                 "128x128": (12, 128, 128, 256), "128x64": (13, 64, 128, 128),
+                 "64x128": (14, 128, 64, 128)}
 
     def dct(self, name: str, blocks: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
         """DctFn<W, H, N> (src/dct.rs) of (count, H, W) blocks named rows x

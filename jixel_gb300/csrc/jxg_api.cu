@@ -1303,10 +1303,10 @@ int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coe
 int32_t jxg_op_dct(void* ctx, int32_t kind, const float* blocks, uint64_t count,
                    float* coefficients, float* dc_values) {
   Context* c = static_cast<Context*>(ctx);
-  static const int kW[12] = {8, 16, 8, 16, 32, 16, 32, 8, 32, 64, 32, 64};
-  static const int kH[12] = {8, 8, 16, 16, 16, 32, 32, 32, 8, 64, 64, 32};
-  static const int kDc[12] = {1, 2, 2, 4, 8, 8, 16, 4, 4, 64, 32, 32};
-  if (!c || !blocks || !coefficients || kind < 0 || kind > 11) return JXG_ERR_INVALID_ARGUMENT;
+  static const int kW[15] = {8, 16, 8, 16, 32, 16, 32, 8, 32, 64, 32, 64, 128, 64, 128};
+  static const int kH[15] = {8, 8, 16, 16, 16, 32, 32, 32, 8, 64, 64, 32, 128, 128, 64};
+  static const int kDc[15] = {1, 2, 2, 4, 8, 8, 16, 4, 4, 64, 32, 32, 256, 128, 128};
+  if (!c || !blocks || !coefficients || kind < 0 || kind > 14) return JXG_ERR_INVALID_ARGUMENT;
   if (count == 0) return JXG_OK;
   if (count > (1ull << 31)) return JXG_ERR_DIMENSION_TOO_LARGE;
   cudaSetDevice(c->device);
@@ -1326,6 +1326,12 @@ int32_t jxg_op_dct(void* ctx, int32_t kind, const float* blocks, uint64_t count,
     kernel<<<static_cast<unsigned>((count + warps - 1) / warps), 32 * warps, 0, s>>>(
         din, cnt, dout, ddc, kind, ndc);
   };
+  // the 128-point family: one warp per block, its tile in dynamic shared memory
+  auto run_large = [&](auto kernel, size_t smem) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(smem));
+    kernel<<<static_cast<unsigned>(count), 32, smem, s>>>(din, cnt, dout, ddc, kind, ndc);
+  };
   st = jxg::launch(c, "k_dct_blocks", c->timing, [&] {
     using namespace jxg;
     switch (kind) {
@@ -1342,7 +1348,15 @@ int32_t jxg_op_dct(void* ctx, int32_t kind, const float* blocks, uint64_t count,
       case kDct8x32: run(k_dct_blocks<32, 8, false>, dct_warps<32, 8>()); break;
       case kDct64x64: run(k_dct_blocks<64, 64, true>, dct_warps<64, 64>()); break;
       case kDct64x32: run(k_dct_blocks<32, 64, true>, dct_warps<32, 64>()); break;
-      default: run(k_dct_blocks<64, 32, false>, dct_warps<64, 32>());  // 32x64
+      case kDct32x64: run(k_dct_blocks<64, 32, false>, dct_warps<64, 32>()); break;
+      case kDct128x128:
+        run_large(k_dct_large_blocks<128, 128, true>, large_dct_smem<128, 128>());
+        break;
+      case kDct128x64:
+        run_large(k_dct_large_blocks<64, 128, true>, large_dct_smem<64, 128>());
+        break;
+      default:  // 64x128
+        run_large(k_dct_large_blocks<128, 64, false>, large_dct_smem<128, 64>());
     }
   });
   if (st) return st;
@@ -1358,9 +1372,9 @@ int32_t jxg_op_dct(void* ctx, int32_t kind, const float* blocks, uint64_t count,
 int32_t jxg_op_idct(void* ctx, int32_t kind, const float* coefficients, uint64_t count,
                     float* blocks) {
   Context* c = static_cast<Context*>(ctx);
-  static const int kW[12] = {8, 16, 8, 16, 32, 16, 32, 8, 32, 64, 32, 64};
-  static const int kH[12] = {8, 8, 16, 16, 16, 32, 32, 32, 8, 64, 64, 32};
-  if (!c || !coefficients || !blocks || kind < 0 || kind > 11) return JXG_ERR_INVALID_ARGUMENT;
+  static const int kW[15] = {8, 16, 8, 16, 32, 16, 32, 8, 32, 64, 32, 64, 128, 64, 128};
+  static const int kH[15] = {8, 8, 16, 16, 16, 32, 32, 32, 8, 64, 64, 32, 128, 128, 64};
+  if (!c || !coefficients || !blocks || kind < 0 || kind > 14) return JXG_ERR_INVALID_ARGUMENT;
   if (count == 0) return JXG_OK;
   if (count > (1ull << 31)) return JXG_ERR_DIMENSION_TOO_LARGE;
   cudaSetDevice(c->device);
@@ -1374,6 +1388,11 @@ int32_t jxg_op_idct(void* ctx, int32_t kind, const float* coefficients, uint64_t
   const int64_t cnt = static_cast<int64_t>(count);
   auto run = [&](auto kernel, int warps) {
     kernel<<<static_cast<unsigned>((count + warps - 1) / warps), 32 * warps, 0, s>>>(din, cnt, dout);
+  };
+  auto run_large = [&](auto kernel, size_t smem) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(smem));
+    kernel<<<static_cast<unsigned>(count), 32, smem, s>>>(din, cnt, dout);
   };
   st = jxg::launch(c, "k_idct_blocks", c->timing, [&] {
     using namespace jxg;
@@ -1389,7 +1408,15 @@ int32_t jxg_op_idct(void* ctx, int32_t kind, const float* coefficients, uint64_t
       case kDct8x32: run(k_idct_blocks<32, 8, kIdctRowsFirst>, dct_warps<32, 8>()); break;
       case kDct64x64: run(k_idct_blocks<64, 64, kIdctSquare>, dct_warps<64, 64>()); break;
       case kDct64x32: run(k_idct_blocks<32, 64, kIdctColsFirst>, dct_warps<32, 64>()); break;
-      default: run(k_idct_blocks<64, 32, kIdctRowsFirst>, dct_warps<64, 32>());  // 32x64
+      case kDct32x64: run(k_idct_blocks<64, 32, kIdctRowsFirst>, dct_warps<64, 32>()); break;
+      case kDct128x128:
+        run_large(k_idct_large_blocks<128, 128, kIdctSquare>, large_dct_smem<128, 128>());
+        break;
+      case kDct128x64:
+        run_large(k_idct_large_blocks<64, 128, kIdctColsFirst>, large_dct_smem<64, 128>());
+        break;
+      default:  // 64x128
+        run_large(k_idct_large_blocks<128, 64, kIdctRowsFirst>, large_dct_smem<128, 64>());
     }
   });
   if (st) return st;

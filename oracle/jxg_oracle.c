@@ -54,7 +54,8 @@
 enum {
   JXG_ORC_DCT8X8 = 0, JXG_ORC_DCT8X16 = 1, JXG_ORC_DCT16X8 = 2, JXG_ORC_DCT16X16 = 3,
   JXG_ORC_DCT16X32 = 4, JXG_ORC_DCT32X16 = 5, JXG_ORC_DCT32X32 = 6, JXG_ORC_DCT32X8 = 7,
-  JXG_ORC_DCT8X32 = 8, JXG_ORC_DCT64X64 = 9, JXG_ORC_DCT64X32 = 10, JXG_ORC_DCT32X64 = 11
+  JXG_ORC_DCT8X32 = 8, JXG_ORC_DCT64X64 = 9, JXG_ORC_DCT64X32 = 10, JXG_ORC_DCT32X64 = 11,
+  JXG_ORC_DCT128X128 = 12, JXG_ORC_DCT128X64 = 13, JXG_ORC_DCT64X128 = 14
 };
 
 static inline float fmla(float a, float b, float c) { return fmaf(a, b, c); }
@@ -941,20 +942,60 @@ static inline void dct1d_64(float* b) {
   }
 }
 
+/* WC128 (src/dct128.rs:76-141), the reference's literals rounded to float. */
+static const float WC128[64] = {
+    0x1.0004fp-1f, 0x1.002c7p-1f, 0x1.007b9p-1f, 0x1.00f28ep-1f,
+    0x1.0191c2p-1f, 0x1.0259aep-1f, 0x1.034aecp-1f, 0x1.04663ap-1f,
+    0x1.05ac7cp-1f, 0x1.071ebap-1f, 0x1.08be24p-1f, 0x1.0a8c1p-1f,
+    0x1.0c8a06p-1f, 0x1.0eb9bap-1f, 0x1.111d12p-1f, 0x1.13b632p-1f,
+    0x1.168776p-1f, 0x1.19937ep-1f, 0x1.1cdd2ep-1f, 0x1.2067c4p-1f,
+    0x1.2436ccp-1f, 0x1.284e3cp-1f, 0x1.2cb272p-1f, 0x1.31684ap-1f,
+    0x1.367524p-1f, 0x1.3bdfp-1f, 0x1.41ac88p-1f, 0x1.47e52cp-1f,
+    0x1.4e914p-1f, 0x1.55ba12p-1f, 0x1.5d6a1ap-1f, 0x1.65ad26p-1f,
+    0x1.6e9088p-1f, 0x1.78235ep-1f, 0x1.8276d8p-1f, 0x1.8d9e9ap-1f,
+    0x1.99b12ep-1f, 0x1.a6c88cp-1f, 0x1.b502c4p-1f, 0x1.c482ep-1f,
+    0x1.d571ep-1f, 0x1.e8001ep-1f, 0x1.fc66f4p-1f, 0x1.09757ep+0f,
+    0x1.15ef74p+0f, 0x1.23d3aep+0f, 0x1.335ffap+0f, 0x1.44e132p+0f,
+    0x1.58b8p+0f, 0x1.6f5fc6p+0f, 0x1.897872p+0f, 0x1.a7d52cp+0f,
+    0x1.cb9292p+0f, 0x1.f639b2p+0f, 0x1.14fc92p+1f, 0x1.350332p+1f,
+    0x1.5da68cp+1f, 0x1.92e00ap+1f, 0x1.db8d12p+1f, 0x1.225298p+2f,
+    0x1.74f8d8p+2f, 0x1.04ec54p+3f, 0x1.b2b282p+3f, 0x1.45f52p+5f,
+};
+
+/* dct1d_128 (src/dct128.rs:330-350), the recursion over dct1d_64. */
+static inline void dct1d_128(float* b) {
+  float t[128];
+  for (int i = 0; i < 64; i++) {
+    t[i] = b[i] + b[127 - i];
+    t[64 + i] = (b[i] - b[127 - i]) * WC128[i];
+  }
+  dct1d_64(t);
+  dct1d_64(t + 64);
+  t[64] = fmla(t[64], SQRT2F, t[65]);
+  for (int i = 65; i < 127; i++) t[i] += t[i + 1];
+  for (int i = 0; i < 64; i++) {
+    b[2 * i] = t[i];
+    b[2 * i + 1] = t[64 + i];
+  }
+}
+
 static inline void dct1d_n(float* b, int n) {
   if (n == 8) dct1d_8(b);
   else if (n == 16) dct1d_16(b);
   else if (n == 32) dct1d_32(b);
-  else dct1d_64(b);
+  else if (n == 64) dct1d_64(b);
+  else dct1d_128(b);
 }
 
 /* An H x W block (H rows of W samples), columns first: each column through
  * the H-point transform, then each row through the W-point one, stored
  * out[u * H + v] scaled by 1 / (W H) -- dct16x8 (src/dct.rs:904),
  * dct16x16 (:1010), dct32x32 (:1980), dct32x16 (:2251), dct32x8 (:1742),
- * dct64x64 (:2576), dct64x32 (:2659). */
+ * dct64x64 (:2576), dct64x32 (:2659); src/dct128.rs dct128x128 :385,
+ * dct128x64 :416. */
 static void dct_cols_first(const float* in, int W, int H, float* out) {
-  float after[4096], col[64], row[64];
+  float* after = malloc(sizeof(float) * (size_t)(W * H));
+  float col[128], row[128];
   for (int u = 0; u < W; u++) {
     for (int i = 0; i < H; i++) col[i] = in[i * W + u];
     dct1d_n(col, H);
@@ -966,12 +1007,15 @@ static void dct_cols_first(const float* in, int W, int H, float* out) {
     dct1d_n(row, W);
     for (int u = 0; u < W; u++) out[u * H + v] = row[u] * scale;
   }
+  free(after);
 }
 
 /* Rows first, then columns, stored out[v * W + u] -- dct8x16
- * (src/dct.rs:823), dct16x32 (:2340), dct8x32 (:1777), dct32x64 (:2689). */
+ * (src/dct.rs:823), dct16x32 (:2340), dct8x32 (:1777), dct32x64 (:2689);
+ * dct64x128 (src/dct128.rs:446). */
 static void dct_rows_first(const float* in, int W, int H, float* out) {
-  float after[4096], col[64], row[64];
+  float* after = malloc(sizeof(float) * (size_t)(W * H));
+  float col[128], row[128];
   for (int i = 0; i < H; i++) {
     for (int u = 0; u < W; u++) row[u] = in[i * W + u];
     dct1d_n(row, W);
@@ -983,6 +1027,7 @@ static void dct_rows_first(const float* in, int W, int H, float* out) {
     dct1d_n(col, H);
     for (int v = 0; v < H; v++) out[v * W + u] = col[v] * scale;
   }
+  free(after);
 }
 
 /* idct1d_4 of the DC extraction (src/dct.rs:2144-2167). */
@@ -1003,6 +1048,7 @@ static void idct1d_4(const float v[4], float out[4]) {
 }
 
 static inline void inv_dct1d_8(float* b);
+static inline void inv_dct1d_16(float* b);
 static void idct_square(const float* c, int n, float* out);
 
 static const float R16_2[2] = {1.0f, 0.9017642f};                         /* :927 */
@@ -1012,6 +1058,33 @@ static const float R64_8[8] = {
     0x1p+0f, 0x1.fcc47ep-1f, 0x1.f3245ep-1f, 0x1.e35656p-1f,
     0x1.cdb40ap-1f, 0x1.b2b7aap-1f, 0x1.92f8dcp-1f, 0x1.6f28ccp-1f,
 };
+
+/* RESAMPLE_SCALE_128_TO_16 (src/dct128.rs:48-65) */
+static const float R128_16[16] = {
+    0x1p+0f, 0x1.ff30d6p-1f, 0x1.fcc47ep-1f, 0x1.f8be6cp-1f,
+    0x1.f3245ep-1f, 0x1.ebfe48p-1f, 0x1.e35656p-1f, 0x1.d938d2p-1f,
+    0x1.cdb40ap-1f, 0x1.c0d848p-1f, 0x1.b2b7aap-1f, 0x1.a3660ap-1f,
+    0x1.92f8dcp-1f, 0x1.81870ap-1f, 0x1.6f28ccp-1f, 0x1.5bf786p-1f,
+};
+
+/* dc_from_dct128x64_normalized (src/dct128.rs:580-609): along the 64-point
+ * axis a, the 128-point axis' 16 lowest coefficients scaled by r8[a]
+ * r16[b] and 16 through the 16-point inverse; then per position, scaled by
+ * 8, the 8-point inverse across a.  norm[i][j]: i along the 64-point axis,
+ * j along the 128-point one. */
+static void dc_128x64_normalized(const float* c, float norm[8][16]) {
+  float rows[8][16];
+  for (int a = 0; a < 8; a++) {
+    for (int b = 0; b < 16; b++) rows[a][b] = c[a * 128 + b] * (R64_8[a] * R128_16[b]) * 16.0f;
+    inv_dct1d_16(rows[a]);
+  }
+  for (int x = 0; x < 16; x++) {
+    float col[8];
+    for (int y = 0; y < 8; y++) col[y] = rows[y][x] * 8.0f;
+    inv_dct1d_8(col);
+    for (int y = 0; y < 8; y++) norm[y][x] = col[y];
+  }
+}
 
 /* dc_from_dct64x32_normalized (:2767-2786): per low horizontal-or-vertical
  * frequency a of the 32-point axis, the 8-point axis' lowest coefficients
@@ -1104,6 +1177,25 @@ static void dc_from(int kind, const float* c, float* dc) {
         }
       break;
     }
+    case JXG_ORC_DCT128X128: { /* dc_from_dct128x128 (src/dct128.rs:561-573) */
+      float low[256];
+      for (int y = 0; y < 16; y++)
+        for (int x = 0; x < 16; x++)
+          low[y * 16 + x] = c[y * 128 + x] * (R128_16[x] * R128_16[y]);
+      idct_square(low, 16, dc);
+      break;
+    }
+    case JXG_ORC_DCT128X64:
+    case JXG_ORC_DCT64X128: { /* dc_from_dct128x64 (:612), dc_from_dct64x128 (:629) */
+      float norm[8][16];
+      dc_128x64_normalized(c, norm);
+      for (int y = 0; y < 8; y++)
+        for (int x = 0; x < 16; x++) {
+          if (kind == JXG_ORC_DCT128X64) dc[x * 8 + y] = norm[y][x];
+          else dc[y * 16 + x] = norm[y][x];
+        }
+      break;
+    }
     default: { /* 32x32 */
       float rr[4][4];
       for (int a = 0; a < 4; a++) {
@@ -1137,6 +1229,9 @@ int orc_dct(int kind, const float* in, float* out, float* dc) {
     case JXG_ORC_DCT64X64: dct_cols_first(in, 64, 64, out); break;
     case JXG_ORC_DCT64X32: dct_cols_first(in, 32, 64, out); break;
     case JXG_ORC_DCT32X64: dct_rows_first(in, 64, 32, out); break;
+    case JXG_ORC_DCT128X128: dct_cols_first(in, 128, 128, out); break;
+    case JXG_ORC_DCT128X64: dct_cols_first(in, 64, 128, out); break;
+    case JXG_ORC_DCT64X128: dct_rows_first(in, 128, 64, out); break;
     default: return -1;
   }
   if (dc) dc_from(kind, out, dc);
@@ -1263,17 +1358,57 @@ static inline void inv_dct1d_64(float* b) {
   }
 }
 
+/* INV_WC128 (src/dct128.rs:143-208): the reference's own literals, not all
+ * equal to 1 / WC128 in float. */
+static const float INV_WC128[64] = {
+    0x1.fff622p+0f, 0x1.ffa72ep+0f, 0x1.ff0956p+0f, 0x1.fe1cbp+0f,
+    0x1.fce16p+0f, 0x1.fb5798p+0f, 0x1.f97f92p+0f, 0x1.f7599ap+0f,
+    0x1.f4e604p+0f, 0x1.f2253p+0f, 0x1.ef178ap+0f, 0x1.ebbd8cp+0f,
+    0x1.e817bap+0f, 0x1.e426a4p+0f, 0x1.dfeae6p+0f, 0x1.db6526p+0f,
+    0x1.d69618p+0f, 0x1.d17e78p+0f, 0x1.cc1f1p+0f, 0x1.c678b4p+0f,
+    0x1.c08c42p+0f, 0x1.ba5aa6p+0f, 0x1.b3e4d4p+0f, 0x1.ad2bcap+0f,
+    0x1.a63092p+0f, 0x1.9ef43ep+0f, 0x1.9777fp+0f, 0x1.8fbccap+0f,
+    0x1.87c4p+0f, 0x1.7f8ecep+0f, 0x1.771e76p+0f, 0x1.6e7446p+0f,
+    0x1.659192p+0f, 0x1.5c77bcp+0f, 0x1.53282ap+0f, 0x1.49a44ap+0f,
+    0x1.3fed96p+0f, 0x1.36058cp+0f, 0x1.2bedb2p+0f, 0x1.21a79ap+0f,
+    0x1.1734d6p+0f, 0x1.0c9704p+0f, 0x1.01cfc8p+0f, 0x1.edc196p-1f,
+    0x1.d79776p-1f, 0x1.c1249ep-1f, 0x1.aa6c82p-1f, 0x1.9372a6p-1f,
+    0x1.7c3a94p-1f, 0x1.64c7dep-1f, 0x1.4d1e24p-1f, 0x1.35410cp-1f,
+    0x1.1d3444p-1f, 0x1.04fb8p-1f, 0x1.d934fep-2f, 0x1.a82a02p-2f,
+    0x1.76dd9ep-2f, 0x1.45576cp-2f, 0x1.139f0cp-2f, 0x1.c3785cp-3f,
+    0x1.5f6dp-3f, 0x1.f656e8p-4f, 0x1.2d8658p-4f, 0x1.921d2p-6f,
+};
+
+/* inv_dct1d_128 (src/dct128.rs:356-378). */
+static inline void inv_dct1d_128(float* b) {
+  float t[128];
+  for (int i = 0; i < 64; i++) {
+    t[i] = b[2 * i];
+    t[64 + i] = b[2 * i + 1];
+  }
+  for (int i = 126; i >= 65; i--) t[i] -= t[i + 1];
+  t[64] = (t[64] - t[65]) * IS2F;
+  inv_dct1d_64(t + 64);
+  for (int i = 0; i < 64; i++) t[64 + i] *= INV_WC128[i];
+  inv_dct1d_64(t);
+  for (int i = 0; i < 64; i++) {
+    b[i] = (t[i] + t[64 + i]) * 0.5f;
+    b[127 - i] = (t[i] - t[64 + i]) * 0.5f;
+  }
+}
+
 static inline void inv_dct1d_n(float* b, int n) {
   if (n == 8) inv_dct1d_8(b);
   else if (n == 16) inv_dct1d_16(b);
   else if (n == 32) inv_dct1d_32(b);
-  else inv_dct1d_64(b);
+  else if (n == 64) inv_dct1d_64(b);
+  else inv_dct1d_128(b);
 }
 
 /* Inverse of a square transform (inv_dct_square, :1590-1620): coefficients
  * transposed and scaled by N, columns, then rows. */
 static void idct_square(const float* c, int n, float* out) {
-  float col[64];
+  float col[128];
   const float scale = (float)(n * n);
   for (int a = 0; a < n; a++)
     for (int b = 0; b < n; b++) out[b * n + a] = c[a * n + b] * scale;
@@ -1286,10 +1421,11 @@ static void idct_square(const float* c, int n, float* out) {
 }
 
 /* Inverse of a rows-first transform (inv_dct8x16 :1634, inv_dct16x32
- * :1683, inv_dct8x32 :1804, inv_dct32x64 :2735): coefficients in place
+ * :1683, inv_dct8x32 :1804, inv_dct32x64 :2735, inv_dct64x128
+ * src/dct128.rs:532): coefficients in place
  * scaled by N, columns (length H), rows. */
 static void idct_rows_first(const float* c, int W, int H, float* out) {
-  float col[64];
+  float col[128];
   const float scale = (float)(W * H);
   for (int k = 0; k < W * H; k++) out[k] = c[k] * scale;
   for (int u = 0; u < W; u++) {
@@ -1301,11 +1437,13 @@ static void idct_rows_first(const float* c, int W, int H, float* out) {
 }
 
 /* Inverse of a columns-first transform (inv_dct16x8 :1658, inv_dct32x16
- * :1705, inv_dct32x8 :1833, inv_dct64x32 :2710): per pixel row v the
+ * :1705, inv_dct32x8 :1833, inv_dct64x32 :2710, inv_dct128x64
+ * src/dct128.rs:502): per pixel row v the
  * W-point inverse of coefficients c[u H + v] scaled by N, then per column
  * the H-point inverse. */
 static void idct_cols_first(const float* c, int W, int H, float* out) {
-  float acd[4096], row[64], col[64];
+  float* acd = malloc(sizeof(float) * (size_t)(W * H));
+  float row[128], col[128];
   const float scale = (float)(W * H);
   for (int v = 0; v < H; v++) {
     for (int u = 0; u < W; u++) row[u] = c[u * H + v] * scale;
@@ -1317,6 +1455,7 @@ static void idct_cols_first(const float* c, int W, int H, float* out) {
     inv_dct1d_n(col, H);
     for (int i = 0; i < H; i++) out[i * W + u] = col[i];
   }
+  free(acd);
 }
 
 /* The inverse of orc_dct's transform `kind`: W H coefficients back to a
@@ -1335,6 +1474,9 @@ int orc_idct(int kind, const float* coeffs, float* out) {
     case JXG_ORC_DCT64X64: idct_square(coeffs, 64, out); break;
     case JXG_ORC_DCT64X32: idct_cols_first(coeffs, 32, 64, out); break;
     case JXG_ORC_DCT32X64: idct_rows_first(coeffs, 64, 32, out); break;
+    case JXG_ORC_DCT128X128: idct_square(coeffs, 128, out); break;
+    case JXG_ORC_DCT128X64: idct_cols_first(coeffs, 64, 128, out); break;
+    case JXG_ORC_DCT64X128: idct_rows_first(coeffs, 128, 64, out); break;
     default: return -1;
   }
   return 0;

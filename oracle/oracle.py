@@ -344,6 +344,7 @@ DCT_KINDS = {
     "16x32": (4, 32, 16, 8), "32x16": (5, 16, 32, 8), "32x32": (6, 32, 32, 16),
     "32x8": (7, 8, 32, 4), "8x32": (8, 32, 8, 4), "64x64": (9, 64, 64, 64),
     "64x32": (10, 32, 64, 32), "32x64": (11, 64, 32, 32),
+    "128x128": (12, 128, 128, 256), "128x64": (13, 64, 128, 128), "64x128": (14, 128, 64, 128),
 }
 
 
@@ -351,8 +352,8 @@ def dct(name: str, block: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
     """`DctFn<W, H, N>` of one (H, W) block (src/dct.rs: dct8x16 :823, dct16x8
     :904, dct16x16 :1010, dct32x32 :1980, dct32x16 :2251, dct16x32 :2340,
     dct32x8 :1742, dct8x32 :1777, dct64x64 :2576, dct64x32 :2659, dct32x64
-    :2689) and its per-8x8 DC values (dc_from_dct*): (N coefficients, DC
-    values)."""
+    :2689; src/dct128.rs dct128x128 :385, dct128x64 :416, dct64x128 :446) and
+    its per-8x8 DC values (dc_from_dct*): (N coefficients, DC values)."""
     kind, w, h, ndc = DCT_KINDS[name]
     b = np.ascontiguousarray(block, np.float32).reshape(h, w)
     out = np.zeros(w * h, np.float32)
@@ -364,9 +365,9 @@ def dct(name: str, block: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
 
 def dct1d(vec: np.ndarray) -> np.ndarray:
     """dct1d_8 / dct1d_16 / dct1d_32 / dct1d_64 (src/dct.rs:109, :687, :1477,
-    :2529) of one vector."""
+    :2529) / dct1d_128 (src/dct128.rs:330) of one vector."""
     v = np.ascontiguousarray(vec, np.float32).copy()
-    assert v.size in (8, 16, 32, 64)
+    assert v.size in (8, 16, 32, 64, 128)
     lib().orc_dct1d(v.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(v.size))
     return v
 

@@ -17,7 +17,7 @@ def ctx():
 
 
 ALL_DCT = ["8x8", "8x16", "16x8", "16x16", "16x32", "32x16", "32x32", "32x8", "8x32",
-           "64x64", "64x32", "32x64"]
+           "64x64", "64x32", "32x64", "128x128", "128x64", "64x128"]
 
 
 @pytest.mark.parametrize("name", ALL_DCT)
@@ -40,8 +40,8 @@ def test_transform_and_dc_match_oracle(ctx, name):
 def test_dct_operator_rejects_bad_kinds(ctx):
     lib = ctx._lib
     b = np.zeros(64, np.float32)
-    assert lib.jxg_op_dct(ctx.handle, 12, b.ctypes.data, 1, b.ctypes.data, None) != 0
-    assert lib.jxg_op_idct(ctx.handle, 12, b.ctypes.data, 1, b.ctypes.data) != 0
+    assert lib.jxg_op_dct(ctx.handle, 15, b.ctypes.data, 1, b.ctypes.data, None) != 0
+    assert lib.jxg_op_idct(ctx.handle, 15, b.ctypes.data, 1, b.ctypes.data) != 0
     assert lib.jxg_op_small_transform(ctx.handle, 11, b.ctypes.data, 1, b.ctypes.data) != 0
     assert lib.jxg_op_dct(ctx.handle, -1, b.ctypes.data, 1, b.ctypes.data, None) != 0
     assert lib.jxg_op_dct(ctx.handle, 3, b.ctypes.data, 0, b.ctypes.data, None) == 0  # no blocks

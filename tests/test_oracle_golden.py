@@ -323,7 +323,7 @@ def test_packed_form_is_decided_per_group():
     assert _pairs(words, woffs, goffs) == toks.tolist()
 
 
-@pytest.mark.parametrize("n", [32, 64])
+@pytest.mark.parametrize("n", [32, 64, 128])
 def test_dct1d_diagonalizes_the_dct_basis(n):
     # src/dct.rs:3265-3289 (32 points; the 64-point recursion alike): the
     # k0-th DCT-II basis vector peaks at k0 only
@@ -566,7 +566,8 @@ def test_dct32x8_dc_matches_the_wider_transforms():
 
 
 @pytest.mark.parametrize("name", ["8x16", "16x8", "16x16", "16x32", "32x16", "32x32",
-                                  "32x8", "8x32", "64x64", "64x32", "32x64"])
+                                  "32x8", "8x32", "64x64", "64x32", "32x64",
+                                  "128x128", "128x64", "64x128"])
 def test_dc_grid_follows_the_block_means(name):
     # on a ramp the DC values approximate the covered 8x8 blocks' means in
     # raster order of the blocks (a transposed grid would be off by 0.2+)
@@ -576,3 +577,55 @@ def test_dc_grid_follows_the_block_means(name):
     _, dc = O.dct(name, blk)
     means = blk.reshape(h // 8, 8, w // 8, 8).mean(axis=(1, 3)).reshape(-1)
     assert np.abs(dc - means).max() < 0.01
+
+
+def _pattern128(w, h):
+    # src/dct128.rs:945-957
+    y, x = np.mgrid[0:h, 0:w]
+    return (np.float32(0.01) * x.astype(np.float32) + np.float32(0.003) * y.astype(np.float32)
+            + ((x // 8 + 2 * (y // 8)) % 5).astype(np.float32) * np.float32(0.05)
+            + ((x * 7 + y * 13) % 11).astype(np.float32) * np.float32(0.002)).astype(np.float32)
+
+
+@pytest.mark.parametrize("name", ["128x128", "128x64", "64x128"])
+def test_dct128_round_trips(name):
+    # src/dct128.rs:976-1010
+    _, w, h, _ = O.DCT_KINDS[name]
+    px = _pattern128(w, h)
+    c, _ = O.dct(name, px)
+    assert np.abs(O.idct(name, c) - px).max() < 2e-4
+
+
+@pytest.mark.parametrize("name", ["128x128", "128x64", "64x128"])
+def test_dct128_dc_grid_tracks_block_means_on_smooth_content(name):
+    # src/dct128.rs:1012-1063: tall and wide blocks are the top-left part of
+    # the 128x128 image
+    y, x = np.mgrid[0:128, 0:128]
+    img = np.array([math.sin(np.float32(v)) for v in (x * np.float32(0.021)).reshape(-1)],
+                   np.float32).reshape(128, 128)
+    img = (img + np.array([math.cos(np.float32(v)) for v in (y * np.float32(0.013)).reshape(-1)],
+                          np.float32).reshape(128, 128) * np.float32(0.5)).astype(np.float32)
+    _, w, h, _ = O.DCT_KINDS[name]
+    blk = np.ascontiguousarray(img[:h, :w])
+    _, dc = O.dct(name, blk)
+    means = blk.reshape(h // 8, 8, w // 8, 8).mean(axis=(1, 3)).reshape(-1)
+    assert np.abs(dc - means).max() < 0.02
+
+
+@pytest.mark.parametrize("name", ["128x128", "128x64", "64x128", "64x64", "64x32", "32x64"])
+def test_large_dct_cosine_basis(name):
+    # src/dct128.rs:851-886: a separable cosine of frequencies (u, v) lands on
+    # one coefficient, 1 / sqrt(2) per non-zero frequency, at u H + v when
+    # H >= W, else v W + u
+    _, w, h, _ = O.DCT_KINDS[name]
+    for u, v in [(0, 0), (1, 0), (0, 1), (w // 2, h // 2), (w - 3, h - 3), (w - 1, h - 1)]:
+        i = np.arange(w * h)
+        xs = np.cos((math.pi * (i % w) + math.pi / 2) * u / w)
+        ys = np.cos((math.pi * (i // w) + math.pi / 2) * v / h)
+        px = (xs * ys).astype(np.float32).reshape(h, w)
+        got, _ = O.dct(name, px)
+        want = np.zeros(w * h, np.float32)
+        index = u * h + v if h >= w else v * w + u
+        want[index] = (1.0 if u == 0 else np.float32(math.sqrt(0.5))) * (
+            1.0 if v == 0 else np.float32(math.sqrt(0.5)))
+        assert np.abs(got - want).max() < 2e-6, (name, u, v, np.abs(got - want).max())
