@@ -104,8 +104,8 @@ struct Context {
   // pass buffers (grown, never shrunk)
   DevBuf pixels, xyb, qf, ytox, ytob, quant_dc, levels, wide_levels, coeffs, nzeros, nz_packed,
       counts, tokens, hist, stats, group_offsets, plan, total, op_in, op_out,
-      alpha, alpha_peak, alpha_zero, fill_flags, fill_deps, fill_queue, group_wide, packed,
-      packed_offs, tok_status;
+      alpha, alpha_peak, alpha_zero, fill_flags, fill_deps, fill_queue, fill_masks, group_wide,
+      packed, packed_offs, tok_status;
   HostBuf plan_host, pixels_host;
   // The plan (frame descriptors + chunk prefixes) lives in a ring of slots,
   // pinned on the host and mirrored on the device, so a pass can be planned
@@ -398,6 +398,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
       (fill_total && (st = ensure(c, c->fill_flags, fill_total))) ||
       (fill_total && (st = ensure(c, c->fill_deps, fill_total * 4))) ||
       (fill_total && (st = ensure(c, c->fill_queue, fill_total * 4))) ||
+      (fill_total && (st = ensure(c, c->fill_masks, fill_total * jxg::kFillMaskWords * 8))) ||
       (!pixels_on_device && stage && (st = ensure_host(c, c->pixels_host, pix))))
     return st;
   // frame descriptors
@@ -518,9 +519,13 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
   uint8_t* fill_flags = static_cast<uint8_t*>(c->fill_flags.ptr);
   uint32_t* fill_deps = static_cast<uint32_t*>(c->fill_deps.ptr);
   uint32_t* fill_queue = static_cast<uint32_t*>(c->fill_queue.ptr);
+  uint64_t* fill_masks = static_cast<uint64_t*>(c->fill_masks.ptr);
   const unsigned fill_grid = static_cast<unsigned>(std::max<int64_t>(
       1, std::min<int64_t>((c->fill_tiles + kFillThreads / 32 - 1) / (kFillThreads / 32),
                            static_cast<int64_t>(c->num_sms) * 3)));
+  // the fill pass: a CTA per tile in flight, as many as fit the SMs
+  const unsigned fill_run_grid = static_cast<unsigned>(std::max<int64_t>(
+      1, std::min<int64_t>(c->fill_tiles, static_cast<int64_t>(c->num_sms) * 8)));
   if (c->fill_tiles) {
     JXG_CUDA(c, cudaMemsetAsync(fill_queue, 0xFF, c->fill_tiles * 4, s));
     JXG_CUDA(c, cudaMemsetAsync(fill_q, 0, sizeof(FillQueue), s));
@@ -541,11 +546,11 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
          })) ||
          (st = launch(c, "k_fill_plan", timed, [&] {
            k_fill_plan<<<fill_grid, kFillThreads, kFillSmemBytes, s>>>(
-               f0, c->fill_tiles, fill_flags, fill_deps, fill_queue, fill_q);
+               f0, c->fill_tiles, fill_flags, fill_deps, fill_masks, fill_queue, fill_q);
          })) ||
          (st = launch(c, "k_fill_invisible", timed, [&] {
-           k_fill_invisible<<<fill_grid, kFillThreads, kFillSmemBytes, s>>>(
-               f0, fill_flags, fill_deps, fill_queue, fill_q);
+           k_fill_invisible<<<fill_run_grid, kFillRunThreads, kFillRunSmemBytes, s>>>(
+               f0, fill_flags, fill_deps, fill_masks, fill_queue, fill_q);
          }))))
       return st;
     if ((st = launch(c, "k_adaptive_quant", timed, [&] {
@@ -573,11 +578,12 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
          })) ||
          (st = launch(c, "k_fill_plan_batch", timed, [&] {
            k_fill_plan_batch<<<fill_grid, kFillThreads, kFillSmemBytes, s>>>(
-               frames, pre_fill, n, c->fill_tiles, fill_flags, fill_deps, fill_queue, fill_q);
+               frames, pre_fill, n, c->fill_tiles, fill_flags, fill_deps, fill_masks, fill_queue,
+               fill_q);
          })) ||
          (st = launch(c, "k_fill_invisible_batch", timed, [&] {
-           k_fill_invisible_batch<<<fill_grid, kFillThreads, kFillSmemBytes, s>>>(
-               frames, pre_fill, n, fill_flags, fill_deps, fill_queue, fill_q);
+           k_fill_invisible_batch<<<fill_run_grid, kFillRunThreads, kFillRunSmemBytes, s>>>(
+               frames, pre_fill, n, fill_flags, fill_deps, fill_masks, fill_queue, fill_q);
          }))))
       return st;
     if ((st = launch(c, "k_adaptive_quant_batch", timed, [&] {
@@ -916,10 +922,10 @@ int32_t jxg_context_create(int32_t device, void** out_ctx) {
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(jxg::kTileSmemBytes)) == cudaSuccess &&
             cudaFuncSetAttribute(jxg::k_fill_invisible, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(jxg::kFillSmemBytes)) == cudaSuccess &&
+                                 static_cast<int>(jxg::kFillRunSmemBytes)) == cudaSuccess &&
             cudaFuncSetAttribute(jxg::k_fill_invisible_batch,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(jxg::kFillSmemBytes)) == cudaSuccess &&
+                                 static_cast<int>(jxg::kFillRunSmemBytes)) == cudaSuccess &&
             cudaFuncSetAttribute(jxg::k_fill_plan, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(jxg::kFillSmemBytes)) == cudaSuccess &&
             cudaFuncSetAttribute(jxg::k_fill_plan_batch,
@@ -943,7 +949,7 @@ void jxg_context_destroy(void* ctx) {
                          &c->tokens, &c->hist, &c->stats,
                          &c->group_offsets, &c->plan, &c->total, &c->op_in, &c->op_out,
                          &c->alpha, &c->alpha_peak, &c->alpha_zero, &c->fill_flags,
-                         &c->fill_deps, &c->fill_queue, &c->group_wide, &c->packed,
+                         &c->fill_deps, &c->fill_queue, &c->fill_masks, &c->group_wide, &c->packed,
                          &c->packed_offs, &c->tok_status})
     if (b->ptr) cudaFree(b->ptr);
   for (jxg::HostBuf* b : {&c->plan_host, &c->pixels_host, &c->async_slot})
