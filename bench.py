@@ -424,7 +424,7 @@ def run_c5(ctxs, streams, flush, args, dev) -> dict:
     size = 8192
     img = synthetic.config5_image(size)
     d_img = torch.from_numpy(img.reshape(-1).view(np.uint8)).to(dev)
-    cfg = J.EncodeConfig(speed=J.Speed.ULTRA_FAST).with_quality(85)
+    cfg = J.EncodeConfig(speed=J.Speed.ULTRA_FAST, transfer=J.TransferFunction.LINEAR).with_quality(85)
 
     def frame(k):
         ctxs[k % 2].run_device(d_img.data_ptr(), size, size, 3, 16, cfg)

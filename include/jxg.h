@@ -46,15 +46,25 @@ extern "C" {
 
 /* The part of `EncodeConfig` (src/encode_image.rs:326-588) the front end
  * reads: distance (set it from a quality with jxg_distance_from_quality, as
- * `with_quality`, src/encode_image.rs:986, does), speed and the host thread
- * budget (`with_num_threads`, :1251).  The device result never depends on
- * num_threads. */
+ * `with_quality`, src/encode_image.rs:986, does), speed, the host thread
+ * budget (`with_num_threads`, :1251) and the samples' transfer function
+ * (`color_encoding.transfer`, an H.273 transfer-characteristics code as
+ * TransferFunction, src/color_encoding.rs:99-160).  The device result never
+ * depends on num_threads.  `transfer` 0 is the default encoding's sRGB
+ * (13); 1, 6, 14, 15 decode as BT.709, 4 BT.470M, 5 BT.470BG, 7 SMPTE 240,
+ * 8 linear, 17 SMPTE 428, and 2, 9-13 as sRGB (select_transfer,
+ * src/color.rs:201-222); PQ (16) and HLG (18) return JXG_ERR_UNSUPPORTED. */
 typedef struct jxg_config {
   float distance;
   int32_t speed;
   int32_t num_threads;
-  int32_t reserved[5];
+  int32_t transfer;
+  int32_t reserved[4];
 } jxg_config;
+
+#define JXG_TRANSFER_SRGB 13
+#define JXG_TRANSFER_LINEAR 8
+#define JXG_TRANSFER_BT709 1
 
 /* Frame geometry (`ImageDim`, src/frame.rs:84-124). */
 typedef struct jxg_frame_info {
@@ -164,8 +174,11 @@ int32_t jxg_validate_input(uint64_t width, uint64_t height, int32_t channels, in
  * near-transparent fringe is cleared (src/alpha_fringe.rs:78), zero-alpha
  * colours are filled from their neighbours (src/invisible.rs:34) and a
  * non-constant alpha scales each block's quant field by its peak alpha
- * (src/adaptive_quant.rs:953-1070)), `bits` 8 (sRGB, as encode_image) or
- * 16 (linear, as encode_image_16bit with a linear transfer). */
+ * (src/adaptive_quant.rs:953-1070)), `bits` 8 (bytes, as encode_image) or
+ * 10, 12, 16 (16-bit words, as encode_image_10bit / _12bit / _16bit and
+ * their _with_alpha forms, src/encode_image.rs:3752-3850, 4230: samples
+ * above the largest code decode to 0, alpha is capped to it), decoded by
+ * config->transfer (sRGB primaries). */
 
 /* Host input: copies the pixels in, runs, and waits for the device. */
 int32_t jxg_frontend_run(void* ctx, const void* pixels, uint64_t width, uint64_t height,

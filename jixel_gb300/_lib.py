@@ -57,7 +57,8 @@ class Config(ctypes.Structure):
         ("distance", ctypes.c_float),
         ("speed", ctypes.c_int32),
         ("num_threads", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 5),
+        ("transfer", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 4),
     ]
 
 

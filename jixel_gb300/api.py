@@ -29,6 +29,27 @@ class Speed(enum.IntEnum):
     EXTRA_SLOW = 6
 
 
+class TransferFunction(enum.IntEnum):
+    """`TransferFunction` (src/color_encoding.rs:99-160): H.273 codes."""
+    BT709 = 1
+    UNSPECIFIED = 2
+    BT470M = 4
+    BT470BG = 5
+    BT601 = 6
+    SMPTE240 = 7
+    LINEAR = 8
+    LOG100 = 9
+    LOG100_SQRT10 = 10
+    IEC61966 = 11
+    BT1361 = 12
+    SRGB = 13
+    BT2020_10BIT = 14
+    BT2020_12BIT = 15
+    SMPTE2084 = 16
+    SMPTE428 = 17
+    HLG = 18
+
+
 _ERRORS = {
     1: "EmptyImage", 2: "InputSizeMismatch", 3: "AlphaSizeMismatch", 4: "InvalidDistance",
     5: "QualityIsNaN", 6: "DimensionTooLarge", 7: "AllocationFailed", 8: "Unsupported",
@@ -55,10 +76,23 @@ def distance_from_quality(quality: float) -> float:
 
 @dataclass
 class EncodeConfig:
-    """The part of `EncodeConfig` (src/encode_image.rs:326-588) the front end reads."""
+    """The part of `EncodeConfig` (src/encode_image.rs:326-588) the front end
+    reads.  `transfer` is `color_encoding.transfer` (default sRGB);
+    `bits_per_sample` picks the entry point for uint16 samples, as
+    encode_image_10bit / _12bit / _16bit do (0: 8 for uint8, 16 for uint16)."""
     distance: float = 1.0
     speed: Speed = Speed.FAST
     num_threads: int = field(default_factory=lambda: os.cpu_count() or 1)
+    transfer: TransferFunction = TransferFunction.SRGB
+    bits_per_sample: int = 0
+
+    def with_transfer(self, transfer: TransferFunction) -> "EncodeConfig":
+        self.transfer = TransferFunction(transfer)
+        return self
+
+    def with_bits_per_sample(self, bits: int) -> "EncodeConfig":
+        self.bits_per_sample = int(bits)
+        return self
 
     def with_quality(self, quality: float) -> "EncodeConfig":
         self.distance = distance_from_quality(quality)
@@ -81,6 +115,7 @@ class EncodeConfig:
         c.distance = self.distance
         c.speed = int(self.speed)
         c.num_threads = self.num_threads
+        c.transfer = int(self.transfer)
         return c
 
 
@@ -136,13 +171,16 @@ class FrontendResult:
     packed_offsets: np.ndarray | None = None  # (groups + 1,) u64 word offsets
 
 
-def _pixels_kind(pixels: np.ndarray) -> tuple[int, int]:
+def _pixels_kind(pixels: np.ndarray, config: "EncodeConfig | None" = None) -> tuple[int, int]:
     if pixels.ndim != 3 or pixels.shape[2] not in (3, 4):
         raise EncodeError(9, f"expected (h, w, 3|4) samples, got {pixels.shape}")
+    want = config.bits_per_sample if config is not None else 0
     if pixels.dtype == np.uint8:
+        if want not in (0, 8):
+            raise EncodeError(10, f"{want}-bit samples need uint16 words")
         return pixels.shape[2], 8
     if pixels.dtype == np.uint16:
-        return pixels.shape[2], 16
+        return pixels.shape[2], want if want else 16
     raise EncodeError(10, f"unsupported sample type {pixels.dtype}")
 
 
@@ -263,7 +301,7 @@ class FrontendContext:
     def run(self, pixels: np.ndarray, config: EncodeConfig):
         """Host input: copy in, run, wait (jxg_frontend_run)."""
         pixels = np.ascontiguousarray(pixels)
-        ch, bits = _pixels_kind(pixels)
+        ch, bits = _pixels_kind(pixels, config)
         h, w = pixels.shape[:2]
         cfg = config._c()
         self._check(self._lib.jxg_frontend_run(self._ctx, pixels.ctypes.data, w, h, ch, bits,
@@ -291,7 +329,7 @@ class FrontendContext:
     def enqueue(self, pixels: np.ndarray, config: EncodeConfig, out: "PinnedOutputs"):
         """Asynchronous front end (jxg_frontend_enqueue): `pixels` and `out`
         should be pinned; call wait() before reading `out`."""
-        ch, bits = _pixels_kind(pixels)
+        ch, bits = _pixels_kind(pixels, config)
         h, w = pixels.shape[:2]
         cfg = config._c()
         self._check(self._lib.jxg_frontend_enqueue(self._ctx, pixels.ctypes.data, w, h, ch, bits,
@@ -511,7 +549,7 @@ class FrontendBatch:
 
     def add(self, pixels: np.ndarray, config: EncodeConfig) -> int:
         pixels = np.ascontiguousarray(pixels)
-        ch, bits = _pixels_kind(pixels)
+        ch, bits = _pixels_kind(pixels, config)
         h, w = pixels.shape[:2]
         return self._add(pixels.ctypes.data, w, h, ch, bits, config, pixels)
 

@@ -309,6 +309,70 @@ void srgb_to_linear_table(float out[256]) {
   }
 }
 
+namespace {
+
+// The transfer functions of integer samples (src/color.rs:44-199), on the
+// sample over the largest code value, in f32 with the C library's powf.
+float unit_clamp(float v) { return v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v); }
+float decode_srgb(float v) {  // srgb_to_linear_f32
+  v = unit_clamp(v);
+  return v <= 0.04045f ? v / 12.92f : ::powf((v + 0.055f) / 1.055f, 2.4f);
+}
+float decode_linear(float v) { return unit_clamp(v); }
+float decode_bt709(float v) {
+  v = unit_clamp(v);
+  const float alpha = 1.0992968f, beta = 0.01805397f;
+  return v < 4.5f * beta ? v / 4.5f : ::powf((v + alpha - 1.0f) / alpha, 1.0f / 0.45f);
+}
+float decode_bt470m(float v) { return ::powf(unit_clamp(v), 2.2f); }
+float decode_bt470bg(float v) { return ::powf(unit_clamp(v), 2.8f); }
+float decode_smpte240(float v) {
+  v = unit_clamp(v);
+  return v < 0.0912f ? v / 4.0f : ::powf((v + 0.1115f) / 1.1115f, 1.0f / 0.45f);
+}
+float decode_smpte428(float v) { return ::powf(unit_clamp(v), 2.6f); }
+
+}  // namespace
+
+namespace {
+
+// select_transfer, src/color.rs:201-222
+int select_decode(int transfer, float (**decode)(float)) {
+  switch (transfer) {
+    case 1: case 6: case 14: case 15: *decode = decode_bt709; return 0;
+    case 4: *decode = decode_bt470m; return 0;
+    case 5: *decode = decode_bt470bg; return 0;
+    case 7: *decode = decode_smpte240; return 0;
+    case 8: *decode = decode_linear; return 0;
+    case 17: *decode = decode_smpte428; return 0;
+    case 0: case 2: case 9: case 10: case 11: case 12: case 13: *decode = decode_srgb; return 0;
+    case 16: case 18: return 1;  // PQ and HLG: display model not built
+    default: return 2;
+  }
+}
+
+}  // namespace
+
+int transfer_status(int transfer) {
+  float (*decode)(float) = nullptr;
+  return select_decode(transfer, &decode);
+}
+
+int transfer_table(int bits, int transfer, float* out) {
+  if (bits != 8 && bits != 10 && bits != 12 && bits != 16) return 2;
+  float (*decode)(float) = nullptr;
+  const int st = select_decode(transfer, &decode);
+  if (st) return st;
+  if (bits == 8 && (transfer == 0 || transfer == 13)) {
+    srgb_to_linear_table(out);
+    return 0;
+  }
+  const int size = 1 << bits, domain = bits == 8 ? 256 : 65536;
+  const float max = static_cast<float>(size - 1);
+  for (int v = 0; v < domain; ++v) out[v] = v < size ? decode(static_cast<float>(v) / max) : 0.0f;
+  return 0;
+}
+
 void exp2_table(float out[64]) {
   // fast_exp2's table: 2^((i - 32) / 64) rounded to f32
   for (int i = 0; i < 64; ++i) out[i] = static_cast<float>(std::exp2((i - 32) / 64.0));

@@ -66,6 +66,14 @@ float distance_from_quality(float quality);
 int32_t epf_sharpness_id(float distance, bool screen_content);
 bool is_screen_content(uint64_t constant_blocks, uint64_t width, uint64_t height);
 void srgb_to_linear_table(float out[256]);
+// TransferLut::build (src/color.rs:297-333) for integer samples of `bits`
+// 8, 10, 12 or 16 and an H.273 transfer code (0 = sRGB, the default
+// encoding): 256 entries for 8-bit samples, else 65536, codes above the
+// largest decoding to 0.  Returns 0, 1 for a transfer the front end does
+// not take (PQ, HLG), 2 for an invalid depth or code.
+int transfer_table(int bits, int transfer, float* out);
+// The same status for a transfer code alone, without building the table.
+int transfer_status(int transfer);
 void exp2_table(float out[64]);
 // libjxl natural 8x8 order: scan position -> raw coefficient index.
 void natural_order_8x8(uint8_t scan[64], uint8_t position[64]);

@@ -56,6 +56,9 @@ inline int64_t fill_tiles(uint64_t w, uint64_t h) {
 
 }  // namespace
 
+// Bytes of one sample: 8-bit samples, or 10/12/16-bit ones in 16-bit words.
+inline size_t sample_bytes(int32_t bits) { return bits > 8 ? 2 : 1; }
+
 // One image of a pass as the caller describes it.
 struct PassImage {
   const void* pixels;
@@ -98,7 +101,9 @@ struct Context {
   cudaStream_t stream = nullptr;
   std::string last_error;
   // constant tables
-  float* d_lut = nullptr;       // sRGB -> linear, 256
+  // transfer tables on the device, one per (bits, transfer) in use:
+  // 256 floats for 8-bit samples, 65536 otherwise
+  std::map<int, float*> luts;
   float* d_exp2 = nullptr;      // fast_exp2 table, 64
   uint8_t* d_pos = nullptr;     // natural 8x8 order, raw index -> scan position
   // pass buffers (grown, never shrunk)
@@ -156,6 +161,25 @@ namespace {
 int fail(Context* c, int code, const std::string& msg) {
   if (c) c->last_error = msg;
   return code;
+}
+
+// The device transfer table of (bits, transfer), built and uploaded on
+// first use and kept for the context's life; null when it cannot be made.
+float* transfer_lut(Context* c, int bits, int transfer) {
+  const int key = (bits << 8) | (transfer & 0xff);
+  const auto it = c->luts.find(key);
+  if (it != c->luts.end()) return it->second;
+  std::vector<float> host(65536);
+  if (transfer_table(bits, transfer, host.data()) != 0) return nullptr;
+  const size_t bytes = (bits == 8 ? 256 : 65536) * sizeof(float);
+  float* d = nullptr;
+  if (cudaMalloc(&d, bytes) != cudaSuccess) return nullptr;
+  if (cudaMemcpy(d, host.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(d);
+    return nullptr;
+  }
+  c->luts[key] = d;
+  return d;
 }
 
 #define JXG_CUDA(ctx, call)                                                                    \
@@ -278,7 +302,11 @@ int validate(Context* c, const void* pixels, uint64_t w, uint64_t h, int32_t cha
   if (w > kMaxDimension || h > kMaxDimension)
     return fail(c, JXG_ERR_DIMENSION_TOO_LARGE, "dimension too large");
   if (channels != 3 && channels != 4) return fail(c, JXG_ERR_BAD_CHANNEL_COUNT, "channels");
-  if (bits != 8 && bits != 16) return fail(c, JXG_ERR_BAD_BIT_DEPTH, "bits");
+  if (bits != 8 && bits != 10 && bits != 12 && bits != 16)
+    return fail(c, JXG_ERR_BAD_BIT_DEPTH, "bits");
+  const int tf = transfer_status(cfg->transfer);
+  if (tf == 1) return fail(c, JXG_ERR_UNSUPPORTED, "PQ and HLG transfers are not built");
+  if (tf != 0) return fail(c, JXG_ERR_INVALID_ARGUMENT, "transfer");
   if (!std::isfinite(cfg->distance) || cfg->distance <= 0.0f)
     return fail(c, JXG_ERR_INVALID_DISTANCE, "distance must be positive and finite");
   if (cfg->speed != JXG_SPEED_ULTRAFAST)
@@ -290,7 +318,7 @@ int validate(Context* c, const void* pixels, uint64_t w, uint64_t h, int32_t cha
 
 // Device buffers of 16-bit samples must be 2-byte aligned.
 int check_device_pixels(Context* c, const void* pixels, int32_t bits) {
-  if (bits == 16 && (reinterpret_cast<uintptr_t>(pixels) & 1))
+  if (bits > 8 && (reinterpret_cast<uintptr_t>(pixels) & 1))
     return fail(c, JXG_ERR_INVALID_ARGUMENT, "16-bit device pixels must be 2-byte aligned");
   return JXG_OK;
 }
@@ -322,7 +350,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     const int64_t px = static_cast<int64_t>(im.width * im.height);
     L.plane = (px + 63) / 64 * 64;
     L.pix_off = pix;
-    pix += align_up(static_cast<size_t>(px) * im.channels * (im.bits / 8), 256);
+    pix += align_up(static_cast<size_t>(px) * im.channels * sample_bytes(im.bits), 256);
     L.xyb_off = xyb;
     xyb += 3 * static_cast<size_t>(L.plane);
     L.block_off = blocks;
@@ -360,7 +388,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
   {
     const FrameLayout& last = c->layouts.back();
     c->pixel_bytes = last.pix_off + static_cast<size_t>(last.width * last.height) *
-                                        imgs[n - 1].channels * (imgs[n - 1].bits / 8);
+                                        imgs[n - 1].channels * sample_bytes(imgs[n - 1].bits);
   }
   c->frames_bytes = align_up(sizeof(Frame) * n, 256);
   const size_t prefix_bytes = align_up(sizeof(int64_t) * (n + 1), 256);
@@ -432,6 +460,9 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     f.pixels = pixels_on_device ? im.pixels : static_cast<const char*>(c->pixels.ptr) + L.pix_off;
     f.channels = im.channels;
     f.bits = im.bits;
+    f.transfer = im.config.transfer;
+    f.lut = transfer_lut(c, im.bits, im.config.transfer);
+    if (!f.lut) return fail(c, JXG_ERR_ALLOCATION_FAILED, "transfer table");
     f.xyb = static_cast<float*>(c->xyb.ptr) + L.xyb_off;
     f.qf = static_cast<uint8_t*>(c->qf.ptr) + L.block_off;
     f.ytox = static_cast<int8_t*>(c->ytox.ptr) + L.tile_off;
@@ -450,7 +481,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
       f.alpha = static_cast<uint16_t*>(c->alpha.ptr) + L.alpha_off;
       f.alpha_peak = static_cast<uint16_t*>(c->alpha_peak.ptr) + L.alpha_block_off;
       f.alpha_zero = static_cast<uint8_t*>(c->alpha_zero.ptr) + L.alpha_block_off;
-      f.alpha_full = im.bits == 8 ? 255 : 65535;
+      f.alpha_full = (1 << im.bits) - 1;
     }
     const int64_t px = static_cast<int64_t>(L.width * L.height);
     pre_xyb[i] = ax;
@@ -501,7 +532,7 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
     for (int i = 0; i < n; ++i) {
       const FrameLayout& L = c->layouts[i];
       const size_t bytes =
-          static_cast<size_t>(L.width * L.height) * imgs[i].channels * (imgs[i].bits / 8);
+          static_cast<size_t>(L.width * L.height) * imgs[i].channels * sample_bytes(imgs[i].bits);
       JXG_CUDA(c, cudaMemcpyAsync(static_cast<char*>(c->pixels.ptr) + L.pix_off, imgs[i].pixels,
                                   bytes, cudaMemcpyHostToDevice, s));
     }
@@ -534,7 +565,7 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
   int st;
   if (single) {
     if ((st = launch(c, "k_xyb", timed, [&] {
-           k_xyb<<<static_cast<unsigned>(c->xyb_chunks), 256, 0, s>>>(f0, c->d_lut);
+           k_xyb<<<static_cast<unsigned>(c->xyb_chunks), 256, 0, s>>>(f0);
          })))
       return st;
     if (c->alpha_tiles &&
@@ -563,8 +594,7 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
       return st;
   } else {
     if ((st = launch(c, "k_xyb_batch", timed, [&] {
-           k_xyb_batch<<<static_cast<unsigned>(c->xyb_chunks), 256, 0, s>>>(frames, pre_xyb, n,
-                                                                            c->d_lut);
+           k_xyb_batch<<<static_cast<unsigned>(c->xyb_chunks), 256, 0, s>>>(frames, pre_xyb, n);
          })))
       return st;
     if (c->alpha_tiles &&
@@ -617,7 +647,7 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
 int stage_host_pixels(Context* c, const PassImage* imgs, int n) {
   for (int i = 0; i < n; ++i) {
     const FrameLayout& L = c->layouts[i];
-    const size_t bytes = static_cast<size_t>(L.width * L.height) * imgs[i].channels * (imgs[i].bits / 8);
+    const size_t bytes = static_cast<size_t>(L.width * L.height) * imgs[i].channels * sample_bytes(imgs[i].bits);
     std::memcpy(static_cast<char*>(c->pixels_host.ptr) + L.pix_off, imgs[i].pixels, bytes);
   }
   return JXG_OK;
@@ -902,18 +932,16 @@ int32_t jxg_context_create(int32_t device, void** out_ctx) {
   if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
       c->num_sms <= 0)
     c->num_sms = 1;
-  float lut[256], e2[64];
+  float e2[64];
   uint8_t scan[64], pos[64];
-  jxg::srgb_to_linear_table(lut);
   jxg::exp2_table(e2);
   jxg::natural_order_8x8(scan, pos);
   bool ok = true;
   for (auto& e : c->plan_uploaded)
     ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
-  ok = ok && cudaMalloc(&c->d_lut, sizeof(lut)) == cudaSuccess &&
+  ok = ok && jxg::transfer_lut(c, 8, 0) != nullptr &&  // the default: 8-bit sRGB
             cudaMalloc(&c->d_exp2, sizeof(e2)) == cudaSuccess &&
             cudaMalloc(&c->d_pos, 64) == cudaSuccess &&
-            cudaMemcpy(c->d_lut, lut, sizeof(lut), cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(c->d_exp2, e2, sizeof(e2), cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(c->d_pos, pos, 64, cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaFuncSetAttribute(jxg::k_tile_quantize, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -954,7 +982,7 @@ void jxg_context_destroy(void* ctx) {
     if (b->ptr) cudaFree(b->ptr);
   for (jxg::HostBuf* b : {&c->plan_host, &c->pixels_host, &c->async_slot})
     if (b->ptr) cudaFreeHost(b->ptr);
-  cudaFree(c->d_lut);
+  for (auto& kv : c->luts) cudaFree(kv.second);
   cudaFree(c->d_exp2);
   cudaFree(c->d_pos);
   for (auto& p : c->pending) {

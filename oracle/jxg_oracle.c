@@ -383,6 +383,72 @@ void orc_srgb_lut(float* lut) {
   }
 }
 
+/* Transfer functions of integer samples (src/color.rs:44-222), as the
+ * H.273 transfer-characteristics codes of TransferFunction
+ * (src/color_encoding.rs:99-160).  Each takes the sample over the largest
+ * code value and returns linear light. */
+static float clamp01(float v) { return v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v); }
+/* srgb_to_linear_f32 (:44-52) */
+static float tf_srgb(float v) {
+  v = clamp01(v);
+  return v <= 0.04045f ? v / 12.92f : powf((v + 0.055f) / 1.055f, 2.4f);
+}
+/* linear_to_linear (:57-59) */
+static float tf_linear(float v) { return clamp01(v); }
+/* bt709_to_linear (:164-174) */
+static float tf_bt709(float v) {
+  v = clamp01(v);
+  const float alpha = 1.0992968f, beta = 0.01805397f;
+  return v < 4.5f * beta ? v / 4.5f : powf((v + alpha - 1.0f) / alpha, 1.0f / 0.45f);
+}
+/* bt470m_to_linear (:176-179), bt470bg_to_linear (:181-184),
+ * smpte428_to_linear (:196-199) */
+static float tf_bt470m(float v) { return powf(clamp01(v), 2.2f); }
+static float tf_bt470bg(float v) { return powf(clamp01(v), 2.8f); }
+static float tf_smpte428(float v) { return powf(clamp01(v), 2.6f); }
+/* smpte240_to_linear (:186-194) */
+static float tf_smpte240(float v) {
+  v = clamp01(v);
+  return v < 0.0912f ? v / 4.0f : powf((v + 0.1115f) / 1.1115f, 1.0f / 0.45f);
+}
+
+typedef float (*transfer_fn)(float);
+
+/* select_transfer (src/color.rs:201-222) for the codes the front end takes:
+ * 0 is the default encoding's sRGB (13); PQ (16) and HLG (18) need the
+ * display model and are not built (NULL); anything else is invalid. */
+static int select_transfer(int code, transfer_fn* fn) {
+  switch (code) {
+    case 1: case 6: case 14: case 15: *fn = tf_bt709; return 0;
+    case 4: *fn = tf_bt470m; return 0;
+    case 5: *fn = tf_bt470bg; return 0;
+    case 7: *fn = tf_smpte240; return 0;
+    case 8: *fn = tf_linear; return 0;
+    case 17: *fn = tf_smpte428; return 0;
+    case 0: case 2: case 9: case 10: case 11: case 12: case 13: *fn = tf_srgb; return 0;
+    case 16: case 18: *fn = NULL; return ORC_ERR_INPUT;
+    default: *fn = NULL; return ORC_ERR_INPUT;
+  }
+}
+
+/* TransferLut::build (src/color.rs:297-333) for `bits` 8, 10, 12 or 16:
+ * 256 entries for 8-bit samples, else 65536 (codes above the largest are 0).
+ * 8-bit sRGB takes the f64 table of srgb_to_linear_u8_ref. */
+int orc_transfer_lut(int bits, int transfer, float* lut) {
+  transfer_fn fn;
+  if (bits != 8 && bits != 10 && bits != 12 && bits != 16) return ORC_ERR_INPUT;
+  int st = select_transfer(transfer, &fn);
+  if (st) return st;
+  const int size = 1 << bits, domain = bits <= 8 ? 256 : 65536;
+  if (bits == 8 && (transfer == 13 || transfer == 0)) {
+    orc_srgb_lut(lut);
+    return 0;
+  }
+  const float max = (float)(size - 1);
+  for (int v = 0; v < domain; v++) lut[v] = v < size ? fn((float)v / max) : 0.0f;
+  return 0;
+}
+
 #define OPSIN_BIAS 0.0037930734f
 #define NEG_BIAS_CBRT (-0.1559542f)
 
@@ -437,15 +503,22 @@ static inline void rgb_to_xyb(const float m[9], float r, float g, float b, float
   *ob = tm2;
 }
 
-/* linearize_rgb (src/encode_image.rs:1498-1519) + to_xyb_in_place
- * (src/xyb.rs:439-470): RGB8 (3 or 4 channels, alpha ignored) or 16-bit
- * linear RGB (TransferLut::build with the Linear transfer,
- * src/color.rs:318-323: v / 65535 clamped to [0, 1]). */
-void orc_to_xyb(const void* pixels, int bytes_per_sample, int channels, size_t w, size_t h,
-                float* xyb) {
-  float lut[256];
+/* linearize_rgb (src/encode_image.rs:1498-1519) with the integer
+ * ColorTransform of sRGB primaries (transform_identity, src/color.rs:498-509:
+ * each sample through the transfer LUT) + to_xyb_in_place
+ * (src/xyb.rs:439-470).  8-bit samples, or 10/12/16-bit samples in 16-bit
+ * words; 3 or 4 channels, alpha ignored.  Returns 0, or ORC_ERR_INPUT for a
+ * depth or transfer the front end does not take. */
+int orc_to_xyb(const void* pixels, int bits, int transfer, int channels, size_t w, size_t h,
+               float* xyb) {
+  float* lut = (float*)malloc(65536 * sizeof(float));
+  if (!lut) return ORC_ERR_ALLOC;
+  int st = orc_transfer_lut(bits, transfer, lut);
+  if (st) {
+    free(lut);
+    return st;
+  }
   float m[9];
-  orc_srgb_lut(lut);
   opsin_matrix(m);
   size_t n = w * h;
 #ifdef _OPENMP
@@ -453,19 +526,21 @@ void orc_to_xyb(const void* pixels, int bytes_per_sample, int channels, size_t w
 #endif
   for (size_t i = 0; i < n; i++) {
     float r, g, b;
-    if (bytes_per_sample == 1) {
+    if (bits == 8) {
       const uint8_t* p = (const uint8_t*)pixels + i * (size_t)channels;
       r = lut[p[0]];
       g = lut[p[1]];
       b = lut[p[2]];
     } else {
       const uint16_t* p = (const uint16_t*)pixels + i * (size_t)channels;
-      r = clampf((float)p[0] / 65535.0f, 0.0f, 1.0f);
-      g = clampf((float)p[1] / 65535.0f, 0.0f, 1.0f);
-      b = clampf((float)p[2] / 65535.0f, 0.0f, 1.0f);
+      r = lut[p[0]];
+      g = lut[p[1]];
+      b = lut[p[2]];
     }
     rgb_to_xyb(m, r, g, b, &xyb[i], &xyb[n + i], &xyb[2 * n + i]);
   }
+  free(lut);
+  return 0;
 }
 
 /* ------------------------------------------------------------------ */
@@ -2250,8 +2325,10 @@ void orc_apply_alpha_factors(uint8_t* qf, const uint16_t* alpha, size_t w, size_
 typedef struct {
   /* inputs */
   const void* pixels;
-  int32_t bytes_per_sample; /* 1 = sRGB 8-bit, 2 = 16-bit linear */
+  int32_t bits;             /* 8, or 10 / 12 / 16 in 16-bit words */
   int32_t channels;         /* 3 or 4 (RGBA: lossy alpha, fill_invisible on) */
+  int32_t transfer;         /* H.273 transfer code; 0 = sRGB (the default encoding) */
+  int32_t pad_;
   uint64_t width, height;
   float distance;
   int32_t num_threads;
@@ -2402,7 +2479,7 @@ static void encode_ac_group(const orc_frame* f, const float* xyb, const float* m
 int orc_frontend(orc_frame* f) {
   size_t w = f->width, h = f->height;
   if (w == 0 || h == 0) return ORC_ERR_EMPTY;
-  if (!(f->bytes_per_sample == 1 || f->bytes_per_sample == 2)) return ORC_ERR_INPUT;
+  if (!(f->bits == 8 || f->bits == 10 || f->bits == 12 || f->bits == 16)) return ORC_ERR_INPUT;
   if (!(f->channels == 3 || f->channels == 4)) return ORC_ERR_INPUT;
   int st = orc_params_for(f->distance, &f->params);
   if (st) return st;
@@ -2426,18 +2503,23 @@ int orc_frontend(orc_frame* f) {
   int16_t* qdc = f->quant_dc ? f->quant_dc : (int16_t*)malloc(3 * nb * sizeof(int16_t));
   if (!xyb || !qf || !ytox || !ytob || !qdc) return ORC_ERR_ALLOC;
   double t0 = now_seconds();
-  orc_to_xyb(f->pixels, f->bytes_per_sample, f->channels, w, h, xyb);
+  st = orc_to_xyb(f->pixels, f->bits, f->transfer, f->channels, w, h, xyb);
+  if (st) return st;
   /* RGBA (encode_lossy_u8_alpha_arms, src/encode_image.rs:3639-3657, and
    * encode_high_depth_rgba :4290-4303): the alpha plane loses its fringe,
    * then the XYB planes their invisible colours (src/frame/encoder.rs:152) */
   uint16_t* alpha = NULL;
-  uint32_t alpha_max = f->bytes_per_sample == 1 ? 255u : 65535u;
+  /* the largest code value; high-depth alpha is capped to it
+   * (encode_high_depth_rgba, src/encode_image.rs:4270-4290) */
+  const uint32_t alpha_max = (1u << f->bits) - 1u;
   if (f->channels == 4) {
     alpha = f->alpha ? f->alpha : (uint16_t*)malloc(n * sizeof(uint16_t));
     if (!alpha) return ORC_ERR_ALLOC;
-    for (size_t i = 0; i < n; i++)
-      alpha[i] = f->bytes_per_sample == 1 ? ((const uint8_t*)f->pixels)[i * 4 + 3]
-                                          : ((const uint16_t*)f->pixels)[i * 4 + 3];
+    for (size_t i = 0; i < n; i++) {
+      const uint32_t a = f->bits == 8 ? ((const uint8_t*)f->pixels)[i * 4 + 3]
+                                      : ((const uint16_t*)f->pixels)[i * 4 + 3];
+      alpha[i] = (uint16_t)(a < alpha_max ? a : alpha_max);
+    }
     orc_alpha_fringe_clear(alpha, w, h, alpha_max);
     orc_fill_invisible(xyb, alpha, w, h);
   }

@@ -39,8 +39,10 @@ class OrcParams(ctypes.Structure):
 class OrcFrame(ctypes.Structure):
     _fields_ = [
         ("pixels", ctypes.c_void_p),
-        ("bytes_per_sample", ctypes.c_int32),
+        ("bits", ctypes.c_int32),
         ("channels", ctypes.c_int32),
+        ("transfer", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
         ("width", ctypes.c_uint64),
         ("height", ctypes.c_uint64),
         ("distance", ctypes.c_float),
@@ -178,11 +180,15 @@ class OracleFrame:
 
 
 def frontend(pixels: np.ndarray, distance: float, num_threads: int = 0,
-             keep_coeffs: bool = True) -> OracleFrame:
-    """Run the oracle on an (h, w, c) uint8 (sRGB) or uint16 (linear) image."""
+             keep_coeffs: bool = True, bits: int | None = None,
+             transfer: int = 0) -> OracleFrame:
+    """Run the oracle on an (h, w, c) uint8 or uint16 image: `bits` 8, or
+    10 / 12 / 16 for uint16 samples (default: the sample type's), `transfer`
+    an H.273 transfer code (0: sRGB, the default encoding; 8: linear)."""
     pixels = np.ascontiguousarray(pixels)
     h, w, ch = pixels.shape
-    bps = 1 if pixels.dtype == np.uint8 else 2
+    if bits is None:
+        bits = 8 if pixels.dtype == np.uint8 else 16
     xb, yb = (w + 7) // 8, (h + 7) // 8
     tx, ty = (xb + 7) // 8, (yb + 7) // 8
     ng = ((w + 255) // 256) * ((h + 255) // 256)
@@ -200,7 +206,8 @@ def frontend(pixels: np.ndarray, distance: float, num_threads: int = 0,
     alpha = np.zeros((h, w), np.uint16) if ch == 4 else None
     f = OrcFrame()
     f.pixels = pixels.ctypes.data
-    f.bytes_per_sample = bps
+    f.bits = bits
+    f.transfer = transfer
     f.channels = ch
     f.width = w
     f.height = h
@@ -419,3 +426,14 @@ def dct4_2d(block: np.ndarray) -> np.ndarray:
     fn = {16: lib().orc_dct4x4_2d, 32: lib().orc_dct4x8_2d}[b.size]
     fn(b.ctypes.data_as(ctypes.c_void_p), out.ctypes.data_as(ctypes.c_void_p))
     return out
+
+
+def transfer_lut(bits: int, transfer: int) -> np.ndarray:
+    """TransferLut::build (src/color.rs:297-333): 256 entries for 8-bit
+    samples, 65536 otherwise."""
+    out = np.zeros(65536, np.float32)
+    st = lib().orc_transfer_lut(ctypes.c_int(bits), ctypes.c_int(transfer),
+                                out.ctypes.data_as(ctypes.c_void_p))
+    if st:
+        raise ValueError(f"transfer {transfer} at {bits} bits: status {st}")
+    return out[:256] if bits == 8 else out

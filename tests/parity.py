@@ -28,3 +28,16 @@ def assert_same(got, want, check_xyb=True):
     assert np.all(got.ac_strategy == 1)
     if getattr(want, "alpha", None) is not None and getattr(got, "alpha", None) is not None:
         assert np.array_equal(got.alpha, want.alpha), "alpha"
+
+
+def high_depth_image(w, h, seed, bits, alpha=False):
+    """Synthetic content scaled to `bits` in uint16 words, plus a few samples
+    above the largest code (they decode to 0; alpha above it is capped)."""
+    from jixel_gb300 import synthetic
+    img = synthetic.generate(w, h, seed, sixteen_bit=True, alpha=alpha).astype(np.uint32)
+    img = (img * ((1 << bits) - 1) // 65535).astype(np.uint16)
+    if bits < 16:
+        rng = np.random.default_rng(seed)
+        ys, xs = rng.integers(0, h, 40), rng.integers(0, w, 40)
+        img[ys, xs, rng.integers(0, img.shape[2], 40)] = (1 << bits) + 7
+    return img

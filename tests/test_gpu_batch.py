@@ -152,3 +152,26 @@ def test_config3_subset_matches_one_frame_passes(ctx):
             assert r.params == s.params, i
     finally:
         b.close()
+
+
+def test_batch_mixes_depths_and_transfers(ctx):
+    # one pass over frames of different depths and transfer functions: each
+    # frame reads its own transfer table
+    from tests.parity import high_depth_image
+    TF = J.TransferFunction
+    cases = [(synthetic.generate(90, 60, 900), 8, TF.SRGB),
+             (high_depth_image(70, 50, 901, 10), 10, TF.SRGB),
+             (high_depth_image(64, 64, 902, 16), 16, TF.LINEAR),
+             (high_depth_image(50, 70, 903, 12, alpha=True), 12, TF.BT709),
+             (synthetic.generate(40, 30, 904), 8, TF.BT709)]
+    b = ctx.batch()
+    try:
+        for img, bits, tf in cases:
+            b.add(img, J.EncodeConfig(distance=1.0, speed=J.Speed.ULTRA_FAST, transfer=tf,
+                                      bits_per_sample=bits))
+        b.run()
+        for i, (img, bits, tf) in enumerate(cases):
+            assert_same(b.result(i), O.frontend(img, 1.0, bits=bits, transfer=int(tf)),
+                        check_xyb=False)
+    finally:
+        b.close()

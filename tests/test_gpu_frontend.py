@@ -10,7 +10,7 @@ import pytest
 import jixel_gb300 as J
 from jixel_gb300 import synthetic
 from oracle import oracle as O
-from tests.parity import assert_same
+from tests.parity import assert_same, high_depth_image as _high_depth
 
 pytestmark = pytest.mark.gpu
 
@@ -22,13 +22,14 @@ def ctx():
     c.close()
 
 
-def ultrafast(distance):
-    return J.EncodeConfig(distance=distance, speed=J.Speed.ULTRA_FAST)
+def ultrafast(distance, transfer=J.TransferFunction.SRGB, bits=0):
+    return J.EncodeConfig(distance=distance, speed=J.Speed.ULTRA_FAST, transfer=transfer,
+                          bits_per_sample=bits)
 
 
-def compare(ctx, img, distance, check_xyb=True):
-    want = O.frontend(img, distance)
-    got = ctx.frontend(img, ultrafast(distance), xyb=check_xyb)
+def compare(ctx, img, distance, check_xyb=True, transfer=J.TransferFunction.SRGB, bits=0):
+    want = O.frontend(img, distance, bits=bits or None, transfer=int(transfer))
+    got = ctx.frontend(img, ultrafast(distance, transfer, bits), xyb=check_xyb)
     assert_same(got, want, check_xyb)
     return got, want
 
@@ -199,7 +200,8 @@ def test_8192_square_rgb16_invariants(ctx):
     # parity on a 2048x2048 crop
     img = synthetic.config5_image()
     d = J.distance_from_quality(85)
-    got = ctx.frontend(img, ultrafast(d), coefficients=False)
+    lin = J.TransferFunction.LINEAR
+    got = ctx.frontend(img, ultrafast(d, lin), coefficients=False)
     fi = J.frame_info(8192, 8192)
     assert fi.num_groups == 1024
     ntok = got.tokens.shape[0]
@@ -210,4 +212,42 @@ def test_8192_square_rgb16_invariants(ctx):
     assert int((got.tokens[:, 1] != 0).sum()) >= int(got.num_nzeros.astype(np.int64).sum())
     assert got.quant_field.min() >= 1 and got.tokens[:, 0].max() < 14850
     crop = np.ascontiguousarray(img[2048:4096, 4096:6144])
-    compare(ctx, crop, d, check_xyb=False)
+    compare(ctx, crop, d, check_xyb=False, transfer=lin)
+
+
+TF = J.TransferFunction
+
+
+@pytest.mark.parametrize("bits,transfer", [
+    (10, TF.SRGB), (12, TF.SRGB), (16, TF.SRGB), (10, TF.LINEAR), (16, TF.LINEAR),
+    (12, TF.BT709), (16, TF.BT470M), (10, TF.BT470BG), (16, TF.SMPTE240), (12, TF.SMPTE428),
+    (10, TF.BT2020_10BIT), (16, TF.UNSPECIFIED)])
+def test_high_depth_transfers(ctx, bits, transfer):
+    # encode_image_10bit / _12bit / _16bit with color_encoding.transfer:
+    # every sample through TransferLut::build's table
+    compare(ctx, _high_depth(150, 90, 40 + bits, bits), 1.0, transfer=transfer, bits=bits)
+
+
+@pytest.mark.parametrize("bits", [10, 12])
+def test_high_depth_alpha(ctx, bits):
+    # encode_image_with_alpha_10bit / _12bit: alpha capped to the largest
+    # code, then the fringe, fill and factors at that full scale
+    compare(ctx, _high_depth(140, 100, 60 + bits, bits, alpha=True), 1.0, bits=bits)
+
+
+@pytest.mark.parametrize("transfer", [TF.BT709, TF.LINEAR, TF.SMPTE428])
+def test_eight_bit_with_other_transfers(ctx, transfer):
+    # 8-bit samples outside the sRGB default decode with the f32 formula
+    compare(ctx, synthetic.generate(120, 80, 70), 1.0, transfer=transfer)
+
+
+def test_unsupported_transfers_and_depths(ctx):
+    img = np.zeros((8, 8, 3), np.uint16)
+    for tf, variant in ((TF.SMPTE2084, "Unsupported"), (TF.HLG, "Unsupported")):
+        with pytest.raises(J.EncodeError) as e:
+            ctx.run(img, ultrafast(1.0, tf))
+        assert e.value.variant == variant
+    with pytest.raises(J.EncodeError) as e:
+        ctx.run(img, ultrafast(1.0, bits=9))
+    assert e.value.variant == "BadBitDepth"
+    compare(ctx, synthetic.generate(40, 40, 6), 1.0)

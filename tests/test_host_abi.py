@@ -52,7 +52,7 @@ def test_frame_info_matches_image_dim():
     ((5, 0, 3, 8), "EmptyImage"),
     ((1 << 30, 1, 3, 8), "DimensionTooLarge"),
     ((8, 8, 2, 8), "BadChannelCount"),
-    ((8, 8, 3, 12), "BadBitDepth"),
+    ((8, 8, 3, 11), "BadBitDepth"),
 ])
 def test_input_validation(args, variant):
     cfg = J.EncodeConfig(distance=1.0, speed=J.Speed.ULTRA_FAST)
@@ -75,3 +75,26 @@ def test_unbuilt_speed_tiers_are_unsupported():
             J.api.validate_input(8, 8, 3, 8, J.EncodeConfig(distance=1.0, speed=s))
         assert e.value.variant == "Unsupported"
     J.api.validate_input(8, 8, 3, 8, J.EncodeConfig(distance=1.0, speed=J.Speed.ULTRA_FAST))
+
+
+def test_transfer_and_depth_validation():
+    # the H.273 codes select_transfer takes; PQ and HLG need the display
+    # model, which is not built; 9-bit samples are no entry point's
+    TF = J.TransferFunction
+    ok = J.EncodeConfig(distance=1.0, speed=J.Speed.ULTRA_FAST)
+    for bits in (8, 10, 12, 16):
+        for tf in (TF.SRGB, TF.LINEAR, TF.BT709, TF.BT470M, TF.BT470BG, TF.SMPTE240, TF.SMPTE428,
+                   TF.UNSPECIFIED, TF.BT2020_12BIT):
+            J.api.validate_input(8, 8, 3, bits, ok.with_transfer(tf))
+    for tf in (TF.SMPTE2084, TF.HLG):
+        with pytest.raises(J.EncodeError) as e:
+            J.api.validate_input(8, 8, 3, 16, ok.with_transfer(tf))
+        assert e.value.variant == "Unsupported"
+    bad = J.EncodeConfig(distance=1.0, speed=J.Speed.ULTRA_FAST)
+    bad.transfer = 3  # reserved code
+    with pytest.raises(J.EncodeError) as e:
+        J.api.validate_input(8, 8, 3, 8, bad)
+    assert e.value.variant == "InvalidArgument"
+    with pytest.raises(J.EncodeError) as e:
+        J.api.validate_input(8, 8, 3, 9, J.EncodeConfig(distance=1.0, speed=J.Speed.ULTRA_FAST))
+    assert e.value.variant == "BadBitDepth"

@@ -629,3 +629,62 @@ def test_large_dct_cosine_basis(name):
         want[index] = (1.0 if u == 0 else np.float32(math.sqrt(0.5))) * (
             1.0 if v == 0 else np.float32(math.sqrt(0.5)))
         assert np.abs(got - want).max() < 2e-6, (name, u, v, np.abs(got - want).max())
+
+
+def test_transfer_tables_follow_transfer_lut_build():
+    # TransferLut::build (src/color.rs:297-333): 8-bit sRGB is the f64
+    # table; other depths decode v / max in f32 over a 65536-entry domain,
+    # codes above the largest decoding to 0
+    s8 = O.transfer_lut(8, 13)
+    assert np.array_equal(s8, O.transfer_lut(8, 0))
+    ref = np.zeros(256, np.float32)
+    O.lib().orc_srgb_lut(ref.ctypes.data_as(__import__("ctypes").c_void_p))
+    assert np.array_equal(s8, ref)
+    for bits in (10, 12, 16):
+        mx = (1 << bits) - 1
+        v = np.arange(mx + 1, dtype=np.float64) / mx
+        f64 = {  # the formulas of src/color.rs:44-199 in float64
+            13: np.where(v <= 0.04045, v / 12.92, ((v + 0.055) / 1.055) ** 2.4),
+            8: v,
+            1: np.where(v < 4.5 * 0.01805397, v / 4.5, ((v + 0.0992968) / 1.0992968) ** (1 / 0.45)),
+            4: v ** 2.2, 5: v ** 2.8, 17: v ** 2.6,
+            7: np.where(v < 0.0912, v / 4.0, ((v + 0.1115) / 1.1115) ** (1 / 0.45)),
+        }
+        for tf, want in f64.items():
+            t = O.transfer_lut(bits, tf)
+            assert t.size == 65536 and t[0] == 0.0 and abs(float(t[mx]) - 1.0) < 1e-6, (bits, tf)
+            assert np.abs(t[: mx + 1] - want).max() < 2e-6, (bits, tf)
+            assert not np.any(t[mx + 1:]), (bits, tf)
+        # linear is the f32 quotient itself
+        lin = (np.arange(mx + 1, dtype=np.float32) / np.float32(mx)).astype(np.float32)
+        assert np.array_equal(O.transfer_lut(bits, 8)[: mx + 1], lin)
+    # the 8-bit non-default transfers take the f32 formula too
+    v = np.arange(256, dtype=np.float64) / 255
+    bt709 = np.where(v < 4.5 * 0.01805397, v / 4.5, ((v + 0.0992968) / 1.0992968) ** (1 / 0.45))
+    assert np.abs(O.transfer_lut(8, 1) - bt709).max() < 1e-6
+
+
+def test_transfer_codes_the_front_end_rejects():
+    for tf in (16, 18, 3, 19, -1):
+        with pytest.raises(ValueError):
+            O.transfer_lut(16, tf)
+    with pytest.raises(ValueError):
+        O.transfer_lut(9, 13)
+
+
+def test_high_depth_samples_above_the_largest_code():
+    # 10-bit: a sample above 1023 decodes to 0 (its LUT slot is empty), and
+    # an alpha above 1023 is capped to it
+    rng = np.random.default_rng(5)
+    img = rng.integers(0, 1024, (24, 24, 4)).astype(np.uint16)
+    img[..., 3] = 1023
+    hi = img.copy()
+    hi[3, 4, 0] = 4000
+    zero = img.copy()
+    zero[3, 4, 0] = 0
+    hi[..., 3][hi[..., 3] == 1023] = 60000
+    a = O.frontend(hi, 1.0, bits=10)
+    b = O.frontend(zero, 1.0, bits=10)
+    assert np.array_equal(a.xyb, b.xyb)
+    assert np.array_equal(a.alpha, np.full((24, 24), 1023, np.uint16))
+    assert a.tokens.tolist() == b.tokens.tolist()
