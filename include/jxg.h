@@ -169,7 +169,11 @@ int32_t jxg_validate_input(uint64_t width, uint64_t height, int32_t channels, in
  * src/group.rs:1259), with the tokens' per-context histograms
  * (build_histograms_with, src/entropy/write.rs:840).
  *
- * `pixels`: interleaved samples, `channels` 3 (RGB) or 4 (RGBA, as
+ * `pixels`: interleaved samples, `channels` 1 (grey, as encode_image_gray
+ * on its lossy path: the luma decoded into all three planes,
+ * src/encode_image.rs:1571-1600; the caller keeps the reference's bi-level
+ * and few-level checks, which route such images to the lossless coder),
+ * 2 (grey + alpha), 3 (RGB) or 4 (RGBA; alpha in the last channel, as
  * encode_image_with_alpha / _16bit with their defaults: lossy alpha, so the
  * near-transparent fringe is cleared (src/alpha_fringe.rs:78), zero-alpha
  * colours are filled from their neighbours (src/invisible.rs:34) and a

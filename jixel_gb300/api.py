@@ -171,9 +171,15 @@ class FrontendResult:
     packed_offsets: np.ndarray | None = None  # (groups + 1,) u64 word offsets
 
 
+def _as_hwc(pixels: np.ndarray) -> np.ndarray:
+    """(h, w) grey samples as (h, w, 1); other shapes unchanged."""
+    pixels = np.ascontiguousarray(pixels)
+    return pixels[:, :, None] if pixels.ndim == 2 else pixels
+
+
 def _pixels_kind(pixels: np.ndarray, config: "EncodeConfig | None" = None) -> tuple[int, int]:
-    if pixels.ndim != 3 or pixels.shape[2] not in (3, 4):
-        raise EncodeError(9, f"expected (h, w, 3|4) samples, got {pixels.shape}")
+    if pixels.ndim != 3 or pixels.shape[2] not in (1, 2, 3, 4):
+        raise EncodeError(9, f"expected (h, w, 1|2|3|4) samples, got {pixels.shape}")
     want = config.bits_per_sample if config is not None else 0
     if pixels.dtype == np.uint8:
         if want not in (0, 8):
@@ -300,7 +306,7 @@ class FrontendContext:
 
     def run(self, pixels: np.ndarray, config: EncodeConfig):
         """Host input: copy in, run, wait (jxg_frontend_run)."""
-        pixels = np.ascontiguousarray(pixels)
+        pixels = _as_hwc(pixels)
         ch, bits = _pixels_kind(pixels, config)
         h, w = pixels.shape[:2]
         cfg = config._c()
@@ -345,9 +351,10 @@ class FrontendContext:
 
     def frontend(self, pixels: np.ndarray, config: EncodeConfig, *, coefficients: bool = True,
                  xyb: bool = False, packed: bool = False) -> FrontendResult:
+        pixels = _as_hwc(pixels)
         self.run(pixels, config)
         return self.fetch(pixels.shape[1], pixels.shape[0], coefficients=coefficients, xyb=xyb,
-                          alpha=pixels.shape[2] == 4, packed=packed)
+                          alpha=pixels.shape[2] in (2, 4), packed=packed)
 
     # operator table -----------------------------------------------------
     def fill_quant_field(self, xyb: np.ndarray, distance: float, inv_scale: float) -> np.ndarray:
@@ -474,7 +481,7 @@ class PinnedOutputs:
         self.group_offsets = pin((fi.num_groups + 1,), torch.int64).view(np.uint64)
         self.histograms = pin((L.NUM_FINE_AC_CONTEXTS, L.ALPHABET_SIZE), torch.int32).view(np.uint32)
         self.xyb = pin((3, height, width), torch.float32) if xyb else None
-        self.alpha = pin((height, width), torch.int16).view(np.uint16) if channels == 4 else None
+        self.alpha = pin((height, width), torch.int16).view(np.uint16) if channels in (2, 4) else None
         self.params = L.FrameParams()
         o = L.FrontendOutput()
         o.quant_field = self.quant_field.ctypes.data
@@ -548,7 +555,7 @@ class FrontendBatch:
         return len(self._sizes)
 
     def add(self, pixels: np.ndarray, config: EncodeConfig) -> int:
-        pixels = np.ascontiguousarray(pixels)
+        pixels = _as_hwc(pixels)
         ch, bits = _pixels_kind(pixels, config)
         h, w = pixels.shape[:2]
         return self._add(pixels.ctypes.data, w, h, ch, bits, config, pixels)
@@ -578,7 +585,7 @@ class FrontendBatch:
                packed: bool = False) -> FrontendResult:
         w, h, ch = self._sizes[index]
         p = self.params(index)
-        r, o = _result_buffers(p, w, h, coefficients, xyb, ch == 4, packed)
+        r, o = _result_buffers(p, w, h, coefficients, xyb, ch in (2, 4), packed)
         self._check(self._lib.jxg_batch_result(self._b, index, None, ctypes.byref(o)))
         return _trim(r)
 

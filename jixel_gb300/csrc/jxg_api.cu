@@ -301,7 +301,7 @@ int validate(Context* c, const void* pixels, uint64_t w, uint64_t h, int32_t cha
   if (w == 0 || h == 0) return fail(c, JXG_ERR_EMPTY_IMAGE, "empty image");
   if (w > kMaxDimension || h > kMaxDimension)
     return fail(c, JXG_ERR_DIMENSION_TOO_LARGE, "dimension too large");
-  if (channels != 3 && channels != 4) return fail(c, JXG_ERR_BAD_CHANNEL_COUNT, "channels");
+  if (channels < 1 || channels > 4) return fail(c, JXG_ERR_BAD_CHANNEL_COUNT, "channels");
   if (bits != 8 && bits != 10 && bits != 12 && bits != 16)
     return fail(c, JXG_ERR_BAD_BIT_DEPTH, "bits");
   const int tf = transfer_status(cfg->transfer);
@@ -361,7 +361,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     groups += L.info.num_groups;
     L.count_off = counts;
     counts += L.info.num_groups * 4096;
-    L.has_alpha = im.channels == 4;
+    L.has_alpha = im.channels == 2 || im.channels == 4;
     if (L.has_alpha) {
       L.alpha_off = alpha_px;
       alpha_px += align_up(static_cast<size_t>(px), 128);

@@ -526,16 +526,18 @@ int orc_to_xyb(const void* pixels, int bits, int transfer, int channels, size_t 
 #endif
   for (size_t i = 0; i < n; i++) {
     float r, g, b;
+    /* grey (1 or 2 channels): R = G = B, linearize_gray (src/encode_image.rs:1571-1600) */
+    const int cg = channels < 3 ? 0 : 1, cb = channels < 3 ? 0 : 2;
     if (bits == 8) {
       const uint8_t* p = (const uint8_t*)pixels + i * (size_t)channels;
       r = lut[p[0]];
-      g = lut[p[1]];
-      b = lut[p[2]];
+      g = lut[p[cg]];
+      b = lut[p[cb]];
     } else {
       const uint16_t* p = (const uint16_t*)pixels + i * (size_t)channels;
       r = lut[p[0]];
-      g = lut[p[1]];
-      b = lut[p[2]];
+      g = lut[p[cg]];
+      b = lut[p[cb]];
     }
     rgb_to_xyb(m, r, g, b, &xyb[i], &xyb[n + i], &xyb[2 * n + i]);
   }
@@ -2480,7 +2482,7 @@ int orc_frontend(orc_frame* f) {
   size_t w = f->width, h = f->height;
   if (w == 0 || h == 0) return ORC_ERR_EMPTY;
   if (!(f->bits == 8 || f->bits == 10 || f->bits == 12 || f->bits == 16)) return ORC_ERR_INPUT;
-  if (!(f->channels == 3 || f->channels == 4)) return ORC_ERR_INPUT;
+  if (f->channels < 1 || f->channels > 4) return ORC_ERR_INPUT;
   int st = orc_params_for(f->distance, &f->params);
   if (st) return st;
   float mat[192], inv[192];
@@ -2512,12 +2514,13 @@ int orc_frontend(orc_frame* f) {
   /* the largest code value; high-depth alpha is capped to it
    * (encode_high_depth_rgba, src/encode_image.rs:4270-4290) */
   const uint32_t alpha_max = (1u << f->bits) - 1u;
-  if (f->channels == 4) {
+  if (f->channels == 4 || f->channels == 2) { /* RGBA, or grey + alpha (encode_gray_impl) */
     alpha = f->alpha ? f->alpha : (uint16_t*)malloc(n * sizeof(uint16_t));
     if (!alpha) return ORC_ERR_ALLOC;
     for (size_t i = 0; i < n; i++) {
-      const uint32_t a = f->bits == 8 ? ((const uint8_t*)f->pixels)[i * 4 + 3]
-                                      : ((const uint16_t*)f->pixels)[i * 4 + 3];
+      const size_t at = i * (size_t)f->channels + (size_t)f->channels - 1;
+      const uint32_t a = f->bits == 8 ? ((const uint8_t*)f->pixels)[at]
+                                      : ((const uint16_t*)f->pixels)[at];
       alpha[i] = (uint16_t)(a < alpha_max ? a : alpha_max);
     }
     orc_alpha_fringe_clear(alpha, w, h, alpha_max);

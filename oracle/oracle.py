@@ -186,6 +186,8 @@ def frontend(pixels: np.ndarray, distance: float, num_threads: int = 0,
     10 / 12 / 16 for uint16 samples (default: the sample type's), `transfer`
     an H.273 transfer code (0: sRGB, the default encoding; 8: linear)."""
     pixels = np.ascontiguousarray(pixels)
+    if pixels.ndim == 2:  # grey
+        pixels = pixels[:, :, None]
     h, w, ch = pixels.shape
     if bits is None:
         bits = 8 if pixels.dtype == np.uint8 else 16
@@ -203,7 +205,7 @@ def frontend(pixels: np.ndarray, distance: float, num_threads: int = 0,
     tokens = np.zeros((cap, 2), np.uint32)
     offs = np.zeros(ng + 1, np.uint64)
     hist = np.zeros((NUM_FINE_AC_CONTEXTS, ALPHABET), np.uint32)
-    alpha = np.zeros((h, w), np.uint16) if ch == 4 else None
+    alpha = np.zeros((h, w), np.uint16) if ch in (2, 4) else None
     f = OrcFrame()
     f.pixels = pixels.ctypes.data
     f.bits = bits

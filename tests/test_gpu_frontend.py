@@ -251,3 +251,18 @@ def test_unsupported_transfers_and_depths(ctx):
         ctx.run(img, ultrafast(1.0, bits=9))
     assert e.value.variant == "BadBitDepth"
     compare(ctx, synthetic.generate(40, 40, 6), 1.0)
+
+
+def _grey(w, h, seed, bits=8, alpha=False):
+    img = synthetic.generate(w, h, seed, sixteen_bit=bits > 8, alpha=alpha)
+    luma = img[..., 1]
+    if bits not in (8, 16):
+        luma = (luma.astype(np.uint32) * ((1 << bits) - 1) // 65535).astype(np.uint16)
+    return np.stack([luma, img[..., 3]], axis=-1) if alpha else luma
+
+
+@pytest.mark.parametrize("bits,alpha", [(8, False), (8, True), (10, False), (12, True), (16, False)])
+def test_grey_input(ctx, bits, alpha):
+    # encode_image_gray (+ _alpha, _10bit, _12bit, _16bit) on the lossy path:
+    # the luma through the transfer table as R = G = B
+    compare(ctx, _grey(130, 90, 80 + bits, bits, alpha), 1.0, bits=bits)

@@ -51,7 +51,7 @@ def test_frame_info_matches_image_dim():
     ((0, 5, 3, 8), "EmptyImage"),
     ((5, 0, 3, 8), "EmptyImage"),
     ((1 << 30, 1, 3, 8), "DimensionTooLarge"),
-    ((8, 8, 2, 8), "BadChannelCount"),
+    ((8, 8, 5, 8), "BadChannelCount"),
     ((8, 8, 3, 11), "BadBitDepth"),
 ])
 def test_input_validation(args, variant):

@@ -688,3 +688,17 @@ def test_high_depth_samples_above_the_largest_code():
     assert np.array_equal(a.xyb, b.xyb)
     assert np.array_equal(a.alpha, np.full((24, 24), 1023, np.uint16))
     assert a.tokens.tolist() == b.tokens.tolist()
+
+
+def test_grey_is_rgb_with_equal_channels():
+    # linearize_gray (src/encode_image.rs:1571-1600) writes the decoded luma
+    # to all three planes, so a grey frame is the RGB frame (g, g, g); grey +
+    # alpha takes its alpha from the second channel
+    from jixel_gb300 import synthetic
+    img = synthetic.generate(72, 40, 9, alpha=True)
+    g, a = img[..., 1], img[..., 3]
+    grey, rgb = O.frontend(g, 1.0), O.frontend(np.stack([g, g, g], -1), 1.0)
+    assert np.array_equal(grey.xyb, rgb.xyb) and grey.tokens.tolist() == rgb.tokens.tolist()
+    ga, rgba = O.frontend(np.stack([g, a], -1), 1.0), O.frontend(np.stack([g, g, g, a], -1), 1.0)
+    assert np.array_equal(ga.alpha, rgba.alpha) and np.array_equal(ga.xyb, rgba.xyb)
+    assert ga.tokens.tolist() == rgba.tokens.tolist()
