@@ -57,7 +57,7 @@ def parse_args():
     return p.parse_args()
 
 
-def workload_config(impl: str) -> dict:
+def workload_config() -> dict:
     return {
         "workload": "VarDCT front end, 3840x2160 RGB8 sRGB, q75/q90/q95 per step, "
                     "UltraFast effort gates (all-DCT8 layout, one pass)",
@@ -70,7 +70,6 @@ def workload_config(impl: str) -> dict:
                    "3 frames in flight); per-kernel times come from a serialised pass of the "
                    "same steps",
         "parallelism": "replicas only (one independent frame stream per GPU)",
-        "impl": impl,
     }
 
 
@@ -201,10 +200,23 @@ def instructions_from_profiles(kernel: str) -> float | None:
     return None
 
 
+def _synthetic():
+    """The seeded image generator, loaded from its file so that the reference
+    arm does not import the package (whose API loads the CUDA library)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location(
+        "_bench_synthetic", os.path.join(ROOT, "jixel_gb300", "synthetic.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def cpu_baseline_run(img, threads: int | None = None, min_seconds: float = 10.0) -> dict:
     """The oracle (C restatement of the reference's scalar path) on the host cores."""
-    from jixel_gb300 import distance_from_quality
     from oracle import oracle as O
+
+    distance_from_quality = O.distance_from_quality
 
     O.lib()
     cores = threads or os.cpu_count() or 1
@@ -227,9 +239,7 @@ def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return
-    from jixel_gb300 import synthetic
-
-    img = synthetic.config2_image()
+    img = _synthetic().config2_image()
     for _ in range(args.warmup):
         cpu_baseline_run(img, min_seconds=0.0)
     times = []
@@ -242,7 +252,7 @@ def run_reference(args):
         "metric": METRIC, "value": value, "unit": "MP/s", "n_gpus": 0, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config("reference"), "impl": "reference",
+        "config": workload_config(), "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "MP/s", "cores": os.cpu_count() or 1,
                          "kind": "port",
                          "sample": "every step the full workload step (three 3840x2160 frames)"},
@@ -398,7 +408,7 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": "MP/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": max_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": workload_config("gb300"),
+            "data": "synthetic", "config": workload_config(), "impl": "gb300",
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
             "clocks": clocks,
             "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(ktimes.items())},

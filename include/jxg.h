@@ -50,10 +50,15 @@ extern "C" {
  * budget (`with_num_threads`, :1251) and the samples' transfer function
  * (`color_encoding.transfer`, an H.273 transfer-characteristics code as
  * TransferFunction, src/color_encoding.rs:99-160).  The device result never
- * depends on num_threads.  `transfer` 0 is the default encoding's sRGB
- * (13); 1, 6, 14, 15 decode as BT.709, 4 BT.470M, 5 BT.470BG, 7 SMPTE 240,
- * 8 linear, 17 SMPTE 428, and 2, 9-13 as sRGB (select_transfer,
- * src/color.rs:201-222); PQ (16) and HLG (18) return JXG_ERR_UNSUPPORTED. */
+ * depends on num_threads.  `transfer` 0 means "not set": a zero-initialised
+ * config is the default encoding, sRGB (13), whose 8-bit table is the f64
+ * formula of srgb_to_linear_u8_ref (src/color.rs:35-42, :315-318).  It is not
+ * H.273's Reserved code: the reference decodes Reserved like Unspecified (2),
+ * through the f32 sRGB formula, so a caller that means Reserved passes 2.
+ * 1, 6, 14, 15 decode as BT.709, 4 BT.470M, 5 BT.470BG, 7 SMPTE 240,
+ * 8 linear, 17 SMPTE 428, and 2, 9-12 through the f32 sRGB formula
+ * (select_transfer, src/color.rs:201-222); PQ (16) and HLG (18) return
+ * JXG_ERR_UNSUPPORTED. */
 typedef struct jxg_config {
   float distance;
   int32_t speed;
@@ -331,8 +336,8 @@ int32_t jxg_op_pack_tokens(void* ctx, const jxg_token* tokens, const uint64_t* g
  * - offsets:       device, num_groups * 3072 uint32 exclusive offsets out;
  * - group_offsets: device, num_groups + 1 uint64 out;
  * - cuda_stream:   a cudaStream_t (NULL = the legacy default stream).
- * Limit: num_groups <= JXG_NOALLOC_MAX_GROUPS (frames up to about 2.8
- * gigapixels); larger requests return JXG_ERR_DIMENSION_TOO_LARGE.  The call
+ * Limit: num_groups <= JXG_NOALLOC_MAX_GROUPS groups of 256x256 pixels
+ * (frames up to about 0.72 gigapixels); larger requests return JXG_ERR_DIMENSION_TOO_LARGE.  The call
  * only enqueues work on the stream; it calls no cudaMalloc, cudaFree or
  * allocating library routine.  The first call on a device looks up the
  * scratch array's device address (cudaGetSymbolAddress) with that device

@@ -363,6 +363,8 @@ int transfer_table(int bits, int transfer, float* out) {
   float (*decode)(float) = nullptr;
   const int st = select_decode(transfer, &decode);
   if (st) return st;
+  // 0 is the C ABI's "not set" (the default encoding, sRGB = 13), not H.273
+  // Reserved; only 8-bit sRGB takes the f64 table (src/color.rs:315-318)
   if (bits == 8 && (transfer == 0 || transfer == 13)) {
     srgb_to_linear_table(out);
     return 0;

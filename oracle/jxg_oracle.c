@@ -545,6 +545,14 @@ int orc_to_xyb(const void* pixels, int bits, int transfer, int channels, size_t 
   return 0;
 }
 
+/* snap_achromatic_xyb (src/frame/encoder.rs:351-357): X = 0, B = Y */
+void orc_snap_achromatic(float* xyb, size_t n) {
+  for (size_t i = 0; i < n; i++) {
+    xyb[i] = 0.0f;
+    xyb[2 * n + i] = xyb[n + i];
+  }
+}
+
 /* ------------------------------------------------------------------ */
 /* Frame statistics (src/frame/chroma.rs)                               */
 /* ------------------------------------------------------------------ */
@@ -2526,6 +2534,10 @@ int orc_frontend(orc_frame* f) {
     orc_alpha_fringe_clear(alpha, w, h, alpha_max);
     orc_fill_invisible(xyb, alpha, w, h);
   }
+  /* grey input is encoded as achromatic (with_grayscale, src/encode_image.rs:3968):
+   * snap_achromatic_xyb (src/frame/encoder.rs:155-157, :351-357) sets X to 0
+   * and B to Y after the XYB conversion and the invisible fill */
+  if (f->channels < 3) orc_snap_achromatic(xyb, n);
   f->constant_blocks = orc_constant_blocks(xyb, w, h);
   f->screen_content = orc_is_screen_content(f->constant_blocks, w, h);
   f->epf_sharpness = orc_epf_sharpness_id(f->params.distance, f->screen_content);

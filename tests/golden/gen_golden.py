@@ -3,7 +3,7 @@
 Run in the container that holds the reference checkout (it is not available
 on the GPU machines):
 
-    python tests/golden/gen_golden.py /root/reference
+    python tests/golden/gen_golden.py <path of the reference checkout>
 
 The reference is Rust and cannot be built here, so its golden data are the
 constant tables and asserted values that its own unit tests pin:
@@ -94,4 +94,6 @@ def main(root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: gen_golden.py <path of the reference checkout>")
+    main(sys.argv[1])

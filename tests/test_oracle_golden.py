@@ -690,15 +690,25 @@ def test_high_depth_samples_above_the_largest_code():
     assert a.tokens.tolist() == b.tokens.tolist()
 
 
-def test_grey_is_rgb_with_equal_channels():
+def test_grey_is_snapped_achromatic():
     # linearize_gray (src/encode_image.rs:1571-1600) writes the decoded luma
-    # to all three planes, so a grey frame is the RGB frame (g, g, g); grey +
-    # alpha takes its alpha from the second channel
+    # to all three planes, and the grey encode is achromatic
+    # (with_grayscale(true), src/encode_image.rs:3968), so encode_frame snaps
+    # the XYB planes after the conversion and the invisible fill:
+    # X = 0 and B = Y exactly (snap_achromatic_xyb, src/frame/encoder.rs:155-157,
+    # :351-357).  The RGB frame (g, g, g) is not snapped: its X plane holds the
+    # rounding noise of the three opsin mixes.
     from jixel_gb300 import synthetic
     img = synthetic.generate(72, 40, 9, alpha=True)
     g, a = img[..., 1], img[..., 3]
     grey, rgb = O.frontend(g, 1.0), O.frontend(np.stack([g, g, g], -1), 1.0)
-    assert np.array_equal(grey.xyb, rgb.xyb) and grey.tokens.tolist() == rgb.tokens.tolist()
+    assert np.all(grey.xyb[0] == 0.0) and not np.signbit(grey.xyb[0]).any()
+    assert np.array_equal(grey.xyb[2], grey.xyb[1])
+    assert np.array_equal(grey.xyb[1], rgb.xyb[1])
+    assert not np.array_equal(grey.xyb, rgb.xyb)
+    # grey + alpha takes its alpha from the second channel; the snap follows
+    # the fill
     ga, rgba = O.frontend(np.stack([g, a], -1), 1.0), O.frontend(np.stack([g, g, g, a], -1), 1.0)
-    assert np.array_equal(ga.alpha, rgba.alpha) and np.array_equal(ga.xyb, rgba.xyb)
-    assert ga.tokens.tolist() == rgba.tokens.tolist()
+    assert np.array_equal(ga.alpha, rgba.alpha)
+    assert np.all(ga.xyb[0] == 0.0) and np.array_equal(ga.xyb[2], ga.xyb[1])
+    assert np.array_equal(ga.xyb[1], rgba.xyb[1])
