@@ -2338,7 +2338,7 @@ typedef struct {
   int32_t bits;             /* 8, or 10 / 12 / 16 in 16-bit words */
   int32_t channels;         /* 3 or 4 (RGBA: lossy alpha, fill_invisible on) */
   int32_t transfer;         /* H.273 transfer code; 0 = sRGB (the default encoding) */
-  int32_t pad_;
+  int32_t speed;            /* 0 UltraFast, 1 Fastest */
   uint64_t width, height;
   float distance;
   int32_t num_threads;
@@ -2355,6 +2355,7 @@ typedef struct {
   uint64_t* group_offsets; /* num_groups + 1 */
   uint32_t* histograms;    /* NUM_FINE_AC_CONTEXTS * 128 */
   uint16_t* alpha;         /* w * h: the alpha plane after fringe clearing (RGBA only) */
+  uint8_t* ac_strategy;    /* xb * yb AcStrategyImage cells: raw << 1 | first */
   /* scalar outputs */
   orc_params params;
   uint32_t qf_threshold;
@@ -2382,6 +2383,8 @@ typedef struct {
   uint32_t* tok; /* pairs */
   uint64_t count;
 } group_tokens;
+
+#include "jxg_oracle_search.inc"
 
 static void encode_ac_group(const orc_frame* f, const float* xyb, const float* mat,
                             const float* inv, const uint8_t* qf, const int8_t* ytox,
@@ -2493,6 +2496,14 @@ int orc_frontend(orc_frame* f) {
   if (f->channels < 1 || f->channels > 4) return ORC_ERR_INPUT;
   int st = orc_params_for(f->distance, &f->params);
   if (st) return st;
+  /* Fastest searches transforms unless the distance takes the DCT8-only
+   * shortcut (use_dct8_only, src/ac_strategy.rs:73-80); up to 1.709 the
+   * reference also reranks merges in the reconstruction domain
+   * (FAST_RERANK_MAX_DISTANCE, src/ac_strategy.rs:67), which is not
+   * restated here */
+  if (f->speed != 0 && f->speed != 1) return ORC_ERR_UNSUPPORTED;
+  const int search = f->speed == 1 && !(f->params.distance <= 0.056713393f);
+  if (search && f->params.distance <= 1.7090991223128462f) return ORC_ERR_UNSUPPORTED;
   float mat[192], inv[192];
   st = orc_dct8_tables(f->params.distance, mat, inv);
   if (st) return st;
@@ -2554,8 +2565,9 @@ int orc_frontend(orc_frame* f) {
     size_t gxb = (gxs + 7) / 8, gyb = (gys + 7) / 8;
     fill_quant_field(xyb, w, h, x0, y0, gxb, gyb, f->params.distance, inv_scale, qf, xb);
   }
-  /* the alpha factors come last in setup_dc_group (src/frame/dc_groups.rs:303-312) */
-  if (alpha) orc_apply_alpha_factors(qf, alpha, w, h, alpha_max);
+  /* the alpha factors come last in setup_dc_group (src/frame/dc_groups.rs:303-312):
+   * for an all-DCT8 layout here, after the transform search otherwise */
+  if (alpha && !search) orc_apply_alpha_factors(qf, alpha, w, h, alpha_max);
   double t2 = now_seconds();
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic) num_threads(threads)
@@ -2569,6 +2581,31 @@ int orc_frontend(orc_frame* f) {
     size_t bxc = minz(8, dcbx_end - bx0), byc = minz(8, dcby_end - by0);
     cmap_tile(xyb, w, h, bx0, by0, bxc, byc, f->params.distance, inv, inv + 128, &ytox[t],
               &ytob[t]);
+  }
+  uint8_t* map = f->ac_strategy ? f->ac_strategy : (uint8_t*)malloc(nb);
+  if (!map) return ORC_ERR_ALLOC;
+  for (size_t i = 0; i < nb; i++) map[i] = 1;
+  orc_tables* tables = NULL;
+  orc_orders* orders = NULL;
+  if (search) {
+    /* fill_ac_strategy per DC group, then the alpha factors over the layout,
+     * then the frame's account_matrix_headers (src/frame/dc_groups.rs:183-312,
+     * src/frame/vardct_encoder.rs:960-969) */
+    tables = (orc_tables*)malloc(sizeof(orc_tables));
+    orders = (orc_orders*)malloc(sizeof(orc_orders));
+    uint8_t* block_qf = (uint8_t*)malloc(nb);
+    if (!tables || !orders || !block_qf) return ORC_ERR_ALLOC;
+    if ((st = orc_build_tables(f->params.distance, tables))) return st;
+    build_orders(orders);
+    init_rate_log2();
+    memcpy(block_qf, qf, nb);
+    search_ctx sc = {xyb, w, h, n, xb, yb, txn, tables, orders, f->params.distance, f->params.scale,
+                     f->params.x_qm_mul, f->params.b_qm_mul, ytox, ytob};
+    const float dampen = clampf(aq_schedule(AQ_STRENGTH, f->params.distance), 0.0f, 1.0f);
+    fastest_search(&sc, qf, map, dampen);
+    if (alpha) apply_alpha_factors_layout(qf, map, alpha, w, h, alpha_max);
+    account_matrix_headers(&sc, qf, block_qf, map);
+    free(block_qf);
   }
   double t3 = now_seconds();
   f->qf_threshold = qf_threshold_of(qf, nb);
@@ -2589,8 +2626,12 @@ int orc_frontend(orc_frame* f) {
 #endif
     for (long g = 0; g < (long)ng; g++) {
       size_t gx = (size_t)g % xg, gy = (size_t)g / xg;
-      encode_ac_group(f, xyb, mat, inv, qf, ytox, ytob, qdc, f->coeffs, f->nzeros, gx, gy,
-                      f->qf_threshold, scan, &gts[g], local);
+      if (search)
+        encode_ac_group_layout(f, xyb, tables, orders, map, qf, ytox, ytob, qdc, f->coeffs,
+                               f->nzeros, gx, gy, f->qf_threshold, &gts[g], local);
+      else
+        encode_ac_group(f, xyb, mat, inv, qf, ytox, ytob, qdc, f->coeffs, f->nzeros, gx, gy,
+                        f->qf_threshold, scan, &gts[g], local);
     }
 #ifdef _OPENMP
 #pragma omp critical
@@ -2624,6 +2665,9 @@ int orc_frontend(orc_frame* f) {
   f->stage_seconds[3] = t4 - t3;
   f->stage_seconds[4] = t5 - t4;
   free(gts);
+  free(tables);
+  free(orders);
+  if (!f->ac_strategy) free(map);
   if (!f->histograms) free(hist);
   if (!f->xyb) free(xyb);
   if (alpha && !f->alpha) free(alpha);

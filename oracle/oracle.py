@@ -42,7 +42,7 @@ class OrcFrame(ctypes.Structure):
         ("bits", ctypes.c_int32),
         ("channels", ctypes.c_int32),
         ("transfer", ctypes.c_int32),
-        ("pad_", ctypes.c_int32),
+        ("speed", ctypes.c_int32),
         ("width", ctypes.c_uint64),
         ("height", ctypes.c_uint64),
         ("distance", ctypes.c_float),
@@ -59,6 +59,7 @@ class OrcFrame(ctypes.Structure):
         ("group_offsets", ctypes.c_void_p),
         ("histograms", ctypes.c_void_p),
         ("alpha", ctypes.c_void_p),
+        ("ac_strategy", ctypes.c_void_p),
         ("params", OrcParams),
         ("qf_threshold", ctypes.c_uint32),
         ("constant_blocks", ctypes.c_uint64),
@@ -106,6 +107,19 @@ def lib() -> ctypes.CDLL:
         _lib.orc_nonzero_context.argtypes = [ctypes.c_int32]
         _lib.orc_constant_blocks.restype = ctypes.c_uint64
         _lib.orc_constant_blocks.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t]
+        _lib.orc_strategy_cost_probe.restype = ctypes.c_float
+        _lib.orc_strategy_cost_probe.argtypes = [
+            ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
+            ctypes.c_float, ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_float]
+        _lib.orc_fastest_select.restype = ctypes.c_int
+        _lib.orc_fastest_select.argtypes = [
+            ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p,
+            ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_uint32, ctypes.c_void_p,
+            ctypes.c_void_p]
+        _lib.orc_large_tables.restype = ctypes.c_int
+        _lib.orc_large_tables.argtypes = [ctypes.c_float] + [ctypes.c_void_p] * 4
+        _lib.orc_natural_scan.restype = None
+        _lib.orc_natural_scan.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         assert _lib.orc_sizeof_frame() == ctypes.sizeof(OrcFrame), "OrcFrame layout mismatch"
     return _lib
 
@@ -172,6 +186,7 @@ class OracleFrame:
     group_offsets: np.ndarray
     histograms: np.ndarray      # (contexts, 128) uint32
     alpha: np.ndarray | None    # (h, w) uint16 alpha after fringe clearing (RGBA only)
+    ac_strategy: np.ndarray
     qf_threshold: int
     constant_blocks: int
     screen_content: bool
@@ -179,12 +194,16 @@ class OracleFrame:
     stage_seconds: list
 
 
+SPEEDS = {"ultrafast": 0, "fastest": 1}
+
+
 def frontend(pixels: np.ndarray, distance: float, num_threads: int = 0,
              keep_coeffs: bool = True, bits: int | None = None,
-             transfer: int = 0) -> OracleFrame:
+             transfer: int = 0, speed: str = "ultrafast") -> OracleFrame:
     """Run the oracle on an (h, w, c) uint8 or uint16 image: `bits` 8, or
     10 / 12 / 16 for uint16 samples (default: the sample type's), `transfer`
-    an H.273 transfer code (0: sRGB, the default encoding; 8: linear)."""
+    an H.273 transfer code (0: sRGB, the default encoding; 8: linear),
+    `speed` "ultrafast" or "fastest"."""
     pixels = np.ascontiguousarray(pixels)
     if pixels.ndim == 2:  # grey
         pixels = pixels[:, :, None]
@@ -206,7 +225,9 @@ def frontend(pixels: np.ndarray, distance: float, num_threads: int = 0,
     offs = np.zeros(ng + 1, np.uint64)
     hist = np.zeros((NUM_FINE_AC_CONTEXTS, ALPHABET), np.uint32)
     alpha = np.zeros((h, w), np.uint16) if ch in (2, 4) else None
+    strategy = np.zeros((yb, xb), np.uint8)
     f = OrcFrame()
+    f.speed = SPEEDS[speed]
     f.pixels = pixels.ctypes.data
     f.bits = bits
     f.transfer = transfer
@@ -227,6 +248,7 @@ def frontend(pixels: np.ndarray, distance: float, num_threads: int = 0,
     f.group_offsets = offs.ctypes.data
     f.histograms = hist.ctypes.data
     f.alpha = alpha.ctypes.data if alpha is not None else None
+    f.ac_strategy = strategy.ctypes.data
     st = lib().orc_frontend(ctypes.byref(f))
     if st:
         raise ValueError(f"oracle frontend status {st}")
@@ -239,6 +261,7 @@ def frontend(pixels: np.ndarray, distance: float, num_threads: int = 0,
                 "dc_step": list(p.dc_step)},
         xyb=xyb, quant_field=qf, ytox=ytox, ytob=ytob, quant_dc=qdc, coeffs=coeffs,
         nzeros=nz, tokens=tokens[: f.num_tokens], group_offsets=offs, histograms=hist, alpha=alpha,
+        ac_strategy=strategy,
         qf_threshold=f.qf_threshold, constant_blocks=f.constant_blocks,
         screen_content=bool(f.screen_content), epf_sharpness=f.epf_sharpness,
         stage_seconds=list(f.stage_seconds),
@@ -439,3 +462,54 @@ def transfer_lut(bits: int, transfer: int) -> np.ndarray:
     if st:
         raise ValueError(f"transfer {transfer} at {bits} bits: status {st}")
     return out[:256] if bits == 8 else out
+
+
+def natural_scan(cx: int, cy: int) -> np.ndarray:
+    """natural_scan_generic: scan position -> raw index of a cx >= cy block."""
+    out = np.zeros(cx * cy * 64, np.uint16)
+    lib().orc_natural_scan(cx, cy, out.ctypes.data)
+    return out
+
+
+def strategy_cost(xyb: np.ndarray, ytox: np.ndarray, ytob: np.ndarray, distance: float,
+                  strategy: int, bx: int, by: int, qac: float) -> float:
+    """strategy_cost (coefficient model, META_R) of one candidate transform
+    with its first block at (bx, by), on (3, h, w) XYB planes and the frame's
+    CfL tile maps."""
+    x = np.ascontiguousarray(xyb, np.float32)
+    tx = np.ascontiguousarray(ytox, np.int8)
+    tb = np.ascontiguousarray(ytob, np.int8)
+    _, h, w = x.shape
+    return float(lib().orc_strategy_cost_probe(x.ctypes.data, w, h, tx.ctypes.data, tb.ctypes.data,
+                                               distance, strategy, bx, by, qac))
+
+
+def fastest_select(xyb: np.ndarray, ytox: np.ndarray, ytob: np.ndarray, qf: np.ndarray,
+                   ctx_distance: float, distance: float, scale: float,
+                   x_qm_scale: int = 2) -> tuple[np.ndarray, np.ndarray]:
+    """fill_ac_strategy at Fastest on one (3, h, w) image: returns the
+    strategy map (raw << 1 | first per block) and the adjusted quant field."""
+    x = np.ascontiguousarray(xyb, np.float32)
+    _, h, w = x.shape
+    q = np.ascontiguousarray(qf, np.uint8).copy()
+    m = np.zeros_like(q)
+    tx = np.ascontiguousarray(ytox, np.int8)
+    tb = np.ascontiguousarray(ytob, np.int8)
+    st = lib().orc_fastest_select(x.ctypes.data, w, h, tx.ctypes.data, tb.ctypes.data,
+                                  ctx_distance, distance, scale, x_qm_scale, q.ctypes.data,
+                                  m.ctypes.data)
+    if st:
+        raise ValueError(f"oracle fastest_select status {st}")
+    return m, q
+
+
+def large_tables(distance: float) -> dict:
+    """DequantMatrices::new_fast's 16x8, 16x16 and 32x32 forward matrices at
+    `distance`, plus the 16x8 table recomputed from its band parameters."""
+    out = {"16x8": np.zeros((3, 128), np.float32), "16x16": np.zeros((3, 256), np.float32),
+           "32x32": np.zeros((3, 1024), np.float32), "16x8_bands": np.zeros((3, 128), np.float32)}
+    st = lib().orc_large_tables(distance, out["16x8"].ctypes.data, out["16x16"].ctypes.data,
+                                out["32x32"].ctypes.data, out["16x8_bands"].ctypes.data)
+    if st:
+        raise ValueError(f"oracle large_tables status {st}")
+    return out

@@ -69,8 +69,41 @@ def main(root: str) -> None:
     afv = afv[: afv.index("];")]
     afv_basis = re.findall(r"-?\d+\.\d+", afv)
     assert len(afv_basis) == 256, len(afv_basis)
+    # larger transforms: the library DCT16X8 table as written (decimal
+    # literals, parsed to f32 by the compilers), the band parameters of the
+    # 16x16 / 32x32 / 16x8 tables, the natural orders and the block-context map
+    m16x8 = qw[qw.index("static DEQUANT_MATRIX_16X8:"):]
+    m16x8 = m16x8[m16x8.index("= [") + 3:]
+    m16x8 = m16x8[: m16x8.index("];")]
+    m16x8 = re.findall(r"-?\d+\.\d+(?:e-?\d+)?", re.sub(r"//[^\n]*", "", m16x8))
+    assert len(m16x8) == 384, len(m16x8)
+
+    def band_strings(name, n):
+        body = qw[qw.index(name):]
+        body = body[body.index("= [") + 3:]
+        body = body[: body.index("];")]
+        vals = re.findall(r"-?\d[\d_]*\.[\d_]*(?:e-?\d+)?", re.sub(r"//[^\n]*", "", body))
+        assert len(vals) == 3 * n, (name, len(vals))
+        return [v.replace("_", "") for v in vals]
+
+    order16x8 = _array(ac, "K_COEFF_ORDER_16X8:")
+    order16x16 = _array(ac, "K_COEFF_ORDER_16X16:")
+    order32x32 = _array(ac, "K_COEFF_ORDER_32X32:")
+    assert (len(order16x8), len(order16x16), len(order32x32)) == (128, 256, 1024)
+    strategy_order = _array(ac, "K_STRATEGY_ORDER:")
+    block_ctx_map = _array(ac, "K_COMPACT_BLOCK_CONTEXT_MAP:")
+    assert len(strategy_order) == 27 and len(block_ctx_map) == 39
     out = {
         "source": "jixel 0.5.14",
+        "dequant_matrix_16x8": m16x8,
+        "dct16x16_bands": band_strings("static DCT16X16_BANDS:", 7),
+        "dct32x32_bands": band_strings("static DCT32X32_BANDS:", 8),
+        "dct16x8_bands": band_strings("static DCT16X8_BANDS:", 7),
+        "coeff_order_16x8": order16x8,
+        "coeff_order_16x16": order16x16,
+        "coeff_order_32x32": order32x32,
+        "strategy_order": strategy_order,
+        "compact_block_context_map": block_ctx_map,
         "afv_basis_transpose": afv_basis,
         "dct8_bands": dct8_bands,
         "dequant_matrix_8x8": dct8_static,
