@@ -35,7 +35,16 @@ extern "C" {
 #define JXG_ERR_DEVICE_TIMEOUT 102    /* a bounded device wait gave up */
 
 /* Speed (src/encode_image.rs:256-286).  This build runs UltraFast's gates
- * (src/effort.rs:305-309); other tiers return JXG_ERR_UNSUPPORTED. */
+ * (src/effort.rs:305-309) and Fastest's (:311-320) for one frame per pass:
+ * the square-merge search over 16x16 / 32x32 DCTs, the coefficient-model
+ * re-tiling with 16x8 / 8x16 pairs, the quant-field aggregation and the
+ * matrix-header accounting, with the layout's DC/AC coding and tokens.
+ * Fastest at distances up to 1.709, where the reference also reranks merges
+ * in the reconstruction domain (FAST_RERANK_MAX_DISTANCE,
+ * src/ac_strategy.rs:67), Fastest in a batch of several frames, and every
+ * slower tier return JXG_ERR_UNSUPPORTED.  At distances up to 0.0567 the
+ * reference's Fastest keeps every block DCT8 (src/ac_strategy.rs:73-80), as
+ * UltraFast does. */
 #define JXG_SPEED_ULTRAFAST 0
 #define JXG_SPEED_FASTEST 1
 #define JXG_SPEED_FAST 2
@@ -122,7 +131,11 @@ typedef struct jxg_frontend_output {
   int8_t* ytox_map;        /* tiles */
   int8_t* ytob_map;        /* tiles */
   int16_t* quant_dc;       /* 3 planes X, Y, B of xb*yb (DcGroupData::quant_dc) */
-  int32_t* coefficients;   /* xb*yb*192: per block X, Y, B, 64 levels each */
+  int32_t* coefficients;   /* xb*yb*192: per block X, Y, B, 64 levels each, in raw
+                              coefficient order; a transform covering several
+                              blocks spreads its channel's levels in runs of 64:
+                              run t of a transform at (bx, by) covering cx
+                              blocks across sits at block (bx + t % cx, by + t / cx) */
   uint8_t* num_nzeros;     /* 3 planes of xb*yb */
   float* xyb;              /* 3 planes of w*h (the opsin image) */
   jxg_token* tokens;       /* pass-one tokens, groups in raster order */

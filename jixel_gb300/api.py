@@ -79,9 +79,12 @@ class EncodeConfig:
     """The part of `EncodeConfig` (src/encode_image.rs:326-588) the front end
     reads.  `transfer` is `color_encoding.transfer` (default sRGB);
     `bits_per_sample` picks the entry point for uint16 samples, as
-    encode_image_10bit / _12bit / _16bit do (0: 8 for uint8, 16 for uint16)."""
+    encode_image_10bit / _12bit / _16bit do (0: 8 for uint8, 16 for uint16).
+    The reference defaults to Speed.FAST; this build runs the UltraFast gates
+    and, above distance 1.709, the Fastest ones, so its default is ULTRA_FAST
+    (any other tier returns EncodeError Unsupported with the reason)."""
     distance: float = 1.0
-    speed: Speed = Speed.FAST
+    speed: Speed = Speed.ULTRA_FAST
     num_threads: int = field(default_factory=lambda: os.cpu_count() or 1)
     transfer: TransferFunction = TransferFunction.SRGB
     bits_per_sample: int = 0

@@ -3,6 +3,7 @@
 // `fmla` (src/dct.rs:31-41) is on aarch64.
 #include "frame_params.h"
 #include "library_dct8.h"
+#include "library_tables.h"
 
 #include <algorithm>
 #include <cmath>
@@ -373,6 +374,214 @@ int transfer_table(int bits, int transfer, float* out) {
   const float max = static_cast<float>(size - 1);
   for (int v = 0; v < domain; ++v) out[v] = v < size ? decode(static_cast<float>(v) / max) : 0.0f;
   return 0;
+}
+
+namespace {
+
+// scaled_override (src/quant_weights.rs:202-222): the base band scaled,
+// every parameter F16 round-tripped as signalled
+void scaled_override(const float* defaults, int nb, float scale, float* out) {
+  for (int c = 0; c < 3; ++c)
+    for (int i = 0; i < nb; ++i) {
+      const float v = i == 0 ? defaults[c * nb] * scale : defaults[c * nb + i];
+      out[c * nb + i] = i == 0 ? half_round(v / 64.0f) * 64.0f : half_round(v);
+    }
+}
+
+// compute_dct16x16_matrix / compute_dct32x32_matrix (src/quant_weights.rs:1588-1651)
+// with fill_ac_reciprocals (:3136-3141)
+void square_band_matrix(const float* src, int nb, int n, float* m, float* inv) {
+  for (int c = 0; c < 3; ++c) {
+    float bands[8];
+    bands[0] = src[c * nb];
+    for (int i = 1; i < nb; ++i) bands[i] = bands[i - 1] * band_mult(src[c * nb + i]);
+    const float scale = (static_cast<float>(nb) - 1.0f) / (1.41421356237309505f + 1e-6f);
+    const float rcp = scale / static_cast<float>(n - 1);
+    for (int y = 0; y < n; ++y) {
+      const float dy = static_cast<float>(y) * rcp;
+      const float dy2 = dy * dy;
+      for (int x = 0; x < n; ++x) {
+        const float dx = static_cast<float>(x) * rcp;
+        const float pos = std::sqrt(fmla(dx, dx, dy2));
+        const float fl = std::floor(pos);
+        const float frac = pos - fl;
+        const size_t idx = static_cast<size_t>(fl);
+        const float a = bands[idx], b = bands[idx + 1];
+        m[c * n * n + y * n + x] = 1.0f / (std::pow(b / a, frac) * a);
+      }
+    }
+    inv[c * n * n] = 0.0f;
+    for (int k = 1; k < n * n; ++k) inv[c * n * n + k] = 1.0f / m[c * n * n + k];
+  }
+}
+
+// natural_scan_generic (src/coeff_order.rs:203-244): scan position -> raw
+// index of a cx >= cy block in its cy*8-row x cx*8-column layout
+void natural_scan(int cx, int cy, uint16_t* scan, uint16_t* pos) {
+  const int side = cx * 8, xs = cx / cy, xsm = xs - 1;
+  int xss = 0;
+  while ((1 << xss) < xs) ++xss;
+  int cur = cx * cy;
+  for (int i = 0; i < side; ++i)
+    for (int j = 0; j <= i; ++j) {
+      int x = j, y = i - j;
+      if (i % 2) std::swap(x, y);
+      if (y & xsm) continue;
+      y >>= xss;
+      const int val = (x < cx && y < cy) ? y * cx + x : cur++;
+      scan[val] = static_cast<uint16_t>(y * side + x);
+    }
+  for (int ip = side - 1; ip >= 1; --ip) {
+    const int i = ip - 1;
+    for (int j = 0; j <= i; ++j) {
+      int x = side - 1 - (i - j), y = side - 1 - j;
+      if (i % 2) std::swap(x, y);
+      if (y & xsm) continue;
+      y >>= xss;
+      scan[cur++] = static_cast<uint16_t>(y * side + x);
+    }
+  }
+  for (int k = 0; k < cx * cy * 64; ++k) pos[scan[k]] = static_cast<uint16_t>(k);
+}
+
+// quantize_ac_thresholds_scaled (src/group.rs:420-455)
+void ac_thresholds_scaled(int c, int xs, int ys, float d, float qm_mul, float thr[4]) {
+  float normal[4] = {0.58f, 0.635f, 0.66f, 0.7f};
+  if (c == 0) {
+    const float up = clamp((d - 0.5f) / (0.75f - 0.5f), 0.0f, 1.0f);
+    const float down = clamp((2.0f - d) / (2.0f - 1.5f), 0.0f, 1.0f);
+    const float w = std::min(up, down);
+    normal[0] += w * (0.5f - normal[0]);
+    for (int i = 1; i < 4; ++i) normal[i] += (1.0f - w) * 0.08f;
+  }
+  if (c == 2) {
+    const float hf = qm_mul > 1.0f ? 0.65f : 0.75f;
+    for (int i = 1; i < 4; ++i) normal[i] = hf;
+  }
+  if (xs > 1 || ys > 1) {
+    const float delta = clamp(0.003f * static_cast<float>(xs) * static_cast<float>(ys), 0.0f,
+                              c > 0 ? 0.08f : 0.12f);
+    for (int i = 0; i < 4; ++i) normal[i] -= delta;
+  }
+  const float hq_y[4] = {0.50f, 0.51f, 0.52f, 0.54f};
+  const float* hq = c == 1 ? hq_y : normal;
+  const float t = clamp((d - 0.1f) / 0.9f, 0.0f, 1.0f);
+  for (int i = 0; i < 4; ++i) thr[i] = hq[i] + t * (normal[i] - hq[i]);
+}
+
+// Banded::at and merge_margin (src/ac_strategy.rs:103-113, :174-180)
+float banded(float hq, float base, float d) {
+  const float t = clamp((d - 0.5f) / (1.5f - 0.5f), 0.0f, 1.0f);
+  return fmla(t, base - hq, hq);
+}
+float merge_margin(float d, float hq, float base) {
+  const float fade = clamp((d - 1.0f) / (4.0f - 1.0f), 0.0f, 1.0f);
+  return banded(hq, base, d) * (1.0f - fade * (1.0f - 0.82f));
+}
+
+}  // namespace
+
+void rate_log2_table(float* out) {
+  for (int i = 0; i < kRateLog2Entries; ++i) out[i] = ::log2f(1.0f + static_cast<float>(i));
+}
+
+int fastest_search_mode(float distance) {
+  const float d = std::max(distance, 0.05f);
+  if (d <= 0.056713393f) return 0;            // DCT8_ONLY_MAX_DISTANCE
+  if (d <= 1.7090991223128462f) return 2;     // FAST_RERANK_MAX_DISTANCE
+  return 1;
+}
+
+int search_tables(const DistanceParams& p, SearchTables* t, SearchParams* sp) {
+  const float d = p.distance;
+  if (t && search_matrices(p, t)) return 1;
+  search_params(d, sp);
+  return 0;
+}
+
+int search_matrices(const DistanceParams& p, SearchTables* t) {
+  const float d = p.distance;
+  if (dct8_tables(d, t->mat8, t->inv8)) return 1;
+  for (int c = 0; c < 3; ++c) {
+    for (int k = 0; k < 128; ++k) t->mat16x8[c][k] = LIB_DCT16X8_MATRIX[c][k];
+    t->inv16x8[c][0] = 0.0f;
+    for (int k = 1; k < 128; ++k) t->inv16x8[c][k] = 1.0f / t->mat16x8[c][k];
+  }
+  // DequantMatrices::new_fast: the 16x16 / 32x32 tables are the library's
+  // below the SS2 gate, their bases scaled by 0.78 / 0.89 from it
+  // (dct16_override / dct32_override, src/quant_weights.rs:2068-2089)
+  const bool ss2 = d >= 2.25f;
+  float b16[21], b32[24];
+  if (ss2) {
+    scaled_override(&LIB_DCT16X16_BANDS[0][0], 7, 0.78f, b16);
+    scaled_override(&LIB_DCT32X32_BANDS[0][0], 8, 0.89f, b32);
+  } else {
+    std::memcpy(b16, LIB_DCT16X16_BANDS, sizeof(b16));
+    std::memcpy(b32, LIB_DCT32X32_BANDS, sizeof(b32));
+  }
+  square_band_matrix(b16, 7, 16, &t->mat16[0][0], &t->inv16[0][0]);
+  square_band_matrix(b32, 8, 32, &t->mat32[0][0], &t->inv32[0][0]);
+  natural_scan(1, 1, t->scan8, t->pos8);
+  natural_scan(2, 1, t->scan16x8, t->pos16x8);
+  natural_scan(2, 2, t->scan16, t->pos16);
+  natural_scan(4, 4, t->scan32, t->pos32);
+  const int dims[4][2] = {{1, 1}, {2, 1}, {2, 2}, {4, 4}};
+  const float qm[3] = {p.x_qm_mul, 1.0f, p.b_qm_mul};
+  for (int k = 0; k < 4; ++k)
+    for (int c = 0; c < 3; ++c) ac_thresholds_scaled(c, dims[k][0], dims[k][1], d, qm[c], t->thr[k][c]);
+  exp2_table(t->exp2);
+  return 0;
+}
+
+void search_params(float d, SearchParams* sp) {
+  // MergeTuning::new at Fastest (site_k = SITE_BIAS_K), arbiter SSIMULACRA2
+  sp->site_k = 0.2f;
+  sp->bias_16x16 = banded(1.2059275f, 1.05f, d);
+  sp->bias_32x32 = banded(1.2059275f, 1.06f, d);
+  sp->accept_16 = 1.0f - merge_margin(d, 0.19243888f, 0.048f);
+  sp->accept_32 = 1.0f - merge_margin(d, 0.21398508f, 0.234f);
+  // risk_k = MERGE_RISK_K while aq_dampen(d) > 0 (AQ_STRENGTH, src/adaptive_quant.rs:105-121)
+  {
+    static const float knots[7] = {0.5f, 1.0f, 1.4f, 1.75f, 3.0f, 5.0f, 8.0f};
+    static const float strength[7] = {0.26565f, 0.275459f, 0.058287f, 0.0f, 0.0f, 0.0f, 0.0f};
+    float v = strength[6];
+    if (d <= knots[0]) {
+      v = strength[0];
+    } else {
+      for (int i = 1; i < 7; ++i)
+        if (d <= knots[i]) {
+          const float fr = (d - knots[i - 1]) / (knots[i] - knots[i - 1]);
+          v = strength[i - 1] + fr * (strength[i] - strength[i - 1]);
+          break;
+        }
+    }
+    sp->risk_k = clamp(v, 0.0f, 1.0f) > 0.0f ? 1.44269504088896340736f : 0.0f;
+  }
+  const float vlq_t = clamp((d - 4.0f) / (7.5f - 4.0f), 0.0f, 1.0f);
+  if (vlq_t > 0.0f) {
+    sp->bias_16x16 = fmla(vlq_t, 0.880f - sp->bias_16x16, sp->bias_16x16);
+    sp->bias_32x32 = fmla(vlq_t, 0.867f - sp->bias_32x32, sp->bias_32x32);
+    sp->accept_16 = fmla(vlq_t, (1.0f - 0.067f) - sp->accept_16, sp->accept_16);
+    sp->accept_32 = fmla(vlq_t, (1.0f - 0.029250f) - sp->accept_32, sp->accept_32);
+  }
+  if (d >= 1.5f) sp->bias_32x32 *= 0.94f;
+  sp->sel_scale = (d >= 1.0f && d <= 4.0f) ? 1 : 0;
+  const bool ss2 = d >= 2.25f;
+  // MatrixHeaderCost of new_fast's tables: the DCT8 override (6 bands), the
+  // 4x8 refit (4 bands + 48), the 8x32 bands (8), and from the SS2 gate the
+  // 16x16 (7), 32x32 (8) and 32x16 (8) overrides
+  std::memset(sp->payload, 0, sizeof(sp->payload));
+  sp->payload[0] = d >= 0.3f ? 4 + 48 * 6 : 0;
+  sp->payload[5] = 4 + 48 * 4 + 48;
+  sp->payload[12] = 4 + 48 * 8;
+  if (ss2) {
+    sp->payload[1] = 4 + 48 * 7;
+    sp->payload[2] = 4 + 48 * 8;
+    sp->payload[4] = 4 + 48 * 8;
+  }
+  sp->custom = 0;
+  for (int i = 0; i < 13; ++i) sp->custom |= static_cast<uint32_t>(sp->payload[i] != 0) << i;
+  sp->headers = ss2 ? 1 : 0;
 }
 
 void exp2_table(float out[64]) {

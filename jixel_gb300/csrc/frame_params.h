@@ -58,6 +58,51 @@ struct KernelArgs {
   float inv_matrix[3][64]; // their reciprocals (index 0 = 0)
 };
 
+// Strategies of the Fastest search (AcStrategyImage raw codes,
+// src/dc_group_data.rs:32-36).
+constexpr int kStDct = 0, kSt16x8 = 1, kSt8x16 = 2, kSt16x16 = 3, kSt32x32 = 4;
+constexpr int kRateLog2Entries = 1 << 18;
+
+// Constant tables of the Fastest search and layout coding of one frame:
+// DequantMatrices::new_fast's tables of the five transforms and their
+// reciprocals (src/quant_weights.rs:1588-1652, :2294-2339, :2606-2730), the
+// natural orders (src/coeff_order.rs:203-244) both ways, the AC thresholds
+// per shape class (1x1, 2x1, 2x2, 4x4 blocks) and channel
+// (quantize_ac_thresholds_scaled, src/group.rs:420-455) and fast_exp2's table.
+struct SearchTables {
+  float inv8[3][64], inv16x8[3][128], inv16[3][256], inv32[3][1024];
+  float mat8[3][64], mat16x8[3][128], mat16[3][256], mat32[3][1024];
+  uint16_t scan8[64], scan16x8[128], scan16[256], scan32[1024];  // scan position -> raw
+  uint16_t pos8[64], pos16x8[128], pos16[256], pos32[1024];      // raw -> scan position
+  float thr[4][3][4];
+  float exp2[64];
+};
+
+// log2(1 + i) by the host's libm for i < kRateLog2Entries (rate_log2_lut,
+// src/inflated_cost.rs:57-66, extended past its 1024 entries with the same
+// function the reference calls beyond them).
+void rate_log2_table(float* out);
+
+// MergeTuning at the frame's distance (src/ac_strategy.rs:87-136, :270-343),
+// the selection quantizer's gate and the matrix-header costs.
+struct SearchParams {
+  float bias_16x16, bias_32x32, accept_16, accept_32, risk_k, site_k;
+  int32_t sel_scale;      // selection_quantizer::enabled at Fastest: 1 <= d <= 4
+  int32_t headers;        // account_matrix_headers can change the layout (d >= 2.25)
+  uint32_t payload[13];   // MatrixHeaderCost (src/quant_weights.rs:54-101)
+  uint32_t custom;        // its custom mask
+};
+
+// Speed::Fastest's transform search runs (not the DCT8-only shortcut,
+// src/ac_strategy.rs:73-80); 2 when the distance also asks for the
+// reconstruction-domain rerank (FAST_RERANK_MAX_DISTANCE, :67), which this
+// build does not have.
+int fastest_search_mode(float distance);
+// The tables (skipped when `t` is null) and the parameters at p's distance.
+int search_tables(const DistanceParams& p, SearchTables* t, SearchParams* sp);
+int search_matrices(const DistanceParams& p, SearchTables* t);
+void search_params(float distance, SearchParams* sp);
+
 int compute_distance_params(float distance, DistanceParams* out);
 // DCT8 tables of DequantMatrices::new_fast (the library table below d = 0.3).
 int dct8_tables(float distance, float matrix[3][64], float inv[3][64]);

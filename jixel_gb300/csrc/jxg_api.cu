@@ -14,6 +14,7 @@
 #include "../../include/jxg.h"
 #include "frame_params.h"
 #include "jxg_kernels.cuh"
+#include "jxg_search.cuh"
 
 namespace jxg {
 namespace {
@@ -93,6 +94,7 @@ struct FrameLayout {
   size_t pix_off = 0, xyb_off = 0, block_off = 0, tile_off = 0, group_off = 0, count_off = 0;
   bool has_alpha = false;
   size_t alpha_off = 0, alpha_block_off = 0;  // RGBA frames only
+  bool searched = false;  // Speed::Fastest's transform search ran on this frame
 };
 
 struct Context {
@@ -106,6 +108,13 @@ struct Context {
   std::map<int, float*> luts;
   float* d_exp2 = nullptr;      // fast_exp2 table, 64
   uint8_t* d_pos = nullptr;     // natural 8x8 order, raw index -> scan position
+  uint8_t* d_pos_identity = nullptr;  // raw index -> itself (layout levels are in raw order)
+  float* d_rate_log2 = nullptr;       // log2(1 + i), kRateLog2Entries
+  // Speed::Fastest: search tables per distance, the frame's SearchFrame and
+  // the search's pass buffers
+  std::map<uint32_t, SearchTables*> search_tables;
+  SearchFrame search_host{};
+  DevBuf search_frame, search_costs, search_map, search_bqf, search_dp, search_sites;
   // pass buffers (grown, never shrunk)
   DevBuf pixels, xyb, qf, ytox, ytob, quant_dc, levels, wide_levels, coeffs, nzeros, nz_packed,
       counts, tokens, hist, stats, group_offsets, plan, total, op_in, op_out,
@@ -309,8 +318,12 @@ int validate(Context* c, const void* pixels, uint64_t w, uint64_t h, int32_t cha
   if (tf != 0) return fail(c, JXG_ERR_INVALID_ARGUMENT, "transfer");
   if (!std::isfinite(cfg->distance) || cfg->distance <= 0.0f)
     return fail(c, JXG_ERR_INVALID_DISTANCE, "distance must be positive and finite");
-  if (cfg->speed != JXG_SPEED_ULTRAFAST)
-    return fail(c, JXG_ERR_UNSUPPORTED, "only Speed::UltraFast gates are built");
+  if (cfg->speed != JXG_SPEED_ULTRAFAST && cfg->speed != JXG_SPEED_FASTEST)
+    return fail(c, JXG_ERR_UNSUPPORTED, "only the Speed::UltraFast and Speed::Fastest gates are built");
+  if (cfg->speed == JXG_SPEED_FASTEST && fastest_search_mode(cfg->distance) == 2)
+    return fail(c, JXG_ERR_UNSUPPORTED,
+                "Speed::Fastest up to distance 1.709 reranks merges in the reconstruction "
+                "domain, which this build does not have");
   if (w * h > (1ull << 31))
     return fail(c, JXG_ERR_DIMENSION_TOO_LARGE, "frames above 2^31 pixels are not supported");
   return JXG_OK;
@@ -323,6 +336,34 @@ int check_device_pixels(Context* c, const void* pixels, int32_t bits) {
   return JXG_OK;
 }
 
+// Device copy of the Fastest search tables at `dp`'s distance, built and
+// uploaded on first use and kept for the context's life.
+SearchTables* search_tables_for(Context* c, const DistanceParams& dp) {
+  uint32_t key;
+  std::memcpy(&key, &dp.distance, 4);
+  const auto it = c->search_tables.find(key);
+  if (it != c->search_tables.end()) return it->second;
+  if (c->search_tables.size() >= 64) {  // bound the cache
+    cudaStreamSynchronize(c->stream);
+    for (auto& kv : c->search_tables) cudaFree(kv.second);
+    c->search_tables.clear();
+  }
+  std::vector<char> host(sizeof(SearchTables));
+  SearchTables* t = reinterpret_cast<SearchTables*>(host.data());
+  SearchParams unused;
+  if (search_tables(dp, t, &unused)) return nullptr;
+  SearchTables* d = nullptr;
+  if (cudaMalloc(&d, sizeof(SearchTables)) != cudaSuccess) return nullptr;
+  if (cudaMemcpy(d, t, sizeof(SearchTables), cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(d);
+    return nullptr;
+  }
+  c->search_tables[key] = d;
+  return d;
+}
+
+constexpr size_t kSearchFrameBytes = (sizeof(SearchFrame) + 255) / 256 * 256;
+
 // Lays out a pass of `n` frames in the context's buffers, sizes them, and
 // fills the pinned plan (frame descriptors + chunk prefixes).  No launch.
 // `stage`: host pixels go through the context's pinned staging buffer (what
@@ -334,6 +375,13 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     if ((st = validate(c, imgs[i].pixels, imgs[i].width, imgs[i].height, imgs[i].channels,
                        imgs[i].bits, &imgs[i].config)))
       return st;
+  // Speed::Fastest searches one frame per pass
+  bool any_search = false;
+  for (int i = 0; i < n; ++i)
+    any_search = any_search || (imgs[i].config.speed == JXG_SPEED_FASTEST &&
+                                fastest_search_mode(imgs[i].config.distance) == 1);
+  if (any_search && n > 1)
+    return fail(c, JXG_ERR_UNSUPPORTED, "Speed::Fastest runs one frame per pass");
   c->have_frame = false;
   c->layouts.assign(n, FrameLayout{});
   size_t pix = 0, xyb = 0, blocks = 0, tiles = 0, groups = 0, counts = 0, tokens = 0;
@@ -392,7 +440,8 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
   }
   c->frames_bytes = align_up(sizeof(Frame) * n, 256);
   const size_t prefix_bytes = align_up(sizeof(int64_t) * (n + 1), 256);
-  const size_t plan_bytes = align_up(c->frames_bytes + kPlanPrefixes * prefix_bytes, 256);
+  const size_t plan_bytes =
+      align_up(c->frames_bytes + kPlanPrefixes * prefix_bytes, 256) + kSearchFrameBytes;
   if (plan_bytes > c->plan_slot_cap) {
     // grow every slot; the stream drains first, so no queued upload reads them
     JXG_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -502,6 +551,97 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
   pre_tok[n] = ak;
   pre_alpha[n] = aa;
   pre_fill[n] = af;
+  if (any_search) {
+    FrameLayout& L = c->layouts[0];
+    L.searched = true;
+    const size_t nb = L.info.xsize_blocks * L.info.ysize_blocks;
+    const size_t tiles8 = L.info.xsize_tiles * L.info.ysize_tiles;
+    if ((st = ensure(c, c->search_costs, 9 * nb * 4)) || (st = ensure(c, c->search_map, nb)) ||
+        (st = ensure(c, c->search_bqf, nb)) || (st = ensure(c, c->search_dp, tiles8 * 64 * 512)) ||
+        (st = ensure(c, c->search_sites, nb * 4)))
+      return st;
+    SearchFrame& sf = c->search_host;
+    sf = SearchFrame{};
+    sf.t = search_tables_for(c, L.dp);
+    if (!sf.t) return fail(c, JXG_ERR_ALLOCATION_FAILED, "search tables");
+    sf.rate_log2 = c->d_rate_log2;
+    search_tables(L.dp, nullptr, &sf.p);
+    sf.qm_mult[0] = L.dp.x_qm_mul;
+    sf.qm_mult[1] = 1.0f;
+    sf.qm_mult[2] = L.dp.b_qm_mul;
+    sf.distance = L.dp.distance;
+    sf.scale = L.dp.scale;
+    float* costs = static_cast<float*>(c->search_costs.ptr);
+    float** arrays[9] = {&sf.c8, &sf.c16s, &sf.c16r, &sf.cw, &sf.ct, &sf.c32, &sf.m16, &sf.m32, &sf.mh_inc};
+    for (int k = 0; k < 9; ++k) *arrays[k] = costs + k * nb;
+    sf.map = static_cast<uint8_t*>(c->search_map.ptr);
+    sf.block_qf = static_cast<uint8_t*>(c->search_bqf.ptr);
+    sf.dp_choices = static_cast<uint8_t*>(c->search_dp.ptr);
+    sf.sites = static_cast<uint32_t*>(c->search_sites.ptr);
+    const size_t search_off = plan_bytes - kSearchFrameBytes;
+    std::memcpy(plan_h + search_off, &sf, sizeof(SearchFrame));
+    frames[0].search = static_cast<char*>(c->plan.ptr) + c->plan_slot * c->plan_slot_cap + search_off;
+  }
+  return JXG_OK;
+}
+
+// Speed::Fastest's transform search and layout coding of the single frame
+// `f` (see jxg_search.cuh), after the tile kernel has made the CfL maps.
+int enqueue_search(Context* c, const Frame& f, bool timed) {
+  cudaStream_t s = c->stream;
+  const FrameLayout& L = c->layouts[0];
+  const SearchFrame& sf = c->search_host;
+  const int64_t xb = static_cast<int64_t>(L.info.xsize_blocks), yb = static_cast<int64_t>(L.info.ysize_blocks);
+  const int64_t nb = xb * yb;
+  const int64_t tiles = static_cast<int64_t>(L.info.xsize_tiles * L.info.ysize_tiles);
+  JXG_CUDA(c, cudaMemcpyAsync(sf.block_qf, f.qf, nb, cudaMemcpyDeviceToDevice, s));
+  JXG_CUDA(c, cudaMemsetAsync(sf.map, 1, nb, s));
+  auto grid4 = [](int64_t n) { return static_cast<unsigned>((n + 3) / 4); };
+  int st;
+  const int64_t n16 = (xb / 2) * (yb / 2), n8x16 = (xb / 2) * yb, n16x8 = xb * (yb / 2);
+  const int64_t n32 = (xb / 4) * (yb / 4);
+  if ((st = launch(c, "k_cost_dct8", timed, [&] {
+         k_cost<kStDct><<<grid4(nb), 128, cost_smem_bytes<kStDct>(), s>>>(f);
+       })))
+    return st;
+  if (n16 && (st = launch(c, "k_cost_16x16", timed, [&] {
+                k_cost<kSt16x16><<<grid4(n16), 128, cost_smem_bytes<kSt16x16>(), s>>>(f);
+              })))
+    return st;
+  if (n8x16 && (st = launch(c, "k_cost_8x16", timed, [&] {
+                  k_cost<kSt8x16><<<grid4(n8x16), 128, cost_smem_bytes<kSt8x16>(), s>>>(f);
+                })))
+    return st;
+  if (n16x8 && (st = launch(c, "k_cost_16x8", timed, [&] {
+                  k_cost<kSt16x8><<<grid4(n16x8), 128, cost_smem_bytes<kSt16x8>(), s>>>(f);
+                })))
+    return st;
+  if (n32 && (st = launch(c, "k_cost_32x32", timed, [&] {
+                k_cost<kSt32x32><<<grid4(n32), 128, cost_smem_bytes<kSt32x32>(), s>>>(f);
+              })))
+    return st;
+  const int64_t cells = ((xb + 3) / 4) * ((yb + 3) / 4);
+  if ((st = launch(c, "k_select", timed, [&] {
+         k_select<<<static_cast<unsigned>((cells + 127) / 128), 128, 0, s>>>(f);
+       })) ||
+      (st = launch(c, "k_retile", timed, [&] {
+         k_retile<<<static_cast<unsigned>((tiles + 63) / 64), 64, 0, s>>>(f);
+       })) ||
+      (st = launch(c, "k_adjust", timed, [&] {
+         k_adjust<<<static_cast<unsigned>((nb + 255) / 256), 256, 0, s>>>(f);
+       })))
+    return st;
+  if (sf.p.headers &&
+      ((st = launch(c, "k_mh_incumbent", timed, [&] {
+          k_mh_incumbent<<<grid4(nb), 128, cost_smem_bytes<kSt32x32>(), s>>>(f);
+        })) ||
+       (st = launch(c, "k_mh_choose", timed, [&] { k_mh_choose<<<1, kMhThreads, 0, s>>>(f); }))))
+    return st;
+  if ((st = launch(c, "k_qf_median", timed, [&] { k_qf_median<<<1, 256, 0, s>>>(f); })) ||
+      (st = launch(c, "k_layout_tile", timed, [&] {
+         k_layout_tile<<<static_cast<unsigned>(tiles), 32 * kLayoutWarps, kLayoutSmemBytes, s>>>(f);
+       })))
+    return st;
   return JXG_OK;
 }
 
@@ -525,6 +665,13 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
     if (!capturing) JXG_CUDA(c, cudaEventRecord(c->plan_uploaded[c->plan_slot], s));
   }
   const Frame& f0 = *reinterpret_cast<const Frame*>(plan_h);
+  const bool searched = single && c->layouts[0].searched;
+  if (searched) {
+    // the SearchFrame the search kernels read, from the pinned plan slot
+    const size_t off = align_up(c->frames_bytes + kPlanPrefixes * prefix_bytes, 256);
+    JXG_CUDA(c, cudaMemcpyAsync(plan_d + off, plan_h + off, sizeof(SearchFrame), cudaMemcpyHostToDevice, s));
+    if (!capturing) JXG_CUDA(c, cudaEventRecord(c->plan_uploaded[c->plan_slot], s));
+  }
   if (src == PixelSource::kStaged)
     JXG_CUDA(c, cudaMemcpyAsync(c->pixels.ptr, c->pixels_host.ptr, c->pixel_bytes,
                                 cudaMemcpyHostToDevice, s));
@@ -592,6 +739,7 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
                f0, c->d_pos);
          })))
       return st;
+    if (searched && (st = enqueue_search(c, f0, timed))) return st;
   } else {
     if ((st = launch(c, "k_xyb_batch", timed, [&] {
            k_xyb_batch<<<static_cast<unsigned>(c->xyb_chunks), 256, 0, s>>>(frames, pre_xyb, n);
@@ -631,7 +779,11 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
   scan.status = static_cast<unsigned long long*>(c->tok_status.ptr);
   scan.chunks = c->token_chunks;
   scan.pass_end = static_cast<uint64_t*>(c->group_offsets.ptr) + c->total_groups;
-  if ((st = single ? launch(c, "k_tokenize", timed, [&] {
+  if ((st = searched ? launch(c, "k_tokenize_layout", timed, [&] {
+         k_tokenize_layout<<<static_cast<unsigned>(c->token_chunks), kLayoutTokThreads, 0, s>>>(
+             f0, static_cast<uint2*>(c->tokens.ptr), scan);
+       })
+       : single ? launch(c, "k_tokenize", timed, [&] {
          k_tokenize<<<static_cast<unsigned>(c->token_chunks), kTokThreads, 0, s>>>(
              f0, static_cast<uint2*>(c->tokens.ptr), scan);
        })
@@ -760,10 +912,12 @@ int enqueue_fixed_downloads(Context* c, int index, const jxg_frontend_output* ou
     st = launch(c, "k_levels_to_raw", c->timing, [&] {
       k_levels_to_raw<<<grid, 256, 0, s>>>(static_cast<const int16_t*>(c->levels.ptr) + 192 * L.block_off,
                                            static_cast<const int32_t*>(c->wide_levels.ptr) + 192 * L.block_off,
-                                           c->d_pos, count, static_cast<int32_t*>(c->coeffs.ptr));
+                                           L.searched ? c->d_pos_identity : c->d_pos, count,
+                                           static_cast<int32_t*>(c->coeffs.ptr));
     });
     if (st) return st;
   }
+  if (L.searched && (st = copy(out->ac_strategy, c->search_map.ptr, nb))) return st;
   if ((st = copy(out->quant_field, static_cast<uint8_t*>(c->qf.ptr) + L.block_off, nb)) ||
       (st = copy(out->ytox_map, static_cast<int8_t*>(c->ytox.ptr) + L.tile_off, nt)) ||
       (st = copy(out->ytob_map, static_cast<int8_t*>(c->ytob.ptr) + L.tile_off, nt)) ||
@@ -861,7 +1015,7 @@ int fetch_frame(Context* c, int index, jxg_frontend_output* out) {
   if ((st = wait(c))) return st;
   if (out->group_offsets)  // frame-local token offsets
     for (uint64_t g = 0; g <= fi.num_groups; ++g) out->group_offsets[g] -= first;
-  if (out->ac_strategy) std::memset(out->ac_strategy, 1, nb);  // all DCT8, first blocks
+  if (out->ac_strategy && !L.searched) std::memset(out->ac_strategy, 1, nb);  // all DCT8, first blocks
   return JXG_OK;
 }
 
@@ -933,9 +1087,12 @@ int32_t jxg_context_create(int32_t device, void** out_ctx) {
       c->num_sms <= 0)
     c->num_sms = 1;
   float e2[64];
-  uint8_t scan[64], pos[64];
+  uint8_t scan[64], pos[64], ident[64];
   jxg::exp2_table(e2);
   jxg::natural_order_8x8(scan, pos);
+  for (int i = 0; i < 64; ++i) ident[i] = static_cast<uint8_t>(i);
+  std::vector<float> rate(jxg::kRateLog2Entries);
+  jxg::rate_log2_table(rate.data());
   bool ok = true;
   for (auto& e : c->plan_uploaded)
     ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
@@ -944,6 +1101,11 @@ int32_t jxg_context_create(int32_t device, void** out_ctx) {
             cudaMalloc(&c->d_pos, 64) == cudaSuccess &&
             cudaMemcpy(c->d_exp2, e2, sizeof(e2), cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(c->d_pos, pos, 64, cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMalloc(&c->d_pos_identity, 64) == cudaSuccess &&
+            cudaMemcpy(c->d_pos_identity, ident, 64, cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMalloc(&c->d_rate_log2, rate.size() * 4) == cudaSuccess &&
+            cudaMemcpy(c->d_rate_log2, rate.data(), rate.size() * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+            jxg::set_search_attributes() == cudaSuccess &&
             cudaFuncSetAttribute(jxg::k_tile_quantize, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(jxg::kTileSmemBytes)) == cudaSuccess &&
             cudaFuncSetAttribute(jxg::k_tile_quantize_batch,
@@ -978,13 +1140,17 @@ void jxg_context_destroy(void* ctx) {
                          &c->group_offsets, &c->plan, &c->total, &c->op_in, &c->op_out,
                          &c->alpha, &c->alpha_peak, &c->alpha_zero, &c->fill_flags,
                          &c->fill_deps, &c->fill_queue, &c->fill_masks, &c->group_wide, &c->packed,
-                         &c->packed_offs, &c->tok_status})
+                         &c->packed_offs, &c->tok_status, &c->search_frame, &c->search_costs,
+                         &c->search_map, &c->search_bqf, &c->search_dp, &c->search_sites})
     if (b->ptr) cudaFree(b->ptr);
   for (jxg::HostBuf* b : {&c->plan_host, &c->pixels_host, &c->async_slot})
     if (b->ptr) cudaFreeHost(b->ptr);
   for (auto& kv : c->luts) cudaFree(kv.second);
   cudaFree(c->d_exp2);
   cudaFree(c->d_pos);
+  cudaFree(c->d_pos_identity);
+  cudaFree(c->d_rate_log2);
+  for (auto& kv : c->search_tables) cudaFree(kv.second);
   for (auto& p : c->pending) {
     cudaEventDestroy(p.start);
     cudaEventDestroy(p.stop);
@@ -1081,7 +1247,7 @@ int32_t jxg_frontend_wait(void* ctx) {
     return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "token buffer too small");
   if (out.packed_tokens && slot->packed_count > out.packed_capacity)
     return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "packed token buffer too small");
-  if (out.ac_strategy)
+  if (out.ac_strategy && !L.searched)
     std::memset(out.ac_strategy, 1, L.info.xsize_blocks * L.info.ysize_blocks);
   // The token streams, whose lengths the host learns only now, leave the
   // device by the copy engine (a single-frame pass starts at token 0).

@@ -25,7 +25,7 @@ def assert_same(got, want, check_xyb=True):
     assert got.tokens.shape == want.tokens.shape, "token count"
     assert np.array_equal(got.tokens, want.tokens), "tokens"
     assert np.array_equal(got.histograms, want.histograms), "histograms"
-    assert np.all(got.ac_strategy == 1)
+    assert np.array_equal(got.ac_strategy, want.ac_strategy), "ac_strategy"
     if getattr(want, "alpha", None) is not None and getattr(got, "alpha", None) is not None:
         assert np.array_equal(got.alpha, want.alpha), "alpha"
 
