@@ -2,14 +2,18 @@
 """VarDCT front-end throughput on GB300 (MP/s).
 
 Workload: one 3840x2160 RGB8 frame from the seeded synthetic generator
-(noise 4, 200 rectangles, 30 % 1/f^2 texture), encoded at qualities 75, 90
-and 95 with the UltraFast gates; one step = those three frames through the
-whole front end (XYB, AQ field, CfL maps, DCT8 + quantisation, tokens and
-per-context histograms).  `value` is timed with CUDA events on the launching
-stream with the input resident in HBM; `e2e` runs the public C ABI with host
-buffers (pinned), the upload and the result download inside the timed region.
-`batch` compares, on 256 images of log-uniform sizes (half RGBA8) at q90,
-one pass per image against one batched pass replayed as a CUDA graph.
+(noise 4, 200 rectangles, 30 % 1/f^2 texture) at quality 75 (distance 2.35)
+with the Speed::Fastest gates; one step = that frame through the whole front
+end (XYB, AQ field, CfL maps, the transform search over 16x16 / 32x32 merges
+and 16x8 / 8x16 re-tiling, the quant-field aggregation and matrix-header
+accounting, the layout's DC/AC quantisation, tokens and per-context
+histograms).  `value` is timed with CUDA events on the launching stream with
+the input resident in HBM; `e2e` runs the public C ABI with host buffers
+(pinned), the upload and the result download inside the timed region.
+`ultrafast` times the same frame at qualities 75, 90 and 95 with the
+UltraFast gates (all-DCT8, one frame each); `batch` compares, on 256 images
+of log-uniform sizes (half RGBA8) at q90 with the UltraFast gates, one pass
+per image against one batched pass replayed as a CUDA graph.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 """
@@ -29,7 +33,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WIDTH, HEIGHT = 3840, 2160
-QUALITIES = (75, 90, 95)
+QUALITIES = (75,)              # the headline workload, Speed::Fastest
+SPEED = "fastest"
+UF_QUALITIES = (75, 90, 95)    # the UltraFast comparison
 METRIC = "VarDCT MP/s"
 L2_FLUSH_BYTES = 256 << 20
 BATCH_IMAGES = 256
@@ -59,10 +65,11 @@ def parse_args():
 
 def workload_config() -> dict:
     return {
-        "workload": "VarDCT front end, 3840x2160 RGB8 sRGB, q75/q90/q95 per step, "
-                    "UltraFast effort gates (all-DCT8 layout, one pass)",
+        "workload": "VarDCT front end, 3840x2160 RGB8 sRGB, q75 (d 2.35) per step, "
+                    "Speed::Fastest gates (square-merge transform search, coefficient "
+                    "re-tiling, matrix-header accounting, layout coding; one pass)",
         "width": WIDTH, "height": HEIGHT, "frames_per_step": len(QUALITIES),
-        "qualities": list(QUALITIES), "effort": "ultrafast",
+        "qualities": list(QUALITIES), "effort": SPEED,
         "input": "synthetic seeded generator (seed 2): cosine gradients, noise sigma 4, "
                  "200 rectangles, 30% 1/f^2 texture, 8-px checker",
         "l2": "256 MB buffer written between timed steps, outside the timed events",
@@ -172,6 +179,17 @@ def algorithmic_bytes(kernel: str, w: int, h: int, tokens_per_frame: float) -> f
         # per block the levels, packed counts, qf and token offsets in; 8-byte
         # tokens and one histogram table out
         "k_tokenize": blocks * (384 + 4 + 1 + 16) + tokens_per_frame * 8 + hist,
+        # Speed::Fastest: each candidate shape reads the three planes once
+        # over the positions it is priced at and writes a cost per position
+        "k_cost_dct8": px * 12 + blocks * 4,
+        "k_cost_16x16": px * 12 + blocks // 4 * 12,
+        "k_cost_8x16": px * 12 + blocks // 2 * 4,
+        "k_cost_16x8": px * 12 + blocks // 2 * 4,
+        "k_cost_32x32": px * 12 + blocks // 16 * 8,
+        # costs, field and map in; map out
+        "k_retile": blocks * (4 * 5 + 2),
+        "k_layout_tile": px * 12 + blocks * (384 + 6 + 3 + 4 + 16),
+        "k_tokenize_layout": blocks * (384 + 4 + 1 + 16) + tokens_per_frame * 8 + hist,
     }
     return table.get(kernel)
 
@@ -224,15 +242,18 @@ def cpu_baseline_run(img, threads: int | None = None, min_seconds: float = 10.0)
     t0 = time.perf_counter()
     while True:
         for q in QUALITIES:
-            O.frontend(img, distance_from_quality(q), num_threads=cores, keep_coeffs=False)
+            O.frontend(img, distance_from_quality(q), num_threads=cores, keep_coeffs=False,
+                       speed=SPEED)
         steps += 1
         dt = time.perf_counter() - t0
         if dt >= min_seconds:
             break
     mp = steps * len(QUALITIES) * img.shape[0] * img.shape[1] / 1e6
     return {"value": mp / dt, "unit": "MP/s", "cores": cores, "kind": "port",
-            "sample": f"{steps} step(s) of {img.shape[1]}x{img.shape[0]} at q75/q90/q95 "
-                      f"({dt:.2f} s, OpenMP over DC groups, tiles and AC groups)"}
+            "sample": f"{steps} step(s) of {img.shape[1]}x{img.shape[0]} at "
+                      f"{'/'.join('q%d' % q for q in QUALITIES)}, Speed::{SPEED.capitalize()} "
+                      f"({dt:.2f} s, OpenMP over DC groups, tiles and AC groups); the C "
+                      "restatement of jixel's scalar path"}
 
 
 def run_reference(args):
@@ -255,7 +276,8 @@ def run_reference(args):
         "config": workload_config(), "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "MP/s", "cores": os.cpu_count() or 1,
                          "kind": "port",
-                         "sample": "every step the full workload step (three 3840x2160 frames)"},
+                         "sample": "every step the full workload step (one 3840x2160 frame at "
+                                   "q75, Speed::Fastest); the C restatement of jixel's scalar path"},
         "e2e": {"value": value, "unit": "MP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -286,7 +308,8 @@ def run_gpu(args):
         assert st.cuda_stream != 0
         c.set_stream(st.cuda_stream)
     ctx = ctxs[0]
-    cfgs = [J.EncodeConfig(speed=J.Speed.ULTRA_FAST).with_quality(q) for q in QUALITIES]
+    speed = J.Speed.FASTEST if SPEED == "fastest" else J.Speed.ULTRA_FAST
+    cfgs = [J.EncodeConfig(speed=speed).with_quality(q) for q in QUALITIES]
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
     turn = [0]
 
@@ -389,6 +412,7 @@ def run_gpu(args):
         "frac": fe_bytes / (fe_ms / 1000.0) / 1e9 / peaks["hbm_gbs"],
     }
 
+    ultrafast = run_ultrafast(ctxs, streams, flush, d_img, args, dev)
     c5 = run_c5(ctxs, streams, flush, args, dev) if args.c5 else None
     batch = None
     if not args.no_batch:
@@ -414,6 +438,7 @@ def run_gpu(args):
             "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(ktimes.items())},
             "tokens_per_frame": [int(x) for x in tokens],
             "batch": batch,
+            "ultrafast": ultrafast,
             "c5": c5,
         }
         print(json.dumps(line), flush=True)
@@ -421,6 +446,47 @@ def run_gpu(args):
         c.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_ultrafast(ctxs, streams, flush, d_img, args, dev) -> dict:
+    """The same frame at q75, q90 and q95 with the UltraFast gates (all-DCT8
+    layout), three frames per step over the contexts in turn, CUDA events on
+    the streams, L2 flushed between steps."""
+    import torch
+
+    import jixel_gb300 as J
+
+    cfgs = [J.EncodeConfig(speed=J.Speed.ULTRA_FAST).with_quality(q) for q in UF_QUALITIES]
+    nctx = len(ctxs)
+    turn = [0]
+
+    def step():
+        for cfg in cfgs:
+            ctxs[turn[0] % nctx].run_device(d_img.data_ptr(), WIDTH, HEIGHT, 3, 8, cfg)
+            turn[0] += 1
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    torch.cuda.synchronize(dev)
+    total = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        s0, e0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(streams[0])
+        for st in streams[1:]:
+            st.wait_event(s0)
+        step()
+        for st in streams[1:]:
+            ek = torch.cuda.Event(enable_timing=True)
+            ek.record(st)
+            streams[0].wait_event(ek)
+        e0.record(streams[0])
+        e0.synchronize()
+        total += s0.elapsed_time(e0)
+    mp = len(cfgs) * WIDTH * HEIGHT / 1e6
+    return {"workload": "3840x2160 RGB8 at q75/q90/q95, UltraFast gates (all-DCT8 layout), "
+                        "three frames per step", "value": args.steps * mp / (total / 1000.0),
+            "unit": "MP/s", "ms_per_step": total / args.steps}
 
 
 def run_c5(ctxs, streams, flush, args, dev) -> dict:
@@ -554,12 +620,11 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
     ctxs = [J.FrontendContext(dev.index or 0) for _ in range(nctx)]
     packed = not args.e2e_wide_tokens
     outs = [J.PinnedOutputs(WIDTH, HEIGHT, packed=packed) for _ in range(nctx)]
-    for o in outs:  # the strategy map is filled on the host; the rest is downloaded
-        o.c.ac_strategy = None
     c_cfgs = [c._c() for c in cfgs]
     nb = fi.xsize_blocks * fi.ysize_blocks
     nt = fi.xsize_tiles * fi.ysize_tiles
-    fixed_d2h = (nb + 2 * nt + 6 * nb + (fi.num_groups + 1) * 8
+    # quant field, strategy map, CfL maps, DC levels, group offsets, histograms
+    fixed_d2h = (nb + nb + 2 * nt + 6 * nb + (fi.num_groups + 1) * 8
                  + L.NUM_FINE_AC_CONTEXTS * L.ALPHABET_SIZE * 4)
     state = {"pending": [False] * nctx, "d2h": 0, "k": 0}
 
@@ -609,7 +674,8 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
     return {"value": value, "unit": "MP/s", "h2d_bytes_per_step": len(QUALITIES) * img.size,
             "d2h_bytes_per_step": int(state["d2h"] / args.steps),
             "path": f"jxg_frontend_enqueue / jxg_frontend_wait (C ABI), {nctx} contexts taking "
-                    "frames in turn: pinned host RGB in; maps, DC levels, tokens "
+                    "frames in turn: pinned host RGB in; quant field, strategy and CfL maps, DC "
+                    "levels, tokens "
                     f"({'packed AcToken words' if packed else 'context/value pairs'}), group "
                     "offsets and histograms out to pinned host memory"}
 

@@ -114,7 +114,7 @@ struct Context {
   // the search's pass buffers
   std::map<uint32_t, SearchTables*> search_tables;
   SearchFrame search_host{};
-  DevBuf search_frame, search_costs, search_map, search_bqf, search_dp, search_sites;
+  DevBuf search_frame, search_costs, search_map, search_bqf, search_dp, search_sites, search_loss;
   // pass buffers (grown, never shrunk)
   DevBuf pixels, xyb, qf, ytox, ytob, quant_dc, levels, wide_levels, coeffs, nzeros, nz_packed,
       counts, tokens, hist, stats, group_offsets, plan, total, op_in, op_out,
@@ -558,7 +558,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     const size_t tiles8 = L.info.xsize_tiles * L.info.ysize_tiles;
     if ((st = ensure(c, c->search_costs, 9 * nb * 4)) || (st = ensure(c, c->search_map, nb)) ||
         (st = ensure(c, c->search_bqf, nb)) || (st = ensure(c, c->search_dp, tiles8 * 64 * 512)) ||
-        (st = ensure(c, c->search_sites, nb * 4)))
+        (st = ensure(c, c->search_sites, nb * 4)) || (st = ensure(c, c->search_loss, nb * 16)))
       return st;
     SearchFrame& sf = c->search_host;
     sf = SearchFrame{};
@@ -578,6 +578,7 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     sf.block_qf = static_cast<uint8_t*>(c->search_bqf.ptr);
     sf.dp_choices = static_cast<uint8_t*>(c->search_dp.ptr);
     sf.sites = static_cast<uint32_t*>(c->search_sites.ptr);
+    sf.mh_loss = static_cast<double*>(c->search_loss.ptr);
     const size_t search_off = plan_bytes - kSearchFrameBytes;
     std::memcpy(plan_h + search_off, &sf, sizeof(SearchFrame));
     frames[0].search = static_cast<char*>(c->plan.ptr) + c->plan_slot * c->plan_slot_cap + search_off;
@@ -625,7 +626,8 @@ int enqueue_search(Context* c, const Frame& f, bool timed) {
          k_select<<<static_cast<unsigned>((cells + 127) / 128), 128, 0, s>>>(f);
        })) ||
       (st = launch(c, "k_retile", timed, [&] {
-         k_retile<<<static_cast<unsigned>((tiles + 63) / 64), 64, 0, s>>>(f);
+         k_retile<<<static_cast<unsigned>((tiles + kRetileThreads - 1) / kRetileThreads),
+                    kRetileThreads, kRetileSmemBytes, s>>>(f);
        })) ||
       (st = launch(c, "k_adjust", timed, [&] {
          k_adjust<<<static_cast<unsigned>((nb + 255) / 256), 256, 0, s>>>(f);
@@ -633,7 +635,7 @@ int enqueue_search(Context* c, const Frame& f, bool timed) {
     return st;
   if (sf.p.headers &&
       ((st = launch(c, "k_mh_incumbent", timed, [&] {
-          k_mh_incumbent<<<grid4(nb), 128, cost_smem_bytes<kSt32x32>(), s>>>(f);
+          k_mh_incumbent<<<grid4(((xb + 1) / 2) * ((yb + 1) / 2)), 128, cost_smem_bytes<kSt32x32>(), s>>>(f);
         })) ||
        (st = launch(c, "k_mh_choose", timed, [&] { k_mh_choose<<<1, kMhThreads, 0, s>>>(f); }))))
     return st;
@@ -1141,7 +1143,8 @@ void jxg_context_destroy(void* ctx) {
                          &c->alpha, &c->alpha_peak, &c->alpha_zero, &c->fill_flags,
                          &c->fill_deps, &c->fill_queue, &c->fill_masks, &c->group_wide, &c->packed,
                          &c->packed_offs, &c->tok_status, &c->search_frame, &c->search_costs,
-                         &c->search_map, &c->search_bqf, &c->search_dp, &c->search_sites})
+                         &c->search_map, &c->search_bqf, &c->search_dp, &c->search_sites,
+                         &c->search_loss})
     if (b->ptr) cudaFree(b->ptr);
   for (jxg::HostBuf* b : {&c->plan_host, &c->pixels_host, &c->async_slot})
     if (b->ptr) cudaFreeHost(b->ptr);

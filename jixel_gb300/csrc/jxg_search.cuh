@@ -70,6 +70,7 @@ struct SearchFrame {
   uint8_t *map, *block_qf;
   uint8_t* dp_choices;  // 32 KB per 8x8-block tile
   uint32_t* sites;      // matrix-header sites in DC-group order
+  double* mh_loss;      // per site: the DCT and 16x16 alternatives' losses
 };
 
 // ---------------------------------------------------------------------------
@@ -377,30 +378,41 @@ __device__ __forceinline__ float util_fast_exp(float x) {
   const float scale = __uint_as_float(static_cast<uint32_t>(exponent + 127) << 23);
   return __fmul_rn(__fadd_rn(1.0f, __fdiv_rn(__fmul_rn(2.0f, r), __fsub_rn(p, r))), scale);
 }
+// The warp stages the site's luma (clipped to the image) in `stage` (n * n
+// floats); lane 0 then takes the f64 sums in raster order.
 __device__ __forceinline__ float site_bias(const Frame& f, const SearchFrame& s, int x0, int y0,
-                                           int n) {
+                                           int n, float* stage) {
   if (s.p.site_k == 0.0f) return 1.0f;
+  const int lane = threadIdx.x & 31;
   const float* yp = f.xyb + f.a.plane;
   const int w = f.a.width, h = f.a.height;
-  double s1 = 0.0, s2 = 0.0;
-  int cnt = 0;
   const int y1 = imin(y0 + n, h), x1 = imin(x0 + n, w);
-  for (int y = y0; y < y1; ++y)
-    for (int x = x0; x < x1; ++x) {
-      const double v = static_cast<double>(__ldg(yp + static_cast<int64_t>(y) * w + x));
+  const int vw = x1 - x0, vh = y1 - y0;
+  for (int k = lane; k < vw * vh; k += 32)
+    stage[k] = __ldg(yp + static_cast<int64_t>(y0 + k / vw) * w + x0 + k % vw);
+  __syncwarp();
+  float out = 1.0f;
+  if (lane == 0) {
+    double s1 = 0.0, s2 = 0.0;
+    const int cnt = vw * vh;
+#pragma unroll 8
+    for (int k = 0; k < cnt; ++k) {
+      const double v = static_cast<double>(stage[k]);
       s1 = __dadd_rn(s1, v);
       s2 = __dadd_rn(s2, __dmul_rn(v, v));
-      ++cnt;
     }
-  float var = 0.0f;
-  if (cnt) {
-    const double mean = __ddiv_rn(s1, static_cast<double>(cnt));
-    const double vv = __dsub_rn(__ddiv_rn(s2, static_cast<double>(cnt)), __dmul_rn(mean, mean));
-    var = static_cast<float>(vv > 0.0 ? vv : 0.0);
+    float var = 0.0f;
+    if (cnt) {
+      const double mean = __ddiv_rn(s1, static_cast<double>(cnt));
+      const double vv = __dsub_rn(__ddiv_rn(s2, static_cast<double>(cnt)), __dmul_rn(mean, mean));
+      var = static_cast<float>(vv > 0.0 ? vv : 0.0);
+    }
+    var = fmaxf(var, 1e-9f);
+    const float sv = fminf(fmaxf(__fdiv_rn(dirty_log2f(__fdiv_rn(var, 0.003f)), 8.0f), -1.0f), 1.0f);
+    out = util_fast_exp(__fmul_rn(s.p.site_k, sv));
   }
-  var = fmaxf(var, 1e-9f);
-  const float sv = fminf(fmaxf(__fdiv_rn(dirty_log2f(__fdiv_rn(var, 0.003f)), 8.0f), -1.0f), 1.0f);
-  return util_fast_exp(__fmul_rn(s.p.site_k, sv));
+  __syncwarp();
+  return __shfl_sync(0xffffffffu, out, 0);
 }
 
 // One warp per candidate of shape S: the costs every consumer of it reads.
@@ -440,6 +452,8 @@ __global__ void __launch_bounds__(128) k_cost(const __grid_constant__ Frame f) {
   }
   const int bi = by * xb + bx;
   const uint8_t* qf = f.qf;  // the pre-selection field
+  float m_site = 1.0f;
+  if (S == kSt16x16 || S == kSt32x32) m_site = site_bias(f, s, bx * 8, by * 8, Shape<S>::W, sm.mag[0]);
   warp_coefficients<S>(f, bx, by, sm);
   if (S == kStDct) {
     const float qac = __fmul_rn(s.scale, static_cast<float>(qf[bi]));
@@ -462,21 +476,19 @@ __global__ void __launch_bounds__(128) k_cost(const __grid_constant__ Frame f) {
                                  static_cast<float>(region_quant(qf, xb, bx, by, 2, 2, s.distance)));
     const float csel = warp_rd<S>(f, s, sm, bx, by, qsel, kMetaR);
     const float creg = qreg == qsel ? csel : warp_rd<S>(f, s, sm, bx, by, qreg, kMetaR);
-    const float m = lane == 0 ? site_bias(f, s, bx * 8, by * 8, 16) : 0.0f;
     if (lane == 0) {
       s.c16s[bi] = csel;
       s.c16r[bi] = creg;
-      s.m16[bi] = m;
+      s.m16[bi] = m_site;
     }
   } else if (S == kSt32x32) {
     const float qac = __fmul_rn(s.scale,
                                 static_cast<float>(region_quant(qf, xb, bx, by, 4, 4, s.distance)));
     const float q = __fmul_rn(qac, warp_selection_scale<S>(s, sm, qac));
     const float c = warp_rd<S>(f, s, sm, bx, by, q, kMetaR);
-    const float m = lane == 0 ? site_bias(f, s, bx * 8, by * 8, 32) : 0.0f;
     if (lane == 0) {
       s.c32[bi] = c;
-      s.m32[bi] = m;
+      s.m32[bi] = m_site;
     }
   } else {
     constexpr int w = Shape<S>::COVX, h = Shape<S>::COVY;
@@ -617,14 +629,26 @@ struct SmallPlan {
   uint8_t cell[64], choice[64];
 };
 
+// The DP's state of one thread: two layers of costs and active lists, in
+// shared memory.
+struct SmallState {
+  float cost_a[512], cost_b[512];
+  uint16_t act_a[512], act_b[512];
+};
+constexpr int kRetileThreads = 16;
+constexpr size_t kRetileSmemBytes = kRetileThreads * sizeof(SmallState);
+
 __device__ float plan_small(const float* leaf, const float* wide, const float* tall,
                             const float* square, const uint8_t* live, uint64_t fixed, int w,
-                            int h, uint8_t* choices, float replace_below, SmallPlan* plan) {
+                            int h, uint8_t* choices, float replace_below, SmallPlan* plan,
+                            SmallState& st) {
   const int cells = w * h, states = 1 << (w + 1), mask = states - 1;
   const int below_bit = 1 << w;
   const int added[5] = {0, 0, 2, below_bit, 2 | below_bit | (2 << w)};
-  float cost_a[512], cost_b[512];
-  uint16_t act_a[512], act_b[512];
+  float* cost_a = st.cost_a;
+  float* cost_b = st.cost_b;
+  uint16_t* act_a = st.act_a;
+  uint16_t* act_b = st.act_b;
   for (int i = 0; i < states; ++i) cost_a[i] = cost_b[i] = INFINITY;
   float* cost = cost_a;
   float* next = cost_b;
@@ -698,7 +722,9 @@ __device__ __forceinline__ bool piece_in(const Piece* set, int n, Piece p) {
   return false;
 }
 
-__global__ void __launch_bounds__(64) k_retile(const __grid_constant__ Frame f) {
+__global__ void __launch_bounds__(kRetileThreads) k_retile(const __grid_constant__ Frame f) {
+  extern __shared__ __align__(16) unsigned char retile_smem_raw[];
+  SmallState& dp = reinterpret_cast<SmallState*>(retile_smem_raw)[threadIdx.x];
   const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
   const int xb = f.a.xb, yb = f.a.yb;
   const int tx = (xb + 7) / 8, ty = (yb + 7) / 8;
@@ -775,12 +801,12 @@ __global__ void __launch_bounds__(64) k_retile(const __grid_constant__ Frame f) 
   SmallPlan plan;
   plan.n = 0;
   const float around = __fadd_rn(plan_small(leaf, wide, tall, square, live, fixed, w, h, choices,
-                                            INFINITY, &plan),
+                                            INFINITY, &plan, dp),
                                  fixed_cost);
   bool keep_fixed = true;
   float winner = around;
   if (fixed != 0) {
-    const float over = plan_small(leaf, wide, tall, square, live, 0, w, h, choices, around, &plan);
+    const float over = plan_small(leaf, wide, tall, square, live, 0, w, h, choices, around, &plan, dp);
     if (over < around) {
       winner = over;
       keep_fixed = false;
@@ -870,6 +896,14 @@ __device__ __forceinline__ void mh_incumbent_warp(const Frame& f, const SearchFr
                                                   int by, unsigned char* raw) {
   CostSmem<S>& sm = reinterpret_cast<CostSmem<S>*>(raw)[threadIdx.x >> 5];
   const int b = by * f.a.xb + bx;
+  // the search priced this transform at the aggregate of the pre-selection
+  // field (region_qac), the value adjust_quant_field gives it unless the
+  // alpha factors moved it: the same cost, no need to recompute
+  const uint8_t agg = region_quant(s.block_qf, f.a.xb, bx, by, Shape<S>::COVX, Shape<S>::COVY, s.distance);
+  if (f.qf[b] == agg) {
+    if ((threadIdx.x & 31) == 0) s.mh_inc[b] = S == kSt16x16 ? s.c16r[b] : s.c32[b];
+    return;
+  }
   warp_coefficients<S>(f, bx, by, sm);
   const float qac = __fmul_rn(s.scale, static_cast<float>(f.qf[b]));
   const float q = __fmul_rn(qac, warp_selection_scale<S>(s, sm, qac));
@@ -881,12 +915,15 @@ __global__ void __launch_bounds__(128) k_mh_incumbent(const __grid_constant__ Fr
   extern __shared__ __align__(16) unsigned char mh_smem_raw[];
   const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
   const int xb = f.a.xb, yb = f.a.yb;
-  const int64_t b = static_cast<int64_t>(blockIdx.x) * 4 + (threadIdx.x >> 5);
-  if (b >= static_cast<int64_t>(xb) * yb) return;
+  // sites sit at even block coordinates
+  const int nx = (xb + 1) / 2;
+  const int64_t e = static_cast<int64_t>(blockIdx.x) * 4 + (threadIdx.x >> 5);
+  if (e >= static_cast<int64_t>(nx) * ((yb + 1) / 2)) return;
+  const int bx = 2 * static_cast<int>(e % nx), by = 2 * static_cast<int>(e / nx);
+  const int64_t b = static_cast<int64_t>(by) * xb + bx;
   const uint8_t cell = s.map[b];
   if (!(cell & 1)) return;
   const int st = cell >> 1;
-  const int bx = static_cast<int>(b % xb), by = static_cast<int>(b / xb);
   if (st == kSt16x16 && (s.p.custom & 2u)) mh_incumbent_warp<kSt16x16>(f, s, bx, by, mh_smem_raw);
   else if (st == kSt32x32 && (s.p.custom & 4u)) mh_incumbent_warp<kSt32x32>(f, s, bx, by, mh_smem_raw);
 }
@@ -899,36 +936,39 @@ __device__ __forceinline__ uint32_t header_bits(const SearchFrame& s, uint32_t u
 }
 
 constexpr int kMhThreads = 1024;
-// One CTA: the sites in DC-group order, each site's alternatives, the
-// families a lower bound pins, the cheapest table set (every subset's sum
-// over the sites in order: losses are non-negative, so the reference's early
-// exit never changes which set wins), and the chosen alternatives.
+// One CTA: the sites in DC-group order, as two lists (16x16 sites, then
+// 32x32 sites: the order in which the reference sums its regions), each
+// site's alternatives, the families a lower bound pins, the cheapest table
+// set (every subset's sum over the sites in order; losses are non-negative,
+// so the reference's early exit never changes which set wins), and the
+// chosen alternatives.
 __global__ void __launch_bounds__(kMhThreads) k_mh_choose(const __grid_constant__ Frame f) {
   const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
   const int xb = f.a.xb, yb = f.a.yb;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  __shared__ uint32_t s_used, s_count, s_warp[32];
-  __shared__ double s_unavoidable[3];
+  __shared__ uint32_t s_used, s_n[2], s_warp[2][32];
+  __shared__ double s_unavoidable[2];
   __shared__ uint32_t s_pinned, s_best;
   __shared__ double s_subset_cost[64];
   if (tid == 0) {
     s_used = 0;
-    s_count = 0;
+    s_n[0] = s_n[1] = 0;
   }
   __syncthreads();
   const int xdc = (xb + 255) / 256, ydc = (yb + 255) / 256;
   uint32_t used_local = 0;
   const int64_t nb = static_cast<int64_t>(xb) * yb;
+  uint32_t* list16 = s.sites;
+  uint32_t* list32 = s.sites + nb / 2;
   // enumerate blocks in DC-group order, raster within each DC group
   for (int64_t base = 0; base < nb; base += kMhThreads) {
     const int64_t k = base + tid;
-    bool site = false;
+    int fam = -1;
     int b = -1;
     if (k < nb) {
-      // DC group g holds blocks [start_g, start_g + size_g) of the order
       int64_t rem = k;
-      int g = 0, gx0 = 0, gy0 = 0, gw = 0, gh = 0;
-      for (g = 0; g < xdc * ydc; ++g) {
+      int gx0 = 0, gy0 = 0, gw = 0, gh = 0;
+      for (int g = 0; g < xdc * ydc; ++g) {
         gx0 = (g % xdc) * 256;
         gy0 = (g / xdc) * 256;
         gw = imin(256, xb - gx0);
@@ -943,74 +983,98 @@ __global__ void __launch_bounds__(kMhThreads) k_mh_choose(const __grid_constant_
         const uint32_t slot = st == kStDct ? 0u : st == kSt16x16 ? 1u : st == kSt32x32 ? 2u : 3u;
         if (s.p.custom & (1u << slot)) {
           used_local |= 1u << slot;
-          site = slot != 0u;
+          if (slot == 1u || slot == 2u) fam = static_cast<int>(slot) - 1;
         }
       }
     }
-    const unsigned ballot = __ballot_sync(0xffffffffu, site);
-    if (lane == 0) s_warp[warp] = __popc(ballot);
+    const unsigned b0 = __ballot_sync(0xffffffffu, fam == 0), b1 = __ballot_sync(0xffffffffu, fam == 1);
+    if (lane == 0) {
+      s_warp[0][warp] = __popc(b0);
+      s_warp[1][warp] = __popc(b1);
+    }
     __syncthreads();
-    uint32_t before = 0;
-    for (int w = 0; w < warp; ++w) before += s_warp[w];
-    uint32_t total = 0;
-    for (int w = 0; w < 32; ++w) total += s_warp[w];
-    if (site) s.sites[s_count + before + __popc(ballot & ((1u << lane) - 1u))] = static_cast<uint32_t>(b);
+    if (fam >= 0) {
+      uint32_t before = 0;
+      for (int w = 0; w < warp; ++w) before += s_warp[fam][w];
+      const unsigned bal = fam == 0 ? b0 : b1;
+      (fam == 0 ? list16 : list32)[s_n[fam] + before + __popc(bal & ((1u << lane) - 1u))] =
+          static_cast<uint32_t>(b);
+    }
     __syncthreads();
-    if (tid == 0) s_count += total;
+    if (tid < 2) {
+      uint32_t total = 0;
+      for (int w = 0; w < 32; ++w) total += s_warp[tid][w];
+      s_n[tid] += total;
+    }
     __syncthreads();
   }
   atomicOr(&s_used, used_local);
   __syncthreads();
-  const uint32_t used = s_used, count = s_count;
+  const uint32_t used = s_used, n16 = s_n[0], n32 = s_n[1], count = n16 + n32;
   if ((used & ~1u) == 0u) return;
-  const double inv_lambda_unit = static_cast<double>(kRdLambda);
-  // per site: the DCT alternative's and (32x32) the 16x16 alternative's loss
-  auto site_losses = [&](uint32_t b, double* l_dct, double* l_16, int* st_out) {
-    const int st = s.map[b] >> 1, cx = cov_x_of(st), cy = cov_y_of(st);
-    *st_out = st;
-    const double inc = static_cast<double>(s.mh_inc[b]) / inv_lambda_unit;
+  const double lambda = static_cast<double>(kRdLambda);
+  // every site's losses, family-major: the DCT alternative's and (32x32)
+  // the 16x16 alternative's, -1 where the alternative is absent
+  double* loss = s.mh_loss;
+  for (uint32_t k = tid; k < count; k += kMhThreads) {
+    const uint32_t b = k < n16 ? list16[k] : list32[k - n16];
+    const int st = k < n16 ? kSt16x16 : kSt32x32, cx = cov_x_of(st), cy = cov_y_of(st);
+    const double inc = static_cast<double>(s.mh_inc[b]) / lambda;
     double c = 0.0;
     for (int iy = 0; iy < cy; ++iy)
       for (int ix = 0; ix < cx; ++ix)
-        c = __dadd_rn(c, static_cast<double>(s.c8[b + iy * xb + ix]) / inv_lambda_unit);
-    *l_dct = (isfinite(c) && isfinite(inc)) ? fmax(c - inc, 0.0) : -1.0;
-    *l_16 = -1.0;
+        c = __dadd_rn(c, static_cast<double>(s.c8[b + iy * xb + ix]) / lambda);
+    loss[2 * k] = (isfinite(c) && isfinite(inc)) ? fmax(c - inc, 0.0) : -1.0;
+    double l16 = -1.0;
     if (st == kSt32x32) {
       double c2 = 0.0;
       for (int iy = 0; iy < 4; iy += 2)
         for (int ix = 0; ix < 4; ix += 2)
-          c2 = __dadd_rn(c2, static_cast<double>(s.c16r[b + iy * xb + ix]) / inv_lambda_unit);
-      *l_16 = (isfinite(c2) && isfinite(inc)) ? fmax(c2 - inc, 0.0) : -1.0;
+          c2 = __dadd_rn(c2, static_cast<double>(s.c16r[b + iy * xb + ix]) / lambda);
+      l16 = (isfinite(c2) && isfinite(inc)) ? fmax(c2 - inc, 0.0) : -1.0;
     }
-  };
-  // the families' unavoidable losses, in site order (thread 1: slot 1, thread 2: slot 2)
-  if (tid == 1 || tid == 2) {
+    loss[2 * k + 1] = l16;
+  }
+  __syncthreads();
+  // the families' unavoidable losses in site order (thread 0: 16x16, 32: 32x32)
+  if (tid == 0 || tid == 32) {
+    const uint32_t lo = tid == 0 ? 0u : n16, hi = tid == 0 ? n16 : count;
     double u = 0.0;
-    for (uint32_t k = 0; k < count; ++k) {
-      const uint32_t b = s.sites[k];
-      double ld, l16;
-      int st;
-      site_losses(b, &ld, &l16, &st);
-      const int slot = st == kSt16x16 ? 1 : 2;
-      if (slot != tid) continue;
+#pragma unroll 8
+    for (uint32_t k = lo; k < hi; ++k) {
+      const double ld = loss[2 * k], l16 = loss[2 * k + 1];
       double mn = INFINITY;
       if (ld >= 0.0) mn = fmin(mn, ld);
       if (l16 >= 0.0) mn = fmin(mn, l16);
       u = __dadd_rn(u, mn);
     }
-    s_unavoidable[tid] = u;
+    s_unavoidable[tid == 0 ? 0 : 1] = u;
   }
   __syncthreads();
   if (tid == 0) {
     uint32_t pinned = used & 1u;
     for (int slot = 1; slot <= 2; ++slot)
       if ((used & (1u << slot)) &&
-          s_unavoidable[slot] > static_cast<double>(s.p.payload[slot] + 17u * 3u))
+          s_unavoidable[slot - 1] > static_cast<double>(s.p.payload[slot] + 17u * 3u))
         pinned |= 1u << slot;
     s_pinned = pinned;
   }
   __syncthreads();
   const uint32_t pinned = s_pinned, custom = s.p.custom;
+  // best_alternative (matrix_overhead.rs:50-63) of site k under `allowed`:
+  // incumbent (requires its own slot), DCT (slot 0 when custom), 16x16
+  // (slot 1 when custom); strict `<` keeps the earlier one on a tie
+  auto best_of = [&](uint32_t k, uint32_t allowed, int* which) -> double {
+    const uint32_t slot = k < n16 ? 1u : 2u;
+    const double ld = loss[2 * k], l16 = loss[2 * k + 1];
+    double best = INFINITY;
+    bool any = false;
+    *which = 0;
+    if (((1u << slot) & ~allowed) == 0u) { best = 0.0; any = true; }
+    if (ld >= 0.0 && ((1u & custom) & ~allowed) == 0u && (!any || ld < best)) { best = ld; any = true; *which = 1; }
+    if (l16 >= 0.0 && ((2u & custom) & ~allowed) == 0u && (!any || l16 < best)) { best = l16; any = true; *which = 2; }
+    return any ? best : INFINITY;
+  };
   // subsets of `custom` in the reference's order: custom, then
   // (prev - 1) & custom down to 0; thread j takes the j-th
   const int nsub = 1 << __popc(custom);
@@ -1020,24 +1084,13 @@ __global__ void __launch_bounds__(kMhThreads) k_mh_choose(const __grid_constant_
     double cost = INFINITY;
     if ((pinned & ~allowed) == 0u) {
       cost = static_cast<double>(header_bits(s, allowed));
-      // the regions family by family (16x16 sites, then 32x32), each in site order
-      for (uint32_t k2 = 0; k2 < 2 * count; ++k2) {
-        const uint32_t fam = k2 < count ? 1u : 2u;
-        const uint32_t b = s.sites[k2 < count ? k2 : k2 - count];
-        double ld, l16;
-        int st;
-        site_losses(b, &ld, &l16, &st);
-        const uint32_t slot = st == kSt16x16 ? 1u : 2u;
-        if (slot != fam) continue;
-        if (pinned & (1u << slot)) continue;  // a pinned family's regions were dropped
-        // best_alternative: incumbent (requires its slot), DCT (requires
-        // slot 0 when custom), 16x16 (slot 1 when custom); strict `<`
-        double best = INFINITY;
-        bool any = false;
-        if (((1u << slot) & ~allowed) == 0u) { best = 0.0; any = true; }
-        if (ld >= 0.0 && ((1u & custom) & ~allowed) == 0u && (!any || ld < best)) { best = ld; any = true; }
-        if (l16 >= 0.0 && ((2u & custom) & ~allowed) == 0u && (!any || l16 < best)) { best = l16; any = true; }
-        cost = __dadd_rn(cost, any ? best : INFINITY);
+      // a pinned family's regions were dropped
+      const uint32_t lo = (pinned & 2u) ? n16 : 0u;
+      const uint32_t hi = (pinned & 4u) ? n16 : count;
+#pragma unroll 8
+      for (uint32_t k = lo; k < hi; ++k) {
+        int which;
+        cost = __dadd_rn(cost, best_of(k, allowed, &which));
       }
     }
     s_subset_cost[tid] = cost;
@@ -1060,19 +1113,14 @@ __global__ void __launch_bounds__(kMhThreads) k_mh_choose(const __grid_constant_
   const uint32_t best = s_best;
   if (best == used) return;
   for (uint32_t k = tid; k < count; k += kMhThreads) {
-    const uint32_t b = s.sites[k];
-    double ld, l16;
-    int st;
-    site_losses(b, &ld, &l16, &st);
-    const uint32_t slot = st == kSt16x16 ? 1u : 2u;
+    const uint32_t slot = k < n16 ? 1u : 2u;
     if (pinned & (1u << slot)) continue;
-    int chosen = st;
-    double bestl = INFINITY;
-    bool any = false;
-    if (((1u << slot) & ~best) == 0u) { bestl = 0.0; any = true; }
-    if (ld >= 0.0 && ((1u & custom) & ~best) == 0u && (!any || ld < bestl)) { bestl = ld; any = true; chosen = kStDct; }
-    if (l16 >= 0.0 && ((2u & custom) & ~best) == 0u && (!any || l16 < bestl)) { bestl = l16; any = true; chosen = kSt16x16; }
-    if (chosen == st) continue;
+    int which;
+    best_of(k, best, &which);
+    if (which == 0) continue;
+    const int chosen = which == 1 ? kStDct : kSt16x16;
+    const uint32_t b = k < n16 ? list16[k] : list32[k - n16];
+    const int st = slot == 2u ? kSt32x32 : kSt16x16;
     const int bx = static_cast<int>(b % xb), by = static_cast<int>(b / xb);
     const int w = cov_x_of(st), h = cov_y_of(st), cx = cov_x_of(chosen), cy = cov_y_of(chosen);
     for (int yy = 0; yy < h; yy += cy)
@@ -1491,6 +1539,7 @@ inline cudaError_t set_search_attributes() {
   set(reinterpret_cast<const void*>(k_cost<kSt32x32>), cost_smem_bytes<kSt32x32>());
   set(reinterpret_cast<const void*>(k_mh_incumbent), cost_smem_bytes<kSt32x32>());
   set(reinterpret_cast<const void*>(k_layout_tile), kLayoutSmemBytes);
+  set(reinterpret_cast<const void*>(k_retile), kRetileSmemBytes);
   return e;
 }
 
