@@ -91,6 +91,10 @@ struct SearchParams {
   int32_t headers;        // account_matrix_headers can change the layout (d >= 2.25)
   uint32_t payload[13];   // MatrixHeaderCost (src/quant_weights.rs:54-101)
   uint32_t custom;        // its custom mask
+  // 1: every f64 running sum the reference keeps is taken serially in its
+  // order, never settled from a parallel sum's error interval (the
+  // environment variable JXG_SERIAL_SUMS=1 sets it; results are the same)
+  int32_t serial_sums;
 };
 
 // Speed::Fastest's transform search runs (not the DCT8-only shortcut,

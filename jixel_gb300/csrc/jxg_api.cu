@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -363,6 +364,11 @@ SearchTables* search_tables_for(Context* c, const DistanceParams& dp) {
 }
 
 constexpr size_t kSearchFrameBytes = (sizeof(SearchFrame) + 255) / 256 * 256;
+// k_mh_sum's CTAs: one thread per 2x2-block cell
+size_t mh_sum_ctas(const FrameLayout& L) {
+  const size_t cells = ((L.info.xsize_blocks + 1) / 2) * ((L.info.ysize_blocks + 1) / 2);
+  return (cells + kMhSumThreads - 1) / kMhSumThreads;
+}
 
 // Lays out a pass of `n` frames in the context's buffers, sizes them, and
 // fills the pinned plan (frame descriptors + chunk prefixes).  No launch.
@@ -558,7 +564,8 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     const size_t tiles8 = L.info.xsize_tiles * L.info.ysize_tiles;
     if ((st = ensure(c, c->search_costs, 9 * nb * 4)) || (st = ensure(c, c->search_map, nb)) ||
         (st = ensure(c, c->search_bqf, nb)) || (st = ensure(c, c->search_dp, tiles8 * 64 * 512)) ||
-        (st = ensure(c, c->search_sites, nb * 4)) || (st = ensure(c, c->search_loss, nb * 16)))
+        (st = ensure(c, c->search_sites, nb * 5)) ||
+        (st = ensure(c, c->search_loss, nb * 16 + mh_sum_ctas(L) * kMhQuantities * 8 + 64)))
       return st;
     SearchFrame& sf = c->search_host;
     sf = SearchFrame{};
@@ -578,7 +585,12 @@ int plan_pass(Context* c, const PassImage* imgs, int n, bool pixels_on_device, b
     sf.block_qf = static_cast<uint8_t*>(c->search_bqf.ptr);
     sf.dp_choices = static_cast<uint8_t*>(c->search_dp.ptr);
     sf.sites = static_cast<uint32_t*>(c->search_sites.ptr);
+    sf.mh_kind = reinterpret_cast<uint8_t*>(sf.sites + nb);
     sf.mh_loss = static_cast<double*>(c->search_loss.ptr);
+    sf.mh_part = sf.mh_loss + 2 * nb;
+    sf.mh_decision = reinterpret_cast<uint32_t*>(sf.mh_part + mh_sum_ctas(L) * kMhQuantities);
+    const char* serial = std::getenv("JXG_SERIAL_SUMS");
+    sf.p.serial_sums = serial && serial[0] == '1' ? 1 : 0;
     const size_t search_off = plan_bytes - kSearchFrameBytes;
     std::memcpy(plan_h + search_off, &sf, sizeof(SearchFrame));
     frames[0].search = static_cast<char*>(c->plan.ptr) + c->plan_slot * c->plan_slot_cap + search_off;
@@ -621,23 +633,35 @@ int enqueue_search(Context* c, const Frame& f, bool timed) {
                 k_cost<kSt32x32><<<grid4(n32), 128, cost_smem_bytes<kSt32x32>(), s>>>(f);
               })))
     return st;
+  if (n32 + n16 && (st = launch(c, "k_site", timed, [&] {
+                      k_site<<<static_cast<unsigned>((n32 + n16 + 63) / 64), 64, 0, s>>>(f);
+                    })))
+    return st;
   const int64_t cells = ((xb + 3) / 4) * ((yb + 3) / 4);
   if ((st = launch(c, "k_select", timed, [&] {
          k_select<<<static_cast<unsigned>((cells + 127) / 128), 128, 0, s>>>(f);
        })) ||
       (st = launch(c, "k_retile", timed, [&] {
-         k_retile<<<static_cast<unsigned>((tiles + kRetileThreads - 1) / kRetileThreads),
-                    kRetileThreads, kRetileSmemBytes, s>>>(f);
+         k_retile<<<static_cast<unsigned>((tiles + kRetileWarps - 1) / kRetileWarps),
+                    32 * kRetileWarps, kRetileSmemBytes, s>>>(f);
        })) ||
       (st = launch(c, "k_adjust", timed, [&] {
          k_adjust<<<static_cast<unsigned>((nb + 255) / 256), 256, 0, s>>>(f);
        })))
     return st;
+  const int64_t cells2 = ((xb + 1) / 2) * ((yb + 1) / 2);
+  const int parts = static_cast<int>(mh_sum_ctas(L));
   if (sf.p.headers &&
       ((st = launch(c, "k_mh_incumbent", timed, [&] {
-          k_mh_incumbent<<<grid4(((xb + 1) / 2) * ((yb + 1) / 2)), 128, cost_smem_bytes<kSt32x32>(), s>>>(f);
+          k_mh_incumbent<<<grid4(cells2), 128, cost_smem_bytes<kSt32x32>(), s>>>(f);
         })) ||
-       (st = launch(c, "k_mh_choose", timed, [&] { k_mh_choose<<<1, kMhThreads, 0, s>>>(f); }))))
+       (st = launch(c, "k_mh_sum", timed, [&] {
+          k_mh_sum<<<static_cast<unsigned>(parts), kMhSumThreads, 0, s>>>(f);
+        })) ||
+       (st = launch(c, "k_mh_choose", timed, [&] { k_mh_choose<<<1, kMhThreads, 0, s>>>(f, parts); })) ||
+       (st = launch(c, "k_mh_apply", timed, [&] {
+          k_mh_apply<<<static_cast<unsigned>((cells2 + 255) / 256), 256, 0, s>>>(f);
+        }))))
     return st;
   if ((st = launch(c, "k_qf_median", timed, [&] { k_qf_median<<<1, 256, 0, s>>>(f); })) ||
       (st = launch(c, "k_layout_tile", timed, [&] {

@@ -7,25 +7,31 @@
 //                      rate/distortion cost (strategy_cost, src/ac_strategy.rs:724,
 //                      :1295-1378; channel_rd / sse_and_rate / model_bits,
 //                      src/inflated_cost.rs:435-547) at the quantizer each
-//                      consumer prices it with, plus the per-site merge bias
+//                      consumer prices it with;
+//   k_site             one thread per 16x16 / 32x32 site: the merge bias
 //                      (site_bias, src/ac_strategy.rs:210-268);
 //   k_select           one thread per 4x4-block cell: select_band /
 //                      select_super_block in the squares scope
 //                      (src/ac_strategy/selection.rs:238-475, :1000-1245);
-//   k_retile           one thread per 8x8-block tile: retile_coefficient's
+//   k_retile           one warp per 8x8-block tile: retile_coefficient's
 //                      exact broken-profile DP (src/ac_strategy/selection/
 //                      layout_dp.rs:1811-2198);
 //   k_adjust           adjust_quant_field (selection.rs:503-527) and the
 //                      alpha factors over the layout (src/adaptive_quant.rs:1036);
-//   k_mh_incumbent / k_mh_choose   account_matrix_headers
+//   k_mh_incumbent, k_mh_sum, k_mh_choose, k_mh_apply   account_matrix_headers
 //                      (src/ac_strategy/matrix_overhead.rs:117-268) where the
 //                      16x16 / 32x32 tables are custom (d >= 2.25);
 //   k_qf_median        ac_qf_threshold over the final field;
 //   k_layout_tile      write_ac_group for every transform (src/group.rs:1259-2426);
 //   k_tokenize_layout  the tokens and histograms (src/group.rs:2428-2660).
 // Every float operation keeps the reference's order: per-coefficient terms
-// are computed in parallel, and each running sum the reference keeps is
-// summed by one lane in the reference's order.
+// are computed in parallel, and each f32 running sum the reference keeps is
+// summed by one lane in the reference's order.  An f64 running sum that is
+// only compared or rounded to f32 (the selection quantizer's erased energy,
+// the matrix-header sums) is summed in parallel and settled from an error
+// interval that provably holds the serial sum, with the serial sum taken
+// whenever the interval leaves the outcome open; the other f64 sums (site
+// variance) run serially, one site per lane.
 #pragma once
 
 namespace jxg {
@@ -69,8 +75,11 @@ struct SearchFrame {
   float *c8, *c16s, *c16r, *cw, *ct, *c32, *m16, *m32, *mh_inc;
   uint8_t *map, *block_qf;
   uint8_t* dp_choices;  // 32 KB per 8x8-block tile
-  uint32_t* sites;      // matrix-header sites in DC-group order
-  double* mh_loss;      // per site: the DCT and 16x16 alternatives' losses
+  uint32_t* sites;      // matrix-header sites in DC-group order (serial path)
+  uint8_t* mh_kind;     // per block: the table slot of the site there, 0 for none
+  double* mh_loss;      // per block at a site: the DCT and 16x16 alternatives' losses
+  double* mh_part;      // k_mh_sum's partials, kMhQuantities per CTA
+  uint32_t* mh_decision;  // {chosen table set, pinned families, used set}
 };
 
 // ---------------------------------------------------------------------------
@@ -225,29 +234,44 @@ __device__ __forceinline__ void warp_coefficients(const Frame& f, int bx, int by
 
 // selection_quantizer::scale (src/ac_strategy/selection_quantizer.rs:78-125):
 // only DCT32X32 here; the erased energy is an f64 sum in raster order.
+//
+// The serial f64 sum R is only ever read as an f32.  The warp sums the same
+// non-negative terms in parallel (P); |R - P| <= (n + 36) u E for n <= 960
+// terms (u = 2^-53, E the exact sum; error bounds of recursive and pairwise
+// summation), below M = 2^-42 P.  Rounding to f32 is monotonic, so when
+// P - M and P + M round to the same f32 that f32 is R's; otherwise lane 0
+// takes the serial sum.
 template <int S>
 __device__ __forceinline__ float warp_selection_scale(const SearchFrame& s, const CostSmem<S>& sm,
                                                       float qac) {
   if (S != kSt32x32 || !s.p.sel_scale) return 1.0f;
   const int lane = threadIdx.x & 31;
-  float out = 1.0f;
-  if (lane == 0) {
-    const float* inv = s.t->inv32[1];
+  const float* inv = s.t->inv32[1];
+  auto erased_term = [&](int i) -> double {
+    const int y = i >> 5, x = i & 31;
+    if (x < 8 && y < 8) return 0.0;
+    const float l = sm.co[1][i];
+    return fabsf(__fmul_rn(__fmul_rn(l, __ldg(inv + i)), qac)) < 0.5f
+               ? __dmul_rn(static_cast<double>(l), static_cast<double>(l))
+               : 0.0;
+  };
+  double part = 0.0;
+#pragma unroll 4
+  for (int i = lane; i < 1024; i += 32) part = __dadd_rn(part, erased_term(i));
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) part = __dadd_rn(part, __shfl_xor_sync(0xffffffffu, part, d));
+  const double margin = __dmul_rn(part, 0x1p-42);
+  float erased = static_cast<float>(__dsub_rn(part, margin));
+  const bool settled = erased == static_cast<float>(__dadd_rn(part, margin)) && !s.p.serial_sums;
+  if (!settled) {
     double energy = 0.0;
-    for (int y = 0; y < 32; ++y)
-      for (int x = 0; x < 32; ++x) {
-        if (x < 8 && y < 8) continue;
-        const int i = y * 32 + x;
-        const float l = sm.co[1][i];
-        if (fabsf(__fmul_rn(__fmul_rn(l, inv[i]), qac)) < 0.5f)
-          energy = __dadd_rn(energy, __dmul_rn(static_cast<double>(l), static_cast<double>(l)));
-      }
-    const float erased = static_cast<float>(energy);
-    const float d = s.distance;
-    const float r = __fsub_rn(__fdiv_rn(erased, __fmul_rn(__fmul_rn(2e-4f, d), d)), 1.0f);
-    out = __fadd_rn(1.0f, __fmul_rn(0.6f, fminf(fmaxf(r, 0.0f), 1.0f)));
+    if (lane == 0)
+      for (int i = 0; i < 1024; ++i) energy = __dadd_rn(energy, erased_term(i));
+    erased = __shfl_sync(0xffffffffu, static_cast<float>(energy), 0);
   }
-  return __shfl_sync(0xffffffffu, out, 0);
+  const float d = s.distance;
+  const float r = __fsub_rn(__fdiv_rn(erased, __fmul_rn(__fmul_rn(2e-4f, d), d)), 1.0f);
+  return __fadd_rn(1.0f, __fmul_rn(0.6f, fminf(fmaxf(r, 0.0f), 1.0f)));
 }
 
 // The coefficient-model cost at quantizer `q` (already scaled by the
@@ -378,49 +402,67 @@ __device__ __forceinline__ float util_fast_exp(float x) {
   const float scale = __uint_as_float(static_cast<uint32_t>(exponent + 127) << 23);
   return __fmul_rn(__fadd_rn(1.0f, __fdiv_rn(__fmul_rn(2.0f, r), __fsub_rn(p, r))), scale);
 }
-// The warp stages the site's luma (clipped to the image) in `stage` (n * n
-// floats); lane 0 then takes the f64 sums in raster order.
-__device__ __forceinline__ float site_bias(const Frame& f, const SearchFrame& s, int x0, int y0,
-                                           int n, float* stage) {
-  if (s.p.site_k == 0.0f) return 1.0f;
-  const int lane = threadIdx.x & 31;
+// The merge bias of the n x n site at pixel (x0, y0), clipped to the image,
+// by one thread: the f64 sums run serially in raster order.  GB300's f64
+// pipe retires a warp instruction in tens of cycles whether one lane or 32
+// are active, so these sums run one site per lane (k_site), never one lane
+// per site.
+__device__ __forceinline__ float site_bias_thread(const Frame& f, const SearchFrame& s, int x0,
+                                                  int y0, int n) {
   const float* yp = f.xyb + f.a.plane;
   const int w = f.a.width, h = f.a.height;
-  const int y1 = imin(y0 + n, h), x1 = imin(x0 + n, w);
-  const int vw = x1 - x0, vh = y1 - y0;
-  for (int k = lane; k < vw * vh; k += 32)
-    stage[k] = __ldg(yp + static_cast<int64_t>(y0 + k / vw) * w + x0 + k % vw);
-  __syncwarp();
-  float out = 1.0f;
-  if (lane == 0) {
-    double s1 = 0.0, s2 = 0.0;
-    const int cnt = vw * vh;
-#pragma unroll 8
-    for (int k = 0; k < cnt; ++k) {
-      const double v = static_cast<double>(stage[k]);
+  const int vw = imin(x0 + n, w) - x0, vh = imin(y0 + n, h) - y0;
+  double s1 = 0.0, s2 = 0.0;
+  for (int y = 0; y < vh; ++y) {
+    const float* row = yp + static_cast<int64_t>(y0 + y) * w + x0;
+#pragma unroll 4
+    for (int x = 0; x < vw; ++x) {
+      const double v = static_cast<double>(__ldg(row + x));
       s1 = __dadd_rn(s1, v);
       s2 = __dadd_rn(s2, __dmul_rn(v, v));
     }
-    float var = 0.0f;
-    if (cnt) {
-      const double mean = __ddiv_rn(s1, static_cast<double>(cnt));
-      const double vv = __dsub_rn(__ddiv_rn(s2, static_cast<double>(cnt)), __dmul_rn(mean, mean));
-      var = static_cast<float>(vv > 0.0 ? vv : 0.0);
-    }
-    var = fmaxf(var, 1e-9f);
-    const float sv = fminf(fmaxf(__fdiv_rn(dirty_log2f(__fdiv_rn(var, 0.003f)), 8.0f), -1.0f), 1.0f);
-    out = util_fast_exp(__fmul_rn(s.p.site_k, sv));
   }
-  __syncwarp();
-  return __shfl_sync(0xffffffffu, out, 0);
+  const int cnt = vw * vh;
+  float var = 0.0f;
+  if (cnt) {
+    const double mean = __ddiv_rn(s1, static_cast<double>(cnt));
+    const double vv = __dsub_rn(__ddiv_rn(s2, static_cast<double>(cnt)), __dmul_rn(mean, mean));
+    var = static_cast<float>(vv > 0.0 ? vv : 0.0);
+  }
+  var = fmaxf(var, 1e-9f);
+  const float sv = fminf(fmaxf(__fdiv_rn(dirty_log2f(__fdiv_rn(var, 0.003f)), 8.0f), -1.0f), 1.0f);
+  return util_fast_exp(__fmul_rn(s.p.site_k, sv));
+}
+
+// One thread per merge site: the 32x32 sites (4-aligned) first, as they take
+// four times longer, then the 16x16 sites (even block coordinates).
+__global__ void __launch_bounds__(64) k_site(const __grid_constant__ Frame f) {
+  const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
+  const int xb = f.a.xb, yb = f.a.yb;
+  const int64_t n32 = static_cast<int64_t>(xb / 4) * (yb / 4);
+  const int64_t n16 = static_cast<int64_t>(xb / 2) * (yb / 2);
+  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= n32 + n16) return;
+  int bx, by, n;
+  float* out;
+  if (t < n32) {
+    const int nx = xb / 4;
+    bx = 4 * static_cast<int>(t % nx), by = 4 * static_cast<int>(t / nx), n = 32, out = s.m32;
+  } else {
+    const int nx = xb / 2;
+    const int64_t u = t - n32;
+    bx = 2 * static_cast<int>(u % nx), by = 2 * static_cast<int>(u / nx), n = 16, out = s.m16;
+  }
+  out[static_cast<int64_t>(by) * xb + bx] =
+      s.p.site_k == 0.0f ? 1.0f : site_bias_thread(f, s, bx * 8, by * 8, n);
 }
 
 // One warp per candidate of shape S: the costs every consumer of it reads.
 //   DCT8     every block, at scale * q (select_super_block's c8, the DP's leaves)
 //   16x16    even (bx, by): at aggregate_qac_2x2 (selection) and at region_qac
-//            (the DP's squares, the matrix-header alternatives), the site bias
+//            (the DP's squares, the matrix-header alternatives)
 //   8x16     even bx (the DP's horizontal pairs), 16x8 even by (vertical pairs)
-//   32x32    4-aligned: at region_qac with the selection quantizer, site bias
+//   32x32    4-aligned: at region_qac with the selection quantizer
 template <int S>
 __global__ void __launch_bounds__(128) k_cost(const __grid_constant__ Frame f) {
   extern __shared__ __align__(16) unsigned char cost_smem_raw[];
@@ -452,8 +494,6 @@ __global__ void __launch_bounds__(128) k_cost(const __grid_constant__ Frame f) {
   }
   const int bi = by * xb + bx;
   const uint8_t* qf = f.qf;  // the pre-selection field
-  float m_site = 1.0f;
-  if (S == kSt16x16 || S == kSt32x32) m_site = site_bias(f, s, bx * 8, by * 8, Shape<S>::W, sm.mag[0]);
   warp_coefficients<S>(f, bx, by, sm);
   if (S == kStDct) {
     const float qac = __fmul_rn(s.scale, static_cast<float>(qf[bi]));
@@ -479,17 +519,13 @@ __global__ void __launch_bounds__(128) k_cost(const __grid_constant__ Frame f) {
     if (lane == 0) {
       s.c16s[bi] = csel;
       s.c16r[bi] = creg;
-      s.m16[bi] = m_site;
     }
   } else if (S == kSt32x32) {
     const float qac = __fmul_rn(s.scale,
                                 static_cast<float>(region_quant(qf, xb, bx, by, 4, 4, s.distance)));
     const float q = __fmul_rn(qac, warp_selection_scale<S>(s, sm, qac));
     const float c = warp_rd<S>(f, s, sm, bx, by, q, kMetaR);
-    if (lane == 0) {
-      s.c32[bi] = c;
-      s.m32[bi] = m_site;
-    }
+    if (lane == 0) s.c32[bi] = c;
   } else {
     constexpr int w = Shape<S>::COVX, h = Shape<S>::COVY;
     const float qac = __fmul_rn(s.scale,
@@ -617,7 +653,7 @@ __global__ void __launch_bounds__(128) k_select(const __grid_constant__ Frame f)
 }
 
 // plan_small and search_tile_coefficient (src/ac_strategy/selection/
-// layout_dp.rs:1864-2198), one thread per tile.
+// layout_dp.rs:1864-2198), one warp per tile.
 constexpr int kSmallLeaf = 1, kSmallWide = 2, kSmallTall = 3, kSmallSquare = 4;
 __device__ __forceinline__ int small_strategy(int choice) {
   return choice == kSmallLeaf ? kStDct : choice == kSmallWide ? kSt8x16
@@ -629,86 +665,173 @@ struct SmallPlan {
   uint8_t cell[64], choice[64];
 };
 
-// The DP's state of one thread: two layers of costs and active lists, in
-// shared memory.
-struct SmallState {
-  float cost_a[512], cost_b[512];
+// One warp's DP state.  The reference walks a layer's active profiles in
+// order and relaxes each successor with a strict `<`, so a successor keeps
+// the cheapest relaxation and, among equal costs, the earliest; the next
+// layer lists the successors in the order they were first reached.  The
+// warp relaxes every profile at once: a successor's 64-bit key (the cost
+// mapped to an order-preserving integer, then the relaxation's rank a * 4 + k)
+// takes an atomicMin, so it ends at the same winner; `first` takes the
+// smallest rank that reached it, and a prefix over the lanes lays the next
+// layer out in that order.
+struct RetileSmem {
+  unsigned long long key_a[512], key_b[512];
+  uint32_t first[512];
   uint16_t act_a[512], act_b[512];
+  float leaf[64], wide[64], tall[64], square[64];
+  uint8_t live[64];
 };
-constexpr int kRetileThreads = 16;
-constexpr size_t kRetileSmemBytes = kRetileThreads * sizeof(SmallState);
+constexpr int kRetileWarps = 4;
+constexpr size_t kRetileSmemBytes = kRetileWarps * sizeof(RetileSmem);
+constexpr unsigned long long kNoKey = ~0ull;
 
-__device__ float plan_small(const float* leaf, const float* wide, const float* tall,
-                            const float* square, const uint8_t* live, uint64_t fixed, int w,
-                            int h, uint8_t* choices, float replace_below, SmallPlan* plan,
-                            SmallState& st) {
+__device__ __forceinline__ uint32_t ordered_bits(float v) {
+  const uint32_t u = __float_as_uint(__fadd_rn(v, 0.0f));  // -0 -> +0
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ordered_float(unsigned long long key) {
+  const uint32_t k = static_cast<uint32_t>(key >> 32);
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// The relaxations of active profile `state` at one cell, in the reference's
+// order: k = 0 keep (a filled cell) or leaf, 1 wide, 2 tall, 3 square; an
+// absent one has an infinite cost.
+struct Relax {
+  int to[4];
+  float cv[4];
+  uint8_t ch[4];
+  int n;
+};
+__device__ __forceinline__ void relaxations(int state, float here, int corner, int mask, int w,
+                                            int shapes, float lf, float wd, float tl, float sq,
+                                            Relax* r) {
+  const int below_bit = 1 << w;
+  r->n = 0;
+  auto add = [&](int filled, float cv, int ch) {
+    r->to[r->n] = ((filled >> 1) | corner) & mask;
+    r->cv[r->n] = cv;
+    r->ch[r->n] = static_cast<uint8_t>(ch);
+    ++r->n;
+  };
+  if (state & 1) {
+    add(state, here, 0);
+    return;
+  }
+  add(state, __fadd_rn(here, lf), kSmallLeaf);
+  const bool right = (state & 2) == 0, below = (state & below_bit) == 0;
+  if (right && (shapes & 1)) add(state | 2, __fadd_rn(here, wd), kSmallWide);
+  else add(0, INFINITY, 0);
+  if (below && (shapes & 2)) add(state | below_bit, __fadd_rn(here, tl), kSmallTall);
+  else add(0, INFINITY, 0);
+  if (right && below && corner == 0 && (shapes & 4))
+    add(state | 2 | below_bit | (2 << w), __fadd_rn(here, sq), kSmallSquare);
+  else add(0, INFINITY, 0);
+}
+
+// The whole warp calls it with the same arguments; the plan is written on lane 0.
+__device__ float plan_small(RetileSmem& sm, uint64_t fixed, int w, int h, uint8_t* choices,
+                            float replace_below, SmallPlan* plan) {
+  const int lane = threadIdx.x & 31;
   const int cells = w * h, states = 1 << (w + 1), mask = states - 1;
   const int below_bit = 1 << w;
-  const int added[5] = {0, 0, 2, below_bit, 2 | below_bit | (2 << w)};
-  float* cost_a = st.cost_a;
-  float* cost_b = st.cost_b;
-  uint16_t* act_a = st.act_a;
-  uint16_t* act_b = st.act_b;
-  for (int i = 0; i < states; ++i) cost_a[i] = cost_b[i] = INFINITY;
-  float* cost = cost_a;
-  float* next = cost_b;
-  uint16_t* active = act_a;
-  uint16_t* next_active = act_b;
+  unsigned long long* cur = sm.key_a;
+  unsigned long long* nxt = sm.key_b;
+  uint16_t* act = sm.act_a;
+  uint16_t* nact = sm.act_b;
+  for (int i = lane; i < states; i += 32) {
+    cur[i] = nxt[i] = kNoKey;
+    sm.first[i] = ~0u;
+  }
+  __syncwarp();
   const int start = static_cast<int>(fixed & static_cast<uint64_t>(mask));
-  cost[start] = 0.0f;
-  active[0] = static_cast<uint16_t>(start);
-  int active_len = 1;
+  if (lane == 0) {
+    cur[start] = static_cast<unsigned long long>(ordered_bits(0.0f)) << 32;
+    act[0] = static_cast<uint16_t>(start);
+  }
+  int len = 1;
   uint64_t incoming = fixed >> (w + 1);
+  __syncwarp();
   for (int i = 0; i < cells; ++i) {
     uint8_t* from = choices + i * states;
     const int corner = static_cast<int>(incoming & 1u) << w;
     incoming >>= 1;
-    const int shapes = live[i];
-    int next_len = 0;
-    for (int a = 0; a < active_len; ++a) {
-      const int state = active[a];
-      const float here = cost[state];
-      cost[state] = INFINITY;
-      auto relax = [&](int filled, float cv, int ch) {
-        const int to = ((filled >> 1) | corner) & mask;
-        if (cv < next[to]) {
-          if (next[to] == INFINITY) next_active[next_len++] = static_cast<uint16_t>(to);
-          next[to] = cv;
-          from[to] = static_cast<uint8_t>(ch);
+    const int shapes = sm.live[i];
+    const float lf = sm.leaf[i], wd = sm.wide[i], tl = sm.tall[i], sq = sm.square[i];
+    for (int a0 = 0; a0 < len; a0 += 32) {
+      const int a = a0 + lane;
+      if (a < len) {
+        const int state = act[a];
+        Relax r;
+        relaxations(state, ordered_float(cur[state]), corner, mask, w, shapes, lf, wd, tl, sq, &r);
+        for (int k = 0; k < r.n; ++k) {
+          if (!(r.cv[k] < INFINITY)) continue;
+          const uint32_t rank = static_cast<uint32_t>(a * 4 + k);
+          atomicMin(&nxt[r.to[k]], (static_cast<unsigned long long>(ordered_bits(r.cv[k])) << 32) | rank);
+          atomicMin(&sm.first[r.to[k]], rank);
         }
-      };
-      if (state & 1) {
-        relax(state, here, 0);
-        continue;
       }
-      relax(state, __fadd_rn(here, leaf[i]), kSmallLeaf);
-      const bool right = (state & 2) == 0, below = (state & below_bit) == 0;
-      if (right && (shapes & 1)) relax(state | 2, __fadd_rn(here, wide[i]), kSmallWide);
-      if (below && (shapes & 2)) relax(state | below_bit, __fadd_rn(here, tall[i]), kSmallTall);
-      if (right && below && corner == 0 && (shapes & 4))
-        relax(state | added[kSmallSquare], __fadd_rn(here, square[i]), kSmallSquare);
     }
-    float* tc = cost;
-    cost = next;
-    next = tc;
-    uint16_t* ta = active;
-    active = next_active;
-    next_active = ta;
-    active_len = next_len;
+    __syncwarp();
+    int nlen = 0;
+    for (int a0 = 0; a0 < len; a0 += 32) {
+      const int a = a0 + lane;
+      Relax r;
+      r.n = 0;
+      if (a < len) {
+        const int state = act[a];
+        relaxations(state, ordered_float(cur[state]), corner, mask, w, shapes, lf, wd, tl, sq, &r);
+      }
+      uint32_t own = 0;
+      for (int k = 0; k < r.n; ++k) {
+        if (!(r.cv[k] < INFINITY)) continue;
+        const uint32_t rank = static_cast<uint32_t>(a * 4 + k);
+        if (sm.first[r.to[k]] == rank) own |= 1u << k;
+        if (static_cast<uint32_t>(nxt[r.to[k]]) == rank) from[r.to[k]] = r.ch[k];
+      }
+      // exclusive prefix of the owned counts over the lanes (ranks ascend with the lane)
+      const int cnt = __popc(own);
+      int incl = cnt;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+      }
+      int pos = nlen + incl - cnt;
+      for (int k = 0; k < 4; ++k)
+        if (own & (1u << k)) nact[pos++] = static_cast<uint16_t>(r.to[k]);
+      nlen += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    __syncwarp();
+    for (int a = lane; a < nlen; a += 32) sm.first[nact[a]] = ~0u;
+    for (int a = lane; a < len; a += 32) cur[act[a]] = kNoKey;
+    __syncwarp();
+    unsigned long long* tk = cur;
+    cur = nxt;
+    nxt = tk;
+    uint16_t* ta = act;
+    act = nact;
+    nact = ta;
+    len = nlen;
   }
-  const float total = cost[0];
+  const float total = cur[0] == kNoKey ? INFINITY : ordered_float(cur[0]);
+  __syncwarp();
   if (!(isfinite(total) && total < replace_below)) return total;
-  plan->n = 0;
-  int state = 0;
-  for (int i = cells - 1; i >= 0; --i) {
-    const int choice = choices[i * states + state];
-    if (choice != 0) {
-      plan->cell[plan->n] = static_cast<uint8_t>(i);
-      plan->choice[plan->n] = static_cast<uint8_t>(choice);
-      ++plan->n;
+  if (lane == 0) {
+    const int added[5] = {0, 0, 2, below_bit, 2 | below_bit | (2 << w)};
+    plan->n = 0;
+    int state = 0;
+    for (int i = cells - 1; i >= 0; --i) {
+      const int choice = choices[i * states + state];
+      if (choice != 0) {
+        plan->cell[plan->n] = static_cast<uint8_t>(i);
+        plan->choice[plan->n] = static_cast<uint8_t>(choice);
+        ++plan->n;
+      }
+      state = (((state << 1) ^ added[choice]) & mask) | (choice == 0 ? 1 : 0);
     }
-    state = (((state << 1) ^ added[choice]) & mask) | (choice == 0 ? 1 : 0);
   }
+  __syncwarp();
   return total;
 }
 
@@ -722,13 +845,14 @@ __device__ __forceinline__ bool piece_in(const Piece* set, int n, Piece p) {
   return false;
 }
 
-__global__ void __launch_bounds__(kRetileThreads) k_retile(const __grid_constant__ Frame f) {
+__global__ void __launch_bounds__(32 * kRetileWarps) k_retile(const __grid_constant__ Frame f) {
   extern __shared__ __align__(16) unsigned char retile_smem_raw[];
-  SmallState& dp = reinterpret_cast<SmallState*>(retile_smem_raw)[threadIdx.x];
+  RetileSmem& sm = reinterpret_cast<RetileSmem*>(retile_smem_raw)[threadIdx.x >> 5];
   const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
+  const int lane = threadIdx.x & 31;
   const int xb = f.a.xb, yb = f.a.yb;
   const int tx = (xb + 7) / 8, ty = (yb + 7) / 8;
-  const int tile = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tile = blockIdx.x * kRetileWarps + (threadIdx.x >> 5);
   if (tile >= tx * ty) return;
   const int bx = 8 * (tile % tx), by = 8 * (tile / tx);
   const int w = imin(8, xb - bx), h = imin(8, yb - by);
@@ -745,74 +869,82 @@ __global__ void __launch_bounds__(kRetileThreads) k_retile(const __grid_constant
       default: return s.c32[b];
     }
   };
-  Piece current[64];
-  int ncur = 0;
-  for (int y = 0; y < h; ++y)
-    for (int x = 0; x < w; ++x) {
-      const uint8_t cell = map[(by + y) * xb + bx + x];
-      if (cell & 1) current[ncur++] = Piece{static_cast<int8_t>(x), static_cast<int8_t>(y), static_cast<int8_t>(cell >> 1)};
-    }
-  float leaf[64], wide[64], tall[64], square[64];
-  for (int i = 0; i < 64; ++i) leaf[i] = wide[i] = tall[i] = square[i] = INFINITY;
-  for (int y = 0; y < h; ++y)
-    for (int x = 0; x < w; ++x) {
-      const int i = y * w + x;
-      const int gx = bx + x, gy = by + y;
-      leaf[i] = score(Piece{static_cast<int8_t>(x), static_cast<int8_t>(y), kStDct});
-      if (x + 2 <= w && gx % 2 == 0 && can_place(xb, yb, gx, gy, kSt8x16))
-        wide[i] = score(Piece{static_cast<int8_t>(x), static_cast<int8_t>(y), kSt8x16});
-      if (y + 2 <= h && gy % 2 == 0 && can_place(xb, yb, gx, gy, kSt16x8))
-        tall[i] = score(Piece{static_cast<int8_t>(x), static_cast<int8_t>(y), kSt16x8});
-      if (x + 2 <= w && y + 2 <= h && gx % 2 == 0 && gy % 2 == 0 && can_place(xb, yb, gx, gy, kSt16x16))
-        square[i] = score(Piece{static_cast<int8_t>(x), static_cast<int8_t>(y), kSt16x16});
-    }
-  uint64_t fixed = 0;
-  float fixed_cost = 0.0f;
-  for (int k = 0; k < ncur; ++k) {
-    if (current[k].s <= kSt16x16) continue;
-    const Piece p = current[k];
-    const uint64_t row = (1ull << cov_x_of(p.s)) - 1ull;
-    for (int yy = 0; yy < cov_y_of(p.s); ++yy) fixed |= row << (p.y * w + p.x + yy * w);
-    fixed_cost = __fadd_rn(fixed_cost, score(p));
+  for (int i = lane; i < 64; i += 32) {
+    sm.leaf[i] = sm.wide[i] = sm.tall[i] = sm.square[i] = INFINITY;
+    sm.live[i] = 0;
   }
+  __syncwarp();
+  for (int i = lane; i < w * h; i += 32) {
+    const int x = i % w, y = i / w, gx = bx + x, gy = by + y;
+    const int8_t px = static_cast<int8_t>(x), py = static_cast<int8_t>(y);
+    sm.leaf[i] = score(Piece{px, py, kStDct});
+    if (x + 2 <= w && gx % 2 == 0 && can_place(xb, yb, gx, gy, kSt8x16))
+      sm.wide[i] = score(Piece{px, py, kSt8x16});
+    if (y + 2 <= h && gy % 2 == 0 && can_place(xb, yb, gx, gy, kSt16x8))
+      sm.tall[i] = score(Piece{px, py, kSt16x8});
+    if (x + 2 <= w && y + 2 <= h && gx % 2 == 0 && gy % 2 == 0 && can_place(xb, yb, gx, gy, kSt16x16))
+      sm.square[i] = score(Piece{px, py, kSt16x16});
+  }
+  __syncwarp();
   // SmallCosts::live_masks
-  uint8_t live[64];
-  for (int i = 0; i < 64; ++i) live[i] = 0;
-  for (int y = 0; y < h; ++y) {
-    const int st = y * w;
+  for (int i = lane; i < w * h; i += 32) {
+    const int x = i % w, y = i / w, st = y * w;
+    const float* leaf = sm.leaf;
+    uint8_t m = 0;
     if (y + 1 == h) {
-      for (int x = 0; x + 1 < w; ++x) live[st + x] = wide[st + x] < __fadd_rn(leaf[st + x], leaf[st + x + 1]);
-      continue;
-    }
-    const int bl = st + w;
-    for (int x = 0; x + 1 < w; ++x) {
+      if (x + 1 < w) m = sm.wide[st + x] < __fadd_rn(leaf[st + x], leaf[st + x + 1]);
+    } else if (x + 1 < w) {
+      const int bl = st + w;
       const float tl = leaf[st + x], tr = leaf[st + x + 1], bll = leaf[bl + x], brr = leaf[bl + x + 1];
       const float top_leaves = __fadd_rn(tl, tr);
       const float leaves = __fadd_rn(__fadd_rn(top_leaves, bll), brr);
-      const float wides = __fadd_rn(wide[st + x], wide[bl + x]);
-      const float talls = __fadd_rn(tall[st + x], tall[st + x + 1]);
-      live[st + x] = static_cast<uint8_t>((wide[st + x] < top_leaves ? 1 : 0) |
-                                          (tall[st + x] < __fadd_rn(tl, bll) ? 2 : 0) |
-                                          (square[st + x] < fminf(fminf(leaves, wides), talls) ? 4 : 0));
+      const float wides = __fadd_rn(sm.wide[st + x], sm.wide[bl + x]);
+      const float talls = __fadd_rn(sm.tall[st + x], sm.tall[st + x + 1]);
+      m = static_cast<uint8_t>((sm.wide[st + x] < top_leaves ? 1 : 0) |
+                               (sm.tall[st + x] < __fadd_rn(tl, bll) ? 2 : 0) |
+                               (sm.square[st + x] < fminf(fminf(leaves, wides), talls) ? 4 : 0));
+    } else {
+      m = sm.tall[st + x] < __fadd_rn(leaf[st + x], leaf[st + w + x]) ? 2 : 0;
     }
-    live[st + w - 1] = tall[st + w - 1] < __fadd_rn(leaf[st + w - 1], leaf[bl + w - 1]) ? 2 : 0;
+    sm.live[i] = m;
   }
+  // the tile's current pieces (raster order of first blocks) and the fixed
+  // (larger than 16x16) ones, on lane 0
+  Piece current[64];
+  int ncur = 0;
+  uint64_t fixed = 0;
+  float fixed_cost = 0.0f;
+  if (lane == 0) {
+    for (int y = 0; y < h; ++y)
+      for (int x = 0; x < w; ++x) {
+        const uint8_t cell = map[(by + y) * xb + bx + x];
+        if (cell & 1) current[ncur++] = Piece{static_cast<int8_t>(x), static_cast<int8_t>(y), static_cast<int8_t>(cell >> 1)};
+      }
+    for (int k = 0; k < ncur; ++k) {
+      if (current[k].s <= kSt16x16) continue;
+      const Piece p = current[k];
+      const uint64_t row = (1ull << cov_x_of(p.s)) - 1ull;
+      for (int yy = 0; yy < cov_y_of(p.s); ++yy) fixed |= row << (p.y * w + p.x + yy * w);
+      fixed_cost = __fadd_rn(fixed_cost, score(p));
+    }
+  }
+  fixed = __shfl_sync(0xffffffffu, fixed, 0);
+  fixed_cost = __shfl_sync(0xffffffffu, fixed_cost, 0);
+  __syncwarp();
   uint8_t* choices = s.dp_choices + static_cast<int64_t>(tile) * 64 * 512;
   SmallPlan plan;
   plan.n = 0;
-  const float around = __fadd_rn(plan_small(leaf, wide, tall, square, live, fixed, w, h, choices,
-                                            INFINITY, &plan, dp),
-                                 fixed_cost);
+  const float around = __fadd_rn(plan_small(sm, fixed, w, h, choices, INFINITY, &plan), fixed_cost);
   bool keep_fixed = true;
   float winner = around;
   if (fixed != 0) {
-    const float over = plan_small(leaf, wide, tall, square, live, 0, w, h, choices, around, &plan, dp);
+    const float over = plan_small(sm, 0, w, h, choices, around, &plan);
     if (over < around) {
       winner = over;
       keep_fixed = false;
     }
   }
-  if (!isfinite(winner)) return;
+  if (lane != 0 || !isfinite(winner)) return;
   Piece layout[64];
   int nl = 0;
   for (int k = 0; k < plan.n; ++k) {
@@ -928,6 +1060,145 @@ __global__ void __launch_bounds__(128) k_mh_incumbent(const __grid_constant__ Fr
   else if (st == kSt32x32 && (s.p.custom & 4u)) mh_incumbent_warp<kSt32x32>(f, s, bx, by, mh_smem_raw);
 }
 
+// The reference sums each family's unavoidable loss and every table
+// subset's cost serially in f64, in DC-group order, and only compares those
+// sums.  The device sums the same non-negative terms in parallel (P) and
+// settles each comparison from an interval that holds the serial result: for
+// n terms both |serial - exact| and |P - exact| stay below n u E (u = 2^-53,
+// error bounds of recursive and pairwise summation; an addition of zero is
+// exact), so the serial sum lies within M = (n + 64) 2^-51 P of P.  A
+// comparison the interval leaves open (in practice an exact tie of different
+// sums) is settled by the serial sums in the reference's order.
+
+// k_mh_sum's per-CTA partials: [0] [1] the 16x16 / 32x32 families'
+// unavoidable losses; [2 + a] / [10 + a] the families' cheapest alternatives
+// under allowed & 7 == a (best_alternative reads only slots 0-2); [18] [19]
+// the families' site counts; [20] the custom slots the layout uses.
+constexpr int kMhQuantities = 21;
+constexpr int kMhSumThreads = 256;
+constexpr int kMhThreads = 1024;
+
+// best_alternative (matrix_overhead.rs:50-63) of a site of table slot `slot`
+// under `allowed`: incumbent (requires its own slot), DCT (slot 0 when
+// custom), 16x16 (slot 1 when custom); strict `<` keeps the earlier one on a
+// tie; `which` is 0, 1, 2 for them, -1 for none.
+__device__ __forceinline__ double mh_best(uint32_t slot, double ld, double l16, uint32_t allowed,
+                                          uint32_t custom, int* which) {
+  double best = INFINITY;
+  *which = -1;
+  if (((1u << slot) & ~allowed) == 0u) { best = 0.0; *which = 0; }
+  if (ld >= 0.0 && ((1u & custom) & ~allowed) == 0u && (*which < 0 || ld < best)) { best = ld; *which = 1; }
+  if (l16 >= 0.0 && ((2u & custom) & ~allowed) == 0u && (*which < 0 || l16 < best)) { best = l16; *which = 2; }
+  return best;
+}
+
+__device__ __forceinline__ uint32_t mh_slot(uint8_t cell) {
+  const int st = cell >> 1;
+  return st == kStDct ? 0u : st == kSt16x16 ? 1u : st == kSt32x32 ? 2u : 3u;
+}
+
+// One thread per 2x2-block cell (its first block at even coordinates): the
+// custom slots its first blocks use, and for a site (a 16x16 / 32x32 whose
+// table is custom) the alternatives' losses (mh_score, matrix_overhead.rs:
+// 65-91, an f64 sum in raster order) and its terms of every sum; then the
+// CTA's partials in a fixed order.
+__global__ void __launch_bounds__(kMhSumThreads) k_mh_sum(const __grid_constant__ Frame f) {
+  const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
+  const int xb = f.a.xb, yb = f.a.yb;
+  const int nx = (xb + 1) / 2;
+  const int64_t e = static_cast<int64_t>(blockIdx.x) * kMhSumThreads + threadIdx.x;
+  const uint32_t custom = s.p.custom;
+  double q[kMhQuantities];
+#pragma unroll
+  for (int i = 0; i < kMhQuantities; ++i) q[i] = 0.0;
+  if (e < static_cast<int64_t>(nx) * ((yb + 1) / 2)) {
+    const int bx = 2 * static_cast<int>(e % nx), by = 2 * static_cast<int>(e / nx);
+    const int64_t b = static_cast<int64_t>(by) * xb + bx;
+    uint32_t used = 0;
+    for (int iy = 0; iy < 2 && by + iy < yb; ++iy)
+      for (int ix = 0; ix < 2 && bx + ix < xb; ++ix) {
+        const uint8_t cell = s.map[b + iy * xb + ix];
+        if ((cell & 1) && (custom & (1u << mh_slot(cell)))) used |= 1u << mh_slot(cell);
+      }
+    q[20] = static_cast<double>(used);
+    const uint8_t cell = s.map[b];
+    const uint32_t slot = mh_slot(cell);
+    uint8_t kind = 0;
+    if ((cell & 1) && (slot == 1u || slot == 2u) && (custom & (1u << slot))) {
+      kind = static_cast<uint8_t>(slot);
+      const int st = cell >> 1, cx = cov_x_of(st), cy = cov_y_of(st);
+      const double lambda = static_cast<double>(kRdLambda);
+      const double inc = static_cast<double>(s.mh_inc[b]) / lambda;
+      double c = 0.0;
+      for (int iy = 0; iy < cy; ++iy)
+        for (int ix = 0; ix < cx; ++ix)
+          c = __dadd_rn(c, static_cast<double>(s.c8[b + iy * xb + ix]) / lambda);
+      double loss = __dsub_rn(c, inc);
+      const double ld = (isfinite(c) && isfinite(inc)) ? (loss > 0.0 ? loss : 0.0) : -1.0;
+      double l16 = -1.0;
+      if (st == kSt32x32) {
+        double c2 = 0.0;
+        for (int iy = 0; iy < 4; iy += 2)
+          for (int ix = 0; ix < 4; ix += 2)
+            c2 = __dadd_rn(c2, static_cast<double>(s.c16r[b + iy * xb + ix]) / lambda);
+        loss = __dsub_rn(c2, inc);
+        l16 = (isfinite(c2) && isfinite(inc)) ? (loss > 0.0 ? loss : 0.0) : -1.0;
+      }
+      s.mh_loss[2 * b] = ld;
+      s.mh_loss[2 * b + 1] = l16;
+      double mn = INFINITY;
+      if (ld >= 0.0) mn = fmin(mn, ld);
+      if (l16 >= 0.0) mn = fmin(mn, l16);
+      double best[8];
+#pragma unroll
+      for (uint32_t a = 0; a < 8; ++a) {
+        int which;
+        best[a] = mh_best(slot, ld, l16, a, custom, &which);
+      }
+      if (slot == 1u) {
+        q[0] = mn;
+        q[18] = 1.0;
+#pragma unroll
+        for (int a = 0; a < 8; ++a) q[2 + a] = best[a];
+      } else {
+        q[1] = mn;
+        q[19] = 1.0;
+#pragma unroll
+        for (int a = 0; a < 8; ++a) q[10 + a] = best[a];
+      }
+    }
+    s.mh_kind[b] = kind;
+  }
+  // the CTA's partials: warp butterflies, then one thread per quantity over the warps
+  __shared__ double part[kMhSumThreads / 32][kMhQuantities];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < kMhQuantities; ++i) {
+    double v = q[i];
+    if (i == 20) {
+      uint32_t u = static_cast<uint32_t>(v);
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) u |= __shfl_xor_sync(0xffffffffu, u, d);
+      v = static_cast<double>(u);
+    } else {
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) v = __dadd_rn(v, __shfl_xor_sync(0xffffffffu, v, d));
+    }
+    if (lane == 0) part[warp][i] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < kMhQuantities) {
+    const int i = threadIdx.x;
+    double v = 0.0;
+    uint32_t u = 0;
+    for (int w = 0; w < kMhSumThreads / 32; ++w) {
+      v = __dadd_rn(v, part[w][i]);
+      u |= static_cast<uint32_t>(part[w][i]);
+    }
+    s.mh_part[static_cast<int64_t>(blockIdx.x) * kMhQuantities + i] = i == 20 ? static_cast<double>(u) : v;
+  }
+}
+
 __device__ __forceinline__ uint32_t header_bits(const SearchFrame& s, uint32_t used) {
   uint32_t payload = 0;
   for (int i = 0; i < 13; ++i)
@@ -935,216 +1206,263 @@ __device__ __forceinline__ uint32_t header_bits(const SearchFrame& s, uint32_t u
   return 1u + payload + (payload != 0u ? 17u * 3u : 0u);
 }
 
-constexpr int kMhThreads = 1024;
-// One CTA: the sites in DC-group order, as two lists (16x16 sites, then
-// 32x32 sites: the order in which the reference sums its regions), each
-// site's alternatives, the families a lower bound pins, the cheapest table
-// set (every subset's sum over the sites in order; losses are non-negative,
-// so the reference's early exit never changes which set wins), and the
-// chosen alternatives.
-__global__ void __launch_bounds__(kMhThreads) k_mh_choose(const __grid_constant__ Frame f) {
+// An interval [lo, hi] that holds the serial sum of `n` non-negative terms
+// whose parallel sum is p.
+struct SumRange {
+  double lo, hi;
+};
+__device__ __forceinline__ SumRange sum_range(double p, double n) {
+  if (!isfinite(p)) return SumRange{p, p};
+  const double m = __dmul_rn(__dmul_rn(p, __dadd_rn(n, 64.0)), 0x1p-51);
+  return SumRange{__dsub_rn(p, m), __dadd_rn(p, m)};
+}
+
+// One CTA: the partials' totals, the pinned families, the cheapest table set
+// (every subset of the custom slots in the reference's order: custom, then
+// (prev - 1) & custom down to 0; losses are non-negative, so the reference's
+// early exits never change which set wins or which family is pinned),
+// written to mh_decision as {best, pinned, used}.  The serial path builds
+// the site lists in DC-group order (16x16 sites, then 32x32 sites: the order
+// in which the reference sums its regions).
+__global__ void __launch_bounds__(kMhThreads) k_mh_choose(const __grid_constant__ Frame f,
+                                                          int parts) {
   const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
   const int xb = f.a.xb, yb = f.a.yb;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  __shared__ uint32_t s_used, s_n[2], s_warp[2][32];
-  __shared__ double s_unavoidable[2];
-  __shared__ uint32_t s_pinned, s_best;
-  __shared__ double s_subset_cost[64];
-  if (tid == 0) {
-    s_used = 0;
-    s_n[0] = s_n[1] = 0;
+  __shared__ double tot[kMhQuantities];
+  __shared__ uint32_t s_n[2], s_warp[2][32], s_flags, s_pinned, s_best;
+  __shared__ double s_unavoidable[2], s_subset_cost[64];
+  if (warp < kMhQuantities) {
+    double v = 0.0;
+    uint32_t u = 0;
+    for (int k = lane; k < parts; k += 32) {
+      const double x = s.mh_part[static_cast<int64_t>(k) * kMhQuantities + warp];
+      v = __dadd_rn(v, x);
+      u |= static_cast<uint32_t>(x);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      v = __dadd_rn(v, __shfl_xor_sync(0xffffffffu, v, d));
+      u |= __shfl_xor_sync(0xffffffffu, u, d);
+    }
+    if (lane == 0) tot[warp] = warp == 20 ? static_cast<double>(u) : v;
   }
   __syncthreads();
+  const uint32_t used = static_cast<uint32_t>(tot[20]), custom = s.p.custom;
+  if ((used & ~1u) == 0u) {
+    if (tid == 0) {
+      s.mh_decision[0] = used;
+      s.mh_decision[1] = 0;
+      s.mh_decision[2] = used;
+    }
+    return;
+  }
+  const double cnt[2] = {tot[18], tot[19]};
+  // 1: the pinned families (matrix_overhead.rs:180-215)
+  if (tid == 0) {
+    uint32_t pinned = used & 1u, open = 0;
+    for (int slot = 1; slot <= 2; ++slot) {
+      if (!(used & (1u << slot))) continue;
+      const double thr = static_cast<double>(s.p.payload[slot] + 17u * 3u);
+      const SumRange r = sum_range(tot[slot - 1], cnt[slot - 1]);
+      if (r.lo > thr) pinned |= 1u << slot;
+      else if (!(r.hi <= thr)) open = 1;
+    }
+    s_pinned = pinned;
+    s_flags = open || s.p.serial_sums;
+  }
+  __syncthreads();
+  const bool serial = s_flags != 0;
   const int xdc = (xb + 255) / 256, ydc = (yb + 255) / 256;
-  uint32_t used_local = 0;
   const int64_t nb = static_cast<int64_t>(xb) * yb;
   uint32_t* list16 = s.sites;
   uint32_t* list32 = s.sites + nb / 2;
-  // enumerate blocks in DC-group order, raster within each DC group
-  for (int64_t base = 0; base < nb; base += kMhThreads) {
-    const int64_t k = base + tid;
-    int fam = -1;
-    int b = -1;
-    if (k < nb) {
-      int64_t rem = k;
-      int gx0 = 0, gy0 = 0, gw = 0, gh = 0;
-      for (int g = 0; g < xdc * ydc; ++g) {
-        gx0 = (g % xdc) * 256;
-        gy0 = (g / xdc) * 256;
-        gw = imin(256, xb - gx0);
-        gh = imin(256, yb - gy0);
-        if (rem < static_cast<int64_t>(gw) * gh) break;
-        rem -= static_cast<int64_t>(gw) * gh;
-      }
-      b = (gy0 + static_cast<int>(rem / gw)) * xb + gx0 + static_cast<int>(rem % gw);
-      const uint8_t cell = s.map[b];
-      if (cell & 1) {
-        const int st = cell >> 1;
-        const uint32_t slot = st == kStDct ? 0u : st == kSt16x16 ? 1u : st == kSt32x32 ? 2u : 3u;
-        if (s.p.custom & (1u << slot)) {
-          used_local |= 1u << slot;
-          if (slot == 1u || slot == 2u) fam = static_cast<int>(slot) - 1;
+  auto build_lists = [&]() {
+    if (tid == 0) s_n[0] = s_n[1] = 0;
+    __syncthreads();
+    for (int64_t base = 0; base < nb; base += kMhThreads) {
+      const int64_t k = base + tid;
+      int fam = -1, b = -1;
+      if (k < nb) {
+        int64_t rem = k;
+        int gx0 = 0, gy0 = 0, gw = 0, gh = 0;
+        for (int g = 0; g < xdc * ydc; ++g) {
+          gx0 = (g % xdc) * 256;
+          gy0 = (g / xdc) * 256;
+          gw = imin(256, xb - gx0);
+          gh = imin(256, yb - gy0);
+          if (rem < static_cast<int64_t>(gw) * gh) break;
+          rem -= static_cast<int64_t>(gw) * gh;
         }
+        b = (gy0 + static_cast<int>(rem / gw)) * xb + gx0 + static_cast<int>(rem % gw);
+        const uint8_t cell = s.map[b];
+        const uint32_t slot = mh_slot(cell);
+        if ((cell & 1) && (slot == 1u || slot == 2u) && (custom & (1u << slot))) fam = static_cast<int>(slot) - 1;
       }
+      const unsigned b0 = __ballot_sync(0xffffffffu, fam == 0), b1 = __ballot_sync(0xffffffffu, fam == 1);
+      if (lane == 0) {
+        s_warp[0][warp] = __popc(b0);
+        s_warp[1][warp] = __popc(b1);
+      }
+      __syncthreads();
+      if (fam >= 0) {
+        uint32_t before = 0;
+        for (int w = 0; w < warp; ++w) before += s_warp[fam][w];
+        const unsigned bal = fam == 0 ? b0 : b1;
+        (fam == 0 ? list16 : list32)[s_n[fam] + before + __popc(bal & ((1u << lane) - 1u))] =
+            static_cast<uint32_t>(b);
+      }
+      __syncthreads();
+      if (tid < 2) {
+        uint32_t total = 0;
+        for (int w = 0; w < 32; ++w) total += s_warp[tid][w];
+        s_n[tid] += total;
+      }
+      __syncthreads();
     }
-    const unsigned b0 = __ballot_sync(0xffffffffu, fam == 0), b1 = __ballot_sync(0xffffffffu, fam == 1);
-    if (lane == 0) {
-      s_warp[0][warp] = __popc(b0);
-      s_warp[1][warp] = __popc(b1);
-    }
-    __syncthreads();
-    if (fam >= 0) {
-      uint32_t before = 0;
-      for (int w = 0; w < warp; ++w) before += s_warp[fam][w];
-      const unsigned bal = fam == 0 ? b0 : b1;
-      (fam == 0 ? list16 : list32)[s_n[fam] + before + __popc(bal & ((1u << lane) - 1u))] =
-          static_cast<uint32_t>(b);
-    }
-    __syncthreads();
-    if (tid < 2) {
-      uint32_t total = 0;
-      for (int w = 0; w < 32; ++w) total += s_warp[tid][w];
-      s_n[tid] += total;
-    }
-    __syncthreads();
-  }
-  atomicOr(&s_used, used_local);
-  __syncthreads();
-  const uint32_t used = s_used, n16 = s_n[0], n32 = s_n[1], count = n16 + n32;
-  if ((used & ~1u) == 0u) return;
-  const double lambda = static_cast<double>(kRdLambda);
-  // every site's losses, family-major: the DCT alternative's and (32x32)
-  // the 16x16 alternative's, -1 where the alternative is absent
-  double* loss = s.mh_loss;
-  for (uint32_t k = tid; k < count; k += kMhThreads) {
-    const uint32_t b = k < n16 ? list16[k] : list32[k - n16];
-    const int st = k < n16 ? kSt16x16 : kSt32x32, cx = cov_x_of(st), cy = cov_y_of(st);
-    const double inc = static_cast<double>(s.mh_inc[b]) / lambda;
-    double c = 0.0;
-    for (int iy = 0; iy < cy; ++iy)
-      for (int ix = 0; ix < cx; ++ix)
-        c = __dadd_rn(c, static_cast<double>(s.c8[b + iy * xb + ix]) / lambda);
-    loss[2 * k] = (isfinite(c) && isfinite(inc)) ? fmax(c - inc, 0.0) : -1.0;
-    double l16 = -1.0;
-    if (st == kSt32x32) {
-      double c2 = 0.0;
-      for (int iy = 0; iy < 4; iy += 2)
-        for (int ix = 0; ix < 4; ix += 2)
-          c2 = __dadd_rn(c2, static_cast<double>(s.c16r[b + iy * xb + ix]) / lambda);
-      l16 = (isfinite(c2) && isfinite(inc)) ? fmax(c2 - inc, 0.0) : -1.0;
-    }
-    loss[2 * k + 1] = l16;
-  }
-  __syncthreads();
-  // the families' unavoidable losses in site order (thread 0: 16x16, 32: 32x32)
-  if (tid == 0 || tid == 32) {
-    const uint32_t lo = tid == 0 ? 0u : n16, hi = tid == 0 ? n16 : count;
-    double u = 0.0;
-#pragma unroll 8
-    for (uint32_t k = lo; k < hi; ++k) {
-      const double ld = loss[2 * k], l16 = loss[2 * k + 1];
-      double mn = INFINITY;
-      if (ld >= 0.0) mn = fmin(mn, ld);
-      if (l16 >= 0.0) mn = fmin(mn, l16);
-      u = __dadd_rn(u, mn);
-    }
-    s_unavoidable[tid == 0 ? 0 : 1] = u;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    uint32_t pinned = used & 1u;
-    for (int slot = 1; slot <= 2; ++slot)
-      if ((used & (1u << slot)) &&
-          s_unavoidable[slot - 1] > static_cast<double>(s.p.payload[slot] + 17u * 3u))
-        pinned |= 1u << slot;
-    s_pinned = pinned;
-  }
-  __syncthreads();
-  const uint32_t pinned = s_pinned, custom = s.p.custom;
-  // best_alternative (matrix_overhead.rs:50-63) of site k under `allowed`:
-  // incumbent (requires its own slot), DCT (slot 0 when custom), 16x16
-  // (slot 1 when custom); strict `<` keeps the earlier one on a tie
-  auto best_of = [&](uint32_t k, uint32_t allowed, int* which) -> double {
-    const uint32_t slot = k < n16 ? 1u : 2u;
-    const double ld = loss[2 * k], l16 = loss[2 * k + 1];
-    double best = INFINITY;
-    bool any = false;
-    *which = 0;
-    if (((1u << slot) & ~allowed) == 0u) { best = 0.0; any = true; }
-    if (ld >= 0.0 && ((1u & custom) & ~allowed) == 0u && (!any || ld < best)) { best = ld; any = true; *which = 1; }
-    if (l16 >= 0.0 && ((2u & custom) & ~allowed) == 0u && (!any || l16 < best)) { best = l16; any = true; *which = 2; }
-    return any ? best : INFINITY;
   };
-  // subsets of `custom` in the reference's order: custom, then
-  // (prev - 1) & custom down to 0; thread j takes the j-th
-  const int nsub = 1 << __popc(custom);
-  if (tid < nsub) {
-    uint32_t allowed = custom;
-    for (int j = 0; j < tid; ++j) allowed = (allowed - 1u) & custom;
-    double cost = INFINITY;
-    if ((pinned & ~allowed) == 0u) {
-      cost = static_cast<double>(header_bits(s, allowed));
-      // a pinned family's regions were dropped
-      const uint32_t lo = (pinned & 2u) ? n16 : 0u;
-      const uint32_t hi = (pinned & 4u) ? n16 : count;
-#pragma unroll 8
-      for (uint32_t k = lo; k < hi; ++k) {
-        int which;
-        cost = __dadd_rn(cost, best_of(k, allowed, &which));
+  if (serial) {
+    build_lists();
+    // the unavoidable losses in site order (thread 0: 16x16, 32: 32x32)
+    if (tid == 0 || tid == 32) {
+      const uint32_t* list = tid == 0 ? list16 : list32;
+      const uint32_t n = s_n[tid == 0 ? 0 : 1];
+      double u = 0.0;
+      for (uint32_t k = 0; k < n; ++k) {
+        const double ld = s.mh_loss[2 * list[k]], l16 = s.mh_loss[2 * list[k] + 1];
+        double mn = INFINITY;
+        if (ld >= 0.0) mn = fmin(mn, ld);
+        if (l16 >= 0.0) mn = fmin(mn, l16);
+        u = __dadd_rn(u, mn);
       }
+      s_unavoidable[tid == 0 ? 0 : 1] = u;
     }
-    s_subset_cost[tid] = cost;
+    __syncthreads();
+    if (tid == 0) {
+      uint32_t pinned = used & 1u;
+      for (int slot = 1; slot <= 2; ++slot)
+        if ((used & (1u << slot)) &&
+            s_unavoidable[slot - 1] > static_cast<double>(s.p.payload[slot] + 17u * 3u))
+          pinned |= 1u << slot;
+      s_pinned = pinned;
+    }
+    __syncthreads();
   }
-  __syncthreads();
+  const uint32_t pinned = s_pinned;
+  const int nsub = 1 << __popc(custom);
+  // 2: the subsets' costs, as intervals; settle the reference's running
+  // choice (strict `<` against the best so far, starting from `used`)
   if (tid == 0) {
-    uint32_t best = used;
-    double best_cost = static_cast<double>(header_bits(s, used));
-    uint32_t allowed = custom;
-    for (int j = 0; j < nsub; ++j) {
-      if ((pinned & ~allowed) == 0u && s_subset_cost[j] < best_cost) {
-        best_cost = s_subset_cost[j];
-        best = allowed;
+    uint32_t best = used, allowed = custom;
+    const double hb_used = static_cast<double>(header_bits(s, used));
+    SumRange best_r{hb_used, hb_used};
+    bool open = serial;
+    for (int j = 0; j < nsub && !open; ++j) {
+      if ((pinned & ~allowed) == 0u) {
+        const uint32_t a = allowed & 7u;
+        double p = static_cast<double>(header_bits(s, allowed)), n = 1.0;
+        if (!(pinned & 2u)) { p = __dadd_rn(p, tot[2 + a]); n = __dadd_rn(n, cnt[0]); }
+        if (!(pinned & 4u)) { p = __dadd_rn(p, tot[10 + a]); n = __dadd_rn(n, cnt[1]); }
+        const SumRange r = sum_range(p, n);
+        if (r.hi < best_r.lo) {
+          best = allowed;
+          best_r = r;
+        } else if (!(r.lo >= best_r.hi)) {
+          open = true;
+        }
       }
       allowed = (allowed - 1u) & custom;
     }
     s_best = best;
+    s_flags = open;
   }
   __syncthreads();
-  const uint32_t best = s_best;
-  if (best == used) return;
-  for (uint32_t k = tid; k < count; k += kMhThreads) {
-    const uint32_t slot = k < n16 ? 1u : 2u;
-    if (pinned & (1u << slot)) continue;
-    int which;
-    best_of(k, best, &which);
-    if (which == 0) continue;
-    const int chosen = which == 1 ? kStDct : kSt16x16;
-    const uint32_t b = k < n16 ? list16[k] : list32[k - n16];
-    const int st = slot == 2u ? kSt32x32 : kSt16x16;
-    const int bx = static_cast<int>(b % xb), by = static_cast<int>(b / xb);
-    const int w = cov_x_of(st), h = cov_y_of(st), cx = cov_x_of(chosen), cy = cov_y_of(chosen);
-    for (int yy = 0; yy < h; yy += cy)
-      for (int xx = 0; xx < w; xx += cx) {
-        map_set_first(s.map, xb, bx + xx, by + yy, chosen);
-        // merged_quant (matrix_overhead.rs:93-113) from the pre-selection field
-        uint8_t q;
-        if (cx * cy == 1) {
-          q = s.block_qf[(by + yy) * xb + bx + xx];
-        } else {
-          uint32_t max_q = 0, sum = 0;
-          for (int iy = 0; iy < cy; ++iy)
-            for (int ix = 0; ix < cx; ++ix) {
-              const uint32_t v = s.block_qf[(by + yy + iy) * xb + bx + xx + ix];
-              max_q = max(max_q, v);
-              sum += v;
-            }
-          q = aggregate_quant(max_q, sum, cx * cy, s.distance);
+  if (s_flags) {
+    if (!serial) build_lists();
+    const uint32_t n16 = s_n[0], count = s_n[0] + s_n[1];
+    if (tid < nsub) {
+      uint32_t allowed = custom;
+      for (int j = 0; j < tid; ++j) allowed = (allowed - 1u) & custom;
+      double cost = INFINITY;
+      if ((pinned & ~allowed) == 0u) {
+        cost = static_cast<double>(header_bits(s, allowed));
+        // a pinned family's regions were dropped
+        const uint32_t lo = (pinned & 2u) ? n16 : 0u;
+        const uint32_t hi = (pinned & 4u) ? n16 : count;
+        for (uint32_t k = lo; k < hi; ++k) {
+          const uint32_t b = k < n16 ? list16[k] : list32[k - n16];
+          int which;
+          cost = __dadd_rn(cost, mh_best(k < n16 ? 1u : 2u, s.mh_loss[2 * b], s.mh_loss[2 * b + 1],
+                                         allowed, custom, &which));
         }
-        for (int iy = 0; iy < cy; ++iy)
-          for (int ix = 0; ix < cx; ++ix) f.qf[(by + yy + iy) * xb + bx + xx + ix] = q;
       }
+      s_subset_cost[tid] = cost;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      uint32_t best = used;
+      double best_cost = static_cast<double>(header_bits(s, used));
+      uint32_t allowed = custom;
+      for (int j = 0; j < nsub; ++j) {
+        if ((pinned & ~allowed) == 0u && s_subset_cost[j] < best_cost) {
+          best_cost = s_subset_cost[j];
+          best = allowed;
+        }
+        allowed = (allowed - 1u) & custom;
+      }
+      s_best = best;
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    s.mh_decision[0] = s_best;
+    s.mh_decision[1] = pinned;
+    s.mh_decision[2] = used;
   }
 }
+
+// One thread per 2x2-block cell: a site of a family not pinned takes its
+// cheapest alternative under the chosen set (matrix_overhead.rs:240-268).
+__global__ void __launch_bounds__(256) k_mh_apply(const __grid_constant__ Frame f) {
+  const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
+  const int xb = f.a.xb, yb = f.a.yb;
+  const int nx = (xb + 1) / 2;
+  const int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= static_cast<int64_t>(nx) * ((yb + 1) / 2)) return;
+  const uint32_t best = s.mh_decision[0], pinned = s.mh_decision[1], used = s.mh_decision[2];
+  if (best == used) return;
+  const int bx = 2 * static_cast<int>(e % nx), by = 2 * static_cast<int>(e / nx);
+  const int64_t b = static_cast<int64_t>(by) * xb + bx;
+  const uint32_t slot = s.mh_kind[b];
+  if (slot == 0u || (pinned & (1u << slot))) return;
+  int which;
+  mh_best(slot, s.mh_loss[2 * b], s.mh_loss[2 * b + 1], best, s.p.custom, &which);
+  if (which <= 0) return;
+  const int chosen = which == 1 ? kStDct : kSt16x16;
+  const int st = slot == 2u ? kSt32x32 : kSt16x16;
+  const int w = cov_x_of(st), h = cov_y_of(st), cx = cov_x_of(chosen), cy = cov_y_of(chosen);
+  for (int yy = 0; yy < h; yy += cy)
+    for (int xx = 0; xx < w; xx += cx) {
+      map_set_first(s.map, xb, bx + xx, by + yy, chosen);
+      // merged_quant (matrix_overhead.rs:93-113) from the pre-selection field
+      uint8_t q;
+      if (cx * cy == 1) {
+        q = s.block_qf[(by + yy) * xb + bx + xx];
+      } else {
+        uint32_t max_q = 0, sum = 0;
+        for (int iy = 0; iy < cy; ++iy)
+          for (int ix = 0; ix < cx; ++ix) {
+            const uint32_t v = s.block_qf[(by + yy + iy) * xb + bx + xx + ix];
+            max_q = max(max_q, v);
+            sum += v;
+          }
+        q = aggregate_quant(max_q, sum, cx * cy, s.distance);
+      }
+      for (int iy = 0; iy < cy; ++iy)
+        for (int ix = 0; ix < cx; ++ix) f.qf[(by + yy + iy) * xb + bx + xx + ix] = q;
+    }
+}
+
 
 // ac_qf_threshold over the final field (src/frame/ac_groups.rs:92-113), one CTA.
 __global__ void __launch_bounds__(256) k_qf_median(const __grid_constant__ Frame f) {

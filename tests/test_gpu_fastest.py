@@ -92,3 +92,12 @@ def test_reranked_distances_are_refused_and_the_dct8_shortcut_is_ultrafast(ctx):
 def test_config2_frame_at_q75_whole(ctx):
     # the benchmarked 3840x2160 frame at q75, compared whole
     compare(ctx, synthetic.config2_image(), J.distance_from_quality(75))
+
+
+def test_serial_sums_give_the_same_frame(ctx, monkeypatch):
+    # JXG_SERIAL_SUMS=1 takes every f64 running sum serially in the
+    # reference's order instead of settling it from a parallel sum's interval
+    monkeypatch.setenv("JXG_SERIAL_SUMS", "1")
+    compare(ctx, synthetic.config1_image(), J.distance_from_quality(40))
+    compare(ctx, synthetic.generate(2100, 300, 21, noise_sigma=4.0, rectangles=40,
+                                    texture_weight=0.3), 2.35)
