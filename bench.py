@@ -186,36 +186,35 @@ def algorithmic_bytes(kernel: str, w: int, h: int, tokens_per_frame: float) -> f
         "k_cost_8x16": px * 12 + blocks // 2 * 4,
         "k_cost_16x8": px * 12 + blocks // 2 * 4,
         "k_cost_32x32": px * 12 + blocks // 16 * 8,
+        # luma in (each site reads its own window), one bias per site out
+        "k_site": px * 4 + blocks // 4 * 4 + blocks // 16 * 4,
         # costs, field and map in; map out
         "k_retile": blocks * (4 * 5 + 2),
-        "k_layout_tile": px * 12 + blocks * (384 + 6 + 3 + 4 + 16),
+        # the coding of the layout: each shape's launch reads the planes under
+        # its transforms and writes their blocks' levels and side data; one
+        # launch of each is counted as the whole frame's
+        "k_layout_dct8": px * 12 + blocks * (384 + 6 + 3 + 4 + 16),
+        "k_layout_16x16": px * 12 + blocks * (384 + 6 + 3 + 4 + 16),
+        "k_layout_32x32": px * 12 + blocks * (384 + 6 + 3 + 4 + 16),
         "k_tokenize_layout": blocks * (384 + 4 + 1 + 16) + tokens_per_frame * 8 + hist,
     }
     return table.get(kernel)
 
 
-def traffic_from_profiles(kernel: str) -> float | None:
-    """DRAM bytes per launch of `kernel` on one 3840x2160 frame, from the
-    committed ncu summary (the capture's own command is in its header)."""
-    path = os.path.join(ROOT, "profiles", "dram_traffic_4k_q90.txt")
-    if not os.path.exists(path):
-        return None
-    for line in open(path):
-        if line.startswith(kernel + ":"):
-            return float(line.split(":", 1)[1])
-    return None
+COUNTERS = os.path.join(ROOT, "profiles", "counters_4k_q75_fastest.txt")
 
 
-def instructions_from_profiles(kernel: str) -> float | None:
-    """Warp instructions (smsp__inst_executed.sum) of one launch of `kernel`
-    on one 3840x2160 q90 frame, from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "warp_instructions_4k_q90.txt")
-    if not os.path.exists(path):
-        return None
-    for line in open(path):
+def counters_from_profiles(kernel: str) -> tuple[float | None, float | None]:
+    """(DRAM bytes, warp instructions) of one launch of `kernel` on one
+    3840x2160 q75 Speed::Fastest frame, from the committed ncu summary (its
+    header gives the capture's command)."""
+    if not os.path.exists(COUNTERS):
+        return None, None
+    for line in open(COUNTERS):
         if line.startswith(kernel + ":"):
-            return float(line.split(":", 1)[1])
-    return None
+            dram, inst = line.split(":", 1)[1].split()[:2]
+            return float(dram), float(inst)
+    return None, None
 
 
 def _synthetic():
@@ -373,29 +372,32 @@ def run_gpu(args):
     dom_name, (dom_ms, dom_n) = dom
     avg_ms = dom_ms / max(dom_n, 1)
     algo = algorithmic_bytes(dom_name, WIDTH, HEIGHT, float(np.mean(tokens)))
-    achieved = algo / (avg_ms / 1000.0) / 1e9 if algo else None
-    traffic = traffic_from_profiles(dom_name)
-    roofline = {
-        "kernel": dom_name, "bound": "hbm",
-        "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-        "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
-        "peak_source": peaks["source"], "traffic": traffic,
-        "algorithmic_bytes_per_launch": algo, "avg_launch_ms": avg_ms,
-        "share_of_kernel_time": dom_ms / sum(v[0] for v in ktimes.values()),
+    hbm = algo / (avg_ms / 1000.0) / 1e9 if algo else None
+    traffic, inst = counters_from_profiles(dom_name)
+    hbm_line = {
+        "achieved": hbm, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+        "frac": (hbm / peaks["hbm_gbs"]) if hbm else None, "peak_source": peaks["source"],
+        "algorithmic_bytes_per_launch": algo, "traffic": traffic,
     }
-    # the kernels are issue-bound, not DRAM-bound: the dominant kernel's warp
-    # instructions per launch (ncu) over its event-timed launch, against the
-    # SMs' issue rate (four schedulers each issuing one warp instruction a
-    # cycle at the sampled SM clock)
-    inst = instructions_from_profiles(dom_name)
+    # The search and coding kernels are issue-bound (ncu: DRAM and FP32 pipes
+    # far from busy): the dominant kernel's warp instructions per launch (ncu)
+    # over its event-timed launch, against the SMs' issue rate (four
+    # schedulers each issuing one warp instruction a cycle at the sampled SM
+    # clock).  The HBM figures stand beside it.
     sm_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
     if inst and sm_mhz:
         issue_peak = torch.cuda.get_device_properties(dev).multi_processor_count * 4 * sm_mhz * 1e6
         issue_rate = inst / (avg_ms / 1000.0)
-        roofline["issue"] = {
-            "warp_instructions_per_launch": inst, "achieved": issue_rate, "peak": issue_peak,
-            "unit": "warp instructions/s", "frac": issue_rate / issue_peak,
+        roofline = {
+            "kernel": dom_name, "bound": "issue", "achieved": issue_rate, "peak": issue_peak,
+            "unit": "warp instructions/s", "frac": issue_rate / issue_peak, "traffic": traffic,
+            "warp_instructions_per_launch": inst, "avg_launch_ms": avg_ms,
+            "share_of_kernel_time": dom_ms / sum(v[0] for v in ktimes.values()),
+            "hbm": hbm_line,
         }
+    else:
+        roofline = dict(hbm_line, kernel=dom_name, bound="hbm", avg_launch_ms=avg_ms,
+                        share_of_kernel_time=dom_ms / sum(v[0] for v in ktimes.values()))
     # the timed region ran the same launch sequence as the per-kernel pass
     launches = int(sum(v[1] for v in ktimes.values()))
     # the whole front end per frame: input bytes + 4 B per token + block side

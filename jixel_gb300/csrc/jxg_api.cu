@@ -630,7 +630,7 @@ int enqueue_search(Context* c, const Frame& f, bool timed) {
                 })))
     return st;
   if (n32 && (st = launch(c, "k_cost_32x32", timed, [&] {
-                k_cost<kSt32x32><<<grid4(n32), 128, cost_smem_bytes<kSt32x32>(), s>>>(f);
+                k_cost<kSt32x32><<<static_cast<unsigned>(n32), 32, cost_smem_bytes<kSt32x32>(), s>>>(f);
               })))
     return st;
   if (n32 + n16 && (st = launch(c, "k_site", timed, [&] {
@@ -653,7 +653,7 @@ int enqueue_search(Context* c, const Frame& f, bool timed) {
   const int parts = static_cast<int>(mh_sum_ctas(L));
   if (sf.p.headers &&
       ((st = launch(c, "k_mh_incumbent", timed, [&] {
-          k_mh_incumbent<<<grid4(cells2), 128, cost_smem_bytes<kSt32x32>(), s>>>(f);
+          k_mh_incumbent<<<grid4(cells2), 128, 4 * sizeof(CostSmem<kSt32x32>), s>>>(f);
         })) ||
        (st = launch(c, "k_mh_sum", timed, [&] {
           k_mh_sum<<<static_cast<unsigned>(parts), kMhSumThreads, 0, s>>>(f);
@@ -663,10 +663,34 @@ int enqueue_search(Context* c, const Frame& f, bool timed) {
           k_mh_apply<<<static_cast<unsigned>((cells2 + 255) / 256), 256, 0, s>>>(f);
         }))))
     return st;
-  if ((st = launch(c, "k_qf_median", timed, [&] { k_qf_median<<<1, 256, 0, s>>>(f); })) ||
-      (st = launch(c, "k_layout_tile", timed, [&] {
-         k_layout_tile<<<static_cast<unsigned>(tiles), 32 * kLayoutWarps, kLayoutSmemBytes, s>>>(f);
+  if ((st = launch(c, "k_qf_median", timed, [&] { k_qf_median<<<1, 256, 0, s>>>(f); })))
+    return st;
+  // the coding of the layout: a launch per transform shape
+  auto layout_grid = [](int64_t n, int warps) { return static_cast<unsigned>((n + warps - 1) / warps); };
+  if ((st = launch(c, "k_layout_dct8", timed, [&] {
+         k_layout<kStDct><<<layout_grid(nb, layout_warps<kStDct>()), 32 * layout_warps<kStDct>(),
+                            layout_smem_bytes<kStDct>(), s>>>(f);
        })))
+    return st;
+  if (n16 && (st = launch(c, "k_layout_16x16", timed, [&] {
+                k_layout<kSt16x16><<<layout_grid(n16, layout_warps<kSt16x16>()), 32 * layout_warps<kSt16x16>(),
+                                     layout_smem_bytes<kSt16x16>(), s>>>(f);
+              })))
+    return st;
+  if (n8x16 && (st = launch(c, "k_layout_8x16", timed, [&] {
+                  k_layout<kSt8x16><<<layout_grid(n8x16, layout_warps<kSt8x16>()), 32 * layout_warps<kSt8x16>(),
+                                      layout_smem_bytes<kSt8x16>(), s>>>(f);
+                })))
+    return st;
+  if (n16x8 && (st = launch(c, "k_layout_16x8", timed, [&] {
+                  k_layout<kSt16x8><<<layout_grid(n16x8, layout_warps<kSt16x8>()), 32 * layout_warps<kSt16x8>(),
+                                      layout_smem_bytes<kSt16x8>(), s>>>(f);
+                })))
+    return st;
+  if (n32 && (st = launch(c, "k_layout_32x32", timed, [&] {
+                k_layout<kSt32x32><<<layout_grid(n32, layout_warps<kSt32x32>()), 32 * layout_warps<kSt32x32>(),
+                                     layout_smem_bytes<kSt32x32>(), s>>>(f);
+              })))
     return st;
   return JXG_OK;
 }

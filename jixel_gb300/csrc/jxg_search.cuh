@@ -22,7 +22,8 @@
 //                      (src/ac_strategy/matrix_overhead.rs:117-268) where the
 //                      16x16 / 32x32 tables are custom (d >= 2.25);
 //   k_qf_median        ac_qf_threshold over the final field;
-//   k_layout_tile      write_ac_group for every transform (src/group.rs:1259-2426);
+//   k_layout<S>        write_ac_group for every transform of shape S, one warp
+//                      each (src/group.rs:1259-2426);
 //   k_tokenize_layout  the tokens and histograms (src/group.rs:2428-2660).
 // Every float operation keeps the reference's order: per-coefficient terms
 // are computed in parallel, and each f32 running sum the reference keeps is
@@ -93,6 +94,39 @@ struct CostSmem {
   float co[3][SIZE];      // coefficients
   float mag[3][SIZE];     // magnitude-rate terms
 };
+// Warps (candidates) per CTA of k_cost<S>: a 32x32 candidate's 37 KB of
+// shared memory goes one to a CTA, so six CTAs share an SM.
+template <int S>
+__host__ __device__ constexpr int cost_warps() { return S == kSt32x32 ? 1 : 4; }
+
+// The block position of candidate `cand` of shape S: every block (DCT8),
+// even bx (8x16), even by (16x8), even bx and by (16x16), 4-aligned (32x32);
+// false past the last.
+template <int S>
+__device__ __forceinline__ bool candidate_position(int64_t cand, int xb, int yb, int* bx, int* by) {
+  if (S == kStDct) {
+    if (cand >= static_cast<int64_t>(xb) * yb) return false;
+    *bx = static_cast<int>(cand % xb), *by = static_cast<int>(cand / xb);
+  } else if (S == kSt8x16) {
+    const int nx = xb / 2;
+    if (nx == 0 || cand >= static_cast<int64_t>(nx) * yb) return false;
+    *bx = 2 * static_cast<int>(cand % nx), *by = static_cast<int>(cand / nx);
+  } else if (S == kSt16x8) {
+    const int ny = yb / 2;
+    if (ny == 0 || cand >= static_cast<int64_t>(xb) * ny) return false;
+    *bx = static_cast<int>(cand % xb), *by = 2 * static_cast<int>(cand / xb);
+  } else if (S == kSt16x16) {
+    const int nx = xb / 2, ny = yb / 2;
+    if (nx == 0 || cand >= static_cast<int64_t>(nx) * ny) return false;
+    *bx = 2 * static_cast<int>(cand % nx), *by = 2 * static_cast<int>(cand / nx);
+  } else {
+    const int nx = xb / 4, ny = yb / 4;
+    if (nx == 0 || cand >= static_cast<int64_t>(nx) * ny) return false;
+    *bx = 4 * static_cast<int>(cand % nx), *by = 4 * static_cast<int>(cand / nx);
+  }
+  return true;
+}
+
 
 __device__ __forceinline__ const float* inv_of(const SearchTables* t, int s, int c) {
   switch (s) {
@@ -144,6 +178,7 @@ __device__ __forceinline__ void warp_forward(const Frame& f, int c, int px, int 
   const int lane = threadIdx.x & 31;
   const int w = f.a.width, h = f.a.height;
   const float* plane = f.xyb + static_cast<int64_t>(c) * f.a.plane;
+#pragma unroll 8
   for (int k = lane; k < W * H; k += 32) {
     const int v = k / W, u = k % W;
     const int sy = imin(py + v, h - 1), sx = imin(px + u, w - 1);
@@ -327,6 +362,7 @@ __device__ __forceinline__ float warp_rd(const Frame& f, const SearchFrame& s, C
   float sum = 0.0f;
   if (lane < 6) {
     const float* terms = lane < 3 ? sse_terms + lane * SIZE : sm.mag[lane - 3];
+#pragma unroll 16
     for (int i = 0; i < SIZE; ++i) sum = __fadd_rn(sum, terms[i]);
   }
   float sse[3], mag[3];
@@ -470,28 +506,9 @@ __global__ void __launch_bounds__(128) k_cost(const __grid_constant__ Frame f) {
   const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
   const int lane = threadIdx.x & 31;
   const int xb = f.a.xb, yb = f.a.yb;
-  const int64_t cand = static_cast<int64_t>(blockIdx.x) * 4 + (threadIdx.x >> 5);
+  const int64_t cand = static_cast<int64_t>(blockIdx.x) * cost_warps<S>() + (threadIdx.x >> 5);
   int bx, by;
-  if (S == kStDct) {
-    if (cand >= static_cast<int64_t>(xb) * yb) return;
-    bx = static_cast<int>(cand % xb), by = static_cast<int>(cand / xb);
-  } else if (S == kSt8x16) {
-    const int nx = xb / 2;
-    if (nx == 0 || cand >= static_cast<int64_t>(nx) * yb) return;
-    bx = 2 * static_cast<int>(cand % nx), by = static_cast<int>(cand / nx);
-  } else if (S == kSt16x8) {
-    const int ny = yb / 2;
-    if (ny == 0 || cand >= static_cast<int64_t>(xb) * ny) return;
-    bx = static_cast<int>(cand % xb), by = 2 * static_cast<int>(cand / xb);
-  } else if (S == kSt16x16) {
-    const int nx = xb / 2, ny = yb / 2;
-    if (nx == 0 || cand >= static_cast<int64_t>(nx) * ny) return;
-    bx = 2 * static_cast<int>(cand % nx), by = 2 * static_cast<int>(cand / nx);
-  } else {
-    const int nx = xb / 4, ny = yb / 4;
-    if (nx == 0 || cand >= static_cast<int64_t>(nx) * ny) return;
-    bx = 4 * static_cast<int>(cand % nx), by = 4 * static_cast<int>(cand / nx);
-  }
+  if (!candidate_position<S>(cand, xb, yb, &bx, &by)) return;
   const int bi = by * xb + bx;
   const uint8_t* qf = f.qf;  // the pre-selection field
   warp_coefficients<S>(f, bx, by, sm);
@@ -536,7 +553,7 @@ __global__ void __launch_bounds__(128) k_cost(const __grid_constant__ Frame f) {
 }
 
 template <int S>
-constexpr size_t cost_smem_bytes() { return 4 * sizeof(CostSmem<S>); }
+constexpr size_t cost_smem_bytes() { return cost_warps<S>() * sizeof(CostSmem<S>); }
 
 // ---------------------------------------------------------------------------
 // Selection (squares scope) and re-tiling
@@ -1207,12 +1224,14 @@ __device__ __forceinline__ uint32_t header_bits(const SearchFrame& s, uint32_t u
 }
 
 // An interval [lo, hi] that holds the serial sum of `n` non-negative terms
-// whose parallel sum is p.
+// whose parallel sum is p; `terms` is the parallel sum of the terms after the
+// first (the header bits).  Zero there means every later term is zero, and
+// adding zero is exact: the serial sum is p itself.
 struct SumRange {
   double lo, hi;
 };
-__device__ __forceinline__ SumRange sum_range(double p, double n) {
-  if (!isfinite(p)) return SumRange{p, p};
+__device__ __forceinline__ SumRange sum_range(double p, double n, double terms) {
+  if (!isfinite(p) || terms == 0.0) return SumRange{p, p};
   const double m = __dmul_rn(__dmul_rn(p, __dadd_rn(n, 64.0)), 0x1p-51);
   return SumRange{__dsub_rn(p, m), __dadd_rn(p, m)};
 }
@@ -1264,7 +1283,7 @@ __global__ void __launch_bounds__(kMhThreads) k_mh_choose(const __grid_constant_
     for (int slot = 1; slot <= 2; ++slot) {
       if (!(used & (1u << slot))) continue;
       const double thr = static_cast<double>(s.p.payload[slot] + 17u * 3u);
-      const SumRange r = sum_range(tot[slot - 1], cnt[slot - 1]);
+      const SumRange r = sum_range(tot[slot - 1], cnt[slot - 1], tot[slot - 1]);
       if (r.lo > thr) pinned |= 1u << slot;
       else if (!(r.hi <= thr)) open = 1;
     }
@@ -1360,10 +1379,11 @@ __global__ void __launch_bounds__(kMhThreads) k_mh_choose(const __grid_constant_
     for (int j = 0; j < nsub && !open; ++j) {
       if ((pinned & ~allowed) == 0u) {
         const uint32_t a = allowed & 7u;
-        double p = static_cast<double>(header_bits(s, allowed)), n = 1.0;
-        if (!(pinned & 2u)) { p = __dadd_rn(p, tot[2 + a]); n = __dadd_rn(n, cnt[0]); }
-        if (!(pinned & 4u)) { p = __dadd_rn(p, tot[10 + a]); n = __dadd_rn(n, cnt[1]); }
-        const SumRange r = sum_range(p, n);
+        double p = static_cast<double>(header_bits(s, allowed)), n = 1.0, terms = 0.0;
+        if (!(pinned & 2u)) { terms = tot[2 + a]; n = __dadd_rn(n, cnt[0]); }
+        if (!(pinned & 4u)) { terms = __dadd_rn(terms, tot[10 + a]); n = __dadd_rn(n, cnt[1]); }
+        p = __dadd_rn(p, terms);
+        const SumRange r = sum_range(p, n, terms);
         if (r.hi < best_r.lo) {
           best = allowed;
           best_r = r;
@@ -1482,12 +1502,20 @@ __global__ void __launch_bounds__(256) k_qf_median(const __grid_constant__ Frame
 // write_ac_group over the layout (src/group.rs:1259-2426)
 // ---------------------------------------------------------------------------
 
-constexpr int kLayoutWarps = 4;
+// One warp's buffers for a transform of shape S: one channel's gathered
+// pixels, the parked Y levels and the three channels' coefficients.
+template <int S>
 struct LayoutSmem {
-  float in[3][32][33];
-  float co[3][1024];
+  static constexpr int W = Shape<S>::W, H = Shape<S>::H, SIZE = W * H;
+  float in[H][W + 1];
+  int32_t ylev[SIZE];
+  float co[3][SIZE];
 };
-constexpr size_t kLayoutSmemBytes = kLayoutWarps * sizeof(LayoutSmem);
+// Warps (transforms) per CTA of k_layout<S>; a 32x32's 20 KB goes one to a CTA.
+template <int S>
+__host__ __device__ constexpr int layout_warps() { return S == kSt32x32 ? 1 : 4; }
+template <int S>
+constexpr size_t layout_smem_bytes() { return layout_warps<S>() * sizeof(LayoutSmem<S>); }
 
 __device__ __forceinline__ int dct_kind_of(int st) {
   switch (st) {
@@ -1515,7 +1543,7 @@ __device__ __forceinline__ float layout_threshold(const float* thr, int i, int c
 
 template <int S>
 __device__ __forceinline__ void layout_piece(const Frame& f, const SearchFrame& s, int bx, int by,
-                                             LayoutSmem& sm) {
+                                             LayoutSmem<S>& sm) {
   constexpr int CX = Shape<S>::CX, CY = Shape<S>::CY, COVX = Shape<S>::COVX;
   constexpr int COVY = Shape<S>::COVY, SIZE = CX * CY * 64, COVERED = CX * CY;
   constexpr int LOG2C = COVERED == 1 ? 0 : COVERED == 2 ? 1 : COVERED == 4 ? 2 : 4;
@@ -1526,9 +1554,7 @@ __device__ __forceinline__ void layout_piece(const Frame& f, const SearchFrame& 
   const int bi = by * xb + bx;
   const SearchTables* t = s.t;
   const int kind = dct_kind_of(S);
-  for (int c = 0; c < 3; ++c)
-    warp_forward<S>(f, c, bx * 8, by * 8, reinterpret_cast<float (*)[Shape<S>::W + 1]>(sm.in[0][0]),
-                    sm.co[c]);
+  for (int c = 0; c < 3; ++c) warp_forward<S>(f, c, bx * 8, by * 8, sm.in, sm.co[c]);
   const int32_t quant = f.qf[bi];
   // Y DC levels of the covered blocks (quantize_dc_scalar, src/group.rs:286-292)
   int16_t ydq[16];
@@ -1548,7 +1574,7 @@ __device__ __forceinline__ void layout_piece(const Frame& f, const SearchFrame& 
   for (int i = lane; i < SIZE; i += 32) {
     const float val = __fmul_rn(__fmul_rn(inv_y[i], qs_y), sm.co[1][i]);
     const int32_t q = quantize_level(val, layout_threshold(thr_y, i, CX, CY));
-    sm.in[1][0][i] = __int_as_float(q);  // park the Y level
+    sm.ylev[i] = q;  // park the Y level
     const int width = CX * 8, r = i / width, u = i % width;
     sm.co[1][i] = (r < CY && u < CX) ? 0.0f
                                      : __fmul_rn(__fmul_rn(bias_level(1, q), mat_y[i]), inv_qac);
@@ -1597,7 +1623,7 @@ __device__ __forceinline__ void layout_piece(const Frame& f, const SearchFrame& 
     for (int i = lane; i < SIZE; i += 32) {
       int32_t q;
       if (c == 1) {
-        q = __float_as_int(sm.in[1][0][i]);
+        q = sm.ylev[i];
       } else {
         const float val = __fmul_rn(__fmul_rn(inv[i], qs), sm.co[c][i]);
         q = quantize_level(val, layout_threshold(thr, i, CX, CY));
@@ -1649,31 +1675,20 @@ __device__ __forceinline__ void layout_piece(const Frame& f, const SearchFrame& 
   __syncwarp();
 }
 
-// One CTA per 64x64 tile; its transforms (first blocks in raster order)
-// taken by the warps in turn.
-__global__ void __launch_bounds__(32 * kLayoutWarps) k_layout_tile(const __grid_constant__ Frame f) {
+// One warp per position a transform of shape S can start at; the warp codes
+// the transform placed there, if any.  Every placement the search makes
+// starts at such a position (squares at even, 32x32 at 4-aligned blocks,
+// pairs at even coordinates along their long side).
+template <int S>
+__global__ void __launch_bounds__(128) k_layout(const __grid_constant__ Frame f) {
   extern __shared__ __align__(16) unsigned char layout_smem_raw[];
-  LayoutSmem& sm = reinterpret_cast<LayoutSmem*>(layout_smem_raw)[threadIdx.x >> 5];
+  LayoutSmem<S>& sm = reinterpret_cast<LayoutSmem<S>*>(layout_smem_raw)[threadIdx.x >> 5];
   const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
-  const int xb = f.a.xb, yb = f.a.yb;
-  const int tx = blockIdx.x % f.a.tiles_x, ty = blockIdx.x / f.a.tiles_x;
-  const int bx0 = tx * 8, by0 = ty * 8;
-  const int w = imin(8, xb - bx0), h = imin(8, yb - by0);
-  const int warp = threadIdx.x >> 5;
-  int k = 0;
-  for (int y = 0; y < h; ++y)
-    for (int x = 0; x < w; ++x) {
-      const uint8_t cell = s.map[(by0 + y) * xb + bx0 + x];
-      if (!(cell & 1)) continue;
-      if ((k++ % kLayoutWarps) != warp) continue;
-      switch (cell >> 1) {
-        case kStDct: layout_piece<kStDct>(f, s, bx0 + x, by0 + y, sm); break;
-        case kSt16x8: layout_piece<kSt16x8>(f, s, bx0 + x, by0 + y, sm); break;
-        case kSt8x16: layout_piece<kSt8x16>(f, s, bx0 + x, by0 + y, sm); break;
-        case kSt16x16: layout_piece<kSt16x16>(f, s, bx0 + x, by0 + y, sm); break;
-        default: layout_piece<kSt32x32>(f, s, bx0 + x, by0 + y, sm); break;
-      }
-    }
+  const int64_t cand = static_cast<int64_t>(blockIdx.x) * layout_warps<S>() + (threadIdx.x >> 5);
+  int bx, by;
+  if (!candidate_position<S>(cand, f.a.xb, f.a.yb, &bx, &by)) return;
+  if (s.map[static_cast<int64_t>(by) * f.a.xb + bx] != static_cast<uint8_t>((S << 1) | 1)) return;
+  layout_piece<S>(f, s, bx, by, sm);
 }
 
 // ---------------------------------------------------------------------------
@@ -1855,8 +1870,12 @@ inline cudaError_t set_search_attributes() {
   set(reinterpret_cast<const void*>(k_cost<kSt8x16>), cost_smem_bytes<kSt8x16>());
   set(reinterpret_cast<const void*>(k_cost<kSt16x16>), cost_smem_bytes<kSt16x16>());
   set(reinterpret_cast<const void*>(k_cost<kSt32x32>), cost_smem_bytes<kSt32x32>());
-  set(reinterpret_cast<const void*>(k_mh_incumbent), cost_smem_bytes<kSt32x32>());
-  set(reinterpret_cast<const void*>(k_layout_tile), kLayoutSmemBytes);
+  set(reinterpret_cast<const void*>(k_mh_incumbent), 4 * sizeof(CostSmem<kSt32x32>));
+  set(reinterpret_cast<const void*>(k_layout<kStDct>), layout_smem_bytes<kStDct>());
+  set(reinterpret_cast<const void*>(k_layout<kSt16x8>), layout_smem_bytes<kSt16x8>());
+  set(reinterpret_cast<const void*>(k_layout<kSt8x16>), layout_smem_bytes<kSt8x16>());
+  set(reinterpret_cast<const void*>(k_layout<kSt16x16>), layout_smem_bytes<kSt16x16>());
+  set(reinterpret_cast<const void*>(k_layout<kSt32x32>), layout_smem_bytes<kSt32x32>());
   set(reinterpret_cast<const void*>(k_retile), kRetileSmemBytes);
   return e;
 }
