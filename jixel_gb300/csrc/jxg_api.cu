@@ -630,12 +630,15 @@ int enqueue_search(Context* c, const Frame& f, bool timed) {
                 })))
     return st;
   if (n32 && (st = launch(c, "k_cost_32x32", timed, [&] {
-                k_cost<kSt32x32><<<static_cast<unsigned>(n32), 32, cost_smem_bytes<kSt32x32>(), s>>>(f);
+                k_cost32<<<static_cast<unsigned>(n32), kCost32Threads, sizeof(Cost32Smem), s>>>(f);
               })))
     return st;
-  if (n32 + n16 && (st = launch(c, "k_site", timed, [&] {
-                      k_site<<<static_cast<unsigned>((n32 + n16 + 63) / 64), 64, 0, s>>>(f);
-                    })))
+  const int64_t strips = site_strips(static_cast<int>(xb), static_cast<int>(yb), 32) +
+                         site_strips(static_cast<int>(xb), static_cast<int>(yb), 16);
+  if (strips && (st = launch(c, "k_site", timed, [&] {
+                   k_site<<<static_cast<unsigned>((strips + kSiteWarps - 1) / kSiteWarps),
+                            32 * kSiteWarps, kSiteSmemBytes, s>>>(f);
+                 })))
     return st;
   const int64_t cells = ((xb + 3) / 4) * ((yb + 3) / 4);
   if ((st = launch(c, "k_select", timed, [&] {
@@ -688,8 +691,7 @@ int enqueue_search(Context* c, const Frame& f, bool timed) {
                 })))
     return st;
   if (n32 && (st = launch(c, "k_layout_32x32", timed, [&] {
-                k_layout<kSt32x32><<<layout_grid(n32, layout_warps<kSt32x32>()), 32 * layout_warps<kSt32x32>(),
-                                     layout_smem_bytes<kSt32x32>(), s>>>(f);
+                k_layout32<<<static_cast<unsigned>(n32), kLayout32Threads, sizeof(Layout32Smem), s>>>(f);
               })))
     return st;
   return JXG_OK;

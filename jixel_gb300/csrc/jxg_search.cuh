@@ -94,10 +94,9 @@ struct CostSmem {
   float co[3][SIZE];      // coefficients
   float mag[3][SIZE];     // magnitude-rate terms
 };
-// Warps (candidates) per CTA of k_cost<S>: a 32x32 candidate's 37 KB of
-// shared memory goes one to a CTA, so six CTAs share an SM.
+// Warps (candidates) per CTA of k_cost<S> (the 32x32 candidates have k_cost32).
 template <int S>
-__host__ __device__ constexpr int cost_warps() { return S == kSt32x32 ? 1 : 4; }
+__host__ __device__ constexpr int cost_warps() { return 4; }
 
 // The block position of candidate `cand` of shape S: every block (DCT8),
 // even bx (8x16), even by (16x8), even bx and by (16x16), 4-aligned (32x32);
@@ -276,16 +275,15 @@ __device__ __forceinline__ void warp_coefficients(const Frame& f, int bx, int by
 // summation), below M = 2^-42 P.  Rounding to f32 is monotonic, so when
 // P - M and P + M round to the same f32 that f32 is R's; otherwise lane 0
 // takes the serial sum.
-template <int S>
-__device__ __forceinline__ float warp_selection_scale(const SearchFrame& s, const CostSmem<S>& sm,
-                                                      float qac) {
-  if (S != kSt32x32 || !s.p.sel_scale) return 1.0f;
+__device__ __forceinline__ float selection_scale_32(const SearchFrame& s, const float* co_y,
+                                                   float qac) {
+  if (!s.p.sel_scale) return 1.0f;
   const int lane = threadIdx.x & 31;
   const float* inv = s.t->inv32[1];
   auto erased_term = [&](int i) -> double {
     const int y = i >> 5, x = i & 31;
     if (x < 8 && y < 8) return 0.0;
-    const float l = sm.co[1][i];
+    const float l = co_y[i];
     return fabsf(__fmul_rn(__fmul_rn(l, __ldg(inv + i)), qac)) < 0.5f
                ? __dmul_rn(static_cast<double>(l), static_cast<double>(l))
                : 0.0;
@@ -308,75 +306,82 @@ __device__ __forceinline__ float warp_selection_scale(const SearchFrame& s, cons
   const float r = __fsub_rn(__fdiv_rn(erased, __fmul_rn(__fmul_rn(2e-4f, d), d)), 1.0f);
   return __fadd_rn(1.0f, __fmul_rn(0.6f, fminf(fmaxf(r, 0.0f), 1.0f)));
 }
-
-// The coefficient-model cost at quantizer `q` (already scaled by the
-// selection quantizer) of the coefficients in `sm`; every lane returns it.
 template <int S>
-__device__ __forceinline__ float warp_rd(const Frame& f, const SearchFrame& s, CostSmem<S>& sm,
-                                         int bx, int by, float q, float meta_r) {
+__device__ __forceinline__ float warp_selection_scale(const SearchFrame& s, const CostSmem<S>& sm,
+                                                      float qac) {
+  return S == kSt32x32 ? selection_scale_32(s, sm.co[1], qac) : 1.0f;
+}
+
+// The coefficient-model terms of channel c at quantizer `q` (already scaled
+// by the selection quantizer), by one warp: each coefficient's squared error
+// into `sse` and magnitude rate into `mag` (0 for the LLF), and the channel's
+// non-zero count and highest non-zero scan position (channel_rd /
+// sse_and_rate, src/inflated_cost.rs:435-537).
+template <int S>
+__device__ __forceinline__ void rd_channel(const SearchFrame& s, const float* co, int c, float q,
+                                           float* sse, float* mag, int* nz, uint32_t* max_scan) {
   constexpr int CX = Shape<S>::CX, CY = Shape<S>::CY, WIDTH = CX * 8, HEIGHT = CY * 8;
   constexpr int SIZE = WIDTH * HEIGHT;
   const int lane = threadIdx.x & 31;
   const SearchTables* t = s.t;
   const uint16_t* pos = pos_of(t, S);
-  float* sse_terms = &sm.in[0][0][0];  // the gather buffer is free again
-  int nz[3];
-  uint32_t max_scan[3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const float* inv = inv_of(t, S, c);
-    const float* thr = t->thr[Shape<S>::CLASS][c];
-    const float q_scaled = __fmul_rn(q, s.qm_mult[c]);
-    int n = 0;
-    uint32_t ms = 0;
-    for (int i = lane; i < SIZE; i += 32) {
-      const int y = i / WIDTH, x = i % WIDTH;
-      float e2 = 0.0f, mag = 0.0f;
-      if (!(x < CX && y < CY)) {
-        const int yfix = y >= HEIGHT / 2 ? 2 : 0;
-        const float threshold = x >= WIDTH / 2 ? thr[yfix + 1] : thr[yfix];
-        const float a = __fmul_rn(__fmul_rn(inv[i], q_scaled), sm.co[c][i]);
-        const float qv = fabsf(a) >= threshold ? roundf(a) : 0.0f;
-        const float e = __fsub_rn(a, bias_level(c, cast_i32(qv)));
-        e2 = __fmul_rn(e, e);
-        if (qv != 0.0f) {
-          ++n;
-          mag = rate_log2(s.rate_log2, fabsf(qv));
-          ms = max(ms, static_cast<uint32_t>(pos[i]));
-        }
+  const float* inv = inv_of(t, S, c);
+  const float* thr = t->thr[Shape<S>::CLASS][c];
+  const float q_scaled = __fmul_rn(q, s.qm_mult[c]);
+  int n = 0;
+  uint32_t ms = 0;
+#pragma unroll 4
+  for (int i = lane; i < SIZE; i += 32) {
+    const int y = i / WIDTH, x = i % WIDTH;
+    float e2 = 0.0f, m = 0.0f;
+    if (!(x < CX && y < CY)) {
+      const int yfix = y >= HEIGHT / 2 ? 2 : 0;
+      const float threshold = x >= WIDTH / 2 ? thr[yfix + 1] : thr[yfix];
+      const float a = __fmul_rn(__fmul_rn(inv[i], q_scaled), co[i]);
+      const float qv = fabsf(a) >= threshold ? roundf(a) : 0.0f;
+      const float e = __fsub_rn(a, bias_level(c, cast_i32(qv)));
+      e2 = __fmul_rn(e, e);
+      if (qv != 0.0f) {
+        ++n;
+        m = rate_log2(s.rate_log2, fabsf(qv));
+        ms = max(ms, static_cast<uint32_t>(pos[i]));
       }
-      sse_terms[c * SIZE + i] = e2;
-      sm.mag[c][i] = mag;
     }
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-      n += __shfl_xor_sync(0xffffffffu, n, d);
-      ms = max(ms, __shfl_xor_sync(0xffffffffu, ms, d));
-    }
-    nz[c] = n;
-    max_scan[c] = ms;
+    sse[i] = e2;
+    mag[i] = m;
   }
-  __syncwarp();
-  // the reference's running sums, each in raster order by one lane (a
-  // skipped coefficient adds +0, which leaves a sum of non-negative terms as it is)
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    n += __shfl_xor_sync(0xffffffffu, n, d);
+    ms = max(ms, __shfl_xor_sync(0xffffffffu, ms, d));
+  }
+  *nz = n;
+  *max_scan = ms;
+}
+
+// A running f32 sum in raster order by one thread (a skipped coefficient
+// adds +0, which leaves a sum of non-negative terms as it is).
+template <int SIZE>
+__device__ __forceinline__ float serial_sum(const float* terms) {
   float sum = 0.0f;
-  if (lane < 6) {
-    const float* terms = lane < 3 ? sse_terms + lane * SIZE : sm.mag[lane - 3];
 #pragma unroll 16
-    for (int i = 0; i < SIZE; ++i) sum = __fadd_rn(sum, terms[i]);
-  }
-  float sse[3], mag[3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    sse[c] = __shfl_sync(0xffffffffu, sum, c);
-    mag[c] = __shfl_sync(0xffffffffu, sum, 3 + c);
-  }
-  __syncwarp();
+  for (int i = 0; i < SIZE; ++i) sum = __fadd_rn(sum, terms[i]);
+  return sum;
+}
+
+// model_bits over the channels, the weighted distortion and the visible
+// fraction: the strategy cost (strategy_cost, src/ac_strategy.rs:1295-1378;
+// model_bits, src/inflated_cost.rs:540-547; Footprint::visible_fraction,
+// :650-659).
+template <int S>
+__device__ __forceinline__ float rd_finish(const Frame& f, const SearchFrame& s, int bx, int by,
+                                           const int* nz, const uint32_t* max_scan,
+                                           const float* sse, const float* mag, float meta_r) {
+  constexpr int CX = Shape<S>::CX, CY = Shape<S>::CY;
   const float weights[3] = {0.30f, 1.0f, 0.28f};
   float d_total = 0.0f, r_total = 0.0f;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    // model_bits (src/inflated_cost.rs:540-547)
     const float header = __fmul_rn(0.4f, rate_log2(s.rate_log2, static_cast<float>(nz[c])));
     float visited = 0.0f;
     if (nz[c]) {
@@ -389,7 +394,6 @@ __device__ __forceinline__ float warp_rd(const Frame& f, const SearchFrame& s, C
     d_total = __fadd_rn(d_total, __fmul_rn(weights[c], sse[c]));
     r_total = __fadd_rn(r_total, bits);
   }
-  // Footprint::visible_fraction (src/inflated_cost.rs:650-659)
   const int px = bx * 8, py = by * 8;
   const int vw = imin(Shape<S>::W, imax(f.a.width - px, 0));
   const int vh = imin(Shape<S>::H, imax(f.a.height - py, 0));
@@ -398,6 +402,33 @@ __device__ __forceinline__ float warp_rd(const Frame& f, const SearchFrame& s, C
                             : __fdiv_rn(static_cast<float>(vw * vh),
                                         static_cast<float>(Shape<S>::W * Shape<S>::H));
   return fmla(kRdLambda, __fadd_rn(r_total, meta_r), __fmul_rn(d_total, visible));
+}
+
+// The coefficient-model cost at quantizer `q` (already scaled by the
+// selection quantizer) of the coefficients in `sm`, by one warp; every lane
+// returns it.  The six running sums go to lanes 0-5.
+template <int S>
+__device__ __forceinline__ float warp_rd(const Frame& f, const SearchFrame& s, CostSmem<S>& sm,
+                                         int bx, int by, float q, float meta_r) {
+  constexpr int SIZE = Shape<S>::W * Shape<S>::H;
+  const int lane = threadIdx.x & 31;
+  float* sse_terms = &sm.in[0][0][0];  // the gather buffer is free again
+  int nz[3];
+  uint32_t max_scan[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    rd_channel<S>(s, sm.co[c], c, q, sse_terms + c * SIZE, sm.mag[c], &nz[c], &max_scan[c]);
+  __syncwarp();
+  float sum = 0.0f;
+  if (lane < 6) sum = serial_sum<SIZE>(lane < 3 ? sse_terms + lane * SIZE : sm.mag[lane - 3]);
+  float sse[3], mag[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    sse[c] = __shfl_sync(0xffffffffu, sum, c);
+    mag[c] = __shfl_sync(0xffffffffu, sum, 3 + c);
+  }
+  __syncwarp();
+  return rd_finish<S>(f, s, bx, by, nz, max_scan, sse, mag, meta_r);
 }
 
 // region_quant (src/ac_strategy/selection.rs:910-927) over a w x h region
@@ -438,27 +469,36 @@ __device__ __forceinline__ float util_fast_exp(float x) {
   const float scale = __uint_as_float(static_cast<uint32_t>(exponent + 127) << 23);
   return __fmul_rn(__fadd_rn(1.0f, __fdiv_rn(__fmul_rn(2.0f, r), __fsub_rn(p, r))), scale);
 }
-// The merge bias of the n x n site at pixel (x0, y0), clipped to the image,
-// by one thread: the f64 sums run serially in raster order.  GB300's f64
-// pipe retires a warp instruction in tens of cycles whether one lane or 32
-// are active, so these sums run one site per lane (k_site), never one lane
-// per site.
-__device__ __forceinline__ float site_bias_thread(const Frame& f, const SearchFrame& s, int x0,
-                                                  int y0, int n) {
-  const float* yp = f.xyb + f.a.plane;
-  const int w = f.a.width, h = f.a.height;
-  const int vw = imin(x0 + n, w) - x0, vh = imin(y0 + n, h) - y0;
-  double s1 = 0.0, s2 = 0.0;
-  for (int y = 0; y < vh; ++y) {
-    const float* row = yp + static_cast<int64_t>(y0 + y) * w + x0;
-#pragma unroll 4
-    for (int x = 0; x < vw; ++x) {
-      const double v = static_cast<double>(__ldg(row + x));
-      s1 = __dadd_rn(s1, v);
-      s2 = __dadd_rn(s2, __dmul_rn(v, v));
-    }
-  }
-  const int cnt = vw * vh;
+// site_variance_rect / site_bias (src/ac_strategy.rs:210-268) of the n x n
+// sites, n = 16 (even block coordinates) or 32 (4-aligned): the variance of
+// the site's luma, clipped to the image, from two f64 sums in raster order.
+//
+// The sums are serial, and GB300's f64 pipe retires a warp instruction in
+// tens of cycles whether one lane or 32 are active, so they run one site per
+// lane: a warp takes a strip of 32 adjacent sites along a row of sites, whose
+// rows together are one contiguous run of luma.  Row by row, the warp loads
+// the run coalesced (the next row's loads in flight while the lanes sum the
+// current one) and stages each sample's two terms in shared memory; each lane
+// then adds its site's terms, one f64 add a sample:
+//   s2: v * v is exact in f64 (a 24-bit mantissa squared has at most 48
+//       significant bits) and is built from v's bits with integer
+//       instructions;
+//   s1: when every sample of the site is a multiple of 2^-42 below 1 in
+//       magnitude (every normal sample from 2^-19 up, and any whose low
+//       mantissa bits are zero, such as black's 2^-26), every partial sum is
+//       a multiple of 2^-42 below 2^10, so no add rounds and the serial f64
+//       sum equals the int64 sum of v * 2^42.
+// A site with any other sample takes s1 serially, and s2 too when a sample
+// is subnormal or non-finite: its warp goes over the rows once more.
+constexpr int kSiteWarps = 1;  // one strip a CTA: the long 32x32 strips spread over the SMs
+struct SiteSmem {
+  double sq[32][33];
+  long long q[32][33];
+  uint32_t odd[32];
+};
+constexpr size_t kSiteSmemBytes = kSiteWarps * sizeof(SiteSmem);
+
+__device__ __forceinline__ float site_bias_of(const SearchFrame& s, double s1, double s2, int cnt) {
   float var = 0.0f;
   if (cnt) {
     const double mean = __ddiv_rn(s1, static_cast<double>(cnt));
@@ -470,27 +510,121 @@ __device__ __forceinline__ float site_bias_thread(const Frame& f, const SearchFr
   return util_fast_exp(__fmul_rn(s.p.site_k, sv));
 }
 
-// One thread per merge site: the 32x32 sites (4-aligned) first, as they take
-// four times longer, then the 16x16 sites (even block coordinates).
-__global__ void __launch_bounds__(64) k_site(const __grid_constant__ Frame f) {
-  const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
-  const int xb = f.a.xb, yb = f.a.yb;
-  const int64_t n32 = static_cast<int64_t>(xb / 4) * (yb / 4);
-  const int64_t n16 = static_cast<int64_t>(xb / 2) * (yb / 2);
-  const int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= n32 + n16) return;
-  int bx, by, n;
-  float* out;
-  if (t < n32) {
-    const int nx = xb / 4;
-    bx = 4 * static_cast<int>(t % nx), by = 4 * static_cast<int>(t / nx), n = 32, out = s.m32;
-  } else {
-    const int nx = xb / 2;
-    const int64_t u = t - n32;
-    bx = 2 * static_cast<int>(u % nx), by = 2 * static_cast<int>(u / nx), n = 16, out = s.m16;
+// the warp's strips: 32x32 sites first (they take longer), then 16x16
+template <int N>
+__device__ __forceinline__ void site_strip(const Frame& f, const SearchFrame& s, SiteSmem& sm,
+                                           int strip) {
+  constexpr int STEP = N / 8;  // blocks between sites
+  constexpr int PER_LANE = N;  // a row of 32 sites is 32 N samples
+  const int lane = threadIdx.x & 31;
+  const int xb = f.a.xb, w = f.a.width, h = f.a.height;
+  const int nx = xb / STEP, per_row = (nx + 31) / 32;
+  const int row = strip / per_row, first = (strip % per_row) * 32;
+  const int sites = imin(32, nx - first);
+  const int x0 = first * N, y0 = row * N;
+  const int vh = imin(y0 + N, h) - y0;
+  const int run = imin(sites * N, w - x0);  // samples of a row inside the image
+  const float* yp = f.xyb + f.a.plane;
+  sm.odd[lane] = 0u;
+  __syncwarp();
+  float v[PER_LANE];
+  auto load = [&](int y) {
+    const float* src = yp + static_cast<int64_t>(y0 + y) * w + x0;
+#pragma unroll
+    for (int m = 0; m < PER_LANE; ++m) {
+      const int k = lane + 32 * m;
+      v[m] = k < run ? __ldg(src + k) : 0.0f;
+    }
+  };
+  const bool mine = lane < sites;
+  const int my_x0 = x0 + lane * N;
+  const int vw = mine ? imax(imin(my_x0 + N, w) - my_x0, 0) : 0;
+  double s2 = 0.0;
+  long long isum = 0;
+  if (vh > 0) load(0);
+  for (int y = 0; y < vh; ++y) {
+#pragma unroll
+    for (int m = 0; m < PER_LANE; ++m) {
+      const int k = lane + 32 * m, i = k / N, x = k % N;
+      const uint32_t u = __float_as_uint(v[m]);
+      const uint32_t ex = (u >> 23) & 0xffu;
+      const uint32_t mant = (u & 0x7fffffu) | 0x800000u;
+      const bool zero = (u & 0x7fffffffu) == 0u;
+      // |v| < 1 and v a multiple of 2^-42: its lowest set bit, 2^(ex - 150 +
+      // ctz(mant)), at or above 2^-42
+      const int lowest = static_cast<int>(ex) + __ffs(static_cast<int>(mant)) - 1;
+      const bool in_range = ex >= 1u && ex <= 126u && lowest >= 108;
+      // bit 0: s1 needs the serial sum; bit 1: s2 too (subnormal, non-finite)
+      if (!zero && !in_range && k < run) atomicOr(&sm.odd[i], (ex == 0u || ex == 0xffu) ? 3u : 1u);
+      // v * v = p * 2^(2 ex - 300), 2^46 <= p < 2^48: biased f64 exponent
+      // 2 ex - 300 + 46 + top + 1023
+      const uint64_t p = static_cast<uint64_t>(mant) * mant;
+      const uint32_t top = static_cast<uint32_t>(p >> 47);
+      const uint64_t frac = (p << (6u - top)) & ((1ull << 52) - 1ull);
+      const uint64_t bits = (static_cast<uint64_t>(2u * ex + top + 769u) << 52) | frac;
+      sm.sq[i][x] = zero ? 0.0 : __longlong_as_double(static_cast<long long>(bits));
+      // v * 2^42 = mant * 2^(ex - 108), exact when in range (a right shift
+      // drops only zero bits)
+      const int sh = static_cast<int>(ex) - 108;
+      const uint64_t mq = sh >= 0 ? static_cast<uint64_t>(mant) << (sh & 31)
+                                  : static_cast<uint64_t>(mant >> ((-sh) & 31));
+      const long long q = in_range ? static_cast<long long>(mq) : 0;
+      sm.q[i][x] = (u >> 31) ? -q : q;
+    }
+    __syncwarp();
+    if (y + 1 < vh) load(y + 1);
+    for (int x = 0; x < vw; ++x) {
+      s2 = __dadd_rn(s2, sm.sq[lane][x]);
+      isum += sm.q[lane][x];
+    }
+    __syncwarp();
   }
-  out[static_cast<int64_t>(by) * xb + bx] =
-      s.p.site_k == 0.0f ? 1.0f : site_bias_thread(f, s, bx * 8, by * 8, n);
+  double s1 = __dmul_rn(static_cast<double>(isum), 0x1p-42);
+  const uint32_t odd = mine ? (s.p.serial_sums ? 3u : sm.odd[lane]) : 0u;
+  // the serial sums of the odd sites: the rows once more, coalesced, staged
+  // as f64 for the lanes that need them
+  if (__any_sync(0xffffffffu, odd != 0u)) {
+    const bool both = (odd & 2u) != 0u;
+    double t1 = 0.0, t2 = 0.0;
+    if (vh > 0) load(0);
+    for (int y = 0; y < vh; ++y) {
+#pragma unroll
+      for (int m = 0; m < PER_LANE; ++m) {
+        const int k = lane + 32 * m;
+        sm.sq[k / N][k % N] = static_cast<double>(v[m]);
+      }
+      __syncwarp();
+      if (y + 1 < vh) load(y + 1);
+      if (odd)
+        for (int x = 0; x < vw; ++x) {
+          const double d = sm.sq[lane][x];
+          t1 = __dadd_rn(t1, d);
+          if (both) t2 = __dadd_rn(t2, __dmul_rn(d, d));
+        }
+      __syncwarp();
+    }
+    if (odd) s1 = t1;
+    if (both) s2 = t2;
+  }
+  if (!mine) return;
+  float* out = N == 32 ? s.m32 : s.m16;
+  out[static_cast<int64_t>(row * STEP) * xb + (first + lane) * STEP] =
+      s.p.site_k == 0.0f ? 1.0f : site_bias_of(s, s1, s2, vw * vh);
+}
+
+__host__ __device__ inline int64_t site_strips(int xb, int yb, int n) {
+  const int step = n / 8, nx = xb / step, ny = yb / step;
+  return nx == 0 ? 0 : static_cast<int64_t>((nx + 31) / 32) * ny;
+}
+
+__global__ void __launch_bounds__(32 * kSiteWarps) k_site(const __grid_constant__ Frame f) {
+  extern __shared__ __align__(16) unsigned char site_smem_raw[];
+  SiteSmem& sm = reinterpret_cast<SiteSmem*>(site_smem_raw)[threadIdx.x >> 5];
+  const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
+  const int64_t strip = static_cast<int64_t>(blockIdx.x) * kSiteWarps + (threadIdx.x >> 5);
+  const int64_t n32 = site_strips(f.a.xb, f.a.yb, 32), n16 = site_strips(f.a.xb, f.a.yb, 16);
+  if (strip < n32) site_strip<32>(f, s, sm, static_cast<int>(strip));
+  else if (strip < n32 + n16) site_strip<16>(f, s, sm, static_cast<int>(strip - n32));
 }
 
 // One warp per candidate of shape S: the costs every consumer of it reads.
@@ -537,12 +671,6 @@ __global__ void __launch_bounds__(128) k_cost(const __grid_constant__ Frame f) {
       s.c16s[bi] = csel;
       s.c16r[bi] = creg;
     }
-  } else if (S == kSt32x32) {
-    const float qac = __fmul_rn(s.scale,
-                                static_cast<float>(region_quant(qf, xb, bx, by, 4, 4, s.distance)));
-    const float q = __fmul_rn(qac, warp_selection_scale<S>(s, sm, qac));
-    const float c = warp_rd<S>(f, s, sm, bx, by, q, kMetaR);
-    if (lane == 0) s.c32[bi] = c;
   } else {
     constexpr int w = Shape<S>::COVX, h = Shape<S>::COVY;
     const float qac = __fmul_rn(s.scale,
@@ -550,6 +678,62 @@ __global__ void __launch_bounds__(128) k_cost(const __grid_constant__ Frame f) {
     const float c = warp_rd<S>(f, s, sm, bx, by, qac, kMetaR);
     if (lane == 0) (S == kSt8x16 ? s.cw : s.ct)[bi] = c;
   }
+}
+
+// The 32x32 candidates (4-aligned, at region_qac with the selection
+// quantizer): a CTA of three warps each, one per channel, so that a
+// candidate's 37 KB of shared memory keeps three warps busy: the gather and
+// forward transform, then chroma-from-luma on X and B while the Y warp takes
+// the selection quantizer, then each channel's terms and its two running
+// sums (lanes 0 and 1), then the cost.
+constexpr int kCost32Threads = 96;
+struct Cost32Smem {
+  float in[3][32][33];  // gathered pixels; then the channel's sse terms
+  float co[3][1024];    // coefficients; then the channel's magnitude-rate terms
+};
+__global__ void __launch_bounds__(kCost32Threads) k_cost32(const __grid_constant__ Frame f) {
+  extern __shared__ __align__(16) unsigned char cost_smem_raw[];
+  Cost32Smem& sm = *reinterpret_cast<Cost32Smem*>(cost_smem_raw);
+  __shared__ float s_scale, s_sum[6];
+  __shared__ int s_nz[3];
+  __shared__ uint32_t s_ms[3];
+  const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
+  const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int xb = f.a.xb, yb = f.a.yb;
+  int bx, by;
+  if (!candidate_position<kSt32x32>(blockIdx.x, xb, yb, &bx, &by)) return;
+  const int bi = by * xb + bx;
+  warp_forward<kSt32x32>(f, c, bx * 8, by * 8, sm.in[c], sm.co[c]);
+  __syncthreads();
+  const float qac = __fmul_rn(s.scale, static_cast<float>(region_quant(f.qf, xb, bx, by, 4, 4, s.distance)));
+  if (c == 1) {
+    const float scale = selection_scale_32(s, sm.co[1], qac);
+    if (lane == 0) s_scale = scale;
+  } else {
+    // cmap_factors (src/ac_strategy.rs:1841-1857): the tile of the first block
+    const int t = (by >> 3) * f.a.tiles_x + (bx >> 3);
+    const float factor = c == 0 ? fmla(static_cast<float>(f.ytox[t]), 1.0f / 84.0f, 0.0f)
+                                : fmla(static_cast<float>(f.ytob[t]), 1.0f / 84.0f, 1.0f);
+    for (int i = lane; i < 1024; i += 32) sm.co[c][i] = fmla(-factor, sm.co[1][i], sm.co[c][i]);
+  }
+  __syncthreads();
+  const float q = __fmul_rn(qac, s_scale);
+  float* sse = &sm.in[c][0][0];  // this channel's gather buffer is free again
+  int n;
+  uint32_t ms;
+  // each lane writes the magnitude term over the coefficient it reads
+  rd_channel<kSt32x32>(s, sm.co[c], c, q, sse, sm.co[c], &n, &ms);
+  __syncwarp();
+  if (lane < 2) {
+    const float sum = serial_sum<1024>(lane == 0 ? sse : sm.co[c]);
+    s_sum[lane * 3 + c] = sum;
+  }
+  if (lane == 0) {
+    s_nz[c] = n;
+    s_ms[c] = ms;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) s.c32[bi] = rd_finish<kSt32x32>(f, s, bx, by, s_nz, s_ms, s_sum, s_sum + 3, kMetaR);
 }
 
 template <int S>
@@ -713,7 +897,7 @@ __device__ __forceinline__ float ordered_float(unsigned long long key) {
 
 // The relaxations of active profile `state` at one cell, in the reference's
 // order: k = 0 keep (a filled cell) or leaf, 1 wide, 2 tall, 3 square; an
-// absent one has an infinite cost.
+// absent one has an infinite cost (n is 4 for an active profile).
 struct Relax {
   int to[4];
   float cv[4];
@@ -733,6 +917,9 @@ __device__ __forceinline__ void relaxations(int state, float here, int corner, i
   };
   if (state & 1) {
     add(state, here, 0);
+    add(0, INFINITY, 0);
+    add(0, INFINITY, 0);
+    add(0, INFINITY, 0);
     return;
   }
   add(state, __fadd_rn(here, lf), kSmallLeaf);
@@ -775,13 +962,15 @@ __device__ float plan_small(RetileSmem& sm, uint64_t fixed, int w, int h, uint8_
     incoming >>= 1;
     const int shapes = sm.live[i];
     const float lf = sm.leaf[i], wd = sm.wide[i], tl = sm.tall[i], sq = sm.square[i];
+#pragma unroll 2
     for (int a0 = 0; a0 < len; a0 += 32) {
       const int a = a0 + lane;
       if (a < len) {
         const int state = act[a];
         Relax r;
         relaxations(state, ordered_float(cur[state]), corner, mask, w, shapes, lf, wd, tl, sq, &r);
-        for (int k = 0; k < r.n; ++k) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
           if (!(r.cv[k] < INFINITY)) continue;
           const uint32_t rank = static_cast<uint32_t>(a * 4 + k);
           atomicMin(&nxt[r.to[k]], (static_cast<unsigned long long>(ordered_bits(r.cv[k])) << 32) | rank);
@@ -800,24 +989,28 @@ __device__ float plan_small(RetileSmem& sm, uint64_t fixed, int w, int h, uint8_
         relaxations(state, ordered_float(cur[state]), corner, mask, w, shapes, lf, wd, tl, sq, &r);
       }
       uint32_t own = 0;
-      for (int k = 0; k < r.n; ++k) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (k >= r.n) break;
         if (!(r.cv[k] < INFINITY)) continue;
         const uint32_t rank = static_cast<uint32_t>(a * 4 + k);
         if (sm.first[r.to[k]] == rank) own |= 1u << k;
         if (static_cast<uint32_t>(nxt[r.to[k]]) == rank) from[r.to[k]] = r.ch[k];
       }
-      // exclusive prefix of the owned counts over the lanes (ranks ascend with the lane)
-      const int cnt = __popc(own);
-      int incl = cnt;
+      // the owned successors of the lanes below come first (ranks ascend
+      // with the lane, then with k): one ballot per k
+      const unsigned below = (1u << lane) - 1u;
+      int pos = nlen, total = 0;
 #pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= d) incl += v;
+      for (int k = 0; k < 4; ++k) {
+        const unsigned b = __ballot_sync(0xffffffffu, (own >> k) & 1u);
+        pos += __popc(b & below);
+        total += __popc(b);
       }
-      int pos = nlen + incl - cnt;
+#pragma unroll
       for (int k = 0; k < 4; ++k)
         if (own & (1u << k)) nact[pos++] = static_cast<uint16_t>(r.to[k]);
-      nlen += __shfl_sync(0xffffffffu, incl, 31);
+      nlen += total;
     }
     __syncwarp();
     for (int a = lane; a < nlen; a += 32) sm.first[nact[a]] = ~0u;
@@ -1511,9 +1704,9 @@ struct LayoutSmem {
   int32_t ylev[SIZE];
   float co[3][SIZE];
 };
-// Warps (transforms) per CTA of k_layout<S>; a 32x32's 20 KB goes one to a CTA.
+// Warps (transforms) per CTA of k_layout<S> (the 32x32 transforms have k_layout32).
 template <int S>
-__host__ __device__ constexpr int layout_warps() { return S == kSt32x32 ? 1 : 4; }
+__host__ __device__ constexpr int layout_warps() { return 4; }
 template <int S>
 constexpr size_t layout_smem_bytes() { return layout_warps<S>() * sizeof(LayoutSmem<S>); }
 
@@ -1541,138 +1734,230 @@ __device__ __forceinline__ float layout_threshold(const float* thr, int i, int c
   return x >= width / 2 ? thr[yfix + 1] : thr[yfix];
 }
 
+// The steps of write_ac_group for one transform of shape S at (bx, by); a
+// warp runs a channel's loops, one thread the DC steps.
 template <int S>
-__device__ __forceinline__ void layout_piece(const Frame& f, const SearchFrame& s, int bx, int by,
-                                             LayoutSmem<S>& sm) {
-  constexpr int CX = Shape<S>::CX, CY = Shape<S>::CY, COVX = Shape<S>::COVX;
-  constexpr int COVY = Shape<S>::COVY, SIZE = CX * CY * 64, COVERED = CX * CY;
-  constexpr int LOG2C = COVERED == 1 ? 0 : COVERED == 2 ? 1 : COVERED == 4 ? 2 : 4;
+struct LayoutShape {
+  static constexpr int CX = Shape<S>::CX, CY = Shape<S>::CY, COVX = Shape<S>::COVX;
+  static constexpr int COVY = Shape<S>::COVY, SIZE = CX * CY * 64, COVERED = CX * CY;
+  static constexpr int LOG2C = COVERED == 1 ? 0 : COVERED == 2 ? 1 : COVERED == 4 ? 2 : 4;
+};
+
+// Y DC levels of the covered blocks (quantize_dc_scalar, src/group.rs:286-292)
+template <int S>
+__device__ __forceinline__ void layout_y_dc(const KernelArgs& a, const float* co_y, int16_t* ydq) {
+  float dcv[16];
+  piece_dc(dct_kind_of(S), co_y, dcv);
+  for (int k = 0; k < LayoutShape<S>::COVERED; ++k)
+    ydq[k] = cast_i16(roundf(__fmul_rn(dcv[k], a.inv_dc_factor[1])));
+}
+
+// Y AC round trip (quantize_roundtrip_y_block, src/group.rs:795-820): the
+// levels parked in ylev, co_y replaced by the dequantised AC
+template <int S>
+__device__ __forceinline__ void layout_y_roundtrip(const SearchFrame& s, int32_t quant, float* co_y,
+                                                   int32_t* ylev) {
+  using L = LayoutShape<S>;
   const int lane = threadIdx.x & 31;
-  const KernelArgs& a = f.a;
-  const int xb = a.xb, yb = a.yb;
-  const int64_t nb = static_cast<int64_t>(xb) * yb;
-  const int bi = by * xb + bx;
   const SearchTables* t = s.t;
-  const int kind = dct_kind_of(S);
-  for (int c = 0; c < 3; ++c) warp_forward<S>(f, c, bx * 8, by * 8, sm.in, sm.co[c]);
-  const int32_t quant = f.qf[bi];
-  // Y DC levels of the covered blocks (quantize_dc_scalar, src/group.rs:286-292)
-  int16_t ydq[16];
-  if (lane == 0) {
-    float dcv[16];
-    piece_dc(kind, sm.co[1], dcv);
-    for (int k = 0; k < COVERED; ++k) ydq[k] = cast_i16(roundf(__fmul_rn(dcv[k], a.inv_dc_factor[1])));
-  }
-  __syncwarp();
-  // Y AC round trip (quantize_roundtrip_y_block, src/group.rs:795-820); the
-  // levels stay in registers until the store
   const float* inv_y = inv_of(t, S, 1);
   const float* mat_y = mat_of(t, S, 1);
   const float* thr_y = t->thr[Shape<S>::CLASS][1];
   const float qs_y = __fmul_rn(__fmul_rn(s.scale, static_cast<float>(quant)), 1.0f);
   const float inv_qac = __fdiv_rn(1.0f, __fmul_rn(s.scale, static_cast<float>(quant)));
-  for (int i = lane; i < SIZE; i += 32) {
-    const float val = __fmul_rn(__fmul_rn(inv_y[i], qs_y), sm.co[1][i]);
-    const int32_t q = quantize_level(val, layout_threshold(thr_y, i, CX, CY));
-    sm.ylev[i] = q;  // park the Y level
-    const int width = CX * 8, r = i / width, u = i % width;
-    sm.co[1][i] = (r < CY && u < CX) ? 0.0f
-                                     : __fmul_rn(__fmul_rn(bias_level(1, q), mat_y[i]), inv_qac);
+  for (int i = lane; i < L::SIZE; i += 32) {
+    const float val = __fmul_rn(__fmul_rn(inv_y[i], qs_y), co_y[i]);
+    const int32_t q = quantize_level(val, layout_threshold(thr_y, i, L::CX, L::CY));
+    ylev[i] = q;
+    const int width = L::CX * 8, r = i / width, u = i % width;
+    co_y[i] = (r < L::CY && u < L::CX) ? 0.0f : __fmul_rn(__fmul_rn(bias_level(1, q), mat_y[i]), inv_qac);
   }
-  __syncwarp();
-  // chroma from luma on the whole block (src/group.rs:1831-1858)
-  const int tt = (by >> 3) * a.tiles_x + (bx >> 3);
-  const float xf = fmla(static_cast<float>(f.ytox[tt]), 1.0f / 84.0f, 0.0f);
-  const float bf = fmla(static_cast<float>(f.ytob[tt]), 1.0f / 84.0f, 1.0f);
-  for (int i = lane; i < SIZE; i += 32) {
-    const float y = sm.co[1][i];
-    sm.co[0][i] = fmla(-xf, y, sm.co[0][i]);
-    sm.co[2][i] = fmla(-bf, y, sm.co[2][i]);
-  }
-  __syncwarp();
-  if (lane == 0) {
-    float xdp[16], bdp[16];
-    piece_dc(kind, sm.co[0], xdp);
-    piece_dc(kind, sm.co[2], bdp);
-    for (int iy = 0; iy < COVY; ++iy)
-      for (int ix = 0; ix < COVX; ++ix) {
-        const int k = iy * COVX + ix;
-        const int64_t b = static_cast<int64_t>(by + iy) * xb + bx + ix;
-        int16_t xq;
-        if (a.cfl_dc_factor_x != 0.0f)
-          xq = cast_i16(roundf(fmla(xdp[k], a.inv_dc_factor[0], __fmul_rn(-static_cast<float>(ydq[k]), a.cfl_dc_factor_x))));
-        else
-          xq = cast_i16(roundf(__fmul_rn(xdp[k], a.inv_dc_factor[0])));
-        const int16_t bq = cast_i16(roundf(fmla(bdp[k], a.inv_dc_factor[2],
-                                                __fmul_rn(-static_cast<float>(ydq[k]), a.cfl_dc_factor_b))));
-        f.quant_dc[b] = xq;
-        f.quant_dc[nb + b] = ydq[k];
-        f.quant_dc[2 * nb + b] = bq;
-      }
-  }
-  // X and B levels, then every channel's store, non-zero count and walk end
+}
+
+// chroma from luma on the whole block (src/group.rs:1831-1858), channel c (0 or 2)
+template <int S>
+__device__ __forceinline__ void layout_cfl(const Frame& f, int bx, int by, int c, float* co_c,
+                                           const float* co_y) {
+  const int lane = threadIdx.x & 31;
+  const int tt = (by >> 3) * f.a.tiles_x + (bx >> 3);
+  const float factor = c == 0 ? fmla(static_cast<float>(f.ytox[tt]), 1.0f / 84.0f, 0.0f)
+                              : fmla(static_cast<float>(f.ytob[tt]), 1.0f / 84.0f, 1.0f);
+  for (int i = lane; i < LayoutShape<S>::SIZE; i += 32) co_c[i] = fmla(-factor, co_y[i], co_c[i]);
+}
+
+// X and B DC levels with the DC chroma-from-luma, and the three channels' DC stores
+template <int S>
+__device__ __forceinline__ void layout_xb_dc(const Frame& f, int bx, int by, const float* co_x,
+                                             const float* co_b, const int16_t* ydq) {
+  using L = LayoutShape<S>;
+  const KernelArgs& a = f.a;
+  const int xb = a.xb;
+  const int64_t nb = static_cast<int64_t>(xb) * a.yb;
+  float xdp[16], bdp[16];
+  piece_dc(dct_kind_of(S), co_x, xdp);
+  piece_dc(dct_kind_of(S), co_b, bdp);
+  for (int iy = 0; iy < L::COVY; ++iy)
+    for (int ix = 0; ix < L::COVX; ++ix) {
+      const int k = iy * L::COVX + ix;
+      const int64_t b = static_cast<int64_t>(by + iy) * xb + bx + ix;
+      int16_t xq;
+      if (a.cfl_dc_factor_x != 0.0f)
+        xq = cast_i16(roundf(fmla(xdp[k], a.inv_dc_factor[0], __fmul_rn(-static_cast<float>(ydq[k]), a.cfl_dc_factor_x))));
+      else
+        xq = cast_i16(roundf(__fmul_rn(xdp[k], a.inv_dc_factor[0])));
+      const int16_t bq = cast_i16(roundf(fmla(bdp[k], a.inv_dc_factor[2],
+                                              __fmul_rn(-static_cast<float>(ydq[k]), a.cfl_dc_factor_b))));
+      f.quant_dc[b] = xq;
+      f.quant_dc[nb + b] = ydq[k];
+      f.quant_dc[2 * nb + b] = bq;
+    }
+}
+
+// channel c's levels (Y's from ylev) stored per covered block, its non-zero
+// count outside the LLF and its highest non-zero scan position
+template <int S>
+__device__ __forceinline__ void layout_levels(const Frame& f, const SearchFrame& s, int bx, int by,
+                                              int32_t quant, int c, const float* co_c,
+                                              const int32_t* ylev, int* nz, uint32_t* last) {
+  using L = LayoutShape<S>;
+  const int lane = threadIdx.x & 31;
+  const int xb = f.a.xb;
+  const SearchTables* t = s.t;
   const uint16_t* pos = pos_of(t, S);
+  const float* inv = inv_of(t, S, c);
+  const float* thr = t->thr[Shape<S>::CLASS][c];
+  const float qs = __fmul_rn(__fmul_rn(s.scale, static_cast<float>(quant)), f.a.qm_mul[c]);
+  int n = 0;
+  uint32_t lst = 0;
+  for (int i = lane; i < L::SIZE; i += 32) {
+    int32_t q;
+    if (c == 1) {
+      q = ylev[i];
+    } else {
+      const float val = __fmul_rn(__fmul_rn(inv[i], qs), co_c[i]);
+      q = quantize_level(val, layout_threshold(thr, i, L::CX, L::CY));
+    }
+    const int chunk = i >> 6;
+    const int64_t b = static_cast<int64_t>(by + chunk / L::COVX) * xb + bx + chunk % L::COVX;
+    const int64_t at = b * 192 + c * 64 + (i & 63);
+    if (q < -32767 || q > 32767) {
+      f.levels[at] = kLevelEscape;
+      f.wide_levels[at] = q;
+    } else {
+      f.levels[at] = static_cast<int16_t>(q);
+    }
+    const int width = L::CX * 8, r = i / width, u = i % width;
+    if (q != 0 && !(r < L::CY && u < L::CX)) {
+      ++n;
+      lst = max(lst, static_cast<uint32_t>(pos[i]));
+    }
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    n += __shfl_xor_sync(0xffffffffu, n, d);
+    lst = max(lst, __shfl_xor_sync(0xffffffffu, lst, d));
+  }
+  *nz = n;
+  *last = lst;
+}
+
+// the shifted non-zero counts of the covered blocks and the token counts at
+// the first block ([Y, X, B, 0] per group-local block), by lanes < COVERED
+template <int S>
+__device__ __forceinline__ void layout_counts(const Frame& f, int bx, int by, const int* nz,
+                                              const uint32_t* last) {
+  using L = LayoutShape<S>;
+  const int lane = threadIdx.x & 31;
+  if (lane >= L::COVERED) return;
+  const KernelArgs& a = f.a;
+  const int xb = a.xb;
+  const int64_t nb = static_cast<int64_t>(xb) * a.yb;
+  const int ix = lane % L::COVX, iy = lane / L::COVX;
+  const int64_t b = static_cast<int64_t>(by + iy) * xb + bx + ix;
+  uint32_t packed = 0;
+  for (int c = 0; c < 3; ++c) {
+    const uint32_t sh = (static_cast<uint32_t>(nz[c]) + L::COVERED - 1u) >> L::LOG2C;
+    f.nzeros[c * nb + b] = static_cast<uint8_t>(sh);
+    packed |= (sh & 0xffu) << (8 * c);
+  }
+  f.nz_packed[b] = packed;
+  const int gx = (bx + ix) / kGroupBlocks, gy = (by + iy) / kGroupBlocks;
+  const int g = gy * a.groups_x + gx;
+  const int lb = ((by + iy) % kGroupBlocks) * kGroupBlocks + (bx + ix) % kGroupBlocks;
+  uint4 cnt = make_uint4(0u, 0u, 0u, 0u);
+  if (lane == 0) {
+    auto walk = [&](int c) { return 1u + (nz[c] ? last[c] - L::COVERED + 1u : 0u); };
+    cnt = make_uint4(walk(1), walk(0), walk(2), 0u);
+  }
+  reinterpret_cast<uint4*>(f.counts)[static_cast<int64_t>(g) * 1024 + lb] = cnt;
+}
+
+// write_ac_group for one transform, by one warp
+template <int S>
+__device__ __forceinline__ void layout_piece(const Frame& f, const SearchFrame& s, int bx, int by,
+                                             LayoutSmem<S>& sm) {
+  const int lane = threadIdx.x & 31;
+  for (int c = 0; c < 3; ++c) warp_forward<S>(f, c, bx * 8, by * 8, sm.in, sm.co[c]);
+  const int32_t quant = f.qf[by * f.a.xb + bx];
+  int16_t ydq[16];
+  if (lane == 0) layout_y_dc<S>(f.a, sm.co[1], ydq);
+  __syncwarp();
+  layout_y_roundtrip<S>(s, quant, sm.co[1], sm.ylev);
+  __syncwarp();
+  layout_cfl<S>(f, bx, by, 0, sm.co[0], sm.co[1]);
+  layout_cfl<S>(f, bx, by, 2, sm.co[2], sm.co[1]);
+  __syncwarp();
+  if (lane == 0) layout_xb_dc<S>(f, bx, by, sm.co[0], sm.co[2], ydq);
   int nz[3];
   uint32_t last[3];
-  for (int c = 0; c < 3; ++c) {
-    int n = 0;
-    uint32_t lst = 0;
-    const float* inv = inv_of(t, S, c);
-    const float* thr = t->thr[Shape<S>::CLASS][c];
-    const float qs = __fmul_rn(__fmul_rn(s.scale, static_cast<float>(quant)), a.qm_mul[c]);
-    for (int i = lane; i < SIZE; i += 32) {
-      int32_t q;
-      if (c == 1) {
-        q = sm.ylev[i];
-      } else {
-        const float val = __fmul_rn(__fmul_rn(inv[i], qs), sm.co[c][i]);
-        q = quantize_level(val, layout_threshold(thr, i, CX, CY));
-      }
-      const int chunk = i >> 6;
-      const int64_t b = static_cast<int64_t>(by + chunk / COVX) * xb + bx + chunk % COVX;
-      const int64_t at = b * 192 + c * 64 + (i & 63);
-      if (q < -32767 || q > 32767) {
-        f.levels[at] = kLevelEscape;
-        f.wide_levels[at] = q;
-      } else {
-        f.levels[at] = static_cast<int16_t>(q);
-      }
-      const int width = CX * 8, r = i / width, u = i % width;
-      if (q != 0 && !(r < CY && u < CX)) {
-        ++n;
-        lst = max(lst, static_cast<uint32_t>(pos[i]));
-      }
-    }
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
-      n += __shfl_xor_sync(0xffffffffu, n, d);
-      lst = max(lst, __shfl_xor_sync(0xffffffffu, lst, d));
-    }
-    nz[c] = n;
-    last[c] = lst;
-  }
-  if (lane < COVERED) {
-    const int ix = lane % COVX, iy = lane / COVX;
-    const int64_t b = static_cast<int64_t>(by + iy) * xb + bx + ix;
-    uint32_t packed = 0;
-    for (int c = 0; c < 3; ++c) {
-      const uint32_t sh = (static_cast<uint32_t>(nz[c]) + COVERED - 1u) >> LOG2C;
-      f.nzeros[c * nb + b] = static_cast<uint8_t>(sh);
-      packed |= (sh & 0xffu) << (8 * c);
-    }
-    f.nz_packed[b] = packed;
-    // token counts at the first block ([Y, X, B, 0] per group-local block)
-    const int gx = (bx + ix) / kGroupBlocks, gy = (by + iy) / kGroupBlocks;
-    const int g = gy * a.groups_x + gx;
-    const int lb = ((by + iy) % kGroupBlocks) * kGroupBlocks + (bx + ix) % kGroupBlocks;
-    uint4 cnt = make_uint4(0u, 0u, 0u, 0u);
-    if (lane == 0) {
-      auto walk = [&](int c) { return 1u + (nz[c] ? last[c] - COVERED + 1u : 0u); };
-      cnt = make_uint4(walk(1), walk(0), walk(2), 0u);
-    }
-    reinterpret_cast<uint4*>(f.counts)[static_cast<int64_t>(g) * 1024 + lb] = cnt;
-  }
+  for (int c = 0; c < 3; ++c) layout_levels<S>(f, s, bx, by, quant, c, sm.co[c], sm.ylev, &nz[c], &last[c]);
+  layout_counts<S>(f, bx, by, nz, last);
   __syncwarp();
+}
+
+// The 32x32 transforms: a CTA of three warps each, one per channel: the
+// three forward transforms, then the Y DC and round trip, then CfL on X and
+// B, then the X/B DC (one thread) beside the three channels' levels, then
+// the counts.
+constexpr int kLayout32Threads = 96;
+struct Layout32Smem {
+  float in[3][32][33];
+  int32_t ylev[1024];
+  float co[3][1024];
+};
+__global__ void __launch_bounds__(kLayout32Threads) k_layout32(const __grid_constant__ Frame f) {
+  extern __shared__ __align__(16) unsigned char layout_smem_raw[];
+  Layout32Smem& sm = *reinterpret_cast<Layout32Smem*>(layout_smem_raw);
+  __shared__ int16_t s_ydq[16];
+  __shared__ int s_nz[3];
+  __shared__ uint32_t s_last[3];
+  constexpr int S = kSt32x32;
+  const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
+  const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int bx, by;
+  if (!candidate_position<S>(blockIdx.x, f.a.xb, f.a.yb, &bx, &by)) return;
+  if (s.map[static_cast<int64_t>(by) * f.a.xb + bx] != static_cast<uint8_t>((S << 1) | 1)) return;
+  warp_forward<S>(f, c, bx * 8, by * 8, sm.in[c], sm.co[c]);
+  const int32_t quant = f.qf[by * f.a.xb + bx];
+  __syncthreads();
+  if (c == 1) {
+    if (lane == 0) layout_y_dc<S>(f.a, sm.co[1], s_ydq);
+    __syncwarp();
+    layout_y_roundtrip<S>(s, quant, sm.co[1], sm.ylev);
+  }
+  __syncthreads();
+  if (c != 1) layout_cfl<S>(f, bx, by, c, sm.co[c], sm.co[1]);
+  __syncthreads();
+  if (threadIdx.x == 0) layout_xb_dc<S>(f, bx, by, sm.co[0], sm.co[2], s_ydq);
+  int n;
+  uint32_t lst;
+  layout_levels<S>(f, s, bx, by, quant, c, sm.co[c], sm.ylev, &n, &lst);
+  if (lane == 0) {
+    s_nz[c] = n;
+    s_last[c] = lst;
+  }
+  __syncthreads();
+  if (c == 0) layout_counts<S>(f, bx, by, s_nz, s_last);
 }
 
 // One warp per position a transform of shape S can start at; the warp codes
@@ -1869,14 +2154,15 @@ inline cudaError_t set_search_attributes() {
   set(reinterpret_cast<const void*>(k_cost<kSt16x8>), cost_smem_bytes<kSt16x8>());
   set(reinterpret_cast<const void*>(k_cost<kSt8x16>), cost_smem_bytes<kSt8x16>());
   set(reinterpret_cast<const void*>(k_cost<kSt16x16>), cost_smem_bytes<kSt16x16>());
-  set(reinterpret_cast<const void*>(k_cost<kSt32x32>), cost_smem_bytes<kSt32x32>());
+  set(reinterpret_cast<const void*>(k_cost32), sizeof(Cost32Smem));
   set(reinterpret_cast<const void*>(k_mh_incumbent), 4 * sizeof(CostSmem<kSt32x32>));
   set(reinterpret_cast<const void*>(k_layout<kStDct>), layout_smem_bytes<kStDct>());
   set(reinterpret_cast<const void*>(k_layout<kSt16x8>), layout_smem_bytes<kSt16x8>());
   set(reinterpret_cast<const void*>(k_layout<kSt8x16>), layout_smem_bytes<kSt8x16>());
   set(reinterpret_cast<const void*>(k_layout<kSt16x16>), layout_smem_bytes<kSt16x16>());
-  set(reinterpret_cast<const void*>(k_layout<kSt32x32>), layout_smem_bytes<kSt32x32>());
+  set(reinterpret_cast<const void*>(k_layout32), sizeof(Layout32Smem));
   set(reinterpret_cast<const void*>(k_retile), kRetileSmemBytes);
+  set(reinterpret_cast<const void*>(k_site), kSiteSmemBytes);
   return e;
 }
 

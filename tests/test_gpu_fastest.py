@@ -101,3 +101,12 @@ def test_serial_sums_give_the_same_frame(ctx, monkeypatch):
     compare(ctx, synthetic.config1_image(), J.distance_from_quality(40))
     compare(ctx, synthetic.generate(2100, 300, 21, noise_sigma=4.0, rectangles=40,
                                     texture_weight=0.3), 2.35)
+
+
+def test_black_regions_take_the_serial_variance(ctx):
+    # black luma sits below 2^-19, where the site variance's exact integer
+    # sum does not apply and the serial f64 sums run
+    img = synthetic.generate(256, 192, 51, rectangles=10)
+    img[32:160, 40:200] = 0
+    img[100:120, 0:256] = (3, 2, 1)
+    compare(ctx, img, 2.6)
