@@ -60,6 +60,9 @@ def parse_args():
                    help="download (context, value) token pairs instead of packed AcToken words")
     p.add_argument("--c5", action="store_true",
                    help="also time one 8192x8192 RGB16 linear frame at q85 per step")
+    p.add_argument("--frames", type=int, default=0,
+                   help="only run this many frames of the headline workload on one context, "
+                        "untimed, and exit (the target of a profiler capture)")
     return p.parse_args()
 
 
@@ -682,10 +685,31 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
                     "offsets and histograms out to pinned host memory"}
 
 
+def run_frames(args):
+    """`--frames K`: K frames of the headline workload, one after another on
+    one context (for ncu: its launches repeat every frame)."""
+    import torch
+
+    import jixel_gb300 as J
+    from jixel_gb300 import synthetic
+
+    img = synthetic.config2_image()
+    d_img = torch.from_numpy(img).cuda().contiguous()
+    ctx = J.FrontendContext(0)
+    speed = J.Speed.FASTEST if SPEED == "fastest" else J.Speed.ULTRA_FAST
+    for k in range(args.frames):
+        for q in QUALITIES:
+            ctx.run_device(d_img.data_ptr(), WIDTH, HEIGHT, 3, 8, J.EncodeConfig(speed=speed).with_quality(q))
+    torch.cuda.synchronize()
+    ctx.close()
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.frames:
+        run_frames(args)
     else:
         run_gpu(args)
 

@@ -154,6 +154,22 @@ def test_config3_subset_matches_one_frame_passes(ctx):
         b.close()
 
 
+def test_config3_batch_matches_the_oracle(ctx):
+    # all 256 images of the log-uniform RGB/RGBA mix in one replayed batch,
+    # each against the oracle's one-frame result
+    imgs = synthetic.config3_batch(256)
+    cfg = J.EncodeConfig(speed=J.Speed.ULTRA_FAST).with_quality(90)
+    b = ctx.batch()
+    try:
+        for img in imgs:
+            b.add(img, cfg)
+        b.run(use_graph=True)
+        for i, img in enumerate(imgs):
+            assert_same(b.result(i), O.frontend(img, cfg.distance), check_xyb=False)
+    finally:
+        b.close()
+
+
 def test_batch_mixes_depths_and_transfers(ctx):
     # one pass over frames of different depths and transfer functions: each
     # frame reads its own transfer table

@@ -148,6 +148,12 @@ def test_large_frame_invariants(ctx):
     compare(ctx, crop, 1.0, check_xyb=False)
 
 
+@pytest.mark.parametrize("q", [75, 90, 95])
+def test_config2_frames_whole(ctx, q):
+    # the benchmarked 3840x2160 frame at each quality, every output compared
+    compare(ctx, synthetic.config2_image(), J.distance_from_quality(q), check_xyb=False)
+
+
 def test_invalid_inputs_raise(ctx):
     img = np.zeros((8, 8, 3), np.uint8)
     with pytest.raises(J.EncodeError) as e:
