@@ -870,11 +870,13 @@ struct SmallPlan {
 // order and relaxes each successor with a strict `<`, so a successor keeps
 // the cheapest relaxation and, among equal costs, the earliest; the next
 // layer lists the successors in the order they were first reached.  The
-// warp relaxes every profile at once: a successor's 64-bit key (the cost
-// mapped to an order-preserving integer, then the relaxation's rank a * 4 + k)
-// takes an atomicMin, so it ends at the same winner; `first` takes the
-// smallest rank that reached it, and a prefix over the lanes lays the next
-// layer out in that order.
+// warp relaxes every profile at once: a successor's 64-bit key (a
+// generation, the cost mapped to an order-preserving integer, then the
+// relaxation's rank a * 4 + k) takes an atomicMin, so it ends at the same
+// winner; `first` takes the smallest (generation, rank) that reached it, and
+// ballots lay the next layer out in that order.  The generation, 64 - cell,
+// makes every entry a later cell writes smaller than the ones earlier cells
+// left behind, so no entry is ever reset.
 struct RetileSmem {
   unsigned long long key_a[512], key_b[512];
   uint32_t first[512];
@@ -890,47 +892,93 @@ __device__ __forceinline__ uint32_t ordered_bits(float v) {
   const uint32_t u = __float_as_uint(__fadd_rn(v, 0.0f));  // -0 -> +0
   return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
-__device__ __forceinline__ float ordered_float(unsigned long long key) {
-  const uint32_t k = static_cast<uint32_t>(key >> 32);
+// key: bits 43-49 generation, 11-42 ordered cost, 0-10 rank
+__device__ __forceinline__ unsigned long long dp_key(uint32_t gen, float cv, uint32_t rank) {
+  return (static_cast<unsigned long long>(gen) << 43) |
+         (static_cast<unsigned long long>(ordered_bits(cv)) << 11) | rank;
+}
+__device__ __forceinline__ float dp_cost(unsigned long long key) {
+  const uint32_t k = static_cast<uint32_t>(key >> 11);
   return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
 // The relaxations of active profile `state` at one cell, in the reference's
 // order: k = 0 keep (a filled cell) or leaf, 1 wide, 2 tall, 3 square; an
-// absent one has an infinite cost (n is 4 for an active profile).
+// absent one has an infinite cost.
 struct Relax {
   int to[4];
   float cv[4];
   uint8_t ch[4];
-  int n;
 };
 __device__ __forceinline__ void relaxations(int state, float here, int corner, int mask, int w,
                                             int shapes, float lf, float wd, float tl, float sq,
                                             Relax* r) {
   const int below_bit = 1 << w;
-  r->n = 0;
-  auto add = [&](int filled, float cv, int ch) {
-    r->to[r->n] = ((filled >> 1) | corner) & mask;
-    r->cv[r->n] = cv;
-    r->ch[r->n] = static_cast<uint8_t>(ch);
-    ++r->n;
+  auto set = [&](int k, int filled, float cv, int ch) {
+    r->to[k] = ((filled >> 1) | corner) & mask;
+    r->cv[k] = cv;
+    r->ch[k] = static_cast<uint8_t>(ch);
   };
   if (state & 1) {
-    add(state, here, 0);
-    add(0, INFINITY, 0);
-    add(0, INFINITY, 0);
-    add(0, INFINITY, 0);
+    set(0, state, here, 0);
+    set(1, 0, INFINITY, 0);
+    set(2, 0, INFINITY, 0);
+    set(3, 0, INFINITY, 0);
     return;
   }
-  add(state, __fadd_rn(here, lf), kSmallLeaf);
+  set(0, state, __fadd_rn(here, lf), kSmallLeaf);
   const bool right = (state & 2) == 0, below = (state & below_bit) == 0;
-  if (right && (shapes & 1)) add(state | 2, __fadd_rn(here, wd), kSmallWide);
-  else add(0, INFINITY, 0);
-  if (below && (shapes & 2)) add(state | below_bit, __fadd_rn(here, tl), kSmallTall);
-  else add(0, INFINITY, 0);
+  if (right && (shapes & 1)) set(1, state | 2, __fadd_rn(here, wd), kSmallWide);
+  else set(1, 0, INFINITY, 0);
+  if (below && (shapes & 2)) set(2, state | below_bit, __fadd_rn(here, tl), kSmallTall);
+  else set(2, 0, INFINITY, 0);
   if (right && below && corner == 0 && (shapes & 4))
-    add(state | 2 | below_bit | (2 << w), __fadd_rn(here, sq), kSmallSquare);
-  else add(0, INFINITY, 0);
+    set(3, state | 2 | below_bit | (2 << w), __fadd_rn(here, sq), kSmallSquare);
+  else set(3, 0, INFINITY, 0);
+}
+
+// The relaxations of one round's profile (a < len) into the next layer.
+__device__ __forceinline__ void relax_push(const Relax& r, int a, uint32_t gen,
+                                           unsigned long long* nxt, uint32_t* first) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (!(r.cv[k] < INFINITY)) continue;
+    const uint32_t rank = static_cast<uint32_t>(a * 4 + k);
+    atomicMin(&nxt[r.to[k]], dp_key(gen, r.cv[k], rank));
+    atomicMin(&first[r.to[k]], (gen << 11) | rank);
+  }
+}
+
+// After the round's atomics: the relaxations that won their successor write
+// its choice; those that reached it first place it in the next layer (ranks
+// ascend with the lane, then with k: one ballot per k).  Returns the
+// round's count of placed successors.
+__device__ __forceinline__ int relax_place(const Relax& r, bool valid, int a, uint32_t gen,
+                                           const unsigned long long* nxt, const uint32_t* first,
+                                           uint8_t* from, uint16_t* nact, int nlen) {
+  const int lane = threadIdx.x & 31;
+  uint32_t own = 0;
+  if (valid) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (!(r.cv[k] < INFINITY)) continue;
+      const uint32_t rank = static_cast<uint32_t>(a * 4 + k);
+      if (first[r.to[k]] == ((gen << 11) | rank)) own |= 1u << k;
+      if ((static_cast<uint32_t>(nxt[r.to[k]]) & 0x7ffu) == rank) from[r.to[k]] = r.ch[k];
+    }
+  }
+  const unsigned below = (1u << lane) - 1u;
+  int pos = nlen, total = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const unsigned b = __ballot_sync(0xffffffffu, (own >> k) & 1u);
+    pos += __popc(b & below);
+    total += __popc(b);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    if (own & (1u << k)) nact[pos++] = static_cast<uint16_t>(r.to[k]);
+  return total;
 }
 
 // The whole warp calls it with the same arguments; the plan is written on lane 0.
@@ -950,71 +998,54 @@ __device__ float plan_small(RetileSmem& sm, uint64_t fixed, int w, int h, uint8_
   __syncwarp();
   const int start = static_cast<int>(fixed & static_cast<uint64_t>(mask));
   if (lane == 0) {
-    cur[start] = static_cast<unsigned long long>(ordered_bits(0.0f)) << 32;
+    cur[start] = dp_key(65u, 0.0f, 0u);  // the layer before cell 0
     act[0] = static_cast<uint16_t>(start);
   }
   int len = 1;
   uint64_t incoming = fixed >> (w + 1);
   __syncwarp();
   for (int i = 0; i < cells; ++i) {
+    const uint32_t gen = static_cast<uint32_t>(64 - i);
     uint8_t* from = choices + i * states;
     const int corner = static_cast<int>(incoming & 1u) << w;
     incoming >>= 1;
     const int shapes = sm.live[i];
     const float lf = sm.leaf[i], wd = sm.wide[i], tl = sm.tall[i], sq = sm.square[i];
+    int nlen = 0;
+    if (len <= 32) {
+      // one round: the relaxations stay in registers between the two steps
+      const bool valid = lane < len;
+      Relax r;
+      if (valid) {
+        const int state = act[lane];
+        relaxations(state, dp_cost(cur[state]), corner, mask, w, shapes, lf, wd, tl, sq, &r);
+        relax_push(r, lane, gen, nxt, sm.first);
+      }
+      __syncwarp();
+      nlen = relax_place(r, valid, lane, gen, nxt, sm.first, from, nact, 0);
+    } else {
 #pragma unroll 2
-    for (int a0 = 0; a0 < len; a0 += 32) {
-      const int a = a0 + lane;
-      if (a < len) {
-        const int state = act[a];
-        Relax r;
-        relaxations(state, ordered_float(cur[state]), corner, mask, w, shapes, lf, wd, tl, sq, &r);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          if (!(r.cv[k] < INFINITY)) continue;
-          const uint32_t rank = static_cast<uint32_t>(a * 4 + k);
-          atomicMin(&nxt[r.to[k]], (static_cast<unsigned long long>(ordered_bits(r.cv[k])) << 32) | rank);
-          atomicMin(&sm.first[r.to[k]], rank);
+      for (int a0 = 0; a0 < len; a0 += 32) {
+        const int a = a0 + lane;
+        if (a < len) {
+          const int state = act[a];
+          Relax r;
+          relaxations(state, dp_cost(cur[state]), corner, mask, w, shapes, lf, wd, tl, sq, &r);
+          relax_push(r, a, gen, nxt, sm.first);
         }
       }
+      __syncwarp();
+      for (int a0 = 0; a0 < len; a0 += 32) {
+        const int a = a0 + lane;
+        const bool valid = a < len;
+        Relax r;
+        if (valid) {
+          const int state = act[a];
+          relaxations(state, dp_cost(cur[state]), corner, mask, w, shapes, lf, wd, tl, sq, &r);
+        }
+        nlen += relax_place(r, valid, a, gen, nxt, sm.first, from, nact, nlen);
+      }
     }
-    __syncwarp();
-    int nlen = 0;
-    for (int a0 = 0; a0 < len; a0 += 32) {
-      const int a = a0 + lane;
-      Relax r;
-      r.n = 0;
-      if (a < len) {
-        const int state = act[a];
-        relaxations(state, ordered_float(cur[state]), corner, mask, w, shapes, lf, wd, tl, sq, &r);
-      }
-      uint32_t own = 0;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        if (k >= r.n) break;
-        if (!(r.cv[k] < INFINITY)) continue;
-        const uint32_t rank = static_cast<uint32_t>(a * 4 + k);
-        if (sm.first[r.to[k]] == rank) own |= 1u << k;
-        if (static_cast<uint32_t>(nxt[r.to[k]]) == rank) from[r.to[k]] = r.ch[k];
-      }
-      // the owned successors of the lanes below come first (ranks ascend
-      // with the lane, then with k): one ballot per k
-      const unsigned below = (1u << lane) - 1u;
-      int pos = nlen, total = 0;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const unsigned b = __ballot_sync(0xffffffffu, (own >> k) & 1u);
-        pos += __popc(b & below);
-        total += __popc(b);
-      }
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-        if (own & (1u << k)) nact[pos++] = static_cast<uint16_t>(r.to[k]);
-      nlen += total;
-    }
-    __syncwarp();
-    for (int a = lane; a < nlen; a += 32) sm.first[nact[a]] = ~0u;
-    for (int a = lane; a < len; a += 32) cur[act[a]] = kNoKey;
     __syncwarp();
     unsigned long long* tk = cur;
     cur = nxt;
@@ -1024,7 +1055,9 @@ __device__ float plan_small(RetileSmem& sm, uint64_t fixed, int w, int h, uint8_
     nact = ta;
     len = nlen;
   }
-  const float total = cur[0] == kNoKey ? INFINITY : ordered_float(cur[0]);
+  // state 0 of the last layer, if the last cell reached it
+  const unsigned long long k0 = cur[0];
+  const float total = (k0 >> 43) == static_cast<unsigned long long>(65 - cells) ? dp_cost(k0) : INFINITY;
   __syncwarp();
   if (!(isfinite(total) && total < replace_below)) return total;
   if (lane == 0) {
