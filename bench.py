@@ -314,6 +314,16 @@ def run_gpu(args):
     ctx = ctxs[0]
     speed = J.Speed.FASTEST if SPEED == "fastest" else J.Speed.ULTRA_FAST
     cfgs = [J.EncodeConfig(speed=speed).with_quality(q) for q in QUALITIES]
+    # the autotuner picks the search kernels' launch geometry on the headline
+    # frame (results do not depend on it); every context takes its choice
+    autotune = None
+    if speed == J.Speed.FASTEST:
+        geo, tune_ms = ctx.autotune(d_img.data_ptr(), WIDTH, HEIGHT, 3, 8, cfgs[0], rounds=2)
+        for c in ctxs[1:]:
+            c.set_launch_geometry(geo)
+        autotune = {"warps_per_cta": geo,
+                    "launch_ms": {k: {str(w): round(v, 4) for w, v in t.items()}
+                                  for k, t in tune_ms.items()}}
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
     inputs = [d_img] + [d_img.clone() for _ in range(INPUT_COPIES - 1)]
     turn = [0]
@@ -434,7 +444,7 @@ def run_gpu(args):
     # end to end through the public C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(ctx, img, cfgs, args, world, dev)
+        e2e = run_e2e(ctx, img, cfgs, args, world, dev, autotune["warps_per_cta"] if autotune else None)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -451,6 +461,7 @@ def run_gpu(args):
             "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(ktimes.items())},
             "tokens_per_frame": [int(x) for x in tokens],
             "batch": batch,
+            "autotune": autotune,
             "ultrafast": ultrafast,
             "c5": c5,
         }
@@ -609,7 +620,7 @@ def run_batch(ctx, stream, flush, args, world, dev) -> dict:
     }
 
 
-def run_e2e(ctx, img, cfgs, args, world, dev):
+def run_e2e(ctx, img, cfgs, args, world, dev, geometry=None):
     """End to end through the public C ABI: every frame is uploaded from
     pinned host memory and its outputs (maps, DC levels, tokens, group
     offsets, histograms) land in pinned host memory, all inside the timed
@@ -631,6 +642,9 @@ def run_e2e(ctx, img, cfgs, args, world, dev):
     h_img.numpy()[:] = img.reshape(-1)
     nctx = max(1, args.e2e_contexts)
     ctxs = [J.FrontendContext(dev.index or 0) for _ in range(nctx)]
+    if geometry:
+        for c in ctxs:
+            c.set_launch_geometry(geometry)
     packed = not args.e2e_wide_tokens
     outs = [J.PinnedOutputs(WIDTH, HEIGHT, packed=packed) for _ in range(nctx)]
     c_cfgs = [c._c() for c in cfgs]

@@ -275,6 +275,18 @@ void jxg_batch_destroy(void* batch);
  * image: `xyb` is 3 planes of w*h floats; writes xb*yb raw field values. */
 int32_t jxg_op_fill_quant_field(void* ctx, const float* xyb, uint64_t width, uint64_t height,
                                 float distance, float inv_scale, uint8_t* quant_field);
+/* gaborish_inverse (src/gaborish.rs:44; the encoder's pre-inversion that
+ * gaborize, src/frame/quantization.rs:240-245, runs with mul 0.9908511 when
+ * Gaborish is enabled): `xyb` is 3 planes of w*h floats, `out` receives the
+ * filtered planes (a symmetric 5x5 with mirror-reflected edges, every output
+ * from the source pixels).  `mul` must be non-negative. */
+int32_t jxg_op_gaborish_inverse(void* ctx, const float* xyb, uint64_t width, uint64_t height,
+                                float mul, float* out);
+/* The decoder's Gaborish (src/epf_filter.rs:165, gaborish_pixel
+ * src/epf_filter/kernels.rs:134): the 3x3 with clamped edges and the
+ * default weights, products fused into the sums as the NEON and AVX2+FMA
+ * backends do. */
+int32_t jxg_op_gaborish(void* ctx, const float* xyb, uint64_t width, uint64_t height, float* out);
 /* DctFn<8, 8, 64> (src/dct.rs:172, scalar dct8x8 :631): `count` blocks of 64
  * row-major samples in, 64 coefficients (transposed storage, 1/64 scale) out. */
 int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coefficients);
@@ -390,6 +402,32 @@ int32_t jxg_selftest_token_lookback(void* ctx, uint32_t polls);
  * smallest differing pattern (0xFFFFFFFF when none). */
 int32_t jxg_selftest_math(void* ctx, int32_t which, uint32_t lo_bits, uint32_t hi_bits,
                           uint64_t* mismatches, uint32_t* first_bad);
+
+/* Launch geometry and its autotuner ---------------------------------------
+ * Warps per CTA of the Speed::Fastest kernels whose warps work
+ * independently (each warp a candidate transform, a placed transform, a
+ * re-tiling tile or a strip of merge sites), in this order: the DCT8,
+ * 16x8, 8x16 and 16x16 costs, the DCT8, 16x8, 8x16 and 16x16 layout
+ * coding, the re-tiling DP, the site variance.  Results never depend on it;
+ * its speed does, by occupancy and tail against the GPU's shared memory and
+ * SM count.  It has no counterpart in the reference, whose thread pool needs
+ * no tuning. */
+#define JXG_TUNE_KERNELS 10
+/* The context's current warps per CTA (JXG_TUNE_KERNELS bytes). */
+int32_t jxg_get_launch_geometry(void* ctx, uint8_t* warps);
+/* Sets them (each 1, 2, 4 or 8), e.g. from a choice saved for this GPU. */
+int32_t jxg_set_launch_geometry(void* ctx, const uint8_t* warps);
+/* Times every candidate (1, 2, 4, 8 warps per CTA, all kernels at once) on
+ * `rounds` passes of the given frame (device pixels, as
+ * jxg_frontend_run_device; a Speed::Fastest config, the only one that
+ * launches these kernels) after one untimed pass each, with CUDA events per
+ * launch, and keeps each kernel's fastest.  `times_ms`, if not NULL,
+ * receives JXG_TUNE_KERNELS x 4 average launch times (NaN where a kernel did
+ * not run).  The passes reuse the context's buffers; the context's
+ * previous outputs are overwritten. */
+int32_t jxg_autotune(void* ctx, const void* pixels, uint64_t width, uint64_t height,
+                     int32_t channels, int32_t bits, const jxg_config* config, int32_t rounds,
+                     double* times_ms);
 
 /* Kernel timing -------------------------------------------------------- */
 /* With `enable`, every launch of this context is bracketed by CUDA events on

@@ -33,6 +33,8 @@ EXPORTS = [
     "jxg_batch_result",
     "jxg_batch_destroy",
     "jxg_op_fill_quant_field",
+    "jxg_op_gaborish_inverse",
+    "jxg_op_gaborish",
     "jxg_op_dct8x8",
     "jxg_op_pack_tokens",
     "jxg_op_dct",
@@ -42,6 +44,9 @@ EXPORTS = [
     "jxg_selftest_bounded_wait",
     "jxg_selftest_token_lookback",
     "jxg_selftest_math",
+    "jxg_get_launch_geometry",
+    "jxg_set_launch_geometry",
+    "jxg_autotune",
     "jxg_enable_kernel_timing",
     "jxg_kernel_times",
     "jxg_reset_kernel_times",
@@ -49,6 +54,7 @@ EXPORTS = [
 
 NUM_FINE_AC_CONTEXTS = 14850
 NOALLOC_MAX_GROUPS = 10922
+TUNE_KERNELS = 10
 ALPHABET_SIZE = 128
 
 
@@ -148,6 +154,8 @@ def load() -> ctypes.CDLL:
                                    ctypes.POINTER(FrontendOutput)]),
         "jxg_batch_destroy": (None, [vp]),
         "jxg_op_fill_quant_field": (i32, [vp, vp, u64, u64, f32, f32, vp]),
+        "jxg_op_gaborish_inverse": (i32, [vp, vp, u64, u64, ctypes.c_float, vp]),
+        "jxg_op_gaborish": (i32, [vp, vp, u64, u64, vp]),
         "jxg_op_dct8x8": (i32, [vp, vp, u64, vp]),
         "jxg_op_pack_tokens": (i32, [vp, vp, vp, u64, vp, u64, vp]),
         "jxg_op_dct": (i32, [vp, i32, vp, u64, vp, vp]),
@@ -158,6 +166,9 @@ def load() -> ctypes.CDLL:
         "jxg_selftest_token_lookback": (i32, [vp, ctypes.c_uint32]),
         "jxg_selftest_math": (i32, [vp, i32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(u64),
                                     ctypes.POINTER(ctypes.c_uint32)]),
+        "jxg_get_launch_geometry": (i32, [vp, vp]),
+        "jxg_set_launch_geometry": (i32, [vp, vp]),
+        "jxg_autotune": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config), i32, vp]),
         "jxg_enable_kernel_timing": (i32, [vp, i32]),
         "jxg_kernel_times": (i32, [vp, ctypes.POINTER(ctypes.c_char_p),
                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(u64), i32]),

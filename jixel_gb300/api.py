@@ -369,6 +369,22 @@ class FrontendContext:
                                                       inv_scale, out.ctypes.data))
         return out
 
+    def gaborish_inverse(self, xyb: np.ndarray, mul: float = 0.9908511) -> np.ndarray:
+        """gaborish_inverse (src/gaborish.rs:44) of (3, h, w) planes."""
+        x = np.ascontiguousarray(xyb, np.float32)
+        out = np.zeros_like(x)
+        self._check(self._lib.jxg_op_gaborish_inverse(self._ctx, x.ctypes.data, x.shape[2],
+                                                      x.shape[1], mul, out.ctypes.data))
+        return out
+
+    def gaborish(self, xyb: np.ndarray) -> np.ndarray:
+        """The decoder's Gaborish (src/epf_filter.rs:165) of (3, h, w) planes."""
+        x = np.ascontiguousarray(xyb, np.float32)
+        out = np.zeros_like(x)
+        self._check(self._lib.jxg_op_gaborish(self._ctx, x.ctypes.data, x.shape[2], x.shape[1],
+                                              out.ctypes.data))
+        return out
+
     def dct8x8(self, blocks: np.ndarray) -> np.ndarray:
         blocks = np.ascontiguousarray(blocks, np.float32).reshape(-1, 64)
         out = np.zeros_like(blocks)
@@ -432,6 +448,34 @@ class FrontendContext:
             self._ctx, tokens.ctypes.data if tokens.size else None, goffs.ctypes.data,
             goffs.shape[0] - 1, words.ctypes.data, words.shape[0], woffs.ctypes.data))
         return words[: int(woffs[-1])], woffs
+
+    # launch geometry and its autotuner --------------------------------------
+    TUNE_KERNELS = ("k_cost_dct8", "k_cost_16x8", "k_cost_8x16", "k_cost_16x16", "k_layout_dct8",
+                    "k_layout_16x8", "k_layout_8x16", "k_layout_16x16", "k_retile", "k_site")
+
+    def launch_geometry(self) -> dict:
+        """Warps per CTA of each tunable Speed::Fastest kernel."""
+        w = (ctypes.c_uint8 * len(self.TUNE_KERNELS))()
+        self._check(self._lib.jxg_get_launch_geometry(self._ctx, w))
+        return dict(zip(self.TUNE_KERNELS, list(w)))
+
+    def set_launch_geometry(self, geometry: dict):
+        cur = self.launch_geometry()
+        cur.update(geometry)
+        w = (ctypes.c_uint8 * len(self.TUNE_KERNELS))(*[cur[k] for k in self.TUNE_KERNELS])
+        self._check(self._lib.jxg_set_launch_geometry(self._ctx, w))
+
+    def autotune(self, device_ptr: int, width: int, height: int, channels: int, bits: int,
+                 config: EncodeConfig, rounds: int = 2) -> tuple[dict, dict]:
+        """jxg_autotune on a frame in device memory: the chosen geometry and
+        every candidate's average launch time {kernel: {warps: ms}}."""
+        times = np.full(len(self.TUNE_KERNELS) * 4, np.nan, np.float64)
+        cfg = config._c()
+        self._check(self._lib.jxg_autotune(self._ctx, device_ptr, width, height, channels, bits,
+                                           ctypes.byref(cfg), rounds, times.ctypes.data))
+        t = {k: {w: float(times[i * 4 + j]) for j, w in enumerate((1, 2, 4, 8))}
+             for i, k in enumerate(self.TUNE_KERNELS)}
+        return self.launch_geometry(), t
 
     # timing -------------------------------------------------------------
     def enable_kernel_timing(self, on: bool = True):

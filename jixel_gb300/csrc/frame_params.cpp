@@ -605,4 +605,29 @@ void natural_order_8x8(uint8_t scan[64], uint8_t position[64]) {
   for (int i = 0; i < 64; ++i) position[scan[i]] = static_cast<uint8_t>(i);
 }
 
+void gaborish_inverse_weights(float mul, float out[6]) {
+  // K_GABORISH (src/gaborish.rs:32-38)
+  static const float k[5] = {-0.09495815671340026f, -0.041031725066768575f, 0.013710004822696948f,
+                             0.006510206083837737f, -0.0014789063378272242f};
+  const float w_r = mul * k[0], w_d = mul * k[1], w_r2 = mul * k[2], w_l = mul * k[3];
+  const float w_d2 = mul * k[4];
+  float sum = 1.0f + mul * 4.0f * (k[0] + k[1] + k[2] + k[4] + 2.0f * k[3]);
+  if (sum < 1e-5f) sum = 1e-5f;
+  const float norm = 1.0f / sum;
+  out[0] = norm;
+  out[1] = norm * w_r;
+  out[2] = norm * w_d;
+  out[3] = norm * w_r2;
+  out[4] = norm * w_l;
+  out[5] = norm * w_d2;
+}
+
+void gaborish_weights(float out[3]) {
+  const float w1 = 1.1f * 0.10469957f, w2 = 1.1f * 0.05568054f;
+  const float norm = 1.0f / (1.0f + 4.0f * (w1 + w2));
+  out[0] = norm;
+  out[1] = w1 * norm;
+  out[2] = w2 * norm;
+}
+
 }  // namespace jxg

@@ -107,6 +107,12 @@ int search_tables(const DistanceParams& p, SearchTables* t, SearchParams* sp);
 int search_matrices(const DistanceParams& p, SearchTables* t);
 void search_params(float distance, SearchParams* sp);
 
+// Gaborish weights: gaborish_inverse's normalised centre, r, d, R, L, D at
+// `mul` (src/gaborish.rs:44-72), and the decoder's 3x3 norm, W1 norm, W2
+// norm (src/epf_filter.rs:165-169).
+void gaborish_inverse_weights(float mul, float out[6]);
+void gaborish_weights(float out[3]);
+
 int compute_distance_params(float distance, DistanceParams* out);
 // DCT8 tables of DequantMatrices::new_fast (the library table below d = 0.3).
 int dct8_tables(float distance, float matrix[3][64], float inv[3][64]);

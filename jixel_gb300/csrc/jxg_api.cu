@@ -16,6 +16,7 @@
 #include "frame_params.h"
 #include "jxg_kernels.cuh"
 #include "jxg_search.cuh"
+#include "jxg_filters.cuh"
 
 namespace jxg {
 namespace {
@@ -138,6 +139,8 @@ struct Context {
   size_t frames_bytes = 0, pixel_bytes = 0;
   bool have_frame = false;
   uint64_t epoch = 0;  // bumped by every plan: batches recorded earlier re-plan
+  // launch geometry of the tunable search and layout kernels (warps per CTA)
+  uint8_t tune[jxg::kTuneKernels] = {4, 4, 4, 4, 4, 4, 4, 4, jxg::kRetileWarps, jxg::kSiteWarps};
   // timing
   bool timing = false;
   std::vector<PendingEvent> pending;
@@ -610,23 +613,30 @@ int enqueue_search(Context* c, const Frame& f, bool timed) {
   JXG_CUDA(c, cudaMemcpyAsync(sf.block_qf, f.qf, nb, cudaMemcpyDeviceToDevice, s));
   JXG_CUDA(c, cudaMemsetAsync(sf.map, 1, nb, s));
   auto grid4 = [](int64_t n) { return static_cast<unsigned>((n + 3) / 4); };
+  // the tuned warps per CTA of kernel k, its grid over n warps' work
+  auto warps = [&](int k) { return static_cast<int>(c->tune[k]); };
+  auto grid_of = [&](int64_t n, int k) { return static_cast<unsigned>((n + warps(k) - 1) / warps(k)); };
   int st;
   const int64_t n16 = (xb / 2) * (yb / 2), n8x16 = (xb / 2) * yb, n16x8 = xb * (yb / 2);
   const int64_t n32 = (xb / 4) * (yb / 4);
   if ((st = launch(c, "k_cost_dct8", timed, [&] {
-         k_cost<kStDct><<<grid4(nb), 128, cost_smem_bytes<kStDct>(), s>>>(f);
+         k_cost<kStDct><<<grid_of(nb, kTuneCostDct8), 32 * warps(kTuneCostDct8),
+                          warps(kTuneCostDct8) * sizeof(CostSmem<kStDct>), s>>>(f);
        })))
     return st;
   if (n16 && (st = launch(c, "k_cost_16x16", timed, [&] {
-                k_cost<kSt16x16><<<grid4(n16), 128, cost_smem_bytes<kSt16x16>(), s>>>(f);
+                k_cost<kSt16x16><<<grid_of(n16, kTuneCost16x16), 32 * warps(kTuneCost16x16),
+                                   warps(kTuneCost16x16) * sizeof(CostSmem<kSt16x16>), s>>>(f);
               })))
     return st;
   if (n8x16 && (st = launch(c, "k_cost_8x16", timed, [&] {
-                  k_cost<kSt8x16><<<grid4(n8x16), 128, cost_smem_bytes<kSt8x16>(), s>>>(f);
+                  k_cost<kSt8x16><<<grid_of(n8x16, kTuneCost8x16), 32 * warps(kTuneCost8x16),
+                                    warps(kTuneCost8x16) * sizeof(CostSmem<kSt8x16>), s>>>(f);
                 })))
     return st;
   if (n16x8 && (st = launch(c, "k_cost_16x8", timed, [&] {
-                  k_cost<kSt16x8><<<grid4(n16x8), 128, cost_smem_bytes<kSt16x8>(), s>>>(f);
+                  k_cost<kSt16x8><<<grid_of(n16x8, kTuneCost16x8), 32 * warps(kTuneCost16x8),
+                                    warps(kTuneCost16x8) * sizeof(CostSmem<kSt16x8>), s>>>(f);
                 })))
     return st;
   if (n32 && (st = launch(c, "k_cost_32x32", timed, [&] {
@@ -636,8 +646,8 @@ int enqueue_search(Context* c, const Frame& f, bool timed) {
   const int64_t strips = site_strips(static_cast<int>(xb), static_cast<int>(yb), 32) +
                          site_strips(static_cast<int>(xb), static_cast<int>(yb), 16);
   if (strips && (st = launch(c, "k_site", timed, [&] {
-                   k_site<<<static_cast<unsigned>((strips + kSiteWarps - 1) / kSiteWarps),
-                            32 * kSiteWarps, kSiteSmemBytes, s>>>(f);
+                   k_site<<<grid_of(strips, kTuneSite), 32 * warps(kTuneSite),
+                            warps(kTuneSite) * sizeof(SiteSmem), s>>>(f);
                  })))
     return st;
   const int64_t cells = ((xb + 3) / 4) * ((yb + 3) / 4);
@@ -645,8 +655,8 @@ int enqueue_search(Context* c, const Frame& f, bool timed) {
          k_select<<<static_cast<unsigned>((cells + 127) / 128), 128, 0, s>>>(f);
        })) ||
       (st = launch(c, "k_retile", timed, [&] {
-         k_retile<<<static_cast<unsigned>((tiles + kRetileWarps - 1) / kRetileWarps),
-                    32 * kRetileWarps, kRetileSmemBytes, s>>>(f);
+         k_retile<<<grid_of(tiles, kTuneRetile), 32 * warps(kTuneRetile),
+                    warps(kTuneRetile) * sizeof(RetileSmem), s>>>(f);
        })) ||
       (st = launch(c, "k_adjust", timed, [&] {
          k_adjust<<<static_cast<unsigned>((nb + 255) / 256), 256, 0, s>>>(f);
@@ -669,25 +679,24 @@ int enqueue_search(Context* c, const Frame& f, bool timed) {
   if ((st = launch(c, "k_qf_median", timed, [&] { k_qf_median<<<1, 256, 0, s>>>(f); })))
     return st;
   // the coding of the layout: a launch per transform shape
-  auto layout_grid = [](int64_t n, int warps) { return static_cast<unsigned>((n + warps - 1) / warps); };
   if ((st = launch(c, "k_layout_dct8", timed, [&] {
-         k_layout<kStDct><<<layout_grid(nb, layout_warps<kStDct>()), 32 * layout_warps<kStDct>(),
-                            layout_smem_bytes<kStDct>(), s>>>(f);
+         k_layout<kStDct><<<grid_of(nb, kTuneLayoutDct8), 32 * warps(kTuneLayoutDct8),
+                            warps(kTuneLayoutDct8) * sizeof(LayoutSmem<kStDct>), s>>>(f);
        })))
     return st;
   if (n16 && (st = launch(c, "k_layout_16x16", timed, [&] {
-                k_layout<kSt16x16><<<layout_grid(n16, layout_warps<kSt16x16>()), 32 * layout_warps<kSt16x16>(),
-                                     layout_smem_bytes<kSt16x16>(), s>>>(f);
+                k_layout<kSt16x16><<<grid_of(n16, kTuneLayout16x16), 32 * warps(kTuneLayout16x16),
+                                     warps(kTuneLayout16x16) * sizeof(LayoutSmem<kSt16x16>), s>>>(f);
               })))
     return st;
   if (n8x16 && (st = launch(c, "k_layout_8x16", timed, [&] {
-                  k_layout<kSt8x16><<<layout_grid(n8x16, layout_warps<kSt8x16>()), 32 * layout_warps<kSt8x16>(),
-                                      layout_smem_bytes<kSt8x16>(), s>>>(f);
+                  k_layout<kSt8x16><<<grid_of(n8x16, kTuneLayout8x16), 32 * warps(kTuneLayout8x16),
+                                      warps(kTuneLayout8x16) * sizeof(LayoutSmem<kSt8x16>), s>>>(f);
                 })))
     return st;
   if (n16x8 && (st = launch(c, "k_layout_16x8", timed, [&] {
-                  k_layout<kSt16x8><<<layout_grid(n16x8, layout_warps<kSt16x8>()), 32 * layout_warps<kSt16x8>(),
-                                      layout_smem_bytes<kSt16x8>(), s>>>(f);
+                  k_layout<kSt16x8><<<grid_of(n16x8, kTuneLayout16x8), 32 * warps(kTuneLayout16x8),
+                                      warps(kTuneLayout16x8) * sizeof(LayoutSmem<kSt16x8>), s>>>(f);
                 })))
     return st;
   if (n32 && (st = launch(c, "k_layout_32x32", timed, [&] {
@@ -1532,6 +1541,51 @@ int32_t jxg_op_fill_quant_field(void* ctx, const float* xyb, uint64_t width, uin
   return jxg::wait(c);
 }
 
+namespace {
+// The gaborish operators: 3 planes in from the host, one launch, 3 planes out.
+int32_t gaborish_op(void* ctx, const float* xyb, uint64_t width, uint64_t height, float* out,
+                    bool inverse, float mul) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !xyb || !out) return JXG_ERR_INVALID_ARGUMENT;
+  if (width == 0 || height == 0) return JXG_OK;
+  if (width > (1u << 20) || height > (1u << 20) || width * height > (1ull << 31))
+    return JXG_ERR_DIMENSION_TOO_LARGE;
+  if (inverse && !(mul >= 0.0f)) return JXG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(c->device);
+  int st;
+  const size_t bytes = 3 * width * height * 4;
+  if ((st = jxg::ensure(c, c->op_in, bytes)) || (st = jxg::ensure(c, c->op_out, bytes))) return st;
+  cudaStream_t s = c->stream;
+  JXG_CUDA(c, cudaMemcpyAsync(c->op_in.ptr, xyb, bytes, cudaMemcpyHostToDevice, s));
+  jxg::GaborishWeights k{};
+  if (inverse) jxg::gaborish_inverse_weights(mul, k.w);
+  else jxg::gaborish_weights(k.w);
+  const dim3 grid(static_cast<unsigned>((width + jxg::kGabTileX - 1) / jxg::kGabTileX),
+                  static_cast<unsigned>((height + jxg::kGabTileY - 1) / jxg::kGabTileY), 3);
+  const float* in = static_cast<const float*>(c->op_in.ptr);
+  float* o = static_cast<float*>(c->op_out.ptr);
+  const int w = static_cast<int>(width), h = static_cast<int>(height);
+  st = inverse ? jxg::launch(c, "k_gaborish_inverse", c->timing, [&] {
+    jxg::k_gaborish_inverse<<<grid, jxg::kGabThreads, 0, s>>>(in, o, w, h, k);
+  })
+               : jxg::launch(c, "k_gaborish", c->timing, [&] {
+                   jxg::k_gaborish<<<grid, jxg::kGabThreads, 0, s>>>(in, o, w, h, k);
+                 });
+  if (st) return st;
+  JXG_CUDA(c, cudaMemcpyAsync(out, c->op_out.ptr, bytes, cudaMemcpyDeviceToHost, s));
+  return jxg::wait(c);
+}
+}  // namespace
+
+int32_t jxg_op_gaborish_inverse(void* ctx, const float* xyb, uint64_t width, uint64_t height,
+                                float mul, float* out) {
+  return gaborish_op(ctx, xyb, width, height, out, true, mul);
+}
+
+int32_t jxg_op_gaborish(void* ctx, const float* xyb, uint64_t width, uint64_t height, float* out) {
+  return gaborish_op(ctx, xyb, width, height, out, false, 0.0f);
+}
+
 int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coefficients) {
   Context* c = static_cast<Context*>(ctx);
   if (!c || !blocks || !coefficients) return JXG_ERR_INVALID_ARGUMENT;
@@ -1845,6 +1899,74 @@ int32_t jxg_selftest_math(void* ctx, int32_t which, uint32_t lo_bits, uint32_t h
   if ((st = jxg::wait(c))) return st;
   *mismatches = n;
   return JXG_OK;
+}
+
+int32_t jxg_get_launch_geometry(void* ctx, uint8_t* warps) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !warps) return JXG_ERR_INVALID_ARGUMENT;
+  std::memcpy(warps, c->tune, jxg::kTuneKernels);
+  return JXG_OK;
+}
+
+int32_t jxg_set_launch_geometry(void* ctx, const uint8_t* warps) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !warps) return JXG_ERR_INVALID_ARGUMENT;
+  for (int k = 0; k < jxg::kTuneKernels; ++k)
+    if (warps[k] != 1 && warps[k] != 2 && warps[k] != 4 && warps[k] != 8)
+      return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "warps per CTA must be 1, 2, 4 or 8");
+  std::memcpy(c->tune, warps, jxg::kTuneKernels);
+  return JXG_OK;
+}
+
+int32_t jxg_autotune(void* ctx, const void* pixels, uint64_t width, uint64_t height,
+                     int32_t channels, int32_t bits, const jxg_config* config, int32_t rounds,
+                     double* times_ms) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !pixels || !config || rounds < 1) return JXG_ERR_INVALID_ARGUMENT;
+  if (c->async_pending) {
+    const int st = jxg_frontend_wait(ctx);
+    if (st) return st;
+  }
+  cudaSetDevice(c->device);
+  static const char* const kNames[jxg::kTuneKernels] = {
+      "k_cost_dct8",   "k_cost_16x8",   "k_cost_8x16",   "k_cost_16x16", "k_layout_dct8",
+      "k_layout_16x8", "k_layout_8x16", "k_layout_16x16", "k_retile",    "k_site"};
+  static const uint8_t kCandidates[4] = {1, 2, 4, 8};
+  const bool was_timing = c->timing;
+  uint8_t pick[jxg::kTuneKernels];
+  double best[jxg::kTuneKernels];
+  std::memcpy(pick, c->tune, sizeof(pick));
+  for (double& b : best) b = INFINITY;
+  int st = JXG_OK;
+  for (int ci = 0; ci < 4 && st == JXG_OK; ++ci) {
+    std::memset(c->tune, kCandidates[ci], sizeof(c->tune));
+    c->timing = false;  // one untimed pass first
+    if ((st = jxg::single_pass(c, pixels, width, height, channels, bits, config, true)) ||
+        (st = jxg::wait(c)))
+      break;
+    jxg::collect_times(c);
+    c->times.clear();
+    c->timing = true;
+    for (int r = 0; r < rounds && st == JXG_OK; ++r)
+      st = jxg::single_pass(c, pixels, width, height, channels, bits, config, true);
+    if (st || (st = jxg::wait(c))) break;
+    jxg::collect_times(c);
+    for (int k = 0; k < jxg::kTuneKernels; ++k) {
+      const auto it = c->times.find(kNames[k]);
+      const double ms = it == c->times.end() || it->second.launches == 0
+                            ? NAN
+                            : it->second.total_ms / static_cast<double>(it->second.launches);
+      if (times_ms) times_ms[k * 4 + ci] = ms;
+      if (ms < best[k]) {
+        best[k] = ms;
+        pick[k] = kCandidates[ci];
+      }
+    }
+  }
+  c->times.clear();
+  c->timing = was_timing;
+  std::memcpy(c->tune, pick, sizeof(pick));
+  return st;
 }
 
 int32_t jxg_enable_kernel_timing(void* ctx, int32_t enable) {

@@ -40,6 +40,17 @@ namespace jxg {
 constexpr float kRdLambda = 0.08086717f;
 constexpr float kMetaR = 4.0f;
 
+// Launch geometry the autotuner chooses (warps, i.e. candidates, tiles or
+// strips, per CTA) for the kernels whose warps work independently: the
+// cost and layout kernels of DCT8 / 16x8 / 8x16 / 16x16, the re-tiling and
+// the site variance.  Results do not depend on it.
+constexpr int kMaxTuneWarps = 8;
+enum TuneKernel {
+  kTuneCostDct8, kTuneCost16x8, kTuneCost8x16, kTuneCost16x16,
+  kTuneLayoutDct8, kTuneLayout16x8, kTuneLayout8x16, kTuneLayout16x16,
+  kTuneRetile, kTuneSite, kTuneKernels
+};
+
 // Shapes: pixel footprint W x H, normalised coefficient block CX >= CY (in
 // 8x8 blocks), and how the forward transform runs (src/dct.rs: dct8x8 rows
 // then transposed columns; dct16x8 / dct16x16 / dct32x32 columns first;
@@ -94,9 +105,6 @@ struct CostSmem {
   float co[3][SIZE];      // coefficients
   float mag[3][SIZE];     // magnitude-rate terms
 };
-// Warps (candidates) per CTA of k_cost<S> (the 32x32 candidates have k_cost32).
-template <int S>
-__host__ __device__ constexpr int cost_warps() { return 4; }
 
 // The block position of candidate `cand` of shape S: every block (DCT8),
 // even bx (8x16), even by (16x8), even bx and by (16x16), 4-aligned (32x32);
@@ -490,13 +498,14 @@ __device__ __forceinline__ float util_fast_exp(float x) {
 //       sum equals the int64 sum of v * 2^42.
 // A site with any other sample takes s1 serially, and s2 too when a sample
 // is subnormal or non-finite: its warp goes over the rows once more.
-constexpr int kSiteWarps = 1;  // one strip a CTA: the long 32x32 strips spread over the SMs
+// Strips per CTA: tuned per device (default one: the long 32x32 strips
+// spread over the SMs); the kernel reads it from blockDim.
+constexpr int kSiteWarps = 1;
 struct SiteSmem {
   double sq[32][33];
   long long q[32][33];
   uint32_t odd[32];
 };
-constexpr size_t kSiteSmemBytes = kSiteWarps * sizeof(SiteSmem);
 
 __device__ __forceinline__ float site_bias_of(const SearchFrame& s, double s1, double s2, int cnt) {
   float var = 0.0f;
@@ -617,11 +626,11 @@ __host__ __device__ inline int64_t site_strips(int xb, int yb, int n) {
   return nx == 0 ? 0 : static_cast<int64_t>((nx + 31) / 32) * ny;
 }
 
-__global__ void __launch_bounds__(32 * kSiteWarps) k_site(const __grid_constant__ Frame f) {
+__global__ void __launch_bounds__(32 * kMaxTuneWarps) k_site(const __grid_constant__ Frame f) {
   extern __shared__ __align__(16) unsigned char site_smem_raw[];
   SiteSmem& sm = reinterpret_cast<SiteSmem*>(site_smem_raw)[threadIdx.x >> 5];
   const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
-  const int64_t strip = static_cast<int64_t>(blockIdx.x) * kSiteWarps + (threadIdx.x >> 5);
+  const int64_t strip = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int64_t n32 = site_strips(f.a.xb, f.a.yb, 32), n16 = site_strips(f.a.xb, f.a.yb, 16);
   if (strip < n32) site_strip<32>(f, s, sm, static_cast<int>(strip));
   else if (strip < n32 + n16) site_strip<16>(f, s, sm, static_cast<int>(strip - n32));
@@ -634,13 +643,13 @@ __global__ void __launch_bounds__(32 * kSiteWarps) k_site(const __grid_constant_
 //   8x16     even bx (the DP's horizontal pairs), 16x8 even by (vertical pairs)
 //   32x32    4-aligned: at region_qac with the selection quantizer
 template <int S>
-__global__ void __launch_bounds__(128) k_cost(const __grid_constant__ Frame f) {
+__global__ void __launch_bounds__(32 * kMaxTuneWarps) k_cost(const __grid_constant__ Frame f) {
   extern __shared__ __align__(16) unsigned char cost_smem_raw[];
   CostSmem<S>& sm = reinterpret_cast<CostSmem<S>*>(cost_smem_raw)[threadIdx.x >> 5];
   const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
   const int lane = threadIdx.x & 31;
   const int xb = f.a.xb, yb = f.a.yb;
-  const int64_t cand = static_cast<int64_t>(blockIdx.x) * cost_warps<S>() + (threadIdx.x >> 5);
+  const int64_t cand = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
   int bx, by;
   if (!candidate_position<S>(cand, xb, yb, &bx, &by)) return;
   const int bi = by * xb + bx;
@@ -736,8 +745,6 @@ __global__ void __launch_bounds__(kCost32Threads) k_cost32(const __grid_constant
   if (threadIdx.x == 0) s.c32[bi] = rd_finish<kSt32x32>(f, s, bx, by, s_nz, s_ms, s_sum, s_sum + 3, kMetaR);
 }
 
-template <int S>
-constexpr size_t cost_smem_bytes() { return cost_warps<S>() * sizeof(CostSmem<S>); }
 
 // ---------------------------------------------------------------------------
 // Selection (squares scope) and re-tiling
@@ -884,8 +891,7 @@ struct RetileSmem {
   float leaf[64], wide[64], tall[64], square[64];
   uint8_t live[64];
 };
-constexpr int kRetileWarps = 4;
-constexpr size_t kRetileSmemBytes = kRetileWarps * sizeof(RetileSmem);
+constexpr int kRetileWarps = 4;  // tiles per CTA by default (tuned per device)
 constexpr unsigned long long kNoKey = ~0ull;
 
 __device__ __forceinline__ uint32_t ordered_bits(float v) {
@@ -1088,14 +1094,14 @@ __device__ __forceinline__ bool piece_in(const Piece* set, int n, Piece p) {
   return false;
 }
 
-__global__ void __launch_bounds__(32 * kRetileWarps) k_retile(const __grid_constant__ Frame f) {
+__global__ void __launch_bounds__(32 * kMaxTuneWarps) k_retile(const __grid_constant__ Frame f) {
   extern __shared__ __align__(16) unsigned char retile_smem_raw[];
   RetileSmem& sm = reinterpret_cast<RetileSmem*>(retile_smem_raw)[threadIdx.x >> 5];
   const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
   const int lane = threadIdx.x & 31;
   const int xb = f.a.xb, yb = f.a.yb;
   const int tx = (xb + 7) / 8, ty = (yb + 7) / 8;
-  const int tile = blockIdx.x * kRetileWarps + (threadIdx.x >> 5);
+  const int tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (tile >= tx * ty) return;
   const int bx = 8 * (tile % tx), by = 8 * (tile / tx);
   const int w = imin(8, xb - bx), h = imin(8, yb - by);
@@ -1737,11 +1743,6 @@ struct LayoutSmem {
   int32_t ylev[SIZE];
   float co[3][SIZE];
 };
-// Warps (transforms) per CTA of k_layout<S> (the 32x32 transforms have k_layout32).
-template <int S>
-__host__ __device__ constexpr int layout_warps() { return 4; }
-template <int S>
-constexpr size_t layout_smem_bytes() { return layout_warps<S>() * sizeof(LayoutSmem<S>); }
 
 __device__ __forceinline__ int dct_kind_of(int st) {
   switch (st) {
@@ -1998,11 +1999,11 @@ __global__ void __launch_bounds__(kLayout32Threads) k_layout32(const __grid_cons
 // starts at such a position (squares at even, 32x32 at 4-aligned blocks,
 // pairs at even coordinates along their long side).
 template <int S>
-__global__ void __launch_bounds__(128) k_layout(const __grid_constant__ Frame f) {
+__global__ void __launch_bounds__(32 * kMaxTuneWarps) k_layout(const __grid_constant__ Frame f) {
   extern __shared__ __align__(16) unsigned char layout_smem_raw[];
   LayoutSmem<S>& sm = reinterpret_cast<LayoutSmem<S>*>(layout_smem_raw)[threadIdx.x >> 5];
   const SearchFrame& s = *static_cast<const SearchFrame*>(f.search);
-  const int64_t cand = static_cast<int64_t>(blockIdx.x) * layout_warps<S>() + (threadIdx.x >> 5);
+  const int64_t cand = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
   int bx, by;
   if (!candidate_position<S>(cand, f.a.xb, f.a.yb, &bx, &by)) return;
   if (s.map[static_cast<int64_t>(by) * f.a.xb + bx] != static_cast<uint8_t>((S << 1) | 1)) return;
@@ -2183,19 +2184,19 @@ inline cudaError_t set_search_attributes() {
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
   };
-  set(reinterpret_cast<const void*>(k_cost<kStDct>), cost_smem_bytes<kStDct>());
-  set(reinterpret_cast<const void*>(k_cost<kSt16x8>), cost_smem_bytes<kSt16x8>());
-  set(reinterpret_cast<const void*>(k_cost<kSt8x16>), cost_smem_bytes<kSt8x16>());
-  set(reinterpret_cast<const void*>(k_cost<kSt16x16>), cost_smem_bytes<kSt16x16>());
+  set(reinterpret_cast<const void*>(k_cost<kStDct>), kMaxTuneWarps * sizeof(CostSmem<kStDct>));
+  set(reinterpret_cast<const void*>(k_cost<kSt16x8>), kMaxTuneWarps * sizeof(CostSmem<kSt16x8>));
+  set(reinterpret_cast<const void*>(k_cost<kSt8x16>), kMaxTuneWarps * sizeof(CostSmem<kSt8x16>));
+  set(reinterpret_cast<const void*>(k_cost<kSt16x16>), kMaxTuneWarps * sizeof(CostSmem<kSt16x16>));
   set(reinterpret_cast<const void*>(k_cost32), sizeof(Cost32Smem));
   set(reinterpret_cast<const void*>(k_mh_incumbent), 4 * sizeof(CostSmem<kSt32x32>));
-  set(reinterpret_cast<const void*>(k_layout<kStDct>), layout_smem_bytes<kStDct>());
-  set(reinterpret_cast<const void*>(k_layout<kSt16x8>), layout_smem_bytes<kSt16x8>());
-  set(reinterpret_cast<const void*>(k_layout<kSt8x16>), layout_smem_bytes<kSt8x16>());
-  set(reinterpret_cast<const void*>(k_layout<kSt16x16>), layout_smem_bytes<kSt16x16>());
+  set(reinterpret_cast<const void*>(k_layout<kStDct>), kMaxTuneWarps * sizeof(LayoutSmem<kStDct>));
+  set(reinterpret_cast<const void*>(k_layout<kSt16x8>), kMaxTuneWarps * sizeof(LayoutSmem<kSt16x8>));
+  set(reinterpret_cast<const void*>(k_layout<kSt8x16>), kMaxTuneWarps * sizeof(LayoutSmem<kSt8x16>));
+  set(reinterpret_cast<const void*>(k_layout<kSt16x16>), kMaxTuneWarps * sizeof(LayoutSmem<kSt16x16>));
   set(reinterpret_cast<const void*>(k_layout32), sizeof(Layout32Smem));
-  set(reinterpret_cast<const void*>(k_retile), kRetileSmemBytes);
-  set(reinterpret_cast<const void*>(k_site), kSiteSmemBytes);
+  set(reinterpret_cast<const void*>(k_retile), kMaxTuneWarps * sizeof(RetileSmem));
+  set(reinterpret_cast<const void*>(k_site), kMaxTuneWarps * sizeof(SiteSmem));
   return e;
 }
 

@@ -1911,6 +1911,110 @@ int orc_small_transform(int kind, const float* in, float* out) {
   return 0;
 }
 
+/* ------------------------------------------------------------------ */
+/* Gaborish                                                             */
+/* ------------------------------------------------------------------ */
+
+/* K_GABORISH (src/gaborish.rs:32-38) */
+static const float GAB_K[5] = {-0.09495815671340026f, -0.041031725066768575f, 0.013710004822696948f,
+                               0.006510206083837737f, -0.0014789063378272242f};
+
+/* reflect (src/gaborish.rs:78-90): mirror about the edges, repeated */
+static size_t gab_reflect(long i, long len) {
+  long j = i;
+  while (j < 0 || j >= len) {
+    if (j < 0) j = -j - 1;
+    else j = 2 * len - j - 1;
+  }
+  return (size_t)j;
+}
+
+/* The normalised weights of gaborish_inverse (src/gaborish.rs:44-72):
+ * c, r, d, R, L, D (centre, distance 1, sqrt 2, 2, sqrt 5, 2 sqrt 2). */
+void orc_gaborish_inverse_weights(float mul, float* w6) {
+  const float w_r = mul * GAB_K[0], w_d = mul * GAB_K[1], w_r2 = mul * GAB_K[2];
+  const float w_l = mul * GAB_K[3], w_d2 = mul * GAB_K[4];
+  float sum = 1.0f + mul * 4.0f * (GAB_K[0] + GAB_K[1] + GAB_K[2] + GAB_K[4] + 2.0f * GAB_K[3]);
+  if (sum < 1e-5f) sum = 1e-5f;
+  const float norm = 1.0f / sum;
+  w6[0] = norm;
+  w6[1] = norm * w_r;
+  w6[2] = norm * w_d;
+  w6[3] = norm * w_r2;
+  w6[4] = norm * w_l;
+  w6[5] = norm * w_d2;
+}
+
+/* gaborish_inverse (src/gaborish.rs:44-258): the symmetric 5x5 of every
+ * channel with mirror-reflected neighbours, each output from source pixels
+ * only (the reference delays its writes by two rows).  `in` and `out` are 3
+ * planes of w*h floats. */
+void orc_gaborish_inverse(const float* in, float* out, size_t w, size_t h, float mul) {
+  float k[6];
+  orc_gaborish_inverse_weights(mul, k);
+  const float n_c = k[0], n_r = k[1], n_d = k[2], n_r2 = k[3], n_l = k[4], n_d2 = k[5];
+  for (int c = 0; c < 3; c++) {
+    const float* p = in + (size_t)c * w * h;
+    float* o = out + (size_t)c * w * h;
+    for (size_t y = 0; y < h; y++) {
+      const float* r0 = p + y * w;
+      const float* rm1 = p + gab_reflect((long)y - 1, (long)h) * w;
+      const float* rp1 = p + gab_reflect((long)y + 1, (long)h) * w;
+      const float* rm2 = p + gab_reflect((long)y - 2, (long)h) * w;
+      const float* rp2 = p + gab_reflect((long)y + 2, (long)h) * w;
+      for (size_t x = 0; x < w; x++) {
+        const size_t xm1 = gab_reflect((long)x - 1, (long)w), xp1 = gab_reflect((long)x + 1, (long)w);
+        const size_t xm2 = gab_reflect((long)x - 2, (long)w), xp2 = gab_reflect((long)x + 2, (long)w);
+        const float s_r = rm1[x] + rp1[x] + r0[xm1] + r0[xp1];
+        const float s_d = rm1[xm1] + rm1[xp1] + rp1[xm1] + rp1[xp1];
+        const float s_r2 = rm2[x] + rp2[x] + r0[xm2] + r0[xp2];
+        const float s_d2 = rm2[xm2] + rm2[xp2] + rp2[xm2] + rp2[xp2];
+        const float s_l = rm2[xm1] + rm2[xp1] + rm1[xm2] + rm1[xp2] + rp1[xm2] + rp1[xp2] +
+                          rp2[xm1] + rp2[xp1];
+        float acc = n_c * r0[x];
+        acc = fmla(n_r, s_r, acc);
+        acc = fmla(n_d, s_d, acc);
+        acc = fmla(n_r2, s_r2, acc);
+        acc = fmla(n_d2, s_d2, acc);
+        acc = fmla(n_l, s_l, acc);
+        o[y * w + x] = acc;
+      }
+    }
+  }
+}
+
+/* The decoder's Gaborish (src/epf_filter.rs:163-188, gaborish_pixel
+ * src/epf_filter/kernels.rs:134-145): the 3x3 with clamped neighbours and
+ * weights norm, W1 norm, W2 norm; products fused into the sums (the NEON
+ * and AVX2+FMA backends). */
+void orc_gaborish_weights(float* w3) {
+  const float w1 = 1.1f * 0.10469957f, w2 = 1.1f * 0.05568054f;
+  const float norm = 1.0f / (1.0f + 4.0f * (w1 + w2));
+  w3[0] = norm;
+  w3[1] = w1 * norm;
+  w3[2] = w2 * norm;
+}
+
+void orc_gaborish(const float* in, float* out, size_t w, size_t h) {
+  float k[3];
+  orc_gaborish_weights(k);
+  for (int c = 0; c < 3; c++) {
+    const float* p = in + (size_t)c * w * h;
+    float* o = out + (size_t)c * w * h;
+    for (size_t y = 0; y < h; y++) {
+      const float* t = p + (y > 0 ? y - 1 : 0) * w;
+      const float* m = p + y * w;
+      const float* b = p + (y + 1 < h ? y + 1 : h - 1) * w;
+      for (size_t x = 0; x < w; x++) {
+        const size_t l = x > 0 ? x - 1 : 0, r = x + 1 < w ? x + 1 : w - 1;
+        const float side = (m[l] + m[r]) + (t[x] + b[x]);
+        const float corner = (t[l] + t[r]) + (b[l] + b[r]);
+        o[y * w + x] = fmla(corner, k[2], fmla(side, k[1], m[x] * k[0]));
+      }
+    }
+  }
+}
+
 /* dct1d_16 / dct1d_32 of one vector in place (n = 8, 16 or 32). */
 void orc_dct1d(float* b, int n) { dct1d_n(b, n); }
 

@@ -404,6 +404,37 @@ def dct1d(vec: np.ndarray) -> np.ndarray:
     return v
 
 
+def gaborish_inverse(xyb: np.ndarray, mul: float = 0.9908511) -> np.ndarray:
+    """gaborish_inverse (src/gaborish.rs:44) of (3, h, w) planes: a new array."""
+    x = np.ascontiguousarray(xyb, np.float32)
+    out = np.zeros_like(x)
+    lib().orc_gaborish_inverse(x.ctypes.data_as(ctypes.c_void_p), out.ctypes.data_as(ctypes.c_void_p),
+                               ctypes.c_size_t(x.shape[2]), ctypes.c_size_t(x.shape[1]),
+                               ctypes.c_float(mul))
+    return out
+
+
+def gaborish_inverse_weights(mul: float = 0.9908511) -> np.ndarray:
+    w = np.zeros(6, np.float32)
+    lib().orc_gaborish_inverse_weights(ctypes.c_float(mul), w.ctypes.data_as(ctypes.c_void_p))
+    return w
+
+
+def gaborish(xyb: np.ndarray) -> np.ndarray:
+    """The decoder's Gaborish (src/epf_filter.rs:165) of (3, h, w) planes."""
+    x = np.ascontiguousarray(xyb, np.float32)
+    out = np.zeros_like(x)
+    lib().orc_gaborish(x.ctypes.data_as(ctypes.c_void_p), out.ctypes.data_as(ctypes.c_void_p),
+                       ctypes.c_size_t(x.shape[2]), ctypes.c_size_t(x.shape[1]))
+    return out
+
+
+def gaborish_weights() -> np.ndarray:
+    w = np.zeros(3, np.float32)
+    lib().orc_gaborish_weights(w.ctypes.data_as(ctypes.c_void_p))
+    return w
+
+
 def idct(name: str, coeffs: np.ndarray) -> np.ndarray:
     """The inverse of `dct(name, ...)` (IdctMethods, src/dct.rs:358-416;
     inv_dct8x16 :1634, inv_dct16x8 :1658, inv_dct16x32 :1683, inv_dct32x16

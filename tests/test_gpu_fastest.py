@@ -110,3 +110,38 @@ def test_black_regions_take_the_serial_variance(ctx):
     img[32:160, 40:200] = 0
     img[100:120, 0:256] = (3, 2, 1)
     compare(ctx, img, 2.6)
+
+
+def test_launch_geometry_does_not_change_the_frame(ctx):
+    # warps per CTA of the tunable kernels: every choice codes the same frame
+    img = synthetic.config1_image()
+    d = J.distance_from_quality(60)
+    want = O.frontend(img, d, speed="fastest")
+    base = ctx.launch_geometry()
+    try:
+        for w in (1, 2, 8):
+            ctx.set_launch_geometry({k: w for k in base})
+            got = ctx.frontend(img, fastest(d), xyb=False)
+            assert np.array_equal(got.ac_strategy, want.ac_strategy), w
+            assert_same(got, want, check_xyb=False)
+        with pytest.raises(J.EncodeError):
+            ctx.set_launch_geometry({"k_retile": 3})
+    finally:
+        ctx.set_launch_geometry(base)
+
+
+def test_autotune_picks_a_geometry_that_codes_the_same_frame(ctx):
+    torch = pytest.importorskip("torch")
+    img = synthetic.config1_image()
+    d_img = torch.from_numpy(img).cuda().contiguous()
+    base = ctx.launch_geometry()
+    try:
+        geo, times = ctx.autotune(d_img.data_ptr(), img.shape[1], img.shape[0], 3, 8,
+                                  fastest(J.distance_from_quality(75)), rounds=1)
+        assert set(geo.values()) <= {1, 2, 4, 8}
+        for k, t in times.items():
+            assert all(np.isfinite(v) and v > 0 for v in t.values()), k
+            assert t[geo[k]] == min(t.values()), k
+        compare(ctx, img, J.distance_from_quality(75))
+    finally:
+        ctx.set_launch_geometry(base)
