@@ -61,6 +61,9 @@ def parse_args():
                    help="download (context, value) token pairs instead of packed AcToken words")
     p.add_argument("--c5", action="store_true",
                    help="also time one 8192x8192 RGB16 linear frame at q85 per step")
+    p.add_argument("--no-refine", action="store_true",
+                   help="skip the quant-field refinement timing")
+    p.add_argument("--refine-steps", type=int, default=8)
     p.add_argument("--frames", type=int, default=0,
                    help="only run this many frames of the headline workload on one context, "
                         "untimed, and exit (the target of a profiler capture)")
@@ -441,6 +444,10 @@ def run_gpu(args):
     if not args.no_batch:
         batch = run_batch(ctx, streams[0], flush, args, world, dev)
 
+    refine = None
+    if not args.no_refine:
+        refine = run_refine(ctx, streams[0], d_img, args, dev)
+
     # end to end through the public C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
@@ -464,6 +471,7 @@ def run_gpu(args):
             "autotune": autotune,
             "ultrafast": ultrafast,
             "c5": c5,
+            "refine": refine,
         }
         print(json.dumps(line), flush=True)
     for c in ctxs:
@@ -511,6 +519,63 @@ def run_ultrafast(ctxs, streams, flush, d_img, args, dev) -> dict:
     return {"workload": "3840x2160 RGB8 at q75/q90/q95, UltraFast gates (all-DCT8 layout), "
                         "three frames per step", "value": args.steps * mp / (total / 1000.0),
             "unit": "MP/s", "ms_per_step": total / args.steps}
+
+
+def run_refine(ctx, stream, d_img, args, dev) -> dict:
+    """Quant-field refinement of the headline frame's UltraFast pass at q90:
+    `--refine-steps` Adam steps (loss, gradient by the adjoint kernels, update)
+    after one untimed step; CUDA events on the context's stream around the
+    steps, each of which reads its loss back to the host."""
+    import torch
+
+    import jixel_gb300 as J
+
+    cfg = J.EncodeConfig(speed=J.Speed.ULTRA_FAST).with_quality(90)
+    lr = 0.05
+    ctx.run_device(d_img.data_ptr(), WIDTH, HEIGHT, 3, 8, cfg)
+    xb, yb = ctx.refine_begin()
+    # lambda at the pass's own rate-distortion slope: the steps move bits
+    # between blocks rather than changing the frame's overall rate
+    lam = ctx.refine_rate_slope(WIDTH * HEIGHT)
+    first = ctx.refine_step(lam, lr)
+    ctx.refine_theta(np.zeros((yb, xb), np.float32))  # restart from theta = 0
+    torch.cuda.synchronize(dev)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    s.record(stream)
+    hist = [ctx.refine_step(lam, lr) for _ in range(args.refine_steps)]
+    e.record(stream)
+    e.synchronize()
+    wall = time.perf_counter() - t0
+    final, _ = ctx.refine_eval(lam)
+    ms = s.elapsed_time(e) / args.refine_steps
+    # per-kernel times of one more step; algorithmic bytes per launch: the
+    # fused SSIM kernel reads the source and decoded planes and writes the
+    # gradient (12 B per pixel and channel at its scale); the forward reads the
+    # source coefficients and writes the decoded XYB and linear planes (2304 B
+    # per block), the backward reads coefficients, decoded XYB and the two
+    # finest gradients (2496 B per block)
+    ctx.enable_kernel_timing(True)
+    ctx.reset_kernel_times()
+    ctx.refine_step(lam, lr)
+    kt = {k: v for k, v in ctx.kernel_times().items() if k.startswith("k_refine")}
+    ctx.enable_kernel_timing(False)
+    nb = xb * yb
+    px = [WIDTH * HEIGHT, (WIDTH // 2) * (HEIGHT // 2), (WIDTH // 4) * (HEIGHT // 4)]
+    algo = {"k_refine_forward": 2304.0 * nb, "k_refine_backward": 2496.0 * nb,
+            "k_refine_ssim": 36.0 * sum(px)}
+    kernels = {}
+    for k, v in sorted(kt.items()):
+        kernels[k] = {"ms": v[0], "launches": v[1]}
+        if k in algo:
+            kernels[k]["algorithmic_gbs"] = algo[k] / (v[0] / 1000.0) / 1e9
+    return {"workload": f"{WIDTH}x{HEIGHT} RGB8 q90 UltraFast pass, {xb * yb} blocks, Adam lr {lr}, "
+                        f"lambda {lam:.4g} (the pass's rate-distortion slope), SSIM at 3 scales + rate model",
+            "steps": args.refine_steps, "ms_per_step": ms, "wall_ms_per_step": 1000.0 * wall / args.refine_steps,
+            "megapixels_per_s": WIDTH * HEIGHT / 1e6 / (ms / 1000.0),
+            "loss_first": hist[0][0], "loss_final": final[0], "distortion_first": hist[0][1],
+            "distortion_final": final[1], "bits_first": hist[0][2], "bits_final": final[2],
+            "untimed_first_step_loss": first[0], "kernels": kernels}
 
 
 def run_c5(ctxs, streams, flush, args, dev) -> dict:

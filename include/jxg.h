@@ -403,6 +403,55 @@ int32_t jxg_selftest_token_lookback(void* ctx, uint32_t polls);
 int32_t jxg_selftest_math(void* ctx, int32_t which, uint32_t lo_bits, uint32_t hi_bits,
                           uint64_t* mismatches, uint32_t* first_bad);
 
+/* Quant-field refinement -------------------------------------------------
+ * No counterpart in the reference, which has no gradients anywhere: the
+ * per-block quant field of an all-DCT8 frame is refined by gradient steps on
+ * a differentiable model of its coding.  Parameters theta are one log quant
+ * scale per 8x8 block: block b quantises at scale * qf_b * exp(theta_b), qf
+ * the frame's adaptive field.  The model (FP32) quantises and dequantises the
+ * AC coefficients exactly as the front end does (with CfL and the decoder's
+ * bias), inverts the 8x8 DCT, converts XYB to linear RGB and scores 1 - SSIM
+ * against the source at three scales, plus a rate model (1.6 + log2(1 +
+ * |level|) bits per non-zero AC level, 2.6 (|v| / max(threshold, 0.5))^4 per
+ * level v that rounds to zero); rounding is straight-through in the backward
+ * pass.  EPF, gaborish and DC smoothing are not modelled.
+ *
+ * jxg_refine_begin takes the frame of the context's last pass (one frame,
+ * Speed::UltraFast), copies what the model needs (a later pass does not
+ * disturb it), sets the context's own theta to zero and returns the block
+ * grid (theta's size) in xsize/ysize_blocks; the others need it. */
+int32_t jxg_refine_begin(void* ctx, uint64_t* xsize_blocks, uint64_t* ysize_blocks);
+/* Loss at `theta` (device memory, xb*yb floats; NULL: the context's own):
+ * loss3 = {distortion + rate_lambda * bits / pixels, distortion, bits} on the
+ * host; `grad` (device, xb*yb floats, or NULL) receives d loss / d theta from
+ * the hand-written adjoint kernels; `levels` (host, xb*yb*192, or NULL) the AC
+ * levels per block, channel X, Y, B and raw coefficient index (row * 8 + col,
+ * the DC slot 0). */
+int32_t jxg_refine_eval(void* ctx, const float* theta, float rate_lambda, float* grad, double* loss3,
+                        int32_t* levels);
+/* One Adam step (beta 0.9 / 0.999) on the context's own theta: loss3 at the
+ * theta before the step, as jxg_refine_eval.  theta stays where
+ * qf * exp(theta) is within 1..255. */
+int32_t jxg_refine_step(void* ctx, float rate_lambda, float learning_rate, double* loss3);
+/* Copy the context's own theta out to `theta` (to_context 0) or in from it
+ * (1; restarts Adam); host or device memory, xb*yb floats. */
+int32_t jxg_refine_theta(void* ctx, float* theta, int32_t to_context);
+/* The integer field of `theta` (NULL: the context's own): round(qf *
+ * exp(theta)) clamped to 1..255, xb*yb bytes into host or device memory. */
+int32_t jxg_refine_field(void* ctx, const float* theta, uint8_t* quant_field);
+/* The model's constants for an outside check: constants = {scale, qm_mul[3],
+ * matrix[3][64], inv_matrix[3][64], thresholds[3][4]} (400 floats); the
+ * source coefficients (xb*yb*192, raw order) and the 64 x 64 inverse
+ * transform [pixel][coefficient] (either may be NULL), all on the host. */
+int32_t jxg_refine_model(void* ctx, float* constants, float* coefficients, float* inverse);
+/* One UltraFast pass with the caller's quant field (xb*yb values 1..255, host
+ * or device memory; e.g. a refined field) in place of the adaptive one; the
+ * AC thresholds' median stage runs over it.  Host pixels: runs and waits, as
+ * jxg_frontend_run; device pixels: enqueues, as jxg_frontend_run_device. */
+int32_t jxg_frontend_run_with_field(void* ctx, const void* pixels, uint64_t width, uint64_t height,
+                                    int32_t channels, int32_t bits, const jxg_config* config,
+                                    const uint8_t* quant_field, int32_t pixels_on_device);
+
 /* Launch geometry and its autotuner ---------------------------------------
  * Warps per CTA of the Speed::Fastest kernels whose warps work
  * independently (each warp a candidate transform, a placed transform, a

@@ -44,6 +44,13 @@ EXPORTS = [
     "jxg_selftest_bounded_wait",
     "jxg_selftest_token_lookback",
     "jxg_selftest_math",
+    "jxg_refine_begin",
+    "jxg_refine_eval",
+    "jxg_refine_step",
+    "jxg_refine_theta",
+    "jxg_refine_field",
+    "jxg_refine_model",
+    "jxg_frontend_run_with_field",
     "jxg_get_launch_geometry",
     "jxg_set_launch_geometry",
     "jxg_autotune",
@@ -166,6 +173,13 @@ def load() -> ctypes.CDLL:
         "jxg_selftest_token_lookback": (i32, [vp, ctypes.c_uint32]),
         "jxg_selftest_math": (i32, [vp, i32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(u64),
                                     ctypes.POINTER(ctypes.c_uint32)]),
+        "jxg_refine_begin": (i32, [vp, vp, vp]),
+        "jxg_refine_eval": (i32, [vp, vp, ctypes.c_float, vp, vp, vp]),
+        "jxg_refine_step": (i32, [vp, ctypes.c_float, ctypes.c_float, vp]),
+        "jxg_refine_theta": (i32, [vp, vp, i32]),
+        "jxg_refine_field": (i32, [vp, vp, vp]),
+        "jxg_refine_model": (i32, [vp, vp, vp, vp]),
+        "jxg_frontend_run_with_field": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config), vp, i32]),
         "jxg_get_launch_geometry": (i32, [vp, vp]),
         "jxg_set_launch_geometry": (i32, [vp, vp]),
         "jxg_autotune": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config), i32, vp]),

@@ -449,6 +449,110 @@ class FrontendContext:
             goffs.shape[0] - 1, words.ctypes.data, words.shape[0], woffs.ctypes.data))
         return words[: int(woffs[-1])], woffs
 
+    # quant-field refinement ----------------------------------------------------
+    def refine_begin(self) -> tuple[int, int]:
+        """jxg_refine_begin: refine the frame of the last (UltraFast) pass;
+        returns its block grid (xsize_blocks, ysize_blocks)."""
+        xb, yb = ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self._lib.jxg_refine_begin(self._ctx, ctypes.byref(xb), ctypes.byref(yb)))
+        self._refine_blocks = (xb.value, yb.value)
+        return self._refine_blocks
+
+    def refine_eval(self, rate_lambda: float, theta_ptr: int | None = None, grad_ptr: int | None = None,
+                    levels: bool = False):
+        """jxg_refine_eval at device `theta_ptr` (None: the context's own
+        theta): ((loss, distortion, bits), levels or None); d loss / d theta
+        into device `grad_ptr` when given.  Levels are (blocks, 3, 64) in raw
+        order."""
+        loss = np.zeros(3, np.float64)
+        lv = None
+        if levels:
+            xb, yb = self._refine_blocks
+            lv = np.zeros((xb * yb, 3, 64), np.int32)
+        self._check(self._lib.jxg_refine_eval(self._ctx, theta_ptr, rate_lambda, grad_ptr,
+                                              loss.ctypes.data, None if lv is None else lv.ctypes.data))
+        return (float(loss[0]), float(loss[1]), float(loss[2])), lv
+
+    def refine_step(self, rate_lambda: float, learning_rate: float) -> tuple[float, float, float]:
+        """One Adam step on the context's theta; the loss before it."""
+        loss = np.zeros(3, np.float64)
+        self._check(self._lib.jxg_refine_step(self._ctx, rate_lambda, learning_rate, loss.ctypes.data))
+        return float(loss[0]), float(loss[1]), float(loss[2])
+
+    def refine_theta(self, theta: np.ndarray | None = None) -> np.ndarray:
+        """The context's theta as (yb, xb) floats; with `theta`, set it first."""
+        xb, yb = self._refine_blocks
+        if theta is not None:
+            t = np.ascontiguousarray(theta, np.float32).reshape(-1)
+            if t.size != xb * yb:
+                raise EncodeError(100, f"theta needs {xb * yb} values")
+            self._check(self._lib.jxg_refine_theta(self._ctx, t.ctypes.data, 1))
+        out = np.zeros((yb, xb), np.float32)
+        self._check(self._lib.jxg_refine_theta(self._ctx, out.ctypes.data, 0))
+        return out
+
+    def refine_field(self, theta_ptr: int | None = None) -> np.ndarray:
+        """round(qf * exp(theta)) in 1..255 as a (yb, xb) uint8 array."""
+        xb, yb = self._refine_blocks
+        out = np.zeros((yb, xb), np.uint8)
+        self._check(self._lib.jxg_refine_field(self._ctx, theta_ptr, out.ctypes.data))
+        return out
+
+    def refine_rate_slope(self, pixels: int, delta: float = 0.1) -> float:
+        """-dD / d(bits per pixel) of a uniform change of theta by +-delta
+        around the context's theta: the lambda at which the frame's overall
+        rate is, to first order, where the pass put it (pixels = width *
+        height of the frame)."""
+        t = self.refine_theta()
+        self.refine_theta(t + delta)
+        (_, d_hi, b_hi), _ = self.refine_eval(0.0)
+        self.refine_theta(t - delta)
+        (_, d_lo, b_lo), _ = self.refine_eval(0.0)
+        self.refine_theta(t)
+        if b_hi == b_lo:
+            return 0.0
+        return max(0.0, -(d_hi - d_lo) / ((b_hi - b_lo) / pixels))
+
+    def refine(self, steps: int = 8, rate_lambda: float = 0.002, learning_rate: float = 0.05):
+        """Refine the last pass's quant field: `steps` Adam steps from theta = 0.
+        Returns (field (yb, xb) uint8, losses per step before it, final loss)."""
+        self.refine_begin()
+        history = [self.refine_step(rate_lambda, learning_rate) for _ in range(steps)]
+        final, _ = self.refine_eval(rate_lambda)
+        return self.refine_field(), history, final
+
+    def refine_model(self) -> dict:
+        """The model's constants, source coefficients and inverse transform."""
+        xb, yb = self._refine_blocks
+        nb = xb * yb
+        k = np.zeros(400, np.float32)
+        coef = np.zeros((nb, 3, 64), np.float32)
+        inv = np.zeros((64, 64), np.float32)
+        self._check(self._lib.jxg_refine_model(self._ctx, k.ctypes.data, coef.ctypes.data,
+                                               inv.ctypes.data))
+        return {"scale": float(k[0]), "qm_mul": k[1:4].copy(), "matrix": k[4:196].reshape(3, 64).copy(),
+                "inv_matrix": k[196:388].reshape(3, 64).copy(), "thresholds": k[388:400].reshape(3, 4).copy(),
+                "coef": coef, "inverse": inv}
+
+    def run_with_field(self, pixels: np.ndarray, config: EncodeConfig, quant_field: np.ndarray):
+        """jxg_frontend_run_with_field, host pixels and a host (yb, xb) field."""
+        pixels = _as_hwc(pixels)
+        ch, bits = _pixels_kind(pixels, config)
+        h, w = pixels.shape[:2]
+        fi = frame_info(w, h)
+        qf = np.ascontiguousarray(quant_field, np.uint8)
+        if qf.shape != (fi.ysize_blocks, fi.xsize_blocks):
+            raise EncodeError(100, f"the field must be ({fi.ysize_blocks}, {fi.xsize_blocks})")
+        cfg = config._c()
+        self._check(self._lib.jxg_frontend_run_with_field(self._ctx, pixels.ctypes.data, w, h, ch, bits,
+                                                          ctypes.byref(cfg), qf.ctypes.data, 0))
+
+    def frontend_with_field(self, pixels: np.ndarray, config: EncodeConfig, quant_field: np.ndarray,
+                            **kw) -> FrontendResult:
+        pixels = _as_hwc(pixels)
+        self.run_with_field(pixels, config, quant_field)
+        return self.fetch(pixels.shape[1], pixels.shape[0], alpha=pixels.shape[2] in (2, 4), **kw)
+
     # launch geometry and its autotuner --------------------------------------
     TUNE_KERNELS = ("k_cost_dct8", "k_cost_16x8", "k_cost_8x16", "k_cost_16x16", "k_layout_dct8",
                     "k_layout_16x8", "k_layout_8x16", "k_layout_16x16", "k_retile", "k_site")

@@ -17,6 +17,7 @@
 #include "jxg_kernels.cuh"
 #include "jxg_search.cuh"
 #include "jxg_filters.cuh"
+#include "jxg_refine.cuh"
 
 namespace jxg {
 namespace {
@@ -139,6 +140,23 @@ struct Context {
   size_t frames_bytes = 0, pixel_bytes = 0;
   bool have_frame = false;
   uint64_t epoch = 0;  // bumped by every plan: batches recorded earlier re-plan
+  // a caller's quant field for the next single-frame UltraFast pass (device
+  // memory), replacing the adaptive field after its stage
+  const uint8_t* qf_override = nullptr;
+  // quant-field refinement of the last UltraFast frame (jxg_refine_*)
+  bool refine_ready = false;
+  jxg::RefineArgs refine{};
+  int64_t refine_n[3] = {0, 0, 0};  // pixels per scale
+  int refine_w[3] = {0, 0, 0}, refine_h[3] = {0, 0, 0};
+  DevBuf refine_buf;
+  float* refine_lin[2][3] = {};  // source / decoded linear RGB per scale
+  float* refine_glin[3] = {};     // the loss's gradient by the decoded planes per scale
+  double* refine_sums = nullptr;  // 4 x kRefineSlots partial sums
+  DevBuf refine_levels;           // levels, when a caller asks for them
+  // the context's own parameters, their gradient and Adam moments
+  float *refine_theta = nullptr, *refine_grad = nullptr, *refine_adam = nullptr;
+  int32_t refine_steps = 0;
+  DevBuf field_buf;  // a caller's field, staged for jxg_frontend_run_with_field
   // launch geometry of the tunable search and layout kernels (warps per CTA)
   uint8_t tune[jxg::kTuneKernels] = {4, 4, 4, 4, 4, 4, 4, 4, jxg::kRetileWarps, jxg::kSiteWarps};
   // timing
@@ -794,8 +812,14 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
       return st;
     if ((st = launch(c, "k_adaptive_quant", timed, [&] {
            k_adaptive_quant<<<static_cast<unsigned>(c->total_tiles), 256, 0, s>>>(f0, c->d_exp2);
-         })) ||
-        (st = launch(c, "k_tile_quantize", timed, [&] {
+         })))
+      return st;
+    if (c->qf_override) {  // the caller's field, and ac_qf_threshold over it
+      JXG_CUDA(c, cudaMemcpyAsync(f0.qf, c->qf_override, static_cast<size_t>(f0.a.xb) * f0.a.yb,
+                                  cudaMemcpyDeviceToDevice, s));
+      if ((st = launch(c, "k_qf_median", timed, [&] { k_qf_median<<<1, 256, 0, s>>>(f0); }))) return st;
+    }
+    if ((st = launch(c, "k_tile_quantize", timed, [&] {
            k_tile_quantize<<<static_cast<unsigned>(c->total_tiles), kTileThreads, kTileSmemBytes, s>>>(
                f0, c->d_pos);
          })))
@@ -1899,6 +1923,315 @@ int32_t jxg_selftest_math(void* ctx, int32_t which, uint32_t lo_bits, uint32_t h
   if ((st = jxg::wait(c))) return st;
   *mismatches = n;
   return JXG_OK;
+}
+
+int32_t jxg_frontend_run_with_field(void* ctx, const void* pixels, uint64_t width, uint64_t height,
+                                    int32_t channels, int32_t bits, const jxg_config* config,
+                                    const uint8_t* quant_field, int32_t pixels_on_device) {
+  using namespace jxg;
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !quant_field || !config) return JXG_ERR_INVALID_ARGUMENT;
+  if (config->speed != JXG_SPEED_ULTRAFAST)
+    return fail(c, JXG_ERR_UNSUPPORTED, "a caller's quant field needs the UltraFast gates");
+  if (c->async_pending) {
+    const int st = jxg_frontend_wait(ctx);
+    if (st) return st;
+  }
+  cudaSetDevice(c->device);
+  int st;
+  if ((st = validate(c, pixels, width, height, channels, bits, config))) return st;
+  const size_t nb = static_cast<size_t>((width + 7) / 8) * ((height + 7) / 8);
+  if ((st = ensure(c, c->field_buf, nb))) return st;
+  cudaPointerAttributes at{};
+  const bool device_field =
+      cudaPointerGetAttributes(&at, quant_field) == cudaSuccess && at.type == cudaMemoryTypeDevice;
+  cudaGetLastError();  // a host pointer may leave an error behind on some drivers
+  JXG_CUDA(c, cudaMemcpyAsync(c->field_buf.ptr, quant_field, nb,
+                              device_field ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream));
+  c->qf_override = static_cast<const uint8_t*>(c->field_buf.ptr);
+  st = single_pass(c, pixels, width, height, channels, bits, config, pixels_on_device != 0);
+  c->qf_override = nullptr;
+  if (st || pixels_on_device) return st;
+  return wait(c);
+}
+
+namespace {
+int refine_grid(int64_t n) { return static_cast<int>((n + 255) / 256); }
+}  // namespace
+
+int32_t jxg_refine_begin(void* ctx, uint64_t* xsize_blocks, uint64_t* ysize_blocks) {
+  using namespace jxg;
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !xsize_blocks || !ysize_blocks) return JXG_ERR_INVALID_ARGUMENT;
+  if (c->async_pending) {
+    const int st = jxg_frontend_wait(ctx);
+    if (st) return st;
+  }
+  c->refine_ready = false;
+  if (!c->have_frame || c->layouts.size() != 1 || c->layouts[0].searched)
+    return fail(c, JXG_ERR_UNSUPPORTED, "refinement needs a one-frame UltraFast pass on the context first");
+  cudaSetDevice(c->device);
+  int st;
+  if ((st = wait(c))) return st;
+  const Frame& f0 = *reinterpret_cast<const Frame*>(static_cast<const char*>(c->plan_host.ptr) +
+                                                    c->plan_slot * c->plan_slot_cap);
+  const KernelArgs& a = f0.a;
+  RefineArgs& r = c->refine;
+  r = RefineArgs{};
+  r.w = a.width;
+  r.h = a.height;
+  r.xb = a.xb;
+  r.yb = a.yb;
+  r.pw = a.xb * 8;
+  r.plane = a.plane;
+  r.xyb = f0.xyb;  // read by this call only
+  r.tiles_x = a.tiles_x;
+  r.scale = a.scale;
+  std::memcpy(r.qm_mul, a.qm_mul, sizeof(r.qm_mul));
+  std::memcpy(r.matrix, a.matrix, sizeof(r.matrix));
+  std::memcpy(r.inv_matrix, a.inv_matrix, sizeof(r.inv_matrix));
+  std::memcpy(r.thresholds, a.thresholds, sizeof(r.thresholds));
+  const int64_t nb = static_cast<int64_t>(r.xb) * r.yb, pp = static_cast<int64_t>(r.pw) * r.yb * 8;
+  for (int k = 0; k < 3; ++k) {
+    c->refine_w[k] = r.w >> k;
+    c->refine_h[k] = r.h >> k;
+    c->refine_n[k] = static_cast<int64_t>(c->refine_w[k]) * c->refine_h[k];
+  }
+  const int64_t n = c->refine_n[0], n1 = c->refine_n[1], n2 = c->refine_n[2];
+  // one allocation: coef, chat, levels (nb x 192), recon and its gradient
+  // (3 pp), bits, M, the linear planes and gradients per scale, the moment,
+  // blur and gradient maps, four f64 sums
+  const int64_t tiles = static_cast<int64_t>(a.tiles_x) * a.tiles_y;
+  // one allocation: source coefficients (nb x 192), the decoded XYB planes
+  // (3 pp), M and M^T, the source and decoded linear planes and the gradient
+  // per scale, the f64 sums, theta, its gradient and Adam moments, copies of
+  // the field and the colour maps; each piece rounded up to 64 floats
+  const size_t floats = nb * 192 + 3 * pp + 2 * 4096 + 3 * 3 * (n + n1 + n2) + 2 * 4 * kRefineSlots + 4 * nb +
+                        (nb + 2 * tiles) / 4 + 64 * 24;
+  if ((st = ensure(c, c->refine_buf, floats * 4 + 256))) return st;
+  float* base = static_cast<float*>(c->refine_buf.ptr);
+  auto take = [&](int64_t count) {
+    float* p = base;
+    base += (count + 63) / 64 * 64;
+    return p;
+  };
+  r.coef = take(nb * 192);
+  r.recon = take(3 * pp);
+  r.m = take(4096);
+  r.mt = take(4096);
+  for (int k = 0; k < 3; ++k) {
+    c->refine_lin[0][k] = take(3 * c->refine_n[k]);
+    c->refine_lin[1][k] = take(3 * c->refine_n[k]);
+    c->refine_glin[k] = take(3 * c->refine_n[k]);
+  }
+  c->refine_sums = reinterpret_cast<double*>(take(2 * 4 * kRefineSlots));
+  c->refine_theta = take(nb);
+  c->refine_grad = take(nb);
+  c->refine_adam = take(2 * nb);
+  // the pass's field and colour maps, copied: a later pass on the context
+  // may overwrite or move its own buffers
+  uint8_t* qf = reinterpret_cast<uint8_t*>(take((nb + 3) / 4));
+  int8_t* ytox = reinterpret_cast<int8_t*>(take((tiles + 3) / 4));
+  int8_t* ytob = reinterpret_cast<int8_t*>(take((tiles + 3) / 4));
+  cudaStream_t s = c->stream;
+  JXG_CUDA(c, cudaMemcpyAsync(qf, f0.qf, nb, cudaMemcpyDeviceToDevice, s));
+  JXG_CUDA(c, cudaMemcpyAsync(ytox, f0.ytox, tiles, cudaMemcpyDeviceToDevice, s));
+  JXG_CUDA(c, cudaMemcpyAsync(ytob, f0.ytob, tiles, cudaMemcpyDeviceToDevice, s));
+  JXG_CUDA(c, cudaMemsetAsync(c->refine_theta, 0, nb * 4, s));
+  r.qf = qf;
+  r.ytox = ytox;
+  r.ytob = ytob;
+  c->refine_steps = 0;
+  // M: the library's 8x8 inverse of each unit coefficient vector
+  std::vector<float> unit(64 * 64, 0.0f), cols(64 * 64);
+  for (int j = 0; j < 64; ++j) unit[j * 64 + j] = 1.0f;
+  if ((st = ensure(c, c->op_in, unit.size() * 4)) || (st = ensure(c, c->op_out, unit.size() * 4))) return st;
+  JXG_CUDA(c, cudaMemcpyAsync(c->op_in.ptr, unit.data(), unit.size() * 4, cudaMemcpyHostToDevice, s));
+  k_idct_blocks<8, 8, kIdctSquare><<<(64 + dct_warps<8, 8>() - 1) / dct_warps<8, 8>(), 32 * dct_warps<8, 8>(), 0, s>>>(
+      static_cast<const float*>(c->op_in.ptr), 64, static_cast<float*>(c->op_out.ptr));
+  JXG_CUDA(c, cudaGetLastError());
+  JXG_CUDA(c, cudaMemcpyAsync(cols.data(), c->op_out.ptr, cols.size() * 4, cudaMemcpyDeviceToHost, s));
+  if ((st = wait(c))) return st;
+  // cols[j][p] is the image of coefficient j: M[p][j], M^T[j][p]
+  std::vector<float> m(4096);
+  for (int j = 0; j < 64; ++j)
+    for (int p = 0; p < 64; ++p) m[p * 64 + j] = cols[j * 64 + p];
+  JXG_CUDA(c, cudaMemcpyAsync(r.m, m.data(), 4096 * 4, cudaMemcpyHostToDevice, s));
+  JXG_CUDA(c, cudaMemcpyAsync(r.mt, cols.data(), 4096 * 4, cudaMemcpyHostToDevice, s));
+  const bool timed = c->timing;
+  if ((st = launch(c, "k_refine_dct", timed, [&] {
+         k_refine_dct<<<static_cast<unsigned>((nb + 7) / 8), 256, 0, s>>>(r);
+       })) ||
+      (st = launch(c, "k_refine_linear", timed, [&] {
+         k_refine_linear<<<refine_grid(n), 256, 0, s>>>(r.xyb, r.plane, r.w, c->refine_lin[0][0], r.w, r.h);
+       })))
+    return st;
+  for (int k = 1; k < 3; ++k)
+    if (c->refine_n[k] && (st = launch(c, "k_refine_down", timed, [&] {
+                             k_refine_down<<<refine_grid(3 * c->refine_n[k]), 256, 0, s>>>(
+                                 c->refine_lin[0][k - 1], c->refine_lin[0][k], c->refine_w[k - 1], c->refine_h[k - 1]);
+                           })))
+      return st;
+  if ((st = wait(c))) return st;
+  r.xyb = nullptr;
+  c->refine_ready = true;
+  *xsize_blocks = static_cast<uint64_t>(r.xb);
+  *ysize_blocks = static_cast<uint64_t>(r.yb);
+  return JXG_OK;
+}
+
+int32_t jxg_refine_eval(void* ctx, const float* theta, float rate_lambda, float* grad, double* loss3,
+                        int32_t* levels) {
+  using namespace jxg;
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !loss3) return JXG_ERR_INVALID_ARGUMENT;
+  if (!c->refine_ready) return fail(c, JXG_ERR_INVALID_ARGUMENT, "jxg_refine_begin first");
+  if (!theta) theta = c->refine_theta;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  const RefineArgs& r = c->refine;
+  const int64_t nb = static_cast<int64_t>(r.xb) * r.yb;
+  const int64_t n = c->refine_n[0];
+  int st;
+  int32_t* dlev = nullptr;
+  if (levels) {
+    if ((st = ensure(c, c->refine_levels, nb * 192 * 4))) return st;
+    dlev = static_cast<int32_t*>(c->refine_levels.ptr);
+  }
+  const bool timed = c->timing;
+  double* sums = c->refine_sums;
+  JXG_CUDA(c, cudaMemsetAsync(sums, 0, 4 * kRefineSlots * sizeof(double), s));
+  const unsigned block_ctas = static_cast<unsigned>((nb + 7) / 8);
+  if ((st = launch(c, "k_refine_forward", timed, [&] {
+         k_refine_forward<<<block_ctas, 256, 0, s>>>(r, theta, dlev, c->refine_lin[1][0], sums + 3 * kRefineSlots);
+       })))
+    return st;
+  for (int k = 1; k < 3; ++k)
+    if (c->refine_n[k] && (st = launch(c, "k_refine_down", timed, [&] {
+                             k_refine_down<<<refine_grid(3 * c->refine_n[k]), 256, 0, s>>>(
+                                 c->refine_lin[1][k - 1], c->refine_lin[1][k], c->refine_w[k - 1], c->refine_h[k - 1]);
+                           })))
+      return st;
+  for (int k = 0; k < 3; ++k) {
+    const int64_t nk = c->refine_n[k];
+    if (!nk) continue;
+    const int w = c->refine_w[k], h = c->refine_h[k];
+    // L_k = sum(1 - SSIM) / (3 channels * pixels * 3 scales)
+    const float weight = static_cast<float>(1.0 / (9.0 * static_cast<double>(nk)));
+    const dim3 grid(static_cast<unsigned>((w + kSsimTW - 1) / kSsimTW), static_cast<unsigned>((h + kSsimTH - 1) / kSsimTH),
+                    3);
+    if ((st = launch(c, "k_refine_ssim", timed, [&] {
+           k_refine_ssim<<<grid, 256, 0, s>>>(c->refine_lin[0][k], c->refine_lin[1][k], w, h, weight,
+                                              c->refine_glin[k], sums + k * kRefineSlots);
+         })))
+      return st;
+  }
+  const float rate_weight = static_cast<float>(static_cast<double>(rate_lambda) / static_cast<double>(n));
+  if (grad) {
+    if (c->refine_n[2] && (st = launch(c, "k_refine_up_add", timed, [&] {
+                             k_refine_up_add<<<refine_grid(3 * c->refine_n[1]), 256, 0, s>>>(
+                                 c->refine_glin[2], c->refine_glin[1], c->refine_w[1], c->refine_h[1]);
+                           })))
+      return st;
+    if ((st = launch(c, "k_refine_backward", timed, [&] {
+           k_refine_backward<<<block_ctas, 256, 0, s>>>(r, theta, c->refine_glin[0], c->refine_glin[1],
+                                                        c->refine_w[1], c->refine_h[1], rate_weight, grad);
+         })))
+      return st;
+  }
+  double host[4 * kRefineSlots];
+  JXG_CUDA(c, cudaMemcpyAsync(host, sums, sizeof(host), cudaMemcpyDeviceToHost, s));
+  if (levels) JXG_CUDA(c, cudaMemcpyAsync(levels, dlev, nb * 192 * 4, cudaMemcpyDeviceToHost, s));
+  if ((st = wait(c))) return st;
+  double total[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int q = 0; q < 4; ++q)
+    for (int k = 0; k < kRefineSlots; ++k) total[q] += host[q * kRefineSlots + k];
+  double dist = 0.0;
+  for (int k = 0; k < 3; ++k)
+    if (c->refine_n[k]) dist += total[k] / (9.0 * static_cast<double>(c->refine_n[k]));
+  loss3[0] = dist + static_cast<double>(rate_lambda) * total[3] / static_cast<double>(n);
+  loss3[1] = dist;
+  loss3[2] = total[3];
+  return JXG_OK;
+}
+
+int32_t jxg_refine_field(void* ctx, const float* theta, uint8_t* quant_field) {
+  using namespace jxg;
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !quant_field) return JXG_ERR_INVALID_ARGUMENT;
+  if (!c->refine_ready) return fail(c, JXG_ERR_INVALID_ARGUMENT, "jxg_refine_begin first");
+  if (!theta) theta = c->refine_theta;
+  cudaSetDevice(c->device);
+  const int64_t nb = static_cast<int64_t>(c->refine.xb) * c->refine.yb;
+  cudaPointerAttributes at{};
+  const bool on_device =
+      cudaPointerGetAttributes(&at, quant_field) == cudaSuccess && at.type == cudaMemoryTypeDevice;
+  cudaGetLastError();
+  int st;
+  if (!on_device && (st = ensure(c, c->field_buf, nb))) return st;
+  uint8_t* out = on_device ? quant_field : static_cast<uint8_t*>(c->field_buf.ptr);
+  k_refine_field<<<refine_grid(nb), 256, 0, c->stream>>>(c->refine.qf, theta, nb, out);
+  JXG_CUDA(c, cudaGetLastError());
+  if (!on_device) JXG_CUDA(c, cudaMemcpyAsync(quant_field, out, nb, cudaMemcpyDeviceToHost, c->stream));
+  return wait(c);
+}
+
+int32_t jxg_refine_step(void* ctx, float rate_lambda, float learning_rate, double* loss3) {
+  using namespace jxg;
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !loss3) return JXG_ERR_INVALID_ARGUMENT;
+  if (!c->refine_ready) return fail(c, JXG_ERR_INVALID_ARGUMENT, "jxg_refine_begin first");
+  if (!(learning_rate > 0.0f) || !std::isfinite(learning_rate) || !(rate_lambda >= 0.0f) ||
+      !std::isfinite(rate_lambda))
+    return fail(c, JXG_ERR_INVALID_ARGUMENT, "learning rate > 0 and lambda >= 0, both finite");
+  const int64_t nb = static_cast<int64_t>(c->refine.xb) * c->refine.yb;
+  int st = jxg_refine_eval(ctx, c->refine_theta, rate_lambda, c->refine_grad, loss3, nullptr);
+  if (st) return st;
+  if (c->refine_steps == 0) JXG_CUDA(c, cudaMemsetAsync(c->refine_adam, 0, 2 * nb * 4, c->stream));
+  const int t = ++c->refine_steps;
+  const float c1 = static_cast<float>(1.0 / (1.0 - std::pow(kAdamBeta1, t)));
+  const float c2 = static_cast<float>(1.0 / (1.0 - std::pow(kAdamBeta2, t)));
+  k_refine_adam<<<refine_grid(nb), 256, 0, c->stream>>>(c->refine.qf, c->refine_grad, nb, learning_rate, c1, c2,
+                                                        c->refine_adam, c->refine_theta);
+  JXG_CUDA(c, cudaGetLastError());
+  return wait(c);
+}
+
+int32_t jxg_refine_theta(void* ctx, float* theta, int32_t to_context) {
+  using namespace jxg;
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !theta) return JXG_ERR_INVALID_ARGUMENT;
+  if (!c->refine_ready) return fail(c, JXG_ERR_INVALID_ARGUMENT, "jxg_refine_begin first");
+  const size_t bytes = static_cast<size_t>(c->refine.xb) * c->refine.yb * 4;
+  if (to_context) {
+    JXG_CUDA(c, cudaMemcpyAsync(c->refine_theta, theta, bytes, cudaMemcpyDefault, c->stream));
+    c->refine_steps = 0;
+  } else {
+    JXG_CUDA(c, cudaMemcpyAsync(theta, c->refine_theta, bytes, cudaMemcpyDefault, c->stream));
+  }
+  return wait(c);
+}
+
+int32_t jxg_refine_model(void* ctx, float* constants, float* coefficients, float* inverse) {
+  using namespace jxg;
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !constants) return JXG_ERR_INVALID_ARGUMENT;
+  if (!c->refine_ready) return fail(c, JXG_ERR_INVALID_ARGUMENT, "jxg_refine_begin first");
+  cudaSetDevice(c->device);
+  const RefineArgs& r = c->refine;
+  float* o = constants;
+  *o++ = r.scale;
+  for (int k = 0; k < 3; ++k) *o++ = r.qm_mul[k];
+  std::memcpy(o, r.matrix, sizeof(r.matrix));
+  o += 192;
+  std::memcpy(o, r.inv_matrix, sizeof(r.inv_matrix));
+  o += 192;
+  std::memcpy(o, r.thresholds, sizeof(r.thresholds));
+  const int64_t nb = static_cast<int64_t>(r.xb) * r.yb;
+  if (coefficients)
+    JXG_CUDA(c, cudaMemcpyAsync(coefficients, r.coef, nb * 192 * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (inverse) JXG_CUDA(c, cudaMemcpyAsync(inverse, r.m, 4096 * 4, cudaMemcpyDeviceToHost, c->stream));
+  return wait(c);
 }
 
 int32_t jxg_get_launch_geometry(void* ctx, uint8_t* warps) {

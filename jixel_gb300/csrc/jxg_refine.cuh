@@ -1,0 +1,559 @@
+// Differentiable quant-field refinement of an all-DCT8 frame (the frame the
+// last UltraFast pass of a context coded).  Not in the reference, which has no
+// gradients anywhere; it refines what adaptive_quant.rs gives it.
+//
+// Parameters: theta, one log quant scale per 8x8 block; block b's quantiser is
+// s_b = scale * qf_b * exp(theta_b), qf the pass's adaptive field.
+//
+// Forward model (FP32), per block, as the front end quantises (k_tile_quantize
+// and write_ac_group, src/group.rs:560-612, :767-818, :1831-1858):
+//   Y AC levels at s, their dequantised values with the decoder's bias
+//   (DequantBias, src/group.rs:767); CfL on X and B from the dequantised Y; X
+//   and B levels at s; the decoder's coefficients X^ = deq(X) + xf Y^,
+//   B^ = deq(B) + bf Y^.  The DC slot keeps the source value (the DC path is
+//   not refined);
+//   the 8x8 inverse transform as a 64 x 64 matrix M taken from the library's
+//   own IDCT (src/dct.rs:1500-1620), so its adjoint is exactly M^T;
+//   XYB to linear RGB (xyb_to_rgb_pixel_f32, src/xyb.rs:265-283);
+//   the distortion proxy: 1 - SSIM of the linear planes against the source's,
+//   at three scales (2x2 box average between them), with a 5-tap binomial blur
+//   (zero outside the image), averaged over channels, pixels and scales;
+//   the rate model: per non-zero AC level 1.6 + log2(1 + |level|) bits (the
+//   coefficient model's per-level terms, src/inflated_cost.rs:540-547); a
+//   level that rounds to zero costs 2.6 (|v| / z)^4 bits, v its quantiser
+//   input and z = max(threshold, 0.5) the edge of its zero region, so that
+//   finer quantisation sees the levels it is about to create;
+//   loss = distortion + lambda * bits / pixels.
+// Rounding is straight-through: the backward pass treats each non-zero level
+// as its unrounded value, keeps zero levels' decoded values at zero, and
+// differentiates the bias for |level| >= 2 (1 + 0.145 / level^2; 0 at
+// |level| = 1).
+// EPF, gaborish (off in the reference's encoder) and DC smoothing are not
+// modelled.
+#pragma once
+
+namespace jxg {
+
+struct RefineArgs {
+  int32_t w, h, xb, yb, pw;  // image, blocks, padded plane width (xb * 8)
+  int64_t plane;             // floats between the source XYB planes
+  const float* xyb;          // source XYB
+  float* coef;               // [block][X, Y, B][64] source DCT8 coefficients
+  const uint8_t* qf;         // the pass's quant field
+  const int8_t* ytox;
+  const int8_t* ytob;
+  int32_t tiles_x;
+  float scale, qm_mul[3];
+  float matrix[3][64], inv_matrix[3][64], thresholds[3][4];
+  float* m;                  // [64 pixels][64 coefficients] inverse DCT8
+  float* mt;                 // the same, [coefficient][pixel]
+  float* recon;              // 3 padded planes (pw x yb * 8) of decoded XYB
+};
+
+// f64 partial sums: kRefineSlots per quantity (the three scales' 1 - SSIM,
+// then the rate), CTAs spread over them; the host adds each quantity's slots.
+constexpr int kRefineSlots = 32;
+
+constexpr float kOpsinBias = 0.0037930734f, kNegBiasCbrt = -0.1559542f;
+// OPSIN_INVERSE_MATRIX (src/xyb.rs:49-59)
+__constant__ const float kOpsinInverse[9] = {11.031567f,   -9.866944f,  -0.16462299f,
+                                             -3.2541473f,  4.4187703f,  -0.16462299f,
+                                             -3.6588514f,  2.712923f,   1.9459282f};
+constexpr float kLn2 = 0.6931471805599453f;
+constexpr float kZeroBits = 2.6f;  // 1.6 + log2(1 + 1): a level of one
+
+__device__ __forceinline__ float refine_bias(int c, int32_t q) { return bias_level(c, q); }
+__device__ __forceinline__ float refine_bias_slope(int32_t q) {
+  if (q == 1 || q == -1 || q == 0) return 0.0f;
+  const float qf = static_cast<float>(q);
+  return 1.0f + 0.145f / (qf * qf);
+}
+
+// One coefficient's decoded values and, for the backward pass, their
+// derivatives by s.
+struct CoefState {
+  int32_t q[3];
+  float hat[3];   // X^, Y^, B^
+  float dhat[3];  // dX^/ds, dY^/ds, dB^/ds
+  float dbits;    // d bits / ds
+  float bits;
+};
+
+__device__ __forceinline__ void refine_coef(const RefineArgs& r, int i, float s, float xf, float bf,
+                                            float cx, float cy, float cb, bool grad, CoefState* o) {
+  const float inv_s = __fdiv_rn(1.0f, s);
+  const int row = i >> 3, col = i & 7, yfix = row >= 4 ? 2 : 0;
+  auto thr = [&](int c) { return col >= 4 ? r.thresholds[c][yfix + 1] : r.thresholds[c][yfix]; };
+  // Y, as k_tile_quantize: (inv * (s * qm)) * c, then (bias * w) * (1 / s)
+  const float vy = __fmul_rn(__fmul_rn(r.inv_matrix[1][i], __fmul_rn(s, r.qm_mul[1])), cy);
+  const int32_t qy = quantize_level(vy, thr(1));
+  const float yh = __fmul_rn(__fmul_rn(refine_bias(1, qy), r.matrix[1][i]), inv_s);
+  float dyh = 0.0f;
+  if (grad && qy != 0)
+    dyh = __fmul_rn(__fdiv_rn(r.matrix[1][i], __fmul_rn(s, s)),
+                    __fsub_rn(__fmul_rn(refine_bias_slope(qy), vy), refine_bias(1, qy)));
+  float bits = 0.0f, dbits = 0.0f;
+  // a level q from the quantiser input v (dv = dv/ds); a level that rounds
+  // to zero costs kZeroBits (|v| / z)^4, z = max(threshold, 0.5) the edge of
+  // its zero region, rising smoothly to the cost of a level of one
+  auto rate = [&](int32_t q, float v, float dv, float t) {
+    if (q == 0) {
+      const float z = fmaxf(t, 0.5f), a = __fdiv_rn(fabsf(v), z), a2 = __fmul_rn(a, a);
+      bits = __fmaf_rn(kZeroBits, __fmul_rn(a2, a2), bits);
+      if (grad)
+        dbits = __fmaf_rn(__fmul_rn(4.0f * kZeroBits, __fmul_rn(a2, a)), __fdiv_rn(copysignf(1.0f, v) * dv, z), dbits);
+      return;
+    }
+    const float a = fabsf(static_cast<float>(q));
+    bits = __fadd_rn(bits, __fadd_rn(1.6f, __log2f(1.0f + a)));
+    if (grad) dbits = __fadd_rn(dbits, __fdiv_rn(copysignf(1.0f, static_cast<float>(q)) * dv,
+                                                 __fmul_rn(1.0f + a, kLn2)));
+  };
+  rate(qy, vy, __fdiv_rn(vy, s), thr(1));
+  // X and B after CfL from the dequantised Y
+  const float cc[2] = {cx, cb}, ff[2] = {xf, bf};
+  const int ch[2] = {0, 2};
+  float hat[2], dhat[2];
+  int32_t qq[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int c = ch[k];
+    const float qm = r.qm_mul[c];
+    const float v = __fmaf_rn(-ff[k], yh, cc[k]);
+    const float u = __fmul_rn(__fmul_rn(r.inv_matrix[c][i], __fmul_rn(s, qm)), v);
+    const int32_t q = quantize_level(u, thr(c));
+    qq[k] = q;
+    const float sq = __fmul_rn(s, qm);
+    const float deq = q == 0 ? 0.0f : __fdiv_rn(__fmul_rn(refine_bias(c, q), r.matrix[c][i]), sq);
+    hat[k] = __fmaf_rn(ff[k], yh, deq);
+    dhat[k] = 0.0f;
+    if (grad) {
+      // du/ds = u / s - inv * s * qm * xf * dY^/ds
+      const float du = __fsub_rn(__fdiv_rn(u, s),
+                                 __fmul_rn(__fmul_rn(r.inv_matrix[c][i], sq), __fmul_rn(ff[k], dyh)));
+      float dd = 0.0f;
+      if (q != 0)
+        dd = __fmul_rn(__fdiv_rn(r.matrix[c][i], sq),
+                       __fsub_rn(__fmul_rn(refine_bias_slope(q), du), __fdiv_rn(refine_bias(c, q), s)));
+      dhat[k] = __fmaf_rn(ff[k], dyh, dd);
+      rate(q, u, du, thr(c));
+    } else {
+      rate(q, u, 0.0f, thr(c));
+    }
+  }
+  o->q[0] = qq[0];
+  o->q[1] = qy;
+  o->q[2] = qq[1];
+  o->hat[0] = hat[0];
+  o->hat[1] = yh;
+  o->hat[2] = hat[1];
+  o->dhat[0] = dhat[0];
+  o->dhat[1] = dyh;
+  o->dhat[2] = dhat[1];
+  o->bits = bits;
+  o->dbits = dbits;
+}
+
+__device__ __forceinline__ float refine_s(const RefineArgs& r, int64_t b, float theta) {
+  return __fmul_rn(__fmul_rn(r.scale, static_cast<float>(r.qf[b])), expf(theta));
+}
+__device__ __forceinline__ void refine_cfl(const RefineArgs& r, int bx, int by, float* xf, float* bf) {
+  const int t = (by >> 3) * r.tiles_x + (bx >> 3);
+  *xf = fmla(static_cast<float>(r.ytox[t]), 1.0f / 84.0f, 0.0f);
+  *bf = fmla(static_cast<float>(r.ytob[t]), 1.0f / 84.0f, 1.0f);
+}
+
+// Source coefficients: one warp per block, the tile kernel's gather with edge
+// replication, rows then columns, stored transposed and scaled by 1/64.
+__global__ void __launch_bounds__(256) k_refine_dct(const RefineArgs r) {
+  __shared__ float buf[8][3][8][9];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t b = static_cast<int64_t>(blockIdx.x) * 8 + warp;
+  if (b >= static_cast<int64_t>(r.xb) * r.yb) return;
+  const int bx = static_cast<int>(b % r.xb), by = static_cast<int>(b / r.xb);
+  if (lane < 24) {
+    const int c = lane >> 3, row = lane & 7;
+    const float* p = r.xyb + c * r.plane;
+    const int y = imin(by * 8 + row, r.h - 1);
+    float v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = p[static_cast<int64_t>(y) * r.w + imin(bx * 8 + k, r.w - 1)];
+    dct1d_8(v);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) buf[warp][c][row][k] = v[k];
+  }
+  __syncwarp();
+  if (lane < 24) {
+    const int c = lane >> 3, cc = lane & 7;
+    float v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = buf[warp][c][k][cc];
+    dct1d_8(v);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) r.coef[(b * 3 + c) * 64 + cc * 8 + k] = v[k] * (1.0f / 64.0f);
+  }
+}
+
+// XYB -> linear RGB of one pixel (xyb_to_rgb_pixel_f32, src/xyb.rs:265-283);
+// with `dcube`, the cube's derivatives 3 (t - bias)^2 for the adjoint.
+__device__ __forceinline__ void xyb_to_linear(float x, float y, float b, float* out, float* dcube) {
+  const float t[3] = {__fadd_rn(y, x), __fsub_rn(y, x), b};
+  float m[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float c = __fsub_rn(t[k], kNegBiasCbrt);
+    m[k] = __fsub_rn(__fmul_rn(__fmul_rn(c, c), c), kOpsinBias);
+    if (dcube) dcube[k] = __fmul_rn(3.0f, __fmul_rn(c, c));
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+    out[j] = __fmaf_rn(kOpsinInverse[j * 3], m[0],
+                       __fmaf_rn(kOpsinInverse[j * 3 + 1], m[1], __fmul_rn(kOpsinInverse[j * 3 + 2], m[2])));
+}
+
+__device__ __forceinline__ void refine_add_slot(double v, double* sums) {
+  __shared__ double part[8];
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+  const int nw = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < nw; ++k) t += part[k];
+    const unsigned cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    atomicAdd(sums + cta % kRefineSlots, t);
+  }
+}
+
+// Forward: one warp per block, two coefficients per lane; the levels (when
+// asked) and the rate, then the block's decoded XYB pixels M * c^ into the
+// padded planes and, inside the image, their linear RGB into `lin`
+// (3 planes of w x h).  The rate's CTA sum goes to `bit_sums`.
+__global__ void __launch_bounds__(256) k_refine_forward(const RefineArgs r, const float* __restrict__ theta,
+                                                        int32_t* __restrict__ levels, float* __restrict__ lin,
+                                                        double* __restrict__ bit_sums) {
+  __shared__ float cs[8][3][64];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t b = static_cast<int64_t>(blockIdx.x) * 8 + warp;
+  const bool active = b < static_cast<int64_t>(r.xb) * r.yb;
+  float bits = 0.0f;
+  if (active) {
+    const int bx = static_cast<int>(b % r.xb), by = static_cast<int>(b / r.xb);
+    const float s = refine_s(r, b, theta[b]);
+    float xf, bf;
+    refine_cfl(r, bx, by, &xf, &bf);
+#pragma unroll
+    for (int h2 = 0; h2 < 2; ++h2) {
+      const int i = lane + 32 * h2;
+      const float* c = r.coef + b * 192;
+      CoefState st;
+      refine_coef(r, i, s, xf, bf, c[i], c[64 + i], c[128 + i], false, &st);
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) {
+        cs[warp][ch][i] = i == 0 ? c[ch * 64] : st.hat[ch];
+        if (levels) levels[b * 192 + ch * 64 + i] = i == 0 ? 0 : st.q[ch];
+      }
+      if (i != 0) bits = __fadd_rn(bits, st.bits);
+    }
+    __syncwarp();
+    const int64_t pp = static_cast<int64_t>(r.pw) * r.yb * 8, n = static_cast<int64_t>(r.w) * r.h;
+#pragma unroll
+    for (int h2 = 0; h2 < 2; ++h2) {
+      const int p = lane + 32 * h2;
+      float acc[3] = {0.0f, 0.0f, 0.0f};
+      for (int i = 0; i < 64; ++i) {
+        const float m = r.mt[i * 64 + p];
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) acc[ch] = __fmaf_rn(m, cs[warp][ch][i], acc[ch]);
+      }
+      const int y = by * 8 + (p >> 3), x = bx * 8 + (p & 7);
+      const int64_t at = static_cast<int64_t>(y) * r.pw + x;
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) r.recon[ch * pp + at] = acc[ch];
+      if (x < r.w && y < r.h) {
+        float o[3];
+        xyb_to_linear(acc[0], acc[1], acc[2], o, nullptr);
+        const int64_t q = static_cast<int64_t>(y) * r.w + x;
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) lin[ch * n + q] = o[ch];
+      }
+    }
+  }
+  refine_add_slot(static_cast<double>(bits), bit_sums);
+}
+
+// Linear RGB of the w x h region of XYB planes with row stride `in_stride`.
+__global__ void __launch_bounds__(256) k_refine_linear(const float* __restrict__ xyb, int64_t in_plane,
+                                                       int in_stride, float* __restrict__ lin, int w,
+                                                       int h) {
+  const int64_t p = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (p >= static_cast<int64_t>(w) * h) return;
+  const int y = static_cast<int>(p / w), x = static_cast<int>(p % w);
+  const int64_t at = static_cast<int64_t>(y) * in_stride + x;
+  float o[3];
+  xyb_to_linear(xyb[at], xyb[in_plane + at], xyb[2 * in_plane + at], o, nullptr);
+  const int64_t n = static_cast<int64_t>(w) * h;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) lin[c * n + p] = o[c];
+}
+
+// 2x2 box average to the next scale (3 planes of w x h -> (w/2) x (h/2)).
+__global__ void __launch_bounds__(256) k_refine_down(const float* __restrict__ in, float* __restrict__ out,
+                                                     int w, int h) {
+  const int w2 = w / 2, h2 = h / 2;
+  const int64_t n2 = static_cast<int64_t>(w2) * h2;
+  const int64_t p = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (p >= 3 * n2) return;
+  const int c = static_cast<int>(p / n2);
+  const int64_t q = p % n2;
+  const int y = static_cast<int>(q / w2), x = static_cast<int>(q % w2);
+  const float* src = in + c * static_cast<int64_t>(w) * h;
+  const int64_t a = static_cast<int64_t>(2 * y) * w + 2 * x;
+  out[p] = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(src[a], src[a + 1]), __fadd_rn(src[a + w], src[a + w + 1])));
+}
+
+// The adjoint: each fine pixel takes a quarter of its coarse pixel's gradient.
+__global__ void __launch_bounds__(256) k_refine_up_add(const float* __restrict__ g2, float* __restrict__ g,
+                                                       int w, int h) {
+  const int w2 = w / 2, h2 = h / 2;
+  const int64_t n = static_cast<int64_t>(w) * h;
+  const int64_t p = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (p >= 3 * n) return;
+  const int c = static_cast<int>(p / n);
+  const int64_t q = p % n;
+  const int y = static_cast<int>(q / w), x = static_cast<int>(q % w);
+  if (y / 2 >= h2 || x / 2 >= w2) return;
+  g[p] = __fadd_rn(g[p], __fmul_rn(0.25f, g2[c * static_cast<int64_t>(w2) * h2 + (y / 2) * w2 + x / 2]));
+}
+
+constexpr float kSsimC1 = 1e-4f, kSsimC2 = 9e-4f;
+// SSIM tile of the fused kernel: 32 x 16 pixels of one channel, 256 threads
+constexpr int kSsimTW = 32, kSsimTH = 16;
+constexpr int kSsimInW = kSsimTW + 8, kSsimInH = kSsimTH + 8;     // inputs with a 4-pixel ring
+constexpr int kSsimRingW = kSsimTW + 4, kSsimRingH = kSsimTH + 4; // SSIM with a 2-pixel ring
+
+__device__ __forceinline__ float blur_tap(int d) {
+  return d == 0 ? 6.0f / 16 : (d == 1 || d == -1 ? 4.0f / 16 : 1.0f / 16);
+}
+
+// 1 - SSIM of one scale and its gradient by the decoded plane, one channel
+// per grid z, fused: the moments a, b, a a, b b, a b of the source a and the
+// decoded b under the 5-tap binomial blur [1 4 6 4 1] / 16 (zero outside
+// the plane, rows then columns), SSIM (C1 1e-4, C2 9e-4) and its partial
+// derivatives by the blurred b, b b and a b on the tile and a 2-pixel ring,
+// their blur (the blur is its own adjoint under zero padding), and
+//   d L / d b = G(g_b) + 2 b G(g_bb) + a G(g_ab)
+// into `grad` (3 planes of w x h).  L = weight * sum(1 - SSIM); the tile's
+// sum goes to `sums`.
+__global__ void __launch_bounds__(256) k_refine_ssim(const float* __restrict__ a_planes,
+                                                     const float* __restrict__ b_planes, int w, int h,
+                                                     float weight, float* __restrict__ grad,
+                                                     double* __restrict__ sums) {
+  __shared__ float in[2][kSsimInH][kSsimInW + 1];
+  __shared__ float xm[5][kSsimInH][kSsimRingW];       // row-blurred moments; later the row-blurred grads
+  __shared__ float g[3][kSsimRingH][kSsimRingW + 1];
+  const int tid = threadIdx.x;
+  const int x0 = blockIdx.x * kSsimTW, y0 = blockIdx.y * kSsimTH, ch = blockIdx.z;
+  const int64_t n = static_cast<int64_t>(w) * h;
+  const float* A = a_planes + ch * n;
+  const float* B = b_planes + ch * n;
+  // 0. inputs over the tile and a 4-pixel ring, zero outside the plane
+  for (int u = tid; u < kSsimInH * kSsimInW; u += 256) {
+    const int r = u / kSsimInW, c = u % kSsimInW;
+    const int y = y0 - 4 + r, x = x0 - 4 + c;
+    const bool inside = x >= 0 && x < w && y >= 0 && y < h;
+    const int64_t at = static_cast<int64_t>(y) * w + x;
+    in[0][r][c] = inside ? A[at] : 0.0f;
+    in[1][r][c] = inside ? B[at] : 0.0f;
+  }
+  __syncthreads();
+  // 1. row blur of the five moments at columns -2 .. kSsimTW + 2
+  for (int u = tid; u < kSsimInH * kSsimRingW; u += 256) {
+    const int r = u / kSsimRingW, c = u % kSsimRingW;
+    float m[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int d = -2; d <= 2; ++d) {
+      const float k = blur_tap(d), va = in[0][r][c + 2 + d], vb = in[1][r][c + 2 + d];
+      m[0] = __fmaf_rn(k, va, m[0]);
+      m[1] = __fmaf_rn(k, vb, m[1]);
+      m[2] = __fmaf_rn(k, __fmul_rn(va, va), m[2]);
+      m[3] = __fmaf_rn(k, __fmul_rn(vb, vb), m[3]);
+      m[4] = __fmaf_rn(k, __fmul_rn(va, vb), m[4]);
+    }
+#pragma unroll
+    for (int q = 0; q < 5; ++q) xm[q][r][c] = m[q];
+  }
+  __syncthreads();
+  // 2. column blur, SSIM and its derivatives on the tile and a 2-pixel ring
+  double loss = 0.0;
+  for (int u = tid; u < kSsimRingH * kSsimRingW; u += 256) {
+    const int r = u / kSsimRingW, c = u % kSsimRingW;
+    const int y = y0 - 2 + r, x = x0 - 2 + c;
+    float m[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int d = -2; d <= 2; ++d) {
+      const float k = blur_tap(d);
+#pragma unroll
+      for (int q = 0; q < 5; ++q) m[q] = __fmaf_rn(k, xm[q][r + 2 + d][c], m[q]);
+    }
+    float gm2 = 0.0f, gs22 = 0.0f, gs12 = 0.0f;
+    if (x >= 0 && x < w && y >= 0 && y < h) {
+      const float m1 = m[0], m2 = m[1];
+      const float v1 = __fsub_rn(m[2], __fmul_rn(m1, m1)), v2 = __fsub_rn(m[3], __fmul_rn(m2, m2));
+      const float c12 = __fsub_rn(m[4], __fmul_rn(m1, m2));
+      const float n1 = __fadd_rn(__fmul_rn(2.0f, __fmul_rn(m1, m2)), kSsimC1);
+      const float n2 = __fadd_rn(__fmul_rn(2.0f, c12), kSsimC2);
+      const float d1 = __fadd_rn(__fadd_rn(__fmul_rn(m1, m1), __fmul_rn(m2, m2)), kSsimC1);
+      const float d2 = __fadd_rn(__fadd_rn(v1, v2), kSsimC2);
+      const float dd = __fmul_rn(d1, d2);
+      const float ssim = __fdiv_rn(__fmul_rn(n1, n2), dd);
+      if (r >= 2 && r < 2 + kSsimTH && c >= 2 && c < 2 + kSsimTW) loss += 1.0 - static_cast<double>(ssim);
+      // d ssim / d m2, d s22, d s12 (the source's moments fixed)
+      const float dm2 = __fdiv_rn(__fsub_rn(__fmul_rn(__fmul_rn(2.0f, m1), __fsub_rn(n2, n1)),
+                                            __fmul_rn(ssim, __fmul_rn(__fmul_rn(2.0f, m2), __fsub_rn(d2, d1)))),
+                                  dd);
+      gm2 = -weight * dm2;
+      gs22 = weight * __fdiv_rn(ssim, d2);
+      gs12 = -weight * __fdiv_rn(__fmul_rn(2.0f, n1), dd);
+    }
+    g[0][r][c] = gm2;
+    g[1][r][c] = gs22;
+    g[2][r][c] = gs12;
+  }
+  __syncthreads();
+  // 3. row blur of the derivatives (into xm, free now) at the tile's columns
+  for (int u = tid; u < kSsimRingH * kSsimTW; u += 256) {
+    const int r = u / kSsimTW, c = u % kSsimTW;
+    float v[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int d = -2; d <= 2; ++d) {
+      const float k = blur_tap(d);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) v[q] = __fmaf_rn(k, g[q][r][c + 2 + d], v[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) xm[q][r][c] = v[q];
+  }
+  __syncthreads();
+  // 4. column blur and the gradient by the decoded plane
+  for (int u = tid; u < kSsimTH * kSsimTW; u += 256) {
+    const int r = u / kSsimTW, c = u % kSsimTW;
+    const int y = y0 + r, x = x0 + c;
+    if (x >= w || y >= h) continue;
+    float v[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int d = -2; d <= 2; ++d) {
+      const float k = blur_tap(d);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) v[q] = __fmaf_rn(k, xm[q][r + 2 + d][c], v[q]);
+    }
+    const float va = in[0][r + 4][c + 4], vb = in[1][r + 4][c + 4];
+    grad[ch * n + static_cast<int64_t>(y) * w + x] =
+        __fmaf_rn(va, v[2], __fmaf_rn(__fmul_rn(2.0f, vb), v[1], v[0]));
+  }
+  refine_add_slot(loss, sums);
+}
+
+// Backward per block: the gradient by the linear planes (scale 0 plus a
+// quarter of scale 1's at the covering coarse pixel; scale 1 already holds
+// scale 2's), back through XYB -> linear to the decoded XYB, M^T to the
+// coefficients, then d L / d theta.
+__global__ void __launch_bounds__(256) k_refine_backward(const RefineArgs r, const float* __restrict__ theta,
+                                                         const float* __restrict__ glin0,
+                                                         const float* __restrict__ glin1, int w1, int h1,
+                                                         float rate_weight, float* __restrict__ gtheta) {
+  __shared__ float gs[8][3][64];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t b = static_cast<int64_t>(blockIdx.x) * 8 + warp;
+  if (b >= static_cast<int64_t>(r.xb) * r.yb) return;
+  const int bx = static_cast<int>(b % r.xb), by = static_cast<int>(b / r.xb);
+  const int64_t pp = static_cast<int64_t>(r.pw) * r.yb * 8, n = static_cast<int64_t>(r.w) * r.h;
+  const int64_t n1 = static_cast<int64_t>(w1) * h1;
+#pragma unroll
+  for (int h2 = 0; h2 < 2; ++h2) {
+    const int p = lane + 32 * h2;
+    const int y = by * 8 + (p >> 3), x = bx * 8 + (p & 7);
+    float gx[3] = {0.0f, 0.0f, 0.0f};
+    if (x < r.w && y < r.h) {
+      const int64_t q = static_cast<int64_t>(y) * r.w + x;
+      float gl[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) gl[k] = glin0[k * n + q];
+      if ((y >> 1) < h1 && (x >> 1) < w1) {
+        const int64_t q1 = static_cast<int64_t>(y >> 1) * w1 + (x >> 1);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) gl[k] = __fmaf_rn(0.25f, glin1[k * n1 + q1], gl[k]);
+      }
+      const int64_t at = static_cast<int64_t>(y) * r.pw + x;
+      float o[3], dc[3];
+      xyb_to_linear(r.recon[at], r.recon[pp + at], r.recon[2 * pp + at], o, dc);
+      float gm[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        gm[k] = __fmul_rn(dc[k], __fmaf_rn(kOpsinInverse[k], gl[0],
+                                           __fmaf_rn(kOpsinInverse[3 + k], gl[1],
+                                                     __fmul_rn(kOpsinInverse[6 + k], gl[2]))));
+      // t0 = y + x, t1 = y - x, t2 = b
+      gx[0] = __fsub_rn(gm[0], gm[1]);
+      gx[1] = __fadd_rn(gm[0], gm[1]);
+      gx[2] = gm[2];
+    }
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) gs[warp][ch][p] = gx[ch];
+  }
+  __syncwarp();
+  const float s = refine_s(r, b, theta[b]);
+  float xf, bf;
+  refine_cfl(r, bx, by, &xf, &bf);
+  float acc = 0.0f;
+#pragma unroll
+  for (int h2 = 0; h2 < 2; ++h2) {
+    const int i = lane + 32 * h2;
+    if (i == 0) continue;  // the DC slot keeps the source value
+    float gc[3] = {0.0f, 0.0f, 0.0f};
+    for (int p = 0; p < 64; ++p) {
+      const float m = r.m[p * 64 + i];
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) gc[ch] = __fmaf_rn(m, gs[warp][ch][p], gc[ch]);
+    }
+    const float* c = r.coef + b * 192;
+    CoefState st;
+    refine_coef(r, i, s, xf, bf, c[i], c[64 + i], c[128 + i], true, &st);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) acc = __fmaf_rn(gc[ch], st.dhat[ch], acc);
+    acc = __fmaf_rn(rate_weight, st.dbits, acc);
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
+  if (lane == 0) gtheta[b] = __fmul_rn(acc, s);  // ds / dtheta = s
+}
+
+// The refined field: qf * exp(theta), rounded, 1..255.
+__global__ void __launch_bounds__(256) k_refine_field(const uint8_t* __restrict__ qf, const float* __restrict__ theta,
+                                                      int64_t nb, uint8_t* __restrict__ out) {
+  const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const float v = __fmul_rn(static_cast<float>(qf[b]), expf(theta[b]));
+  out[b] = static_cast<uint8_t>(fminf(fmaxf(rintf(v), 1.0f), 255.0f));
+}
+
+// One Adam step on theta (beta 0.9 / 0.999, eps 1e-8; c1, c2 the bias
+// corrections), clamped so that qf * exp(theta) stays within 1..255.
+constexpr double kAdamBeta1 = 0.9, kAdamBeta2 = 0.999;
+__global__ void __launch_bounds__(256) k_refine_adam(const uint8_t* __restrict__ qf, const float* __restrict__ g,
+                                                     int64_t nb, float lr, float c1, float c2,
+                                                     float* __restrict__ mv, float* __restrict__ theta) {
+  const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const float gv = g[b];
+  const float m = __fmaf_rn(0.9f, mv[b], 0.1f * gv);
+  const float v = __fmaf_rn(0.999f, mv[nb + b], 0.001f * gv * gv);
+  mv[b] = m;
+  mv[nb + b] = v;
+  const float q = static_cast<float>(qf[b]);
+  const float t = theta[b] - lr * (m * c1) / (sqrtf(v * c2) + 1e-8f);
+  theta[b] = fminf(fmaxf(t, logf(1.0f / q)), logf(255.0f / q));
+}
+
+}  // namespace jxg

@@ -1,0 +1,289 @@
+"""Quant-field refinement: the forward model, its hand-written adjoint and the
+optimiser, against an FP64 PyTorch restatement of the same model.
+
+The library has no counterpart in the reference (which computes no
+gradients); what can be pinned is (1) the model's levels at theta = 0 are the
+front end's own levels, bit for bit; (2) its loss and its gradient match an
+FP64 autograd model of the same straight-through quantiser (levels frozen to
+the kernel's, so both sides round alike); (3) that FP64 model's gradient is
+the derivative of the frozen-offset surrogate, checked by central
+differences; (4) Adam steps lower the true (rounded) loss; (5) a pass with a
+caller's field equals the plain pass when the field is the adaptive one.
+"""
+import numpy as np
+import pytest
+
+import jixel_gb300 as J
+from jixel_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+OPSIN_INVERSE = np.array([[11.031567, -9.866944, -0.16462299],
+                          [-3.2541473, 4.4187703, -0.16462299],
+                          [-3.6588514, 2.712923, 1.9459282]])
+OPSIN_BIAS, NEG_BIAS_CBRT = 0.0037930734, -0.1559542
+BIAS_ONE = np.array([1.0 - 0.05465007330715401, 1.0 - 0.07005449891748593, 1.0 - 0.049935103337343655])
+C1, C2 = 1e-4, 9e-4
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = J.FrontendContext(0)
+    yield c
+    c.close()
+
+
+def ultrafast(d):
+    return J.EncodeConfig(distance=d, speed=J.Speed.ULTRA_FAST)
+
+
+class Fp64Model:
+    """The refinement model in FP64 with levels frozen at `q0` (the kernel's
+    levels at theta0): quantiser inputs u become q0 + (u - u(theta0)), so the
+    value at theta0 is the rounded model and the derivative is the
+    straight-through one."""
+
+    def __init__(self, ctx, res, w, h):
+        m = ctx.refine_model()
+        xb, yb = ctx._refine_blocks
+        self.w, self.h, self.xb, self.yb = w, h, xb, yb
+        d = torch.float64
+        self.scale = m["scale"]
+        self.qm = torch.tensor(m["qm_mul"], dtype=d)
+        self.mat = torch.tensor(m["matrix"], dtype=d)
+        self.inv = torch.tensor(m["inv_matrix"], dtype=d)
+        self.coef = torch.tensor(m["coef"], dtype=d)
+        self.M = torch.tensor(m["inverse"], dtype=d)
+        thr = m["thresholds"]
+        z = np.zeros((3, 64))
+        for i in range(64):  # the zero region's edge per coefficient
+            t = thr[:, (2 if i >> 3 >= 4 else 0) + (1 if i & 7 >= 4 else 0)]
+            z[:, i] = np.maximum(t, 0.5)
+        self.zero_edge = torch.tensor(z, dtype=d)
+        self.qf = torch.tensor(res.quant_field.reshape(-1).astype(np.float64))
+        by, bx = np.divmod(np.arange(xb * yb), xb)
+        tiles = (by >> 3, bx >> 3)
+        self.xf = torch.tensor(res.ytox[tiles].astype(np.float64) / 84.0)
+        self.bf = torch.tensor(1.0 + res.ytob[tiles].astype(np.float64) / 84.0)
+        self.src = [self._linear(torch.tensor(res.xyb.astype(np.float64)))]
+        for _ in range(2):
+            self.src.append(self._down(self.src[-1]))
+
+    @staticmethod
+    def _linear(xyb):
+        x, y, b = xyb[0], xyb[1], xyb[2]
+        t = torch.stack([y + x, y - x, b])
+        m = (t - NEG_BIAS_CBRT) ** 3 - OPSIN_BIAS
+        return torch.einsum("jk,khw->jhw", torch.tensor(OPSIN_INVERSE), m)
+
+    @staticmethod
+    def _down(p):
+        h2, w2 = p.shape[1] // 2, p.shape[2] // 2
+        q = p[:, : 2 * h2, : 2 * w2]
+        return 0.25 * (q[:, 0::2, 0::2] + q[:, 0::2, 1::2] + q[:, 1::2, 0::2] + q[:, 1::2, 1::2])
+
+    @staticmethod
+    def _blur(p):
+        k = torch.tensor([1.0, 4.0, 6.0, 4.0, 1.0], dtype=p.dtype) / 16.0
+        c = p.shape[0]
+        x = torch.nn.functional.conv2d(p[None], k.view(1, 1, 1, 5).repeat(c, 1, 1, 1), padding=(0, 2),
+                                       groups=c)
+        x = torch.nn.functional.conv2d(x, k.view(1, 1, 5, 1).repeat(c, 1, 1, 1), padding=(2, 0), groups=c)
+        return x[0]
+
+    def _ssim_loss(self, a, b):
+        m1, m2 = self._blur(a), self._blur(b)
+        s11, s22, s12 = self._blur(a * a), self._blur(b * b), self._blur(a * b)
+        v1, v2, c12 = s11 - m1 * m1, s22 - m2 * m2, s12 - m1 * m2
+        ssim = (2 * m1 * m2 + C1) * (2 * c12 + C2) / ((m1 * m1 + m2 * m2 + C1) * (v1 + v2 + C2))
+        return (1.0 - ssim).mean()
+
+    def _inputs(self, s, q0, offset):
+        """The three quantiser inputs at s: Y, then X and B after CfL from the
+        dequantised Y (at the frozen levels, or at q0 itself for offset None)."""
+        uy = self.inv[1] * (s * self.qm[1])[:, None] * self.coef[:, 1]
+        yst = q0[:, 1] if offset is None else uy + offset[1]
+        yh = self._bias(1, q0[:, 1], yst) * self.mat[1] / s[:, None]
+        u = {1: uy}
+        for c, f in ((0, self.xf), (2, self.bf)):
+            v = self.coef[:, c] - f[:, None] * yh
+            u[c] = self.inv[c] * (s * self.qm[c])[:, None] * v
+        return u, yh
+
+    def loss(self, theta, theta0, q0, lam):
+        """(loss, distortion, bits) at theta with levels frozen at theta0."""
+        q0 = torch.tensor(q0, dtype=torch.float64)  # (nb, 3, 64)
+        nz = q0 != 0
+        with torch.no_grad():
+            u0, _ = self._inputs(self.scale * self.qf * torch.exp(theta0), q0, None)
+        offset = {c: q0[:, c] - u0[c] for c in range(3)}
+        s = self.scale * self.qf * torch.exp(theta)
+        u, yh = self._inputs(s, q0, offset)
+        chat = []
+        bits = torch.zeros((), dtype=torch.float64)
+        for c in range(3):
+            ust = u[c] + offset[c]
+            if c == 1:
+                hat = yh
+            else:
+                f = self.xf if c == 0 else self.bf
+                hat = self._bias(c, q0[:, c], ust) * self.mat[c] / (s * self.qm[c])[:, None] + f[:, None] * yh
+            hat = torch.cat([self.coef[:, c, :1], hat[:, 1:]], dim=1)  # the DC slot keeps the source
+            chat.append(hat)
+            a = torch.where(nz[:, c], ust.abs(), torch.zeros_like(ust))
+            zero = 2.6 * (u[c].abs() / self.zero_edge[c]) ** 4  # a zero level: its unrounded input
+            term = torch.where(nz[:, c], 1.6 + torch.log2(1.0 + a), zero)
+            bits = bits + term[:, 1:].sum()
+        chat = torch.stack(chat, dim=1)  # (nb, 3, 64)
+        rec = [self._linear(self.planes(chat))]
+        for _ in range(2):
+            rec.append(self._down(rec[-1]))
+        dist = sum(self._ssim_loss(a, b) for a, b in zip(self.src, rec)) / 3.0
+        return dist + lam * bits / (self.w * self.h), dist, bits
+
+    def planes(self, chat):
+        """The w x h XYB planes of (nb, 3, 64) coefficients through M."""
+        pix = chat @ self.M.T  # (nb, 3, 64), pixel p = row * 8 + col
+        planes = pix.view(self.yb, self.xb, 3, 8, 8).permute(2, 0, 3, 1, 4).reshape(3, self.yb * 8, self.xb * 8)
+        return planes[:, : self.h, : self.w]
+
+    @staticmethod
+    def _bias(c, q, ust):
+        one = torch.sign(q) * BIAS_ONE[c]
+        safe = torch.where(q.abs() >= 2, ust, torch.ones_like(ust))
+        big = safe - 0.145 / safe
+        return torch.where(q == 0, torch.zeros_like(ust), torch.where(q.abs() == 1, one, big))
+
+
+def begin(ctx, w, h, seed, d=1.0):
+    img = synthetic.generate(w, h, seed)
+    res = ctx.frontend(img, ultrafast(d), xyb=True)
+    xb, yb = ctx.refine_begin()
+    assert (xb, yb) == ((w + 7) // 8, (h + 7) // 8)
+    return img, res
+
+
+@pytest.mark.parametrize("w,h,seed,d", [(70, 54, 11, 1.0), (256, 192, 12, 2.0), (33, 17, 13, 0.5)])
+def test_levels_at_zero_are_the_front_ends(ctx, w, h, seed, d):
+    img, res = begin(ctx, w, h, seed, d)
+    nb = res.quant_field.size
+    theta = torch.zeros(nb, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()  # the library runs on its own stream
+    _, lv = ctx.refine_eval(0.0, theta.data_ptr(), levels=True)
+    got = lv.reshape(res.coefficients.shape)  # both in raw order
+    want = res.coefficients.copy()
+    got[..., 0] = want[..., 0] = 0  # the DC slot is not modelled
+    bad = np.argwhere(got != want)
+    assert bad.size == 0, (f"{len(bad)} levels differ (per channel {np.bincount(bad[:, 2], minlength=3)}, "
+                           f"{np.count_nonzero(want)} non-zero), first {bad[:4].tolist()}, "
+                           f"got {got[tuple(bad[0][:3])][:8]} want {want[tuple(bad[0][:3])][:8]}")
+
+
+@pytest.mark.parametrize("w,h,seed", [(70, 54, 14), (256, 192, 15)])
+def test_inverse_reproduces_the_source(ctx, w, h, seed):
+    # the source coefficients through the model's inverse transform give the
+    # pass's XYB planes back: coefficient layout, transform and crop agree
+    img, res = begin(ctx, w, h, seed)
+    model = Fp64Model(ctx, res, w, h)
+    back = model.planes(model.coef).numpy()
+    err = np.abs(back - res.xyb).max()
+    assert err <= 1e-5 * max(1.0, np.abs(res.xyb).max()), err
+
+
+def fp64_check(ctx, w, h, seed, lam, spread):
+    img, res = begin(ctx, w, h, seed)
+    nb = res.quant_field.size
+    rng = np.random.default_rng(seed)
+    th = rng.normal(0.0, spread, nb).astype(np.float32)
+    theta = torch.tensor(th, device="cuda")
+    grad = torch.zeros(nb, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    (loss, dist, bits), lv = ctx.refine_eval(lam, theta.data_ptr(), grad.data_ptr(), levels=True)
+    g_gpu = grad.cpu().numpy().astype(np.float64)
+    model = Fp64Model(ctx, res, w, h)
+    t64 = torch.tensor(th.astype(np.float64), requires_grad=True)
+    l64, d64, b64 = model.loss(t64, t64.detach().clone(), lv, lam)
+    l64.backward()
+    g_ref = t64.grad.numpy()
+    # FP32 sums over every pixel against FP64: relative 1e-4 on the loss terms
+    assert abs(bits - b64.item()) <= 1e-4 * max(b64.item(), 1.0), (bits, b64.item())
+    assert abs(dist - d64.item()) <= 1e-4 * max(d64.item(), 1e-3), (dist, d64.item())
+    assert abs(loss - l64.item()) <= 1e-4 * max(l64.item(), 1e-3), (loss, l64.item())
+    # the adjoint: per block, within 1e-3 of the largest gradient
+    tol = 1e-3 * np.abs(g_ref).max()
+    err = np.abs(g_gpu - g_ref)
+    assert err.max() <= tol, (err.max(), tol, int(err.argmax()))
+    return model, t64.detach(), lv, g_ref, lam
+
+
+@pytest.mark.parametrize("w,h,seed,lam,spread", [(70, 54, 21, 0.002, 0.3), (200, 136, 22, 0.01, 0.1)])
+def test_loss_and_gradient_match_fp64(ctx, w, h, seed, lam, spread):
+    fp64_check(ctx, w, h, seed, lam, spread)
+
+
+def test_fp64_gradient_is_the_surrogates_derivative(ctx):
+    # central differences of the frozen-offset surrogate on 64 random blocks
+    model, th, lv, g_ref, lam = fp64_check(ctx, 72, 68, 31, 0.002, 0.3)
+    step = 1e-5
+    for b in np.random.default_rng(31).choice(th.numel(), 64, replace=False):
+        e = torch.zeros_like(th)
+        e[b] = step
+        hi = model.loss(th + e, th, lv, lam)[0].item()
+        lo = model.loss(th - e, th, lv, lam)[0].item()
+        fd = (hi - lo) / (2 * step)
+        assert abs(fd - g_ref[b]) <= 1e-6 + 1e-4 * abs(g_ref[b]), (b, fd, g_ref[b])
+
+
+def test_adam_steps_lower_the_rounded_loss(ctx):
+    img, res = begin(ctx, 256, 192, 41, 1.0)
+    field, history, final = ctx.refine(steps=8, rate_lambda=0.002, learning_rate=0.05)
+    assert final[0] < history[0][0], (history[0], final)
+    theta = ctx.refine_theta()
+    q = res.quant_field.astype(np.float64)
+    v = q * np.exp(theta.astype(np.float64))
+    assert np.all(v >= 1.0 - 1e-3) and np.all(v <= 255.0 + 1e-3)
+    want = np.clip(np.rint(res.quant_field.astype(np.float32) * np.exp(theta)), 1, 255)
+    assert np.abs(field.astype(np.int32) - want.astype(np.int32)).max() <= 1  # expf vs numpy exp
+    # setting theta back to zero restores the starting loss
+    ctx.refine_theta(np.zeros_like(theta))
+    again, _ = ctx.refine_eval(0.002)
+    assert again == history[0]
+
+
+def test_pass_with_the_adaptive_field_is_the_plain_pass(ctx):
+    img = synthetic.generate(300, 200, 51)
+    plain = ctx.frontend(img, ultrafast(1.0))
+    got = ctx.frontend_with_field(img, ultrafast(1.0), plain.quant_field)
+    for k in ("quant_field", "ytox", "ytob", "quant_dc", "coefficients", "num_nzeros", "tokens",
+              "group_offsets", "histograms"):
+        assert np.array_equal(getattr(got, k), getattr(plain, k)), k
+    assert got.params == plain.params
+
+
+def test_pass_with_a_refined_field(ctx):
+    img, res = begin(ctx, 256, 192, 61, 1.0)
+    field, _, _ = ctx.refine(steps=4)
+    got = ctx.frontend_with_field(img, ultrafast(1.0), field)
+    assert np.array_equal(got.quant_field, field)
+    # the refined field was taken from a copy: refinement state survives the pass
+    again = ctx.refine_field()
+    assert np.array_equal(again, field)
+
+
+def test_refinement_errors(ctx):
+    img = synthetic.generate(64, 64, 71)
+    with pytest.raises(J.EncodeError):
+        ctx.frontend_with_field(img, J.EncodeConfig(distance=2.0, speed=J.Speed.FASTEST),
+                                np.ones((8, 8), np.uint8))
+    with pytest.raises(J.EncodeError):
+        ctx.frontend_with_field(img, ultrafast(1.0), np.ones((4, 4), np.uint8))
+    fresh = J.FrontendContext(0)
+    try:
+        with pytest.raises(J.EncodeError):
+            fresh.refine_begin()
+        ctx.frontend(img, J.EncodeConfig(distance=3.0, speed=J.Speed.FASTEST))
+        with pytest.raises(J.EncodeError):
+            ctx.refine_begin()  # a searched frame is not all DCT8
+    finally:
+        fresh.close()
