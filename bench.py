@@ -64,6 +64,8 @@ def parse_args():
     p.add_argument("--no-refine", action="store_true",
                    help="skip the quant-field refinement timing")
     p.add_argument("--refine-steps", type=int, default=8)
+    p.add_argument("--refine-only", action="store_true",
+                   help="only run the refinement record on one context and print it (a profiler target)")
     p.add_argument("--frames", type=int, default=0,
                    help="only run this many frames of the headline workload on one context, "
                         "untimed, and exit (the target of a profiler capture)")
@@ -446,7 +448,7 @@ def run_gpu(args):
 
     refine = None
     if not args.no_refine:
-        refine = run_refine(ctx, streams[0], d_img, args, dev)
+        refine = run_refine(ctx, streams[0], args, dev)
 
     # end to end through the public C ABI with pinned host buffers
     e2e = None
@@ -521,22 +523,29 @@ def run_ultrafast(ctxs, streams, flush, d_img, args, dev) -> dict:
             "unit": "MP/s", "ms_per_step": total / args.steps}
 
 
-def run_refine(ctx, stream, d_img, args, dev) -> dict:
-    """Quant-field refinement of the headline frame's UltraFast pass at q90:
-    `--refine-steps` Adam steps (loss, gradient by the adjoint kernels, update)
-    after one untimed step; CUDA events on the context's stream around the
-    steps, each of which reads its loss back to the host."""
+def run_refine(ctx, stream, args, dev) -> dict:
+    """Quant-field refinement of one 1920x1080 RGB8 frame (the 3840x2160
+    generator, seed 4: 240 x 135 blocks) after its UltraFast pass at q90:
+    `--refine-steps` Adam steps (loss, gradient by the adjoint kernels,
+    update) after one untimed step, CUDA events on the context's stream
+    around the steps, each of which reads its loss back to the host.  Then
+    the refined field is rounded and coded: the model's distortion at that
+    field and the pass's AC bits (`ac_bits_estimate`) against the adaptive
+    field's."""
     import torch
 
     import jixel_gb300 as J
+    from jixel_gb300 import synthetic
 
+    img = synthetic.config4_image()
+    h, w = img.shape[:2]
     cfg = J.EncodeConfig(speed=J.Speed.ULTRA_FAST).with_quality(90)
     lr = 0.05
-    ctx.run_device(d_img.data_ptr(), WIDTH, HEIGHT, 3, 8, cfg)
+    base = ctx.frontend(img, cfg, coefficients=False)
     xb, yb = ctx.refine_begin()
-    # lambda at the pass's own rate-distortion slope: the steps move bits
-    # between blocks rather than changing the frame's overall rate
-    lam = ctx.refine_rate_slope(WIDTH * HEIGHT)
+    # lambda at the pass's own rate-distortion slope: the steps trade bits
+    # between blocks at the exchange rate the frame already has
+    lam = ctx.refine_rate_slope(w * h)
     first = ctx.refine_step(lam, lr)
     ctx.refine_theta(np.zeros((yb, xb), np.float32))  # restart from theta = 0
     torch.cuda.synchronize(dev)
@@ -555,13 +564,14 @@ def run_refine(ctx, stream, d_img, args, dev) -> dict:
     # source coefficients and writes the decoded XYB and linear planes (2304 B
     # per block), the backward reads coefficients, decoded XYB and the two
     # finest gradients (2496 B per block)
+    theta = ctx.refine_theta()
     ctx.enable_kernel_timing(True)
     ctx.reset_kernel_times()
     ctx.refine_step(lam, lr)
     kt = {k: v for k, v in ctx.kernel_times().items() if k.startswith("k_refine")}
     ctx.enable_kernel_timing(False)
     nb = xb * yb
-    px = [WIDTH * HEIGHT, (WIDTH // 2) * (HEIGHT // 2), (WIDTH // 4) * (HEIGHT // 4)]
+    px = [w * h, (w // 2) * (h // 2), (w // 4) * (h // 4)]
     algo = {"k_refine_forward": 2304.0 * nb, "k_refine_backward": 2496.0 * nb,
             "k_refine_ssim": 36.0 * sum(px)}
     kernels = {}
@@ -569,13 +579,57 @@ def run_refine(ctx, stream, d_img, args, dev) -> dict:
         kernels[k] = {"ms": v[0], "launches": v[1]}
         if k in algo:
             kernels[k]["algorithmic_gbs"] = algo[k] / (v[0] / 1000.0) / 1e9
-    return {"workload": f"{WIDTH}x{HEIGHT} RGB8 q90 UltraFast pass, {xb * yb} blocks, Adam lr {lr}, "
+    # the refined field as coded: the model at theta = log(field / qf), and
+    # the pass over that field
+    ctx.refine_theta(theta)
+    field = ctx.refine_field()
+    qf = base.quant_field.astype(np.float64)
+    def at_field(f):
+        ctx.refine_theta(np.log(f.astype(np.float64) / qf).astype(np.float32))
+        return ctx.refine_eval(lam)[0]
+
+    coded = at_field(field)
+    # the same model distortion from a uniform change of the adaptive field
+    # (bisection on one log scale; a larger field quantises finer), for an
+    # equal-distortion rate comparison
+    def uniform(c):
+        return np.clip(np.rint(qf * np.exp(c)), 1, 255).astype(np.uint8)
+
+    lo, hi = -1.0, 1.0
+    for _ in range(20):
+        mid = 0.5 * (lo + hi)
+        if at_field(uniform(mid))[1] < coded[1]:
+            hi = mid
+        else:
+            lo = mid
+    # integer fields move in steps: code the two uniform fields that bracket
+    # the refined distortion and interpolate their rate at it
+    brackets = []
+    for c in (lo, hi):
+        f = uniform(c)
+        d = at_field(f)[1]
+        brackets.append((c, d, J.ac_bits_estimate(ctx.frontend_with_field(img, cfg, f, coefficients=False))))
+    (c_lo, d_lo, b_lo), (c_hi, d_hi, b_hi) = brackets
+    t = 0.0 if d_lo == d_hi else (coded[1] - d_hi) / (d_lo - d_hi)
+    bits2 = b_hi + t * (b_lo - b_hi)
+    refined = ctx.frontend_with_field(img, cfg, field, coefficients=False)
+    bits0, bits1 = J.ac_bits_estimate(base), J.ac_bits_estimate(refined)
+    return {"workload": f"{w}x{h} RGB8 (seed 4) q90 UltraFast pass, {nb} blocks, Adam lr {lr}, "
                         f"lambda {lam:.4g} (the pass's rate-distortion slope), SSIM at 3 scales + rate model",
             "steps": args.refine_steps, "ms_per_step": ms, "wall_ms_per_step": 1000.0 * wall / args.refine_steps,
-            "megapixels_per_s": WIDTH * HEIGHT / 1e6 / (ms / 1000.0),
+            "megapixels_per_s": w * h / 1e6 / (ms / 1000.0),
             "loss_first": hist[0][0], "loss_final": final[0], "distortion_first": hist[0][1],
-            "distortion_final": final[1], "bits_first": hist[0][2], "bits_final": final[2],
-            "untimed_first_step_loss": first[0], "kernels": kernels}
+            "distortion_final": final[1], "model_bits_first": hist[0][2], "model_bits_final": final[2],
+            "untimed_first_step_loss": first[0],
+            "coded": {"distortion_adaptive_field": hist[0][1], "distortion_refined_field": coded[1],
+                      "ac_bpp_adaptive_field": bits0 / (w * h), "ac_bpp_refined_field": bits1 / (w * h),
+                      "uniform_scale_same_distortion": {
+                          "brackets": [{"log_scale": c, "distortion": d, "ac_bpp": b / (w * h)}
+                                       for c, d, b in brackets],
+                          "ac_bpp_interpolated": bits2 / (w * h)},
+                      "refined_over_uniform_bits": bits1 / bits2,
+                      "ac_bits_estimate": "per-context symbol entropy + raw bits of the tokens"},
+            "kernels": kernels}
 
 
 def run_c5(ctxs, streams, flush, args, dev) -> dict:
@@ -797,6 +851,16 @@ def main():
         run_reference(args)
     elif args.frames:
         run_frames(args)
+    elif args.refine_only:
+        import torch
+
+        import jixel_gb300 as J
+        stream = torch.cuda.Stream()
+        torch.cuda.set_stream(stream)
+        ctx = J.FrontendContext(0)
+        ctx.set_stream(stream.cuda_stream)
+        print(json.dumps({"refine": run_refine(ctx, stream, args, torch.device("cuda", 0))}), flush=True)
+        ctx.close()
     else:
         run_gpu(args)
 

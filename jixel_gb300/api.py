@@ -174,6 +174,23 @@ class FrontendResult:
     packed_offsets: np.ndarray | None = None  # (groups + 1,) u64 word offsets
 
 
+def ac_bits_estimate(result: "FrontendResult") -> float:
+    """AC bits of a pass as an ideal coder would spend them on its tokens: the
+    per-context symbol entropy of the histograms plus each token's raw bits
+    (values >= 16 carry floor(log2 v) - 2 of them under the 4-2-0 hybrid
+    split).  Context clustering and the headers are not counted, so this is a
+    rate to compare passes by, not a file size."""
+    h = result.histograms.astype(np.float64)
+    tot = h.sum(axis=1, keepdims=True)
+    p = np.divide(h, tot, out=np.ones_like(h), where=h > 0)
+    bits = float(-(h * np.log2(p)).sum())
+    if result.tokens is not None and len(result.tokens):
+        v = result.tokens[:, 1].astype(np.int64)
+        big = v[v >= 16]
+        bits += float((np.floor(np.log2(big)) - 2).sum())
+    return bits
+
+
 def _as_hwc(pixels: np.ndarray) -> np.ndarray:
     """(h, w) grey samples as (h, w, 1); other shapes unchanged."""
     pixels = np.ascontiguousarray(pixels)

@@ -211,12 +211,15 @@ __device__ __forceinline__ void xyb_to_linear(float x, float y, float b, float* 
                        __fmaf_rn(kOpsinInverse[j * 3 + 1], m[1], __fmul_rn(kOpsinInverse[j * 3 + 2], m[2])));
 }
 
-__device__ __forceinline__ void refine_add_slot(double v, double* sums) {
+// A CTA's sum of one quantity into its slot: each thread's partial (a few
+// terms) and the warp's tree in FP32, the warps' sums and the slot in FP64
+// (GB300's FP64 pipe is narrow: no per-term FP64 work).
+__device__ __forceinline__ void refine_add_slot(float v, double* sums) {
   __shared__ double part[8];
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
   const int nw = blockDim.x >> 5;
-  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = static_cast<double>(v);
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
@@ -280,7 +283,7 @@ __global__ void __launch_bounds__(256) k_refine_forward(const RefineArgs r, cons
       }
     }
   }
-  refine_add_slot(static_cast<double>(bits), bit_sums);
+  refine_add_slot(bits, bit_sums);
 }
 
 // Linear RGB of the w x h region of XYB planes with row stride `in_stride`.
@@ -368,89 +371,137 @@ __global__ void __launch_bounds__(256) k_refine_ssim(const float* __restrict__ a
     in[1][r][c] = inside ? B[at] : 0.0f;
   }
   __syncthreads();
-  // 1. row blur of the five moments at columns -2 .. kSsimTW + 2
-  for (int u = tid; u < kSsimInH * kSsimRingW; u += 256) {
-    const int r = u / kSsimRingW, c = u % kSsimRingW;
-    float m[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  // Each blur below gives a thread a run of neighbouring outputs along the
+  // blur's direction, so one window of loads in registers serves the run.
+  // 1. row blur of the five moments at columns -2 .. kSsimTW + 2: runs of 3
+  //    columns (12 runs a row)
+  constexpr int kRun1 = 3, kRuns1 = kSsimRingW / kRun1;
+  static_assert(kSsimRingW % kRun1 == 0, "row runs tile the ring");
+  for (int u = tid; u < kSsimInH * kRuns1; u += 256) {
+    const int r = u / kRuns1, c0 = (u % kRuns1) * kRun1;
+    float va[kRun1 + 4], vb[kRun1 + 4];
 #pragma unroll
-    for (int d = -2; d <= 2; ++d) {
-      const float k = blur_tap(d), va = in[0][r][c + 2 + d], vb = in[1][r][c + 2 + d];
-      m[0] = __fmaf_rn(k, va, m[0]);
-      m[1] = __fmaf_rn(k, vb, m[1]);
-      m[2] = __fmaf_rn(k, __fmul_rn(va, va), m[2]);
-      m[3] = __fmaf_rn(k, __fmul_rn(vb, vb), m[3]);
-      m[4] = __fmaf_rn(k, __fmul_rn(va, vb), m[4]);
+    for (int k = 0; k < kRun1 + 4; ++k) {
+      va[k] = in[0][r][c0 + k];
+      vb[k] = in[1][r][c0 + k];
     }
 #pragma unroll
-    for (int q = 0; q < 5; ++q) xm[q][r][c] = m[q];
+    for (int j = 0; j < kRun1; ++j) {
+      float m[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int d = -2; d <= 2; ++d) {
+        const float k = blur_tap(d), a = va[j + 2 + d], b = vb[j + 2 + d];
+        m[0] = __fmaf_rn(k, a, m[0]);
+        m[1] = __fmaf_rn(k, b, m[1]);
+        m[2] = __fmaf_rn(k, __fmul_rn(a, a), m[2]);
+        m[3] = __fmaf_rn(k, __fmul_rn(b, b), m[3]);
+        m[4] = __fmaf_rn(k, __fmul_rn(a, b), m[4]);
+      }
+#pragma unroll
+      for (int q = 0; q < 5; ++q) xm[q][r][c0 + j] = m[q];
+    }
   }
   __syncthreads();
-  // 2. column blur, SSIM and its derivatives on the tile and a 2-pixel ring
-  double loss = 0.0;
-  for (int u = tid; u < kSsimRingH * kSsimRingW; u += 256) {
-    const int r = u / kSsimRingW, c = u % kSsimRingW;
-    const int y = y0 - 2 + r, x = x0 - 2 + c;
-    float m[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  // 2. column blur, SSIM and its derivatives on the tile and a 2-pixel ring:
+  //    runs of 3 rows (7 runs a column, the last one short)
+  constexpr int kRun2 = 3, kRuns2 = (kSsimRingH + kRun2 - 1) / kRun2;
+  static_assert(kRuns2 * kSsimRingW <= 256, "one run per thread");
+  float loss = 0.0f;
+  if (tid < kRuns2 * kSsimRingW) {
+    const int c = tid % kSsimRingW, r0 = (tid / kSsimRingW) * kRun2;
+    float win[5][kRun2 + 4];
 #pragma unroll
-    for (int d = -2; d <= 2; ++d) {
-      const float k = blur_tap(d);
+    for (int k = 0; k < kRun2 + 4; ++k)
 #pragma unroll
-      for (int q = 0; q < 5; ++q) m[q] = __fmaf_rn(k, xm[q][r + 2 + d][c], m[q]);
+      for (int q = 0; q < 5; ++q) win[q][k] = r0 + k < kSsimInH ? xm[q][r0 + k][c] : 0.0f;
+#pragma unroll
+    for (int j = 0; j < kRun2; ++j) {
+      const int r = r0 + j;
+      if (r >= kSsimRingH) break;
+      const int y = y0 - 2 + r, x = x0 - 2 + c;
+      float m[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int d = -2; d <= 2; ++d) {
+        const float k = blur_tap(d);
+#pragma unroll
+        for (int q = 0; q < 5; ++q) m[q] = __fmaf_rn(k, win[q][j + 2 + d], m[q]);
+      }
+      float gm2 = 0.0f, gs22 = 0.0f, gs12 = 0.0f;
+      if (x >= 0 && x < w && y >= 0 && y < h) {
+        const float m1 = m[0], m2 = m[1];
+        const float v1 = __fsub_rn(m[2], __fmul_rn(m1, m1)), v2 = __fsub_rn(m[3], __fmul_rn(m2, m2));
+        const float c12 = __fsub_rn(m[4], __fmul_rn(m1, m2));
+        const float n1 = __fadd_rn(__fmul_rn(2.0f, __fmul_rn(m1, m2)), kSsimC1);
+        const float n2 = __fadd_rn(__fmul_rn(2.0f, c12), kSsimC2);
+        const float d1 = __fadd_rn(__fadd_rn(__fmul_rn(m1, m1), __fmul_rn(m2, m2)), kSsimC1);
+        const float d2 = __fadd_rn(__fadd_rn(v1, v2), kSsimC2);
+        // one division: 1 / (d1 d2), and 1 / d2 = d1 / (d1 d2)
+        const float inv_dd = __fdiv_rn(1.0f, __fmul_rn(d1, d2));
+        const float ssim = __fmul_rn(__fmul_rn(n1, n2), inv_dd);
+        if (r >= 2 && r < 2 + kSsimTH && c >= 2 && c < 2 + kSsimTW) loss += 1.0f - ssim;
+        // d ssim / d m2, d s22, d s12 (the source's moments fixed)
+        const float dm2 = __fmul_rn(__fsub_rn(__fmul_rn(__fmul_rn(2.0f, m1), __fsub_rn(n2, n1)),
+                                              __fmul_rn(ssim, __fmul_rn(__fmul_rn(2.0f, m2), __fsub_rn(d2, d1)))),
+                                    inv_dd);
+        gm2 = -weight * dm2;
+        gs22 = weight * __fmul_rn(ssim, __fmul_rn(d1, inv_dd));
+        gs12 = -weight * __fmul_rn(__fmul_rn(2.0f, n1), inv_dd);
+      }
+      g[0][r][c] = gm2;
+      g[1][r][c] = gs22;
+      g[2][r][c] = gs12;
     }
-    float gm2 = 0.0f, gs22 = 0.0f, gs12 = 0.0f;
-    if (x >= 0 && x < w && y >= 0 && y < h) {
-      const float m1 = m[0], m2 = m[1];
-      const float v1 = __fsub_rn(m[2], __fmul_rn(m1, m1)), v2 = __fsub_rn(m[3], __fmul_rn(m2, m2));
-      const float c12 = __fsub_rn(m[4], __fmul_rn(m1, m2));
-      const float n1 = __fadd_rn(__fmul_rn(2.0f, __fmul_rn(m1, m2)), kSsimC1);
-      const float n2 = __fadd_rn(__fmul_rn(2.0f, c12), kSsimC2);
-      const float d1 = __fadd_rn(__fadd_rn(__fmul_rn(m1, m1), __fmul_rn(m2, m2)), kSsimC1);
-      const float d2 = __fadd_rn(__fadd_rn(v1, v2), kSsimC2);
-      const float dd = __fmul_rn(d1, d2);
-      const float ssim = __fdiv_rn(__fmul_rn(n1, n2), dd);
-      if (r >= 2 && r < 2 + kSsimTH && c >= 2 && c < 2 + kSsimTW) loss += 1.0 - static_cast<double>(ssim);
-      // d ssim / d m2, d s22, d s12 (the source's moments fixed)
-      const float dm2 = __fdiv_rn(__fsub_rn(__fmul_rn(__fmul_rn(2.0f, m1), __fsub_rn(n2, n1)),
-                                            __fmul_rn(ssim, __fmul_rn(__fmul_rn(2.0f, m2), __fsub_rn(d2, d1)))),
-                                  dd);
-      gm2 = -weight * dm2;
-      gs22 = weight * __fdiv_rn(ssim, d2);
-      gs12 = -weight * __fdiv_rn(__fmul_rn(2.0f, n1), dd);
-    }
-    g[0][r][c] = gm2;
-    g[1][r][c] = gs22;
-    g[2][r][c] = gs12;
   }
   __syncthreads();
-  // 3. row blur of the derivatives (into xm, free now) at the tile's columns
-  for (int u = tid; u < kSsimRingH * kSsimTW; u += 256) {
-    const int r = u / kSsimTW, c = u % kSsimTW;
-    float v[3] = {0.0f, 0.0f, 0.0f};
+  // 3. row blur of the derivatives (into xm, free now) at the tile's
+  //    columns: runs of 4 columns
+  constexpr int kRun3 = 4, kRuns3 = kSsimTW / kRun3;
+  for (int u = tid; u < kSsimRingH * kRuns3; u += 256) {
+    const int r = u / kRuns3, c0 = (u % kRuns3) * kRun3;
+    float win[3][kRun3 + 4];
 #pragma unroll
-    for (int d = -2; d <= 2; ++d) {
-      const float k = blur_tap(d);
+    for (int k = 0; k < kRun3 + 4; ++k)
 #pragma unroll
-      for (int q = 0; q < 3; ++q) v[q] = __fmaf_rn(k, g[q][r][c + 2 + d], v[q]);
+      for (int q = 0; q < 3; ++q) win[q][k] = g[q][r][c0 + k];
+#pragma unroll
+    for (int j = 0; j < kRun3; ++j) {
+      float v[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int d = -2; d <= 2; ++d) {
+        const float k = blur_tap(d);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) v[q] = __fmaf_rn(k, win[q][j + 2 + d], v[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < 3; ++q) xm[q][r][c0 + j] = v[q];
     }
-#pragma unroll
-    for (int q = 0; q < 3; ++q) xm[q][r][c] = v[q];
   }
   __syncthreads();
-  // 4. column blur and the gradient by the decoded plane
-  for (int u = tid; u < kSsimTH * kSsimTW; u += 256) {
-    const int r = u / kSsimTW, c = u % kSsimTW;
-    const int y = y0 + r, x = x0 + c;
-    if (x >= w || y >= h) continue;
-    float v[3] = {0.0f, 0.0f, 0.0f};
+  // 4. column blur and the gradient by the decoded plane: runs of 2 rows
+  constexpr int kRun4 = 2;
+  static_assert((kSsimTH / kRun4) * kSsimTW == 256, "one run per thread");
+  {
+    const int c = tid % kSsimTW, r0 = (tid / kSsimTW) * kRun4;
+    float win[3][kRun4 + 4];
 #pragma unroll
-    for (int d = -2; d <= 2; ++d) {
-      const float k = blur_tap(d);
+    for (int k = 0; k < kRun4 + 4; ++k)
 #pragma unroll
-      for (int q = 0; q < 3; ++q) v[q] = __fmaf_rn(k, xm[q][r + 2 + d][c], v[q]);
+      for (int q = 0; q < 3; ++q) win[q][k] = xm[q][r0 + k][c];
+#pragma unroll
+    for (int j = 0; j < kRun4; ++j) {
+      const int r = r0 + j, y = y0 + r, x = x0 + c;
+      if (x >= w || y >= h) continue;
+      float v[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int d = -2; d <= 2; ++d) {
+        const float k = blur_tap(d);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) v[q] = __fmaf_rn(k, win[q][j + 2 + d], v[q]);
+      }
+      const float va = in[0][r + 4][c + 4], vb = in[1][r + 4][c + 4];
+      grad[ch * n + static_cast<int64_t>(y) * w + x] =
+          __fmaf_rn(va, v[2], __fmaf_rn(__fmul_rn(2.0f, vb), v[1], v[0]));
     }
-    const float va = in[0][r + 4][c + 4], vb = in[1][r + 4][c + 4];
-    grad[ch * n + static_cast<int64_t>(y) * w + x] =
-        __fmaf_rn(va, v[2], __fmaf_rn(__fmul_rn(2.0f, vb), v[1], v[0]));
   }
   refine_add_slot(loss, sums);
 }

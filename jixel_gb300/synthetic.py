@@ -126,6 +126,12 @@ def config2_image(width: int = 3840, height: int = 2160) -> np.ndarray:
     return generate(width, height, 2, noise_sigma=4.0, rectangles=200, texture_weight=0.3)
 
 
+def config4_image(width: int = 1920, height: int = 1080) -> np.ndarray:
+    """1920x1080 RGB8 from the 3840x2160 generator, seed 4 (the refinement
+    workload: 240 x 135 blocks)."""
+    return generate(width, height, 4, noise_sigma=4.0, rectangles=200, texture_weight=0.3)
+
+
 def config5_image(size: int = 8192) -> np.ndarray:
     """size x size RGB 16-bit linear, seed 5: 50 % 1/f^2 texture."""
     return generate(size, size, 5, sixteen_bit=True, texture_weight=0.5)
