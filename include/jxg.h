@@ -410,7 +410,8 @@ int32_t jxg_selftest_math(void* ctx, int32_t which, uint32_t lo_bits, uint32_t h
  * scale per 8x8 block: block b quantises at scale * qf_b * exp(theta_b), qf
  * the frame's adaptive field.  The model (FP32) quantises and dequantises the
  * AC coefficients exactly as the front end does (with CfL and the decoder's
- * bias), inverts the 8x8 DCT, converts XYB to linear RGB and scores 1 - SSIM
+ * bias; the DC slot holds the pass's decoded DC), inverts the 8x8 DCT,
+ * converts XYB to linear RGB and scores 1 - SSIM
  * against the source at three scales, plus a rate model (1.6 + log2(1 +
  * |level|) bits per non-zero AC level, 2.6 (|v| / max(threshold, 0.5))^4 per
  * level v that rounds to zero); rounding is straight-through in the backward
@@ -441,9 +442,11 @@ int32_t jxg_refine_theta(void* ctx, float* theta, int32_t to_context);
 int32_t jxg_refine_field(void* ctx, const float* theta, uint8_t* quant_field);
 /* The model's constants for an outside check: constants = {scale, qm_mul[3],
  * matrix[3][64], inv_matrix[3][64], thresholds[3][4]} (400 floats); the
- * source coefficients (xb*yb*192, raw order) and the 64 x 64 inverse
- * transform [pixel][coefficient] (either may be NULL), all on the host. */
-int32_t jxg_refine_model(void* ctx, float* constants, float* coefficients, float* inverse);
+ * source coefficients (xb*yb*192, raw order), the 64 x 64 inverse transform
+ * [pixel][coefficient] and the decoded DC per block (xb*yb*3: X, Y, B; the
+ * pass's DC levels dequantised, which the model's DC slot holds); any of the
+ * last three may be NULL; all on the host. */
+int32_t jxg_refine_model(void* ctx, float* constants, float* coefficients, float* inverse, float* dc);
 /* One UltraFast pass with the caller's quant field (xb*yb values 1..255, host
  * or device memory; e.g. a refined field) in place of the adaptive one; the
  * AC thresholds' median stage runs over it.  Host pixels: runs and waits, as

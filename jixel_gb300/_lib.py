@@ -178,7 +178,7 @@ def load() -> ctypes.CDLL:
         "jxg_refine_step": (i32, [vp, ctypes.c_float, ctypes.c_float, vp]),
         "jxg_refine_theta": (i32, [vp, vp, i32]),
         "jxg_refine_field": (i32, [vp, vp, vp]),
-        "jxg_refine_model": (i32, [vp, vp, vp, vp]),
+        "jxg_refine_model": (i32, [vp, vp, vp, vp, vp]),
         "jxg_frontend_run_with_field": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config), vp, i32]),
         "jxg_get_launch_geometry": (i32, [vp, vp]),
         "jxg_set_launch_geometry": (i32, [vp, vp]),

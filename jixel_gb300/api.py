@@ -539,17 +539,19 @@ class FrontendContext:
         return self.refine_field(), history, final
 
     def refine_model(self) -> dict:
-        """The model's constants, source coefficients and inverse transform."""
+        """The model's constants, source coefficients, inverse transform and
+        decoded DC."""
         xb, yb = self._refine_blocks
         nb = xb * yb
         k = np.zeros(400, np.float32)
         coef = np.zeros((nb, 3, 64), np.float32)
         inv = np.zeros((64, 64), np.float32)
+        dc = np.zeros((nb, 3), np.float32)
         self._check(self._lib.jxg_refine_model(self._ctx, k.ctypes.data, coef.ctypes.data,
-                                               inv.ctypes.data))
+                                               inv.ctypes.data, dc.ctypes.data))
         return {"scale": float(k[0]), "qm_mul": k[1:4].copy(), "matrix": k[4:196].reshape(3, 64).copy(),
                 "inv_matrix": k[196:388].reshape(3, 64).copy(), "thresholds": k[388:400].reshape(3, 4).copy(),
-                "coef": coef, "inverse": inv}
+                "coef": coef, "inverse": inv, "dc": dc}
 
     def run_with_field(self, pixels: np.ndarray, config: EncodeConfig, quant_field: np.ndarray):
         """jxg_frontend_run_with_field, host pixels and a host (yb, xb) field."""

@@ -2006,8 +2006,8 @@ int32_t jxg_refine_begin(void* ctx, uint64_t* xsize_blocks, uint64_t* ysize_bloc
   // (3 pp), M and M^T, the source and decoded linear planes and the gradient
   // per scale, the f64 sums, theta, its gradient and Adam moments, copies of
   // the field and the colour maps; each piece rounded up to 64 floats
-  const size_t floats = nb * 192 + 3 * pp + 2 * 4096 + 3 * 3 * (n + n1 + n2) + 2 * 4 * kRefineSlots + 4 * nb +
-                        (nb + 2 * tiles) / 4 + 64 * 24;
+  const size_t floats = nb * 192 + 3 * nb + 3 * pp + 2 * 4096 + 3 * 3 * (n + n1 + n2) + 2 * 4 * kRefineSlots +
+                        4 * nb + (nb + 2 * tiles) / 4 + 64 * 25;
   if ((st = ensure(c, c->refine_buf, floats * 4 + 256))) return st;
   float* base = static_cast<float*>(c->refine_buf.ptr);
   auto take = [&](int64_t count) {
@@ -2016,6 +2016,7 @@ int32_t jxg_refine_begin(void* ctx, uint64_t* xsize_blocks, uint64_t* ysize_bloc
     return p;
   };
   r.coef = take(nb * 192);
+  r.dc = take(3 * nb);
   r.recon = take(3 * pp);
   r.m = take(4096);
   r.mt = take(4096);
@@ -2061,6 +2062,10 @@ int32_t jxg_refine_begin(void* ctx, uint64_t* xsize_blocks, uint64_t* ysize_bloc
   const bool timed = c->timing;
   if ((st = launch(c, "k_refine_dct", timed, [&] {
          k_refine_dct<<<static_cast<unsigned>((nb + 7) / 8), 256, 0, s>>>(r);
+       })) ||
+      (st = launch(c, "k_refine_dc", timed, [&] {
+         k_refine_dc<<<refine_grid(nb), 256, 0, s>>>(f0.quant_dc, nb, a.inv_dc_factor[0], a.inv_dc_factor[1],
+                                                     a.inv_dc_factor[2], a.cfl_dc_factor_x, a.cfl_dc_factor_b, r.dc);
        })) ||
       (st = launch(c, "k_refine_linear", timed, [&] {
          k_refine_linear<<<refine_grid(n), 256, 0, s>>>(r.xyb, r.plane, r.w, c->refine_lin[0][0], r.w, r.h);
@@ -2212,7 +2217,7 @@ int32_t jxg_refine_theta(void* ctx, float* theta, int32_t to_context) {
   return wait(c);
 }
 
-int32_t jxg_refine_model(void* ctx, float* constants, float* coefficients, float* inverse) {
+int32_t jxg_refine_model(void* ctx, float* constants, float* coefficients, float* inverse, float* dc) {
   using namespace jxg;
   Context* c = static_cast<Context*>(ctx);
   if (!c || !constants) return JXG_ERR_INVALID_ARGUMENT;
@@ -2231,6 +2236,7 @@ int32_t jxg_refine_model(void* ctx, float* constants, float* coefficients, float
   if (coefficients)
     JXG_CUDA(c, cudaMemcpyAsync(coefficients, r.coef, nb * 192 * 4, cudaMemcpyDeviceToHost, c->stream));
   if (inverse) JXG_CUDA(c, cudaMemcpyAsync(inverse, r.m, 4096 * 4, cudaMemcpyDeviceToHost, c->stream));
+  if (dc) JXG_CUDA(c, cudaMemcpyAsync(dc, r.dc, nb * 3 * 4, cudaMemcpyDeviceToHost, c->stream));
   return wait(c);
 }
 

@@ -10,8 +10,10 @@
 //   Y AC levels at s, their dequantised values with the decoder's bias
 //   (DequantBias, src/group.rs:767); CfL on X and B from the dequantised Y; X
 //   and B levels at s; the decoder's coefficients X^ = deq(X) + xf Y^,
-//   B^ = deq(B) + bf Y^.  The DC slot keeps the source value (the DC path is
-//   not refined);
+//   B^ = deq(B) + bf Y^.  The DC slot holds the decoded DC: the pass's DC
+//   levels dequantised (quantize_dc / quantize_dc_cfl inverted,
+//   src/group.rs:286-306); theta does not move it, and the decoder's
+//   adaptive DC smoothing (src/frame/dc_smoothing.rs) is not modelled;
 //   the 8x8 inverse transform as a 64 x 64 matrix M taken from the library's
 //   own IDCT (src/dct.rs:1500-1620), so its adjoint is exactly M^T;
 //   XYB to linear RGB (xyb_to_rgb_pixel_f32, src/xyb.rs:265-283);
@@ -45,6 +47,7 @@ struct RefineArgs {
   int32_t tiles_x;
   float scale, qm_mul[3];
   float matrix[3][64], inv_matrix[3][64], thresholds[3][4];
+  float* dc;                 // [block][X, Y, B] decoded DC (the pass's DC levels dequantised)
   float* m;                  // [64 pixels][64 coefficients] inverse DCT8
   float* mt;                 // the same, [coefficient][pixel]
   float* recon;              // 3 padded planes (pw x yb * 8) of decoded XYB
@@ -254,7 +257,7 @@ __global__ void __launch_bounds__(256) k_refine_forward(const RefineArgs r, cons
       refine_coef(r, i, s, xf, bf, c[i], c[64 + i], c[128 + i], false, &st);
 #pragma unroll
       for (int ch = 0; ch < 3; ++ch) {
-        cs[warp][ch][i] = i == 0 ? c[ch * 64] : st.hat[ch];
+        cs[warp][ch][i] = i == 0 ? r.dc[b * 3 + ch] : st.hat[ch];
         if (levels) levels[b * 192 + ch * 64 + i] = i == 0 ? 0 : st.q[ch];
       }
       if (i != 0) bits = __fadd_rn(bits, st.bits);
@@ -284,6 +287,21 @@ __global__ void __launch_bounds__(256) k_refine_forward(const RefineArgs r, cons
     }
   }
   refine_add_slot(bits, bit_sums);
+}
+
+// The decoded DC of every block from the pass's DC levels (3 planes of
+// xb*yb): Y = q_Y / f_Y, X = (q_X + q_Y c_X) / f_X, B = (q_B + q_Y c_B) / f_B,
+// f the inverse DC steps and c the DC chroma-from-luma factors the levels
+// were taken with.
+__global__ void __launch_bounds__(256) k_refine_dc(const int16_t* __restrict__ quant_dc, int64_t nb,
+                                                   float fx, float fy, float fb, float cx, float cb,
+                                                   float* __restrict__ dc) {
+  const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const float qx = quant_dc[b], qy = quant_dc[nb + b], qb = quant_dc[2 * nb + b];
+  dc[b * 3 + 0] = __fdiv_rn(__fmaf_rn(qy, cx, qx), fx);
+  dc[b * 3 + 1] = __fdiv_rn(qy, fy);
+  dc[b * 3 + 2] = __fdiv_rn(__fmaf_rn(qy, cb, qb), fb);
 }
 
 // Linear RGB of the w x h region of XYB planes with row stride `in_stride`.

@@ -55,6 +55,7 @@ class Fp64Model:
         self.inv = torch.tensor(m["inv_matrix"], dtype=d)
         self.coef = torch.tensor(m["coef"], dtype=d)
         self.M = torch.tensor(m["inverse"], dtype=d)
+        self.dc = torch.tensor(m["dc"], dtype=d)  # (nb, 3) decoded DC
         thr = m["thresholds"]
         z = np.zeros((3, 64))
         for i in range(64):  # the zero region's edge per coefficient
@@ -129,7 +130,7 @@ class Fp64Model:
             else:
                 f = self.xf if c == 0 else self.bf
                 hat = self._bias(c, q0[:, c], ust) * self.mat[c] / (s * self.qm[c])[:, None] + f[:, None] * yh
-            hat = torch.cat([self.coef[:, c, :1], hat[:, 1:]], dim=1)  # the DC slot keeps the source
+            hat = torch.cat([self.dc[:, c:c + 1], hat[:, 1:]], dim=1)  # the DC slot: decoded DC
             chat.append(hat)
             a = torch.where(nz[:, c], ust.abs(), torch.zeros_like(ust))
             zero = 2.6 * (u[c].abs() / self.zero_edge[c]) ** 4  # a zero level: its unrounded input
@@ -178,6 +179,27 @@ def test_levels_at_zero_are_the_front_ends(ctx, w, h, seed, d):
     assert bad.size == 0, (f"{len(bad)} levels differ (per channel {np.bincount(bad[:, 2], minlength=3)}, "
                            f"{np.count_nonzero(want)} non-zero), first {bad[:4].tolist()}, "
                            f"got {got[tuple(bad[0][:3])][:8]} want {want[tuple(bad[0][:3])][:8]}")
+
+
+def test_decoded_dc_is_the_dequantised_dc_levels(ctx):
+    img, res = begin(ctx, 96, 72, 16)
+    m = ctx.refine_model()
+    dc = m["dc"].reshape(res.quant_field.shape + (3,))
+    q = res.quant_dc.astype(np.float64)  # (3, yb, xb): X, Y, B
+    # the DC step per channel from the Y plane's levels: decoded / level
+    nz = q[1] != 0
+    step_y = dc[..., 1][nz] / q[1][nz]
+    assert np.allclose(step_y, step_y[0], rtol=1e-6)
+    # within half a step of the source block means (the rounding of the levels)
+    src = m["coef"][:, :, 0].reshape(dc.shape)
+    assert np.all(np.abs(src[..., 1] - dc[..., 1]) <= 0.5 * abs(step_y[0]) * (1 + 1e-5))
+    # X and B: their own levels plus the luma levels' chroma-from-luma share
+    for c in (0, 2):
+        nzc = q[c] != 0
+        if nzc.any():
+            step = (dc[..., c] * 1.0)[nzc & (q[1] == 0)] / q[c][nzc & (q[1] == 0)]
+            if step.size:
+                assert np.allclose(step, step[0], rtol=1e-6)
 
 
 @pytest.mark.parametrize("w,h,seed", [(70, 54, 14), (256, 192, 15)])
