@@ -411,11 +411,13 @@ int32_t jxg_selftest_math(void* ctx, int32_t which, uint32_t lo_bits, uint32_t h
  * the frame's adaptive field.  The model (FP32) quantises and dequantises the
  * AC coefficients exactly as the front end does (with CfL and the decoder's
  * bias; the DC slot holds the pass's decoded DC), inverts the 8x8 DCT,
- * converts XYB to linear RGB and scores 1 - SSIM
+ * applies the decoder's EPF at the frame's settings (its adjoint with the
+ * weights held), converts XYB to linear RGB and scores 1 - SSIM
  * against the source at three scales, plus a rate model (1.6 + log2(1 +
  * |level|) bits per non-zero AC level, 2.6 (|v| / max(threshold, 0.5))^4 per
  * level v that rounds to zero); rounding is straight-through in the backward
- * pass.  EPF, gaborish and DC smoothing are not modelled.
+ * pass.  Gaborish (off in the reference's encoder) and DC smoothing are not
+ * modelled.
  *
  * jxg_refine_begin takes the frame of the context's last pass (one frame,
  * Speed::UltraFast), copies what the model needs (a later pass does not
@@ -441,7 +443,9 @@ int32_t jxg_refine_theta(void* ctx, float* theta, int32_t to_context);
  * exp(theta)) clamped to 1..255, xb*yb bytes into host or device memory. */
 int32_t jxg_refine_field(void* ctx, const float* theta, uint8_t* quant_field);
 /* The model's constants for an outside check: constants = {scale, qm_mul[3],
- * matrix[3][64], inv_matrix[3][64], thresholds[3][4]} (400 floats); the
+ * matrix[3][64], inv_matrix[3][64], thresholds[3][4], then the EPF's stage
+ * count, stage ids[3] (-1 unused), SAD multipliers[3], border multiplier,
+ * channel scales[3], quant_mul, sharpness / 7, quantizer scale} (414 floats); the
  * source coefficients (xb*yb*192, raw order), the 64 x 64 inverse transform
  * [pixel][coefficient] and the decoded DC per block (xb*yb*3: X, Y, B; the
  * pass's DC levels dequantised, which the model's DC slot holds); any of the

@@ -543,7 +543,7 @@ class FrontendContext:
         decoded DC."""
         xb, yb = self._refine_blocks
         nb = xb * yb
-        k = np.zeros(400, np.float32)
+        k = np.zeros(414, np.float32)
         coef = np.zeros((nb, 3, 64), np.float32)
         inv = np.zeros((64, 64), np.float32)
         dc = np.zeros((nb, 3), np.float32)
@@ -551,6 +551,9 @@ class FrontendContext:
                                                inv.ctypes.data, dc.ctypes.data))
         return {"scale": float(k[0]), "qm_mul": k[1:4].copy(), "matrix": k[4:196].reshape(3, 64).copy(),
                 "inv_matrix": k[196:388].reshape(3, 64).copy(), "thresholds": k[388:400].reshape(3, 4).copy(),
+                "epf": {"stages": [(int(k[401 + i]), float(k[404 + i])) for i in range(int(k[400]))],
+                        "border": float(k[407]), "channel_scale": k[408:411].copy(),
+                        "quant_mul": float(k[411]), "lut": float(k[412]), "quant_scale": float(k[413])},
                 "coef": coef, "inverse": inv, "dc": dc}
 
     def run_with_field(self, pixels: np.ndarray, config: EncodeConfig, quant_field: np.ndarray):

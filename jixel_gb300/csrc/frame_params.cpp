@@ -296,6 +296,31 @@ int32_t epf_sharpness_id(float d, bool screen) {
   return 4;
 }
 
+// LoopFilter::new at the encoder's defaults for XYB (src/epf_filter.rs:56-85)
+// with compute_distance_params' pass-0 scale (src/frame/quantization.rs:
+// 116-127, :200-216): a signalled bundle is read back through F16.
+void loop_filter_params(float d, LoopFilterParams* out) {
+  DistanceParams p{};
+  compute_distance_params(d, &p);
+  out->iters = p.epf_iters;
+  const float t = vlq_t(d);
+  out->channel_scale[0] = 40.0f;
+  out->channel_scale[1] = 5.0f;
+  out->channel_scale[2] = 3.5f;
+  if (d >= 2.5f && t < 0.5f) {
+    const float pass0 = fmla(2.0f * t, 0.9f - 3.6f, 3.6f);
+    out->quant_mul = half_round(0.46f);
+    out->pass0 = half_round(pass0);
+    out->pass2 = half_round(6.5f);
+    out->border = half_round(2.0f / 3.0f);
+  } else {
+    out->quant_mul = 0.46f;
+    out->pass0 = 0.9f;
+    out->pass2 = 6.5f;
+    out->border = 2.0f / 3.0f;
+  }
+}
+
 bool is_screen_content(uint64_t constant_blocks, uint64_t w, uint64_t h) {
   uint64_t bw = w / 8, bh = h / 8;
   if (bw == 0 || bh == 0) return false;

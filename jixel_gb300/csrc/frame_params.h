@@ -119,6 +119,13 @@ int dct8_tables(float distance, float matrix[3][64], float inv[3][64]);
 void fill_kernel_args(const DistanceParams& p, KernelArgs* a);
 float distance_from_quality(float quality);
 int32_t epf_sharpness_id(float distance, bool screen_content);
+// The decoder's loop-filter bundle for an XYB frame at `distance`.
+struct LoopFilterParams {
+  uint32_t iters;
+  float quant_mul, pass0, pass2, border;
+  float channel_scale[3];
+};
+void loop_filter_params(float distance, LoopFilterParams* out);
 bool is_screen_content(uint64_t constant_blocks, uint64_t width, uint64_t height);
 void srgb_to_linear_table(float out[256]);
 // TransferLut::build (src/color.rs:297-333) for integer samples of `bits`

@@ -153,6 +153,11 @@ struct Context {
   float* refine_glin[3] = {};     // the loss's gradient by the decoded planes per scale
   double* refine_sums = nullptr;  // 4 x kRefineSlots partial sums
   DevBuf refine_levels;           // levels, when a caller asks for them
+  // the EPF model: each stage's output and weights, the adjoint's ping-pong
+  float* refine_epf_out[3] = {};
+  float* refine_epf_nw[3] = {};
+  float* refine_epf_cw[3] = {};
+  float* refine_epf_g[2] = {};
   // the context's own parameters, their gradient and Adam moments
   float *refine_theta = nullptr, *refine_grad = nullptr, *refine_adam = nullptr;
   int32_t refine_steps = 0;
@@ -2002,12 +2007,46 @@ int32_t jxg_refine_begin(void* ctx, uint64_t* xsize_blocks, uint64_t* ysize_bloc
   // (3 pp), bits, M, the linear planes and gradients per scale, the moment,
   // blur and gradient maps, four f64 sums
   const int64_t tiles = static_cast<int64_t>(a.tiles_x) * a.tiles_y;
+  // the decoder's EPF at this frame's loop-filter settings
+  jxg_frame_params fp{};
+  if ((st = read_params(c, 0, &fp))) return st;
+  LoopFilterParams lfp{};
+  loop_filter_params(a.distance, &lfp);
+  r.epf_stages = 0;
+  if (fp.epf_iters > 0 && fp.epf_sharpness > 0 && r.w >= 4 && r.h >= 4) {
+    const float sad_mul = 1.65f;  // SAD_MUL, src/epf_filter.rs:45
+    if (fp.epf_iters == 1) {
+      r.epf_stages = 1;
+      r.epf_stage[0] = 1;
+      r.epf_sm[0] = sad_mul;
+    } else if (fp.epf_iters == 2) {
+      r.epf_stages = 2;
+      r.epf_stage[0] = 1;
+      r.epf_sm[0] = sad_mul;
+      r.epf_stage[1] = 2;
+      r.epf_sm[1] = sad_mul * lfp.pass2;
+    } else {
+      r.epf_stages = 3;
+      r.epf_stage[0] = 0;
+      r.epf_sm[0] = sad_mul * lfp.pass0;
+      r.epf_stage[1] = 1;
+      r.epf_sm[1] = sad_mul;
+      r.epf_stage[2] = 2;
+      r.epf_sm[2] = sad_mul * lfp.pass2;
+    }
+  }
+  r.epf_border = lfp.border;
+  std::memcpy(r.epf_channel, lfp.channel_scale, sizeof(r.epf_channel));
+  r.epf_quant_mul = lfp.quant_mul;
+  r.epf_lut = static_cast<float>(fp.epf_sharpness) / 7.0f;
+  r.epf_quant_scale = a.scale;
+  const int64_t epf_planes = r.epf_stages ? 3 * r.epf_stages + 20 + r.epf_stages + 6 : 0;
   // one allocation: source coefficients (nb x 192), the decoded XYB planes
   // (3 pp), M and M^T, the source and decoded linear planes and the gradient
   // per scale, the f64 sums, theta, its gradient and Adam moments, copies of
   // the field and the colour maps; each piece rounded up to 64 floats
   const size_t floats = nb * 192 + 3 * nb + 3 * pp + 2 * 4096 + 3 * 3 * (n + n1 + n2) + 2 * 4 * kRefineSlots +
-                        4 * nb + (nb + 2 * tiles) / 4 + 64 * 25;
+                        4 * nb + (nb + 2 * tiles) / 4 + nb + epf_planes * n + 64 * 60;
   if ((st = ensure(c, c->refine_buf, floats * 4 + 256))) return st;
   float* base = static_cast<float*>(c->refine_buf.ptr);
   auto take = [&](int64_t count) {
@@ -2017,6 +2056,17 @@ int32_t jxg_refine_begin(void* ctx, uint64_t* xsize_blocks, uint64_t* ysize_bloc
   };
   r.coef = take(nb * 192);
   r.dc = take(3 * nb);
+  r.sigma = take(nb);
+  for (int k = 0; k < r.epf_stages; ++k) {
+    const int nn = r.epf_stage[k] == 0 ? 12 : 4;
+    c->refine_epf_out[k] = take(3 * n);
+    c->refine_epf_nw[k] = take(nn * n);
+    c->refine_epf_cw[k] = take(n);
+  }
+  if (r.epf_stages) {
+    c->refine_epf_g[0] = take(3 * n);
+    c->refine_epf_g[1] = take(3 * n);
+  }
   r.recon = take(3 * pp);
   r.m = take(4096);
   r.mt = take(4096);
@@ -2107,10 +2157,35 @@ int32_t jxg_refine_eval(void* ctx, const float* theta, float rate_lambda, float*
   double* sums = c->refine_sums;
   JXG_CUDA(c, cudaMemsetAsync(sums, 0, 4 * kRefineSlots * sizeof(double), s));
   const unsigned block_ctas = static_cast<unsigned>((nb + 7) / 8);
-  if ((st = launch(c, "k_refine_forward", timed, [&] {
-         k_refine_forward<<<block_ctas, 256, 0, s>>>(r, theta, dlev, c->refine_lin[1][0], sums + 3 * kRefineSlots);
+  const bool epf = r.epf_stages > 0;
+  if ((epf && (st = launch(c, "k_refine_sigma", timed, [&] {
+                 k_refine_sigma<<<refine_grid(nb), 256, 0, s>>>(r, theta);
+               }))) ||
+      (st = launch(c, "k_refine_forward", timed, [&] {
+         k_refine_forward<<<block_ctas, 256, 0, s>>>(r, theta, dlev, epf ? nullptr : c->refine_lin[1][0],
+                                                     sums + 3 * kRefineSlots);
        })))
     return st;
+  if (epf) {
+    const int64_t pp = static_cast<int64_t>(r.pw) * r.yb * 8;
+    for (int k = 0; k < r.epf_stages; ++k) {
+      const float* in = k == 0 ? r.recon : c->refine_epf_out[k - 1];
+      const int64_t plane = k == 0 ? pp : n;
+      const int stride = k == 0 ? r.pw : r.w;
+      if ((st = launch(c, "k_refine_epf", timed, [&] {
+             const dim3 grid(static_cast<unsigned>((r.w + kEpfTW - 1) / kEpfTW),
+                             static_cast<unsigned>((r.h + kEpfTH - 1) / kEpfTH));
+             k_refine_epf<<<grid, 256, 0, s>>>(r, r.epf_stage[k], r.epf_sm[k], in, plane, stride,
+                                               c->refine_epf_out[k], c->refine_epf_nw[k], c->refine_epf_cw[k]);
+           })))
+        return st;
+    }
+    if ((st = launch(c, "k_refine_linear", timed, [&] {
+           k_refine_linear<<<refine_grid(n), 256, 0, s>>>(c->refine_epf_out[r.epf_stages - 1], n, r.w,
+                                                          c->refine_lin[1][0], r.w, r.h);
+         })))
+      return st;
+  }
   for (int k = 1; k < 3; ++k)
     if (c->refine_n[k] && (st = launch(c, "k_refine_down", timed, [&] {
                              k_refine_down<<<refine_grid(3 * c->refine_n[k]), 256, 0, s>>>(
@@ -2138,9 +2213,30 @@ int32_t jxg_refine_eval(void* ctx, const float* theta, float rate_lambda, float*
                                  c->refine_glin[2], c->refine_glin[1], c->refine_w[1], c->refine_h[1]);
                            })))
       return st;
+    const float* gx = nullptr;
+    if (epf) {
+      // back through XYB -> linear at the filtered values, then each stage
+      int cur = 0;
+      if ((st = launch(c, "k_refine_linear_adjoint", timed, [&] {
+             k_refine_linear_adjoint<<<refine_grid(n), 256, 0, s>>>(
+                 c->refine_epf_out[r.epf_stages - 1], c->refine_glin[0], c->refine_glin[1], r.w, r.h,
+                 c->refine_w[1], c->refine_h[1], c->refine_epf_g[cur]);
+           })))
+        return st;
+      for (int k = r.epf_stages - 1; k >= 0; --k) {
+        if ((st = launch(c, "k_refine_epf_adjoint", timed, [&] {
+               k_refine_epf_adjoint<<<refine_grid(n), 256, 0, s>>>(r, r.epf_stage[k], c->refine_epf_g[cur],
+                                                                   c->refine_epf_nw[k], c->refine_epf_cw[k],
+                                                                   c->refine_epf_g[1 - cur]);
+             })))
+          return st;
+        cur = 1 - cur;
+      }
+      gx = c->refine_epf_g[cur];
+    }
     if ((st = launch(c, "k_refine_backward", timed, [&] {
            k_refine_backward<<<block_ctas, 256, 0, s>>>(r, theta, c->refine_glin[0], c->refine_glin[1],
-                                                        c->refine_w[1], c->refine_h[1], rate_weight, grad);
+                                                        c->refine_w[1], c->refine_h[1], gx, rate_weight, grad);
          })))
       return st;
   }
@@ -2232,6 +2328,17 @@ int32_t jxg_refine_model(void* ctx, float* constants, float* coefficients, float
   std::memcpy(o, r.inv_matrix, sizeof(r.inv_matrix));
   o += 192;
   std::memcpy(o, r.thresholds, sizeof(r.thresholds));
+  o += 12;
+  // the EPF model: stages, their ids and SAD multipliers, border multiplier,
+  // channel scales, quant_mul, sharpness / 7, quantizer scale
+  *o++ = static_cast<float>(r.epf_stages);
+  for (int k = 0; k < 3; ++k) *o++ = k < r.epf_stages ? static_cast<float>(r.epf_stage[k]) : -1.0f;
+  for (int k = 0; k < 3; ++k) *o++ = k < r.epf_stages ? r.epf_sm[k] : 0.0f;
+  *o++ = r.epf_border;
+  for (int k = 0; k < 3; ++k) *o++ = r.epf_channel[k];
+  *o++ = r.epf_quant_mul;
+  *o++ = r.epf_lut;
+  *o++ = r.epf_quant_scale;
   const int64_t nb = static_cast<int64_t>(r.xb) * r.yb;
   if (coefficients)
     JXG_CUDA(c, cudaMemcpyAsync(coefficients, r.coef, nb * 192 * 4, cudaMemcpyDeviceToHost, c->stream));

@@ -30,8 +30,12 @@
 // as its unrounded value, keeps zero levels' decoded values at zero, and
 // differentiates the bias for |level| >= 2 (1 + 0.145 / level^2; 0 at
 // |level| = 1).
-// EPF, gaborish (off in the reference's encoder) and DC smoothing are not
-// modelled.
+// The decoder's edge-preserving filter is modelled (Epf::apply,
+// src/epf_filter.rs:268-350: the frame's stages, per-block sigma from the
+// field at theta, patch SADs over mirrored borders); its adjoint holds the
+// weights fixed at the forward's values, the same straight-through stance
+// as the rounding.  Gaborish (off in the reference's encoder) and DC
+// smoothing are not modelled.
 #pragma once
 
 namespace jxg {
@@ -48,6 +52,13 @@ struct RefineArgs {
   float scale, qm_mul[3];
   float matrix[3][64], inv_matrix[3][64], thresholds[3][4];
   float* dc;                 // [block][X, Y, B] decoded DC (the pass's DC levels dequantised)
+  // the decoder's edge-preserving filter (EPF): its stages in order (ids 0-2)
+  int32_t epf_stages, epf_stage[3];
+  float epf_sm[3];           // SAD multiplier of each stage (SAD_MUL x its sigma scale)
+  float epf_border;          // border_sad_mul
+  float epf_channel[3];      // channel_scale
+  float epf_quant_mul, epf_lut, epf_quant_scale;
+  float* sigma;              // per block: the inverse sigma at the current theta
   float* m;                  // [64 pixels][64 coefficients] inverse DCT8
   float* mt;                 // the same, [coefficient][pixel]
   float* recon;              // 3 padded planes (pw x yb * 8) of decoded XYB
@@ -234,8 +245,9 @@ __device__ __forceinline__ void refine_add_slot(float v, double* sums) {
 
 // Forward: one warp per block, two coefficients per lane; the levels (when
 // asked) and the rate, then the block's decoded XYB pixels M * c^ into the
-// padded planes and, inside the image, their linear RGB into `lin`
-// (3 planes of w x h).  The rate's CTA sum goes to `bit_sums`.
+// padded planes and, inside the image and without the EPF, their linear RGB
+// into `lin` (3 planes of w x h; NULL when the EPF comes first).  The rate's
+// CTA sum goes to `bit_sums`.
 __global__ void __launch_bounds__(256) k_refine_forward(const RefineArgs r, const float* __restrict__ theta,
                                                         int32_t* __restrict__ levels, float* __restrict__ lin,
                                                         double* __restrict__ bit_sums) {
@@ -277,7 +289,7 @@ __global__ void __launch_bounds__(256) k_refine_forward(const RefineArgs r, cons
       const int64_t at = static_cast<int64_t>(y) * r.pw + x;
 #pragma unroll
       for (int ch = 0; ch < 3; ++ch) r.recon[ch * pp + at] = acc[ch];
-      if (x < r.w && y < r.h) {
+      if (lin && x < r.w && y < r.h) {
         float o[3];
         xyb_to_linear(acc[0], acc[1], acc[2], o, nullptr);
         const int64_t q = static_cast<int64_t>(y) * r.w + x;
@@ -302,6 +314,208 @@ __global__ void __launch_bounds__(256) k_refine_dc(const int16_t* __restrict__ q
   dc[b * 3 + 0] = __fdiv_rn(__fmaf_rn(qy, cx, qx), fx);
   dc[b * 3 + 1] = __fdiv_rn(qy, fy);
   dc[b * 3 + 2] = __fdiv_rn(__fmaf_rn(qy, cb, qb), fb);
+}
+
+// ---------------------------------------------------------------------------
+// The decoder's EPF (src/epf_filter.rs:213-263, :320-350, epf_filter/
+// kernels.rs:88-132, epf_filter/stream.rs:157-265)
+// ---------------------------------------------------------------------------
+
+constexpr float kEpfInvSigmaNum = -1.1715729f, kEpfMinSigma = -3.905243f;
+constexpr int kEpfMaxNeighbors = 12;
+// The three stages: difference directions (dx, dy) and neighbours as
+// (direction, along), in the decoder's order.
+struct EpfStageTable {
+  int dirs, neighbors, patch;
+  int8_t dx[6], dy[6];
+  int8_t dir[kEpfMaxNeighbors];
+  int8_t along[kEpfMaxNeighbors];
+};
+__constant__ const EpfStageTable kEpfStages[3] = {
+    {6, 12, 1, {1, 2, 0, 0, 1, -1}, {0, 0, 1, 2, 1, 1},
+     {3, 4, 2, 5, 1, 0, 0, 1, 5, 2, 4, 3}, {0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1}},
+    {2, 4, 1, {1, 0}, {0, 1}, {1, 0, 0, 1}, {0, 0, 1, 1}},
+    {2, 4, 0, {1, 0}, {0, 1}, {1, 0, 0, 1}, {0, 0, 1, 1}},
+};
+
+__device__ __forceinline__ int epf_mirror(int i, int n) {
+  while (i < 0 || i >= n) i = i < 0 ? -i - 1 : 2 * n - 1 - i;
+  return i;
+}
+
+// The inverse sigma of every block at theta: the field qf * exp(theta) in
+// place of the decoder's integer field (FrameBlocks::new and the sigma
+// kernel, src/epf_filter.rs:118-146, epf_filter/kernels.rs:151-155).
+__global__ void __launch_bounds__(256) k_refine_sigma(const RefineArgs r, const float* __restrict__ theta) {
+  const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (b >= static_cast<int64_t>(r.xb) * r.yb) return;
+  const float q = __fmul_rn(static_cast<float>(r.qf[b]), expf(theta[b]));
+  const float sq = __fmul_rn(__fmul_rn(r.epf_quant_scale, q), kEpfInvSigmaNum);
+  r.sigma[b] = __fdiv_rn(1.0f, fminf(__fmul_rn(__fdiv_rn(r.epf_quant_mul, sq), r.epf_lut), -1e-4f));
+}
+
+struct EpfPlanes {
+  const float* p;
+  int64_t plane;
+  int stride, w, h;
+  __device__ __forceinline__ float at(int c, int x, int y) const {
+    return p[c * plane + static_cast<int64_t>(epf_mirror(y, h)) * stride + epf_mirror(x, w)];
+  }
+};
+
+// One EPF stage over the w x h image: `in` (planes of stride `in_stride`,
+// `in_plane` apart), `out` (3 planes of w x h); for the adjoint the
+// normalised neighbour weights (`nw`, one plane of w x h per neighbour) and
+// the centre's (`cw`).  A CTA takes a 32 x 8 tile: the pixels with a 4-pixel
+// mirrored ring into shared memory, then each direction's channel-weighted
+// differences once per position, then per pixel the patch SADs, weights and
+// the weighted mean.
+constexpr int kEpfTW = 32, kEpfTH = 8, kEpfHalo = 4;
+constexpr int kEpfInW = kEpfTW + 2 * kEpfHalo, kEpfInH = kEpfTH + 2 * kEpfHalo;  // 40 x 16
+// differences at x0-3 .. x0+33 and y0-3 .. y0+8: a SAD's centre lies within
+// (-2, -2) .. (+1, 0) of its pixel (the neighbour offsets), its patch one more
+constexpr int kEpfDW = kEpfTW + 5, kEpfDH = kEpfTH + 4;
+__global__ void __launch_bounds__(256) k_refine_epf(const RefineArgs r, int stage, float sm,
+                                                    const float* __restrict__ in, int64_t in_plane, int in_stride,
+                                                    float* __restrict__ out, float* __restrict__ nw,
+                                                    float* __restrict__ cw) {
+  __shared__ float pix[3][kEpfInH][kEpfInW + 1];
+  __shared__ float dif[6][kEpfDH][kEpfDW + 1];
+  const int tid = threadIdx.x;
+  const int x0 = blockIdx.x * kEpfTW, y0 = blockIdx.y * kEpfTH;
+  const int w = r.w, h = r.h;
+  const int64_t n = static_cast<int64_t>(w) * h;
+  const EpfPlanes src{in, in_plane, in_stride, w, h};
+  const EpfStageTable& t = kEpfStages[stage];
+  for (int u = tid; u < kEpfInH * kEpfInW; u += 256) {
+    const int ry = u / kEpfInW, rx = u % kEpfInW;
+    const int X = x0 - kEpfHalo + rx, Y = y0 - kEpfHalo + ry;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) pix[c][ry][rx] = src.at(c, X, Y);
+  }
+  __syncthreads();
+  // d(P) = sum_c scale_c |p_c(P) - p_c(P + dir)|, P at x0 - 3 + i, y0 - 3 + j
+  for (int u = tid; u < t.dirs * kEpfDH * kEpfDW; u += 256) {
+    const int d = u / (kEpfDH * kEpfDW), rem = u % (kEpfDH * kEpfDW);
+    const int j = rem / kEpfDW, i = rem % kEpfDW;
+    const int px = i + 1, py = j + 1;  // P in the pixel tile (its ring starts at -4)
+    const int qx = px + t.dx[d], qy = py + t.dy[d];
+    float v = __fmul_rn(fabsf(__fsub_rn(pix[0][py][px], pix[0][qy][qx])), r.epf_channel[0]);
+    v = __fadd_rn(__fmul_rn(fabsf(__fsub_rn(pix[1][py][px], pix[1][qy][qx])), r.epf_channel[1]), v);
+    dif[d][j][i] = __fadd_rn(__fmul_rn(fabsf(__fsub_rn(pix[2][py][px], pix[2][qy][qx])), r.epf_channel[2]), v);
+  }
+  __syncthreads();
+  const int lx = tid % kEpfTW, ly = tid / kEpfTW;
+  const int x = x0 + lx, y = y0 + ly;
+  if (x >= w || y >= h) return;
+  const int64_t q = static_cast<int64_t>(y) * w + x;
+  const int cx = lx + kEpfHalo, cy = ly + kEpfHalo;  // the pixel in `pix`
+  float acc[3] = {pix[0][cy][cx], pix[1][cy][cx], pix[2][cy][cx]};
+  const float s = r.sigma[static_cast<int64_t>(y >> 3) * r.xb + (x >> 3)];
+  if (s < kEpfMinSigma) {  // unfiltered block: the centre, exactly
+#pragma unroll
+    for (int c = 0; c < 3; ++c) out[c * n + q] = acc[c];
+    for (int k = 0; k < t.neighbors; ++k) nw[k * n + q] = 0.0f;
+    cw[q] = 1.0f;
+    return;
+  }
+  const bool border = (y & 7) == 0 || (y & 7) == 7 || (x & 7) == 0 || (x & 7) == 7;
+  const float inv = __fmul_rn(s, border ? __fmul_rn(sm, r.epf_border) : sm);
+  float sum = 1.0f, wk[kEpfMaxNeighbors];
+  for (int k = 0; k < t.neighbors; ++k) {
+    const int d = t.dir[k], dx = t.dx[d], dy = t.dy[d];
+    const bool along = t.along[k] != 0;
+    // the SAD's centre P = (sx, sy), as an index into `dif` (offset 3)
+    const int di = (along ? lx : lx - dx) + 3, dj = (along ? ly : ly - dy) + 3;
+    float sad;
+    if (t.patch)
+      sad = __fadd_rn(__fadd_rn(dif[d][dj][di], __fadd_rn(dif[d][dj][di - 1], dif[d][dj][di + 1])),
+                      __fadd_rn(dif[d][dj - 1][di], dif[d][dj + 1][di]));
+    else
+      sad = dif[d][dj][di];
+    const float wt = fmaxf(__fadd_rn(__fmul_rn(sad, inv), 1.0f), 0.0f);
+    wk[k] = wt;
+    sum = __fadd_rn(sum, wt);
+    const int nx = cx + (along ? dx : -dx), ny = cy + (along ? dy : -dy);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) acc[c] = __fadd_rn(__fmul_rn(wt, pix[c][ny][nx]), acc[c]);
+  }
+  const float inv_sum = __fdiv_rn(1.0f, sum);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) out[c * n + q] = __fmul_rn(acc[c], inv_sum);
+  for (int k = 0; k < t.neighbors; ++k) nw[k * n + q] = __fmul_rn(wk[k], inv_sum);
+  cw[q] = inv_sum;
+}
+
+// Its adjoint with the weights held: g_in(q) = cw(q) g_out(q) plus, for every
+// output pixel p whose neighbour k is q (through the mirrored borders),
+// nw_k(p) g_out(p).  A gather: the candidates for p are q's mirror images
+// less the neighbour's offset.
+__global__ void __launch_bounds__(256) k_refine_epf_adjoint(const RefineArgs r, int stage,
+                                                            const float* __restrict__ gout,
+                                                            const float* __restrict__ nw,
+                                                            const float* __restrict__ cw,
+                                                            float* __restrict__ gin) {
+  const int w = r.w, h = r.h;
+  const int64_t n = static_cast<int64_t>(w) * h;
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int qx = static_cast<int>(q % w), qy = static_cast<int>(q / w);
+  const EpfStageTable& t = kEpfStages[stage];
+  float g[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) g[c] = __fmul_rn(cw[q], gout[c * n + q]);
+  const bool interior = qx >= 3 && qx < w - 3 && qy >= 3 && qy < h - 3;
+  const int cxs[3] = {qx, -1 - qx, 2 * w - 1 - qx}, cys[3] = {qy, -1 - qy, 2 * h - 1 - qy};
+  for (int k = 0; k < t.neighbors; ++k) {
+    const int d = t.dir[k];
+    const int ox = t.along[k] ? t.dx[d] : -t.dx[d], oy = t.along[k] ? t.dy[d] : -t.dy[d];
+    for (int iy = 0; iy < (interior ? 1 : 3); ++iy)
+      for (int ix = 0; ix < (interior ? 1 : 3); ++ix) {
+        const int px = cxs[ix] - ox, py = cys[iy] - oy;
+        if (px < 0 || px >= w || py < 0 || py >= h) continue;
+        if (!interior && (epf_mirror(px + ox, w) != qx || epf_mirror(py + oy, h) != qy)) continue;
+        if (ix > 0 && cxs[ix] == cxs[0]) continue;  // the same mirror image twice
+        if (iy > 0 && cys[iy] == cys[0]) continue;
+        const int64_t p = static_cast<int64_t>(py) * w + px;
+        const float wv = nw[k * n + p];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) g[c] = __fadd_rn(g[c], __fmul_rn(wv, gout[c * n + p]));
+      }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) gin[c * n + q] = g[c];
+}
+
+// The gradient by the filtered XYB planes (w x h): scale 0's linear-plane
+// gradient plus a quarter of scale 1's, back through XYB -> linear at the
+// filtered values.
+__global__ void __launch_bounds__(256) k_refine_linear_adjoint(const float* __restrict__ xyb,
+                                                               const float* __restrict__ glin0,
+                                                               const float* __restrict__ glin1, int w, int h,
+                                                               int w1, int h1, float* __restrict__ gxyb) {
+  const int64_t n = static_cast<int64_t>(w) * h, n1 = static_cast<int64_t>(w1) * h1;
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int x = static_cast<int>(q % w), y = static_cast<int>(q / w);
+  float gl[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) gl[k] = glin0[k * n + q];
+  if ((y >> 1) < h1 && (x >> 1) < w1) {
+    const int64_t q1 = static_cast<int64_t>(y >> 1) * w1 + (x >> 1);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) gl[k] = __fmaf_rn(0.25f, glin1[k * n1 + q1], gl[k]);
+  }
+  float o[3], dc[3];
+  xyb_to_linear(xyb[q], xyb[n + q], xyb[2 * n + q], o, dc);
+  float gm[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    gm[k] = __fmul_rn(dc[k], __fmaf_rn(kOpsinInverse[k], gl[0],
+                                       __fmaf_rn(kOpsinInverse[3 + k], gl[1], __fmul_rn(kOpsinInverse[6 + k], gl[2]))));
+  gxyb[q] = __fsub_rn(gm[0], gm[1]);
+  gxyb[n + q] = __fadd_rn(gm[0], gm[1]);
+  gxyb[2 * n + q] = gm[2];
 }
 
 // Linear RGB of the w x h region of XYB planes with row stride `in_stride`.
@@ -524,13 +738,14 @@ __global__ void __launch_bounds__(256) k_refine_ssim(const float* __restrict__ a
   refine_add_slot(loss, sums);
 }
 
-// Backward per block: the gradient by the linear planes (scale 0 plus a
-// quarter of scale 1's at the covering coarse pixel; scale 1 already holds
-// scale 2's), back through XYB -> linear to the decoded XYB, M^T to the
-// coefficients, then d L / d theta.
+// Backward per block: the gradient by the decoded XYB (given, when the EPF
+// is modelled; else from the linear planes: scale 0 plus a quarter of scale
+// 1's at the covering coarse pixel, scale 1 already holding scale 2's, back
+// through XYB -> linear), M^T to the coefficients, then d L / d theta.
 __global__ void __launch_bounds__(256) k_refine_backward(const RefineArgs r, const float* __restrict__ theta,
                                                          const float* __restrict__ glin0,
                                                          const float* __restrict__ glin1, int w1, int h1,
+                                                         const float* __restrict__ gxyb_in,
                                                          float rate_weight, float* __restrict__ gtheta) {
   __shared__ float gs[8][3][64];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -544,7 +759,11 @@ __global__ void __launch_bounds__(256) k_refine_backward(const RefineArgs r, con
     const int p = lane + 32 * h2;
     const int y = by * 8 + (p >> 3), x = bx * 8 + (p & 7);
     float gx[3] = {0.0f, 0.0f, 0.0f};
-    if (x < r.w && y < r.h) {
+    if (x < r.w && y < r.h && gxyb_in) {  // through the EPF's adjoint already
+      const int64_t q = static_cast<int64_t>(y) * r.w + x;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) gx[k] = gxyb_in[k * n + q];
+    } else if (x < r.w && y < r.h) {
       const int64_t q = static_cast<int64_t>(y) * r.w + x;
       float gl[3];
 #pragma unroll

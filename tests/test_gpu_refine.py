@@ -4,8 +4,9 @@ optimiser, against an FP64 PyTorch restatement of the same model.
 The library has no counterpart in the reference (which computes no
 gradients); what can be pinned is (1) the model's levels at theta = 0 are the
 front end's own levels, bit for bit; (2) its loss and its gradient match an
-FP64 autograd model of the same straight-through quantiser (levels frozen to
-the kernel's, so both sides round alike); (3) that FP64 model's gradient is
+FP64 autograd model of the same straight-through quantiser and of the
+decoder's EPF with its weights held (levels and weights frozen to the
+kernel's, so both sides round alike); (3) that FP64 model's gradient is
 the derivative of the frozen-offset surrogate, checked by central
 differences; (4) Adam steps lower the true (rounded) loss; (5) a pass with a
 caller's field equals the plain pass when the field is the adaptive one.
@@ -25,6 +26,19 @@ OPSIN_INVERSE = np.array([[11.031567, -9.866944, -0.16462299],
 OPSIN_BIAS, NEG_BIAS_CBRT = 0.0037930734, -0.1559542
 BIAS_ONE = np.array([1.0 - 0.05465007330715401, 1.0 - 0.07005449891748593, 1.0 - 0.049935103337343655])
 C1, C2 = 1e-4, 9e-4
+EPF_STAGES = {  # (dx, dy) directions and neighbours (direction, along), the decoder's order
+    0: ([(1, 0), (2, 0), (0, 1), (0, 2), (1, 1), (-1, 1)],
+        [(3, 0), (4, 0), (2, 0), (5, 0), (1, 0), (0, 0), (0, 1), (1, 1), (5, 1), (2, 1), (4, 1), (3, 1)], True),
+    1: ([(1, 0), (0, 1)], [(1, 0), (0, 0), (0, 1), (1, 1)], True),
+    2: ([(1, 0), (0, 1)], [(1, 0), (0, 0), (0, 1), (1, 1)], False),
+}
+EPF_INV_SIGMA_NUM, EPF_MIN_SIGMA = -1.1715729, -3.905243
+
+
+def mirror(i, n):
+    while i < 0 or i >= n:
+        i = -i - 1 if i < 0 else 2 * n - 1 - i
+    return i
 
 
 @pytest.fixture(scope="module")
@@ -56,6 +70,11 @@ class Fp64Model:
         self.coef = torch.tensor(m["coef"], dtype=d)
         self.M = torch.tensor(m["inverse"], dtype=d)
         self.dc = torch.tensor(m["dc"], dtype=d)  # (nb, 3) decoded DC
+        self.epf = m["epf"]
+        pad = 8  # mirrored coordinates for offsets up to +-8
+        self.mx = torch.tensor([mirror(i, w) for i in range(-pad, w + pad)])
+        self.my = torch.tensor([mirror(i, h) for i in range(-pad, h + pad)])
+        self.pad = pad
         thr = m["thresholds"]
         z = np.zeros((3, 64))
         for i in range(64):  # the zero region's edge per coefficient
@@ -112,13 +131,63 @@ class Fp64Model:
             u[c] = self.inv[c] * (s * self.qm[c])[:, None] * v
         return u, yh
 
-    def loss(self, theta, theta0, q0, lam):
-        """(loss, distortion, bits) at theta with levels frozen at theta0."""
-        q0 = torch.tensor(q0, dtype=torch.float64)  # (nb, 3, 64)
+    def _shift(self, img, ox, oy):
+        """img at (x + ox, y + oy) through the mirrored borders."""
+        ys = self.my[torch.arange(self.h) + oy + self.pad]
+        xs = self.mx[torch.arange(self.w) + ox + self.pad]
+        return img[:, ys][:, :, xs]
+
+    def _epf_weights(self, img, theta):
+        """One stage's weights at a fixed input: per stage (normalised
+        neighbour weights, centre weight), computed from the values given
+        (the decoder's Epf::apply); the caller holds them fixed."""
+        e = self.epf
+        q = self.qf * torch.exp(theta)
+        sq = e["quant_scale"] * q * EPF_INV_SIGMA_NUM
+        sigma = 1.0 / torch.clamp((e["quant_mul"] / sq) * e["lut"], max=-1e-4)
+        sig = sigma.view(self.yb, self.xb).repeat_interleave(8, 0).repeat_interleave(8, 1)[: self.h, : self.w]
+        yy, xx = torch.meshgrid(torch.arange(self.h), torch.arange(self.w), indexing="ij")
+        border = ((yy % 8 == 0) | (yy % 8 == 7) | (xx % 8 == 0) | (xx % 8 == 7))
+        cs = torch.tensor(e["channel_scale"], dtype=torch.float64)
+        out = []
+        for stage, sm in e["stages"]:
+            dirs, neighbors, patch = EPF_STAGES[stage]
+            inv = sig * torch.where(border, torch.tensor(sm * e["border"], dtype=torch.float64),
+                                    torch.tensor(sm, dtype=torch.float64))
+
+            def diff(sx, sy, dx, dy):
+                a, b = self._shift(img, sx, sy), self._shift(img, sx + dx, sy + dy)
+                return ((a - b).abs() * cs[:, None, None]).sum(0)
+
+            ws = []
+            for d, along in neighbors:
+                dx, dy = dirs[d]
+                sx, sy = (0, 0) if along else (-dx, -dy)
+                if patch:
+                    sad = sum(diff(sx + ax, sy + ay, dx, dy) for ax, ay in ((0, 0), (-1, 0), (1, 0), (0, -1), (0, 1)))
+                else:
+                    sad = diff(sx, sy, dx, dy)
+                ws.append(torch.clamp(sad * inv + 1.0, min=0.0))
+            wsum = 1.0 + sum(ws)
+            filtered = sig >= EPF_MIN_SIGMA
+            norm = [torch.where(filtered, wk / wsum, torch.zeros_like(wk)) for wk in ws]
+            centre = torch.where(filtered, 1.0 / wsum, torch.ones_like(wsum))
+            out.append((norm, centre))
+            img = self._epf_apply(img, stage, (norm, centre))
+        return out
+
+    def _epf_apply(self, img, stage, weights):
+        dirs, neighbors, _ = EPF_STAGES[stage]
+        norm, centre = weights
+        acc = img * centre
+        for (d, along), wk in zip(neighbors, norm):
+            dx, dy = dirs[d]
+            acc = acc + wk * (self._shift(img, dx, dy) if along else self._shift(img, -dx, -dy))
+        return acc
+
+    def _decode(self, theta, q0, offset):
+        """The decoded coefficients (nb, 3, 64) and the model bits at theta."""
         nz = q0 != 0
-        with torch.no_grad():
-            u0, _ = self._inputs(self.scale * self.qf * torch.exp(theta0), q0, None)
-        offset = {c: q0[:, c] - u0[c] for c in range(3)}
         s = self.scale * self.qf * torch.exp(theta)
         u, yh = self._inputs(s, q0, offset)
         chat = []
@@ -136,8 +205,23 @@ class Fp64Model:
             zero = 2.6 * (u[c].abs() / self.zero_edge[c]) ** 4  # a zero level: its unrounded input
             term = torch.where(nz[:, c], 1.6 + torch.log2(1.0 + a), zero)
             bits = bits + term[:, 1:].sum()
-        chat = torch.stack(chat, dim=1)  # (nb, 3, 64)
-        rec = [self._linear(self.planes(chat))]
+        return torch.stack(chat, dim=1), bits
+
+    def loss(self, theta, theta0, q0, lam):
+        """(loss, distortion, bits) at theta with levels (and the EPF's
+        weights) frozen at theta0."""
+        q0 = torch.tensor(q0, dtype=torch.float64)  # (nb, 3, 64)
+        with torch.no_grad():
+            u0, _ = self._inputs(self.scale * self.qf * torch.exp(theta0), q0, None)
+        offset = {c: q0[:, c] - u0[c] for c in range(3)}
+        chat, bits = self._decode(theta, q0, offset)
+        img = self.planes(chat)
+        if self.epf["stages"]:
+            with torch.no_grad():
+                frozen = self._epf_weights(self.planes(self._decode(theta0, q0, offset)[0]), theta0)
+            for (stage, _), wts in zip(self.epf["stages"], frozen):
+                img = self._epf_apply(img, stage, wts)
+        rec = [self._linear(img)]
         for _ in range(2):
             rec.append(self._down(rec[-1]))
         dist = sum(self._ssim_loss(a, b) for a, b in zip(self.src, rec)) / 3.0
@@ -213,8 +297,8 @@ def test_inverse_reproduces_the_source(ctx, w, h, seed):
     assert err <= 1e-5 * max(1.0, np.abs(res.xyb).max()), err
 
 
-def fp64_check(ctx, w, h, seed, lam, spread):
-    img, res = begin(ctx, w, h, seed)
+def fp64_check(ctx, w, h, seed, lam, spread, d=1.0):
+    img, res = begin(ctx, w, h, seed, d)
     nb = res.quant_field.size
     rng = np.random.default_rng(seed)
     th = rng.normal(0.0, spread, nb).astype(np.float32)
@@ -228,10 +312,12 @@ def fp64_check(ctx, w, h, seed, lam, spread):
     l64, d64, b64 = model.loss(t64, t64.detach().clone(), lv, lam)
     l64.backward()
     g_ref = t64.grad.numpy()
-    # FP32 sums over every pixel against FP64: relative 1e-4 on the loss terms
+    # FP32 against FP64: the rate within 1e-4 relative; the distortion within
+    # 5e-4 relative plus 2e-6 (SSIM's FP32 variances cancel where the
+    # decoded image is close to the source, as at d 0.5)
     assert abs(bits - b64.item()) <= 1e-4 * max(b64.item(), 1.0), (bits, b64.item())
-    assert abs(dist - d64.item()) <= 1e-4 * max(d64.item(), 1e-3), (dist, d64.item())
-    assert abs(loss - l64.item()) <= 1e-4 * max(l64.item(), 1e-3), (loss, l64.item())
+    assert abs(dist - d64.item()) <= 5e-4 * d64.item() + 2e-6, (dist, d64.item())
+    assert abs(loss - l64.item()) <= 5e-4 * l64.item() + 2e-6, (loss, l64.item())
     # the adjoint: per block, within 1e-3 of the largest gradient
     tol = 1e-3 * np.abs(g_ref).max()
     err = np.abs(g_gpu - g_ref)
@@ -239,14 +325,18 @@ def fp64_check(ctx, w, h, seed, lam, spread):
     return model, t64.detach(), lv, g_ref, lam
 
 
-@pytest.mark.parametrize("w,h,seed,lam,spread", [(70, 54, 21, 0.002, 0.3), (200, 136, 22, 0.01, 0.1)])
-def test_loss_and_gradient_match_fp64(ctx, w, h, seed, lam, spread):
-    fp64_check(ctx, w, h, seed, lam, spread)
+@pytest.mark.parametrize("w,h,seed,lam,spread,d", [(70, 54, 21, 0.002, 0.3, 1.0), (200, 136, 22, 0.01, 0.1, 1.0),
+                                                    (72, 64, 23, 0.002, 0.2, 3.0), (45, 37, 24, 0.005, 0.2, 0.5)])
+def test_loss_and_gradient_match_fp64(ctx, w, h, seed, lam, spread, d):
+    # d 1.0: one EPF stage; d 3.0: three (pass-0 scale signalled); d 0.5: none
+    fp64_check(ctx, w, h, seed, lam, spread, d)
+    stages = len(ctx.refine_model()["epf"]["stages"])
+    assert stages == {1.0: 1, 3.0: 3, 0.5: 0}[d]
 
 
 def test_fp64_gradient_is_the_surrogates_derivative(ctx):
     # central differences of the frozen-offset surrogate on 64 random blocks
-    model, th, lv, g_ref, lam = fp64_check(ctx, 72, 68, 31, 0.002, 0.3)
+    model, th, lv, g_ref, lam = fp64_check(ctx, 72, 68, 31, 0.002, 0.3, 3.0)  # three EPF stages
     step = 1e-5
     for b in np.random.default_rng(44).choice(th.numel(), 64, replace=False):
         e = torch.zeros_like(th)
