@@ -66,6 +66,8 @@ def parse_args():
     p.add_argument("--refine-steps", type=int, default=8)
     p.add_argument("--refine-only", action="store_true",
                    help="only run the refinement record on one context and print it (a profiler target)")
+    p.add_argument("--frames-ultrafast", action="store_true",
+                   help="with --frames: the UltraFast gates at q75, q90 and q95 instead of the headline")
     p.add_argument("--frames", type=int, default=0,
                    help="only run this many frames of the headline workload on one context, "
                         "untimed, and exit (the target of a profiler capture)")
@@ -838,8 +840,11 @@ def run_frames(args):
     d_img = torch.from_numpy(img).cuda().contiguous()
     ctx = J.FrontendContext(0)
     speed = J.Speed.FASTEST if SPEED == "fastest" else J.Speed.ULTRA_FAST
+    qualities = QUALITIES
+    if args.frames_ultrafast:
+        speed, qualities = J.Speed.ULTRA_FAST, UF_QUALITIES
     for k in range(args.frames):
-        for q in QUALITIES:
+        for q in qualities:
             ctx.run_device(d_img.data_ptr(), WIDTH, HEIGHT, 3, 8, J.EncodeConfig(speed=speed).with_quality(q))
     torch.cuda.synchronize()
     ctx.close()
