@@ -581,41 +581,18 @@ def run_refine(ctx, stream, args, dev) -> dict:
         kernels[k] = {"ms": v[0], "launches": v[1]}
         if k in algo:
             kernels[k]["algorithmic_gbs"] = algo[k] / (v[0] / 1000.0) / 1e9
-    # the refined field as coded: the model at theta = log(field / qf), and
-    # the pass over that field
     ctx.refine_theta(theta)
-    field = ctx.refine_field()
-    qf = base.quant_field.astype(np.float64)
-    def at_field(f):
-        ctx.refine_theta(np.log(f.astype(np.float64) / qf).astype(np.float32))
-        return ctx.refine_eval(lam)[0]
-
-    coded = at_field(field)
-    # the same model distortion from a uniform change of the adaptive field
-    # (bisection on one log scale; a larger field quantises finer), for an
-    # equal-distortion rate comparison
-    def uniform(c):
-        return np.clip(np.rint(qf * np.exp(c)), 1, 255).astype(np.uint8)
-
-    lo, hi = -1.0, 1.0
-    for _ in range(20):
-        mid = 0.5 * (lo + hi)
-        if at_field(uniform(mid))[1] < coded[1]:
-            hi = mid
-        else:
-            lo = mid
-    # integer fields move in steps: code the two uniform fields that bracket
-    # the refined distortion and interpolate their rate at it
-    brackets = []
-    for c in (lo, hi):
-        f = uniform(c)
-        d = at_field(f)[1]
-        brackets.append((c, d, J.ac_bits_estimate(ctx.frontend_with_field(img, cfg, f, coefficients=False))))
-    (c_lo, d_lo, b_lo), (c_hi, d_hi, b_hi) = brackets
-    t = 0.0 if d_lo == d_hi else (coded[1] - d_hi) / (d_lo - d_hi)
-    bits2 = b_hi + t * (b_lo - b_hi)
-    refined = ctx.frontend_with_field(img, cfg, field, coefficients=False)
-    bits0, bits1 = J.ac_bits_estimate(base), J.ac_bits_estimate(refined)
+    coded = _refined_field_report(ctx, img, cfg, base, ctx.refine_field(), lam)
+    # the same refinement with the reference's own luma proxy as the
+    # distortion (weights 0, 1), from theta = 0 at that measure's slope
+    ctx.refine_weights(0.0, 1.0)
+    ctx.refine_theta(np.zeros((yb, xb), np.float32))
+    lam_p = ctx.refine_rate_slope(w * h)
+    for _ in range(args.refine_steps):
+        ctx.refine_step(lam_p, lr)
+    coded_proxy = _refined_field_report(ctx, img, cfg, base, ctx.refine_field(), lam_p)
+    coded_proxy["lambda"] = lam_p
+    ctx.refine_weights(1.0, 0.0)
     return {"workload": f"{w}x{h} RGB8 (seed 4) q90 UltraFast pass, {nb} blocks, Adam lr {lr}, "
                         f"lambda {lam:.4g} (the pass's rate-distortion slope), SSIM at 3 scales + rate model",
             "steps": args.refine_steps, "ms_per_step": ms, "wall_ms_per_step": 1000.0 * wall / args.refine_steps,
@@ -623,15 +600,61 @@ def run_refine(ctx, stream, args, dev) -> dict:
             "loss_first": hist[0][0], "loss_final": final[0], "distortion_first": hist[0][1],
             "distortion_final": final[1], "model_bits_first": hist[0][2], "model_bits_final": final[2],
             "untimed_first_step_loss": first[0],
-            "coded": {"distortion_adaptive_field": hist[0][1], "distortion_refined_field": coded[1],
-                      "ac_bpp_adaptive_field": bits0 / (w * h), "ac_bpp_refined_field": bits1 / (w * h),
-                      "uniform_scale_same_distortion": {
-                          "brackets": [{"log_scale": c, "distortion": d, "ac_bpp": b / (w * h)}
-                                       for c, d, b in brackets],
-                          "ac_bpp_interpolated": bits2 / (w * h)},
-                      "refined_over_uniform_bits": bits1 / bits2,
-                      "ac_bits_estimate": "per-context symbol entropy + raw bits of the tokens"},
+            "coded": coded, "coded_luma_proxy_objective": coded_proxy,
             "kernels": kernels}
+
+
+def _refined_field_report(ctx, img, cfg, base, field, lam) -> dict:
+    """A refined field as coded, under the context's distortion weights: the
+    model's distortion at theta = log(field / qf) and the pass's AC bits
+    (`ac_bits_estimate`: per-context symbol entropy + the tokens' raw bits)
+    against the adaptive field's, and against uniform rescalings of the
+    adaptive field at the same distortion (the two integer fields that
+    bracket it, coded, their rates interpolated); then both distortion
+    measures (1 - SSIM, the luma proxy) at every field."""
+    import jixel_gb300 as J
+
+    h, w = img.shape[:2]
+    qf = base.quant_field.astype(np.float64)
+
+    def at_field(f):
+        ctx.refine_theta(np.log(f.astype(np.float64) / qf).astype(np.float32))
+        return ctx.refine_eval(lam)[0]
+
+    def uniform(c):  # a larger field quantises finer
+        return np.clip(np.rint(qf * np.exp(c)), 1, 255).astype(np.uint8)
+
+    d0, d1 = at_field(base.quant_field)[1], at_field(field)[1]
+    lo, hi = -1.0, 1.0
+    for _ in range(20):
+        mid = 0.5 * (lo + hi)
+        if at_field(uniform(mid))[1] < d1:
+            hi = mid
+        else:
+            lo = mid
+    brackets = []
+    for c in (lo, hi):
+        f = uniform(c)
+        brackets.append((c, at_field(f)[1], J.ac_bits_estimate(ctx.frontend_with_field(img, cfg, f, coefficients=False))))
+    (_, d_lo, b_lo), (_, d_hi, b_hi) = brackets
+    t = 0.0 if d_lo == d_hi else (d1 - d_hi) / (d_lo - d_hi)
+    bits_uniform = b_hi + t * (b_lo - b_hi)
+    bits0 = J.ac_bits_estimate(base)
+    bits1 = J.ac_bits_estimate(ctx.frontend_with_field(img, cfg, field, coefficients=False))
+    measures = {}
+    ws, wp = ctx.refine_weights_now
+    for name, wts in (("ssim", (1.0, 0.0)), ("luma_proxy", (0.0, 1.0))):
+        ctx.refine_weights(*wts)
+        measures[name] = {"adaptive_field": at_field(base.quant_field)[1], "refined_field": at_field(field)[1],
+                          "uniform_brackets": [at_field(uniform(c))[1] for c, _, _ in brackets]}
+    ctx.refine_weights(ws, wp)
+    return {"distortion_adaptive_field": d0, "distortion_refined_field": d1,
+            "ac_bpp_adaptive_field": bits0 / (w * h), "ac_bpp_refined_field": bits1 / (w * h),
+            "uniform_scale_same_distortion": {
+                "brackets": [{"log_scale": c, "distortion": d, "ac_bpp": b / (w * h)} for c, d, b in brackets],
+                "ac_bpp_interpolated": bits_uniform / (w * h)},
+            "refined_over_uniform_bits": bits1 / bits_uniform,
+            "measures": measures}
 
 
 def run_c5(ctxs, streams, flush, args, dev) -> dict:

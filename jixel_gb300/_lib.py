@@ -46,6 +46,7 @@ EXPORTS = [
     "jxg_selftest_math",
     "jxg_refine_begin",
     "jxg_refine_eval",
+    "jxg_refine_set_weights",
     "jxg_refine_step",
     "jxg_refine_theta",
     "jxg_refine_field",
@@ -175,6 +176,7 @@ def load() -> ctypes.CDLL:
                                     ctypes.POINTER(ctypes.c_uint32)]),
         "jxg_refine_begin": (i32, [vp, vp, vp]),
         "jxg_refine_eval": (i32, [vp, vp, ctypes.c_float, vp, vp, vp]),
+        "jxg_refine_set_weights": (i32, [vp, ctypes.c_float, ctypes.c_float]),
         "jxg_refine_step": (i32, [vp, ctypes.c_float, ctypes.c_float, vp]),
         "jxg_refine_theta": (i32, [vp, vp, i32]),
         "jxg_refine_field": (i32, [vp, vp, vp]),

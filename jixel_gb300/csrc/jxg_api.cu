@@ -157,7 +157,19 @@ struct Context {
   float* refine_epf_out[3] = {};
   float* refine_epf_nw[3] = {};
   float* refine_epf_cw[3] = {};
-  float* refine_epf_g[2] = {};
+  float* refine_epf_g[2] = {};   // the decoded-XYB gradient (EPF or proxy), ping-pong
+  // the distortion's mix: weight of 1 - SSIM and of the luma proxy
+  float refine_w_ssim = 1.0f, refine_w_proxy = 0.0f;
+  bool refine_proxy = false;  // the frame is large enough for the proxy (4 x 4)
+  struct ProxyLevel {
+    int w = 0, h = 0;
+    float *ref_vals = nullptr, *ref_mv = nullptr;               // the source's level, mean and variance
+    float *vals = nullptr, *tmp = nullptr, *box = nullptr, *s = nullptr, *parts = nullptr, *g = nullptr,
+          *gtmp = nullptr, *gv = nullptr;
+  } refine_pl[2];
+  float* refine_src_y = nullptr;
+  double* refine_proxy_sums = nullptr;
+  jxg::ProxyScalars* refine_proxy_k = nullptr;
   // the context's own parameters, their gradient and Adam moments
   float *refine_theta = nullptr, *refine_grad = nullptr, *refine_adam = nullptr;
   int32_t refine_steps = 0;
@@ -2040,13 +2052,18 @@ int32_t jxg_refine_begin(void* ctx, uint64_t* xsize_blocks, uint64_t* ysize_bloc
   r.epf_quant_mul = lfp.quant_mul;
   r.epf_lut = static_cast<float>(fp.epf_sharpness) / 7.0f;
   r.epf_quant_scale = a.scale;
-  const int64_t epf_planes = r.epf_stages ? 3 * r.epf_stages + 20 + r.epf_stages + 6 : 0;
+  const int64_t epf_planes = r.epf_stages ? 3 * r.epf_stages + 20 + r.epf_stages : 0;
+  // the luma proxy's levels (half and quarter) and the source's Y plane
+  c->refine_proxy = r.w >= 4 && r.h >= 4;
+  const int64_t w2 = r.w / 2, h2 = r.h / 2, w4 = w2 / 2, h4 = h2 / 2;
+  const int64_t proxy_floats = c->refine_proxy ? n + 20 * (w2 * h2 + w4 * h4) : 0;
   // one allocation: source coefficients (nb x 192), the decoded XYB planes
   // (3 pp), M and M^T, the source and decoded linear planes and the gradient
   // per scale, the f64 sums, theta, its gradient and Adam moments, copies of
   // the field and the colour maps; each piece rounded up to 64 floats
   const size_t floats = nb * 192 + 3 * nb + 3 * pp + 2 * 4096 + 3 * 3 * (n + n1 + n2) + 2 * 4 * kRefineSlots +
-                        4 * nb + (nb + 2 * tiles) / 4 + nb + epf_planes * n + 64 * 60;
+                        4 * nb + (nb + 2 * tiles) / 4 + nb + epf_planes * n + 6 * n + proxy_floats +
+                        2 * kProxySums * kRefineSlots + 64 + 64 * 90;
   if ((st = ensure(c, c->refine_buf, floats * 4 + 256))) return st;
   float* base = static_cast<float*>(c->refine_buf.ptr);
   auto take = [&](int64_t count) {
@@ -2063,9 +2080,29 @@ int32_t jxg_refine_begin(void* ctx, uint64_t* xsize_blocks, uint64_t* ysize_bloc
     c->refine_epf_nw[k] = take(nn * n);
     c->refine_epf_cw[k] = take(n);
   }
-  if (r.epf_stages) {
-    c->refine_epf_g[0] = take(3 * n);
-    c->refine_epf_g[1] = take(3 * n);
+  c->refine_epf_g[0] = take(3 * n);
+  c->refine_epf_g[1] = take(3 * n);
+  c->refine_proxy_sums = reinterpret_cast<double*>(take(2 * kProxySums * kRefineSlots));
+  c->refine_proxy_k = reinterpret_cast<ProxyScalars*>(take(64));
+  if (c->refine_proxy) {
+    c->refine_src_y = take(n);
+    const int64_t dims[2][2] = {{w2, h2}, {w4, h4}};
+    for (int l = 0; l < 2; ++l) {
+      auto& L = c->refine_pl[l];
+      L.w = static_cast<int>(dims[l][0]);
+      L.h = static_cast<int>(dims[l][1]);
+      const int64_t m = dims[l][0] * dims[l][1];
+      L.ref_vals = take(m);
+      L.ref_mv = take(2 * m);
+      L.vals = take(m);
+      L.tmp = take(3 * m);
+      L.box = take(3 * m);
+      L.s = take(m);
+      L.parts = take(3 * m);
+      L.g = take(3 * m);
+      L.gtmp = take(3 * m);
+      L.gv = take(m);
+    }
   }
   r.recon = take(3 * pp);
   r.m = take(4096);
@@ -2127,6 +2164,23 @@ int32_t jxg_refine_begin(void* ctx, uint64_t* xsize_blocks, uint64_t* ysize_bloc
                                  c->refine_lin[0][k - 1], c->refine_lin[0][k], c->refine_w[k - 1], c->refine_h[k - 1]);
                            })))
       return st;
+  if (c->refine_proxy) {
+    // the source's Y plane and its proxy levels: values, box mean and variance
+    JXG_CUDA(c, cudaMemcpyAsync(c->refine_src_y, r.xyb + r.plane, n * 4, cudaMemcpyDeviceToDevice, s));
+    auto& H = c->refine_pl[0];
+    auto& Q = c->refine_pl[1];
+    k_proxy_half<<<refine_grid(static_cast<int64_t>(H.w) * H.h), 256, 0, s>>>(c->refine_src_y, r.w, r.w, r.h, 1,
+                                                                              H.ref_vals);
+    k_proxy_half<<<refine_grid(static_cast<int64_t>(Q.w) * Q.h), 256, 0, s>>>(H.ref_vals, H.w, H.w, H.h, 0,
+                                                                              Q.ref_vals);
+    for (auto* L : {&H, &Q}) {
+      const int64_t m = static_cast<int64_t>(L->w) * L->h;
+      k_proxy_box_v<<<refine_grid(m), 256, 0, s>>>(L->ref_vals, nullptr, L->w, L->h, L->tmp);
+      k_proxy_box_h<<<refine_grid(2 * m), 256, 0, s>>>(L->tmp, 2, L->w, L->h, L->ref_mv);
+      k_proxy_variance<<<refine_grid(m), 256, 0, s>>>(L->ref_mv, m);
+    }
+    JXG_CUDA(c, cudaGetLastError());
+  }
   if ((st = wait(c))) return st;
   r.xyb = nullptr;
   c->refine_ready = true;
@@ -2147,6 +2201,7 @@ int32_t jxg_refine_eval(void* ctx, const float* theta, float rate_lambda, float*
   const RefineArgs& r = c->refine;
   const int64_t nb = static_cast<int64_t>(r.xb) * r.yb;
   const int64_t n = c->refine_n[0];
+  const int64_t pp = static_cast<int64_t>(r.pw) * r.yb * 8;
   int st;
   int32_t* dlev = nullptr;
   if (levels) {
@@ -2155,7 +2210,11 @@ int32_t jxg_refine_eval(void* ctx, const float* theta, float rate_lambda, float*
   }
   const bool timed = c->timing;
   double* sums = c->refine_sums;
+  double* psums = c->refine_proxy_sums;
+  const bool use_ssim = c->refine_w_ssim > 0.0f;
+  const bool use_proxy = c->refine_proxy && c->refine_w_proxy > 0.0f;
   JXG_CUDA(c, cudaMemsetAsync(sums, 0, 4 * kRefineSlots * sizeof(double), s));
+  if (use_proxy) JXG_CUDA(c, cudaMemsetAsync(psums, 0, kProxySums * kRefineSlots * sizeof(double), s));
   const unsigned block_ctas = static_cast<unsigned>((nb + 7) / 8);
   const bool epf = r.epf_stages > 0;
   if ((epf && (st = launch(c, "k_refine_sigma", timed, [&] {
@@ -2166,8 +2225,11 @@ int32_t jxg_refine_eval(void* ctx, const float* theta, float rate_lambda, float*
                                                      sums + 3 * kRefineSlots);
        })))
     return st;
+  // the decoded XYB the distortion sees: after the EPF, or the padded recon
+  const float* dec = r.recon;
+  int64_t dec_plane = pp;
+  int dec_stride = r.pw;
   if (epf) {
-    const int64_t pp = static_cast<int64_t>(r.pw) * r.yb * 8;
     for (int k = 0; k < r.epf_stages; ++k) {
       const float* in = k == 0 ? r.recon : c->refine_epf_out[k - 1];
       const int64_t plane = k == 0 ? pp : n;
@@ -2180,47 +2242,101 @@ int32_t jxg_refine_eval(void* ctx, const float* theta, float rate_lambda, float*
            })))
         return st;
     }
-    if ((st = launch(c, "k_refine_linear", timed, [&] {
-           k_refine_linear<<<refine_grid(n), 256, 0, s>>>(c->refine_epf_out[r.epf_stages - 1], n, r.w,
-                                                          c->refine_lin[1][0], r.w, r.h);
-         })))
+    dec = c->refine_epf_out[r.epf_stages - 1];
+    dec_plane = n;
+    dec_stride = r.w;
+    if (use_ssim && (st = launch(c, "k_refine_linear", timed, [&] {
+                       k_refine_linear<<<refine_grid(n), 256, 0, s>>>(dec, n, r.w, c->refine_lin[1][0], r.w, r.h);
+                     })))
       return st;
   }
-  for (int k = 1; k < 3; ++k)
-    if (c->refine_n[k] && (st = launch(c, "k_refine_down", timed, [&] {
-                             k_refine_down<<<refine_grid(3 * c->refine_n[k]), 256, 0, s>>>(
-                                 c->refine_lin[1][k - 1], c->refine_lin[1][k], c->refine_w[k - 1], c->refine_h[k - 1]);
-                           })))
-      return st;
-  for (int k = 0; k < 3; ++k) {
-    const int64_t nk = c->refine_n[k];
-    if (!nk) continue;
-    const int w = c->refine_w[k], h = c->refine_h[k];
-    // L_k = sum(1 - SSIM) / (3 channels * pixels * 3 scales)
-    const float weight = static_cast<float>(1.0 / (9.0 * static_cast<double>(nk)));
-    const dim3 grid(static_cast<unsigned>((w + kSsimTW - 1) / kSsimTW), static_cast<unsigned>((h + kSsimTH - 1) / kSsimTH),
-                    3);
-    if ((st = launch(c, "k_refine_ssim", timed, [&] {
-           k_refine_ssim<<<grid, 256, 0, s>>>(c->refine_lin[0][k], c->refine_lin[1][k], w, h, weight,
-                                              c->refine_glin[k], sums + k * kRefineSlots);
-         })))
-      return st;
+  if (use_ssim) {
+    for (int k = 1; k < 3; ++k)
+      if (c->refine_n[k] && (st = launch(c, "k_refine_down", timed, [&] {
+                               k_refine_down<<<refine_grid(3 * c->refine_n[k]), 256, 0, s>>>(
+                                   c->refine_lin[1][k - 1], c->refine_lin[1][k], c->refine_w[k - 1],
+                                   c->refine_h[k - 1]);
+                             })))
+        return st;
+    for (int k = 0; k < 3; ++k) {
+      const int64_t nk = c->refine_n[k];
+      if (!nk) continue;
+      const int w = c->refine_w[k], h = c->refine_h[k];
+      // L_k = w_ssim sum(1 - SSIM) / (3 channels * pixels * 3 scales)
+      const float weight = static_cast<float>(c->refine_w_ssim / (9.0 * static_cast<double>(nk)));
+      const dim3 grid(static_cast<unsigned>((w + kSsimTW - 1) / kSsimTW),
+                      static_cast<unsigned>((h + kSsimTH - 1) / kSsimTH), 3);
+      if ((st = launch(c, "k_refine_ssim", timed, [&] {
+             k_refine_ssim<<<grid, 256, 0, s>>>(c->refine_lin[0][k], c->refine_lin[1][k], w, h, weight,
+                                                c->refine_glin[k], sums + k * kRefineSlots);
+           })))
+        return st;
+    }
   }
+  // the luma proxy on the decoded Y plane
+  const float* dec_y = dec + dec_plane;
+  auto& PH = c->refine_pl[0];
+  auto& PQ = c->refine_pl[1];
+  const int64_t npairs = static_cast<int64_t>(r.h) * (r.w - 1) + static_cast<int64_t>(r.h - 1) * r.w;
+  if (use_proxy &&
+      (st = launch(c, "k_refine_proxy", timed, [&] {
+         k_proxy_half<<<refine_grid(static_cast<int64_t>(PH.w) * PH.h), 256, 0, s>>>(dec_y, dec_stride, r.w, r.h, 1,
+                                                                                     PH.vals);
+         k_proxy_half<<<refine_grid(static_cast<int64_t>(PQ.w) * PQ.h), 256, 0, s>>>(PH.vals, PH.w, PH.w, PH.h, 0,
+                                                                                     PQ.vals);
+         for (int l = 0; l < 2; ++l) {
+           auto& L = c->refine_pl[l];
+           const int64_t m = static_cast<int64_t>(L.w) * L.h;
+           k_proxy_box_v<<<refine_grid(m), 256, 0, s>>>(L.vals, L.ref_vals, L.w, L.h, L.tmp);
+           k_proxy_box_h<<<refine_grid(3 * m), 256, 0, s>>>(L.tmp, 3, L.w, L.h, L.box);
+           k_proxy_pool<<<refine_grid(m), 256, 0, s>>>(L.ref_mv, L.box, m, L.s, L.parts,
+                                                       psums + 2 * l * kRefineSlots);
+         }
+         k_proxy_gradients<<<refine_grid(n), 256, 0, s>>>(c->refine_src_y, dec_y, dec_stride, r.w, r.h,
+                                                          psums + 4 * kRefineSlots);
+       })))
+    return st;
   const float rate_weight = static_cast<float>(static_cast<double>(rate_lambda) / static_cast<double>(n));
   if (grad) {
-    if (c->refine_n[2] && (st = launch(c, "k_refine_up_add", timed, [&] {
-                             k_refine_up_add<<<refine_grid(3 * c->refine_n[1]), 256, 0, s>>>(
-                                 c->refine_glin[2], c->refine_glin[1], c->refine_w[1], c->refine_h[1]);
-                           })))
+    if (use_ssim && c->refine_n[2] && (st = launch(c, "k_refine_up_add", timed, [&] {
+                                         k_refine_up_add<<<refine_grid(3 * c->refine_n[1]), 256, 0, s>>>(
+                                             c->refine_glin[2], c->refine_glin[1], c->refine_w[1], c->refine_h[1]);
+                                       })))
       return st;
     const float* gx = nullptr;
-    if (epf) {
-      // back through XYB -> linear at the filtered values, then each stage
+    if (epf || use_proxy || !use_ssim) {
+      // the decoded-XYB gradient as planes: SSIM's through XYB -> linear,
+      // plus the proxy's on Y, then back through each EPF stage
       int cur = 0;
-      if ((st = launch(c, "k_refine_linear_adjoint", timed, [&] {
-             k_refine_linear_adjoint<<<refine_grid(n), 256, 0, s>>>(
-                 c->refine_epf_out[r.epf_stages - 1], c->refine_glin[0], c->refine_glin[1], r.w, r.h,
-                 c->refine_w[1], c->refine_h[1], c->refine_epf_g[cur]);
+      float* g = c->refine_epf_g[cur];
+      if (use_ssim) {
+        if ((st = launch(c, "k_refine_linear_adjoint", timed, [&] {
+               k_refine_linear_adjoint<<<refine_grid(n), 256, 0, s>>>(dec, dec_plane, dec_stride, c->refine_glin[0],
+                                                                      c->refine_glin[1], r.w, r.h, c->refine_w[1],
+                                                                      c->refine_h[1], g);
+             })))
+          return st;
+      } else {
+        JXG_CUDA(c, cudaMemsetAsync(g, 0, 3 * n * sizeof(float), s));
+      }
+      if (use_proxy &&
+          (st = launch(c, "k_refine_proxy_adjoint", timed, [&] {
+             const double n2 = static_cast<double>(PH.w) * PH.h, n4 = static_cast<double>(PQ.w) * PQ.h;
+             k_proxy_finalize<<<1, 32, 0, s>>>(psums, n2, n4, static_cast<double>(npairs), c->refine_w_proxy,
+                                               c->refine_proxy_k);
+             for (int l = 0; l < 2; ++l) {
+               auto& L = c->refine_pl[l];
+               const int64_t m = static_cast<int64_t>(L.w) * L.h;
+               k_proxy_pool_grad<<<refine_grid(m), 256, 0, s>>>(L.s, L.parts, m, c->refine_proxy_k, l, L.g);
+               k_proxy_box_adjoint_h<<<refine_grid(3 * m), 256, 0, s>>>(L.g, L.w, L.h, L.gtmp);
+               cudaMemsetAsync(L.gv, 0, m * sizeof(float), s);
+               k_proxy_box_adjoint_v<<<refine_grid(m), 256, 0, s>>>(L.gtmp, L.vals, L.ref_vals, L.w, L.h, L.gv);
+             }
+             k_proxy_up<<<refine_grid(static_cast<int64_t>(PH.w) * PH.h), 256, 0, s>>>(PQ.gv, PQ.w, PQ.h, PH.gv,
+                                                                                        PH.w, PH.h, PH.w);
+             k_proxy_up<<<refine_grid(n), 256, 0, s>>>(PH.gv, PH.w, PH.h, g + n, r.w, r.h, r.w);
+             k_proxy_gradients_adjoint<<<refine_grid(n), 256, 0, s>>>(c->refine_src_y, dec_y, dec_stride, r.w, r.h,
+                                                                      c->refine_proxy_k, g + n, r.w);
            })))
         return st;
       for (int k = r.epf_stages - 1; k >= 0; --k) {
@@ -2240,19 +2356,49 @@ int32_t jxg_refine_eval(void* ctx, const float* theta, float rate_lambda, float*
          })))
       return st;
   }
-  double host[4 * kRefineSlots];
+  double host[4 * kRefineSlots], phost[kProxySums * kRefineSlots];
   JXG_CUDA(c, cudaMemcpyAsync(host, sums, sizeof(host), cudaMemcpyDeviceToHost, s));
+  if (use_proxy) JXG_CUDA(c, cudaMemcpyAsync(phost, psums, sizeof(phost), cudaMemcpyDeviceToHost, s));
   if (levels) JXG_CUDA(c, cudaMemcpyAsync(levels, dlev, nb * 192 * 4, cudaMemcpyDeviceToHost, s));
   if ((st = wait(c))) return st;
   double total[4] = {0.0, 0.0, 0.0, 0.0};
   for (int q = 0; q < 4; ++q)
     for (int k = 0; k < kRefineSlots; ++k) total[q] += host[q * kRefineSlots + k];
   double dist = 0.0;
-  for (int k = 0; k < 3; ++k)
-    if (c->refine_n[k]) dist += total[k] / (9.0 * static_cast<double>(c->refine_n[k]));
+  if (use_ssim)
+    for (int k = 0; k < 3; ++k)
+      if (c->refine_n[k]) dist += c->refine_w_ssim * total[k] / (9.0 * static_cast<double>(c->refine_n[k]));
+  if (use_proxy) {
+    double t[kProxySums];
+    for (int q = 0; q < kProxySums; ++q) {
+      t[q] = 0.0;
+      for (int k = 0; k < kRefineSlots; ++k) t[q] += phost[q * kRefineSlots + k];
+    }
+    const double n2 = static_cast<double>(PH.w) * PH.h, n4 = static_cast<double>(PQ.w) * PQ.h;
+    const double np = static_cast<double>(npairs);
+    // src/epf_proxy.rs:181-199 (the weights, as kProxyWeights)
+    static const double kW[6] = {109.4163228369586, 4.685925102200196, 2.491781270704224,
+                                 2.167275675983448, 4.55227651921194,  2.847714678987977};
+    const double terms[6] = {t[2] / n4, t[0] / n2, std::sqrt(std::sqrt(t[1] / n2)), t[4] / np, t[5] / np,
+                             std::sqrt(std::sqrt(t[6] / np))};
+    double proxy = 0.0;
+    for (int k = 0; k < 6; ++k) proxy += kW[k] * terms[k];
+    dist += c->refine_w_proxy * proxy;
+  }
   loss3[0] = dist + static_cast<double>(rate_lambda) * total[3] / static_cast<double>(n);
   loss3[1] = dist;
   loss3[2] = total[3];
+  return JXG_OK;
+}
+
+int32_t jxg_refine_set_weights(void* ctx, float ssim_weight, float proxy_weight) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c) return JXG_ERR_INVALID_ARGUMENT;
+  if (!std::isfinite(ssim_weight) || !std::isfinite(proxy_weight) || ssim_weight < 0.0f || proxy_weight < 0.0f ||
+      (ssim_weight == 0.0f && proxy_weight == 0.0f))
+    return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "weights finite, non-negative and not both zero");
+  c->refine_w_ssim = ssim_weight;
+  c->refine_w_proxy = proxy_weight;
   return JXG_OK;
 }
 

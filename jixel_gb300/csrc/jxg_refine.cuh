@@ -228,11 +228,15 @@ __device__ __forceinline__ void xyb_to_linear(float x, float y, float b, float* 
 // A CTA's sum of one quantity into its slot: each thread's partial (a few
 // terms) and the warp's tree in FP32, the warps' sums and the slot in FP64
 // (GB300's FP64 pipe is narrow: no per-term FP64 work).
+// Every thread of the CTA calls it; calls may follow one another (the
+// barrier first keeps a call's writes of `part` after the previous call's
+// read).
 __device__ __forceinline__ void refine_add_slot(float v, double* sums) {
   __shared__ double part[8];
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
   const int nw = blockDim.x >> 5;
+  __syncthreads();
   if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = static_cast<double>(v);
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -487,11 +491,11 @@ __global__ void __launch_bounds__(256) k_refine_epf_adjoint(const RefineArgs r, 
   for (int c = 0; c < 3; ++c) gin[c * n + q] = g[c];
 }
 
-// The gradient by the filtered XYB planes (w x h): scale 0's linear-plane
+// The gradient by the decoded XYB planes (w x h): scale 0's linear-plane
 // gradient plus a quarter of scale 1's, back through XYB -> linear at the
-// filtered values.
-__global__ void __launch_bounds__(256) k_refine_linear_adjoint(const float* __restrict__ xyb,
-                                                               const float* __restrict__ glin0,
+// decoded values (`xyb`: planes `xyb_plane` apart, rows `xyb_stride`).
+__global__ void __launch_bounds__(256) k_refine_linear_adjoint(const float* __restrict__ xyb, int64_t xyb_plane,
+                                                               int xyb_stride, const float* __restrict__ glin0,
                                                                const float* __restrict__ glin1, int w, int h,
                                                                int w1, int h1, float* __restrict__ gxyb) {
   const int64_t n = static_cast<int64_t>(w) * h, n1 = static_cast<int64_t>(w1) * h1;
@@ -507,7 +511,8 @@ __global__ void __launch_bounds__(256) k_refine_linear_adjoint(const float* __re
     for (int k = 0; k < 3; ++k) gl[k] = __fmaf_rn(0.25f, glin1[k * n1 + q1], gl[k]);
   }
   float o[3], dc[3];
-  xyb_to_linear(xyb[q], xyb[n + q], xyb[2 * n + q], o, dc);
+  const int64_t at = static_cast<int64_t>(y) * xyb_stride + x;
+  xyb_to_linear(xyb[at], xyb[xyb_plane + at], xyb[2 * xyb_plane + at], o, dc);
   float gm[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k)
@@ -815,6 +820,296 @@ __global__ void __launch_bounds__(256) k_refine_backward(const RefineArgs r, con
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
   if (lane == 0) gtheta[b] = __fmul_rn(acc, s);  // ds / dtheta = s
+}
+
+// ---------------------------------------------------------------------------
+// The reference's six-term luma proxy as a distortion term (LumaProxy,
+// src/epf_proxy.rs:132-214; box moments src/epf_proxy/box_filter.rs:84-240;
+// pool and gradients src/epf_proxy/row_kernels.rs:60-115), on the decoded
+// XYB Y plane against the source's, with its adjoint.  The box sums are
+// direct 5-tap sums (the reference streams running sums: the same values to
+// rounding) and the pools are parallel sums.
+// ---------------------------------------------------------------------------
+
+// src/epf_proxy.rs:186-193
+__constant__ const float kProxyWeights[6] = {109.4163228369586f, 4.685925102200196f, 2.491781270704224f,
+                                             2.167275675983448f, 4.55227651921194f,  2.847714678987977f};
+constexpr int kProxySums = 7;  // half s, half s^4, quarter s, quarter s^4, error, excess, loss^4
+
+__device__ __forceinline__ int proxy_mirror(int i, int n) {  // src/epf_proxy.rs:17-28
+  if (i >= 0 && i < n) return i;
+  i %= 2 * n;
+  if (i < 0) i += 2 * n;
+  return i < n ? i : 2 * n - i - 1;
+}
+
+// 2x2 means (half / half_y, row_kernels.rs:60-71), +0.01 a tap with `bias`.
+__global__ void __launch_bounds__(256) k_proxy_half(const float* __restrict__ in, int in_stride, int w, int h,
+                                                    int bias, float* __restrict__ out) {
+  const int w2 = w / 2, h2 = h / 2;
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= static_cast<int64_t>(w2) * h2) return;
+  const int x = static_cast<int>(q % w2), y = static_cast<int>(q / w2);
+  const float* r0 = in + static_cast<int64_t>(2 * y) * in_stride + 2 * x;
+  const float* r1 = r0 + in_stride;
+  const float b = bias ? 0.01f : 0.0f;
+  float t00 = r0[0], t01 = r0[1], t10 = r1[0], t11 = r1[1];
+  if (bias) {
+    t00 = __fadd_rn(t00, b);
+    t01 = __fadd_rn(t01, b);
+    t10 = __fadd_rn(t10, b);
+    t11 = __fadd_rn(t11, b);
+  }
+  out[q] = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(t00, t10), t01), t11));
+}
+
+// Vertical pass of the reflected 5x5 box (x 0.2) of t, t^2 and, with `ref`,
+// ref * t: `count` planes of w x h into `out`.
+__global__ void __launch_bounds__(256) k_proxy_box_v(const float* __restrict__ t, const float* __restrict__ ref,
+                                                     int w, int h, float* __restrict__ out) {
+  const int64_t n = static_cast<int64_t>(w) * h;
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int x = static_cast<int>(q % w), y = static_cast<int>(q / w);
+  float m = 0.0f, sq = 0.0f, cr = 0.0f;
+#pragma unroll
+  for (int d = -2; d <= 2; ++d) {
+    const int64_t at = static_cast<int64_t>(proxy_mirror(y + d, h)) * w + x;
+    const float v = t[at];
+    m = __fadd_rn(m, v);
+    sq = __fadd_rn(sq, __fmul_rn(v, v));
+    if (ref) cr = __fadd_rn(cr, __fmul_rn(ref[at], v));
+  }
+  out[q] = __fmul_rn(m, 0.2f);
+  out[n + q] = __fmul_rn(sq, 0.2f);
+  if (ref) out[2 * n + q] = __fmul_rn(cr, 0.2f);
+}
+
+// Horizontal pass (x 0.2) of `count` planes.
+__global__ void __launch_bounds__(256) k_proxy_box_h(const float* __restrict__ in, int count, int w, int h,
+                                                     float* __restrict__ out) {
+  const int64_t n = static_cast<int64_t>(w) * h;
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= n * count) return;
+  const int64_t c = q / n, p = q % n;
+  const int x = static_cast<int>(p % w), y = static_cast<int>(p / w);
+  const float* row = in + c * n + static_cast<int64_t>(y) * w;
+  float s = 0.0f;
+#pragma unroll
+  for (int d = -2; d <= 2; ++d) s = __fadd_rn(s, row[proxy_mirror(x + d, w)]);
+  out[q] = __fmul_rn(s, 0.2f);
+}
+
+// The source level's variance max(E[t^2] - mean^2, 0) (variance,
+// row_kernels.rs:81-85), in place of the box's second plane.
+__global__ void __launch_bounds__(256) k_proxy_variance(float* __restrict__ moments, int64_t n) {
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const float m = moments[q];
+  moments[n + q] = fmaxf(__fsub_rn(moments[n + q], __fmul_rn(m, m)), 0.0f);
+}
+
+// The per-pixel structure loss s (pool, row_kernels.rs:86-103) of the test
+// moments against the source's mean and variance; s and s^4 summed into two
+// slot sets; the partial derivatives of s by the test mean, E[t^2] and
+// E[ref t] into `parts` (3 planes).
+__global__ void __launch_bounds__(256) k_proxy_pool(const float* __restrict__ ref_mv, const float* __restrict__ box,
+                                                    int64_t n, float* __restrict__ s_out, float* __restrict__ parts,
+                                                    double* __restrict__ sums) {
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  float sv = 0.0f, s4 = 0.0f;
+  if (q < n) {
+    const float a = ref_mv[q], vr = ref_mv[n + q];
+    const float b = box[q], sq = box[n + q], cross = box[2 * n + q];
+    const float vraw = __fsub_rn(sq, __fmul_rn(b, b));
+    const float var = fmaxf(vraw, 0.0f);
+    const bool cov_on = !(vr == 0.0f || var == 0.0f);
+    const float cov = cov_on ? __fsub_rn(cross, __fmul_rn(a, b)) : 0.0f;
+    const float dab = __fsub_rn(a, b);
+    const float e1 = __fsub_rn(1.0f, __fmul_rn(dab, dab));
+    const float num = __fadd_rn(__fmul_rn(2.0f, cov), 0.0009f);
+    const float den = __fadd_rn(__fadd_rn(vr, var), 0.0009f);
+    const float raw = __fsub_rn(1.0f, __fdiv_rn(__fmul_rn(e1, num), den));
+    sv = fmaxf(raw, 0.0f);
+    float pb = 0.0f, psq = 0.0f, pc = 0.0f;
+    if (raw > 0.0f) {
+      // s = 1 - e1 N / D: ds = -(de1 N / D + e1 dN / D - e1 N dD / D^2)
+      const float inv_d = __fdiv_rn(1.0f, den);
+      const float ratio = __fmul_rn(__fmul_rn(e1, num), __fmul_rn(inv_d, inv_d));  // e1 N / D^2
+      const float dvar_on = vraw > 0.0f ? 1.0f : 0.0f;
+      // d/db: de1 = 2 (a - b), dN = -2a (cov on), dD = -2b (var on)
+      pb = -(__fmul_rn(__fmul_rn(2.0f, dab), __fmul_rn(num, inv_d)) +
+             (cov_on ? __fmul_rn(e1, __fmul_rn(-2.0f * a, inv_d)) : 0.0f) -
+             __fmul_rn(ratio, __fmul_rn(-2.0f * b, dvar_on)));
+      psq = __fmul_rn(ratio, dvar_on);                                  // dD/dsq = 1
+      pc = cov_on ? -__fmul_rn(e1, __fmul_rn(2.0f, inv_d)) : 0.0f;     // dN/dcross = 2
+    }
+    s_out[q] = sv;
+    parts[q] = pb;
+    parts[n + q] = psq;
+    parts[2 * n + q] = pc;
+    const float s2 = __fmul_rn(sv, sv);
+    s4 = __fmul_rn(__fmul_rn(s2, sv), sv);
+  }
+  refine_add_slot(sv, sums);
+  refine_add_slot(s4, sums + kRefineSlots);
+}
+
+// The full-resolution gradient terms (src/epf_proxy.rs:216-247): each pixel
+// takes its pairs with the right and the lower neighbour.
+__device__ __forceinline__ float proxy_pair(float a, float b, float* err, float* exc) {
+  *err = fabsf(__fsub_rn(b, a));
+  *exc = fmaxf(__fsub_rn(fabsf(b), fabsf(a)), 0.0f);
+  const float l = fmaxf(__fsub_rn(fabsf(a), fabsf(b)), 0.0f);
+  const float l2 = __fmul_rn(l, l);
+  return __fmul_rn(__fmul_rn(l2, l), l);
+}
+__global__ void __launch_bounds__(256) k_proxy_gradients(const float* __restrict__ src, const float* __restrict__ test,
+                                                         int test_stride, int w, int h, double* __restrict__ sums) {
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  float err = 0.0f, exc = 0.0f, l4 = 0.0f;
+  if (q < static_cast<int64_t>(w) * h) {
+    const int x = static_cast<int>(q % w), y = static_cast<int>(q / w);
+    const float s0 = src[q], t0 = test[static_cast<int64_t>(y) * test_stride + x];
+    float e, x2;
+    if (x + 1 < w) {
+      l4 = __fadd_rn(l4, proxy_pair(__fsub_rn(src[q + 1], s0),
+                                    __fsub_rn(test[static_cast<int64_t>(y) * test_stride + x + 1], t0), &e, &x2));
+      err = __fadd_rn(err, e);
+      exc = __fadd_rn(exc, x2);
+    }
+    if (y + 1 < h) {
+      l4 = __fadd_rn(l4, proxy_pair(__fsub_rn(src[q + w], s0),
+                                    __fsub_rn(test[static_cast<int64_t>(y + 1) * test_stride + x], t0), &e, &x2));
+      err = __fadd_rn(err, e);
+      exc = __fadd_rn(exc, x2);
+    }
+  }
+  refine_add_slot(err, sums);
+  refine_add_slot(exc, sums + kRefineSlots);
+  refine_add_slot(l4, sums + 2 * kRefineSlots);
+}
+
+// The scalars the adjoint needs, from the slot sums: per level the weight of
+// a pixel's s and of its s^3 (the 4th-root pool), and the gradient terms'.
+struct ProxyScalars {
+  float g_s[2], g_s3[2];   // half, quarter
+  float g_err, g_exc, g_l3;
+};
+__global__ void k_proxy_finalize(const double* __restrict__ sums, double n2, double n4, double npairs,
+                                 float weight, ProxyScalars* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double t[kProxySums];
+  for (int k = 0; k < kProxySums; ++k) {
+    t[k] = 0.0;
+    for (int j = 0; j < kRefineSlots; ++j) t[k] += sums[k * kRefineSlots + j];
+  }
+  // terms: qs0 = S_q / n4 (w 0), hs0 = S_h / n2 (w 1), hs1 = (S4_h / n2)^(1/4) (w 2),
+  // error / np (w 3), excess / np (w 4), (L4 / np)^(1/4) (w 5)
+  const double f_h = t[1] / n2;
+  out->g_s[0] = static_cast<float>(weight * kProxyWeights[1] / n2);
+  out->g_s3[0] = f_h > 0.0 ? static_cast<float>(weight * kProxyWeights[2] / (n2 * pow(f_h, 0.75))) : 0.0f;
+  out->g_s[1] = static_cast<float>(weight * kProxyWeights[0] / n4);
+  out->g_s3[1] = 0.0f;
+  out->g_err = static_cast<float>(weight * kProxyWeights[3] / npairs);
+  out->g_exc = static_cast<float>(weight * kProxyWeights[4] / npairs);
+  const double f_l = t[6] / npairs;
+  out->g_l3 = f_l > 0.0 ? static_cast<float>(weight * kProxyWeights[5] / (npairs * pow(f_l, 0.75))) : 0.0f;
+}
+
+// d L / d (test mean, E[t^2], E[ref t]) of one level: gs times the parts.
+__global__ void __launch_bounds__(256) k_proxy_pool_grad(const float* __restrict__ s_map, const float* __restrict__ parts,
+                                                         int64_t n, const ProxyScalars* __restrict__ k, int level,
+                                                         float* __restrict__ g) {
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const float sv = s_map[q];
+  const float gs = __fadd_rn(k->g_s[level], __fmul_rn(k->g_s3[level], __fmul_rn(__fmul_rn(sv, sv), sv)));
+#pragma unroll
+  for (int c = 0; c < 3; ++c) g[c * n + q] = __fmul_rn(gs, parts[c * n + q]);
+}
+
+// The adjoint of one reflected 5-tap pass (x 0.2) along x (dir 0) or y (1):
+// g_in(j) = 0.2 sum over outputs o and taps d with mirror(o + d) = j.
+__device__ __forceinline__ float proxy_box_adjoint_1d(const float* __restrict__ g, int j, int n, int64_t step) {
+  float acc = 0.0f;
+  if (j >= 2 && j < n - 2) {
+#pragma unroll
+    for (int d = -2; d <= 2; ++d) acc = __fadd_rn(acc, g[static_cast<int64_t>(j - d) * step]);
+    return __fmul_rn(acc, 0.2f);
+  }
+  // near an edge: every output within 4 whose taps reflect onto j
+  for (int o = j - 4 < 0 ? 0 : j - 4; o <= j + 4 && o < n; ++o)
+#pragma unroll
+    for (int d = -2; d <= 2; ++d)
+      if (proxy_mirror(o + d, n) == j) acc = __fadd_rn(acc, g[static_cast<int64_t>(o) * step]);
+  return __fmul_rn(acc, 0.2f);
+}
+__global__ void __launch_bounds__(256) k_proxy_box_adjoint_h(const float* __restrict__ g, int w, int h,
+                                                             float* __restrict__ out) {
+  const int64_t n = static_cast<int64_t>(w) * h;
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= 3 * n) return;
+  const int64_t c = q / n, p = q % n;
+  const int x = static_cast<int>(p % w), y = static_cast<int>(p / w);
+  out[q] = proxy_box_adjoint_1d(g + c * n + static_cast<int64_t>(y) * w, x, w, 1);
+}
+// ... then the vertical adjoint, and the test plane's gradient:
+// g_t = A(g_mean) + 2 t A(g_sq) + ref A(g_cross), added to `gt`.
+__global__ void __launch_bounds__(256) k_proxy_box_adjoint_v(const float* __restrict__ g, const float* __restrict__ t,
+                                                             const float* __restrict__ ref, int w, int h,
+                                                             float* __restrict__ gt) {
+  const int64_t n = static_cast<int64_t>(w) * h;
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int x = static_cast<int>(q % w), y = static_cast<int>(q / w);
+  const float am = proxy_box_adjoint_1d(g + x, y, h, w);
+  const float asq = proxy_box_adjoint_1d(g + n + x, y, h, w);
+  const float acr = proxy_box_adjoint_1d(g + 2 * n + x, y, h, w);
+  gt[q] = __fadd_rn(gt[q], __fmaf_rn(ref[q], acr, __fmaf_rn(__fmul_rn(2.0f, t[q]), asq, am)));
+}
+
+// A level's gradient into the finer level: each of the four pixels under a
+// coarse pixel takes a quarter (the +0.01 bias is a constant).
+__global__ void __launch_bounds__(256) k_proxy_up(const float* __restrict__ gc, int wc, int hc,
+                                                  float* __restrict__ gf, int wf, int hf, int f_stride) {
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= static_cast<int64_t>(wf) * hf) return;
+  const int x = static_cast<int>(q % wf), y = static_cast<int>(q / wf);
+  if ((x >> 1) >= wc || (y >> 1) >= hc) return;
+  float* at = gf + static_cast<int64_t>(y) * f_stride + x;
+  *at = __fadd_rn(*at, __fmul_rn(0.25f, gc[static_cast<int64_t>(y >> 1) * wc + (x >> 1)]));
+}
+
+// The gradient terms' adjoint at each test pixel (the pairs it belongs to),
+// added to `gt` (row stride `g_stride`).
+__device__ __forceinline__ float proxy_pair_grad(float a, float b, const ProxyScalars& k) {
+  // d/db of g_err |b - a| + g_exc max(|b| - |a|, 0) + (L4 pool) max(|a| - |b|, 0)^4
+  float g = __fmul_rn(k.g_err, b > a ? 1.0f : (b < a ? -1.0f : 0.0f));
+  const float sb = b > 0.0f ? 1.0f : (b < 0.0f ? -1.0f : 0.0f);
+  if (fabsf(b) > fabsf(a)) g = __fadd_rn(g, __fmul_rn(k.g_exc, sb));
+  const float l = __fsub_rn(fabsf(a), fabsf(b));
+  if (l > 0.0f) g = __fsub_rn(g, __fmul_rn(k.g_l3, __fmul_rn(__fmul_rn(l, l), __fmul_rn(l, sb))));
+  return g;
+}
+__global__ void __launch_bounds__(256) k_proxy_gradients_adjoint(const float* __restrict__ src,
+                                                                 const float* __restrict__ test, int test_stride,
+                                                                 int w, int h, const ProxyScalars* __restrict__ ks,
+                                                                 float* __restrict__ gt, int g_stride) {
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= static_cast<int64_t>(w) * h) return;
+  const ProxyScalars k = *ks;
+  const int x = static_cast<int>(q % w), y = static_cast<int>(q / w);
+  auto T = [&](int xx, int yy) { return test[static_cast<int64_t>(yy) * test_stride + xx]; };
+  auto S = [&](int xx, int yy) { return src[static_cast<int64_t>(yy) * w + xx]; };
+  float g = 0.0f;
+  // b = t(right) - t(here): d b / d t(here) = -1, as the right member +1
+  if (x + 1 < w) g = __fsub_rn(g, proxy_pair_grad(__fsub_rn(S(x + 1, y), S(x, y)), __fsub_rn(T(x + 1, y), T(x, y)), k));
+  if (x > 0) g = __fadd_rn(g, proxy_pair_grad(__fsub_rn(S(x, y), S(x - 1, y)), __fsub_rn(T(x, y), T(x - 1, y)), k));
+  if (y + 1 < h) g = __fsub_rn(g, proxy_pair_grad(__fsub_rn(S(x, y + 1), S(x, y)), __fsub_rn(T(x, y + 1), T(x, y)), k));
+  if (y > 0) g = __fadd_rn(g, proxy_pair_grad(__fsub_rn(S(x, y), S(x, y - 1)), __fsub_rn(T(x, y), T(x, y - 1)), k));
+  float* at = gt + static_cast<int64_t>(y) * g_stride + x;
+  *at = __fadd_rn(*at, g);
 }
 
 // The refined field: qf * exp(theta), rounded, 1..255.

@@ -33,6 +33,57 @@ EPF_STAGES = {  # (dx, dy) directions and neighbours (direction, along), the dec
     2: ([(1, 0), (0, 1)], [(1, 0), (0, 0), (0, 1), (1, 1)], False),
 }
 EPF_INV_SIGMA_NUM, EPF_MIN_SIGMA = -1.1715729, -3.905243
+PROXY_WEIGHTS = [109.4163228369586, 4.685925102200196, 2.491781270704224, 2.167275675983448,
+                 4.55227651921194, 2.847714678987977]
+
+
+def proxy_mirror(i, n):
+    if 0 <= i < n:
+        return i
+    i %= 2 * n
+    return i if i < n else 2 * n - i - 1
+
+
+def proxy_half(t, bias):
+    h2, w2 = t.shape[0] // 2, t.shape[1] // 2
+    a = t[: 2 * h2, : 2 * w2]
+    b = 0.01 if bias else 0.0
+    t00, t01, t10, t11 = a[0::2, 0::2] + b, a[0::2, 1::2] + b, a[1::2, 0::2] + b, a[1::2, 1::2] + b
+    return 0.25 * (((t00 + t10) + t01) + t11)
+
+
+def proxy_box(t):
+    """The reflected 5x5 box mean (direct sums)."""
+    h, w = t.shape
+    ys = torch.tensor([[proxy_mirror(y + d, h) for d in range(-2, 3)] for y in range(h)])
+    xs = torch.tensor([[proxy_mirror(x + d, w) for d in range(-2, 3)] for x in range(w)])
+    v = t[ys].sum(1) * 0.2          # (h, w)
+    return v[:, xs].sum(2) * 0.2    # (h, w)
+
+
+def proxy_level(ref, test):
+    a, vr = proxy_box(ref), torch.clamp(proxy_box(ref * ref) - proxy_box(ref) ** 2, min=0.0)
+    b, sq, cross = proxy_box(test), proxy_box(test * test), proxy_box(ref * test)
+    var = torch.clamp(sq - b * b, min=0.0)
+    cov = torch.where((vr == 0) | (var == 0), torch.zeros_like(var), cross - a * b)
+    s = torch.clamp(1.0 - (1.0 - (a - b) ** 2) * (2.0 * cov + 0.0009) / (vr + var + 0.0009), min=0.0)
+    return s.mean(), (s ** 4).mean() ** 0.25
+
+
+def luma_proxy(src, y):
+    """The reference's six-term luma proxy in FP64 (src/epf_proxy.rs:132-214)."""
+    hs, hy = proxy_half(src, True), proxy_half(y, True)
+    qs, qy = proxy_half(hs, False), proxy_half(hy, False)
+    h_mean, h_fourth = proxy_level(hs, hy)
+    q_mean, _ = proxy_level(qs, qy)
+    a = torch.cat([(src[:, 1:] - src[:, :-1]).reshape(-1), (src[1:] - src[:-1]).reshape(-1)])
+    b = torch.cat([(y[:, 1:] - y[:, :-1]).reshape(-1), (y[1:] - y[:-1]).reshape(-1)])
+    n = a.numel()
+    err = (b - a).abs().sum() / n
+    exc = torch.clamp(b.abs() - a.abs(), min=0.0).sum() / n
+    l4 = (torch.clamp(a.abs() - b.abs(), min=0.0) ** 4).sum() / n
+    terms = [q_mean, h_mean, h_fourth, err, exc, l4 ** 0.25]
+    return sum(w * t for w, t in zip(PROXY_WEIGHTS, terms))
 
 
 def mirror(i, n):
@@ -86,6 +137,8 @@ class Fp64Model:
         tiles = (by >> 3, bx >> 3)
         self.xf = torch.tensor(res.ytox[tiles].astype(np.float64) / 84.0)
         self.bf = torch.tensor(1.0 + res.ytob[tiles].astype(np.float64) / 84.0)
+        self.src_y = torch.tensor(res.xyb[1].astype(np.float64))
+        self.weights = (1.0, 0.0)  # ssim, proxy
         self.src = [self._linear(torch.tensor(res.xyb.astype(np.float64)))]
         for _ in range(2):
             self.src.append(self._down(self.src[-1]))
@@ -221,10 +274,16 @@ class Fp64Model:
                 frozen = self._epf_weights(self.planes(self._decode(theta0, q0, offset)[0]), theta0)
             for (stage, _), wts in zip(self.epf["stages"], frozen):
                 img = self._epf_apply(img, stage, wts)
-        rec = [self._linear(img)]
-        for _ in range(2):
-            rec.append(self._down(rec[-1]))
-        dist = sum(self._ssim_loss(a, b) for a, b in zip(self.src, rec)) / 3.0
+        self.decoded = img
+        ws, wp = self.weights
+        dist = torch.zeros((), dtype=torch.float64)
+        if ws > 0:
+            rec = [self._linear(img)]
+            for _ in range(2):
+                rec.append(self._down(rec[-1]))
+            dist = dist + ws * sum(self._ssim_loss(a, b) for a, b in zip(self.src, rec)) / 3.0
+        if wp > 0:
+            dist = dist + wp * luma_proxy(self.src_y, img[1])
         return dist + lam * bits / (self.w * self.h), dist, bits
 
     def planes(self, chat):
@@ -297,8 +356,9 @@ def test_inverse_reproduces_the_source(ctx, w, h, seed):
     assert err <= 1e-5 * max(1.0, np.abs(res.xyb).max()), err
 
 
-def fp64_check(ctx, w, h, seed, lam, spread, d=1.0):
+def fp64_check(ctx, w, h, seed, lam, spread, d=1.0, weights=(1.0, 0.0)):
     img, res = begin(ctx, w, h, seed, d)
+    ctx.refine_weights(*weights)
     nb = res.quant_field.size
     rng = np.random.default_rng(seed)
     th = rng.normal(0.0, spread, nb).astype(np.float32)
@@ -308,6 +368,7 @@ def fp64_check(ctx, w, h, seed, lam, spread, d=1.0):
     (loss, dist, bits), lv = ctx.refine_eval(lam, theta.data_ptr(), grad.data_ptr(), levels=True)
     g_gpu = grad.cpu().numpy().astype(np.float64)
     model = Fp64Model(ctx, res, w, h)
+    model.weights = weights
     t64 = torch.tensor(th.astype(np.float64), requires_grad=True)
     l64, d64, b64 = model.loss(t64, t64.detach().clone(), lv, lam)
     l64.backward()
@@ -322,6 +383,7 @@ def fp64_check(ctx, w, h, seed, lam, spread, d=1.0):
     tol = 1e-3 * np.abs(g_ref).max()
     err = np.abs(g_gpu - g_ref)
     assert err.max() <= tol, (err.max(), tol, int(err.argmax()))
+    ctx.refine_weights(1.0, 0.0)
     return model, t64.detach(), lv, g_ref, lam
 
 
@@ -332,6 +394,37 @@ def test_loss_and_gradient_match_fp64(ctx, w, h, seed, lam, spread, d):
     fp64_check(ctx, w, h, seed, lam, spread, d)
     stages = len(ctx.refine_model()["epf"]["stages"])
     assert stages == {1.0: 1, 3.0: 3, 0.5: 0}[d]
+
+
+@pytest.mark.parametrize("d,weights", [(1.0, (0.0, 1.0)), (3.0, (0.5, 0.2))])
+def test_luma_proxy_loss_and_gradient_match_fp64(ctx, d, weights):
+    # the proxy alone, and mixed with 1 - SSIM, through the EPF
+    fp64_check(ctx, 80, 60, 25, 0.002, 0.2, d, weights)
+
+
+def test_luma_proxy_matches_the_oracle(ctx):
+    # the device proxy of the decoded Y plane against the restated reference
+    # (float32, the reference's sum order) of the FP64 model's decoded plane:
+    # within 5e-4 relative (the device decodes in FP32 and sums in parallel)
+    from oracle import luma_proxy as LP
+    img, res = begin(ctx, 96, 72, 26, 1.0)
+    nb = res.quant_field.size
+    th = np.random.default_rng(26).normal(0.0, 0.2, nb).astype(np.float32)
+    theta = torch.tensor(th, device="cuda")
+    torch.cuda.synchronize()
+    ctx.refine_weights(0.0, 1.0)
+    try:
+        (loss, dist, _), lv = ctx.refine_eval(0.0, theta.data_ptr(), levels=True)
+    finally:
+        ctx.refine_weights(1.0, 0.0)
+    model = Fp64Model(ctx, res, 96, 72)
+    model.weights = (0.0, 1.0)
+    t64 = torch.tensor(th.astype(np.float64))
+    model.loss(t64, t64, lv, 0.0)
+    y = model.decoded[1].numpy().astype(np.float32)
+    want, _ = LP.LumaProxy(res.xyb[1].astype(np.float32)).compare(y)
+    assert abs(dist - float(want)) <= 5e-4 * float(want), (dist, float(want))
+    assert loss == dist
 
 
 def test_fp64_gradient_is_the_surrogates_derivative(ctx):
