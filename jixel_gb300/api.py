@@ -540,13 +540,28 @@ class FrontendContext:
             return 0.0
         return max(0.0, -(d_hi - d_lo) / ((b_hi - b_lo) / pixels))
 
-    def refine(self, steps: int = 8, rate_lambda: float = 0.002, learning_rate: float = 0.05):
+    def refine(self, steps: int = 8, rate_lambda: float = 0.002, learning_rate: float = 0.05,
+               monotone: bool = True):
         """Refine the last pass's quant field: `steps` Adam steps from theta = 0.
-        Returns (field (yb, xb) uint8, losses per step before it, final loss)."""
+        With `monotone`, a step whose rounded loss is higher than the loss
+        before it is taken back and the learning rate halved (Adam restarts
+        there), so the loss never rises.  Returns (field (yb, xb) uint8,
+        the loss before each step, the final loss)."""
         self.refine_begin()
-        history = [self.refine_step(rate_lambda, learning_rate) for _ in range(steps)]
-        final, _ = self.refine_eval(rate_lambda)
-        return self.refine_field(), history, final
+        current, _ = self.refine_eval(rate_lambda)
+        history = []
+        lr = learning_rate
+        for _ in range(steps):
+            history.append(current)
+            before = self.refine_theta() if monotone else None
+            self.refine_step(rate_lambda, lr)
+            after, _ = self.refine_eval(rate_lambda)
+            if monotone and after[0] > current[0]:
+                self.refine_theta(before)
+                lr *= 0.5
+            else:
+                current = after
+        return self.refine_field(), history, current
 
     def refine_model(self) -> dict:
         """The model's constants, source coefficients, inverse transform and

@@ -444,6 +444,8 @@ def test_adam_steps_lower_the_rounded_loss(ctx):
     img, res = begin(ctx, 256, 192, 41, 1.0)
     field, history, final = ctx.refine(steps=8, rate_lambda=0.002, learning_rate=0.05)
     assert final[0] < history[0][0], (history[0], final)
+    losses = [h[0] for h in history] + [final[0]]
+    assert all(b <= a for a, b in zip(losses, losses[1:])), losses  # the monotone driver
     theta = ctx.refine_theta()
     q = res.quant_field.astype(np.float64)
     v = q * np.exp(theta.astype(np.float64))
