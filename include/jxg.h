@@ -287,6 +287,19 @@ int32_t jxg_op_gaborish_inverse(void* ctx, const float* xyb, uint64_t width, uin
  * default weights, products fused into the sums as the NEON and AVX2+FMA
  * backends do. */
 int32_t jxg_op_gaborish(void* ctx, const float* xyb, uint64_t width, uint64_t height, float* out);
+/* The decoder's edge-preserving filter (Epf::apply, src/epf_filter.rs:268-350):
+ * `xyb` 3 planes of w*h floats in, `out` the filtered planes.  `sigma_quant`
+ * holds one value per 8x8 block (xb*yb, FrameBlocks::sigma_quant: the
+ * quantizer scale x the block's field x -1.1715729); `iters` 0..3 picks the
+ * stages (1: the 4-neighbour patch stage; 2: + the single-pixel stage at
+ * `pass2`; 3: the 12-neighbour stage at `pass0` first); `quant_mul`,
+ * `border_mul` and `channel_scale` are LoopFilter's fields as the decoder
+ * reads them; `sharpness` 0..7 (0, like iters 0, leaves the planes as they
+ * are).  Products and sums round separately, as the reference's scalar
+ * backend. */
+int32_t jxg_op_epf(void* ctx, const float* xyb, uint64_t width, uint64_t height, const float* sigma_quant,
+                   int32_t iters, float quant_mul, float pass0, float pass2, float border_mul,
+                   const float* channel_scale, int32_t sharpness, float* out);
 /* DctFn<8, 8, 64> (src/dct.rs:172, scalar dct8x8 :631): `count` blocks of 64
  * row-major samples in, 64 coefficients (transposed storage, 1/64 scale) out. */
 int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coefficients);

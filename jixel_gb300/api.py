@@ -402,6 +402,22 @@ class FrontendContext:
                                               out.ctypes.data))
         return out
 
+    def epf(self, xyb: np.ndarray, sigma_quant: np.ndarray, iters: int, quant_mul: float = 0.46,
+            pass0: float = 0.9, pass2: float = 6.5, border_mul: float = 2.0 / 3.0,
+            channel_scale=(40.0, 5.0, 3.5), sharpness: int = 7) -> np.ndarray:
+        """jxg_op_epf: the decoder's edge-preserving filter over (3, h, w)
+        planes with one sigma_quant value per 8x8 block."""
+        x = np.ascontiguousarray(xyb, np.float32)
+        _, h, w = x.shape
+        sq = np.ascontiguousarray(sigma_quant, np.float32)
+        if sq.size != ((w + 7) // 8) * ((h + 7) // 8):
+            raise EncodeError(100, "one sigma_quant value per 8x8 block")
+        cs = np.ascontiguousarray(channel_scale, np.float32)
+        out = np.zeros_like(x)
+        self._check(self._lib.jxg_op_epf(self._ctx, x.ctypes.data, w, h, sq.ctypes.data, iters, quant_mul,
+                                         pass0, pass2, border_mul, cs.ctypes.data, sharpness, out.ctypes.data))
+        return out
+
     def dct8x8(self, blocks: np.ndarray) -> np.ndarray:
         blocks = np.ascontiguousarray(blocks, np.float32).reshape(-1, 64)
         out = np.zeros_like(blocks)

@@ -1627,6 +1627,78 @@ int32_t jxg_op_gaborish(void* ctx, const float* xyb, uint64_t width, uint64_t he
   return gaborish_op(ctx, xyb, width, height, out, false, 0.0f);
 }
 
+int32_t jxg_op_epf(void* ctx, const float* xyb, uint64_t width, uint64_t height, const float* sigma_quant,
+                   int32_t iters, float quant_mul, float pass0, float pass2, float border_mul,
+                   const float* channel_scale, int32_t sharpness, float* out) {
+  using namespace jxg;
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !xyb || !sigma_quant || !channel_scale || !out) return JXG_ERR_INVALID_ARGUMENT;
+  if (width == 0 || height == 0) return fail(c, JXG_ERR_EMPTY_IMAGE, "empty image");
+  if (width > kMaxDimension || height > kMaxDimension)
+    return fail(c, JXG_ERR_DIMENSION_TOO_LARGE, "dimension too large");
+  if (iters < 0 || iters > 3 || sharpness < 0 || sharpness > 7)
+    return fail(c, JXG_ERR_INVALID_ARGUMENT, "iters 0..3, sharpness 0..7");
+  cudaSetDevice(c->device);
+  const int64_t n = static_cast<int64_t>(width) * height;
+  const size_t bytes = static_cast<size_t>(n) * 3 * 4;
+  if (iters == 0 || sharpness == 0) {  // Epf::apply returns the image itself
+    std::memcpy(out, xyb, bytes);
+    return JXG_OK;
+  }
+  RefineArgs r{};
+  r.w = static_cast<int32_t>(width);
+  r.h = static_cast<int32_t>(height);
+  r.xb = static_cast<int32_t>((width + 7) / 8);
+  r.yb = static_cast<int32_t>((height + 7) / 8);
+  r.epf_border = border_mul;
+  for (int k = 0; k < 3; ++k) r.epf_channel[k] = channel_scale[k];
+  const int64_t nb = static_cast<int64_t>(r.xb) * r.yb;
+  // planes: input, two stage outputs, the largest stage's weights and centre
+  // weights; then the per-block sigma values
+  const size_t floats = static_cast<size_t>(3 * n * 3 + 13 * n) + 2 * nb + 64;
+  int st;
+  if ((st = ensure(c, c->op_in, floats * 4))) return st;
+  float* in = static_cast<float*>(c->op_in.ptr);
+  float* buf[2] = {in + 3 * n, in + 6 * n};
+  float* nw = in + 9 * n;
+  float* cw = nw + 12 * n;
+  float* sq = cw + n;
+  r.sigma = sq + nb;
+  cudaStream_t s = c->stream;
+  JXG_CUDA(c, cudaMemcpyAsync(in, xyb, bytes, cudaMemcpyHostToDevice, s));
+  JXG_CUDA(c, cudaMemcpyAsync(sq, sigma_quant, nb * 4, cudaMemcpyHostToDevice, s));
+  const float sad_mul = 1.65f;  // SAD_MUL, src/epf_filter.rs:45
+  int stages[3], count = 0;
+  float sms[3];
+  if (iters >= 3) {
+    stages[count] = 0;
+    sms[count++] = sad_mul * pass0;
+  }
+  stages[count] = 1;
+  sms[count++] = sad_mul;
+  if (iters >= 2) {
+    stages[count] = 2;
+    sms[count++] = sad_mul * pass2;
+  }
+  st = launch(c, "k_epf_sigma", c->timing, [&] {
+    k_epf_sigma<<<static_cast<unsigned>((nb + 255) / 256), 256, 0, s>>>(sq, nb, quant_mul,
+                                                                         static_cast<float>(sharpness) / 7.0f, r.sigma);
+  });
+  if (st) return st;
+  const float* src = in;
+  for (int k = 0; k < count; ++k) {
+    float* dst = buf[k & 1];
+    st = launch(c, "k_refine_epf", c->timing, [&] {
+      const dim3 grid(static_cast<unsigned>((r.w + kEpfTW - 1) / kEpfTW), static_cast<unsigned>((r.h + kEpfTH - 1) / kEpfTH));
+      k_refine_epf<<<grid, 256, 0, s>>>(r, stages[k], sms[k], src, n, r.w, dst, nw, cw);
+    });
+    if (st) return st;
+    src = dst;
+  }
+  JXG_CUDA(c, cudaMemcpyAsync(out, src, bytes, cudaMemcpyDeviceToHost, s));
+  return wait(c);
+}
+
 int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coefficients) {
   Context* c = static_cast<Context*>(ctx);
   if (!c || !blocks || !coefficients) return JXG_ERR_INVALID_ARGUMENT;

@@ -358,6 +358,15 @@ __global__ void __launch_bounds__(256) k_refine_sigma(const RefineArgs r, const 
   r.sigma[b] = __fdiv_rn(1.0f, fminf(__fmul_rn(__fdiv_rn(r.epf_quant_mul, sq), r.epf_lut), -1e-4f));
 }
 
+// The inverse sigma of every block from FrameBlocks' sigma_quant (the EPF
+// operator): 1 / min(quant_mul / sigma_quant * lut, -1e-4).
+__global__ void __launch_bounds__(256) k_epf_sigma(const float* __restrict__ sigma_quant, int64_t nb,
+                                                   float quant_mul, float lut, float* __restrict__ out) {
+  const int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  out[b] = __fdiv_rn(1.0f, fminf(__fmul_rn(__fdiv_rn(quant_mul, sigma_quant[b]), lut), -1e-4f));
+}
+
 struct EpfPlanes {
   const float* p;
   int64_t plane;
