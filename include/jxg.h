@@ -300,6 +300,15 @@ int32_t jxg_op_gaborish(void* ctx, const float* xyb, uint64_t width, uint64_t he
 int32_t jxg_op_epf(void* ctx, const float* xyb, uint64_t width, uint64_t height, const float* sigma_quant,
                    int32_t iters, float quant_mul, float pass0, float pass2, float border_mul,
                    const float* channel_scale, int32_t sharpness, float* out);
+/* The reference's six-term luma proxy (LumaProxy::new / compare,
+ * src/epf_proxy.rs:148-214): `source` and `test` Y planes of w*h floats
+ * (both at least 4 x 4); `terms` (6 floats, may be NULL) receives the
+ * quarter-resolution structure mean, the half-resolution structure mean and
+ * fourth-power pool, and the adjacent-gradient error, excess and
+ * fourth-power pool; `score` their weighted sum.  The pools are parallel
+ * sums (the reference's are sequential): equal to rounding. */
+int32_t jxg_op_luma_proxy(void* ctx, const float* source, const float* test, uint64_t width, uint64_t height,
+                          double* score, double* terms);
 /* DctFn<8, 8, 64> (src/dct.rs:172, scalar dct8x8 :631): `count` blocks of 64
  * row-major samples in, 64 coefficients (transposed storage, 1/64 scale) out. */
 int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coefficients);

@@ -418,6 +418,19 @@ class FrontendContext:
                                          pass0, pass2, border_mul, cs.ctypes.data, sharpness, out.ctypes.data))
         return out
 
+    def luma_proxy(self, source: np.ndarray, test: np.ndarray) -> tuple[float, np.ndarray]:
+        """jxg_op_luma_proxy: the reference's six-term luma proxy of `test`
+        against `source` ((h, w) Y planes): (score, the six terms)."""
+        a = np.ascontiguousarray(source, np.float32)
+        b = np.ascontiguousarray(test, np.float32)
+        if a.shape != b.shape or a.ndim != 2:
+            raise EncodeError(100, "two (h, w) planes of one size")
+        score = ctypes.c_double()
+        terms = np.zeros(6, np.float64)
+        self._check(self._lib.jxg_op_luma_proxy(self._ctx, a.ctypes.data, b.ctypes.data, a.shape[1], a.shape[0],
+                                                ctypes.byref(score), terms.ctypes.data))
+        return score.value, terms
+
     def dct8x8(self, blocks: np.ndarray) -> np.ndarray:
         blocks = np.ascontiguousarray(blocks, np.float32).reshape(-1, 64)
         out = np.zeros_like(blocks)

@@ -1699,6 +1699,84 @@ int32_t jxg_op_epf(void* ctx, const float* xyb, uint64_t width, uint64_t height,
   return wait(c);
 }
 
+int32_t jxg_op_luma_proxy(void* ctx, const float* source, const float* test, uint64_t width, uint64_t height,
+                          double* score, double* terms) {
+  using namespace jxg;
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !source || !test || !score) return JXG_ERR_INVALID_ARGUMENT;
+  if (width < 4 || height < 4) return fail(c, JXG_ERR_INVALID_ARGUMENT, "the proxy needs 4 x 4 pixels");
+  if (width > kMaxDimension || height > kMaxDimension)
+    return fail(c, JXG_ERR_DIMENSION_TOO_LARGE, "dimension too large");
+  cudaSetDevice(c->device);
+  const int w = static_cast<int>(width), h = static_cast<int>(height);
+  const int64_t n = static_cast<int64_t>(w) * h;
+  const int lw[2] = {w / 2, (w / 2) / 2}, lh[2] = {h / 2, (h / 2) / 2};  // half, quarter
+  const int64_t m[2] = {static_cast<int64_t>(lw[0]) * lh[0], static_cast<int64_t>(lw[1]) * lh[1]};
+  // per level: source values, its mean and variance, test values, two sets of
+  // three box planes, s and the three partials; then the slot sums
+  const size_t floats = 2 * n + 14 * (m[0] + m[1]) + 2 * kProxySums * kRefineSlots + 64;
+  int st;
+  if ((st = ensure(c, c->op_in, floats * 4))) return st;
+  float* p = static_cast<float*>(c->op_in.ptr);
+  float* src = p;
+  float* tst = p + n;
+  p += 2 * n;
+  float *rv[2], *rmv[2], *tv[2], *tmp[2], *box[2], *sm[2], *parts[2];
+  for (int l = 0; l < 2; ++l) {
+    rv[l] = p;
+    rmv[l] = rv[l] + m[l];
+    tv[l] = rmv[l] + 2 * m[l];
+    tmp[l] = tv[l] + m[l];
+    box[l] = tmp[l] + 3 * m[l];
+    sm[l] = box[l] + 3 * m[l];
+    parts[l] = sm[l] + m[l];
+    p = parts[l] + 3 * m[l];
+  }
+  double* sums = reinterpret_cast<double*>(p + (reinterpret_cast<uintptr_t>(p) & 4 ? 1 : 0));
+  cudaStream_t s = c->stream;
+  JXG_CUDA(c, cudaMemcpyAsync(src, source, n * 4, cudaMemcpyHostToDevice, s));
+  JXG_CUDA(c, cudaMemcpyAsync(tst, test, n * 4, cudaMemcpyHostToDevice, s));
+  JXG_CUDA(c, cudaMemsetAsync(sums, 0, kProxySums * kRefineSlots * sizeof(double), s));
+  auto grid = [](int64_t k) { return static_cast<unsigned>((k + 255) / 256); };
+  st = launch(c, "k_proxy", c->timing, [&] {
+    k_proxy_half<<<grid(m[0]), 256, 0, s>>>(src, w, w, h, 1, rv[0]);
+    k_proxy_half<<<grid(m[1]), 256, 0, s>>>(rv[0], lw[0], lw[0], lh[0], 0, rv[1]);
+    k_proxy_half<<<grid(m[0]), 256, 0, s>>>(tst, w, w, h, 1, tv[0]);
+    k_proxy_half<<<grid(m[1]), 256, 0, s>>>(tv[0], lw[0], lw[0], lh[0], 0, tv[1]);
+    for (int l = 0; l < 2; ++l) {
+      k_proxy_box_v<<<(lw[l] + 127) / 128, 128, 0, s>>>(rv[l], nullptr, lw[l], lh[l], tmp[l]);
+      k_proxy_box_h<<<(2 * lh[l] + 127) / 128, 128, 0, s>>>(tmp[l], 2, lw[l], lh[l], rmv[l]);
+      k_proxy_variance<<<grid(m[l]), 256, 0, s>>>(rmv[l], m[l]);
+      k_proxy_box_v<<<(lw[l] + 127) / 128, 128, 0, s>>>(tv[l], rv[l], lw[l], lh[l], tmp[l]);
+      k_proxy_box_h<<<(3 * lh[l] + 127) / 128, 128, 0, s>>>(tmp[l], 3, lw[l], lh[l], box[l]);
+      k_proxy_pool<<<grid(m[l]), 256, 0, s>>>(rmv[l], box[l], m[l], sm[l], parts[l], sums + 2 * l * kRefineSlots);
+    }
+    k_proxy_gradients<<<grid(n), 256, 0, s>>>(src, tst, w, w, h, sums + 4 * kRefineSlots);
+  });
+  if (st) return st;
+  double host[kProxySums * kRefineSlots];
+  JXG_CUDA(c, cudaMemcpyAsync(host, sums, sizeof(host), cudaMemcpyDeviceToHost, s));
+  if ((st = wait(c))) return st;
+  double t[kProxySums];
+  for (int q = 0; q < kProxySums; ++q) {
+    t[q] = 0.0;
+    for (int k = 0; k < kRefineSlots; ++k) t[q] += host[q * kRefineSlots + k];
+  }
+  const double np = static_cast<double>(h) * (w - 1) + static_cast<double>(h - 1) * w;
+  const double v[6] = {t[2] / static_cast<double>(m[1]), t[0] / static_cast<double>(m[0]),
+                       std::sqrt(std::sqrt(t[1] / static_cast<double>(m[0]))), t[4] / np, t[5] / np,
+                       std::sqrt(std::sqrt(t[6] / np))};
+  static const double kW[6] = {109.4163228369586, 4.685925102200196, 2.491781270704224,
+                               2.167275675983448, 4.55227651921194,  2.847714678987977};
+  double total = 0.0;
+  for (int k = 0; k < 6; ++k) {
+    total += kW[k] * v[k];
+    if (terms) terms[k] = v[k];
+  }
+  *score = total;
+  return JXG_OK;
+}
+
 int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coefficients) {
   Context* c = static_cast<Context*>(ctx);
   if (!c || !blocks || !coefficients) return JXG_ERR_INVALID_ARGUMENT;
@@ -2247,8 +2325,8 @@ int32_t jxg_refine_begin(void* ctx, uint64_t* xsize_blocks, uint64_t* ysize_bloc
                                                                               Q.ref_vals);
     for (auto* L : {&H, &Q}) {
       const int64_t m = static_cast<int64_t>(L->w) * L->h;
-      k_proxy_box_v<<<refine_grid(m), 256, 0, s>>>(L->ref_vals, nullptr, L->w, L->h, L->tmp);
-      k_proxy_box_h<<<refine_grid(2 * m), 256, 0, s>>>(L->tmp, 2, L->w, L->h, L->ref_mv);
+      k_proxy_box_v<<<(L->w + 127) / 128, 128, 0, s>>>(L->ref_vals, nullptr, L->w, L->h, L->tmp);
+      k_proxy_box_h<<<(2 * L->h + 127) / 128, 128, 0, s>>>(L->tmp, 2, L->w, L->h, L->ref_mv);
       k_proxy_variance<<<refine_grid(m), 256, 0, s>>>(L->ref_mv, m);
     }
     JXG_CUDA(c, cudaGetLastError());
@@ -2359,8 +2437,8 @@ int32_t jxg_refine_eval(void* ctx, const float* theta, float rate_lambda, float*
          for (int l = 0; l < 2; ++l) {
            auto& L = c->refine_pl[l];
            const int64_t m = static_cast<int64_t>(L.w) * L.h;
-           k_proxy_box_v<<<refine_grid(m), 256, 0, s>>>(L.vals, L.ref_vals, L.w, L.h, L.tmp);
-           k_proxy_box_h<<<refine_grid(3 * m), 256, 0, s>>>(L.tmp, 3, L.w, L.h, L.box);
+           k_proxy_box_v<<<(L.w + 127) / 128, 128, 0, s>>>(L.vals, L.ref_vals, L.w, L.h, L.tmp);
+           k_proxy_box_h<<<(3 * L.h + 127) / 128, 128, 0, s>>>(L.tmp, 3, L.w, L.h, L.box);
            k_proxy_pool<<<refine_grid(m), 256, 0, s>>>(L.ref_mv, L.box, m, L.s, L.parts,
                                                        psums + 2 * l * kRefineSlots);
          }

@@ -835,9 +835,9 @@ __global__ void __launch_bounds__(256) k_refine_backward(const RefineArgs r, con
 // The reference's six-term luma proxy as a distortion term (LumaProxy,
 // src/epf_proxy.rs:132-214; box moments src/epf_proxy/box_filter.rs:84-240;
 // pool and gradients src/epf_proxy/row_kernels.rs:60-115), on the decoded
-// XYB Y plane against the source's, with its adjoint.  The box sums are
-// direct 5-tap sums (the reference streams running sums: the same values to
-// rounding) and the pools are parallel sums.
+// XYB Y plane against the source's, with its adjoint.  The box moments use
+// the reference's running sums in its order (the moments' variances cancel,
+// so their rounding shows in the score); the pools are parallel sums.
 // ---------------------------------------------------------------------------
 
 // src/epf_proxy.rs:186-193
@@ -873,40 +873,53 @@ __global__ void __launch_bounds__(256) k_proxy_half(const float* __restrict__ in
 }
 
 // Vertical pass of the reflected 5x5 box (x 0.2) of t, t^2 and, with `ref`,
-// ref * t: `count` planes of w x h into `out`.
-__global__ void __launch_bounds__(256) k_proxy_box_v(const float* __restrict__ t, const float* __restrict__ ref,
+// ref * t (2 or 3 planes of w x h into `out`), one thread per column walking
+// down it with the reference's running sums (Scratch::run, accumulate and
+// step, src/epf_proxy/box_filter.rs:84-226): the sums start at -0 over rows
+// -2..2, each output row is sum x 0.2, then the entering row minus the
+// leaving one is added (a a - b b for the squares, ra a - rb b for the cross).
+__global__ void __launch_bounds__(128) k_proxy_box_v(const float* __restrict__ t, const float* __restrict__ ref,
                                                      int w, int h, float* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= w) return;
   const int64_t n = static_cast<int64_t>(w) * h;
-  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (q >= n) return;
-  const int x = static_cast<int>(q % w), y = static_cast<int>(q / w);
-  float m = 0.0f, sq = 0.0f, cr = 0.0f;
-#pragma unroll
+  auto at = [&](int y) { return static_cast<int64_t>(proxy_mirror(y, h)) * w + x; };
+  float m = -0.0f, sq = -0.0f, cr = -0.0f;
   for (int d = -2; d <= 2; ++d) {
-    const int64_t at = static_cast<int64_t>(proxy_mirror(y + d, h)) * w + x;
-    const float v = t[at];
+    const float v = t[at(d)];
     m = __fadd_rn(m, v);
     sq = __fadd_rn(sq, __fmul_rn(v, v));
-    if (ref) cr = __fadd_rn(cr, __fmul_rn(ref[at], v));
+    if (ref) cr = __fadd_rn(cr, __fmul_rn(ref[at(d)], v));
   }
-  out[q] = __fmul_rn(m, 0.2f);
-  out[n + q] = __fmul_rn(sq, 0.2f);
-  if (ref) out[2 * n + q] = __fmul_rn(cr, 0.2f);
+  for (int y = 0; y < h; ++y) {
+    const int64_t q = static_cast<int64_t>(y) * w + x;
+    out[q] = __fmul_rn(m, 0.2f);
+    out[n + q] = __fmul_rn(sq, 0.2f);
+    if (ref) out[2 * n + q] = __fmul_rn(cr, 0.2f);
+    if (y + 1 < h) {
+      const int64_t ea = at(y + 3), lb = at(y - 2);
+      const float a = t[ea], b = t[lb];
+      m = __fadd_rn(m, __fsub_rn(a, b));
+      sq = __fadd_rn(sq, __fsub_rn(__fmul_rn(a, a), __fmul_rn(b, b)));
+      if (ref) cr = __fadd_rn(cr, __fsub_rn(__fmul_rn(ref[ea], a), __fmul_rn(ref[lb], b)));
+    }
+  }
 }
 
-// Horizontal pass (x 0.2) of `count` planes.
-__global__ void __launch_bounds__(256) k_proxy_box_h(const float* __restrict__ in, int count, int w, int h,
+// Horizontal pass (x 0.2) of `count` planes, one thread per row with the
+// running sum of `horizontal_scalar` (box_filter.rs:228-240).
+__global__ void __launch_bounds__(128) k_proxy_box_h(const float* __restrict__ in, int count, int w, int h,
                                                      float* __restrict__ out) {
-  const int64_t n = static_cast<int64_t>(w) * h;
-  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (q >= n * count) return;
-  const int64_t c = q / n, p = q % n;
-  const int x = static_cast<int>(p % w), y = static_cast<int>(p / w);
-  const float* row = in + c * n + static_cast<int64_t>(y) * w;
-  float s = 0.0f;
-#pragma unroll
-  for (int d = -2; d <= 2; ++d) s = __fadd_rn(s, row[proxy_mirror(x + d, w)]);
-  out[q] = __fmul_rn(s, 0.2f);
+  const int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (r >= static_cast<int64_t>(count) * h) return;
+  const float* row = in + r * w;
+  float* dst = out + r * w;
+  float sum = 0.0f;
+  for (int d = -2; d <= 2; ++d) sum = __fadd_rn(sum, row[proxy_mirror(d, w)]);
+  for (int x = 0; x < w; ++x) {
+    dst[x] = __fmul_rn(sum, 0.2f);
+    if (x + 1 < w) sum = __fadd_rn(sum, __fsub_rn(row[proxy_mirror(x + 3, w)], row[proxy_mirror(x - 2, w)]));
+  }
 }
 
 // The source level's variance max(E[t^2] - mean^2, 0) (variance,
