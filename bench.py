@@ -55,7 +55,7 @@ def parse_args():
     p.add_argument("--batch-images", type=int, default=BATCH_IMAGES)
     p.add_argument("--contexts", type=int, default=3,
                    help="contexts (one stream each) the device-resident run alternates frames over")
-    p.add_argument("--e2e-contexts", type=int, default=4,
+    p.add_argument("--e2e-contexts", type=int, default=3,
                    help="contexts the end-to-end run alternates frames over")
     p.add_argument("--e2e-wide-tokens", action="store_true",
                    help="download (context, value) token pairs instead of packed AcToken words")
