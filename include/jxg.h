@@ -443,9 +443,10 @@ int32_t jxg_selftest_math(void* ctx, int32_t which, uint32_t lo_bits, uint32_t h
  *
  * jxg_refine_begin takes the frame of the context's last pass (one frame,
  * Speed::UltraFast), copies what the model needs (a later pass does not
- * disturb it), sets the context's own theta to zero and returns the block
- * grid (theta's size) in xsize/ysize_blocks; the others need it. */
-int32_t jxg_refine_begin(void* ctx, uint64_t* xsize_blocks, uint64_t* ysize_blocks);
+ * disturb it), sets the context's own theta to zero and returns the
+ * frame's size (theta holds one value per 8x8 block: ceil(width / 8) x
+ * ceil(height / 8)); the others need it. */
+int32_t jxg_refine_begin(void* ctx, uint64_t* width, uint64_t* height);
 /* Loss at `theta` (device memory, xb*yb floats; NULL: the context's own):
  * loss3 = {distortion + rate_lambda * bits / pixels, distortion, bits} on the
  * host; `grad` (device, xb*yb floats, or NULL) receives d loss / d theta from
@@ -467,6 +468,11 @@ int32_t jxg_refine_step(void* ctx, float rate_lambda, float learning_rate, doubl
 /* Copy the context's own theta out to `theta` (to_context 0) or in from it
  * (1; restarts Adam); host or device memory, xb*yb floats. */
 int32_t jxg_refine_theta(void* ctx, float* theta, int32_t to_context);
+/* The model's decoded frame at `theta` (NULL: the context's own): the XYB
+ * planes after dequantisation, the inverse transforms, the decoded DC and
+ * the EPF, 3 planes of w*h floats on the host (a decoder's reconstruction
+ * of the all-DCT8 frame, short of DC smoothing). */
+int32_t jxg_refine_decoded(void* ctx, const float* theta, float* xyb);
 /* The integer field of `theta` (NULL: the context's own): round(qf *
  * exp(theta)) clamped to 1..255, xb*yb bytes into host or device memory. */
 int32_t jxg_refine_field(void* ctx, const float* theta, uint8_t* quant_field);

@@ -51,6 +51,7 @@ EXPORTS = [
     "jxg_refine_set_weights",
     "jxg_refine_step",
     "jxg_refine_theta",
+    "jxg_refine_decoded",
     "jxg_refine_field",
     "jxg_refine_model",
     "jxg_frontend_run_with_field",
@@ -184,6 +185,7 @@ def load() -> ctypes.CDLL:
         "jxg_refine_set_weights": (i32, [vp, ctypes.c_float, ctypes.c_float]),
         "jxg_refine_step": (i32, [vp, ctypes.c_float, ctypes.c_float, vp]),
         "jxg_refine_theta": (i32, [vp, vp, i32]),
+        "jxg_refine_decoded": (i32, [vp, vp, vp]),
         "jxg_refine_field": (i32, [vp, vp, vp]),
         "jxg_refine_model": (i32, [vp, vp, vp, vp, vp]),
         "jxg_frontend_run_with_field": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config), vp, i32]),

@@ -499,9 +499,10 @@ class FrontendContext:
     def refine_begin(self) -> tuple[int, int]:
         """jxg_refine_begin: refine the frame of the last (UltraFast) pass;
         returns its block grid (xsize_blocks, ysize_blocks)."""
-        xb, yb = ctypes.c_uint64(), ctypes.c_uint64()
-        self._check(self._lib.jxg_refine_begin(self._ctx, ctypes.byref(xb), ctypes.byref(yb)))
-        self._refine_blocks = (xb.value, yb.value)
+        w, h = ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self._lib.jxg_refine_begin(self._ctx, ctypes.byref(w), ctypes.byref(h)))
+        self._refine_size = (w.value, h.value)
+        self._refine_blocks = ((w.value + 7) // 8, (h.value + 7) // 8)
         return self._refine_blocks
 
     def refine_eval(self, rate_lambda: float, theta_ptr: int | None = None, grad_ptr: int | None = None,
@@ -545,6 +546,16 @@ class FrontendContext:
             self._check(self._lib.jxg_refine_theta(self._ctx, t.ctypes.data, 1))
         out = np.zeros((yb, xb), np.float32)
         self._check(self._lib.jxg_refine_theta(self._ctx, out.ctypes.data, 0))
+        return out
+
+    def refine_decoded(self, theta_ptr: int | None = None) -> np.ndarray:
+        """The model's decoded XYB planes (3, h, w) at theta (the context's own
+        by default): dequantised, inverse-transformed, decoded DC, EPF."""
+        if not hasattr(self, "_refine_size"):
+            raise EncodeError(100, "refine_begin first")
+        w, h = self._refine_size
+        out = np.zeros((3, h, w), np.float32)
+        self._check(self._lib.jxg_refine_decoded(self._ctx, theta_ptr, out.ctypes.data))
         return out
 
     def refine_field(self, theta_ptr: int | None = None) -> np.ndarray:

@@ -2126,10 +2126,10 @@ namespace {
 int refine_grid(int64_t n) { return static_cast<int>((n + 255) / 256); }
 }  // namespace
 
-int32_t jxg_refine_begin(void* ctx, uint64_t* xsize_blocks, uint64_t* ysize_blocks) {
+int32_t jxg_refine_begin(void* ctx, uint64_t* width, uint64_t* height) {
   using namespace jxg;
   Context* c = static_cast<Context*>(ctx);
-  if (!c || !xsize_blocks || !ysize_blocks) return JXG_ERR_INVALID_ARGUMENT;
+  if (!c || !width || !height) return JXG_ERR_INVALID_ARGUMENT;
   if (c->async_pending) {
     const int st = jxg_frontend_wait(ctx);
     if (st) return st;
@@ -2334,8 +2334,8 @@ int32_t jxg_refine_begin(void* ctx, uint64_t* xsize_blocks, uint64_t* ysize_bloc
   if ((st = wait(c))) return st;
   r.xyb = nullptr;
   c->refine_ready = true;
-  *xsize_blocks = static_cast<uint64_t>(r.xb);
-  *ysize_blocks = static_cast<uint64_t>(r.yb);
+  *width = static_cast<uint64_t>(r.w);
+  *height = static_cast<uint64_t>(r.h);
   return JXG_OK;
 }
 
@@ -2550,6 +2550,28 @@ int32_t jxg_refine_set_weights(void* ctx, float ssim_weight, float proxy_weight)
   c->refine_w_ssim = ssim_weight;
   c->refine_w_proxy = proxy_weight;
   return JXG_OK;
+}
+
+int32_t jxg_refine_decoded(void* ctx, const float* theta, float* xyb) {
+  using namespace jxg;
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !xyb) return JXG_ERR_INVALID_ARGUMENT;
+  if (!c->refine_ready) return fail(c, JXG_ERR_INVALID_ARGUMENT, "jxg_refine_begin first");
+  double loss3[3];
+  int st;
+  if ((st = jxg_refine_eval(ctx, theta, 0.0f, nullptr, loss3, nullptr))) return st;
+  const RefineArgs& r = c->refine;
+  const int64_t n = static_cast<int64_t>(r.w) * r.h, pp = static_cast<int64_t>(r.pw) * r.yb * 8;
+  for (int k = 0; k < 3; ++k) {
+    if (r.epf_stages)
+      JXG_CUDA(c, cudaMemcpyAsync(xyb + k * n, c->refine_epf_out[r.epf_stages - 1] + k * n, n * 4,
+                                  cudaMemcpyDeviceToHost, c->stream));
+    else
+      JXG_CUDA(c, cudaMemcpy2DAsync(xyb + k * n, static_cast<size_t>(r.w) * 4, r.recon + k * pp,
+                                    static_cast<size_t>(r.pw) * 4, static_cast<size_t>(r.w) * 4, r.h,
+                                    cudaMemcpyDeviceToHost, c->stream));
+  }
+  return wait(c);
 }
 
 int32_t jxg_refine_field(void* ctx, const float* theta, uint8_t* quant_field) {

@@ -324,6 +324,27 @@ def test_levels_at_zero_are_the_front_ends(ctx, w, h, seed, d):
                            f"got {got[tuple(bad[0][:3])][:8]} want {want[tuple(bad[0][:3])][:8]}")
 
 
+def test_decoded_frame_is_the_models(ctx):
+    # jxg_refine_decoded: the FP64 model's decoded planes, within FP32, at
+    # theta = 0 and at a random theta; and close to the source at d 1
+    img, res = begin(ctx, 70, 54, 17, 1.0)
+    nb = res.quant_field.size
+    model = Fp64Model(ctx, res, 70, 54)
+    for spread in (0.0, 0.3):
+        th = np.random.default_rng(17).normal(0.0, spread, nb).astype(np.float32)
+        ctx.refine_theta(th.reshape(res.quant_field.shape))
+        dec = ctx.refine_decoded()
+        _, lv = ctx.refine_eval(0.0, levels=True)
+        t64 = torch.tensor(th.astype(np.float64))
+        model.loss(t64, t64, lv, 0.0)
+        want = model.decoded.numpy()
+        assert dec.shape == (3, 54, 70)
+        assert np.abs(dec - want).max() <= 2e-5 * max(1.0, np.abs(want).max()), np.abs(dec - want).max()
+    ctx.refine_theta(np.zeros(res.quant_field.shape, np.float32))
+    err = ctx.refine_decoded() - res.xyb
+    assert np.sqrt(np.mean(err[1] ** 2)) < 0.02
+
+
 def test_decoded_dc_is_the_dequantised_dc_levels(ctx):
     img, res = begin(ctx, 96, 72, 16)
     m = ctx.refine_model()
