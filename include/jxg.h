@@ -309,6 +309,17 @@ int32_t jxg_op_epf(void* ctx, const float* xyb, uint64_t width, uint64_t height,
  * sums (the reference's are sequential): equal to rounding. */
 int32_t jxg_op_luma_proxy(void* ctx, const float* source, const float* test, uint64_t width, uint64_t height,
                           double* score, double* terms);
+/* The encoder's EPF fit (fit and choose, src/epf_filter.rs:599-671,
+ * :807-873; MediumSlow and up in the reference): candidate loop-filter
+ * settings rendered over `recon` (3 planes of w*h) with the EPF and ranked
+ * by the luma proxy of their Y plane against `source_y` (w*h): the
+ * baseline, no filtering, four shape pilots at strength 2 / distance, the
+ * best pilot's endpoints and a log-quadratic vertex.  A setting is {iters,
+ * quant_mul, pass0, sharpness} with NaN for an unset quant_mul or pass0;
+ * `choice` (4 floats) carries the baseline in and the chosen setting out,
+ * `score` its proxy score.  Frames of at least 4 x 4 pixels. */
+int32_t jxg_op_epf_fit(void* ctx, const float* source_y, const float* recon, uint64_t width, uint64_t height,
+                       const float* sigma_quant, float distance, float* choice, double* score);
 /* DctFn<8, 8, 64> (src/dct.rs:172, scalar dct8x8 :631): `count` blocks of 64
  * row-major samples in, 64 coefficients (transposed storage, 1/64 scale) out. */
 int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coefficients);

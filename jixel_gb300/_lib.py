@@ -37,6 +37,7 @@ EXPORTS = [
     "jxg_op_gaborish",
     "jxg_op_epf",
     "jxg_op_luma_proxy",
+    "jxg_op_epf_fit",
     "jxg_op_dct8x8",
     "jxg_op_pack_tokens",
     "jxg_op_dct",
@@ -170,6 +171,7 @@ def load() -> ctypes.CDLL:
         "jxg_op_epf": (i32, [vp, vp, u64, u64, vp, i32, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                              ctypes.c_float, vp, i32, vp]),
         "jxg_op_luma_proxy": (i32, [vp, vp, vp, u64, u64, vp, vp]),
+        "jxg_op_epf_fit": (i32, [vp, vp, vp, u64, u64, vp, ctypes.c_float, vp, vp]),
         "jxg_op_dct8x8": (i32, [vp, vp, u64, vp]),
         "jxg_op_pack_tokens": (i32, [vp, vp, vp, u64, vp, u64, vp]),
         "jxg_op_dct": (i32, [vp, i32, vp, u64, vp, vp]),

@@ -431,6 +431,27 @@ class FrontendContext:
                                                 ctypes.byref(score), terms.ctypes.data))
         return score.value, terms
 
+    def epf_fit(self, source_y: np.ndarray, recon: np.ndarray, sigma_quant: np.ndarray, distance: float,
+                baseline=(2, None, None, 7)):
+        """jxg_op_epf_fit: the encoder's EPF fit over a reconstruction;
+        baseline and result as (iters, quant_mul or None, pass0 or None,
+        sharpness); returns (choice, its proxy score)."""
+        y = np.ascontiguousarray(source_y, np.float32)
+        r = np.ascontiguousarray(recon, np.float32)
+        h, w = y.shape
+        if r.shape != (3, h, w):
+            raise EncodeError(100, "recon must be (3, h, w) like source_y")
+        sq = np.ascontiguousarray(sigma_quant, np.float32)
+        if sq.size != ((w + 7) // 8) * ((h + 7) // 8):
+            raise EncodeError(100, "one sigma_quant value per 8x8 block")
+        ch = np.array([baseline[0], np.nan if baseline[1] is None else baseline[1],
+                       np.nan if baseline[2] is None else baseline[2], baseline[3]], np.float32)
+        score = ctypes.c_double()
+        self._check(self._lib.jxg_op_epf_fit(self._ctx, y.ctypes.data, r.ctypes.data, w, h, sq.ctypes.data,
+                                             distance, ch.ctypes.data, ctypes.byref(score)))
+        opt = lambda v: None if np.isnan(v) else float(v)  # noqa: E731
+        return (int(ch[0]), opt(ch[1]), opt(ch[2]), int(ch[3])), score.value
+
     def dct8x8(self, blocks: np.ndarray) -> np.ndarray:
         blocks = np.ascontiguousarray(blocks, np.float32).reshape(-1, 64)
         out = np.zeros_like(blocks)

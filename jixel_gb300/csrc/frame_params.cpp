@@ -321,6 +321,8 @@ void loop_filter_params(float d, LoopFilterParams* out) {
   }
 }
 
+float f16_round(float v) { return half_round(v); }
+
 bool is_screen_content(uint64_t constant_blocks, uint64_t w, uint64_t h) {
   uint64_t bw = w / 8, bh = h / 8;
   if (bw == 0 || bh == 0) return false;

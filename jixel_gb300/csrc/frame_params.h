@@ -126,6 +126,8 @@ struct LoopFilterParams {
   float channel_scale[3];
 };
 void loop_filter_params(float distance, LoopFilterParams* out);
+// A float read back through F16 (a signalled field's value).
+float f16_round(float v);
 bool is_screen_content(uint64_t constant_blocks, uint64_t width, uint64_t height);
 void srgb_to_linear_table(float out[256]);
 // TransferLut::build (src/color.rs:297-333) for integer samples of `bits`

@@ -1166,6 +1166,63 @@ int single_pass(Context* c, const void* pixels, uint64_t w, uint64_t h, int32_t 
 }  // namespace
 }  // namespace jxg
 
+namespace {
+// Choice (src/epf_filter.rs:577-594); NaN stands for None
+struct EpfChoice {
+  int iters;
+  float quant_mul, pass0;
+  int sharpness;
+  bool operator==(const EpfChoice& o) const {
+    auto same = [](float a, float b) { return (std::isnan(a) && std::isnan(b)) || a == b; };
+    return iters == o.iters && same(quant_mul, o.quant_mul) && same(pass0, o.pass0) && sharpness == o.sharpness;
+  }
+};
+EpfChoice epf_candidate(int iters, float strength, float pass0) { return {iters, 0.46f * strength, pass0, 7}; }
+
+// choose (src/epf_filter.rs:599-671), float arithmetic as the reference's
+template <class Score>
+EpfChoice epf_choose(float distance, EpfChoice baseline, Score&& score) {
+  std::vector<std::pair<EpfChoice, float>> rows;
+  auto trial = [&](const EpfChoice& c) {
+    for (const auto& r : rows)
+      if (r.first == c) return r;
+    const float loss = score(c);
+    rows.push_back({c, std::isfinite(loss) ? loss : INFINITY});
+    return rows.back();
+  };
+  const float nan = std::numeric_limits<float>::quiet_NaN();
+  trial(baseline);
+  trial(EpfChoice{0, nan, nan, baseline.sharpness});
+  const float center = std::min(std::max(2.0f / distance, 0.0625f), 4.0f);
+  std::pair<EpfChoice, float> best_pilot{baseline, INFINITY};
+  bool first = true;
+  const std::pair<int, float> shapes[4] = {{1, nan}, {2, nan}, {3, 0.9f}, {3, 3.6f}};
+  for (const auto& sh : shapes) {
+    const auto r = trial(epf_candidate(sh.first, center, sh.second));
+    if (first || r.second < best_pilot.second) best_pilot = r;  // the first of equal minima
+    first = false;
+  }
+  const EpfChoice pilot = best_pilot.first;
+  const float middle = best_pilot.second;
+  const float lo = std::max(center / 2.0f, 0.0625f), hi = std::min(center * 2.0f, 4.0f);
+  const float low = trial(epf_candidate(pilot.iters, lo, pilot.pass0)).second;
+  const float high = trial(epf_candidate(pilot.iters, hi, pilot.pass0)).second;
+  if (lo < center && center < hi) {
+    const float x0 = std::log2(lo), x1 = std::log2(center), x2 = std::log2(hi);
+    const float a = ((middle - low) / (x1 - x0) - (high - middle) / (x2 - x1)) / (x0 - x2);
+    const float b = (middle - low) / (x1 - x0) - a * (x0 + x1);
+    if (a > 1e-12f) {
+      const float v = std::min(std::max(-b / (2.0f * a), x0), x2);
+      trial(epf_candidate(pilot.iters, std::pow(2.0f, v), pilot.pass0));
+    }
+  }
+  size_t k = 0;
+  for (size_t i = 1; i < rows.size(); ++i)
+    if (rows[i].second < rows[k].second) k = i;
+  return rows[k].first;
+}
+}  // namespace
+
 using jxg::Batch;
 using jxg::Context;
 
@@ -1775,6 +1832,174 @@ int32_t jxg_op_luma_proxy(void* ctx, const float* source, const float* test, uin
   }
   *score = total;
   return JXG_OK;
+}
+
+int32_t jxg_op_epf_fit(void* ctx, const float* source_y, const float* recon, uint64_t width, uint64_t height,
+                       const float* sigma_quant, float distance, float* choice, double* score) {
+  using namespace jxg;
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !source_y || !recon || !sigma_quant || !choice || !score) return JXG_ERR_INVALID_ARGUMENT;
+  if (width < 4 || height < 4) return fail(c, JXG_ERR_INVALID_ARGUMENT, "the fit needs 4 x 4 pixels");
+  if (width > kMaxDimension || height > kMaxDimension)
+    return fail(c, JXG_ERR_DIMENSION_TOO_LARGE, "dimension too large");
+  if (!(distance > 0.0f) || !std::isfinite(distance)) return fail(c, JXG_ERR_INVALID_DISTANCE, "distance");
+  cudaSetDevice(c->device);
+  const int w = static_cast<int>(width), h = static_cast<int>(height);
+  const int64_t n = static_cast<int64_t>(w) * h;
+  const int xb = (w + 7) / 8, yb = (h + 7) / 8;
+  const int64_t nb = static_cast<int64_t>(xb) * yb;
+  const int lw[2] = {w / 2, (w / 2) / 2}, lh[2] = {h / 2, (h / 2) / 2};
+  const int64_t m[2] = {static_cast<int64_t>(lw[0]) * lh[0], static_cast<int64_t>(lw[1]) * lh[1]};
+  const size_t floats = 3 * n * 3 + 13 * n + n + 2 * nb + 17 * (m[0] + m[1]) + 2 * kProxySums * kRefineSlots + 64;
+  int st;
+  if ((st = ensure(c, c->op_in, floats * 4))) return st;
+  float* p = static_cast<float*>(c->op_in.ptr);
+  float* rec = p;
+  float* outb[2] = {p + 3 * n, p + 6 * n};
+  float* nw = p + 9 * n;
+  float* cw = nw + 12 * n;
+  float* src = cw + n;
+  float* sq = src + n;
+  float* sig = sq + nb;
+  p = sig + nb;
+  float *rv[2], *rmv[2], *tv[2], *tmp[2], *box[2], *sm[2], *parts[2];
+  for (int l = 0; l < 2; ++l) {
+    rv[l] = p;
+    rmv[l] = rv[l] + m[l];
+    tv[l] = rmv[l] + 2 * m[l];
+    tmp[l] = tv[l] + m[l];
+    box[l] = tmp[l] + 3 * m[l];
+    sm[l] = box[l] + 3 * m[l];
+    parts[l] = sm[l] + m[l];
+    p = parts[l] + 3 * m[l];
+  }
+  double* sums = reinterpret_cast<double*>(p + (reinterpret_cast<uintptr_t>(p) & 4 ? 1 : 0));
+  cudaStream_t s = c->stream;
+  JXG_CUDA(c, cudaMemcpyAsync(rec, recon, 3 * n * 4, cudaMemcpyHostToDevice, s));
+  JXG_CUDA(c, cudaMemcpyAsync(src, source_y, n * 4, cudaMemcpyHostToDevice, s));
+  JXG_CUDA(c, cudaMemcpyAsync(sq, sigma_quant, nb * 4, cudaMemcpyHostToDevice, s));
+  auto grid = [](int64_t k) { return static_cast<unsigned>((k + 255) / 256); };
+  // the source's proxy levels, once (LumaProxy::new)
+  k_proxy_half<<<grid(m[0]), 256, 0, s>>>(src, w, w, h, 1, rv[0]);
+  k_proxy_half<<<grid(m[1]), 256, 0, s>>>(rv[0], lw[0], lw[0], lh[0], 0, rv[1]);
+  for (int l = 0; l < 2; ++l) {
+    k_proxy_box_v<<<(lw[l] + 127) / 128, 128, 0, s>>>(rv[l], nullptr, lw[l], lh[l], tmp[l]);
+    k_proxy_box_h<<<(2 * lh[l] + 127) / 128, 128, 0, s>>>(tmp[l], 2, lw[l], lh[l], rmv[l]);
+    k_proxy_variance<<<grid(m[l]), 256, 0, s>>>(rmv[l], m[l]);
+  }
+  JXG_CUDA(c, cudaGetLastError());
+  RefineArgs r{};
+  r.w = w;
+  r.h = h;
+  r.xb = xb;
+  r.yb = yb;
+  r.epf_channel[0] = 40.0f;  // the encoder's XYB channel scales (LoopFilter defaults)
+  r.epf_channel[1] = 5.0f;
+  r.epf_channel[2] = 3.5f;
+  r.sigma = sig;
+  const double np_pairs = static_cast<double>(h) * (w - 1) + static_cast<double>(h - 1) * w;
+  std::vector<float> host_sigma(nb);
+  bool have_unfiltered = false;
+  float unfiltered_score = 0.0f;
+  int failure = JXG_OK;
+  auto proxy_of = [&](const float* y) -> float {
+    cudaMemsetAsync(sums, 0, kProxySums * kRefineSlots * sizeof(double), s);
+    k_proxy_half<<<grid(m[0]), 256, 0, s>>>(y, w, w, h, 1, tv[0]);
+    k_proxy_half<<<grid(m[1]), 256, 0, s>>>(tv[0], lw[0], lw[0], lh[0], 0, tv[1]);
+    for (int l = 0; l < 2; ++l) {
+      k_proxy_box_v<<<(lw[l] + 127) / 128, 128, 0, s>>>(tv[l], rv[l], lw[l], lh[l], tmp[l]);
+      k_proxy_box_h<<<(3 * lh[l] + 127) / 128, 128, 0, s>>>(tmp[l], 3, lw[l], lh[l], box[l]);
+      k_proxy_pool<<<grid(m[l]), 256, 0, s>>>(rmv[l], box[l], m[l], sm[l], parts[l], sums + 2 * l * kRefineSlots);
+    }
+    k_proxy_gradients<<<grid(n), 256, 0, s>>>(src, y, w, w, h, sums + 4 * kRefineSlots);
+    double host[kProxySums * kRefineSlots];
+    if (cudaMemcpyAsync(host, sums, sizeof(host), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+      failure = fail(c, JXG_ERR_CUDA, "proxy");
+      return INFINITY;
+    }
+    double t[kProxySums];
+    for (int q = 0; q < kProxySums; ++q) {
+      t[q] = 0.0;
+      for (int k = 0; k < kRefineSlots; ++k) t[q] += host[q * kRefineSlots + k];
+    }
+    static const double kW[6] = {109.4163228369586, 4.685925102200196, 2.491781270704224,
+                                 2.167275675983448, 4.55227651921194,  2.847714678987977};
+    const double v[6] = {t[2] / static_cast<double>(m[1]), t[0] / static_cast<double>(m[0]),
+                         std::sqrt(std::sqrt(t[1] / static_cast<double>(m[0]))), t[4] / np_pairs, t[5] / np_pairs,
+                         std::sqrt(std::sqrt(t[6] / np_pairs))};
+    double total = 0.0;
+    for (int k = 0; k < 6; ++k) total += kW[k] * v[k];
+    return static_cast<float>(total);
+  };
+  auto score_of = [&](const EpfChoice& ch) -> float {
+    if (failure) return INFINITY;
+    bool unfiltered = ch.iters == 0 || ch.sharpness == 0;
+    const float* y = rec + n;
+    if (!unfiltered) {
+      // LoopFilter::new(iters, pass0, quant_mul, None): a signalled bundle
+      // is read back through F16
+      float q = 0.46f, p0 = 0.9f, p2 = 6.5f, border = 2.0f / 3.0f;
+      const float s0 = !std::isnan(ch.pass0) ? ch.pass0 : (!std::isnan(ch.quant_mul) ? 0.9f : NAN);
+      if (!std::isnan(s0)) {
+        q = f16_round(!std::isnan(ch.quant_mul) ? ch.quant_mul : 0.46f);
+        p0 = f16_round(s0);
+        p2 = f16_round(6.5f);
+        border = f16_round(2.0f / 3.0f);
+      }
+      r.epf_border = border;
+      k_epf_sigma<<<grid(nb), 256, 0, s>>>(sq, nb, q, static_cast<float>(ch.sharpness) / 7.0f, sig);
+      if (cudaMemcpyAsync(host_sigma.data(), sig, nb * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaStreamSynchronize(s) != cudaSuccess) {
+        failure = fail(c, JXG_ERR_CUDA, "sigma");
+        return INFINITY;
+      }
+      bool any = false;
+      for (float v : host_sigma) any = any || v >= -3.905243f;  // MIN_SIGMA
+      if (!any) {
+        unfiltered = true;
+      } else {
+        int stages[3], count = 0;
+        float sms[3];
+        if (ch.iters >= 3) {
+          stages[count] = 0;
+          sms[count++] = 1.65f * p0;
+        }
+        stages[count] = 1;
+        sms[count++] = 1.65f;
+        if (ch.iters >= 2) {
+          stages[count] = 2;
+          sms[count++] = 1.65f * p2;
+        }
+        const float* in = rec;
+        for (int k = 0; k < count; ++k) {
+          const dim3 g(static_cast<unsigned>((w + kEpfTW - 1) / kEpfTW), static_cast<unsigned>((h + kEpfTH - 1) / kEpfTH));
+          k_refine_epf<<<g, 256, 0, s>>>(r, stages[k], sms[k], in, n, w, outb[k & 1], nw, cw);
+          in = outb[k & 1];
+        }
+        y = in + n;
+      }
+    }
+    if (unfiltered && have_unfiltered) return unfiltered_score;
+    const float v = proxy_of(y);
+    if (unfiltered) {
+      have_unfiltered = true;
+      unfiltered_score = v;
+    }
+    return v;
+  };
+  const EpfChoice base{static_cast<int>(choice[0]), choice[1], choice[2], static_cast<int>(choice[3])};
+  if (base.iters < 0 || base.iters > 3 || base.sharpness < 0 || base.sharpness > 7)
+    return fail(c, JXG_ERR_INVALID_ARGUMENT, "baseline iters 0..3, sharpness 0..7");
+  const EpfChoice best = epf_choose(distance, base, score_of);
+  if (failure) return failure;
+  JXG_CUDA(c, cudaGetLastError());
+  choice[0] = static_cast<float>(best.iters);
+  choice[1] = best.quant_mul;
+  choice[2] = best.pass0;
+  choice[3] = static_cast<float>(best.sharpness);
+  *score = score_of(best);
+  return failure;
 }
 
 int32_t jxg_op_dct8x8(void* ctx, const float* blocks, uint64_t count, float* coefficients) {
