@@ -849,10 +849,21 @@ class FrontendBatch:
         return _trim(r)
 
 
-def encode_frontend(pixels: np.ndarray, config: EncodeConfig, device: int = 0) -> FrontendResult:
-    """One-shot front end: the device half of `encode_image` (src/encode_image.rs:1610)."""
+def encode_frontend(pixels: np.ndarray, config: EncodeConfig, device: int = 0, *,
+                    refine_steps: int = 0, learning_rate: float = 0.05) -> FrontendResult:
+    """One-shot front end: the device half of `encode_image` (src/encode_image.rs:1610).
+    With `refine_steps` (UltraFast only), the pass's quant field is refined
+    by that many monotone steps at the frame's own rate-distortion slope and
+    the frame coded again with the refined field."""
     ctx = FrontendContext(device)
     try:
-        return ctx.frontend(pixels, config)
+        res = ctx.frontend(pixels, config)
+        if refine_steps <= 0:
+            return res
+        pixels = _as_hwc(pixels)
+        ctx.refine_begin()
+        lam = ctx.refine_rate_slope(pixels.shape[0] * pixels.shape[1])
+        field, _, _ = ctx.refine(steps=refine_steps, rate_lambda=lam, learning_rate=learning_rate)
+        return ctx.frontend_with_field(pixels, config, field)
     finally:
         ctx.close()

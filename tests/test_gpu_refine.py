@@ -518,6 +518,19 @@ def test_ac_bits_estimate_counts_symbols_and_raw_bits(ctx):
     assert res.histograms.sum() == len(res.tokens)
 
 
+def test_encode_frontend_with_refinement():
+    # the one-shot path: a refined field, then the frame coded with it
+    img = synthetic.generate(160, 120, 91)
+    cfg = ultrafast(1.0)
+    plain = J.encode_frontend(img, cfg)
+    refined = J.encode_frontend(img, cfg, refine_steps=4)
+    assert refined.quant_field.shape == plain.quant_field.shape
+    assert not np.array_equal(refined.quant_field, plain.quant_field)
+    assert refined.params["num_tokens"] > 0
+    with pytest.raises(J.EncodeError):
+        J.encode_frontend(img, J.EncodeConfig(distance=3.0, speed=J.Speed.FASTEST), refine_steps=2)
+
+
 def test_refinement_errors(ctx):
     img = synthetic.generate(64, 64, 71)
     with pytest.raises(J.EncodeError):
