@@ -64,6 +64,8 @@ def parse_args():
     p.add_argument("--no-refine", action="store_true",
                    help="skip the quant-field refinement timing")
     p.add_argument("--refine-steps", type=int, default=8)
+    p.add_argument("--refine-weights", default="1,0.1",
+                   help="the refinement's distortion mix: weight of 1 - SSIM, weight of the luma proxy")
     p.add_argument("--refine-only", action="store_true",
                    help="only run the refinement record on one context and print it (a profiler target)")
     p.add_argument("--frames-ultrafast", action="store_true",
@@ -545,6 +547,8 @@ def run_refine(ctx, stream, args, dev) -> dict:
     lr = 0.05
     base = ctx.frontend(img, cfg, coefficients=False)
     xb, yb = ctx.refine_begin()
+    weights = tuple(float(v) for v in args.refine_weights.split(","))
+    ctx.refine_weights(*weights)
     # lambda at the pass's own rate-distortion slope: the steps trade bits
     # between blocks at the exchange rate the frame already has
     lam = ctx.refine_rate_slope(w * h)
@@ -592,9 +596,11 @@ def run_refine(ctx, stream, args, dev) -> dict:
         ctx.refine_step(lam_p, lr)
     coded_proxy = _refined_field_report(ctx, img, cfg, base, ctx.refine_field(), lam_p)
     coded_proxy["lambda"] = lam_p
-    ctx.refine_weights(1.0, 0.0)
+    ctx.refine_weights(*weights)
     return {"workload": f"{w}x{h} RGB8 (seed 4) q90 UltraFast pass, {nb} blocks, Adam lr {lr}, "
-                        f"lambda {lam:.4g} (the pass's rate-distortion slope), SSIM at 3 scales + rate model",
+                        f"lambda {lam:.4g} (the pass's rate-distortion slope), distortion "
+                        f"{weights[0]} x (1 - SSIM at 3 scales) + {weights[1]} x luma proxy, rate model",
+            "weights": weights,
             "steps": args.refine_steps, "ms_per_step": ms, "wall_ms_per_step": 1000.0 * wall / args.refine_steps,
             "megapixels_per_s": w * h / 1e6 / (ms / 1000.0),
             "loss_first": hist[0][0], "loss_final": final[0], "distortion_first": hist[0][1],

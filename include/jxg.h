@@ -470,7 +470,7 @@ int32_t jxg_refine_eval(void* ctx, const float* theta, float rate_lambda, float*
  * the reference's six-term luma proxy (LumaProxy, src/epf_proxy.rs:132-214:
  * structure terms of the decoded XYB Y plane at half and quarter resolution
  * and its adjacent gradients, against the source's; frames of at least 4 x 4
- * pixels).  Defaults 1 and 0; both finite, non-negative, not both zero. */
+ * pixels).  Defaults 1 and 0.1; both finite, non-negative, not both zero. */
 int32_t jxg_refine_set_weights(void* ctx, float ssim_weight, float proxy_weight);
 /* One Adam step (beta 0.9 / 0.999) on the context's own theta: loss3 at the
  * theta before the step, as jxg_refine_eval.  theta stays where

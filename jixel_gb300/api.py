@@ -541,7 +541,7 @@ class FrontendContext:
                                               loss.ctypes.data, None if lv is None else lv.ctypes.data))
         return (float(loss[0]), float(loss[1]), float(loss[2])), lv
 
-    def refine_weights(self, ssim: float = 1.0, proxy: float = 0.0):
+    def refine_weights(self, ssim: float = 1.0, proxy: float = 0.1):
         """jxg_refine_set_weights: distortion = ssim x (1 - SSIM) + proxy x the
         reference's luma proxy."""
         self._check(self._lib.jxg_refine_set_weights(self._ctx, ssim, proxy))
@@ -549,7 +549,7 @@ class FrontendContext:
 
     @property
     def refine_weights_now(self) -> tuple[float, float]:
-        return getattr(self, "_refine_weights", (1.0, 0.0))
+        return getattr(self, "_refine_weights", (1.0, 0.1))
 
     def refine_step(self, rate_lambda: float, learning_rate: float) -> tuple[float, float, float]:
         """One Adam step on the context's theta; the loss before it."""

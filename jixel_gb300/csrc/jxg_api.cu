@@ -159,7 +159,7 @@ struct Context {
   float* refine_epf_cw[3] = {};
   float* refine_epf_g[2] = {};   // the decoded-XYB gradient (EPF or proxy), ping-pong
   // the distortion's mix: weight of 1 - SSIM and of the luma proxy
-  float refine_w_ssim = 1.0f, refine_w_proxy = 0.0f;
+  float refine_w_ssim = 1.0f, refine_w_proxy = 0.1f;
   bool refine_proxy = false;  // the frame is large enough for the proxy (4 x 4)
   struct ProxyLevel {
     int w = 0, h = 0;
@@ -2550,8 +2550,8 @@ int32_t jxg_refine_begin(void* ctx, uint64_t* width, uint64_t* height) {
                                                                               Q.ref_vals);
     for (auto* L : {&H, &Q}) {
       const int64_t m = static_cast<int64_t>(L->w) * L->h;
-      k_proxy_box_v<<<(L->w + 127) / 128, 128, 0, s>>>(L->ref_vals, nullptr, L->w, L->h, L->tmp);
-      k_proxy_box_h<<<(2 * L->h + 127) / 128, 128, 0, s>>>(L->tmp, 2, L->w, L->h, L->ref_mv);
+      k_proxy_box_v_par<<<refine_grid(m), 256, 0, s>>>(L->ref_vals, nullptr, L->w, L->h, L->tmp);
+      k_proxy_box_h_par<<<refine_grid(2 * m), 256, 0, s>>>(L->tmp, 2, L->w, L->h, L->ref_mv);
       k_proxy_variance<<<refine_grid(m), 256, 0, s>>>(L->ref_mv, m);
     }
     JXG_CUDA(c, cudaGetLastError());
@@ -2662,8 +2662,8 @@ int32_t jxg_refine_eval(void* ctx, const float* theta, float rate_lambda, float*
          for (int l = 0; l < 2; ++l) {
            auto& L = c->refine_pl[l];
            const int64_t m = static_cast<int64_t>(L.w) * L.h;
-           k_proxy_box_v<<<(L.w + 127) / 128, 128, 0, s>>>(L.vals, L.ref_vals, L.w, L.h, L.tmp);
-           k_proxy_box_h<<<(3 * L.h + 127) / 128, 128, 0, s>>>(L.tmp, 3, L.w, L.h, L.box);
+           k_proxy_box_v_par<<<refine_grid(m), 256, 0, s>>>(L.vals, L.ref_vals, L.w, L.h, L.tmp);
+           k_proxy_box_h_par<<<refine_grid(3 * m), 256, 0, s>>>(L.tmp, 3, L.w, L.h, L.box);
            k_proxy_pool<<<refine_grid(m), 256, 0, s>>>(L.ref_mv, L.box, m, L.s, L.parts,
                                                        psums + 2 * l * kRefineSlots);
          }

@@ -922,6 +922,42 @@ __global__ void __launch_bounds__(128) k_proxy_box_h(const float* __restrict__ i
   }
 }
 
+// The same two passes as direct 5-tap sums, one thread per output: the
+// refinement's model (the box's values to rounding, fully parallel; the
+// running sums above keep the reference's rounding for the operators).
+__global__ void __launch_bounds__(256) k_proxy_box_v_par(const float* __restrict__ t, const float* __restrict__ ref,
+                                                         int w, int h, float* __restrict__ out) {
+  const int64_t n = static_cast<int64_t>(w) * h;
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int x = static_cast<int>(q % w), y = static_cast<int>(q / w);
+  float m = 0.0f, sq = 0.0f, cr = 0.0f;
+#pragma unroll
+  for (int d = -2; d <= 2; ++d) {
+    const int64_t at = static_cast<int64_t>(proxy_mirror(y + d, h)) * w + x;
+    const float v = t[at];
+    m = __fadd_rn(m, v);
+    sq = __fadd_rn(sq, __fmul_rn(v, v));
+    if (ref) cr = __fadd_rn(cr, __fmul_rn(ref[at], v));
+  }
+  out[q] = __fmul_rn(m, 0.2f);
+  out[n + q] = __fmul_rn(sq, 0.2f);
+  if (ref) out[2 * n + q] = __fmul_rn(cr, 0.2f);
+}
+__global__ void __launch_bounds__(256) k_proxy_box_h_par(const float* __restrict__ in, int count, int w, int h,
+                                                         float* __restrict__ out) {
+  const int64_t n = static_cast<int64_t>(w) * h;
+  const int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= n * count) return;
+  const int64_t c = q / n, p = q % n;
+  const int x = static_cast<int>(p % w), y = static_cast<int>(p / w);
+  const float* row = in + c * n + static_cast<int64_t>(y) * w;
+  float s = 0.0f;
+#pragma unroll
+  for (int d = -2; d <= 2; ++d) s = __fadd_rn(s, row[proxy_mirror(x + d, w)]);
+  out[q] = __fmul_rn(s, 0.2f);
+}
+
 // The source level's variance max(E[t^2] - mean^2, 0) (variance,
 // row_kernels.rs:81-85), in place of the box's second plane.
 __global__ void __launch_bounds__(256) k_proxy_variance(float* __restrict__ moments, int64_t n) {

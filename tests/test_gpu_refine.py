@@ -409,7 +409,7 @@ def fp64_check(ctx, w, h, seed, lam, spread, d=1.0, weights=(1.0, 0.0)):
     tol = (1e-2 if weights[1] > 0 else 1e-3) * np.abs(g_ref).max()
     err = np.abs(g_gpu - g_ref)
     assert err.max() <= tol, (err.max(), tol, int(err.argmax()))
-    ctx.refine_weights(1.0, 0.0)
+    ctx.refine_weights()
     return model, t64.detach(), lv, g_ref, lam
 
 
@@ -443,7 +443,7 @@ def test_luma_proxy_matches_the_oracle(ctx):
     try:
         (loss, dist, _), lv = ctx.refine_eval(0.0, theta.data_ptr(), levels=True)
     finally:
-        ctx.refine_weights(1.0, 0.0)
+        ctx.refine_weights()
     model = Fp64Model(ctx, res, 96, 72)
     model.weights = (0.0, 1.0)
     t64 = torch.tensor(th.astype(np.float64))
