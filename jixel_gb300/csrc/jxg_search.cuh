@@ -868,11 +868,6 @@ __device__ __forceinline__ int small_strategy(int choice) {
          : choice == kSmallTall ? kSt16x8 : kSt16x16;
 }
 
-struct SmallPlan {
-  int n;
-  uint8_t cell[64], choice[64];
-};
-
 // One warp's DP state.  The reference walks a layer's active profiles in
 // order and relaxes each successor with a strict `<`, so a successor keeps
 // the cheapest relaxation and, among equal costs, the earliest; the next
@@ -890,6 +885,8 @@ struct RetileSmem {
   uint16_t act_a[512], act_b[512];
   float leaf[64], wide[64], tall[64], square[64];
   uint8_t live[64];
+  int8_t current[64];  // the map's strategy at each first block of the tile, -1 elsewhere
+  int8_t plan[64];     // the winning plan's strategy at each first block it places, -1 elsewhere
 };
 constexpr int kRetileWarps = 4;  // tiles per CTA by default (tuned per device)
 constexpr unsigned long long kNoKey = ~0ull;
@@ -987,9 +984,10 @@ __device__ __forceinline__ int relax_place(const Relax& r, bool valid, int a, ui
   return total;
 }
 
-// The whole warp calls it with the same arguments; the plan is written on lane 0.
+// The whole warp calls it with the same arguments.  When its total is finite
+// and below `replace_below`, its plan replaces `sm.plan`.
 __device__ float plan_small(RetileSmem& sm, uint64_t fixed, int w, int h, uint8_t* choices,
-                            float replace_below, SmallPlan* plan) {
+                            float replace_below) {
   const int lane = threadIdx.x & 31;
   const int cells = w * h, states = 1 << (w + 1), mask = states - 1;
   const int below_bit = 1 << w;
@@ -1066,19 +1064,39 @@ __device__ float plan_small(RetileSmem& sm, uint64_t fixed, int w, int h, uint8_
   const float total = (k0 >> 43) == static_cast<unsigned long long>(65 - cells) ? dp_cost(k0) : INFINITY;
   __syncwarp();
   if (!(isfinite(total) && total < replace_below)) return total;
-  if (lane == 0) {
-    const int added[5] = {0, 0, 2, below_bit, 2 | below_bit | (2 << w)};
-    plan->n = 0;
-    int state = 0;
-    for (int i = cells - 1; i >= 0; --i) {
-      const int choice = choices[i * states + state];
-      if (choice != 0) {
-        plan->cell[plan->n] = static_cast<uint8_t>(i);
-        plan->choice[plan->n] = static_cast<uint8_t>(choice);
-        ++plan->n;
-      }
-      state = (((state << 1) ^ added[choice]) & mask) | (choice == 0 ? 1 : 0);
+  for (int i = lane; i < 64; i += 32) sm.plan[i] = -1;
+  __syncwarp();
+  // The backtrack from state 0 of the last layer: the profile before cell i
+  // follows from the profile after it and the cell's choice.  Each round
+  // loads, at once, the choice of cell i, the five choices cell i - 1 could
+  // be asked for (one per choice at i) and the 25 of cell i - 2, then
+  // follows the three the walk takes: three cells a memory round trip, the
+  // same walk as one cell at a time.
+  auto before = [&](int state, int choice) {
+    const int added = choice == 2 ? 2 : choice == 3 ? below_bit : choice == 4 ? 2 | below_bit | (2 << w) : 0;
+    return (((state << 1) ^ added) & mask) | (choice == 0 ? 1 : 0);
+  };
+  const int c1 = lane >= 6 ? (lane - 6) / 5 : lane - 1, c2 = (lane - 6) % 5;
+  const int depth = lane == 0 ? 0 : lane <= 5 ? 1 : lane <= 30 ? 2 : -1;
+  int state = 0;
+  for (int i = cells - 1; i >= 0; i -= 3) {
+    int mine = 0;
+    const int cell = i - depth;
+    if (depth >= 0 && cell >= 0) {
+      const int st = depth == 0 ? state : depth == 1 ? before(state, c1) : before(before(state, c1), c2);
+      mine = choices[cell * states + st];
     }
+    const int a = __shfl_sync(0xffffffffu, mine, 0);
+    const int a_in = a <= 4 ? a : 0;
+    const int b = __shfl_sync(0xffffffffu, mine, 1 + a_in);
+    const int b_in = b <= 4 ? b : 0;
+    const int c = __shfl_sync(0xffffffffu, mine, 6 + 5 * a_in + b_in);
+    if (lane == 0) {
+      if (a != 0) sm.plan[i] = static_cast<int8_t>(small_strategy(a));
+      if (i >= 1 && b != 0) sm.plan[i - 1] = static_cast<int8_t>(small_strategy(b));
+      if (i >= 2 && c != 0) sm.plan[i - 2] = static_cast<int8_t>(small_strategy(c));
+    }
+    state = before(before(before(state, a), b), c);
   }
   __syncwarp();
   return total;
@@ -1087,12 +1105,6 @@ __device__ float plan_small(RetileSmem& sm, uint64_t fixed, int w, int h, uint8_
 struct Piece {
   int8_t x, y, s;
 };
-
-__device__ __forceinline__ bool piece_in(const Piece* set, int n, Piece p) {
-  for (int i = 0; i < n; ++i)
-    if (set[i].x == p.x && set[i].y == p.y && set[i].s == p.s) return true;
-  return false;
-}
 
 __global__ void __launch_bounds__(32 * kMaxTuneWarps) k_retile(const __grid_constant__ Frame f) {
   extern __shared__ __align__(16) unsigned char retile_smem_raw[];
@@ -1157,73 +1169,95 @@ __global__ void __launch_bounds__(32 * kMaxTuneWarps) k_retile(const __grid_cons
     }
     sm.live[i] = m;
   }
-  // the tile's current pieces (raster order of first blocks) and the fixed
-  // (larger than 16x16) ones, on lane 0
-  Piece current[64];
-  int ncur = 0;
-  uint64_t fixed = 0;
-  float fixed_cost = 0.0f;
-  if (lane == 0) {
-    for (int y = 0; y < h; ++y)
-      for (int x = 0; x < w; ++x) {
-        const uint8_t cell = map[(by + y) * xb + bx + x];
-        if (cell & 1) current[ncur++] = Piece{static_cast<int8_t>(x), static_cast<int8_t>(y), static_cast<int8_t>(cell >> 1)};
-      }
-    for (int k = 0; k < ncur; ++k) {
-      if (current[k].s <= kSt16x16) continue;
-      const Piece p = current[k];
-      const uint64_t row = (1ull << cov_x_of(p.s)) - 1ull;
-      for (int yy = 0; yy < cov_y_of(p.s); ++yy) fixed |= row << (p.y * w + p.x + yy * w);
-      fixed_cost = __fadd_rn(fixed_cost, score(p));
+  // The tile's current pieces (the map's strategy at each first block) and
+  // the fixed ones (larger than 16x16): their cells and their cost, summed in
+  // raster order of first blocks.
+  uint32_t fixed_half[2] = {0u, 0u};
+  float fixed_term[2] = {0.0f, 0.0f};
+  unsigned fixed_first[2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int i = lane + 32 * r;
+    int cs = -1;
+    if (i < w * h) {
+      const uint8_t cell = map[(by + i / w) * xb + bx + i % w];
+      if (cell & 1) cs = cell >> 1;
     }
+    sm.current[i] = static_cast<int8_t>(cs);
+    const bool big = cs > kSt16x16;
+    if (big) {
+      const int x = i % w, y = i / w;
+      const uint64_t row = (1ull << cov_x_of(cs)) - 1ull;
+      uint64_t cover = 0;
+      for (int yy = 0; yy < cov_y_of(cs); ++yy) cover |= row << (y * w + x + yy * w);
+      fixed_half[0] |= static_cast<uint32_t>(cover);
+      fixed_half[1] |= static_cast<uint32_t>(cover >> 32);
+      fixed_term[r] = score(Piece{static_cast<int8_t>(x), static_cast<int8_t>(y), static_cast<int8_t>(cs)});
+    }
+    fixed_first[r] = __ballot_sync(0xffffffffu, big);
   }
-  fixed = __shfl_sync(0xffffffffu, fixed, 0);
-  fixed_cost = __shfl_sync(0xffffffffu, fixed_cost, 0);
+  const uint64_t fixed = static_cast<uint64_t>(__reduce_or_sync(0xffffffffu, fixed_half[0])) |
+                         (static_cast<uint64_t>(__reduce_or_sync(0xffffffffu, fixed_half[1])) << 32);
+  float fixed_cost = 0.0f;
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+    for (unsigned m = fixed_first[r]; m != 0u; m &= m - 1u)
+      fixed_cost = __fadd_rn(fixed_cost, __shfl_sync(0xffffffffu, fixed_term[r], __ffs(m) - 1));
   __syncwarp();
   uint8_t* choices = s.dp_choices + static_cast<int64_t>(tile) * 64 * 512;
-  SmallPlan plan;
-  plan.n = 0;
-  const float around = __fadd_rn(plan_small(sm, fixed, w, h, choices, INFINITY, &plan), fixed_cost);
+  const float around = __fadd_rn(plan_small(sm, fixed, w, h, choices, INFINITY), fixed_cost);
   bool keep_fixed = true;
   float winner = around;
   if (fixed != 0) {
-    const float over = plan_small(sm, 0, w, h, choices, around, &plan);
+    const float over = plan_small(sm, 0, w, h, choices, around);
     if (over < around) {
       winner = over;
       keep_fixed = false;
     }
   }
-  if (lane != 0 || !isfinite(winner)) return;
-  Piece layout[64];
-  int nl = 0;
-  for (int k = 0; k < plan.n; ++k) {
-    const int i = plan.cell[k];
-    layout[nl++] = Piece{static_cast<int8_t>(i % w), static_cast<int8_t>(i / w),
-                         static_cast<int8_t>(small_strategy(plan.choice[k]))};
+  if (!isfinite(winner)) return;
+  // The new layout at each first block: the winning plan, with the fixed
+  // pieces when they stay.  A piece is in both layouts when the same
+  // strategy starts at the same block, so the pieces that change are the
+  // blocks where the two strategies differ.  Their costs, summed in raster
+  // order of first blocks, decide.  The DP's cost arrays are free again and
+  // hold the terms: the old layout's in `leaf`, the new one's in `wide`.
+  int ns_of[2];
+  unsigned gone[2], added[2];
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int i = lane + 32 * r;
+    const int cs = sm.current[i];
+    int ns = sm.plan[i];
+    if (keep_fixed && cs > kSt16x16) ns = cs;
+    ns_of[r] = ns;
+    const int8_t x = static_cast<int8_t>(i % w), y = static_cast<int8_t>(i / w);
+    const bool g = cs >= 0 && ns != cs, a = ns >= 0 && ns != cs;
+    if (g) sm.leaf[i] = score(Piece{x, y, static_cast<int8_t>(cs)});
+    if (a) sm.wide[i] = score(Piece{x, y, static_cast<int8_t>(ns)});
+    gone[r] = __ballot_sync(0xffffffffu, g);
+    added[r] = __ballot_sync(0xffffffffu, a);
   }
-  if (keep_fixed)
-    for (int k = 0; k < ncur; ++k)
-      if (current[k].s > kSt16x16) layout[nl++] = current[k];
-  // sort by (y, x, strategy): insertion sort over at most 64 pieces
-  for (int i = 1; i < nl; ++i) {
-    const Piece p = layout[i];
-    int j = i - 1;
-    while (j >= 0 && (layout[j].y > p.y || (layout[j].y == p.y && (layout[j].x > p.x ||
-                                             (layout[j].x == p.x && layout[j].s > p.s))))) {
-      layout[j + 1] = layout[j];
-      --j;
-    }
-    layout[j + 1] = p;
-  }
+  __syncwarp();
   float old_cost = 0.0f, new_cost = 0.0f;
-  for (int k = 0; k < ncur; ++k)
-    if (!piece_in(layout, nl, current[k])) old_cost = __fadd_rn(old_cost, score(current[k]));
-  for (int k = 0; k < nl; ++k)
-    if (!piece_in(current, ncur, layout[k])) new_cost = __fadd_rn(new_cost, score(layout[k]));
-  if (new_cost < old_cost)
-    for (int k = 0; k < nl; ++k)
-      if (!piece_in(current, ncur, layout[k]))
-        map_set_first(map, xb, bx + layout[k].x, by + layout[k].y, layout[k].s);
+  if (lane == 0) {
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        if (gone[r] & (1u << j)) old_cost = __fadd_rn(old_cost, sm.leaf[32 * r + j]);
+        if (added[r] & (1u << j)) new_cost = __fadd_rn(new_cost, sm.wide[32 * r + j]);
+      }
+  }
+  old_cost = __shfl_sync(0xffffffffu, old_cost, 0);
+  new_cost = __shfl_sync(0xffffffffu, new_cost, 0);
+  if (!(new_cost < old_cost)) return;
+  // the new pieces cover exactly the blocks the changed old ones did
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int i = lane + 32 * r;
+    if (added[r] & (1u << lane)) map_set_first(map, xb, bx + i % w, by + i / w, ns_of[r]);
+  }
 }
 
 // adjust_quant_field (src/ac_strategy/selection.rs:503-527), then the alpha
