@@ -99,11 +99,13 @@ struct SearchFrame {
 // ---------------------------------------------------------------------------
 
 template <int S>
-struct CostSmem {
+struct alignas(16) CostSmem {
   static constexpr int W = Shape<S>::W, H = Shape<S>::H, SIZE = W * H;
   float in[3][H][W + 1];  // gathered pixels; then the sse terms
   float co[3][SIZE];      // coefficients
   float mag[3][SIZE];     // magnitude-rate terms
+  // the running sums read whole channels of terms four at a time
+  static_assert(SIZE % 4 == 0 && (3 * H * (W + 1) + 3 * SIZE) % 4 == 0, "16-byte aligned terms");
 };
 
 // The block position of candidate `cand` of shape S: every block (DCT8),
@@ -255,13 +257,101 @@ __device__ __forceinline__ void warp_forward(const Frame& f, int c, int px, int 
   __syncwarp();
 }
 
+// warp_forward for the three channels at once: one gather, then each pass of
+// 1-D transforms spread over the channels' rows or columns together, so a
+// DCT8 takes two passes of 24 lanes instead of six of 8.  Every coefficient
+// comes from the same operations in the same order.
+template <int S>
+__device__ __forceinline__ void warp_forward3(const Frame& f, int px, int py,
+                                              float (*in)[Shape<S>::H][Shape<S>::W + 1],
+                                              float (*out)[Shape<S>::W * Shape<S>::H]) {
+  constexpr int W = Shape<S>::W, H = Shape<S>::H;
+  const int lane = threadIdx.x & 31;
+  const int w = f.a.width, h = f.a.height;
+  const int64_t plane = f.a.plane;
+#pragma unroll 4
+  for (int k = lane; k < W * H; k += 32) {
+    const int v = k / W, u = k % W;
+    const int64_t at = static_cast<int64_t>(imin(py + v, h - 1)) * w + imin(px + u, w - 1);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) in[c][v][u] = __ldg(f.xyb + c * plane + at);
+  }
+  __syncwarp();
+  if (S == kStDct) {
+    // dct8x8: rows, then the columns stored transposed, scaled 1/64
+    const int c = lane >> 3, r = lane & 7;
+    if (lane < 24) {
+      float b[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) b[k] = in[c][r][k];
+      dct1d_8(b);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) in[c][r][k] = b[k];
+    }
+    __syncwarp();
+    if (lane < 24) {
+      float b[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) b[k] = in[c][k][r];
+      dct1d_8(b);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) out[c][r * 8 + k] = b[k] * (1.0f / 64.0f);
+    }
+  } else if (S == kSt8x16) {
+    // rows first, stored out[v W + u]
+    const float scale = 1.0f / static_cast<float>(W * H);
+    for (int j = lane; j < 3 * H; j += 32) {
+      const int c = j / H, r = j % H;
+      float row[W];
+#pragma unroll
+      for (int u = 0; u < W; ++u) row[u] = in[c][r][u];
+      dct1d_n<W>(row);
+#pragma unroll
+      for (int u = 0; u < W; ++u) in[c][r][u] = row[u];
+    }
+    __syncwarp();
+    for (int j = lane; j < 3 * W; j += 32) {
+      const int c = j / W, u = j % W;
+      float col[H];
+#pragma unroll
+      for (int i = 0; i < H; ++i) col[i] = in[c][i][u];
+      dct1d_n<H>(col);
+#pragma unroll
+      for (int v = 0; v < H; ++v) out[c][v * W + u] = col[v] * scale;
+    }
+  } else {
+    // columns first, stored out[u H + v]
+    const float scale = 1.0f / static_cast<float>(W * H);
+    for (int j = lane; j < 3 * W; j += 32) {
+      const int c = j / W, u = j % W;
+      float col[H];
+#pragma unroll
+      for (int i = 0; i < H; ++i) col[i] = in[c][i][u];
+      dct1d_n<H>(col);
+#pragma unroll
+      for (int v = 0; v < H; ++v) in[c][v][u] = col[v];
+    }
+    __syncwarp();
+    for (int j = lane; j < 3 * H; j += 32) {
+      const int c = j / H, v = j % H;
+      float row[W];
+#pragma unroll
+      for (int u = 0; u < W; ++u) row[u] = in[c][v][u];
+      dct1d_n<W>(row);
+#pragma unroll
+      for (int u = 0; u < W; ++u) out[c][u * H + v] = row[u] * scale;
+    }
+  }
+  __syncwarp();
+}
+
 // The three channels' coefficients with chroma-from-luma applied
 // (prepare_strategy_coeffs, src/ac_strategy.rs:1380-1407).
 template <int S>
 __device__ __forceinline__ void warp_coefficients(const Frame& f, int bx, int by, CostSmem<S>& sm) {
   constexpr int SIZE = Shape<S>::W * Shape<S>::H;
   const int lane = threadIdx.x & 31;
-  for (int c = 0; c < 3; ++c) warp_forward<S>(f, c, bx * 8, by * 8, sm.in[c], sm.co[c]);
+  warp_forward3<S>(f, bx * 8, by * 8, sm.in, sm.co);
   // cmap_factors (src/ac_strategy.rs:1841-1857): the tile of the first block
   const int t = (by >> 3) * f.a.tiles_x + (bx >> 3);
   const float xf = fmla(static_cast<float>(f.ytox[t]), 1.0f / 84.0f, 0.0f);
@@ -369,11 +459,20 @@ __device__ __forceinline__ void rd_channel(const SearchFrame& s, const float* co
 
 // A running f32 sum in raster order by one thread (a skipped coefficient
 // adds +0, which leaves a sum of non-negative terms as it is).
+// `terms` is 16-byte aligned: four terms a shared load.
 template <int SIZE>
 __device__ __forceinline__ float serial_sum(const float* terms) {
+  static_assert(SIZE % 4 == 0, "terms are read four at a time");
+  const float4* quad = reinterpret_cast<const float4*>(terms);
   float sum = 0.0f;
-#pragma unroll 16
-  for (int i = 0; i < SIZE; ++i) sum = __fadd_rn(sum, terms[i]);
+#pragma unroll 4
+  for (int i = 0; i < SIZE / 4; ++i) {
+    const float4 v = quad[i];
+    sum = __fadd_rn(sum, v.x);
+    sum = __fadd_rn(sum, v.y);
+    sum = __fadd_rn(sum, v.z);
+    sum = __fadd_rn(sum, v.w);
+  }
   return sum;
 }
 
@@ -696,8 +795,8 @@ __global__ void __launch_bounds__(32 * kMaxTuneWarps) k_cost(const __grid_consta
 // the selection quantizer, then each channel's terms and its two running
 // sums (lanes 0 and 1), then the cost.
 constexpr int kCost32Threads = 96;
-struct Cost32Smem {
-  float in[3][32][33];  // gathered pixels; then the channel's sse terms
+struct alignas(16) Cost32Smem {
+  float in[3][32][33];  // gathered pixels; then the channel's sse terms (16-byte aligned)
   float co[3][1024];    // coefficients; then the channel's magnitude-rate terms
 };
 __global__ void __launch_bounds__(kCost32Threads) k_cost32(const __grid_constant__ Frame f) {
