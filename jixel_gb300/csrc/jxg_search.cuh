@@ -368,7 +368,9 @@ __device__ __forceinline__ void warp_coefficients(const Frame& f, int bx, int by
 // only DCT32X32 here; the erased energy is an f64 sum in raster order.
 //
 // The serial f64 sum R is only ever read as an f32.  The warp sums the same
-// non-negative terms in parallel (P); |R - P| <= (n + 36) u E for n <= 960
+// non-negative terms in parallel (P: four running sums of eight terms a
+// lane, their pairwise sum, then a butterfly over the lanes, so no term goes
+// through more than 14 additions); |R - P| <= (n + 36) u E for n <= 960
 // terms (u = 2^-53, E the exact sum; error bounds of recursive and pairwise
 // summation), below M = 2^-42 P.  Rounding to f32 is monotonic, so when
 // P - M and P + M round to the same f32 that f32 is R's; otherwise lane 0
@@ -386,9 +388,10 @@ __device__ __forceinline__ float selection_scale_32(const SearchFrame& s, const 
                ? __dmul_rn(static_cast<double>(l), static_cast<double>(l))
                : 0.0;
   };
-  double part = 0.0;
-#pragma unroll 4
-  for (int i = lane; i < 1024; i += 32) part = __dadd_rn(part, erased_term(i));
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+  for (int i = lane; i < 1024; i += 32) acc[(i >> 5) & 3] = __dadd_rn(acc[(i >> 5) & 3], erased_term(i));
+  double part = __dadd_rn(__dadd_rn(acc[0], acc[1]), __dadd_rn(acc[2], acc[3]));
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) part = __dadd_rn(part, __shfl_xor_sync(0xffffffffu, part, d));
   const double margin = __dmul_rn(part, 0x1p-42);
@@ -831,17 +834,20 @@ __global__ void __launch_bounds__(kCost32Threads) k_cost32(const __grid_constant
   uint32_t ms;
   // each lane writes the magnitude term over the coefficient it reads
   rd_channel<kSt32x32>(s, sm.co[c], c, q, sse, sm.co[c], &n, &ms);
-  __syncwarp();
-  if (lane < 2) {
-    const float sum = serial_sum<1024>(lane == 0 ? sse : sm.co[c]);
-    s_sum[lane * 3 + c] = sum;
-  }
   if (lane == 0) {
     s_nz[c] = n;
     s_ms[c] = ms;
   }
   __syncthreads();
-  if (threadIdx.x == 0) s.c32[bi] = rd_finish<kSt32x32>(f, s, bx, by, s_nz, s_ms, s_sum, s_sum + 3, kMetaR);
+  // the six running sums (sse, then magnitude, per channel) on lanes 0-5 of
+  // one warp: the same chains, a third of the instructions
+  if (c != 0) return;
+  if (lane < 6) {
+    const int ch = lane % 3;
+    s_sum[lane] = serial_sum<1024>(lane < 3 ? &sm.in[ch][0][0] : sm.co[ch]);
+  }
+  __syncwarp();
+  if (lane == 0) s.c32[bi] = rd_finish<kSt32x32>(f, s, bx, by, s_nz, s_ms, s_sum, s_sum + 3, kMetaR);
 }
 
 
@@ -1920,7 +1926,9 @@ __device__ __forceinline__ void layout_y_dc(const KernelArgs& a, const float* co
 }
 
 // Y AC round trip (quantize_roundtrip_y_block, src/group.rs:795-820): the
-// levels parked in ylev, co_y replaced by the dequantised AC
+// levels parked in ylev, co_y's AC replaced by the dequantised AC.  The
+// round trip's LLF is zero; co_y keeps its LLF coefficients (the Y DC reads
+// them) and the chroma-from-luma step reads zero there.
 template <int S>
 __device__ __forceinline__ void layout_y_roundtrip(const SearchFrame& s, int32_t quant, float* co_y,
                                                    int32_t* ylev) {
@@ -1937,7 +1945,7 @@ __device__ __forceinline__ void layout_y_roundtrip(const SearchFrame& s, int32_t
     const int32_t q = quantize_level(val, layout_threshold(thr_y, i, L::CX, L::CY));
     ylev[i] = q;
     const int width = L::CX * 8, r = i / width, u = i % width;
-    co_y[i] = (r < L::CY && u < L::CX) ? 0.0f : __fmul_rn(__fmul_rn(bias_level(1, q), mat_y[i]), inv_qac);
+    if (!(r < L::CY && u < L::CX)) co_y[i] = __fmul_rn(__fmul_rn(bias_level(1, q), mat_y[i]), inv_qac);
   }
 }
 
@@ -1949,7 +1957,28 @@ __device__ __forceinline__ void layout_cfl(const Frame& f, int bx, int by, int c
   const int tt = (by >> 3) * f.a.tiles_x + (bx >> 3);
   const float factor = c == 0 ? fmla(static_cast<float>(f.ytox[tt]), 1.0f / 84.0f, 0.0f)
                               : fmla(static_cast<float>(f.ytob[tt]), 1.0f / 84.0f, 1.0f);
-  for (int i = lane; i < LayoutShape<S>::SIZE; i += 32) co_c[i] = fmla(-factor, co_y[i], co_c[i]);
+  constexpr int CX = LayoutShape<S>::CX, CY = LayoutShape<S>::CY, WIDTH = CX * 8;
+  for (int i = lane; i < LayoutShape<S>::SIZE; i += 32) {
+    const bool llf = i / WIDTH < CY && i % WIDTH < CX;  // the round trip's zeros
+    co_c[i] = fmla(-factor, llf ? 0.0f : co_y[i], co_c[i]);
+  }
+}
+
+// one covered block's X and B DC levels with the DC chroma-from-luma, and
+// its three channels' DC stores
+__device__ __forceinline__ void layout_dc_block(const Frame& f, int64_t b, int64_t nb, float xdp,
+                                                float bdp, int16_t ydq) {
+  const KernelArgs& a = f.a;
+  int16_t xq;
+  if (a.cfl_dc_factor_x != 0.0f)
+    xq = cast_i16(roundf(fmla(xdp, a.inv_dc_factor[0], __fmul_rn(-static_cast<float>(ydq), a.cfl_dc_factor_x))));
+  else
+    xq = cast_i16(roundf(__fmul_rn(xdp, a.inv_dc_factor[0])));
+  const int16_t bq = cast_i16(roundf(fmla(bdp, a.inv_dc_factor[2],
+                                          __fmul_rn(-static_cast<float>(ydq), a.cfl_dc_factor_b))));
+  f.quant_dc[b] = xq;
+  f.quant_dc[nb + b] = ydq;
+  f.quant_dc[2 * nb + b] = bq;
 }
 
 // X and B DC levels with the DC chroma-from-luma, and the three channels' DC stores
@@ -1966,17 +1995,7 @@ __device__ __forceinline__ void layout_xb_dc(const Frame& f, int bx, int by, con
   for (int iy = 0; iy < L::COVY; ++iy)
     for (int ix = 0; ix < L::COVX; ++ix) {
       const int k = iy * L::COVX + ix;
-      const int64_t b = static_cast<int64_t>(by + iy) * xb + bx + ix;
-      int16_t xq;
-      if (a.cfl_dc_factor_x != 0.0f)
-        xq = cast_i16(roundf(fmla(xdp[k], a.inv_dc_factor[0], __fmul_rn(-static_cast<float>(ydq[k]), a.cfl_dc_factor_x))));
-      else
-        xq = cast_i16(roundf(__fmul_rn(xdp[k], a.inv_dc_factor[0])));
-      const int16_t bq = cast_i16(roundf(fmla(bdp[k], a.inv_dc_factor[2],
-                                              __fmul_rn(-static_cast<float>(ydq[k]), a.cfl_dc_factor_b))));
-      f.quant_dc[b] = xq;
-      f.quant_dc[nb + b] = ydq[k];
-      f.quant_dc[2 * nb + b] = bq;
+      layout_dc_block(f, static_cast<int64_t>(by + iy) * xb + bx + ix, nb, xdp[k], bdp[k], ydq[k]);
     }
 }
 
@@ -2083,9 +2102,11 @@ __device__ __forceinline__ void layout_piece(const Frame& f, const SearchFrame& 
 }
 
 // The 32x32 transforms: a CTA of three warps each, one per channel: the
-// three forward transforms, then the Y DC and round trip, then CfL on X and
-// B, then the X/B DC (one thread) beside the three channels' levels, then
-// the counts.
+// three forward transforms; then the Y round trip beside the Y DC (one
+// thread of the X warp: it reads the LLF, which the round trip leaves
+// alone); then on each warp its channel's levels, the X and B warps first
+// taking chroma-from-luma and their DC (one thread each); then the counts
+// beside the 16 blocks' DC stores.
 constexpr int kLayout32Threads = 96;
 struct Layout32Smem {
   float in[3][32][33];
@@ -2096,6 +2117,7 @@ __global__ void __launch_bounds__(kLayout32Threads) k_layout32(const __grid_cons
   extern __shared__ __align__(16) unsigned char layout_smem_raw[];
   Layout32Smem& sm = *reinterpret_cast<Layout32Smem*>(layout_smem_raw);
   __shared__ int16_t s_ydq[16];
+  __shared__ float s_dc[2][16];  // X and B DC of the covered blocks
   __shared__ int s_nz[3];
   __shared__ uint32_t s_last[3];
   constexpr int S = kSt32x32;
@@ -2107,15 +2129,14 @@ __global__ void __launch_bounds__(kLayout32Threads) k_layout32(const __grid_cons
   warp_forward<S>(f, c, bx * 8, by * 8, sm.in[c], sm.co[c]);
   const int32_t quant = f.qf[by * f.a.xb + bx];
   __syncthreads();
-  if (c == 1) {
-    if (lane == 0) layout_y_dc<S>(f.a, sm.co[1], s_ydq);
+  if (c == 1) layout_y_roundtrip<S>(s, quant, sm.co[1], sm.ylev);
+  else if (c == 0 && lane == 0) layout_y_dc<S>(f.a, sm.co[1], s_ydq);
+  __syncthreads();
+  if (c != 1) {
+    layout_cfl<S>(f, bx, by, c, sm.co[c], sm.co[1]);
     __syncwarp();
-    layout_y_roundtrip<S>(s, quant, sm.co[1], sm.ylev);
+    if (lane == 0) piece_dc(dct_kind_of(S), sm.co[c], s_dc[c >> 1]);
   }
-  __syncthreads();
-  if (c != 1) layout_cfl<S>(f, bx, by, c, sm.co[c], sm.co[1]);
-  __syncthreads();
-  if (threadIdx.x == 0) layout_xb_dc<S>(f, bx, by, sm.co[0], sm.co[2], s_ydq);
   int n;
   uint32_t lst;
   layout_levels<S>(f, s, bx, by, quant, c, sm.co[c], sm.ylev, &n, &lst);
@@ -2124,7 +2145,12 @@ __global__ void __launch_bounds__(kLayout32Threads) k_layout32(const __grid_cons
     s_last[c] = lst;
   }
   __syncthreads();
-  if (c == 0) layout_counts<S>(f, bx, by, s_nz, s_last);
+  if (c == 0) {
+    layout_counts<S>(f, bx, by, s_nz, s_last);
+  } else if (c == 1 && lane < 16) {
+    const int64_t b = static_cast<int64_t>(by + lane / 4) * f.a.xb + bx + lane % 4;
+    layout_dc_block(f, b, static_cast<int64_t>(f.a.xb) * f.a.yb, s_dc[0][lane], s_dc[1][lane], s_ydq[lane]);
+  }
 }
 
 // One warp per position a transform of shape S can start at; the warp codes
