@@ -836,9 +836,10 @@ int enqueue_pass(Context* c, const PassImage* imgs, int n, PixelSource src, bool
                                   cudaMemcpyDeviceToDevice, s));
       if ((st = launch(c, "k_qf_median", timed, [&] { k_qf_median<<<1, 256, 0, s>>>(f0); }))) return st;
     }
+    // a searched frame takes only the CfL maps from the tile kernel
     if ((st = launch(c, "k_tile_quantize", timed, [&] {
            k_tile_quantize<<<static_cast<unsigned>(c->total_tiles), kTileThreads, kTileSmemBytes, s>>>(
-               f0, c->d_pos);
+               f0, c->d_pos, searched ? 1 : 0);
          })))
       return st;
     if (searched && (st = enqueue_search(c, f0, timed))) return st;
