@@ -218,6 +218,34 @@ int32_t jxg_frontend(void* ctx, const void* pixels, uint64_t width, uint64_t hei
                      int32_t channels, int32_t bits, const jxg_config* config,
                      jxg_frame_params* params, jxg_frontend_output* out);
 
+/* Coefficient-order statistics --------------------------------------------
+ * The first AC pass's tally for custom coefficient orders (OrderStats,
+ * src/coeff_order.rs:511-540, tallied by the tokeniser at
+ * src/group.rs:2555-2574; the reference collects it from Speed::Fast up and
+ * derives the orders with derive_orders, src/frame/vardct_encoder.rs:1147-1153).
+ * The order groups are ORDER_SPECS (src/coeff_order.rs:117-125): slot
+ * s = 0..6 holds order group s with 64, 64, 256, 1024, 128, 256 and 512
+ * coefficients (DCT8; the 8x8-sized transforms; DCT16X16; DCT32X32;
+ * DCT16X8 / DCT8X16; DCT32X8 / DCT8X32; DCT32X16 / DCT16X32).  Counters
+ * are laid out [slot][channel X, Y, B][raw coefficient index], slot s
+ * starting at 3 x the sizes of the slots before it, JXG_ORDER_COUNTERS in
+ * all; orders use the same layout with scan position in place of raw index. */
+#define JXG_ORDER_SLOTS 7
+#define JXG_ORDER_COUNTERS 6912
+/* The order statistics of the context's last pass (its first frame): per
+ * slot, channel and raw index the transforms whose level there is non-zero,
+ * counted over the whole transform; `blocks` per slot the transforms.
+ * `counts` holds JXG_ORDER_COUNTERS, `blocks` JXG_ORDER_SLOTS.  Waits. */
+int32_t jxg_order_stats(void* ctx, uint32_t* counts, uint32_t* blocks);
+/* derive_orders (src/coeff_order.rs:621-673), on the host: from statistics
+ * laid out as jxg_order_stats writes them, the used-order mask (bit = order
+ * group), every slot's three orders (scan position -> raw index; natural
+ * where not adopted; JXG_ORDER_COUNTERS entries) and, when `scan_moved` is
+ * set, the share of the expected scan walk the adopted orders remove.  Needs
+ * no device. */
+int32_t jxg_derive_orders(const uint32_t* counts, const uint32_t* blocks, uint16_t* used_mask,
+                          uint32_t* orders, double* scan_moved);
+
 /* Asynchronous front end --------------------------------------------------
  * jxg_frontend_enqueue enqueues on the context's stream the upload of
  * `pixels`, the pass, and the download of `params` and every requested

@@ -25,6 +25,8 @@ EXPORTS = [
     "jxg_frontend_params",
     "jxg_frontend_fetch",
     "jxg_frontend",
+    "jxg_order_stats",
+    "jxg_derive_orders",
     "jxg_frontend_enqueue",
     "jxg_frontend_wait",
     "jxg_batch_create",
@@ -155,6 +157,8 @@ def load() -> ctypes.CDLL:
         "jxg_frontend_fetch": (i32, [vp, ctypes.POINTER(FrontendOutput)]),
         "jxg_frontend": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config),
                                ctypes.POINTER(FrameParams), ctypes.POINTER(FrontendOutput)]),
+        "jxg_order_stats": (i32, [vp, vp, vp]),
+        "jxg_derive_orders": (i32, [vp, vp, vp, vp, vp]),
         "jxg_frontend_enqueue": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config),
                                        ctypes.POINTER(FrameParams),
                                        ctypes.POINTER(FrontendOutput)]),

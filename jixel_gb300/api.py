@@ -191,6 +191,42 @@ def ac_bits_estimate(result: "FrontendResult") -> float:
     return bits
 
 
+# ORDER_SPECS (src/coeff_order.rs:117-125): the coefficients of each order
+# slot (DCT8; the 8x8-sized transforms; 16x16; 32x32; 16x8 / 8x16; 32x8 /
+# 8x32; 32x16 / 16x32); statistics and orders hold three channels of each
+ORDER_SLOT_SIZES = (64, 64, 256, 1024, 128, 256, 512)
+_ORDER_COUNTERS = 3 * sum(ORDER_SLOT_SIZES)
+
+
+def _split_orders(flat: np.ndarray) -> list[np.ndarray]:
+    out, off = [], 0
+    for n in ORDER_SLOT_SIZES:
+        out.append(flat[off:off + 3 * n].reshape(3, n).copy())
+        off += 3 * n
+    return out
+
+
+def derive_orders(counts, blocks) -> tuple[int, list[np.ndarray], float]:
+    """`derive_orders` (src/coeff_order.rs:621-673) on the host
+    (jxg_derive_orders): from per-slot statistics, as
+    `FrontendContext.order_stats` returns them, the used-order mask (bit =
+    order group), per slot its (3, size) orders (scan position -> raw index,
+    natural where not adopted) and the share of the expected scan walk the
+    adopted orders remove."""
+    flat = np.ascontiguousarray(np.concatenate([np.asarray(c, np.uint32).reshape(-1) for c in counts]))
+    blk = np.ascontiguousarray(np.asarray(blocks, np.uint32))
+    if flat.size != _ORDER_COUNTERS or blk.size != len(ORDER_SLOT_SIZES):
+        raise EncodeError(100, "order statistics: one (3, size) array and one count per slot")
+    orders = np.zeros(_ORDER_COUNTERS, np.uint32)
+    used = ctypes.c_uint16()
+    moved = ctypes.c_double()
+    st = L.load().jxg_derive_orders(flat.ctypes.data, blk.ctypes.data, ctypes.byref(used),
+                                    orders.ctypes.data, ctypes.byref(moved))
+    if st:
+        raise EncodeError(st, "jxg_derive_orders")
+    return used.value, _split_orders(orders), moved.value
+
+
 def _as_hwc(pixels: np.ndarray) -> np.ndarray:
     """(h, w) grey samples as (h, w, 1); other shapes unchanged."""
     pixels = np.ascontiguousarray(pixels)
@@ -364,6 +400,16 @@ class FrontendContext:
 
     def wait(self):
         self._check(self._lib.jxg_frontend_wait(self._ctx))
+
+    def order_stats(self) -> tuple[list[np.ndarray], np.ndarray]:
+        """The coefficient-order statistics of the last pass's first frame
+        (jxg_order_stats): per order slot a (3, size) u32 array of the
+        transforms whose level is non-zero at each raw index, and the
+        transforms per slot."""
+        counts = np.zeros(_ORDER_COUNTERS, np.uint32)
+        blocks = np.zeros(len(ORDER_SLOT_SIZES), np.uint32)
+        self._check(self._lib.jxg_order_stats(self._ctx, counts.ctypes.data, blocks.ctypes.data))
+        return _split_orders(counts), blocks
 
     def batch(self, pixels_on_device: bool = False) -> "FrontendBatch":
         """A batch of frames run as one pass on this context."""

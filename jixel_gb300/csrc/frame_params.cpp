@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 namespace jxg {
 namespace {
@@ -506,7 +507,121 @@ float merge_margin(float d, float hq, float base) {
   return banded(hq, base, d) * (1.0f - fade * (1.0f - 0.82f));
 }
 
+// tokenize_permutation (src/coeff_order.rs:89-105) of `zigzag` (a
+// permutation in natural-scan space), its first `skip` entries left alone:
+// only the count of its tokens, the length of the Lehmer code (Fenwick tree,
+// compute_lehmer_code, :54-71) without its trailing zeros, plus one.
+size_t permutation_token_count(const std::vector<uint32_t>& zigzag, int skip) {
+  const int n = static_cast<int>(zigzag.size());
+  std::vector<uint32_t> tree(n + 1, 0), code(n);
+  for (int idx = 0; idx < n; ++idx) {
+    const uint32_t s = zigzag[idx];
+    uint32_t penalty = 0;
+    for (uint32_t i = s + 1; i != 0; i &= i - 1) penalty += tree[i];
+    code[idx] = s - penalty;
+    for (uint32_t i = s + 1; i < static_cast<uint32_t>(n + 1); i += i & (~i + 1)) ++tree[i];
+  }
+  int end = n;
+  while (end > skip && code[end - 1] == 0) --end;
+  return 1 + static_cast<size_t>(end - skip);
+}
+
+// OrderStats::expected_walk (src/coeff_order.rs:570-581): the expected
+// tokens a block under `order` walks, in f64.
+double expected_walk(const uint32_t* counts, uint32_t blocks, const std::vector<uint32_t>& order,
+                     int llf) {
+  const double inv = 1.0 / static_cast<double>(std::max(blocks, 1u));
+  double none_at_or_after = 1.0, expected = 0.0;
+  for (int k = static_cast<int>(order.size()) - 1; k >= llf; --k) {
+    expected += 1.0 - none_at_or_after;
+    const double p = std::clamp(static_cast<double>(counts[order[k]]) * inv, 0.0, 1.0);
+    none_at_or_after *= 1.0 - p;
+  }
+  return expected;
+}
+
+// OrderStats::derive (src/coeff_order.rs:586-601): the LLF entries stay, the
+// rest by descending count, ties by natural rank (unique keys).
+std::vector<uint32_t> derive_order(const uint32_t* counts, const std::vector<uint32_t>& natural,
+                                   int llf) {
+  const int n = static_cast<int>(natural.size());
+  std::vector<uint64_t> ranked;
+  ranked.reserve(n - llf);
+  for (int rank = llf; rank < n; ++rank)
+    ranked.push_back((static_cast<uint64_t>(0xFFFFFFFFu - counts[natural[rank]]) << 32) |
+                     static_cast<uint64_t>(rank));
+  std::sort(ranked.begin(), ranked.end());
+  std::vector<uint32_t> out(natural.begin(), natural.begin() + llf);
+  for (uint64_t key : ranked) out.push_back(natural[static_cast<uint32_t>(key)]);
+  return out;
+}
+
 }  // namespace
+
+// ORDER_SPECS (src/coeff_order.rs:117-125)
+const OrderSpec kOrderSpecs[kOrderSlots] = {{0, 1, 64},    {1, 1, 64},   {2, 4, 256}, {3, 16, 1024},
+                                            {4, 2, 128},   {5, 4, 256},  {6, 8, 512}};
+
+int order_slot_offset(int slot) {
+  int off = 0;
+  for (int k = 0; k < slot; ++k) off += 3 * kOrderSpecs[k].size;
+  return off;
+}
+
+// derive_orders (src/coeff_order.rs:621-673).  The natural order of each
+// slot is natural_scan_generic's (CoeffOrders::natural, :425-448): 8x8 for
+// the DCT8 and 8x8-sized groups, then 16x16, 32x32, 16x8, 8x32 and 32x16.
+double derive_orders(const uint32_t* counts, const uint32_t* blocks, uint16_t* used_mask,
+                     uint32_t* orders) {
+  constexpr uint32_t kMinBlocks = 64;           // MIN_BLOCKS_FOR_ORDER, :606
+  constexpr double kBitsPerSavedToken = 0.2;    // :608
+  constexpr double kGateMargin = 1.5;           // :611
+  constexpr double kBitsPerPermutationToken = 5.0;  // :616
+  static const int shape[kOrderSlots][2] = {{1, 1}, {1, 1}, {2, 2}, {4, 4}, {2, 1}, {4, 1}, {4, 2}};
+  uint16_t used = 0;
+  double natural_walk = 0.0, saved_walk = 0.0;
+  for (int slot = 0; slot < kOrderSlots; ++slot) {
+    const OrderSpec& spec = kOrderSpecs[slot];
+    const int off = order_slot_offset(slot), size = spec.size, llf = spec.llf;
+    std::vector<uint16_t> scan16(size), pos16(size);
+    natural_scan(shape[slot][0], shape[slot][1], scan16.data(), pos16.data());
+    const std::vector<uint32_t> natural(scan16.begin(), scan16.end());
+    for (int c = 0; c < 3; ++c) std::copy(natural.begin(), natural.end(), orders + off + c * size);
+    const uint32_t nb = blocks[slot];
+    if (nb < kMinBlocks) continue;
+    std::vector<uint32_t> derived[3];
+    double saved_bits = 0.0, cost_bits = 0.0, slot_saved_walk = 0.0;
+    bool any = false;
+    for (int c = 0; c < 3; ++c) {
+      const uint32_t* cnt = counts + off + c * size;
+      std::vector<uint32_t> candidate = derive_order(cnt, natural, llf);
+      const double walk = expected_walk(cnt, nb, natural, llf);
+      const double gain = walk - expected_walk(cnt, nb, candidate, llf);
+      natural_walk += walk * static_cast<double>(nb);
+      std::vector<uint32_t> zigzag(size);
+      for (int k = 0; k < size; ++k) zigzag[k] = pos16[candidate[k]];
+      const size_t tokens = permutation_token_count(zigzag, llf);
+      const double channel_saved = gain * static_cast<double>(nb) * kBitsPerSavedToken;
+      const double channel_cost = static_cast<double>(tokens) * kBitsPerPermutationToken;
+      if (gain > 0.0 && channel_saved > channel_cost * kGateMargin) {
+        any = true;
+        slot_saved_walk += gain * static_cast<double>(nb);
+        saved_bits += channel_saved;
+        cost_bits += channel_cost;
+        derived[c] = std::move(candidate);
+      } else {
+        derived[c] = natural;
+      }
+    }
+    if (any && saved_bits > cost_bits * kGateMargin) {
+      used = static_cast<uint16_t>(used | (1u << spec.group));
+      for (int c = 0; c < 3; ++c) std::copy(derived[c].begin(), derived[c].end(), orders + off + c * size);
+      saved_walk += slot_saved_walk;
+    }
+  }
+  *used_mask = used;
+  return natural_walk > 0.0 ? saved_walk / natural_walk : 0.0;
+}
 
 void rate_log2_table(float* out) {
   for (int i = 0; i < kRateLog2Entries; ++i) out[i] = ::log2f(1.0f + static_cast<float>(i));

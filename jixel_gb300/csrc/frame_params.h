@@ -142,4 +142,23 @@ void exp2_table(float out[64]);
 // libjxl natural 8x8 order: scan position -> raw coefficient index.
 void natural_order_8x8(uint8_t scan[64], uint8_t position[64]);
 
+// Coefficient-order statistics (src/coeff_order.rs).  The order groups the
+// reference signals, ORDER_SPECS (:117-125), as (order group, LLF entries,
+// coefficients); statistics and orders are laid out [slot][channel][raw]
+// (orders: [slot][channel][scan position]), slot s starting at
+// order_slot_offset(s).
+constexpr int kOrderSlots = 7;
+constexpr int kOrderCounters = 3 * (64 + 64 + 256 + 1024 + 128 + 256 + 512);
+struct OrderSpec {
+  int group, llf, size;
+};
+extern const OrderSpec kOrderSpecs[kOrderSlots];
+int order_slot_offset(int slot);
+// derive_orders (src/coeff_order.rs:621-673) from the natural orders, over
+// pass-one statistics (`counts`, `blocks` per slot): the used-order mask, the
+// orders (natural where not adopted) and the share of the expected scan
+// walk the adopted orders remove.
+double derive_orders(const uint32_t* counts, const uint32_t* blocks, uint16_t* used_mask,
+                     uint32_t* orders);
+
 }  // namespace jxg

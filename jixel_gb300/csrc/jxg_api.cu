@@ -174,6 +174,7 @@ struct Context {
   float *refine_theta = nullptr, *refine_grad = nullptr, *refine_adam = nullptr;
   int32_t refine_steps = 0;
   DevBuf field_buf;  // a caller's field, staged for jxg_frontend_run_with_field
+  DevBuf order_buf;  // the order statistics' counters and per-slot block counts
   // launch geometry of the tunable search and layout kernels (warps per CTA)
   uint8_t tune[jxg::kTuneKernels] = {4, 4, 4, 4, 4, 4, 4, 4, jxg::kRetileWarps, jxg::kSiteWarps};
   // timing
@@ -1389,6 +1390,46 @@ int32_t jxg_frontend_fetch(void* ctx, jxg_frontend_output* out) {
   if (!c || !out) return JXG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(c->device);
   return jxg::fetch_frame(c, 0, out);
+}
+
+int32_t jxg_order_stats(void* ctx, uint32_t* counts, uint32_t* blocks) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !counts || !blocks) return JXG_ERR_INVALID_ARGUMENT;
+  if (!c->have_frame || c->layouts.empty())
+    return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "no frame in the last pass");
+  cudaSetDevice(c->device);
+  const jxg::FrameLayout& L = c->layouts[0];
+  const int xb = static_cast<int>(L.info.xsize_blocks), yb = static_cast<int>(L.info.ysize_blocks);
+  const size_t bytes = (jxg::kOrderCounters + jxg::kOrderSlots) * sizeof(uint32_t);
+  int st = jxg::ensure(c, c->order_buf, bytes);
+  if (st) return st;
+  uint32_t* d_counts = static_cast<uint32_t*>(c->order_buf.ptr);
+  uint32_t* d_blocks = d_counts + jxg::kOrderCounters;
+  cudaStream_t s = c->stream;
+  JXG_CUDA(c, cudaMemsetAsync(d_counts, 0, bytes, s));
+  const int64_t nb = static_cast<int64_t>(xb) * yb;
+  const int warps = jxg::kOrderStatsThreads / 32;
+  const unsigned grid = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((nb + warps - 1) / warps, 608)));
+  st = jxg::launch(c, "k_order_stats", c->timing, [&] {
+    jxg::k_order_stats<<<grid, jxg::kOrderStatsThreads, 0, s>>>(
+        static_cast<const int16_t*>(c->levels.ptr) + 192 * L.block_off,
+        L.searched ? static_cast<const uint8_t*>(c->search_map.ptr) : nullptr,
+        L.searched ? c->d_pos_identity : c->d_pos, xb, yb, d_counts, d_blocks);
+  });
+  if (st) return st;
+  JXG_CUDA(c, cudaMemcpyAsync(counts, d_counts, jxg::kOrderCounters * sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, s));
+  JXG_CUDA(c, cudaMemcpyAsync(blocks, d_blocks, jxg::kOrderSlots * sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, s));
+  return jxg::wait(c);
+}
+
+int32_t jxg_derive_orders(const uint32_t* counts, const uint32_t* blocks, uint16_t* used_mask,
+                          uint32_t* orders, double* scan_moved) {
+  if (!counts || !blocks || !used_mask || !orders) return JXG_ERR_INVALID_ARGUMENT;
+  const double moved = jxg::derive_orders(counts, blocks, used_mask, orders);
+  if (scan_moved) *scan_moved = moved;
+  return JXG_OK;
 }
 
 int32_t jxg_frontend_wait(void* ctx) {

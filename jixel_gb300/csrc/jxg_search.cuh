@@ -2336,6 +2336,70 @@ __global__ void __launch_bounds__(kLayoutTokThreads) k_tokenize_layout(
   }
 }
 
+// OrderStats::tally / tally_block (src/coeff_order.rs:511-540) over a
+// frame's pass-one levels, as the tokeniser calls them (src/group.rs:
+// 2555-2574): per order slot the transforms (first blocks) it holds, and per
+// slot, channel and raw coefficient index the transforms whose level there is
+// non-zero, over the whole transform.  `map` is the strategy map of a
+// searched frame (null: every block a DCT8); `position_g` maps a raw index to
+// its place in a block's stored levels.  A warp takes one block at a time;
+// the CTA's counts gather in shared memory, then one global add per non-zero
+// counter (integer counts: the order of the adds does not matter).
+constexpr int kOrderStatsThreads = 256;
+__device__ __forceinline__ int order_slot_of_strategy(int st) {
+  // STRATEGY_CODE_LUT (src/dc_group_data.rs:79-81), K_STRATEGY_ORDER
+  // (src/ac_context.rs:80-83) and ORDER_SPECS (src/coeff_order.rs:117-125)
+  // for the strategies a frame of this build holds
+  switch (st) {
+    case kStDct: return 0;
+    case kSt16x16: return 2;
+    case kSt32x32: return 3;
+    case kSt16x8:
+    case kSt8x16: return 4;
+    default: return -1;
+  }
+}
+__device__ __forceinline__ int order_counter_offset(int slot) {
+  // 3 x (64, 64, 256, 1024, 128, 256, 512), accumulated
+  constexpr int kOffsets[kOrderSlots] = {0, 192, 384, 1152, 4224, 4608, 5376};
+  return kOffsets[slot];
+}
+__global__ void __launch_bounds__(kOrderStatsThreads)
+    k_order_stats(const int16_t* __restrict__ levels, const uint8_t* __restrict__ map,
+                  const uint8_t* __restrict__ position_g, int xb, int yb,
+                  uint32_t* __restrict__ counts, uint32_t* __restrict__ blocks) {
+  __shared__ uint32_t s_counts[kOrderCounters];
+  __shared__ uint32_t s_blocks[kOrderSlots];
+  __shared__ uint8_t position[64];
+  for (int i = threadIdx.x; i < kOrderCounters; i += blockDim.x) s_counts[i] = 0u;
+  if (threadIdx.x < kOrderSlots) s_blocks[threadIdx.x] = 0u;
+  if (threadIdx.x < 64) position[threadIdx.x] = position_g[threadIdx.x];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+  const int64_t nb = static_cast<int64_t>(xb) * yb;
+  for (int64_t b = static_cast<int64_t>(blockIdx.x) * warps + (threadIdx.x >> 5); b < nb;
+       b += static_cast<int64_t>(gridDim.x) * warps) {
+    const uint8_t cell = map ? map[b] : static_cast<uint8_t>(1);
+    if (!(cell & 1)) continue;
+    const int st = cell >> 1, slot = order_slot_of_strategy(st);
+    if (slot < 0) continue;
+    const int bx = static_cast<int>(b % xb), by = static_cast<int>(b / xb);
+    const int cx = cov_x_of(st), size = cx * cov_y_of(st) * 64;
+    if (lane == 0) atomicAdd(&s_blocks[slot], 1u);
+    uint32_t* sc = s_counts + order_counter_offset(slot);
+    for (int c = 0; c < 3; ++c)
+      for (int i = lane; i < size; i += 32) {
+        const int chunk = i >> 6;
+        const int64_t blk = static_cast<int64_t>(by + chunk / cx) * xb + bx + chunk % cx;
+        if (levels[blk * 192 + c * 64 + position[i & 63]] != 0) atomicAdd(&sc[c * size + i], 1u);
+      }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kOrderCounters; i += blockDim.x)
+    if (s_counts[i]) atomicAdd(&counts[i], s_counts[i]);
+  if (threadIdx.x < kOrderSlots && s_blocks[threadIdx.x]) atomicAdd(&blocks[threadIdx.x], s_blocks[threadIdx.x]);
+}
+
 // Dynamic shared memory above the 48 KB default for the search kernels.
 inline cudaError_t set_search_attributes() {
   cudaError_t e = cudaSuccess;

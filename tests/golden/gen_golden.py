@@ -90,6 +90,11 @@ def main(root: str) -> None:
     order16x16 = _array(ac, "K_COEFF_ORDER_16X16:")
     order32x32 = _array(ac, "K_COEFF_ORDER_32X32:")
     assert (len(order16x8), len(order16x16), len(order32x32)) == (128, 256, 1024)
+    order32x16 = _array(ac, "K_COEFF_ORDER_32X16:")
+    assert len(order32x16) == 512
+    dgd = open(os.path.join(root, "src/dc_group_data.rs")).read()
+    strategy_code_lut = _array(dgd, "STRATEGY_CODE_LUT:")
+    assert len(strategy_code_lut) == 24
     strategy_order = _array(ac, "K_STRATEGY_ORDER:")
     block_ctx_map = _array(ac, "K_COMPACT_BLOCK_CONTEXT_MAP:")
     assert len(strategy_order) == 27 and len(block_ctx_map) == 39
@@ -102,6 +107,8 @@ def main(root: str) -> None:
         "coeff_order_16x8": order16x8,
         "coeff_order_16x16": order16x16,
         "coeff_order_32x32": order32x32,
+        "coeff_order_32x16": order32x16,
+        "strategy_code_lut": strategy_code_lut,
         "strategy_order": strategy_order,
         "compact_block_context_map": block_ctx_map,
         "afv_basis_transpose": afv_basis,
