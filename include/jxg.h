@@ -237,6 +237,15 @@ int32_t jxg_frontend(void* ctx, const void* pixels, uint64_t width, uint64_t hei
  * counted over the whole transform; `blocks` per slot the transforms.
  * `counts` holds JXG_ORDER_COUNTERS, `blocks` JXG_ORDER_SLOTS.  Waits. */
 int32_t jxg_order_stats(void* ctx, uint32_t* counts, uint32_t* blocks);
+/* pixel_chromacity_steps (src/frame/chroma.rs:89-165; the reference runs it
+ * in configure_chroma, :389-450, from Speed::Fast up at distances from
+ * PIXEL_CHROMACITY_MIN_DISTANCE, to raise the X and B quant-scale floors) on
+ * the context's last pass (its first frame's XYB, after the invisible fill
+ * and the grey snap, as the reference's).  `counts` (7, optional): the X
+ * steps reaching 0.015 / 0.022 / 0.026, the B - Y steps above 0.28 / 0.33 /
+ * 0.38, the strongly exposed blue pixels; `x_steps` / `b_steps` (optional):
+ * the extra steps.  Waits. */
+int32_t jxg_pixel_chromacity(void* ctx, uint32_t* counts, uint32_t* x_steps, uint32_t* b_steps);
 /* derive_orders (src/coeff_order.rs:621-673), on the host: from statistics
  * laid out as jxg_order_stats writes them, the used-order mask (bit = order
  * group), every slot's three orders (scan position -> raw index; natural

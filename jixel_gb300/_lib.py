@@ -26,6 +26,7 @@ EXPORTS = [
     "jxg_frontend_fetch",
     "jxg_frontend",
     "jxg_order_stats",
+    "jxg_pixel_chromacity",
     "jxg_derive_orders",
     "jxg_frontend_enqueue",
     "jxg_frontend_wait",
@@ -158,6 +159,7 @@ def load() -> ctypes.CDLL:
         "jxg_frontend": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config),
                                ctypes.POINTER(FrameParams), ctypes.POINTER(FrontendOutput)]),
         "jxg_order_stats": (i32, [vp, vp, vp]),
+        "jxg_pixel_chromacity": (i32, [vp, vp, vp, vp]),
         "jxg_derive_orders": (i32, [vp, vp, vp, vp, vp]),
         "jxg_frontend_enqueue": (i32, [vp, vp, u64, u64, i32, i32, ctypes.POINTER(Config),
                                        ctypes.POINTER(FrameParams),

@@ -401,6 +401,17 @@ class FrontendContext:
     def wait(self):
         self._check(self._lib.jxg_frontend_wait(self._ctx))
 
+    def pixel_chromacity(self) -> tuple[np.ndarray, int, int]:
+        """pixel_chromacity_steps (src/frame/chroma.rs:89-165) on the last
+        pass's XYB (jxg_pixel_chromacity): the seven counts (X steps at three
+        levels, B - Y steps at three, exposed blue) and the extra X and B
+        quant-scale steps."""
+        counts = np.zeros(7, np.uint32)
+        xs, bs = ctypes.c_uint32(), ctypes.c_uint32()
+        self._check(self._lib.jxg_pixel_chromacity(self._ctx, counts.ctypes.data, ctypes.byref(xs),
+                                                   ctypes.byref(bs)))
+        return counts, xs.value, bs.value
+
     def order_stats(self) -> tuple[list[np.ndarray], np.ndarray]:
         """The coefficient-order statistics of the last pass's first frame
         (jxg_order_stats): per order slot a (3, size) u32 array of the

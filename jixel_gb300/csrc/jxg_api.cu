@@ -175,6 +175,7 @@ struct Context {
   int32_t refine_steps = 0;
   DevBuf field_buf;  // a caller's field, staged for jxg_frontend_run_with_field
   DevBuf order_buf;  // the order statistics' counters and per-slot block counts
+  DevBuf chroma_buf;  // the pixel-chromacity counts
   // launch geometry of the tunable search and layout kernels (warps per CTA)
   uint8_t tune[jxg::kTuneKernels] = {4, 4, 4, 4, 4, 4, 4, 4, jxg::kRetileWarps, jxg::kSiteWarps};
   // timing
@@ -1422,6 +1423,45 @@ int32_t jxg_order_stats(void* ctx, uint32_t* counts, uint32_t* blocks) {
   JXG_CUDA(c, cudaMemcpyAsync(blocks, d_blocks, jxg::kOrderSlots * sizeof(uint32_t),
                               cudaMemcpyDeviceToHost, s));
   return jxg::wait(c);
+}
+
+int32_t jxg_pixel_chromacity(void* ctx, uint32_t* counts, uint32_t* x_steps, uint32_t* b_steps) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c) return JXG_ERR_INVALID_ARGUMENT;
+  if (!c->have_frame || c->layouts.empty())
+    return jxg::fail(c, JXG_ERR_INVALID_ARGUMENT, "no frame in the last pass");
+  cudaSetDevice(c->device);
+  const jxg::FrameLayout& L = c->layouts[0];
+  const int w = static_cast<int>(L.width), h = static_cast<int>(L.height);
+  int st = jxg::ensure(c, c->chroma_buf, 7 * sizeof(uint32_t));
+  if (st) return st;
+  uint32_t* d_counts = static_cast<uint32_t*>(c->chroma_buf.ptr);
+  cudaStream_t s = c->stream;
+  JXG_CUDA(c, cudaMemsetAsync(d_counts, 0, 7 * sizeof(uint32_t), s));
+  if (w >= 2 && h >= 2) {
+    const int64_t total = static_cast<int64_t>(w - 1) * (h - 1);
+    const unsigned grid = static_cast<unsigned>(
+        std::min<int64_t>((total + jxg::kChromacityThreads - 1) / jxg::kChromacityThreads, 1216));
+    st = jxg::launch(c, "k_pixel_chromacity", c->timing, [&] {
+      jxg::k_pixel_chromacity<<<grid, jxg::kChromacityThreads, 0, s>>>(
+          static_cast<const float*>(c->xyb.ptr) + L.xyb_off, w, h, static_cast<int64_t>(L.plane), d_counts);
+    });
+    if (st) return st;
+  }
+  uint32_t n[7];
+  JXG_CUDA(c, cudaMemcpyAsync(n, d_counts, sizeof(n), cudaMemcpyDeviceToHost, s));
+  if ((st = jxg::wait(c))) return st;
+  // a level needs PIXEL_CHROMACITY_MIN_PIXELS (4) pixels; the B steps add one
+  // for exposed blue once a level is reached (src/frame/chroma.rs:154-163)
+  uint32_t lx = 0, lb = 0;
+  for (int k = 0; k < 3; ++k) {
+    lx += n[k] >= 4u ? 1u : 0u;
+    lb += n[3 + k] >= 4u ? 1u : 0u;
+  }
+  if (counts) std::memcpy(counts, n, sizeof(n));
+  if (x_steps) *x_steps = lx;
+  if (b_steps) *b_steps = lb == 0 ? 0u : lb - 1u + (n[6] > 0 ? 1u : 0u);
+  return JXG_OK;
 }
 
 int32_t jxg_derive_orders(const uint32_t* counts, const uint32_t* blocks, uint16_t* used_mask,

@@ -2400,6 +2400,57 @@ __global__ void __launch_bounds__(kOrderStatsThreads)
   if (threadIdx.x < kOrderSlots && s_blocks[threadIdx.x]) atomicAdd(&blocks[threadIdx.x], s_blocks[threadIdx.x]);
 }
 
+// pixel_chromacity_steps (src/frame/chroma.rs:89-165), its counts: over
+// every pixel with a left and an upper neighbour, the X steps reaching
+// 0.015 / 0.022 / 0.026, the B - Y steps above 0.28 / 0.33 / 0.38 and the
+// strongly exposed blue.  A thread per pixel; each test is counted with a
+// ballot, a CTA's counts gather in shared memory, then one global add each
+// (integer counts: the order of the adds does not matter).  The steps
+// follow from the counts on the host.
+constexpr int kChromacityThreads = 256;
+__global__ void __launch_bounds__(kChromacityThreads)
+    k_pixel_chromacity(const float* __restrict__ xyb, int w, int h, int64_t plane,
+                       uint32_t* __restrict__ counts) {
+  __shared__ uint32_t s_counts[7];
+  if (threadIdx.x < 7) s_counts[threadIdx.x] = 0u;
+  __syncthreads();
+  const float* X = xyb;
+  const float* Y = xyb + plane;
+  const float* B = xyb + 2 * plane;
+  const int64_t cols = w - 1, total = cols * (h - 1);
+  uint32_t mine[7] = {0u, 0u, 0u, 0u, 0u, 0u, 0u};
+  // the trip count is the CTA's, so every ballot has the whole warp
+  for (int64_t i0 = static_cast<int64_t>(blockIdx.x) * blockDim.x; i0 < total;
+       i0 += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t i = i0 + threadIdx.x;
+    bool t[7] = {false, false, false, false, false, false, false};
+    if (i < total) {
+      const int64_t at = (1 + i / cols) * w + 1 + i % cols, left = at - 1, up = at - w;
+      const float xv = X[at], yv = Y[at], bv = B[at];
+      const float step_x = fmaxf(fabsf(__fsub_rn(xv, X[left])), fabsf(__fsub_rn(xv, X[up])));
+      const float diff_b = __fsub_rn(bv, yv);
+      const float left_diff = __fsub_rn(B[left], Y[left]), up_diff = __fsub_rn(B[up], Y[up]);
+      const float step_b = fmaxf(fabsf(__fsub_rn(diff_b, left_diff)), fabsf(__fsub_rn(diff_b, up_diff)));
+      t[0] = step_x >= 0.015f;
+      t[1] = step_x >= 0.022f;
+      t[2] = step_x >= 0.026f;
+      t[3] = step_b > 0.28f;
+      t[4] = step_b > 0.33f;
+      t[5] = step_b > 0.38f;
+      const float step = __fadd_rn(fabsf(__fsub_rn(bv, B[left])), fabsf(__fsub_rn(bv, B[up])));
+      t[6] = __fmul_rn(__fsub_rn(bv, __fmul_rn(yv, 1.2f)), step) >= 0.13f;
+    }
+#pragma unroll
+    for (int k = 0; k < 7; ++k) mine[k] += __popc(__ballot_sync(0xffffffffu, t[k]));
+  }
+  if ((threadIdx.x & 31) == 0)
+#pragma unroll
+    for (int k = 0; k < 7; ++k)
+      if (mine[k]) atomicAdd(&s_counts[k], mine[k]);
+  __syncthreads();
+  if (threadIdx.x < 7 && s_counts[threadIdx.x]) atomicAdd(&counts[threadIdx.x], s_counts[threadIdx.x]);
+}
+
 // Dynamic shared memory above the 48 KB default for the search kernels.
 inline cudaError_t set_search_attributes() {
   cudaError_t e = cudaSuccess;

@@ -583,6 +583,49 @@ int orc_is_screen_content(uint64_t constant, size_t w, size_t h) {
   return (float)constant / (float)(bw * bh) >= 0.15f;
 }
 
+/* pixel_chromacity_steps (src/frame/chroma.rs:89-165): over every pixel
+ * with a left and an upper neighbour, the counts of X steps reaching
+ * 0.015 / 0.022 / 0.026, of B - Y steps above 0.28 / 0.33 / 0.38, and of
+ * strongly exposed blue; then the extra X and B quant-scale steps, each level
+ * needing 4 pixels.  counts = {x[3], b[3], exposed blue}, steps = {x, b}. */
+void orc_pixel_chromacity(const float* xyb, size_t w, size_t h, uint32_t counts[7],
+                          uint32_t steps[2]) {
+  static const float x_levels[3] = {0.015f, 0.022f, 0.026f};
+  static const float b_levels[3] = {0.28f, 0.33f, 0.38f};
+  const size_t n = w * h;
+  for (int k = 0; k < 7; k++) counts[k] = 0;
+  steps[0] = steps[1] = 0;
+  if (w < 2 || h < 2) return;
+  const float *X = xyb, *Y = xyb + n, *B = xyb + 2 * n;
+  for (size_t y = 1; y < h; y++) {
+    const size_t r = y * w, u = (y - 1) * w;
+    float left_x = X[r], left_b = B[r], left_diff = B[r] - Y[r];
+    for (size_t x = 1; x < w; x++) {
+      const float xv = X[r + x], yv = Y[r + x], bv = B[r + x];
+      const float px = X[u + x], py = Y[u + x], pb = B[u + x];
+      const float step_x = fmaxf(fabsf(xv - left_x), fabsf(xv - px));
+      const float diff_b = bv - yv;
+      const float step_b = fmaxf(fabsf(diff_b - left_diff), fabsf(diff_b - (pb - py)));
+      for (int k = 0; k < 3; k++) {
+        counts[k] += step_x >= x_levels[k];
+        counts[3 + k] += step_b > b_levels[k];
+      }
+      const float step = fabsf(bv - left_b) + fabsf(bv - pb);
+      counts[6] += (bv - yv * 1.2f) * step >= 0.13f;
+      left_x = xv;
+      left_b = bv;
+      left_diff = diff_b;
+    }
+  }
+  uint32_t lx = 0, lb = 0;
+  for (int k = 0; k < 3; k++) {
+    lx += counts[k] >= 4u;
+    lb += counts[3 + k] >= 4u;
+  }
+  steps[0] = lx;
+  steps[1] = lb == 0 ? 0 : lb - 1 + (counts[6] > 0);
+}
+
 /* ------------------------------------------------------------------ */
 /* Adaptive quantisation (src/adaptive_quant.rs)                        */
 /* ------------------------------------------------------------------ */

@@ -105,6 +105,9 @@ def lib() -> ctypes.CDLL:
         _lib.orc_freq_context.argtypes = [ctypes.c_int32]
         _lib.orc_nonzero_context.restype = ctypes.c_int32
         _lib.orc_nonzero_context.argtypes = [ctypes.c_int32]
+        _lib.orc_pixel_chromacity.restype = None
+        _lib.orc_pixel_chromacity.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
+                                              ctypes.c_void_p, ctypes.c_void_p]
         _lib.orc_constant_blocks.restype = ctypes.c_uint64
         _lib.orc_constant_blocks.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t]
         _lib.orc_strategy_cost_probe.restype = ctypes.c_float
@@ -493,6 +496,18 @@ def transfer_lut(bits: int, transfer: int) -> np.ndarray:
     if st:
         raise ValueError(f"transfer {transfer} at {bits} bits: status {st}")
     return out[:256] if bits == 8 else out
+
+
+def pixel_chromacity(xyb: np.ndarray) -> tuple[np.ndarray, int, int]:
+    """pixel_chromacity_steps (src/frame/chroma.rs:89-165) of (3, h, w) XYB
+    planes: the seven counts (X steps at three levels, B - Y steps at three,
+    exposed blue) and the extra X and B quant-scale steps."""
+    xyb = np.ascontiguousarray(xyb, np.float32)
+    _, h, w = xyb.shape
+    counts = np.zeros(7, np.uint32)
+    steps = np.zeros(2, np.uint32)
+    lib().orc_pixel_chromacity(xyb.ctypes.data, w, h, counts.ctypes.data, steps.ctypes.data)
+    return counts, int(steps[0]), int(steps[1])
 
 
 def natural_scan(cx: int, cy: int) -> np.ndarray:
