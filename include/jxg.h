@@ -312,6 +312,14 @@ void jxg_batch_destroy(void* batch);
  * image: `xyb` is 3 planes of w*h floats; writes xb*yb raw field values. */
 int32_t jxg_op_fill_quant_field(void* ctx, const float* xyb, uint64_t width, uint64_t height,
                                 float distance, float inv_scale, uint8_t* quant_field);
+/* apply_chroma_hf_protection (src/adaptive_quant.rs:303-402; the reference
+ * runs it after the field, per DC group, when the Slow chroma policy marks
+ * the frame X- or B-heavy, src/frame/dc_groups.rs:100-108) over a whole
+ * frame: `xyb` is 3 planes of w*h floats, `quant_field` the xb*yb raw field,
+ * raised in place where a block's edges are mostly chromatic.  Outside
+ * distances 0.35 to 2 the field is left as it is. */
+int32_t jxg_op_chroma_hf_protection(void* ctx, const float* xyb, uint64_t width, uint64_t height,
+                                    float distance, uint8_t* quant_field);
 /* gaborish_inverse (src/gaborish.rs:44; the encoder's pre-inversion that
  * gaborize, src/frame/quantization.rs:240-245, runs with mul 0.9908511 when
  * Gaborish is enabled): `xyb` is 3 planes of w*h floats, `out` receives the

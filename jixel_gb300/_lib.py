@@ -36,6 +36,7 @@ EXPORTS = [
     "jxg_batch_result",
     "jxg_batch_destroy",
     "jxg_op_fill_quant_field",
+    "jxg_op_chroma_hf_protection",
     "jxg_op_gaborish_inverse",
     "jxg_op_gaborish",
     "jxg_op_epf",
@@ -172,6 +173,7 @@ def load() -> ctypes.CDLL:
                                    ctypes.POINTER(FrontendOutput)]),
         "jxg_batch_destroy": (None, [vp]),
         "jxg_op_fill_quant_field": (i32, [vp, vp, u64, u64, f32, f32, vp]),
+        "jxg_op_chroma_hf_protection": (i32, [vp, vp, u64, u64, ctypes.c_float, vp]),
         "jxg_op_gaborish_inverse": (i32, [vp, vp, u64, u64, ctypes.c_float, vp]),
         "jxg_op_gaborish": (i32, [vp, vp, u64, u64, vp]),
         "jxg_op_epf": (i32, [vp, vp, u64, u64, vp, i32, ctypes.c_float, ctypes.c_float, ctypes.c_float,

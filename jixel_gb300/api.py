@@ -434,6 +434,16 @@ class FrontendContext:
                           alpha=pixels.shape[2] in (2, 4), packed=packed)
 
     # operator table -----------------------------------------------------
+    def chroma_hf_protection(self, xyb: np.ndarray, distance: float, field: np.ndarray) -> np.ndarray:
+        """apply_chroma_hf_protection (src/adaptive_quant.rs:303-402) of (3, h, w)
+        XYB planes on a copy of the (yb, xb) u8 field (jxg_op_chroma_hf_protection)."""
+        xyb = np.ascontiguousarray(xyb, np.float32)
+        _, h, w = xyb.shape
+        out = np.ascontiguousarray(field, np.uint8).copy()
+        self._check(self._lib.jxg_op_chroma_hf_protection(self._ctx, xyb.ctypes.data, w, h,
+                                                          float(distance), out.ctypes.data))
+        return out
+
     def fill_quant_field(self, xyb: np.ndarray, distance: float, inv_scale: float) -> np.ndarray:
         xyb = np.ascontiguousarray(xyb, np.float32)
         _, h, w = xyb.shape

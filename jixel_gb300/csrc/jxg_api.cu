@@ -1668,6 +1668,44 @@ void jxg_batch_destroy(void* batch) {
   delete b;
 }
 
+int32_t jxg_op_chroma_hf_protection(void* ctx, const float* xyb, uint64_t width, uint64_t height,
+                                    float distance, uint8_t* quant_field) {
+  Context* c = static_cast<Context*>(ctx);
+  if (!c || !xyb || !quant_field) return JXG_ERR_INVALID_ARGUMENT;
+  if (width == 0 || height == 0) return JXG_ERR_EMPTY_IMAGE;
+  if (!std::isfinite(distance)) return JXG_ERR_INVALID_DISTANCE;
+  // ChromaHfFit (src/adaptive_quant.rs:319-342): the boost fades in from
+  // distance 0.35 over 0.40 and out from 1.0 over 1.0, at strength 0.40
+  auto clamp01 = [](float v) { return v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v); };
+  if (distance < 0.35f) return JXG_OK;
+  const float fade_in = clamp01((distance - 0.35f) / 0.40f);
+  const float fade_out = 1.0f - clamp01((distance - 1.0f) / 1.0f);
+  const float strength = 0.40f * fade_in * fade_out;
+  if (strength <= 0.0f) return JXG_OK;
+  cudaSetDevice(c->device);
+  jxg_frame_info fi;
+  jxg::frame_info(width, height, &fi);
+  const int64_t n = static_cast<int64_t>(width * height);
+  const size_t nb = fi.xsize_blocks * fi.ysize_blocks;
+  int st;
+  if ((st = jxg::ensure(c, c->op_in, jxg::align_up(3 * n * 4, 256))) ||
+      (st = jxg::ensure(c, c->op_out, jxg::align_up(nb, 256))))
+    return st;
+  float* d_xyb = static_cast<float*>(c->op_in.ptr);
+  uint8_t* d_field = static_cast<uint8_t*>(c->op_out.ptr);
+  cudaStream_t s = c->stream;
+  JXG_CUDA(c, cudaMemcpyAsync(d_xyb, xyb, 3 * n * 4, cudaMemcpyHostToDevice, s));
+  JXG_CUDA(c, cudaMemcpyAsync(d_field, quant_field, nb, cudaMemcpyHostToDevice, s));
+  st = jxg::launch(c, "k_chroma_hf_protection", c->timing, [&] {
+    jxg::k_chroma_hf_protection<<<static_cast<unsigned>((nb + 127) / 128), 128, 0, s>>>(
+        d_xyb, static_cast<int>(width), static_cast<int>(height), n, static_cast<int>(fi.xsize_blocks),
+        static_cast<int>(fi.ysize_blocks), strength, d_field);
+  });
+  if (st) return st;
+  JXG_CUDA(c, cudaMemcpyAsync(quant_field, d_field, nb, cudaMemcpyDeviceToHost, s));
+  return jxg::wait(c);
+}
+
 int32_t jxg_op_fill_quant_field(void* ctx, const float* xyb, uint64_t width, uint64_t height,
                                 float distance, float inv_scale, uint8_t* quant_field) {
   Context* c = static_cast<Context*>(ctx);

@@ -2451,6 +2451,69 @@ __global__ void __launch_bounds__(kChromacityThreads)
   if (threadIdx.x < 7 && s_counts[threadIdx.x]) atomicAdd(&counts[threadIdx.x], s_counts[threadIdx.x]);
 }
 
+// apply_chroma_hf_protection (src/adaptive_quant.rs:303-402) with
+// chroma_hf_stats_scalar (:222-279): a thread per 8x8 block (cut at the
+// image edge) sums the opponent magnitude, then the chroma and luma
+// gradients of the horizontal and the vertical neighbour pairs, in the
+// reference's order; a block whose edges are mostly chromatic has its field
+// value raised by the fitted gain.  `strength` is the distance's fade
+// (positive; the host skips the launch otherwise).
+__global__ void __launch_bounds__(128)
+    k_chroma_hf_protection(const float* __restrict__ xyb, int w, int h, int64_t plane, int xb, int yb,
+                           float strength, uint8_t* __restrict__ field) {
+  const int64_t blk = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (blk >= static_cast<int64_t>(xb) * yb) return;
+  const int bx = static_cast<int>(blk % xb), by = static_cast<int>(blk / xb);
+  const int px = bx * 8, py = by * 8, bw = imin(8, w - px), bh = imin(8, h - py);
+  const float* X = xyb;
+  const float* Y = xyb + plane;
+  const float* B = xyb + 2 * plane;
+  float chroma_sum = 0.0f, chroma_grad = 0.0f, luma_grad = 0.0f;
+  int edges = 0;
+  for (int y = py; y < py + bh; ++y)
+    for (int x = px; x < px + bw; ++x) {
+      const int64_t i = static_cast<int64_t>(y) * w + x;
+      chroma_sum = __fadd_rn(chroma_sum, __fadd_rn(fabsf(X[i]), fabsf(__fsub_rn(B[i], Y[i]))));
+    }
+  auto pair = [&](int64_t i, int64_t j) {
+    const float dx = fabsf(__fsub_rn(X[j], X[i]));
+    const float db = fabsf(__fsub_rn(__fsub_rn(B[j], Y[j]), __fsub_rn(B[i], Y[i])));
+    chroma_grad = __fadd_rn(chroma_grad, __fadd_rn(dx, db));
+    luma_grad = __fadd_rn(luma_grad, fabsf(__fsub_rn(Y[j], Y[i])));
+  };
+  if (bw > 1) {
+    for (int y = py; y < py + bh; ++y)
+      for (int x = px; x + 1 < px + bw; ++x) {
+        const int64_t i = static_cast<int64_t>(y) * w + x;
+        pair(i, i + 1);
+      }
+    edges += (bw - 1) * bh;
+  }
+  if (bh > 1) {
+    for (int y = py; y + 1 < py + bh; ++y)
+      for (int x = px; x < px + bw; ++x) {
+        const int64_t i = static_cast<int64_t>(y) * w + x;
+        pair(i, i + w);
+      }
+    edges += bw * (bh - 1);
+  }
+  if (edges == 0) return;
+  auto unit = [](float v) { return v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v); };
+  const float mean_chroma = __fdiv_rn(chroma_sum, static_cast<float>(bw * bh));
+  const float mean_gradient = __fdiv_rn(chroma_grad, static_cast<float>(edges));
+  const float chroma_share = __fdiv_rn(chroma_grad, __fadd_rn(__fadd_rn(chroma_grad, luma_grad), 1e-4f));
+  const float chroma_w = unit(__fdiv_rn(__fsub_rn(mean_chroma, 0.025f), 0.075f));
+  const float gradient_w = unit(__fdiv_rn(__fsub_rn(mean_gradient, 0.006f), 0.030f));
+  const float share_w = unit(__fdiv_rn(__fsub_rn(chroma_share, 0.25f), 0.55f));
+  const float risk = __fmul_rn(__fmul_rn(chroma_w, gradient_w), share_w);
+  if (!(risk > 0.0f)) return;
+  const float ceiling = fmla(1.4f, __fmul_rn(share_w, share_w), 0.35f);
+  const float gain = fmla(__fmul_rn(ceiling, strength), risk, 1.0f);
+  const float q = static_cast<float>(field[blk]);
+  const float r = roundf(__fmul_rn(q, gain));
+  field[blk] = static_cast<uint8_t>(r < 1.0f ? 1.0f : (r > 255.0f ? 255.0f : r));
+}
+
 // Dynamic shared memory above the 48 KB default for the search kernels.
 inline cudaError_t set_search_attributes() {
   cudaError_t e = cudaSuccess;

@@ -2828,6 +2828,67 @@ int orc_frontend(orc_frame* f) {
 
 /* fill_quant_field over every DC group of an XYB image (the oracle side of
  * the FillQuantFieldFn operator, src/adaptive_quant.rs:474). */
+/* apply_chroma_hf_protection (src/adaptive_quant.rs:303-402) over a whole
+ * frame's field, with chroma_hf_stats_scalar (:222-279): per 8x8 block (cut
+ * at the image edge) the opponent magnitude and the chroma and luma gradient
+ * sums in the reference's order, then the fitted boost of blocks whose edges
+ * are mostly chromatic. */
+void orc_chroma_hf_protection(const float* xyb, size_t w, size_t h, float distance, uint8_t* field) {
+  const float fade_in_start = 0.35f, fade_in_width = 0.40f, fade_out_start = 1.0f;
+  const float fade_out_width = 1.0f, strength = 0.40f, ceil_base = 0.35f, ceil_share = 1.4f;
+  const size_t xb = (w + 7) / 8, yb = (h + 7) / 8, n = w * h;
+  if (xb == 0 || yb == 0 || distance < fade_in_start) return;
+  const float fade_in = clampf((distance - fade_in_start) / fade_in_width, 0.0f, 1.0f);
+  const float fade_out = 1.0f - clampf((distance - fade_out_start) / fade_out_width, 0.0f, 1.0f);
+  const float distance_strength = strength * fade_in * fade_out;
+  if (distance_strength <= 0.0f) return;
+  const float *X = xyb, *Y = xyb + n, *B = xyb + 2 * n;
+  for (size_t by = 0; by < yb; by++)
+    for (size_t bx = 0; bx < xb; bx++) {
+      const size_t px = bx * 8, py = by * 8;
+      const size_t bw = w - px < 8 ? w - px : 8, bh = h - py < 8 ? h - py : 8;
+      float chroma_sum = 0.0f, chroma_grad = 0.0f, luma_grad = 0.0f;
+      size_t edges = 0;
+      for (size_t y = py; y < py + bh; y++)
+        for (size_t x = px; x < px + bw; x++) {
+          const size_t i = y * w + x;
+          chroma_sum += fabsf(X[i]) + fabsf(B[i] - Y[i]);
+        }
+      if (bw > 1) {
+        for (size_t y = py; y < py + bh; y++)
+          for (size_t x = px; x + 1 < px + bw; x++) {
+            const size_t i = y * w + x, j = i + 1;
+            chroma_grad += fabsf(X[j] - X[i]) + fabsf((B[j] - Y[j]) - (B[i] - Y[i]));
+            luma_grad += fabsf(Y[j] - Y[i]);
+          }
+        edges += (bw - 1) * bh;
+      }
+      if (bh > 1) {
+        for (size_t y = py; y + 1 < py + bh; y++)
+          for (size_t x = px; x < px + bw; x++) {
+            const size_t i = y * w + x, j = i + w;
+            chroma_grad += fabsf(X[j] - X[i]) + fabsf((B[j] - Y[j]) - (B[i] - Y[i]));
+            luma_grad += fabsf(Y[j] - Y[i]);
+          }
+        edges += bw * (bh - 1);
+      }
+      if (edges == 0) continue;
+      const float mean_chroma = chroma_sum / (float)(bw * bh);
+      const float mean_gradient = chroma_grad / (float)edges;
+      const float chroma_share = chroma_grad / (chroma_grad + luma_grad + 1e-4f);
+      const float chroma_w = clampf((mean_chroma - 0.025f) / 0.075f, 0.0f, 1.0f);
+      const float gradient_w = clampf((mean_gradient - 0.006f) / 0.030f, 0.0f, 1.0f);
+      const float share_w = clampf((chroma_share - 0.25f) / 0.55f, 0.0f, 1.0f);
+      const float risk = chroma_w * gradient_w * share_w;
+      if (risk > 0.0f) {
+        const float ceiling = fmla(ceil_share, share_w * share_w, ceil_base);
+        const float gain = fmla(ceiling * distance_strength, risk, 1.0f);
+        const float q = (float)field[by * xb + bx];
+        field[by * xb + bx] = (uint8_t)clampf(roundf(q * gain), 1.0f, 255.0f);
+      }
+    }
+}
+
 void orc_fill_quant_field_image(const float* xyb, size_t w, size_t h, float distance,
                                 float inv_scale, uint8_t* qf) {
   init_exp2_table();

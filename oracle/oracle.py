@@ -105,6 +105,9 @@ def lib() -> ctypes.CDLL:
         _lib.orc_freq_context.argtypes = [ctypes.c_int32]
         _lib.orc_nonzero_context.restype = ctypes.c_int32
         _lib.orc_nonzero_context.argtypes = [ctypes.c_int32]
+        _lib.orc_chroma_hf_protection.restype = None
+        _lib.orc_chroma_hf_protection.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
+                                                  ctypes.c_float, ctypes.c_void_p]
         _lib.orc_pixel_chromacity.restype = None
         _lib.orc_pixel_chromacity.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
                                               ctypes.c_void_p, ctypes.c_void_p]
@@ -496,6 +499,16 @@ def transfer_lut(bits: int, transfer: int) -> np.ndarray:
     if st:
         raise ValueError(f"transfer {transfer} at {bits} bits: status {st}")
     return out[:256] if bits == 8 else out
+
+
+def chroma_hf_protection(xyb: np.ndarray, distance: float, field: np.ndarray) -> np.ndarray:
+    """apply_chroma_hf_protection (src/adaptive_quant.rs:303-402) of (3, h, w)
+    XYB planes on a copy of the (yb, xb) u8 field."""
+    xyb = np.ascontiguousarray(xyb, np.float32)
+    _, h, w = xyb.shape
+    out = np.ascontiguousarray(field, np.uint8).copy()
+    lib().orc_chroma_hf_protection(xyb.ctypes.data, w, h, float(distance), out.ctypes.data)
+    return out
 
 
 def pixel_chromacity(xyb: np.ndarray) -> tuple[np.ndarray, int, int]:

@@ -53,3 +53,39 @@ def test_flat_and_grey_planes_take_no_steps():
     xyb[2] = xyb[1]
     counts, xs, bs = O.pixel_chromacity(xyb)
     assert counts[:6].sum() == 0 and xs == 0 and bs == 0
+
+
+def reference_test_image(w=19, h=17):
+    """The image of selected_chroma_hf_stats_match_scalar (src/adaptive_quant.rs:811-852)."""
+    y, x = np.mgrid[0:h, 0:w]
+    return np.stack([((((x * 37 + y * 53 + c * 97 + x * y * 3) % 257).astype(F) - F(128)) / F(211))
+                     .astype(F) for c in range(3)])
+
+
+def chromatic(w, h, seed, amp):
+    rng = np.random.default_rng(seed)
+    xyb = np.zeros((3, h, w), F)
+    xyb[1] = 0.4 + rng.normal(0, 0.002, (h, w))
+    xyb[0] = amp * np.sign(rng.normal(0, 1, (h, w)))
+    xyb[2] = xyb[1] + amp * 4 * np.sign(rng.normal(0, 1, (h, w)))
+    return xyb.astype(F)
+
+
+def test_chroma_hf_protection_only_raises_in_its_distance_band():
+    # ChromaHfFit (src/adaptive_quant.rs:319-342): fades in from 0.35, out at 2
+    xyb = chromatic(40, 24, 1, 0.05)
+    field = np.full((3, 5), 40, np.uint8)
+    for d in (0.2, 0.35, 2.0, 3.0):
+        assert np.array_equal(O.chroma_hf_protection(xyb, d, field), field), d
+    for d in (0.5, 0.75, 1.0, 1.5):
+        out = O.chroma_hf_protection(xyb, d, field)
+        assert np.all(out >= field) and np.any(out > field), d
+        assert np.all(out <= np.round(field * (1.0 + 1.75 * 0.4)) + 1)
+
+
+def test_chroma_hf_protection_leaves_achromatic_blocks():
+    xyb = reference_test_image()
+    xyb[0] = 0.0
+    xyb[2] = xyb[1]
+    field = np.arange(9, dtype=np.uint8).reshape(3, 3) * 20 + 5
+    assert np.array_equal(O.chroma_hf_protection(xyb, 0.9, field), field)
