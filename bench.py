@@ -231,6 +231,25 @@ def counters_from_profiles(kernel: str) -> tuple[float | None, float | None]:
     return None, None
 
 
+FP32_OPS = os.path.join(ROOT, "profiles", "fp32_ops_4k_q75_fastest.txt")
+
+
+def fp32_ops_from_profiles() -> dict[str, float] | None:
+    """FP32 operations per launch of each kernel of one 3840x2160 q75
+    Speed::Fastest frame, from the committed ncu summary (thread-level
+    FADD / FMUL / FFMA counts and their packed forms; its header gives the
+    capture's command)."""
+    if not os.path.exists(FP32_OPS):
+        return None
+    ops = {}
+    for line in open(FP32_OPS):
+        if line.startswith("#") or ":" not in line:
+            continue
+        name, rest = line.split(":", 1)
+        ops[name.strip()] = float(rest.split()[0])
+    return ops or None
+
+
 def _synthetic():
     """The seeded image generator, loaded from its file so that the reference
     arm does not import the package (whose API loads the CUDA library)."""
@@ -443,6 +462,22 @@ def run_gpu(args):
         "achieved": fe_bytes / (fe_ms / 1000.0) / 1e9,
         "frac": fe_bytes / (fe_ms / 1000.0) / 1e9 / peaks["hbm_gbs"],
     }
+    # FP32 work: the operations the frame's kernels executed (ncu counts of
+    # the same frame) over the frame's summed kernel time, against the CUDA
+    # cores' nominal FP32 rate (128 lanes an SM, an FMA two operations, at the
+    # sampled SM clock); no measured FP32 peak exists for this machine
+    ops = fp32_ops_from_profiles()
+    if ops and sm_mhz:
+        total_ops = sum(ops.values())
+        fp32_peak = torch.cuda.get_device_properties(dev).multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+        achieved = total_ops / (fe_ms / 1000.0) / 1e12
+        top = max(ops.items(), key=lambda kv: kv[1] / max(ktimes.get(kv[0], (1e30, 1))[0], 1e-9))
+        roofline["fp32"] = {
+            "ops_per_frame": total_ops, "kernel_ms_per_frame": fe_ms, "achieved": achieved,
+            "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+            "peak_source": "nominal (152 SMs x 128 FP32 lanes x 2 at the sampled SM clock)",
+            "densest_kernel": top[0],
+        }
 
     ultrafast = run_ultrafast(ctxs, streams, flush, d_img, args, dev)
     c5 = run_c5(ctxs, streams, flush, args, dev) if args.c5 else None
