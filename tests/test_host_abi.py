@@ -26,6 +26,12 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(lib, n), n
 
 
+def test_rust_binding_declares_every_entry_point():
+    # the extern "C" block a jixel maintainer would add
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    assert [n for n in header_functions() if f"fn {n}(" not in text] == []
+
+
 def test_distance_from_quality_matches_oracle():
     for q in np.linspace(-10, 110, 481):
         assert J.distance_from_quality(float(q)) == O.distance_from_quality(float(q)), q
